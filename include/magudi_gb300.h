@@ -1,0 +1,208 @@
+/*
+ * magudi_gb300.h -- C ABI of the GB300 (sm_103a) implementation of magudi's
+ * forward and discrete-adjoint compressible Navier-Stokes right-hand side,
+ * its RK4 stage updates, the acoustic-noise functional, the thermal-actuator
+ * gradient and uniform checkpointing.
+ *
+ * Every entry point is plain C: pointers, sizes and status codes. Status 0 is
+ * success; a positive value is an error whose text mgd_last_error() returns.
+ * Arrays use magudi's Fortran column-major layout x(nGridPoints, nComponents):
+ * component c of grid point p = i + Nx*(j + Ny*k) (0-based) sits at
+ * x[p + nGridPoints*c]. A Fortran caller therefore passes c_loc(array) with no
+ * copy. One context owns one region (a set of blocks on one GPU) and one CUDA
+ * stream; calls on one context must come from one host thread at a time.
+ *
+ * The reference interface each call replaces is named beside it
+ * (paths relative to the magudi source tree).
+ */
+#ifndef MAGUDI_GB300_H
+#define MAGUDI_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MGD_MAX_BLOCKS 8
+#define MGD_MAX_PATCHES 64
+#define MGD_MAX_SOURCES 8
+#define MGD_NAME_LEN 64
+
+/* include/Region.f90:9-11 (FORWARD = +1, ADJOINT = -1, LINEARIZED = 0). */
+enum { MGD_FORWARD = 1, MGD_ADJOINT = -1 };
+
+/* src/GridImpl.f90:202-210 periodicity types. */
+enum { MGD_PERIODIC_NONE = 0, MGD_PERIODIC_PLANE = 1, MGD_PERIODIC_OVERLAP = 2 };
+
+/* Patch types of src/PatchFactoryImpl.f90:43-84 that this library implements. */
+enum {
+  MGD_PATCH_SAT_FAR_FIELD = 1,
+  MGD_PATCH_SPONGE = 2,
+  MGD_PATCH_ACTUATOR = 3,
+  MGD_PATCH_COST_TARGET = 4
+};
+
+/* Fields that mgd_set_field / mgd_get_field move between host and device. */
+enum {
+  MGD_FIELD_CONSERVED = 0,         /* state%conservedVariables (N, nU)   */
+  MGD_FIELD_ADJOINT = 1,           /* state%adjointVariables   (N, nU)   */
+  MGD_FIELD_TARGET = 2,            /* state%targetState        (N, nU)   */
+  MGD_FIELD_RHS = 3,               /* state%rightHandSide      (N, nU)   */
+  MGD_FIELD_CONTROL_MOLLIFIER = 4, /* grid%controlMollifier    (N, 1)    */
+  MGD_FIELD_TARGET_MOLLIFIER = 5,  /* grid%targetMollifier     (N, 1)    */
+  MGD_FIELD_MEAN_PRESSURE = 6,     /* AcousticNoise meanPressure (N, 1)  */
+  MGD_FIELD_METRICS = 7,           /* grid%metrics   (N, nD*nD)  read-only */
+  MGD_FIELD_JACOBIAN = 8,          /* grid%jacobian  (N, 1) = 1/det      */
+  MGD_FIELD_NORM = 9,              /* grid%norm      (N, 1) = H*det      */
+  MGD_FIELD_PRESSURE = 10,         /* state%pressure (N, 1)  read-only   */
+  MGD_FIELD_TEMPERATURE = 11,      /* state%temperature (N, 1) read-only */
+  MGD_FIELD_ARC_LENGTHS = 12       /* grid%arcLengths (N, nD) read-only  */
+};
+
+/* Region-wide options: the keys of magudi.inp that parameterize the hot path
+ * (src/SimulationFlagsImpl.f90:24-45, src/SolverOptionsImpl.f90:46-135). */
+typedef struct {
+  int n_dimensions;                  /* 2 or 3 */
+  int viscous;                       /* include_viscous_terms */
+  int dissipation;                   /* add_dissipation */
+  int composite_dissipation;         /* composite_dissipation (only 0 supported) */
+  int curvilinear;                   /* curvilinear_domain */
+  int use_constant_cfl;              /* use_constant_CFL_mode */
+  int enable_controller;             /* enable_controller */
+  int enable_functional;             /* enable_functional */
+  int controller_switch;             /* controller_switch: add the control forcing */
+  int adjoint_forcing_switch;        /* adjoint_forcing_switch */
+  double ratio_of_specific_heats;    /* ratio_of_specific_heats */
+  double reynolds_number;            /* Reynolds_number */
+  double prandtl_number;             /* Prandtl_number */
+  double viscosity_power_law_exponent;
+  double bulk_viscosity_ratio;
+  double dissipation_amount;
+  double time_step_size;
+  double cfl;
+} mgd_options;
+
+/* One block of the region: its size and periodicity (grid00N/dirM/...). */
+typedef struct {
+  int grid_size[3];                  /* 1 for unused dimensions */
+  int periodicity_type[3];           /* MGD_PERIODIC_* */
+  double periodic_length[3];
+} mgd_block_desc;
+
+/* One row of bc.dat plus the patch options read from magudi.inp
+ * (src/RegionImpl.f90:175-337, src/PatchDescriptorImpl.f90:40-100). */
+typedef struct {
+  char name[MGD_NAME_LEN];
+  int type;                          /* MGD_PATCH_* */
+  int grid_index;                    /* 1-based block index */
+  int normal_direction;              /* +-1..3, 0 */
+  int extent[6];                     /* iMin iMax jMin jMax kMin kMax as in bc.dat */
+  double inviscid_penalty_amount;    /* patches/<name>/inviscid_penalty_amount */
+  double viscous_penalty_amount;     /* patches/<name>/viscous_penalty_amount */
+  double sponge_amount;              /* patches/<name>/sponge_amount */
+  int sponge_exponent;               /* patches/<name>/sponge_exponent */
+} mgd_patch_desc;
+
+/* acoustic_sourceNN/... (src/AcousticSourceImpl.f90:3-32). */
+typedef struct {
+  double location[3];
+  double amplitude;
+  double frequency;
+  double radius;
+  double phase;
+} mgd_acoustic_source;
+
+typedef struct mgd_ctx mgd_ctx;
+
+/* Text of the last error on ctx (or of the last failed mgd_create when ctx is
+ * NULL). Replaces gracefulExit's message, src/ErrorHandlerImpl.f90:162. */
+const char* mgd_last_error(const mgd_ctx* ctx);
+
+/* Region%setup + Solver%setup options (src/RegionImpl.f90:1225,
+ * src/SolverImpl.f90:445). Creates a context on the current CUDA device. */
+int mgd_create(const mgd_options* options, mgd_ctx** out);
+int mgd_destroy(mgd_ctx* ctx);
+
+/* Grid%setup + Grid%update (src/GridImpl.f90:487-1066): adds block
+ * number (count of earlier calls + 1) with its coordinates (N, nD) and iblank
+ * (N); metrics, 1/det, H*det and arc lengths are computed on the device. */
+int mgd_add_block(mgd_ctx* ctx, const mgd_block_desc* block,
+                  const double* coordinates, const int* iblank);
+
+/* Region%readBoundaryConditions (src/RegionImpl.f90:175) for one bc.dat row. */
+int mgd_add_patch(mgd_ctx* ctx, const mgd_patch_desc* patch);
+
+/* State%setup acoustic sources (src/StateImpl.f90:135-150). */
+int mgd_add_acoustic_source(mgd_ctx* ctx, const mgd_acoustic_source* source);
+
+/* Region%loadData / saveData for one field of one block (src/RegionImpl.f90:1489). */
+int mgd_set_field(mgd_ctx* ctx, int block, int field, const double* host);
+int mgd_get_field(mgd_ctx* ctx, int block, int field, double* host);
+
+/* The rest of Solver%setup: computeSpongeStrengths (src/PatchFactoryImpl.f90:161),
+ * updatePatchFactories (:446), mollifier normalization
+ * (src/RegionImpl.f90:459-603) and the time-invariant far-field SAT matrices.
+ * Call once after blocks, patches, target state and mollifiers are set. */
+int mgd_finalize_setup(mgd_ctx* ctx);
+
+/* State%update on every block (src/StateImpl.f90:466-537). */
+int mgd_update_state(mgd_ctx* ctx);
+
+/* Region%computeRhs (src/RegionImpl.f90:1877-2027). mode = MGD_FORWARD or
+ * MGD_ADJOINT; time is state%time; adjoint_forcing_factor is
+ * state%adjointForcingFactor. The result stays on the device
+ * (read it with mgd_get_field(..., MGD_FIELD_RHS, ...)). */
+int mgd_compute_rhs(mgd_ctx* ctx, int mode, double time, double adjoint_forcing_factor);
+
+/* Functional%updateAdjointForcing (src/FunctionalImpl.f90:26-72). */
+int mgd_update_adjoint_forcing(mgd_ctx* ctx, int no_adjoint_forcing);
+
+/* AcousticNoise%compute (src/AcousticNoiseImpl.f90:123-206). */
+int mgd_compute_functional(mgd_ctx* ctx, double* value);
+
+/* ThermalActuator%computeSensitivity (src/ThermalActuatorImpl.f90:83-159). */
+int mgd_compute_sensitivity(mgd_ctx* ctx, double* value);
+
+/* RK4Integrator%substepForward / substepAdjoint
+ * (src/RK4IntegratorImpl.f90:65-270), followed for the forward mode by
+ * State%update as Solver%runForward does (src/SolverImpl.f90:827-834).
+ * *time is advanced (forward) or retreated (adjoint) as the reference does. */
+int mgd_rk4_substep(mgd_ctx* ctx, int mode, double* time, double dt, int stage);
+
+/* Control forcing for controller_switch = true, in the order the reference
+ * reads it from <prefix>.control_forcing_<patch>.dat: entry e (0-based) holds
+ * the actuator-patch values of the (e)-th stage counted backwards from the
+ * last stage of the run, nPatchPoints doubles each
+ * (src/ThermalActuatorImpl.f90:161-233, src/ActuatorPatchImpl.f90:226). */
+int mgd_set_control_forcing(mgd_ctx* ctx, const double* host, long long n_entries);
+
+/* Number of actuator-patch points (the length of one forcing/gradient entry). */
+int mgd_actuator_patch_size(mgd_ctx* ctx, long long* n_points);
+
+/* Solver%runForward (src/SolverImpl.f90:672-912) from the current conserved
+ * variables at time t0 for n_steps RK4 steps with constant dt; keeps a
+ * snapshot every save_interval steps in device memory for a following
+ * mgd_run_adjoint. *cost = the time-integrated functional. */
+int mgd_run_forward(mgd_ctx* ctx, int n_steps, int save_interval, double t0, double* cost);
+
+/* Solver%runAdjoint (src/SolverImpl.f90:914-1245) over the horizon of the
+ * preceding mgd_run_forward, with UniformCheckpointer recomputation
+ * (src/UniformCheckpointerImpl.f90:80-208) from the device snapshots.
+ * *sensitivity = the time-integrated cost sensitivity (Grad0). */
+int mgd_run_adjoint(mgd_ctx* ctx, double* sensitivity);
+
+/* The gradient vector of the last mgd_run_adjoint, in the order the reference
+ * writes <prefix>.gradient_<patch>.dat (ThermalActuator%updateGradient,
+ * src/ThermalActuatorImpl.f90:383-443): 4*n_steps entries of nPatchPoints. */
+int mgd_get_gradient(mgd_ctx* ctx, double* host, long long n_entries);
+
+/* CUDA stream the context launches on (cudaStream_t as void*). */
+void* mgd_stream(mgd_ctx* ctx);
+
+/* Counts kernel launches made by the context since the last reset. */
+long long mgd_kernel_launches(mgd_ctx* ctx, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MAGUDI_GB300_H */

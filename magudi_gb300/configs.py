@@ -1,0 +1,144 @@
+"""Generators for the synthetic workloads (the role of magudi's
+examples/*/config.py): grids, initial states, mollifiers, bc.dat patches.
+
+monopole_2d      2D acoustic monopole on [-14,14]^2 with far-field SATs,
+                 sponges, a Gaussian cost-target mollifier at (0,10) and a
+                 Gaussian control mollifier at (0,0) (sigma = 1).
+taylor_green_3d  3D periodic Taylor-Green vortex on [0, 2 pi)^3.
+random_state     the randomized state of test/adjoint_relation/full_rhs.f90:289-301.
+"""
+import math
+
+import numpy as np
+
+from .problem import AcousticSource, Block, Options, Patch, Problem, quiescent_state
+
+
+def _extents(x, lo, hi):
+    """1-based first/last index of the points of a sorted 1D coordinate in [lo, hi]."""
+    idx = np.nonzero((x >= lo) & (x <= hi))[0]
+    return int(idx[0]) + 1, int(idx[-1]) + 1
+
+
+def uniform_grid_2d(nx, ny, lo=-14.0, hi=14.0):
+    x = np.linspace(lo, hi, nx)
+    y = np.linspace(lo, hi, ny)
+    X, Y = np.meshgrid(x, y, indexing="xy")  # (ny, nx): p = i + nx*j
+    return np.stack([X.ravel(), Y.ravel()]), x, y
+
+
+def monopole_2d(n=201, ny=None, dt=0.05, n_steps=960, sponge_points=20, sponge_amount=0.2,
+                dissipation_amount=0.01, reynolds=200.0, prandtl=0.72,
+                power_law=0.666, bulk_viscosity_ratio=0.6, save_interval=10,
+                controller_switch=False, half_width=14.0, target_center=(0.0, 10.0),
+                control_center=(0.0, 0.0), mollifier_sigma=1.0):
+    """Acoustic monopole: quiescent ambient rho = 1, u = 0, p = 1/gamma; pressure
+    source 0.01 sin(2 pi 0.2 t) with a Gaussian of sigma 0.5 at the origin.
+    magudi's source is A cos(w t + phase) exp(-9/(2 R^2) r^2)
+    (src/AcousticSourceImpl.f90:27,55-62), so sin -> phase = -pi/2 and
+    sigma = 0.5 -> R = 3 sigma = 1.5."""
+    ny = ny or n
+    gamma = 1.4
+    opts = Options(
+        n_dimensions=2, viscous=True, dissipation=True, composite_dissipation=False,
+        curvilinear=False, use_constant_cfl=False, enable_controller=True,
+        enable_functional=True, controller_switch=controller_switch,
+        ratio_of_specific_heats=gamma, reynolds_number=reynolds, prandtl_number=prandtl,
+        viscosity_power_law_exponent=power_law, bulk_viscosity_ratio=bulk_viscosity_ratio,
+        dissipation_amount=dissipation_amount, time_step_size=dt)
+    coords, x, y = uniform_grid_2d(n, ny, -half_width, half_width)
+    N = n * ny
+    X, Y = coords
+    target = quiescent_state(N, 2, gamma)
+    sigma = mollifier_sigma
+    tx, ty = target_center
+    cx, cy = control_center
+    tm = np.exp(-((X - tx) ** 2 + (Y - ty) ** 2) / (2 * sigma ** 2))
+    cm = np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2 * sigma ** 2))
+    block = Block(grid_size=(n, ny, 1), coordinates=np.ascontiguousarray(coords),
+                  initial_state=target.copy(), target_state=target.copy(),
+                  control_mollifier=cm, target_mollifier=tm,
+                  mean_pressure=np.full(N, 1.0 / gamma))
+    s = sponge_points
+    patches = [
+        Patch("farField.E", "SAT_FAR_FIELD", 1, 1, (1, 1, 1, -1, 1, -1)),
+        Patch("farField.W", "SAT_FAR_FIELD", 1, -1, (-1, -1, 1, -1, 1, -1)),
+        Patch("farField.S", "SAT_FAR_FIELD", 1, 2, (1, -1, 1, 1, 1, -1)),
+        Patch("farField.N", "SAT_FAR_FIELD", 1, -2, (1, -1, -1, -1, 1, -1)),
+        Patch("sponge.E", "SPONGE", 1, 1, (1, s, 1, -1, 1, -1), sponge_amount=sponge_amount),
+        Patch("sponge.W", "SPONGE", 1, -1, (-s, -1, 1, -1, 1, -1), sponge_amount=sponge_amount),
+        Patch("sponge.S", "SPONGE", 1, 2, (1, -1, 1, s, 1, -1), sponge_amount=sponge_amount),
+        Patch("sponge.N", "SPONGE", 1, -2, (1, -1, -s, -1, 1, -1), sponge_amount=sponge_amount),
+    ]
+    w = 4.0 * sigma  # supports truncated at 4 sigma
+    ti = _extents(x, tx - w, tx + w)
+    tj = _extents(y, ty - w, ty + w)
+    patches.append(Patch("targetRegion", "COST_TARGET", 1, 0, (ti[0], ti[1], tj[0], tj[1], 1, -1)))
+    ci = _extents(x, cx - w, cx + w)
+    cj = _extents(y, cy - w, cy + w)
+    patches.append(Patch("controlRegion", "ACTUATOR", 1, 0, (ci[0], ci[1], cj[0], cj[1], 1, -1)))
+    sources = [AcousticSource((0.0, 0.0), 0.01, 0.2, 1.5, -math.pi / 2)]
+    return Problem(options=opts, blocks=[block], patches=patches, sources=sources,
+                   n_steps=n_steps, save_interval=save_interval)
+
+
+def random_state(n_points, n_dimensions, gamma, rng):
+    """full_rhs.f90:289-301: rho in U[0.01,10], u in U[-10,10], p in U[0.01,10]/gamma."""
+    nU = n_dimensions + 2
+    q = np.zeros((nU, n_points))
+    q[0] = rng.uniform(0.01, 10.0, n_points)
+    for d in range(n_dimensions):
+        q[1 + d] = q[0] * rng.uniform(-10.0, 10.0, n_points)
+    q[nU - 1] = (q[0] * rng.uniform(0.01, 10.0, n_points) / gamma
+                 + 0.5 / q[0] * np.sum(q[1:1 + n_dimensions] ** 2, axis=0))
+    return q
+
+
+def smooth_perturbed_state(block, n_dimensions, gamma, rng, amplitude=1e-2):
+    """A smooth non-trivial state: quiescent plus Gaussian-modulated waves."""
+    N = block.n_points
+    xs = block.coordinates
+    q = quiescent_state(N, n_dimensions, gamma)
+    phase = rng.uniform(0, 2 * np.pi, 4)
+    r2 = np.sum(xs ** 2, axis=0)
+    env = np.exp(-r2 / (2 * 6.0 ** 2))
+    rho = 1.0 + amplitude * env * np.sin(0.7 * xs[0] + phase[0])
+    u = [amplitude * env * np.cos(0.5 * xs[d % n_dimensions] + phase[1 + d % 3]) for d in range(n_dimensions)]
+    p = 1.0 / gamma + amplitude * env * np.cos(0.6 * xs[n_dimensions - 1] + phase[3])
+    q[0] = rho
+    for d in range(n_dimensions):
+        q[1 + d] = rho * u[d]
+    q[n_dimensions + 1] = p / (gamma - 1.0) + 0.5 * rho * sum(ud ** 2 for ud in u)
+    return q
+
+
+def taylor_green_3d(n=256, mach=0.1, reynolds=1600.0, cfl=0.5, n_steps=2000,
+                    dissipation_amount=0.01, power_law=0.666, bulk_viscosity_ratio=0.6):
+    """Taylor-Green vortex, PLANE periodicity on [0, 2 pi)^3:
+    rho = 1, u = sin x cos y cos z, v = -cos x sin y cos z, w = 0,
+    p = 1/(gamma M^2) + (cos 2x + cos 2y)(cos 2z + 2)/16."""
+    gamma = 1.4
+    L = 2.0 * np.pi
+    x = np.arange(n) * (L / n)
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")  # (nz, ny, nx)
+    coords = np.stack([X.ravel(), Y.ravel(), Z.ravel()])
+    N = n ** 3
+    Xr, Yr, Zr = coords
+    u = np.sin(Xr) * np.cos(Yr) * np.cos(Zr)
+    v = -np.cos(Xr) * np.sin(Yr) * np.cos(Zr)
+    w = np.zeros(N)
+    p = 1.0 / (gamma * mach ** 2) + (np.cos(2 * Xr) + np.cos(2 * Yr)) * (np.cos(2 * Zr) + 2.0) / 16.0
+    q = np.zeros((5, N))
+    q[0] = 1.0
+    q[1], q[2], q[3] = u, v, w
+    q[4] = p / (gamma - 1.0) + 0.5 * (u ** 2 + v ** 2 + w ** 2)
+    opts = Options(
+        n_dimensions=3, viscous=True, dissipation=True, composite_dissipation=False,
+        curvilinear=False, use_constant_cfl=True, cfl=cfl, enable_controller=False,
+        enable_functional=False, ratio_of_specific_heats=gamma, reynolds_number=reynolds,
+        prandtl_number=0.72, viscosity_power_law_exponent=power_law,
+        bulk_viscosity_ratio=bulk_viscosity_ratio, dissipation_amount=dissipation_amount)
+    block = Block(grid_size=(n, n, n), coordinates=np.ascontiguousarray(coords),
+                  periodicity_type=(1, 1, 1), periodic_length=(L, L, L),
+                  initial_state=q, target_state=q.copy(), mean_pressure=np.full(N, 1.0 / gamma))
+    return Problem(options=opts, blocks=[block], patches=[], sources=[], n_steps=n_steps)

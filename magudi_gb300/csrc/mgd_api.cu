@@ -1,0 +1,1067 @@
+// mgd_api.cu -- the C ABI of include/magudi_gb300.h: context lifetime,
+// one-time setup (grid metrics, patches, SAT matrices, mollifier
+// normalization), RHS and RK4 substep calls, and the graph-captured forward
+// and adjoint runs with device-resident uniform checkpointing.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mgd_internal.h"
+#include "sbp_tables.h"
+
+using namespace mgd;
+
+struct mgd_ctx {
+  Context c;
+};
+
+static std::string g_createError;
+
+#define CUDA_TRY(ctx, call)                                                        \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess) {                                                       \
+      (ctx).error = std::string(#call) + ": " + cudaGetErrorString(e_);            \
+      return 1;                                                                    \
+    }                                                                              \
+  } while (0)
+
+static int fail(Context& c, const std::string& msg) {
+  c.error = msg;
+  return 1;
+}
+
+template <class T>
+static cudaError_t devAlloc(DevBlock& b, T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e == cudaSuccess) {
+    b.allocations.push_back((void*)*p);
+    cudaMemset(*p, 0, count * sizeof(T));
+  }
+  return e;
+}
+
+static void freeBlock(DevBlock& b) {
+  for (void* p : b.allocations) cudaFree(p);
+  b.allocations.clear();
+}
+
+static int checkLaunch(Context& c) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(c, std::string("kernel launch: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+static int ncompOf(const Context& c, int field) {
+  switch (field) {
+    case MGD_FIELD_CONSERVED: case MGD_FIELD_ADJOINT: case MGD_FIELD_TARGET: case MGD_FIELD_RHS:
+      return c.nU;
+    case MGD_FIELD_METRICS: return c.nD * c.nD;
+    case MGD_FIELD_ARC_LENGTHS: return c.nD;
+    default: return 1;
+  }
+}
+
+// Definitions below take C linkage from their declarations in magudi_gb300.h.
+
+const char* mgd_last_error(const mgd_ctx* ctx) {
+  return ctx ? ctx->c.error.c_str() : g_createError.c_str();
+}
+
+int mgd_create(const mgd_options* o, mgd_ctx** out) {
+  *out = nullptr;
+  if (!o || (o->n_dimensions != 2 && o->n_dimensions != 3)) {
+    g_createError = "n_dimensions must be 2 or 3";
+    return 1;
+  }
+  if (o->composite_dissipation) {
+    g_createError = "composite_dissipation = true is not supported (pin composite_dissipation = false)";
+    return 1;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    g_createError = "no CUDA device available";
+    return 1;
+  }
+  mgd_ctx* h = new mgd_ctx();
+  Context& c = h->c;
+  c.opts = *o;
+  c.nD = o->n_dimensions;
+  c.nU = c.nD + 2;
+  cudaGetDevice(&c.device);
+  // src/SolverOptionsImpl.f90:46-71
+  Physics& P = c.phys;
+  P.g = o->ratio_of_specific_heats;
+  P.gm1 = P.g - 1.0;
+  P.gOverGm1 = P.g / P.gm1;
+  P.viscous = o->viscous;
+  P.dissipation = o->dissipation;
+  P.reInv = 0.0; P.prInv = 0.0; P.powerLawExponent = 0.0; P.laFactor = 0.0;
+  if (o->viscous) {
+    const double re = std::max(0.0, o->reynolds_number), pr = std::max(0.0, o->prandtl_number);
+    if (re <= 0.0 || pr <= 0.0) {
+      P.reInv = re; P.prInv = pr;
+      P.laFactor = (0.0 - 2.0 / 3.0);
+    } else {
+      P.reInv = 1.0 / re; P.prInv = 1.0 / pr;
+      P.powerLawExponent = o->viscosity_power_law_exponent;
+      P.laFactor = o->bulk_viscosity_ratio - 2.0 / 3.0;
+    }
+  }
+  if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    g_createError = "cudaStreamCreate failed";
+    delete h;
+    return 1;
+  }
+  uploadOperatorTables();
+  cudaMalloc((void**)&c.dCounters, 4 * sizeof(int));
+  const int init[4] = {1, 0, 1, 0};
+  cudaMemcpy(c.dCounters, init, sizeof init, cudaMemcpyHostToDevice);
+  cudaMalloc((void**)&c.dApiAmp, MGD_MAX_SOURCES * sizeof(double));
+  cudaMemset(c.dApiAmp, 0, MGD_MAX_SOURCES * sizeof(double));
+  if (cudaGetLastError() != cudaSuccess) {
+    g_createError = "device allocation failed";
+    delete h;
+    return 1;
+  }
+  *out = h;
+  return 0;
+}
+
+int mgd_destroy(mgd_ctx* h) {
+  if (!h) return 0;
+  Context& c = h->c;
+  cudaStreamSynchronize(c.stream);
+  for (DevBlock& b : c.blocks) freeBlock(b);
+  cudaFree(c.dCounters); cudaFree(c.dApiAmp); cudaFree(c.dAmp); cudaFree(c.dForcing);
+  cudaFree(c.dGradient); cudaFree(c.dPartials); cudaFree(c.dStageValues);
+  cudaFree(c.dSnapshots); cudaFree(c.dStageBuf);
+  if (c.gForward) cudaGraphExecDestroy(c.gForward);
+  if (c.gRecompute) cudaGraphExecDestroy(c.gRecompute);
+  if (c.gAdjoint) cudaGraphExecDestroy(c.gAdjoint);
+  cudaStreamDestroy(c.stream);
+  delete h;
+  return 0;
+}
+
+void* mgd_stream(mgd_ctx* h) { return h ? (void*)h->c.stream : nullptr; }
+
+long long mgd_kernel_launches(mgd_ctx* h, int reset) {
+  const long long n = h->c.launches;
+  if (reset) h->c.launches = 0;
+  return n;
+}
+
+// Grid%update (src/GridImpl.f90:746-1066) from device coordinate derivatives.
+static int computeMetrics(Context& c, DevBlock& b) {
+  const int nD = c.nD;
+  const long long N = b.v.N;
+  double* dJmi = nullptr;
+  CUDA_TRY(c, cudaMalloc((void**)&dJmi, (size_t)N * nD * nD * sizeof(double)));
+  // coordinates staged in q
+  CUDA_TRY(c, cudaMemcpyAsync(b.v.q, b.hostCoords.data(), (size_t)N * nD * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+  for (int d = 0; d < nD; ++d) launchCoordinateDerivative(c, b, d, dJmi + (size_t)N * nD * d);
+  if (checkLaunch(c)) { cudaFree(dJmi); return 1; }
+  std::vector<double> jmi((size_t)N * nD * nD);
+  CUDA_TRY(c, cudaMemcpyAsync(jmi.data(), dJmi, jmi.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  b.hostJmi = jmi;
+  for (int i = 0; i < nD * nD; ++i)
+    for (long long p = 0; p < N; ++p)
+      if (b.hostIblank[p] == 0) jmi[(size_t)N * i + p] = 0.0;
+  auto J = [&](int k, long long p) { return jmi[(size_t)N * (k - 1) + p]; };
+  std::vector<double> det(N), metrics((size_t)N * nD * nD, 0.0), arc((size_t)N * nD, 0.0);
+  auto M = [&](int k, long long p) -> double& { return metrics[(size_t)N * (k - 1) + p]; };
+  const bool curv = c.opts.curvilinear != 0;
+  if (nD == 2) {
+    for (long long p = 0; p < N; ++p) {
+      if (curv) {
+        det[p] = J(1, p) * J(4, p) - J(2, p) * J(3, p);
+        M(1, p) = J(4, p); M(2, p) = -J(3, p); M(3, p) = -J(2, p); M(4, p) = J(1, p);
+        arc[p] = std::sqrt(M(1, p) * M(1, p) + M(2, p) * M(2, p));
+        arc[N + p] = std::sqrt(M(3, p) * M(3, p) + M(4, p) * M(4, p));
+      } else {
+        det[p] = J(1, p) * J(4, p);
+        M(1, p) = J(4, p); M(4, p) = J(1, p);
+        arc[p] = std::fabs(M(1, p));
+        arc[N + p] = std::fabs(M(4, p));
+      }
+    }
+  } else {
+    bool plane = false;
+    for (int d = 0; d < 3; ++d) plane = plane || b.desc.periodicity_type[d] == MGD_PERIODIC_PLANE;
+    for (long long p = 0; p < N; ++p)
+      det[p] = curv ? J(1, p) * (J(5, p) * J(9, p) - J(8, p) * J(6, p)) +
+                          J(4, p) * (J(8, p) * J(3, p) - J(2, p) * J(9, p)) +
+                          J(7, p) * (J(2, p) * J(6, p) - J(5, p) * J(3, p))
+                    : J(1, p) * J(5, p) * J(9, p);
+    if (plane) {
+      for (long long p = 0; p < N; ++p) {
+        if (curv) {
+          M(1, p) = J(5, p) * J(9, p) - J(8, p) * J(6, p);
+          M(2, p) = J(7, p) * J(6, p) - J(4, p) * J(9, p);
+          M(3, p) = J(4, p) * J(8, p) - J(7, p) * J(5, p);
+          M(4, p) = J(8, p) * J(3, p) - J(2, p) * J(9, p);
+          M(5, p) = J(1, p) * J(9, p) - J(7, p) * J(3, p);
+          M(6, p) = J(7, p) * J(2, p) - J(1, p) * J(8, p);
+          M(7, p) = J(2, p) * J(6, p) - J(5, p) * J(3, p);
+          M(8, p) = J(4, p) * J(3, p) - J(1, p) * J(6, p);
+          M(9, p) = J(1, p) * J(5, p) - J(4, p) * J(2, p);
+        } else {
+          M(1, p) = J(5, p) * J(9, p);
+          M(5, p) = J(1, p) * J(9, p);
+          M(9, p) = J(1, p) * J(5, p);
+        }
+      }
+    } else {
+      // conservative form: metric = D_a(jmi * coordinate) - D_b(jmi * coordinate)
+      struct Term { int metric, ja, ca, da, jb, cb, db; bool cartesian; };
+      const Term terms[9] = {{1, 5, 3, 3, 8, 3, 2, true},  {2, 6, 1, 3, 9, 1, 2, false},
+                             {3, 4, 2, 3, 7, 2, 2, false}, {4, 8, 3, 1, 2, 3, 3, false},
+                             {5, 9, 1, 1, 3, 1, 3, true},  {6, 7, 2, 1, 1, 2, 3, false},
+                             {7, 2, 3, 2, 5, 3, 1, false}, {8, 3, 1, 2, 6, 1, 1, false},
+                             {9, 1, 2, 2, 4, 2, 1, true}};
+      std::vector<double> F(N), G(N);
+      double* dF = dJmi;  // reuse as scratch (jmi already on the host)
+      auto derivOfProduct = [&](int ja, int ca, int da) -> int {
+        for (long long p = 0; p < N; ++p) F[p] = J(ja, p) * b.hostCoords[(size_t)N * (ca - 1) + p];
+        CUDA_TRY(c, cudaMemcpyAsync(dF, F.data(), N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        launchApplyD1(c, b, da - 1, dF, dF + N, 1);
+        CUDA_TRY(c, cudaMemcpyAsync(G.data(), dF + N, N * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+        return 0;
+      };
+      for (const Term& t : terms) {
+        if (!t.cartesian && !curv) continue;
+        if (derivOfProduct(t.ja, t.ca, t.da)) { cudaFree(dJmi); return 1; }
+        for (long long p = 0; p < N; ++p) M(t.metric, p) = G[p];
+        if (curv) {
+          if (derivOfProduct(t.jb, t.cb, t.db)) { cudaFree(dJmi); return 1; }
+          for (long long p = 0; p < N; ++p) M(t.metric, p) = M(t.metric, p) - G[p];
+        }
+      }
+      for (int i = 1; i <= 9; ++i)
+        for (long long p = 0; p < N; ++p)
+          if (b.hostIblank[p] == 0) M(i, p) = 0.0;
+    }
+    for (long long p = 0; p < N; ++p)
+      for (int d = 0; d < 3; ++d)
+        arc[N * d + p] = curv ? std::sqrt(M(3 * d + 1, p) * M(3 * d + 1, p) + M(3 * d + 2, p) * M(3 * d + 2, p) +
+                                          M(3 * d + 3, p) * M(3 * d + 3, p))
+                              : std::fabs(M(4 * d + 1, p));
+  }
+  cudaFree(dJmi);
+  for (long long p = 0; p < N; ++p)
+    if (b.hostIblank[p] == 0) det[p] = 1.0;
+  for (long long p = 0; p < N; ++p)
+    if (!(det[p] > 0.0)) {
+      char msg[128];
+      std::snprintf(msg, sizeof msg, "Jacobian at point %lld is non-positive!", p);
+      return fail(c, msg);
+    }
+  // norm = H (per non-periodic direction) * det, jacobian = 1/det
+  const HostOp d1 = makeFirstDerivative48();
+  std::vector<double> norm(N, 1.0), jac(N), arcA((size_t)N * nD);
+  for (int d = 0; d < nD; ++d) {
+    if (b.desc.periodicity_type[d] != MGD_PERIODIC_NONE) continue;
+    const int n = b.v.gs[d];
+    const long long st = b.v.ax[d].stride;
+    for (long long p = 0; p < N; ++p) {
+      const int i = (int)((p / st) % n);
+      if (i < 8) norm[p] = d1.norm[i] * norm[p];
+      else if (i >= n - 8) norm[p] = d1.norm[n - 1 - i] * norm[p];
+    }
+  }
+  for (long long p = 0; p < N; ++p) {
+    norm[p] = norm[p] * det[p];
+    jac[p] = 1.0 / det[p];
+  }
+  for (long long k = 0; k < (long long)arc.size(); ++k) arcA[k] = -c.opts.dissipation_amount * arc[k];
+  CUDA_TRY(c, cudaMemcpyAsync((void*)b.v.metrics, metrics.data(), metrics.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+  CUDA_TRY(c, cudaMemcpyAsync((void*)b.v.jac, jac.data(), N * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+  CUDA_TRY(c, cudaMemcpyAsync((void*)b.v.arcA, arcA.data(), arcA.size() * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+  // keep host copies needed by finalize (norm, arc lengths along each direction of x)
+  b.hostNorm = norm;
+  b.hostMetricsArc = arc;
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  return 0;
+}
+
+int mgd_add_block(mgd_ctx* h, const mgd_block_desc* desc, const double* coordinates, const int* iblank) {
+  Context& c = h->c;
+  if (c.finalized) return fail(c, "mgd_add_block after mgd_finalize_setup");
+  if (!c.blocks.empty()) return fail(c, "only one block per context is supported");
+  DevBlock b;
+  b.desc = *desc;
+  BlockView& v = b.v;
+  std::memset(&v, 0, sizeof v);
+  v.nD = c.nD;
+  v.nU = c.nU;
+  for (int i = 0; i < 3; ++i) v.gs[i] = i < c.nD ? desc->grid_size[i] : 1;
+  for (int i = 0; i < c.nD; ++i)
+    if (v.gs[i] < 2 * 12 + 1 && desc->periodicity_type[i] == MGD_PERIODIC_NONE)
+      return fail(c, "each non-periodic direction needs at least 25 points for the SBP 4-8 closures");
+  v.N = (long long)v.gs[0] * v.gs[1] * v.gs[2];
+  for (int i = 0; i < 3; ++i) {
+    v.ax[i].n = v.gs[i];
+    v.ax[i].per = i < c.nD ? desc->periodicity_type[i] : MGD_PERIODIC_NONE;
+    v.ax[i].stride = i == 0 ? 1 : (i == 1 ? v.gs[0] : (long long)v.gs[0] * v.gs[1]);
+  }
+  v.curvilinear = c.opts.curvilinear;
+  const long long N = v.N;
+  const int nD = c.nD, nU = c.nU;
+  PrimLayout L{nD};
+  double *metrics, *jac, *arcA;
+  int* ib;
+  double *qt, *sponge, *mc, *mt, *meanP, *wT, *wA, *tgt, *srcG;
+  int *actIdx, *ffOf;
+  cudaError_t e = cudaSuccess;
+  auto chk = [&](cudaError_t x) { if (x != cudaSuccess) e = x; };
+  chk(devAlloc(b, &metrics, N * nD * nD));
+  chk(devAlloc(b, &jac, N));
+  chk(devAlloc(b, &arcA, N * nD));
+  chk(devAlloc(b, &ib, N));
+  chk(devAlloc(b, &v.q, N * nU));
+  chk(devAlloc(b, &v.lam, N * nU));
+  chk(devAlloc(b, &qt, N * nU));
+  chk(devAlloc(b, &v.rhs, N * nU));
+  chk(devAlloc(b, &v.b1, N * nU));
+  chk(devAlloc(b, &v.b2, N * nU));
+  chk(devAlloc(b, &v.prim, N * L.count()));
+  chk(devAlloc(b, &v.tau, N * nD * nD));
+  chk(devAlloc(b, &v.hf, N * nD));
+  chk(devAlloc(b, &v.fhat, N * nD * nU));
+  chk(devAlloc(b, &v.dq, N * nD * nU));
+  chk(devAlloc(b, &v.rcore, N * nU));
+  chk(devAlloc(b, &v.ad, N * nD * (nU - 1)));
+  chk(devAlloc(b, &sponge, N));
+  chk(devAlloc(b, &mc, N));
+  chk(devAlloc(b, &mt, N));
+  chk(devAlloc(b, &meanP, N));
+  chk(devAlloc(b, &wT, N));
+  chk(devAlloc(b, &wA, N));
+  chk(devAlloc(b, &tgt, N));
+  chk(devAlloc(b, &actIdx, N));
+  chk(devAlloc(b, &ffOf, 3 * N));
+  chk(devAlloc(b, &srcG, N * MGD_MAX_SOURCES));
+  if (e != cudaSuccess) {
+    freeBlock(b);
+    return fail(c, std::string("device allocation failed: ") + cudaGetErrorString(e));
+  }
+  v.metrics = metrics; v.jac = jac; v.arcA = arcA; v.iblank = ib; v.qt = qt;
+  v.sponge = sponge; v.mc = mc; v.mt = mt; v.meanP = meanP; v.wT = wT; v.wA = wA;
+  v.tgtCount = tgt; v.actIdx = actIdx; v.ffOfPoint = ffOf; v.srcG = srcG;
+  b.hostCoords.assign(coordinates, coordinates + (size_t)N * nD);
+  b.hostIblank.assign(iblank, iblank + N);
+  // defaults: quiescent target (State%makeQuiescent), unit mollifiers, p = 1/gamma
+  std::vector<double> tmp((size_t)N * nU, 0.0);
+  for (long long p = 0; p < N; ++p) {
+    tmp[p] = 1.0;
+    tmp[(size_t)N * (nD + 1) + p] = 1.0 / c.phys.g / (c.phys.g - 1.0);
+  }
+  CUDA_TRY(c, cudaMemcpy(qt, tmp.data(), tmp.size() * sizeof(double), cudaMemcpyHostToDevice));
+  std::vector<double> ones(N, 1.0), pm(N, 1.0 / c.phys.g);
+  CUDA_TRY(c, cudaMemcpy(mc, ones.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(mt, ones.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(meanP, pm.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(ib, iblank, N * sizeof(int), cudaMemcpyHostToDevice));
+  std::vector<int> neg(3 * N, -1);
+  CUDA_TRY(c, cudaMemcpy(actIdx, neg.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy(ffOf, neg.data(), 3 * N * sizeof(int), cudaMemcpyHostToDevice));
+  c.blocks.push_back(std::move(b));
+  if (computeMetrics(c, c.blocks.back())) {
+    freeBlock(c.blocks.back());
+    c.blocks.pop_back();
+    return 1;
+  }
+  return 0;
+}
+
+int mgd_add_patch(mgd_ctx* h, const mgd_patch_desc* p) {
+  Context& c = h->c;
+  if (c.finalized) return fail(c, "mgd_add_patch after mgd_finalize_setup");
+  if (p->type < MGD_PATCH_SAT_FAR_FIELD || p->type > MGD_PATCH_COST_TARGET)
+    return fail(c, std::string("unsupported patch type for patch '") + p->name + "'");
+  if (p->grid_index < 1) return fail(c, "patch grid index must be >= 1");
+  c.patches.push_back(*p);
+  return 0;
+}
+
+int mgd_add_acoustic_source(mgd_ctx* h, const mgd_acoustic_source* s) {
+  Context& c = h->c;
+  if ((int)c.sources.size() >= MGD_MAX_SOURCES) return fail(c, "too many acoustic sources");
+  c.sources.push_back(*s);
+  return 0;
+}
+
+static double* fieldPtr(Context& c, DevBlock& b, int field, bool write) {
+  BlockView& v = b.v;
+  switch (field) {
+    case MGD_FIELD_CONSERVED: return v.q;
+    case MGD_FIELD_ADJOINT: return v.lam;
+    case MGD_FIELD_TARGET: return (double*)v.qt;
+    case MGD_FIELD_RHS: return v.rhs;
+    case MGD_FIELD_CONTROL_MOLLIFIER: return (double*)v.mc;
+    case MGD_FIELD_TARGET_MOLLIFIER: return (double*)v.mt;
+    case MGD_FIELD_MEAN_PRESSURE: return (double*)v.meanP;
+    case MGD_FIELD_METRICS: return write ? nullptr : (double*)v.metrics;
+    case MGD_FIELD_JACOBIAN: return write ? nullptr : (double*)v.jac;
+    case MGD_FIELD_PRESSURE: return write ? nullptr : v.prim + v.N * PrimLayout{c.nD}.p();
+    case MGD_FIELD_TEMPERATURE: return write ? nullptr : v.prim + v.N * PrimLayout{c.nD}.T();
+    default: return nullptr;
+  }
+}
+
+int mgd_set_field(mgd_ctx* h, int block, int field, const double* host) {
+  Context& c = h->c;
+  if (block < 1 || block > (int)c.blocks.size()) return fail(c, "invalid block index");
+  DevBlock& b = c.blocks[block - 1];
+  if (c.finalized && (field == MGD_FIELD_CONTROL_MOLLIFIER || field == MGD_FIELD_TARGET_MOLLIFIER ||
+                      field == MGD_FIELD_TARGET))
+    return fail(c, "target state and mollifiers must be set before mgd_finalize_setup");
+  double* d = fieldPtr(c, b, field, true);
+  if (!d) return fail(c, "field is read-only or unknown");
+  CUDA_TRY(c, cudaMemcpyAsync(d, host, (size_t)b.v.N * ncompOf(c, field) * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  return 0;
+}
+
+int mgd_get_field(mgd_ctx* h, int block, int field, double* host) {
+  Context& c = h->c;
+  if (block < 1 || block > (int)c.blocks.size()) return fail(c, "invalid block index");
+  DevBlock& b = c.blocks[block - 1];
+  const size_t n = (size_t)b.v.N * ncompOf(c, field);
+  if (field == MGD_FIELD_NORM) {
+    std::copy(b.hostNorm.begin(), b.hostNorm.end(), host);
+    return 0;
+  }
+  if (field == MGD_FIELD_ARC_LENGTHS) {
+    std::copy(b.hostMetricsArc.begin(), b.hostMetricsArc.end(), host);
+    return 0;
+  }
+  double* d = fieldPtr(c, b, field, false);
+  if (!d) return fail(c, "unknown field");
+  CUDA_TRY(c, cudaMemcpyAsync(host, d, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  return 0;
+}
+
+// Patch extents with negative indices counted from the end
+// (src/PatchDescriptorImpl.f90:57-63).
+static void resolveExtent(const mgd_patch_desc& p, const int gs[3], int nD, int ext[6]) {
+  for (int i = 0; i < 3; ++i) {
+    int lo = p.extent[2 * i], hi = p.extent[2 * i + 1];
+    if (i >= nD) lo = hi = 1;
+    if (lo < 0) lo += gs[i] + 1;
+    if (hi < 0) hi += gs[i] + 1;
+    ext[2 * i] = lo;
+    ext[2 * i + 1] = hi;
+  }
+}
+
+template <class F>
+static void forExtent(const int ext[6], const int gs[3], F f) {
+  long long pi = 0;
+  for (int k = ext[4]; k <= ext[5]; ++k)
+    for (int j = ext[2]; j <= ext[3]; ++j)
+      for (int i = ext[0]; i <= ext[1]; ++i, ++pi)
+        f((long long)(i - 1) + (long long)gs[0] * ((j - 1) + (long long)gs[1] * (k - 1)), pi);
+}
+
+int mgd_finalize_setup(mgd_ctx* h) {
+  Context& c = h->c;
+  if (c.finalized) return 0;
+  if (c.blocks.empty()) return fail(c, "no block");
+  DevBlock& b = c.blocks[0];
+  const int nD = c.nD, nU = c.nU;
+  const long long N = b.v.N;
+  const int* gs = b.v.gs;
+  std::vector<int> exts;
+  for (const mgd_patch_desc& p : c.patches) {
+    if (p.grid_index != 1) return fail(c, std::string("patch '") + p.name + "' refers to a missing block");
+    int e[6];
+    resolveExtent(p, gs, nD, e);
+    for (int i = 0; i < nD; ++i)
+      if (e[2 * i] < 1 || e[2 * i + 1] > gs[i] || e[2 * i] > e[2 * i + 1])
+        return fail(c, std::string("patch '") + p.name + "' has an invalid extent");
+    if (p.type == MGD_PATCH_SAT_FAR_FIELD || p.type == MGD_PATCH_SPONGE) {
+      const int d = std::abs(p.normal_direction);
+      if (d < 1 || d > nD) return fail(c, std::string("patch '") + p.name + "' has an invalid normal direction");
+      if (p.type == MGD_PATCH_SAT_FAR_FIELD && e[2 * (d - 1)] != e[2 * (d - 1) + 1])
+        return fail(c, std::string("patch '") + p.name + "' extends more than 1 grid point along its normal direction");
+    }
+    exts.insert(exts.end(), e, e + 6);
+  }
+  // sponge strengths (computeSpongeStrengths, src/PatchFactoryImpl.f90:161-374)
+  std::vector<double> sponge(N, 0.0);
+  for (size_t pi = 0; pi < c.patches.size(); ++pi) {
+    const mgd_patch_desc& p = c.patches[pi];
+    if (p.type != MGD_PATCH_SPONGE) continue;
+    const int* e = &exts[6 * pi];
+    const int dir = std::abs(p.normal_direction) - 1;
+    const long long st = b.v.ax[dir].stride;
+    const int lo = e[2 * dir], hi = e[2 * dir + 1];
+    std::vector<double> strength;
+    forExtent(e, gs, [&](long long gi, long long) {
+      const int i = (int)((gi / st) % gs[dir]) + 1;
+      const long long line0 = gi - (long long)(i - 1) * st;
+      auto curve = [&](int i1) {
+        double s = 0.0;
+        for (int x = 0; x < nD; ++x) {
+          const double v = b.hostJmi[(size_t)N * (nD * dir + x) + line0 + (long long)(i1 - 1) * st];
+          s += v * v;
+        }
+        return std::sqrt(s);
+      };
+      double num = 0.0, den = 0.0;
+      if (p.normal_direction > 0) {
+        for (int t = lo; t <= i - 1; ++t) num += curve(t);
+        for (int t = lo; t <= hi - 1; ++t) den += curve(t);
+      } else {
+        for (int t = i + 1; t <= hi; ++t) num += curve(t);
+        for (int t = lo + 1; t <= hi; ++t) den += curve(t);
+      }
+      const double s = num / den;
+      strength.push_back(p.sponge_amount * std::pow(1.0 - s, (double)p.sponge_exponent));
+    });
+    size_t k = 0;
+    forExtent(e, gs, [&](long long gi, long long) {
+      if (b.hostIblank[gi] != 0) sponge[gi] += strength[k];
+      ++k;
+    });
+  }
+  // masks, actuator indices, cost-target counts, far-field entries
+  std::vector<double> maskT(N, 0.0), maskA(N, 0.0), tgt(N, 0.0);
+  std::vector<int> actIdx(N, -1), ffOf(3 * N, -1);
+  std::vector<int> ffPoint, ffDir, ffSigned;
+  std::vector<double> ffSigInv, ffSigV, ffSigVRaw;
+  const HostOp d1 = makeFirstDerivative48();
+  long long actOffset = 0;
+  for (size_t pi = 0; pi < c.patches.size(); ++pi) {
+    const mgd_patch_desc& p = c.patches[pi];
+    const int* e = &exts[6 * pi];
+    switch (p.type) {
+      case MGD_PATCH_COST_TARGET:
+        forExtent(e, gs, [&](long long gi, long long) {
+          maskT[gi] = 1.0;
+          if (b.hostIblank[gi] != 0) tgt[gi] += 1.0;
+        });
+        break;
+      case MGD_PATCH_ACTUATOR: {
+        bool overlap = false;
+        forExtent(e, gs, [&](long long gi, long long k) {
+          maskA[gi] = 1.0;
+          if (actIdx[gi] >= 0) overlap = true;
+          actIdx[gi] = (int)(actOffset + k);
+        });
+        if (overlap) return fail(c, "overlapping actuator patches are not supported");
+        actOffset += (long long)(e[1] - e[0] + 1) * (e[3] - e[2] + 1) * (e[5] - e[4] + 1);
+        break;
+      }
+      case MGD_PATCH_SAT_FAR_FIELD: {
+        // src/FarFieldPatchImpl.f90:53-74
+        const int dir = std::abs(p.normal_direction);
+        const double nb = d1.norm[0];
+        const double sInv = std::copysign(p.inviscid_penalty_amount, (double)p.normal_direction) / nb;
+        const double sVis = c.opts.viscous ? std::copysign(p.viscous_penalty_amount, (double)p.normal_direction) / nb : 0.0;
+        bool full = false;
+        forExtent(e, gs, [&](long long gi, long long) {
+          if (b.hostIblank[gi] == 0) return;
+          int slot = 0;
+          while (slot < 3 && ffOf[3 * gi + slot] >= 0) ++slot;
+          if (slot == 3) { full = true; return; }
+          ffOf[3 * gi + slot] = (int)ffPoint.size();
+          ffPoint.push_back((int)gi);
+          ffDir.push_back(dir);
+          ffSigned.push_back(p.normal_direction);
+          ffSigInv.push_back(sInv);
+          ffSigVRaw.push_back(sVis);
+          ffSigV.push_back(sVis);  // times 1/det below
+        });
+        if (full) return fail(c, "more than three far-field patches meet at one point");
+        break;
+      }
+      default:
+        break;
+    }
+  }
+  c.actuatorPoints = actOffset;
+  for (long long p = 0; p < N; ++p)
+    if (b.hostIblank[p] == 0) { maskT[p] = 0.0; maskA[p] = 0.0; }
+  // mollifier normalization (src/RegionImpl.f90:459-603, L1 norm)
+  std::vector<double> mcH(N), mtH(N);
+  CUDA_TRY(c, cudaMemcpy(mcH.data(), b.v.mc, N * sizeof(double), cudaMemcpyDeviceToHost));
+  CUDA_TRY(c, cudaMemcpy(mtH.data(), b.v.mt, N * sizeof(double), cudaMemcpyDeviceToHost));
+  if (c.opts.enable_controller) {
+    double s = 0.0;
+    for (long long p = 0; p < N; ++p) s += maskA[p] * b.hostNorm[p] * mcH[p];
+    for (long long p = 0; p < N; ++p) mcH[p] = mcH[p] / s;
+  }
+  if (c.opts.enable_functional) {
+    double s = 0.0;
+    for (long long p = 0; p < N; ++p) s += maskT[p] * b.hostNorm[p] * mtH[p];
+    for (long long p = 0; p < N; ++p) mtH[p] = mtH[p] / s;
+  }
+  std::vector<double> wT(N), wA(N);
+  for (long long p = 0; p < N; ++p) {
+    wT[p] = maskT[p] * b.hostNorm[p];
+    wA[p] = maskA[p] * b.hostNorm[p];
+  }
+  // acoustic source Gaussians exp(-9/(2 R^2) |x - x0|^2) (src/AcousticSourceImpl.f90:34-64)
+  std::vector<double> srcG((size_t)N * std::max<size_t>(1, c.sources.size()), 0.0);
+  for (size_t s = 0; s < c.sources.size(); ++s) {
+    const mgd_acoustic_source& src = c.sources[s];
+    const double gf = 9.0 / (2.0 * src.radius * src.radius);
+    for (long long p = 0; p < N; ++p) {
+      if (b.hostIblank[p] == 0) continue;
+      double r = 0.0;
+      for (int d = 0; d < nD; ++d) {
+        const double x = b.hostCoords[(size_t)N * d + p] - src.location[d];
+        r += x * x;
+      }
+      srcG[(size_t)N * s + p] = std::exp(-gf * r);
+    }
+  }
+  BlockView& v = b.v;
+  v.nSources = (int)c.sources.size();
+  CUDA_TRY(c, cudaMemcpy((void*)v.sponge, sponge.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy((void*)v.mc, mcH.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy((void*)v.mt, mtH.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy((void*)v.wT, wT.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy((void*)v.wA, wA.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy((void*)v.tgtCount, tgt.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy((void*)v.actIdx, actIdx.data(), N * sizeof(int), cudaMemcpyHostToDevice));
+  CUDA_TRY(c, cudaMemcpy((void*)v.ffOfPoint, ffOf.data(), 3 * N * sizeof(int), cudaMemcpyHostToDevice));
+  if (!c.sources.empty())
+    CUDA_TRY(c, cudaMemcpy((void*)v.srcG, srcG.data(), srcG.size() * sizeof(double), cudaMemcpyHostToDevice));
+  // far-field entries
+  const int nFF = (int)ffPoint.size();
+  FarFieldEntries& ff = v.ff;
+  ff.n = nFF;
+  if (nFF > 0) {
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) { if (x != cudaSuccess) e = x; };
+    chk(devAlloc(b, &ff.point, nFF));
+    chk(devAlloc(b, &ff.normalDir, nFF));
+    chk(devAlloc(b, &ff.M, (size_t)nFF * nU * nU));
+    chk(devAlloc(b, &ff.sigV, nFF));
+    chk(devAlloc(b, &ff.sigVRaw, nFF));
+    chk(devAlloc(b, &ff.visc, (size_t)nFF * nU));
+    chk(devAlloc(b, &ff.viscT, (size_t)nFF * nU));
+    double* dSig = nullptr;
+    int* dSigned = nullptr;
+    chk(devAlloc(b, &dSig, nFF));
+    chk(devAlloc(b, &dSigned, nFF));
+    if (e != cudaSuccess) return fail(c, "device allocation failed for far-field entries");
+    std::vector<double> jacH(N);
+    CUDA_TRY(c, cudaMemcpy(jacH.data(), v.jac, N * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < nFF; ++k) ffSigV[k] = ffSigV[k] * jacH[ffPoint[k]];
+    CUDA_TRY(c, cudaMemcpy(ff.point, ffPoint.data(), nFF * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(ff.normalDir, ffDir.data(), nFF * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(ff.sigV, ffSigV.data(), nFF * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(ff.sigVRaw, ffSigVRaw.data(), nFF * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(dSig, ffSigInv.data(), nFF * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(dSigned, ffSigned.data(), nFF * sizeof(int), cudaMemcpyHostToDevice));
+    launchFarFieldMatricesWith(c, b, dSig, dSigned);
+    if (c.opts.viscous) {
+      // target viscous fluxes: primitives and stress of the target state
+      launchPrims(c, b, v.qt, false);
+      double* qSave = v.q;
+      v.q = (double*)v.qt;
+      launchGradFlux(c, b, false, false, true, nullptr, 0, false);
+      v.q = qSave;
+      launchFarFieldTargetVisc(c, b);
+    }
+    if (checkLaunch(c)) return 1;
+    CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  }
+  c.finalized = true;
+  return 0;
+}
+
+static RunScalars apiScalars(Context& c) {
+  RunScalars r{};
+  r.step = c.dCounters + 2;
+  r.segBase = c.dCounters + 3;
+  r.amp = c.dApiAmp;
+  r.dt = c.opts.time_step_size;
+  r.adjointForcingSwitch = c.opts.adjoint_forcing_switch;
+  r.nPartialBlocks = stageBlocks(c.blocks[0]);
+  return r;
+}
+
+static int setApiTime(Context& c, double time) {
+  double amp[MGD_MAX_SOURCES] = {0};
+  const double pi = 4.0 * std::atan(1.0);
+  for (size_t s = 0; s < c.sources.size(); ++s) {
+    const mgd_acoustic_source& src = c.sources[s];
+    amp[s] = src.amplitude * std::cos(2.0 * pi * src.frequency * time + src.phase);
+  }
+  CUDA_TRY(c, cudaMemcpyAsync(c.dApiAmp, amp, sizeof amp, cudaMemcpyHostToDevice, c.stream));
+  return 0;
+}
+
+static int requireReady(Context& c) {
+  if (!c.finalized) return fail(c, "mgd_finalize_setup has not been called");
+  return 0;
+}
+
+int mgd_update_state(mgd_ctx* h) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  DevBlock& b = c.blocks[0];
+  launchPrims(c, b, b.v.q, false);
+  if (c.phys.viscous) launchGradFlux(c, b, false, false, true, nullptr, 0, false);
+  if (checkLaunch(c)) return 1;
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  return 0;
+}
+
+int mgd_compute_rhs(mgd_ctx* h, int mode, double time, double adjoint_forcing_factor) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  DevBlock& b = c.blocks[0];
+  RunScalars rs = apiScalars(c);
+  if (mode == MGD_FORWARD) {
+    if (setApiTime(c, time)) return 1;
+    launchPrims(c, b, b.v.q, false);
+    launchGradFlux(c, b, true, true, false, &rs, 1, false);
+    launchForwardRhs(c, b, 0, rs, true, false, false);
+  } else if (mode == MGD_ADJOINT) {
+    launchPrims(c, b, b.v.q, false);
+    if (c.phys.viscous) launchGradFlux(c, b, false, false, true, &rs, 1, false);
+    launchAdjointA(c, b, rs, 1, false);
+    launchAdjointB(c, b, 0, rs, 1, adjoint_forcing_factor, true);
+  } else {
+    return fail(c, "mode must be MGD_FORWARD or MGD_ADJOINT");
+  }
+  if (checkLaunch(c)) return 1;
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  return 0;
+}
+
+int mgd_update_adjoint_forcing(mgd_ctx* h, int no_adjoint_forcing) {
+  // The adjoint forcing is evaluated inside the adjoint RHS from the current
+  // forward state; this call only records whether it is switched off.
+  Context& c = h->c;
+  c.opts.adjoint_forcing_switch = no_adjoint_forcing ? 0 : 1;
+  return 0;
+}
+
+static int reduceToHost(Context& c, int nSlots, std::vector<double>& out) {
+  const int nb = stageBlocks(c.blocks[0]);
+  if (c.stageValueCapacity < nSlots) {
+    cudaFree(c.dStageValues);
+    CUDA_TRY(c, cudaMalloc((void**)&c.dStageValues, (size_t)std::max(1, nSlots) * sizeof(double)));
+    c.stageValueCapacity = nSlots;
+  }
+  launchReducePartials(c, c.dPartials, nb, nSlots, c.dStageValues);
+  out.resize(nSlots);
+  if (nSlots > 0)
+    CUDA_TRY(c, cudaMemcpyAsync(out.data(), c.dStageValues, (size_t)nSlots * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  return checkLaunch(c);
+}
+
+static int ensurePartials(Context& c, long long nSlots) {
+  const long long need = nSlots * stageBlocks(c.blocks[0]);
+  if (c.partialCapacity < need) {
+    cudaFree(c.dPartials);
+    CUDA_TRY(c, cudaMalloc((void**)&c.dPartials, (size_t)std::max(1LL, need) * sizeof(double)));
+    c.partialCapacity = need;
+  }
+  return 0;
+}
+
+int mgd_compute_functional(mgd_ctx* h, double* value) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  DevBlock& b = c.blocks[0];
+  const long long N = b.v.N;
+  std::vector<double> w(N), mt(N), mp(N), pr(N);
+  CUDA_TRY(c, cudaMemcpy(w.data(), b.v.wT, N * sizeof(double), cudaMemcpyDeviceToHost));
+  CUDA_TRY(c, cudaMemcpy(mt.data(), b.v.mt, N * sizeof(double), cudaMemcpyDeviceToHost));
+  CUDA_TRY(c, cudaMemcpy(mp.data(), b.v.meanP, N * sizeof(double), cudaMemcpyDeviceToHost));
+  CUDA_TRY(c, cudaMemcpy(pr.data(), b.v.prim + N * PrimLayout{c.nD}.p(), N * sizeof(double), cudaMemcpyDeviceToHost));
+  double s = 0.0;
+  for (long long p = 0; p < N; ++p) {
+    const double F = pr[p] - mp[p];
+    s += w[p] * (F * F * mt[p]);
+  }
+  *value = s;
+  return 0;
+}
+
+int mgd_compute_sensitivity(mgd_ctx* h, double* value) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  DevBlock& b = c.blocks[0];
+  const long long N = b.v.N;
+  std::vector<double> w(N), mc(N), lam(N);
+  CUDA_TRY(c, cudaMemcpy(w.data(), b.v.wA, N * sizeof(double), cudaMemcpyDeviceToHost));
+  CUDA_TRY(c, cudaMemcpy(mc.data(), b.v.mc, N * sizeof(double), cudaMemcpyDeviceToHost));
+  CUDA_TRY(c, cudaMemcpy(lam.data(), b.v.lam + N * (c.nD + 1), N * sizeof(double), cudaMemcpyDeviceToHost));
+  double s = 0.0;
+  for (long long p = 0; p < N; ++p) {
+    const double F = lam[p] * mc[p];
+    s += w[p] * (F * F);
+  }
+  *value = s;
+  return 0;
+}
+
+int mgd_rk4_substep(mgd_ctx* h, int mode, double* time, double dt, int stage) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  if (stage < 1 || stage > 4) return fail(c, "stage must be 1..4");
+  DevBlock& b = c.blocks[0];
+  RunScalars rs = apiScalars(c);
+  rs.dt = dt;
+  if (mode == MGD_FORWARD) {
+    if (stage == 2 || stage == 4) *time = *time + dt / 2.0;
+    if (setApiTime(c, *time)) return 1;
+    launchPrims(c, b, b.v.q, false);
+    launchGradFlux(c, b, true, true, false, &rs, 1, false);
+    launchForwardRhs(c, b, stage, rs, true, false, false);
+  } else if (mode == MGD_ADJOINT) {
+    const double factor = c.opts.adjoint_forcing_switch ? (stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0)) : 0.0;
+    launchPrims(c, b, b.v.q, false);
+    if (c.phys.viscous) launchGradFlux(c, b, false, false, true, &rs, 1, false);
+    launchAdjointA(c, b, rs, 1, false);
+    launchAdjointB(c, b, stage, rs, 1, factor, true);
+    if (stage == 3 || stage == 1) *time = *time - dt / 2.0;
+  } else {
+    return fail(c, "mode must be MGD_FORWARD or MGD_ADJOINT");
+  }
+  if (checkLaunch(c)) return 1;
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  return 0;
+}
+
+int mgd_actuator_patch_size(mgd_ctx* h, long long* n) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  *n = c.actuatorPoints;
+  return 0;
+}
+
+int mgd_set_control_forcing(mgd_ctx* h, const double* host, long long n_entries) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  cudaFree(c.dForcing);
+  c.dForcing = nullptr;
+  c.nForcingEntries = 0;
+  const size_t n = (size_t)std::max(0LL, n_entries) * c.actuatorPoints;
+  if (n == 0) return 0;
+  CUDA_TRY(c, cudaMalloc((void**)&c.dForcing, n * sizeof(double)));
+  CUDA_TRY(c, cudaMemcpy(c.dForcing, host, n * sizeof(double), cudaMemcpyHostToDevice));
+  c.nForcingEntries = n_entries;
+  return 0;
+}
+
+static const double kRkNorm[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+
+static RunScalars runScalars(Context& c) {
+  RunScalars r{};
+  r.step = c.dCounters + 0;
+  r.segBase = c.dCounters + 1;
+  r.amp = c.dAmp;
+  r.forcing = c.dForcing;
+  r.nForcingEntries = c.nForcingEntries;
+  r.nSteps = c.runSteps;
+  r.P = c.actuatorPoints;
+  r.gradient = c.dGradient;
+  r.partials = c.dPartials;
+  r.nPartialBlocks = stageBlocks(c.blocks[0]);
+  r.stageBuf = c.dStageBuf;
+  r.dt = c.opts.time_step_size;
+  r.adjointForcingSwitch = c.opts.adjoint_forcing_switch;
+  return r;
+}
+
+static int setCounters(Context& c, int step, int segBase) {
+  const int v[2] = {step, segBase};
+  CUDA_TRY(c, cudaMemcpyAsync(c.dCounters, v, sizeof v, cudaMemcpyHostToDevice, c.stream));
+  return 0;
+}
+
+// Captures `body` into an executable graph on the context stream.
+template <class F>
+static int capture(Context& c, cudaGraphExec_t* exec, F body) {
+  if (*exec) {
+    cudaGraphExecDestroy(*exec);
+    *exec = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  CUDA_TRY(c, cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+  body();
+  CUDA_TRY(c, cudaStreamEndCapture(c.stream, &g));
+  CUDA_TRY(c, cudaGraphInstantiate(exec, g, 0));
+  cudaGraphDestroy(g);
+  return 0;
+}
+
+int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, double* cost) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  if (n_steps < 1) return fail(c, "n_steps must be >= 1");
+  if (save_interval < 1) save_interval = n_steps;
+  DevBlock& b = c.blocks[0];
+  const long long N = b.v.N;
+  const int nU = c.nU;
+  const double dt = c.opts.time_step_size;
+  if (!(dt > 0.0)) return fail(c, "time_step_size must be positive (constant-CFL mode is not supported)");
+  c.runSteps = n_steps;
+  c.saveInterval = save_interval;
+  c.runT0 = t0;
+  // stage times as Solver%runForward accumulates them (src/RK4IntegratorImpl.f90:95-140)
+  c.stageTimes.assign((size_t)4 * n_steps, 0.0);
+  double t = t0;
+  for (int s = 0; s < n_steps; ++s)
+    for (int i = 1; i <= 4; ++i) {
+      if (i == 2 || i == 4) t = t + dt / 2.0;
+      c.stageTimes[(size_t)4 * s + i - 1] = t;
+    }
+  const int nSrc = (int)c.sources.size();
+  const long long nAmp = (long long)4 * n_steps * std::max(1, nSrc);
+  if (c.ampCapacity < nAmp) {
+    cudaFree(c.dAmp);
+    CUDA_TRY(c, cudaMalloc((void**)&c.dAmp, nAmp * sizeof(double)));
+    c.ampCapacity = nAmp;
+  }
+  {
+    std::vector<double> amp(nAmp, 0.0);
+    const double pi = 4.0 * std::atan(1.0);
+    for (long long k = 0; k < 4LL * n_steps; ++k)
+      for (int s = 0; s < nSrc; ++s) {
+        const mgd_acoustic_source& src = c.sources[s];
+        amp[k * nSrc + s] = src.amplitude * std::cos(2.0 * pi * src.frequency * c.stageTimes[k] + src.phase);
+      }
+    CUDA_TRY(c, cudaMemcpy(c.dAmp, amp.data(), nAmp * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  const long long nSnap = n_steps / save_interval + 2;
+  if (c.snapshotCapacity < nSnap * nU * N) {
+    cudaFree(c.dSnapshots);
+    CUDA_TRY(c, cudaMalloc((void**)&c.dSnapshots, (size_t)nSnap * nU * N * sizeof(double)));
+    c.snapshotCapacity = nSnap * nU * N;
+  }
+  if (ensurePartials(c, 4LL * n_steps)) return 1;
+  const long long nGrad = 4LL * n_steps * std::max(1LL, c.actuatorPoints);
+  if (c.gradientCapacity < nGrad) {
+    cudaFree(c.dGradient);
+    CUDA_TRY(c, cudaMalloc((void**)&c.dGradient, nGrad * sizeof(double)));
+    c.gradientCapacity = nGrad;
+  }
+  const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
+  const bool functional = c.opts.enable_functional != 0;
+  RunScalars rs = runScalars(c);
+  // state%update of the initial condition, step-0 snapshot
+  launchPrims(c, b, b.v.q, false);
+  launchSnapshot(c, b, c.dSnapshots, save_interval, true);
+  if (setCounters(c, 1, 0)) return 1;
+  if (capture(c, &c.gForward, [&]() {
+        for (int i = 1; i <= 4; ++i) {
+          launchGradFlux(c, b, true, true, false, &rs, i, false);
+          launchForwardRhs(c, b, i, rs, false, functional, controller);
+        }
+        launchSnapshot(c, b, c.dSnapshots, save_interval, false);
+        launchStepAdvance(c, 1);
+      }))
+    return 1;
+  const long long before = c.launches;
+  const long long perStep = before;  // launches recorded during capture
+  (void)perStep;
+  for (int s = 0; s < n_steps; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gForward, c.stream));
+  if (checkLaunch(c)) return 1;
+  double J = 0.0;
+  if (functional) {
+    std::vector<double> vals;
+    if (reduceToHost(c, 4 * n_steps, vals)) return 1;
+    for (int s = 0; s < n_steps; ++s)
+      for (int i = 0; i < 4; ++i) J = J + kRkNorm[i] * dt * vals[(size_t)4 * s + i];
+  } else {
+    CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  }
+  *cost = J;
+  return 0;
+}
+
+int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  if (c.runSteps < 1) return fail(c, "mgd_run_adjoint needs a preceding mgd_run_forward");
+  DevBlock& b = c.blocks[0];
+  const long long N = b.v.N;
+  const int nU = c.nU, T = c.runSteps, S = c.saveInterval;
+  const double dt = c.opts.time_step_size;
+  const long long needStage = 4LL * S * nU * N;
+  if (c.stageBufCapacity < needStage) {
+    cudaFree(c.dStageBuf);
+    CUDA_TRY(c, cudaMalloc((void**)&c.dStageBuf, needStage * sizeof(double)));
+    c.stageBufCapacity = needStage;
+  }
+  const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
+  RunScalars rs = runScalars(c);
+  // adjoint initial condition at the final state (its primitives are current)
+  launchPrims(c, b, b.v.q, false);
+  launchAdjointInitial(c, b, c.opts.adjoint_forcing_switch ? -dt / 6.0 : 0.0);
+  if (capture(c, &c.gRecompute, [&]() {
+        for (int i = 1; i <= 4; ++i) {
+          launchGradFlux(c, b, true, true, false, &rs, i, true);
+          launchForwardRhs(c, b, i, rs, false, false, controller);
+        }
+        launchStepAdvance(c, 1);
+      }))
+    return 1;
+  if (capture(c, &c.gAdjoint, [&]() {
+        for (int i = 4; i >= 1; --i) {
+          launchPrims(c, b, nullptr, true, &rs, i);
+          if (c.phys.viscous) launchGradFlux(c, b, false, false, true, &rs, i, false);
+          launchAdjointA(c, b, rs, i, true);
+          launchAdjointB(c, b, i, rs, i, 0.0, false);
+        }
+        launchStepAdvance(c, -1);
+      }))
+    return 1;
+  const int nSeg = (T + S - 1) / S;
+  for (int k = nSeg - 1; k >= 0; --k) {
+    const int L = k * S, end = std::min(T, L + S);
+    // UniformCheckpointer: reload the snapshot and recompute the segment's stages
+    CUDA_TRY(c, cudaMemcpyAsync(b.v.q, c.dSnapshots + (size_t)k * nU * N, (size_t)nU * N * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c.stream));
+    launchPrims(c, b, b.v.q, false);
+    if (setCounters(c, L + 1, L)) return 1;
+    for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gRecompute, c.stream));
+    if (setCounters(c, end, L)) return 1;
+    for (int s = end; s >= L + 1; --s) CUDA_TRY(c, cudaGraphLaunch(c.gAdjoint, c.stream));
+  }
+  if (checkLaunch(c)) return 1;
+  std::vector<double> vals;
+  if (reduceToHost(c, 4 * T, vals)) return 1;
+  double sum = 0.0;
+  for (int n = T; n >= 1; --n)
+    for (int i = 4; i >= 1; --i) {
+      const long long entry = (long long)(T - n) * 4 + (4 - i);
+      sum = sum + kRkNorm[i - 1] * dt * vals[entry];
+    }
+  *sensitivity = sum;
+  return 0;
+}
+
+int mgd_get_gradient(mgd_ctx* h, double* host, long long n_entries) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  const long long avail = 4LL * c.runSteps;
+  const long long n = std::min(n_entries, avail) * c.actuatorPoints;
+  if (n <= 0) return 0;
+  CUDA_TRY(c, cudaMemcpy(host, c.dGradient, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+  return 0;
+}
+

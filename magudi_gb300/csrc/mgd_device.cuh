@@ -1,0 +1,341 @@
+// mgd_device.cuh -- device-side building blocks: SBP operator application
+// from constant-memory tables and the pointwise gas dynamics of magudi's
+// CNSHelper (src/CNSHelperImpl.f90), all in FP64.
+//
+// Design note: on GB300 FP64 arithmetic runs on a narrow pipe while integer,
+// FP32 and load/store issue slots are plentiful, so these routines minimise
+// FP64 instruction count (no recomputation, algebraic sharing) and leave
+// index arithmetic and loads unoptimised.
+#pragma once
+
+#include <cstdint>
+
+namespace mgd {
+
+enum OpId { OP_D1 = 0, OP_D1ADJ = 1, OP_DISS = 2, OP_DISST = 3, OP_COUNT = 4 };
+
+// Compile-time shape of each operator's boundary block.
+template <int OP> struct OpShape;
+template <> struct OpShape<OP_D1> { static constexpr int depth = 8, width = 12, half = 4; static constexpr bool skew = true; };
+template <> struct OpShape<OP_D1ADJ> { static constexpr int depth = 12, width = 16, half = 4; static constexpr bool skew = true; };
+template <> struct OpShape<OP_DISS> { static constexpr int depth = 2, width = 5, half = 2; static constexpr bool skew = false; };
+template <> struct OpShape<OP_DISST> { static constexpr int depth = 8, width = 10, half = 2; static constexpr bool skew = false; };
+
+struct OpTables {
+  double interior[OP_COUNT][9];         // offsets -half..half
+  double left[OP_COUNT][16 * 12];       // depth x width row-major
+};
+
+// One copy per translation unit; only mgd_kernels.cu launches kernels and fills it.
+static __constant__ OpTables c_ops;
+
+// One direction of a block: n points along it, memory stride, periodicity.
+struct Axis {
+  int n;
+  int per;          // 0 none, 1 plane, 2 overlap
+  long long stride;
+};
+
+// Index of point i + j along a periodic line (fillGhostPoints for one
+// process, src/MPIHelperImpl.f90:113-390): PLANE wraps with period n;
+// OVERLAP skips the duplicated end point.
+__device__ __forceinline__ int wrapIndex(int i, int n, int per) {
+  if (i < 0) return per == 2 ? i + n - 1 : i + n;
+  if (i >= n) return per == 2 ? i - n + 1 : i - n;
+  return i;
+}
+
+// y_i = (Op x)_i along one axis; `line` points at element 0 of the pencil.
+// Follows applyOperator_{1,2,3} (src/StencilOperatorImpl.f90:35-457):
+// sum over taps left to right, boundary rows from the left block and its
+// (skew-)reflection on the right.
+template <int OP>
+__device__ __forceinline__ double applyOp(const double* __restrict__ line, int i, const Axis& ax) {
+  using S = OpShape<OP>;
+  const double* __restrict__ cin = c_ops.interior[OP];
+  const long long st = ax.stride;
+  if (ax.per == 0) {
+    if (i < S::depth) {
+      const double* __restrict__ row = &c_ops.left[OP][i * S::width];
+      double s = row[0] * __ldg(line);
+#pragma unroll
+      for (int k = 1; k < S::width; ++k) s += row[k] * __ldg(line + k * st);
+      return s;
+    }
+    if (i >= ax.n - S::depth) {
+      const int m = ax.n - 1 - i;
+      const double* __restrict__ row = &c_ops.left[OP][m * S::width];
+      const double* __restrict__ end = line + (long long)(ax.n - S::width) * st;
+      // right block = reflection of the left block, negated for skew operators
+      double s = row[S::width - 1] * __ldg(end);
+#pragma unroll
+      for (int k = 1; k < S::width; ++k) s += row[S::width - 1 - k] * __ldg(end + k * st);
+      return S::skew ? -s : s;
+    }
+    const double* __restrict__ c = line + (long long)i * st;
+    if (S::skew) {
+      double s = cin[S::half + 1] * (__ldg(c + st) - __ldg(c - st));
+#pragma unroll
+      for (int j = 2; j <= S::half; ++j) s += cin[S::half + j] * (__ldg(c + j * st) - __ldg(c - j * st));
+      return s;
+    } else {
+      double s = cin[S::half + 1] * (__ldg(c + st) + __ldg(c - st));
+#pragma unroll
+      for (int j = 2; j <= S::half; ++j) s += cin[S::half + j] * (__ldg(c + j * st) + __ldg(c - j * st));
+      return s + cin[S::half] * __ldg(c);
+    }
+  }
+  // periodic: interior stencil everywhere with wrapped indices
+  auto at = [&](int j) { return __ldg(line + (long long)wrapIndex(i + j, ax.n, ax.per) * st); };
+  if (S::skew) {
+    double s = cin[S::half + 1] * (at(1) - at(-1));
+#pragma unroll
+    for (int j = 2; j <= S::half; ++j) s += cin[S::half + j] * (at(j) - at(-j));
+    return s;
+  } else {
+    double s = cin[S::half + 1] * (at(1) + at(-1));
+#pragma unroll
+    for (int j = 2; j <= S::half; ++j) s += cin[S::half + j] * (at(j) + at(-j));
+    return s + cin[S::half] * at(0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pointwise gas dynamics (FP64). Layouts follow the reference: metrics of
+// direction i are m[nD*i + 0..nD-1]; stress tau[nD*c + d] = tau_{c,d}.
+// ---------------------------------------------------------------------------
+
+// Incoming Jacobian A+ of the inviscid flux along `metrics` for a state of
+// conserved variables cv (computeIncomingJacobianOfInviscidFlux{2D,3D},
+// src/CNSHelperImpl.f90:1669-2343). out(i,j) at out[i + nU*j].
+template <int ND>
+__host__ __device__ inline void incomingJacobian(const double* cv, const double* metrics, double g,
+                                                 int incomingDirection, double* out) {
+  constexpr int nU = ND + 2;
+  double arc = 0.0;
+  for (int d = 0; d < ND; ++d) arc += metrics[d] * metrics[d];
+  arc = sqrt(arc);
+  double nm[3];
+  for (int d = 0; d < ND; ++d) nm[d] = metrics[d] / arc;
+  const double v = 1.0 / cv[0];
+  double u[3], u2 = 0.0;
+  for (int d = 0; d < ND; ++d) u[d] = v * cv[d + 1];
+  for (int d = 0; d < ND; ++d) u2 += u[d] * u[d];
+  const double T = g * (v * cv[ND + 1] - 0.5 * u2);
+  double U = 0.0;
+  for (int d = 0; d < ND; ++d) U += nm[d] * u[d];
+  const double c = sqrt((g - 1.0) * T);
+  const double phi2 = 0.5 * (g - 1.0) * u2;
+  const double rho = cv[0];
+  double R[nU][nU], L[nU][nU], lam[nU];
+  if constexpr (ND == 2) {
+    lam[0] = U; lam[1] = U; lam[2] = U + c; lam[3] = U - c;
+    R[0][0] = 1.0; R[1][0] = u[0]; R[2][0] = u[1]; R[3][0] = phi2 / (g - 1.0);
+    R[0][1] = 0.0; R[1][1] = nm[1] * rho; R[2][1] = -nm[0] * rho;
+    R[3][1] = rho * (nm[1] * u[0] - nm[0] * u[1]);
+    R[0][2] = 1.0; R[1][2] = u[0] + nm[0] * c; R[2][2] = u[1] + nm[1] * c;
+    R[3][2] = T + phi2 / (g - 1.0) + c * U;
+    R[0][3] = 1.0; R[1][3] = u[0] - nm[0] * c; R[2][3] = u[1] - nm[1] * c;
+    R[3][3] = T + phi2 / (g - 1.0) - c * U;
+    L[0][0] = 1.0 - phi2 / (c * c);
+    L[1][0] = -v * (nm[1] * u[0] - nm[0] * u[1]);
+    L[2][0] = 0.5 * (phi2 / (c * c) - U / c);
+    L[3][0] = 0.5 * (phi2 / (c * c) + U / c);
+    L[0][1] = u[0] / T; L[1][1] = v * nm[1];
+    L[2][1] = -0.5 * (u[0] / T - nm[0] / c); L[3][1] = -0.5 * (u[0] / T + nm[0] / c);
+    L[0][2] = u[1] / T; L[1][2] = -v * nm[0];
+    L[2][2] = -0.5 * (u[1] / T - nm[1] / c); L[3][2] = -0.5 * (u[1] / T + nm[1] / c);
+    L[0][3] = -1.0 / T; L[1][3] = 0.0; L[2][3] = 0.5 / T; L[3][3] = 0.5 / T;
+  } else {
+    lam[0] = U; lam[1] = U; lam[2] = U; lam[3] = U + c; lam[4] = U - c;
+    const double h0 = phi2 / (g - 1.0);
+    const double q = 1.0 - phi2 / (c * c);
+    double (*r)[nU] = R;
+    r[0][0] = nm[0]; r[1][0] = nm[0] * u[0]; r[2][0] = nm[0] * u[1] + rho * nm[2];
+    r[3][0] = nm[0] * u[2] - rho * nm[1];
+    r[4][0] = rho * (nm[2] * u[1] - nm[1] * u[2]) + h0 * nm[0];
+    r[0][1] = nm[1]; r[1][1] = nm[1] * u[0] - rho * nm[2]; r[2][1] = nm[1] * u[1];
+    r[3][1] = nm[1] * u[2] + rho * nm[0];
+    r[4][1] = rho * (nm[0] * u[2] - nm[2] * u[0]) + h0 * nm[1];
+    r[0][2] = nm[2]; r[1][2] = nm[2] * u[0] + rho * nm[1]; r[2][2] = nm[2] * u[1] - rho * nm[0];
+    r[3][2] = nm[2] * u[2];
+    r[4][2] = rho * (nm[1] * u[0] - nm[0] * u[1]) + h0 * nm[2];
+    r[0][3] = 1.0; r[1][3] = u[0] + nm[0] * c; r[2][3] = u[1] + nm[1] * c;
+    r[3][3] = u[2] + nm[2] * c; r[4][3] = T + h0 + c * U;
+    r[0][4] = 1.0; r[1][4] = u[0] - nm[0] * c; r[2][4] = u[1] - nm[1] * c;
+    r[3][4] = u[2] - nm[2] * c; r[4][4] = T + h0 - c * U;
+    double (*l)[nU] = L;
+    l[0][0] = nm[0] * q - v * (nm[2] * u[1] - nm[1] * u[2]);
+    l[1][0] = nm[1] * q - v * (nm[0] * u[2] - nm[2] * u[0]);
+    l[2][0] = nm[2] * q - v * (nm[1] * u[0] - nm[0] * u[1]);
+    l[3][0] = 0.5 * (phi2 / (c * c) - U / c);
+    l[4][0] = 0.5 * (phi2 / (c * c) + U / c);
+    l[0][1] = nm[0] * u[0] / T; l[1][1] = nm[1] * u[0] / T - v * nm[2];
+    l[2][1] = nm[2] * u[0] / T + v * nm[1];
+    l[3][1] = -0.5 * (u[0] / T - nm[0] / c); l[4][1] = -0.5 * (u[0] / T + nm[0] / c);
+    l[0][2] = nm[0] * u[1] / T + v * nm[2]; l[1][2] = nm[1] * u[1] / T;
+    l[2][2] = nm[2] * u[1] / T - v * nm[0];
+    l[3][2] = -0.5 * (u[1] / T - nm[1] / c); l[4][2] = -0.5 * (u[1] / T + nm[1] / c);
+    l[0][3] = nm[0] * u[2] / T - v * nm[1]; l[1][3] = nm[1] * u[2] / T + v * nm[0];
+    l[2][3] = nm[2] * u[2] / T;
+    l[3][3] = -0.5 * (u[2] / T - nm[2] / c); l[4][3] = -0.5 * (u[2] / T + nm[2] / c);
+    l[0][4] = -nm[0] / T; l[1][4] = -nm[1] / T; l[2][4] = -nm[2] / T;
+    l[3][4] = 0.5 / T; l[4][4] = 0.5 / T;
+  }
+  for (int k = 0; k < nU; ++k) {
+    lam[k] = arc * lam[k];
+    if (incomingDirection * lam[k] < 0.0) lam[k] = 0.0;
+  }
+  for (int j = 0; j < nU; ++j)
+    for (int i = 0; i < nU; ++i) {
+      double s = R[i][0] * lam[0] * L[0][j];
+      for (int k = 1; k < nU; ++k) s += R[i][k] * lam[k] * L[k][j];
+      out[i + nU * j] = s;
+    }
+}
+
+// y += (A_i - B1_i)^T w for the inviscid flux Jacobian A along metric m
+// (computeJacobianOfInviscidFlux{2D,3D}, src/CNSHelperImpl.f90:1098-1445) and
+// the first partial viscous Jacobian B1 (computeFirstPartialViscousJacobian,
+// :2412-2601), formed column by column and contracted immediately.
+template <int ND, bool VISC>
+__device__ __forceinline__ void addFluxJacobianTransposeProduct(
+    const double* m, const double* u, double T, double v, double g, double n,
+    const double* tau, const double* hf, const double* w, double* y) {
+  constexpr int nU = ND + 2, E = ND + 1;
+  double U = m[0] * u[0];
+  for (int d = 1; d < ND; ++d) U += m[d] * u[d];
+  double u2 = u[0] * u[0];
+  for (int d = 1; d < ND; ++d) u2 += u[d] * u[d];
+  const double phi2 = 0.5 * (g - 1.0) * u2;
+  // column 0 of A: (0, phi2 m_d - U u_d, U((g-2)/(g-1) phi2 - T))
+  double ct[3] = {0.0, 0.0, 0.0}, t1 = 0.0, uct = 0.0, nTv = 0.0;
+  if (VISC) {
+    for (int a = 0; a < ND; ++a) {
+      double s = m[0] * tau[ND * a];
+      for (int d = 1; d < ND; ++d) s += m[d] * tau[ND * a + d];
+      ct[a] = s;
+    }
+    double cq = m[0] * hf[0];
+    for (int d = 1; d < ND; ++d) cq += m[d] * hf[d];
+    uct = u[0] * ct[0];
+    for (int d = 1; d < ND; ++d) uct += u[d] * ct[d];
+    t1 = uct - cq;
+    nTv = n * g * v / T;
+  }
+  // y_j += sum_i (A(i,j) - B(i,j)) w_i for each column j
+  {
+    // j = 0
+    double s = 0.0;
+    for (int d = 0; d < ND; ++d) s += (phi2 * m[d] - U * u[d]) * w[1 + d];
+    s += U * ((g - 2.0) / (g - 1.0) * phi2 - T) * w[E];
+    if (VISC) {
+      const double t2 = nTv * (phi2 / (g - 1.0) - T / g);
+      double sb = 0.0;
+      for (int d = 0; d < ND; ++d) sb += t2 * ct[d] * w[1 + d];
+      sb += (t2 * t1 - v * uct) * w[E];
+      s -= sb;
+    }
+    y[0] += s;
+  }
+  for (int c = 0; c < ND; ++c) {
+    double s = m[c] * w[0];
+    for (int d = 0; d < ND; ++d) {
+      const double a = d == c ? U - (g - 2.0) * u[c] * m[c] : u[d] * m[c] - (g - 1.0) * u[c] * m[d];
+      s += a * w[1 + d];
+    }
+    s += ((T + phi2 / (g - 1.0)) * m[c] - (g - 1.0) * U * u[c]) * w[E];
+    if (VISC) {
+      const double t2 = -nTv * u[c];
+      double sb = 0.0;
+      for (int d = 0; d < ND; ++d) sb += t2 * ct[d] * w[1 + d];
+      sb += (t2 * t1 + v * ct[c]) * w[E];
+      s -= sb;
+    }
+    y[1 + c] += s;
+  }
+  {
+    double s = 0.0;
+    for (int d = 0; d < ND; ++d) s += (g - 1.0) * m[d] * w[1 + d];
+    s += g * U * w[E];
+    if (VISC) {
+      double sb = 0.0;
+      for (int d = 0; d < ND; ++d) sb += nTv * ct[d] * w[1 + d];
+      sb += nTv * t1 * w[E];
+      s -= sb;
+    }
+    y[E] += s;
+  }
+  (void)nU;
+}
+
+// y += B1^T w alone (first partial viscous Jacobian transpose product), used
+// by the far-field adjoint viscous penalty (src/FarFieldPatchImpl.f90:237-257).
+template <int ND>
+__device__ __forceinline__ void firstPartialViscousTransposeProduct(
+    const double* m, const double* u, double T, double v, double g, double n,
+    const double* tau, const double* hf, const double* w, double* y) {
+  constexpr int E = ND + 1;
+  double u2 = u[0] * u[0];
+  for (int d = 1; d < ND; ++d) u2 += u[d] * u[d];
+  const double phi2 = 0.5 * (g - 1.0) * u2;
+  double ct[3];
+  for (int a = 0; a < ND; ++a) {
+    double s = m[0] * tau[ND * a];
+    for (int d = 1; d < ND; ++d) s += m[d] * tau[ND * a + d];
+    ct[a] = s;
+  }
+  double cq = m[0] * hf[0];
+  for (int d = 1; d < ND; ++d) cq += m[d] * hf[d];
+  double uct = u[0] * ct[0];
+  for (int d = 1; d < ND; ++d) uct += u[d] * ct[d];
+  const double t1 = uct - cq, nTv = n * g * v / T;
+  {
+    const double t2 = nTv * (phi2 / (g - 1.0) - T / g);
+    double s = 0.0;
+    for (int d = 0; d < ND; ++d) s += t2 * ct[d] * w[1 + d];
+    y[0] += s + (t2 * t1 - v * uct) * w[E];
+  }
+  for (int c = 0; c < ND; ++c) {
+    const double t2 = -nTv * u[c];
+    double s = 0.0;
+    for (int d = 0; d < ND; ++d) s += t2 * ct[d] * w[1 + d];
+    y[1 + c] += s + (t2 * t1 + v * ct[c]) * w[E];
+  }
+  {
+    double s = 0.0;
+    for (int d = 0; d < ND; ++d) s += nTv * ct[d] * w[1 + d];
+    y[E] += s + nTv * t1 * w[E];
+  }
+}
+
+// y += B2(m1, m2)^T w for the second partial viscous Jacobian
+// (computeSecondPartialViscousJacobian{2D,3D}, src/CNSHelperImpl.f90:2636-2757);
+// w and y have nD+1 entries (momentum, energy).
+template <int ND>
+__device__ __forceinline__ void secondPartialViscousTransposeProduct(
+    const double* u, double mu, double la, double k, double jac, const double* m1,
+    const double* m2, const double* w, double* y) {
+  double t1 = m1[0] * m2[0], t2 = m2[0] * u[0], t3 = m1[0] * u[0];
+  for (int d = 1; d < ND; ++d) {
+    t1 += m1[d] * m2[d];
+    t2 += m2[d] * u[d];
+    t3 += m1[d] * u[d];
+  }
+  t2 = mu * t2;
+  t3 = la * t3;
+  // column c of B2 (c < ND): rows r < ND and energy row ND
+  for (int c = 0; c < ND; ++c) {
+    double s = 0.0;
+    for (int r = 0; r < ND; ++r) {
+      const double b = r == c ? mu * t1 + (mu + la) * m1[c] * m2[c]
+                              : mu * m1[c] * m2[r] + la * m1[r] * m2[c];
+      s += b * w[r];
+    }
+    s += (mu * t1 * u[c] + m1[c] * t2 + m2[c] * t3) * w[ND];
+    y[c] += jac * s;
+  }
+  y[ND] += jac * (k * t1) * w[ND];
+}
+
+}  // namespace mgd

@@ -1,0 +1,182 @@
+// mgd_internal.h -- device-resident region state of one context and the
+// launchers of the kernels in mgd_kernels.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/magudi_gb300.h"
+#include "mgd_device.cuh"
+
+namespace mgd {
+
+// Component offsets inside the primitive-variable array `prim` (N x nPrim):
+// v = 1/rho, u_1..u_nD, p, T, mu, lambda (second coefficient), k.
+struct PrimLayout {
+  int nD;
+  __host__ __device__ int v() const { return 0; }
+  __host__ __device__ int u(int d) const { return 1 + d; }
+  __host__ __device__ int p() const { return 1 + nD; }
+  __host__ __device__ int T() const { return 2 + nD; }
+  __host__ __device__ int mu() const { return 3 + nD; }
+  __host__ __device__ int la() const { return 4 + nD; }
+  __host__ __device__ int k() const { return 5 + nD; }
+  __host__ __device__ int count() const { return 6 + nD; }
+};
+
+// Far-field SAT entry: one (patch, point) pair.
+struct FarFieldEntries {
+  int n = 0;
+  int* point = nullptr;      // grid point
+  int* normalDir = nullptr;  // 1-based normal direction (unsigned)
+  double* M = nullptr;       // nU*nU: inviscidPenaltyAmount * jacobian * A+(target), column-major
+  double* sigV = nullptr;    // viscousPenaltyAmount * jacobian
+  double* sigVRaw = nullptr; // viscousPenaltyAmount
+  double* visc = nullptr;    // nU: viscous flux contracted with the normal metric (current state)
+  double* viscT = nullptr;   // nU: the same for the target state
+};
+
+// Plain-old-data view of a block that kernels receive by value.
+struct BlockView {
+  int nD, nU;
+  long long N;
+  int gs[3];
+  Axis ax[3];
+  int curvilinear;
+  // grid
+  const double* metrics;
+  const double* jac;
+  const double* arcA;   // nD components: -dissipationAmount * arcLength_i
+  const int* iblank;
+  // state
+  double* q;
+  double* lam;
+  const double* qt;
+  double* rhs;
+  double* b1;
+  double* b2;
+  double* prim;
+  double* tau;
+  double* hf;
+  double* fhat;   // nD x nU
+  double* dq;     // nD x nU
+  double* rcore;  // nU
+  double* ad;     // nD x (nU-1)
+  // patches
+  const double* sponge;   // summed sponge strength
+  const double* mc;       // control mollifier (normalized)
+  const double* mt;       // target mollifier (normalized)
+  const double* meanP;
+  const double* wT;       // cost-target quadrature weight: mask * norm
+  const double* wA;       // actuator quadrature weight: mask * norm
+  const double* tgtCount; // number of cost-target patches holding the point (0 if hole)
+  const int* actIdx;      // actuator-patch point index, -1 if none
+  const int* ffOfPoint;   // 3 far-field entry indices per point, -1 if none
+  const double* srcG;     // nSources x N: exp(-gaussianFactor r^2), 0 on holes
+  int nSources;
+  FarFieldEntries ff;
+};
+
+// Constants of the physics and of the run.
+struct Physics {
+  double g, gm1, gOverGm1, reInv, prInv, powerLawExponent, laFactor;
+  int viscous, dissipation;
+};
+
+struct RunScalars {
+  // device pointers read by the kernels of a captured step
+  const int* step;        // 1-based forward step of the current RK step
+  const int* segBase;     // first step of the checkpoint segment minus 1
+  const double* amp;      // source amplitudes per (step-1)*4 + stage-1, nSources each
+  const double* forcing;  // control forcing entries, P each (file order)
+  long long nForcingEntries;
+  int nSteps;
+  long long P;            // actuator-patch points
+  double* gradient;       // gradient entries, P each (file order)
+  double* partials;       // block partial sums per stage slot
+  int nPartialBlocks;
+  double* stageBuf;       // stage inputs of the current segment (4*S slots of nU*N)
+  double dt;
+  int adjointForcingSwitch;
+};
+
+struct DevBlock {
+  mgd_block_desc desc;
+  BlockView v;
+  std::vector<void*> allocations;
+  int nStagePartialBlocks = 0;
+  // host copies kept for setup
+  std::vector<double> hostCoords;
+  std::vector<int> hostIblank;
+  std::vector<double> hostNorm;        // H * det
+  std::vector<double> hostMetricsArc;  // arc lengths of the metrics per direction
+  std::vector<double> hostJmi;         // coordinate derivatives d x_c / d xi_d (unmasked)
+  // ffOfPoint etc. are built on the host at finalize
+};
+
+struct Context {
+  mgd_options opts;
+  Physics phys;
+  int nD = 2, nU = 4;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  std::string error;
+  std::vector<DevBlock> blocks;
+  std::vector<mgd_patch_desc> patches;
+  std::vector<mgd_acoustic_source> sources;
+  bool finalized = false;
+  long long launches = 0;
+  long long actuatorPoints = 0;
+  // device scalars: [0] step, [1] segBase, [2] api step (always 1), [3] api segBase
+  int* dCounters = nullptr;
+  double* dApiAmp = nullptr;
+  double* dAmp = nullptr;           // per-stage source amplitudes of the run
+  long long ampCapacity = 0;
+  double* dForcing = nullptr;       // control forcing entries
+  long long nForcingEntries = 0;
+  double* dGradient = nullptr;      // gradient entries
+  long long gradientCapacity = 0;
+  double* dPartials = nullptr;      // stage partial sums
+  long long partialCapacity = 0;
+  double* dStageValues = nullptr;   // per-stage reduced values
+  long long stageValueCapacity = 0;
+  // checkpoints of the last forward run
+  int runSteps = 0, saveInterval = 0;
+  double runT0 = 0.0;
+  std::vector<double> stageTimes;   // time of every forward stage of the run
+  double* dSnapshots = nullptr;     // (nSnap) x nU x N per block (single block supported)
+  long long snapshotCapacity = 0;
+  double* dStageBuf = nullptr;
+  long long stageBufCapacity = 0;
+  cudaGraphExec_t gForward = nullptr, gRecompute = nullptr, gAdjoint = nullptr;
+};
+
+// ----- launchers (mgd_kernels.cu) -----
+void uploadOperatorTables();
+// K1: primitive variables of qSrc (or, when fromStage, of the stage-buffer slot
+// of the current step/stage); copyToQ also stores that state as the conserved variables.
+void launchPrims(Context& c, DevBlock& b, const double* qSrc, bool copyToQ, const RunScalars* rs = nullptr,
+                 int stage = 0);
+// K2: gradient, stress, fluxes, dissipation stage 1
+void launchGradFlux(Context& c, DevBlock& b, bool writeFlux, bool writeDiss, bool writeStress,
+                    const RunScalars* rs, int stage, bool storeStage);
+// K3: divergence, dissipation stage 2, patches, then either write rhs (rkStage = 0)
+// or fuse the RK4 forward update of stage rkStage
+void launchForwardRhs(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bool api,
+                      bool accumulateFunctional, bool controller);
+void launchAdjointA(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool record);
+void launchAdjointB(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage,
+                    double apiFactor, bool api);
+void launchAdjointInitial(Context& c, DevBlock& b, double factor);
+void launchSnapshot(Context& c, DevBlock& b, double* snapshots, int saveInterval, bool initial);
+void launchStepAdvance(Context& c, int delta);
+void launchReducePartials(Context& c, const double* partials, int nBlocks, int nSlots, double* out);
+void launchCoordinateDerivative(Context& c, DevBlock& b, int dir, double* out);
+void launchApplyD1(Context& c, DevBlock& b, int dir, const double* in, double* out, int ncomp);
+void launchFarFieldMatricesWith(Context& c, DevBlock& b, const double* sigInv, const int* signedNormal);
+void launchFarFieldTargetVisc(Context& c, DevBlock& b);
+int stageBlocks(const DevBlock& b);
+
+}  // namespace mgd

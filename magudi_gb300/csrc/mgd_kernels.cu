@@ -1,0 +1,841 @@
+// mgd_kernels.cu -- FP64 kernels of the forward and discrete-adjoint RHS and
+// the RK4 stage updates, plus the setup kernels (grid metrics, far-field SAT
+// matrices). One thread per grid point; stencil taps are read through the
+// read-only cache. Each RK stage is two kernels forward (K2: gradients,
+// stress, fluxes, first dissipation sweep; K3: flux divergence, second
+// dissipation sweep, SATs, sources, RK update, primitive variables of the new
+// state, functional partial sums) and four adjoint (forward-state update x2,
+// adjoint part A, adjoint part B with the RK update).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+
+#include "mgd_internal.h"
+#include "sbp_tables.h"
+
+namespace mgd {
+
+
+__constant__ double c_norm[8];
+
+constexpr int kBlock = 128;
+
+static inline int gridFor(long long n) { return (int)((n + kBlock - 1) / kBlock); }
+
+int stageBlocks(const DevBlock& b) { return gridFor(b.v.N); }
+
+void uploadOperatorTables() {
+  static bool done[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && done[dev]) return;
+  OpTables t;
+  std::memset(&t, 0, sizeof t);
+  const HostOp d1 = makeFirstDerivative48();
+  const HostOp ad = makeAdjoint(d1);
+  const HostOp di = makeDissipation48();
+  const HostOp dt = makeDissipationTransposeNormInverse48(d1);
+  const HostOp* ops[OP_COUNT] = {&d1, &ad, &di, &dt};
+  for (int o = 0; o < OP_COUNT; ++o) {
+    for (size_t j = 0; j < ops[o]->interior.size(); ++j) t.interior[o][j] = ops[o]->interior[j];
+    for (size_t j = 0; j < ops[o]->left.size(); ++j) t.left[o][j] = ops[o]->left[j];
+  }
+  cudaMemcpyToSymbol(c_ops, &t, sizeof t);
+  cudaMemcpyToSymbol(c_norm, d1.norm.data(), 8 * sizeof(double));
+  if (dev < 64) done[dev] = true;
+}
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+struct PointIndex {
+  int idx[3];
+  long long base[3];  // first point of the pencil through p along each axis
+};
+
+__device__ __forceinline__ PointIndex pointIndex(const BlockView& B, long long p) {
+  PointIndex r;
+  const long long plane = (long long)B.gs[0] * B.gs[1];
+  r.idx[0] = (int)(p % B.gs[0]);
+  r.idx[1] = (int)((p / B.gs[0]) % B.gs[1]);
+  r.idx[2] = (int)(p / plane);
+  for (int d = 0; d < 3; ++d) r.base[d] = p - (long long)r.idx[d] * B.ax[d].stride;
+  return r;
+}
+
+// Primitive variables of one state (computeDependentVariables +
+// computeTransportVariables, src/CNSHelperImpl.f90:3-177).
+template <int ND>
+__device__ __forceinline__ void primitives(const double* q, const Physics& P, double* out /*6+ND*/) {
+  const double v = 1.0 / q[0];
+  out[0] = v;
+  double u2 = 0.0;
+  for (int d = 0; d < ND; ++d) {
+    const double u = v * q[1 + d];
+    out[1 + d] = u;
+    u2 = d == 0 ? u * u : u2 + u * u;
+  }
+  const double pr = P.gm1 * (q[ND + 1] - 0.5 * q[0] * u2);
+  const double T = P.gOverGm1 * pr * v;
+  out[1 + ND] = pr;
+  out[2 + ND] = T;
+  double mu = P.reInv;
+  if (P.powerLawExponent > 0.0) mu = pow(P.gm1 * T, P.powerLawExponent) * P.reInv;
+  out[3 + ND] = mu;
+  out[4 + ND] = P.laFactor * mu;
+  out[5 + ND] = mu * P.prInv;
+}
+
+// Deterministic block sum of one value per thread; thread 0 gets the result.
+__device__ __forceinline__ double blockSum(double v) {
+  __shared__ double warpSums[kBlock / 32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) warpSums[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < kBlock / 32; ++i) s += warpSums[i];
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// K1: primitive variables (State%update pointwise part, src/StateImpl.f90:466-492)
+// ---------------------------------------------------------------------------
+template <int ND>
+__global__ void __launch_bounds__(kBlock) kPrims(BlockView B, Physics P, const double* __restrict__ qSrc,
+                                                 int copyToQ, RunScalars rs, int stage) {
+  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
+  if (p >= B.N) return;
+  constexpr int nU = ND + 2;
+  if (stage > 0) {
+    const int slot = ((*rs.step) - (*rs.segBase) - 1) * 4 + stage - 1;
+    qSrc = rs.stageBuf + (long long)slot * nU * B.N;
+  }
+  double q[nU], pr[6 + ND];
+  for (int c = 0; c < nU; ++c) q[c] = qSrc[p + B.N * c];
+  if (copyToQ)
+    for (int c = 0; c < nU; ++c) B.q[p + B.N * c] = q[c];
+  primitives<ND>(q, P, pr);
+  for (int c = 0; c < 6 + ND; ++c) B.prim[p + B.N * c] = pr[c];
+}
+
+// ---------------------------------------------------------------------------
+// K2: velocity and temperature gradients, stress and heat flux (State%update,
+// src/StateImpl.f90:494-533 with Grid%computeGradient, src/GridImpl.f90:1172-1421),
+// Cartesian inviscid and viscous fluxes transformed to contravariant form
+// (computeRhsForward, src/RhsHelperImpl.f90:295-339) and the first sweep of
+// the artificial dissipation (addDissipation, src/RhsHelperImpl.f90:54-66).
+// ---------------------------------------------------------------------------
+enum { GF_FLUX = 1, GF_DISS = 2, GF_STRESS = 4, GF_STORE = 8 };
+
+template <int ND, bool CURV, bool VISC>
+__global__ void __launch_bounds__(kBlock) kGradFlux(BlockView B, Physics P, RunScalars rs, int flags,
+                                                    int stage) {
+  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
+  if (p >= B.N) return;
+  constexpr int nU = ND + 2, E = ND + 1;
+  const long long N = B.N;
+  const PointIndex I = pointIndex(B, p);
+  const PrimLayout L{ND};
+  double q[nU];
+  for (int c = 0; c < nU; ++c) q[c] = B.q[p + N * c];
+  if (flags & GF_STORE) {
+    const int slot = ((*rs.step) - (*rs.segBase) - 1) * 4 + stage - 1;
+    double* dst = rs.stageBuf + (long long)slot * nU * N;
+    for (int c = 0; c < nU; ++c) dst[p + N * c] = q[c];
+  }
+  double m[ND * ND];
+  for (int c = 0; c < ND * ND; ++c) m[c] = (CURV || (c % (ND + 1)) == 0) ? B.metrics[p + N * c] : 0.0;
+  double u[ND];
+  for (int d = 0; d < ND; ++d) u[d] = B.prim[p + N * L.u(d)];
+  double tau[ND * ND], hf[ND];
+  if (VISC && (flags & (GF_FLUX | GF_STRESS))) {
+    const double jac = B.jac[p];
+    double du[ND][ND], dT[ND];
+    for (int d = 0; d < ND; ++d) {
+      for (int c = 0; c < ND; ++c) du[c][d] = applyOp<OP_D1>(B.prim + N * L.u(c) + I.base[d], I.idx[d], B.ax[d]);
+      dT[d] = applyOp<OP_D1>(B.prim + N * L.T() + I.base[d], I.idx[d], B.ax[d]);
+    }
+    double gu[ND][ND], gT[ND];
+    for (int x = 0; x < ND; ++x) {
+      if (CURV) {
+        for (int c = 0; c < ND; ++c) {
+          double s = m[x] * du[c][0];
+          for (int d = 1; d < ND; ++d) s += m[ND * d + x] * du[c][d];
+          gu[c][x] = jac * s;
+        }
+        double s = m[x] * dT[0];
+        for (int d = 1; d < ND; ++d) s += m[ND * d + x] * dT[d];
+        gT[x] = jac * s;
+      } else {
+        const double jm = jac * m[ND * x + x];
+        for (int c = 0; c < ND; ++c) gu[c][x] = jm * du[c][x];
+        gT[x] = jm * dT[x];
+      }
+    }
+    const double mu = B.prim[p + N * L.mu()], la = B.prim[p + N * L.la()], kd = B.prim[p + N * L.k()];
+    double div = gu[0][0];
+    for (int d = 1; d < ND; ++d) div += gu[d][d];
+    div = la * div;
+    for (int c = 0; c < ND; ++c) {
+      tau[ND * c + c] = 2.0 * mu * gu[c][c] + div;
+      for (int d = c + 1; d < ND; ++d) {
+        const double t = mu * (gu[c][d] + gu[d][c]);
+        tau[ND * c + d] = t;
+        tau[ND * d + c] = t;
+      }
+    }
+    for (int x = 0; x < ND; ++x) hf[x] = -kd * gT[x];
+    if (flags & GF_STRESS) {
+      for (int c = 0; c < ND * ND; ++c) B.tau[p + N * c] = tau[c];
+      for (int x = 0; x < ND; ++x) B.hf[p + N * x] = hf[x];
+    }
+  }
+  if (flags & GF_FLUX) {
+    const double pr = B.prim[p + N * L.p()];
+    double F[nU][ND];
+    for (int d = 0; d < ND; ++d) {
+      F[0][d] = q[1 + d];
+      for (int c = 0; c < ND; ++c) {
+        double v = c < d ? q[1 + c] * u[d] : q[1 + d] * u[c];
+        if (c == d) v = v + pr;
+        F[1 + c][d] = v;
+      }
+      F[E][d] = u[d] * (q[E] + pr);
+    }
+    if (VISC) {
+      double Fv[nU][ND];
+      for (int d = 0; d < ND; ++d) {
+        Fv[0][d] = 0.0;
+        for (int c = 0; c < ND; ++c) Fv[1 + c][d] = tau[ND * c + d];
+        double e = u[0] * tau[d];
+        for (int c = 1; c < ND; ++c) e += u[c] * tau[ND * c + d];
+        Fv[E][d] = e - hf[d];
+      }
+      for (int s = 0; s < 3; ++s) {
+        const int e = B.ffOfPoint[3 * p + s];
+        if (e < 0) continue;
+        const double* mn = m + ND * (B.ff.normalDir[e] - 1);
+        for (int r = 0; r < nU; ++r) {
+          double t = Fv[r][0] * mn[0];
+          for (int d = 1; d < ND; ++d) t += Fv[r][d] * mn[d];
+          B.ff.visc[(long long)e * nU + r] = t;
+        }
+      }
+      for (int r = 1; r < nU; ++r)
+        for (int d = 0; d < ND; ++d) F[r][d] = F[r][d] - Fv[r][d];
+    }
+    for (int i = 0; i < ND; ++i)
+      for (int c = 0; c < nU; ++c) {
+        double s;
+        if (CURV) {
+          s = m[ND * i] * F[c][0];
+          for (int d = 1; d < ND; ++d) s += m[ND * i + d] * F[c][d];
+        } else {
+          s = m[ND * i + i] * F[c][i];
+        }
+        B.fhat[p + N * (i * nU + c)] = s;
+      }
+  }
+  if (flags & GF_DISS) {
+    for (int d = 0; d < ND; ++d) {
+      const double a = B.arcA[p + N * d];
+      for (int c = 0; c < nU; ++c)
+        B.dq[p + N * (d * nU + c)] = a * applyOp<OP_DISS>(B.q + N * c + I.base[d], I.idx[d], B.ax[d]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K3: forward RHS (computeRhsForward + Region%computeRhs,
+// src/RhsHelperImpl.f90:330-351, src/RegionImpl.f90:1968-2023) fused with the
+// RK4 forward stage update (src/RK4IntegratorImpl.f90:104-158), the
+// primitive variables of the new state and the functional's partial sums.
+// ---------------------------------------------------------------------------
+template <int ND>
+__global__ void __launch_bounds__(kBlock) kForwardRhs(BlockView B, Physics P, RunScalars rs, int rkStage,
+                                                      int stage, int accumulate, int controller) {
+  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
+  const bool active = p < B.N;
+  constexpr int nU = ND + 2, E = ND + 1;
+  const long long N = B.N;
+  double fval = 0.0;
+  if (active) {
+    const PointIndex I = pointIndex(B, p);
+    double r[nU];
+    for (int c = 0; c < nU; ++c) {
+      double s = applyOp<OP_D1>(B.fhat + N * c + I.base[0], I.idx[0], B.ax[0]);
+      for (int i = 1; i < ND; ++i) s += applyOp<OP_D1>(B.fhat + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
+      r[c] = -s;
+    }
+    if (P.dissipation)
+      for (int c = 0; c < nU; ++c)
+        for (int i = 0; i < ND; ++i)
+          r[c] += applyOp<OP_DISST>(B.dq + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
+    const double jac = B.jac[p];
+    for (int c = 0; c < nU; ++c) r[c] = r[c] * jac;
+    double q[nU];
+    for (int c = 0; c < nU; ++c) q[c] = B.q[p + N * c];
+    // far-field SAT (addFarFieldPenalty FORWARD, src/FarFieldPatchImpl.f90:227-235)
+    for (int s = 0; s < 3; ++s) {
+      const int e = B.ffOfPoint[3 * p + s];
+      if (e < 0) continue;
+      const double* M = B.ff.M + (long long)e * nU * nU;
+      double dqv[nU];
+      for (int c = 0; c < nU; ++c) dqv[c] = q[c] - B.qt[p + N * c];
+      for (int row = 0; row < nU; ++row) {
+        double t = M[row] * dqv[0];
+        for (int c = 1; c < nU; ++c) t += M[row + nU * c] * dqv[c];
+        r[row] -= t;
+      }
+      if (P.viscous) {
+        const double sv = B.ff.sigV[e];
+        for (int row = 0; row < nU; ++row)
+          r[row] += sv * (B.ff.visc[(long long)e * nU + row] - B.ff.viscT[(long long)e * nU + row]);
+      }
+    }
+    // sponge (addDamping FORWARD, src/SpongePatchImpl.f90:86-104)
+    const double S = B.sponge[p];
+    if (S != 0.0)
+      for (int c = 0; c < nU; ++c) r[c] -= S * (q[c] - B.qt[p + N * c]);
+    const int step = *rs.step;
+    // actuator (updateActuatorPatch FORWARD, src/ActuatorPatchImpl.f90:134-168)
+    if (controller) {
+      const int ai = B.actIdx[p];
+      if (ai >= 0) {
+        const long long e = (long long)(rs.nSteps - step) * 4 + (4 - stage);
+        if (e >= 0 && e < rs.nForcingEntries) r[E] += B.mc[p] * rs.forcing[e * rs.P + ai];
+      }
+    }
+    // acoustic sources (AcousticSource%add, src/AcousticSourceImpl.f90:34-64)
+    if (B.nSources > 0) {
+      const double* amp = rs.amp + ((long long)(step - 1) * 4 + (stage - 1)) * B.nSources;
+      for (int s = 0; s < B.nSources; ++s) r[E] += amp[s] * B.srcG[p + N * s];
+    }
+    if (B.iblank[p] == 0)
+      for (int c = 0; c < nU; ++c) r[c] = 0.0;
+    if (rkStage == 0) {
+      for (int c = 0; c < nU; ++c) B.rhs[p + N * c] = r[c];
+    } else {
+      const double h6 = rs.dt / 6.0, h3 = rs.dt / 3.0, h2 = rs.dt / 2.0;
+      double qn[nU];
+      for (int c = 0; c < nU; ++c) {
+        const long long k = p + N * c;
+        switch (rkStage) {
+          case 1:
+            B.b1[k] = q[c];
+            B.b2[k] = q[c] + h6 * r[c];
+            qn[c] = q[c] + h2 * r[c];
+            break;
+          case 2:
+            B.b2[k] = B.b2[k] + h3 * r[c];
+            qn[c] = B.b1[k] + h2 * r[c];
+            break;
+          case 3:
+            B.b2[k] = B.b2[k] + h3 * r[c];
+            qn[c] = B.b1[k] + rs.dt * r[c];
+            break;
+          default:
+            qn[c] = B.b2[k] + h6 * r[c];
+            break;
+        }
+        B.q[k] = qn[c];
+      }
+      double pr[6 + ND];
+      primitives<ND>(qn, P, pr);
+      for (int c = 0; c < 6 + ND; ++c) B.prim[p + N * c] = pr[c];
+      if (accumulate) {
+        const double w = B.wT[p];
+        if (w != 0.0) {
+          const double F = pr[1 + ND] - B.meanP[p];
+          fval = w * (F * F * B.mt[p]);
+        }
+      }
+    }
+  }
+  if (accumulate) {
+    const double s = blockSum(fval);
+    if (threadIdx.x == 0) {
+      const int slot = ((*rs.step) - 1) * 4 + (stage - 1);
+      rs.partials[(long long)slot * rs.nPartialBlocks + blockIdx.x] = s;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint part A (computeRhsAdjoint, src/RhsHelperImpl.f90:398-560, first half):
+// adjoint derivatives of lambda, inviscid minus first-partial viscous
+// Jacobian-transpose products, second-partial viscous products (plus the
+// far-field viscous adjoint penalty of src/RhsHelperImpl.f90:89-250 folded
+// into the same adjoint sweep), the first adjoint dissipation sweep, the
+// gradient entry and the sensitivity partial sums of this stage
+// (src/ThermalActuatorImpl.f90:83-159, 383-443).
+// ---------------------------------------------------------------------------
+template <int ND, bool VISC>
+__global__ void __launch_bounds__(kBlock) kAdjointA(BlockView B, Physics P, RunScalars rs, int stage,
+                                                    int record) {
+  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
+  const bool active = p < B.N;
+  constexpr int nU = ND + 2, E = ND + 1, nV = ND + 1;
+  const long long N = B.N;
+  const PrimLayout L{ND};
+  double sval = 0.0;
+  if (active) {
+    const PointIndex I = pointIndex(B, p);
+    double w[ND][nU];
+    for (int i = 0; i < ND; ++i)
+      for (int c = 0; c < nU; ++c) w[i][c] = applyOp<OP_D1ADJ>(B.lam + N * c + I.base[i], I.idx[i], B.ax[i]);
+    double m[ND * ND];
+    for (int c = 0; c < ND * ND; ++c) m[c] = B.metrics[p + N * c];
+    double u[ND];
+    for (int d = 0; d < ND; ++d) u[d] = B.prim[p + N * L.u(d)];
+    const double v = B.prim[p + N * L.v()], T = B.prim[p + N * L.T()];
+    double tau[ND * ND], hf[ND];
+    if (VISC) {
+      for (int c = 0; c < ND * ND; ++c) tau[c] = B.tau[p + N * c];
+      for (int d = 0; d < ND; ++d) hf[d] = B.hf[p + N * d];
+    }
+    double y[nU];
+    for (int c = 0; c < nU; ++c) y[c] = 0.0;
+    for (int i = 0; i < ND; ++i)
+      addFluxJacobianTransposeProduct<ND, VISC>(m + ND * i, u, T, v, P.g, P.powerLawExponent, tau, hf, w[i], y);
+    for (int c = 0; c < nU; ++c) B.rcore[p + N * c] = y[c];
+    double lp[nU];
+    for (int c = 0; c < nU; ++c) lp[c] = B.lam[p + N * c];
+    if (VISC) {
+      const double mu = B.prim[p + N * L.mu()], la = B.prim[p + N * L.la()], kd = B.prim[p + N * L.k()];
+      const double jac = B.jac[p];
+      double ad[ND][nV];
+      for (int j = 0; j < ND; ++j) {
+        for (int c = 0; c < nV; ++c) ad[j][c] = 0.0;
+        for (int i = 0; i < ND; ++i)
+          secondPartialViscousTransposeProduct<ND>(u, mu, la, kd, jac, m + ND * i, m + ND * j, &w[i][1], ad[j]);
+      }
+      for (int s = 0; s < 3; ++s) {
+        const int e = B.ffOfPoint[3 * p + s];
+        if (e < 0) continue;
+        const double* mn = m + ND * (B.ff.normalDir[e] - 1);
+        const double sv = B.ff.sigVRaw[e];
+        for (int l = 0; l < ND; ++l) {
+          double t[nV];
+          for (int c = 0; c < nV; ++c) t[c] = 0.0;
+          secondPartialViscousTransposeProduct<ND>(u, mu, la, kd, jac, mn, m + ND * l, &lp[1], t);
+          for (int c = 0; c < nV; ++c) ad[l][c] += sv * t[c];
+        }
+      }
+      for (int j = 0; j < ND; ++j)
+        for (int c = 0; c < nV; ++c) B.ad[p + N * (j * nV + c)] = ad[j][c];
+    }
+    if (P.dissipation)
+      for (int d = 0; d < ND; ++d) {
+        const double a = -B.arcA[p + N * d];
+        for (int c = 0; c < nU; ++c)
+          B.dq[p + N * (d * nU + c)] = a * applyOp<OP_DISS>(B.lam + N * c + I.base[d], I.idx[d], B.ax[d]);
+      }
+    if (record) {
+      const long long entry = (long long)(rs.nSteps - *rs.step) * 4 + (4 - stage);
+      const double g = lp[E] * B.mc[p];
+      const int ai = B.actIdx[p];
+      if (ai >= 0) rs.gradient[entry * rs.P + ai] = g;
+      const double wA = B.wA[p];
+      if (wA != 0.0) sval = wA * (g * g);
+    }
+  }
+  if (record) {
+    const double s = blockSum(sval);
+    if (threadIdx.x == 0) {
+      const long long entry = (long long)(rs.nSteps - *rs.step) * 4 + (4 - stage);
+      rs.partials[entry * rs.nPartialBlocks + blockIdx.x] = s;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint part B: adjoint divergence of the viscous diffusion term and its
+// primitive-to-conservative map (src/RhsHelperImpl.f90:562-582), the second
+// adjoint dissipation sweep, 1/det, the far-field / sponge / cost-target
+// adjoint terms (src/FarFieldPatchImpl.f90:237-257, src/SpongePatchImpl.f90:
+// 106-124, src/CostTargetPatchImpl.f90:72-136 with the AcousticNoise forcing
+// of src/AcousticNoiseImpl.f90:208-280) and the RK4 adjoint stage update
+// (src/RK4IntegratorImpl.f90:203-266).
+// ---------------------------------------------------------------------------
+template <int ND, bool VISC>
+__global__ void __launch_bounds__(kBlock) kAdjointB(BlockView B, Physics P, RunScalars rs, int rkStage,
+                                                    int stage, double apiFactor, int api) {
+  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
+  if (p >= B.N) return;
+  constexpr int nU = ND + 2, E = ND + 1, nV = ND + 1;
+  const long long N = B.N;
+  const PrimLayout L{ND};
+  const PointIndex I = pointIndex(B, p);
+  double r[nU];
+  for (int c = 0; c < nU; ++c) r[c] = B.rcore[p + N * c];
+  double u[ND];
+  for (int d = 0; d < ND; ++d) u[d] = B.prim[p + N * L.u(d)];
+  const double v = B.prim[p + N * L.v()];
+  if (VISC) {
+    double t2[nV];
+    for (int c = 0; c < nV; ++c) {
+      double s = applyOp<OP_D1ADJ>(B.ad + N * c + I.base[0], I.idx[0], B.ax[0]);
+      for (int j = 1; j < ND; ++j) s += applyOp<OP_D1ADJ>(B.ad + N * (j * nV + c) + I.base[j], I.idx[j], B.ax[j]);
+      t2[c] = s;
+    }
+    const double xE = P.g * v * t2[ND];
+    double x[ND];
+    for (int d = 0; d < ND; ++d) x[d] = v * t2[d] - u[d] * xE;
+    for (int d = 0; d < ND; ++d) r[1 + d] -= x[d];
+    r[E] -= xE;
+    double su = u[0] * x[0];
+    for (int d = 1; d < ND; ++d) su += u[d] * x[d];
+    r[0] += v * B.q[p + N * E] * xE + su;
+  }
+  if (P.dissipation)
+    for (int c = 0; c < nU; ++c)
+      for (int i = 0; i < ND; ++i)
+        r[c] += applyOp<OP_DISST>(B.dq + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
+  const double jac = B.jac[p];
+  for (int c = 0; c < nU; ++c) r[c] = r[c] * jac;
+  double lp[nU];
+  for (int c = 0; c < nU; ++c) lp[c] = B.lam[p + N * c];
+  for (int s = 0; s < 3; ++s) {
+    const int e = B.ffOfPoint[3 * p + s];
+    if (e < 0) continue;
+    const double* M = B.ff.M + (long long)e * nU * nU;
+    for (int row = 0; row < nU; ++row) {
+      double t = M[nU * row] * lp[0];
+      for (int c = 1; c < nU; ++c) t += M[c + nU * row] * lp[c];
+      r[row] += t;
+    }
+    if (VISC) {
+      double m[ND], tau[ND * ND], hf[ND], y[nU];
+      const int nd = B.ff.normalDir[e] - 1;
+      for (int d = 0; d < ND; ++d) m[d] = B.metrics[p + N * (ND * nd + d)];
+      for (int c = 0; c < ND * ND; ++c) tau[c] = B.tau[p + N * c];
+      for (int d = 0; d < ND; ++d) hf[d] = B.hf[p + N * d];
+      for (int c = 0; c < nU; ++c) y[c] = 0.0;
+      firstPartialViscousTransposeProduct<ND>(m, u, B.prim[p + N * L.T()], v, P.g, P.powerLawExponent, tau, hf, lp, y);
+      const double sv = B.ff.sigV[e];
+      for (int c = 0; c < nU; ++c) r[c] -= sv * y[c];
+    }
+  }
+  const double S = B.sponge[p];
+  if (S != 0.0)
+    for (int c = 0; c < nU; ++c) r[c] += S * lp[c];
+  const double cnt = B.tgtCount[p];
+  if (cnt != 0.0) {
+    double factor;
+    if (api) {
+      factor = apiFactor;
+    } else {
+      const bool finalStage = (*rs.step == 1 && stage == 1);
+      factor = (!rs.adjointForcingSwitch || finalStage) ? 0.0
+               : (stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0));
+    }
+    if (factor != 0.0) {
+      const double F = -2.0 * B.mt[p] * P.gm1 * (B.prim[p + N * L.p()] - B.meanP[p]);
+      double u2 = u[0] * u[0];
+      for (int d = 1; d < ND; ++d) u2 += u[d] * u[d];
+      for (int k = 0; k < (int)cnt; ++k) {
+        r[E] += factor * F;
+        for (int d = 0; d < ND; ++d) r[1 + d] += factor * (-u[d] * F);
+        r[0] += factor * (0.5 * u2 * F);
+      }
+    }
+  }
+  if (B.iblank[p] == 0)
+    for (int c = 0; c < nU; ++c) r[c] = 0.0;
+  if (rkStage == 0) {
+    for (int c = 0; c < nU; ++c) B.rhs[p + N * c] = r[c];
+    return;
+  }
+  const double h6 = rs.dt / 6.0, h3 = rs.dt / 3.0, h2 = rs.dt / 2.0;
+  for (int c = 0; c < nU; ++c) {
+    const long long k = p + N * c;
+    switch (rkStage) {
+      case 4:
+        B.b1[k] = lp[c];
+        B.b2[k] = lp[c] - h6 * r[c];
+        B.lam[k] = lp[c] - h2 * r[c];
+        break;
+      case 3:
+        B.b2[k] = B.b2[k] - h3 * r[c];
+        B.lam[k] = B.b1[k] - h2 * r[c];
+        break;
+      case 2:
+        B.b2[k] = B.b2[k] - h3 * r[c];
+        B.lam[k] = B.b1[k] - rs.dt * r[c];
+        break;
+      default:
+        B.lam[k] = B.b2[k] - h6 * r[c];
+        break;
+    }
+  }
+}
+
+// Adjoint initial condition lambda(T) = factor * adjointForcing(q(T)),
+// factor = -dt/6 (loadInitialCondition ADJOINT, src/SolverImpl.f90:368-427).
+template <int ND>
+__global__ void __launch_bounds__(kBlock) kAdjointInitial(BlockView B, Physics P, double factor) {
+  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
+  if (p >= B.N) return;
+  constexpr int nU = ND + 2, E = ND + 1;
+  const long long N = B.N;
+  const PrimLayout L{ND};
+  double r[nU];
+  for (int c = 0; c < nU; ++c) r[c] = 0.0;
+  const double cnt = B.tgtCount[p];
+  if (cnt != 0.0 && factor != 0.0) {
+    double u[ND];
+    for (int d = 0; d < ND; ++d) u[d] = B.prim[p + N * L.u(d)];
+    const double F = -2.0 * B.mt[p] * P.gm1 * (B.prim[p + N * L.p()] - B.meanP[p]);
+    double u2 = u[0] * u[0];
+    for (int d = 1; d < ND; ++d) u2 += u[d] * u[d];
+    for (int k = 0; k < (int)cnt; ++k) {
+      r[E] += factor * F;
+      for (int d = 0; d < ND; ++d) r[1 + d] += factor * (-u[d] * F);
+      r[0] += factor * (0.5 * u2 * F);
+    }
+  }
+  for (int c = 0; c < nU; ++c) B.lam[p + N * c] = r[c];
+}
+
+// Snapshot of the conserved variables after a completed forward step.
+__global__ void kSnapshot(double* __restrict__ snap, const double* __restrict__ q, long long n,
+                          const int* __restrict__ step, int saveInterval, int initial) {
+  const long long i = (long long)blockIdx.x * kBlock + threadIdx.x;
+  const int s = initial ? 0 : *step;
+  if (s % saveInterval != 0 || i >= n) return;
+  snap[(long long)(s / saveInterval) * n + i] = q[i];
+}
+
+__global__ void kStepAdvance(int* counters, int delta) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) counters[0] += delta;
+}
+
+// out[s] = sum over blocks of partials[s * nBlocks + b], fixed order.
+__global__ void kReducePartials(const double* __restrict__ partials, int nBlocks, int nSlots,
+                                double* __restrict__ out) {
+  const int s = blockIdx.x;
+  if (s >= nSlots) return;
+  double v = 0.0;
+  for (int b = threadIdx.x; b < nBlocks; b += kBlock) v += partials[(long long)s * nBlocks + b];
+  const double t = blockSum(v);
+  if (threadIdx.x == 0) out[s] = t;
+}
+
+// ---------------------------------------------------------------------------
+// setup kernels (Grid%update, src/GridImpl.f90:621-1066)
+// ---------------------------------------------------------------------------
+
+// d x_c / d xi_dir for every coordinate component c (computeCoordinateDerivatives);
+// PLANE periodicity shifts the wrapped coordinate by the periodic length.
+template <int ND>
+__global__ void kCoordinateDerivative(BlockView B, const double* __restrict__ coords, int dir,
+                                      double periodicLength, double* __restrict__ out) {
+  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
+  if (p >= B.N) return;
+  const PointIndex I = pointIndex(B, p);
+  const Axis ax = B.ax[dir];
+  for (int c = 0; c < ND; ++c) {
+    const double* line = coords + B.N * c + I.base[dir];
+    double s;
+    if (ax.per != MGD_PERIODIC_PLANE) {
+      s = applyOp<OP_D1>(line, I.idx[dir], ax);
+    } else {
+      const double* cin = c_ops.interior[OP_D1];
+      auto at = [&](int j) {
+        const int k = I.idx[dir] + j;
+        double x = line[(long long)wrapIndex(k, ax.n, ax.per) * ax.stride];
+        if (c == dir) {
+          if (k < 0) x = x - periodicLength;
+          if (k >= ax.n) x = x + periodicLength;
+        }
+        return x;
+      };
+      s = cin[5] * (at(1) - at(-1));
+      for (int j = 2; j <= 4; ++j) s += cin[4 + j] * (at(j) - at(-j));
+    }
+    out[p + B.N * c] = s;
+  }
+}
+
+__global__ void kApplyD1(BlockView B, int dir, const double* __restrict__ in, double* __restrict__ out, int ncomp) {
+  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
+  if (p >= B.N) return;
+  const PointIndex I = pointIndex(B, p);
+  for (int c = 0; c < ncomp; ++c) out[p + B.N * c] = applyOp<OP_D1>(in + B.N * c + I.base[dir], I.idx[dir], B.ax[dir]);
+}
+
+// Far-field SAT matrices sigma_inv * (1/det) * A+(q_target, metric_normal).
+template <int ND>
+__global__ void kFarFieldMatrices(BlockView B, double g, const double* __restrict__ sigInv,
+                                  const int* __restrict__ signedNormal) {
+  const int e = blockIdx.x * kBlock + threadIdx.x;
+  if (e >= B.ff.n) return;
+  constexpr int nU = ND + 2;
+  const long long p = B.ff.point[e];
+  const int nd = B.ff.normalDir[e] - 1;
+  double cv[nU], m[ND], A[nU * nU];
+  for (int c = 0; c < nU; ++c) cv[c] = B.qt[p + B.N * c];
+  for (int d = 0; d < ND; ++d) m[d] = B.metrics[p + B.N * (ND * nd + d)];
+  incomingJacobian<ND>(cv, m, g, signedNormal[e], A);
+  const double s = sigInv[e] * B.jac[p];
+  for (int k = 0; k < nU * nU; ++k) B.ff.M[(long long)e * nU * nU + k] = s * A[k];
+}
+
+// Target viscous flux contracted with the normal metric at every far-field
+// entry (updatePatchFactories, src/PatchFactoryImpl.f90:539-571); prim, tau
+// and hf hold the target state's values when this runs.
+template <int ND>
+__global__ void kFarFieldTargetVisc(BlockView B) {
+  const int e = blockIdx.x * kBlock + threadIdx.x;
+  if (e >= B.ff.n) return;
+  constexpr int nU = ND + 2, E = ND + 1;
+  const long long p = B.ff.point[e], N = B.N;
+  const PrimLayout L{ND};
+  const int nd = B.ff.normalDir[e] - 1;
+  double m[ND], u[ND], tau[ND * ND], hf[ND];
+  for (int d = 0; d < ND; ++d) m[d] = B.metrics[p + N * (ND * nd + d)];
+  for (int d = 0; d < ND; ++d) u[d] = B.prim[p + N * L.u(d)];
+  for (int c = 0; c < ND * ND; ++c) tau[c] = B.tau[p + N * c];
+  for (int d = 0; d < ND; ++d) hf[d] = B.hf[p + N * d];
+  double Fv[nU][ND];
+  for (int d = 0; d < ND; ++d) {
+    Fv[0][d] = 0.0;
+    for (int c = 0; c < ND; ++c) Fv[1 + c][d] = tau[ND * c + d];
+    double s = u[0] * tau[d];
+    for (int c = 1; c < ND; ++c) s += u[c] * tau[ND * c + d];
+    Fv[E][d] = s - hf[d];
+  }
+  for (int r = 0; r < nU; ++r) {
+    double t = Fv[r][0] * m[0];
+    for (int d = 1; d < ND; ++d) t += Fv[r][d] * m[d];
+    B.ff.viscT[(long long)e * nU + r] = t;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+#define MGD_LAUNCH(c) (++(c).launches)
+
+void launchPrims(Context& c, DevBlock& b, const double* qSrc, bool copyToQ, const RunScalars* rs, int stage) {
+  RunScalars r{};
+  if (rs) r = *rs;
+  MGD_LAUNCH(c);
+  if (c.nD == 2) kPrims<2><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, qSrc, copyToQ, r, stage);
+  else kPrims<3><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, qSrc, copyToQ, r, stage);
+}
+
+void launchGradFlux(Context& c, DevBlock& b, bool writeFlux, bool writeDiss, bool writeStress,
+                    const RunScalars* rs, int stage, bool storeStage) {
+  int flags = (writeFlux ? GF_FLUX : 0) | (writeDiss && c.phys.dissipation ? GF_DISS : 0) |
+              (writeStress ? GF_STRESS : 0) | (storeStage ? GF_STORE : 0);
+  RunScalars r{};
+  if (rs) r = *rs;
+  const int G = gridFor(b.v.N);
+  const bool curv = b.v.curvilinear != 0, visc = c.phys.viscous != 0;
+  MGD_LAUNCH(c);
+#define GF(ND, CU, VI) kGradFlux<ND, CU, VI><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, r, flags, stage)
+  if (c.nD == 2) {
+    if (curv) { if (visc) GF(2, true, true); else GF(2, true, false); }
+    else { if (visc) GF(2, false, true); else GF(2, false, false); }
+  } else {
+    if (curv) { if (visc) GF(3, true, true); else GF(3, true, false); }
+    else { if (visc) GF(3, false, true); else GF(3, false, false); }
+  }
+#undef GF
+}
+
+void launchForwardRhs(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bool api,
+                      bool accumulate, bool controller) {
+  const int stage = api ? 1 : rkStage;
+  MGD_LAUNCH(c);
+  if (c.nD == 2)
+    kForwardRhs<2><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, accumulate, controller);
+  else
+    kForwardRhs<3><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, accumulate, controller);
+}
+
+void launchAdjointA(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool record) {
+  const int G = gridFor(b.v.N);
+  MGD_LAUNCH(c);
+  if (c.nD == 2) {
+    if (c.phys.viscous) kAdjointA<2, true><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, stage, record);
+    else kAdjointA<2, false><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, stage, record);
+  } else {
+    if (c.phys.viscous) kAdjointA<3, true><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, stage, record);
+    else kAdjointA<3, false><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, stage, record);
+  }
+}
+
+void launchAdjointB(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage, double apiFactor,
+                    bool api) {
+  const int G = gridFor(b.v.N);
+  MGD_LAUNCH(c);
+  if (c.nD == 2) {
+    if (c.phys.viscous) kAdjointB<2, true><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api);
+    else kAdjointB<2, false><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api);
+  } else {
+    if (c.phys.viscous) kAdjointB<3, true><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api);
+    else kAdjointB<3, false><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api);
+  }
+}
+
+void launchAdjointInitial(Context& c, DevBlock& b, double factor) {
+  MGD_LAUNCH(c);
+  if (c.nD == 2) kAdjointInitial<2><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, factor);
+  else kAdjointInitial<3><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, factor);
+}
+
+void launchSnapshot(Context& c, DevBlock& b, double* snapshots, int saveInterval, bool initial) {
+  const long long n = b.v.N * b.v.nU;
+  MGD_LAUNCH(c);
+  kSnapshot<<<gridFor(n), kBlock, 0, c.stream>>>(snapshots, b.v.q, n, c.dCounters, saveInterval, initial);
+}
+
+void launchStepAdvance(Context& c, int delta) {
+  MGD_LAUNCH(c);
+  kStepAdvance<<<1, 32, 0, c.stream>>>(c.dCounters, delta);
+}
+
+void launchReducePartials(Context& c, const double* partials, int nBlocks, int nSlots, double* out) {
+  if (nSlots <= 0) return;
+  MGD_LAUNCH(c);
+  kReducePartials<<<nSlots, kBlock, 0, c.stream>>>(partials, nBlocks, nSlots, out);
+}
+
+void launchCoordinateDerivative(Context& c, DevBlock& b, int dir, double* out) {
+  const double* coords = b.v.q;  // caller stages the coordinates in q
+  MGD_LAUNCH(c);
+  if (c.nD == 2)
+    kCoordinateDerivative<2><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, coords, dir, b.desc.periodic_length[dir], out);
+  else
+    kCoordinateDerivative<3><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, coords, dir, b.desc.periodic_length[dir], out);
+}
+
+void launchApplyD1(Context& c, DevBlock& b, int dir, const double* in, double* out, int ncomp) {
+  MGD_LAUNCH(c);
+  kApplyD1<<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, dir, in, out, ncomp);
+}
+
+void launchFarFieldTargetVisc(Context& c, DevBlock& b) {
+  if (b.v.ff.n == 0) return;
+  MGD_LAUNCH(c);
+  if (c.nD == 2) kFarFieldTargetVisc<2><<<gridFor(b.v.ff.n), kBlock, 0, c.stream>>>(b.v);
+  else kFarFieldTargetVisc<3><<<gridFor(b.v.ff.n), kBlock, 0, c.stream>>>(b.v);
+}
+
+// Far-field matrices from per-entry inviscid penalty and signed normal direction.
+void launchFarFieldMatricesWith(Context& c, DevBlock& b, const double* sigInv, const int* signedNormal) {
+  if (b.v.ff.n == 0) return;
+  MGD_LAUNCH(c);
+  if (c.nD == 2)
+    kFarFieldMatrices<2><<<gridFor(b.v.ff.n), kBlock, 0, c.stream>>>(b.v, c.phys.g, sigInv, signedNormal);
+  else
+    kFarFieldMatrices<3><<<gridFor(b.v.ff.n), kBlock, 0, c.stream>>>(b.v, c.phys.g, sigInv, signedNormal);
+}
+
+}  // namespace mgd

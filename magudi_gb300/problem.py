@@ -1,0 +1,173 @@
+"""Problem description shared by every front end of the library.
+
+A Problem holds what magudi reads from magudi.inp, bc.dat and the PLOT3D
+input files for one region: options, blocks (grid coordinates and iblank),
+patches, acoustic sources and the initial, target and mollifier fields.
+
+Array convention: a field with nc components on a block of N points is a
+float64 numpy array of shape (nc, N), C-contiguous, so that component c of
+point p = i + Nx*(j + Ny*k) sits at flat index p + N*c -- magudi's Fortran
+column-major x(N, nc) layout.
+"""
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+
+from . import capi
+
+
+@dataclass
+class Options:
+    """Hot-path keys of magudi.inp (src/SimulationFlagsImpl.f90:24-45,
+    src/SolverOptionsImpl.f90:46-135). Defaults are the reference defaults,
+    except composite_dissipation, which only the non-composite path supports."""
+
+    n_dimensions: int = 2
+    viscous: bool = False
+    dissipation: bool = False
+    composite_dissipation: bool = False
+    curvilinear: bool = True
+    use_constant_cfl: bool = True
+    enable_controller: bool = False
+    enable_functional: bool = False
+    controller_switch: bool = False
+    adjoint_forcing_switch: bool = True
+    ratio_of_specific_heats: float = 1.4
+    reynolds_number: float = 0.0
+    prandtl_number: float = 0.72
+    viscosity_power_law_exponent: float = 0.666
+    bulk_viscosity_ratio: float = 0.6
+    dissipation_amount: float = 0.0
+    time_step_size: float = 0.0
+    cfl: float = 0.5
+
+    def to_c(self) -> capi.Options:
+        o = capi.Options()
+        for name, _ in capi.Options._fields_:
+            v = getattr(self, name)
+            setattr(o, name, int(v) if isinstance(v, bool) else v)
+        return o
+
+
+@dataclass
+class Patch:
+    """One bc.dat row and its patches/<name>/... options."""
+
+    name: str
+    type: str
+    grid_index: int
+    normal_direction: int
+    extent: tuple  # (iMin, iMax, jMin, jMax, kMin, kMax), bc.dat convention
+    inviscid_penalty_amount: float = 1.0
+    viscous_penalty_amount: float = 1.0
+    sponge_amount: float = 1.0
+    sponge_exponent: int = 2
+
+    def to_c(self) -> capi.PatchDesc:
+        p = capi.PatchDesc()
+        p.name = self.name.encode()[: capi.MGD_NAME_LEN - 1]
+        p.type = capi.PATCH_TYPES[self.type]
+        p.grid_index = self.grid_index
+        p.normal_direction = self.normal_direction
+        for i in range(6):
+            p.extent[i] = int(self.extent[i])
+        p.inviscid_penalty_amount = self.inviscid_penalty_amount
+        p.viscous_penalty_amount = self.viscous_penalty_amount
+        p.sponge_amount = self.sponge_amount
+        p.sponge_exponent = int(self.sponge_exponent)
+        return p
+
+    def resolved_extent(self, grid_size):
+        """Extent with negative indices counted from the end
+        (src/PatchDescriptorImpl.f90:57-63); unused dimensions become 1..1."""
+        e = list(self.extent)
+        out = []
+        for i in range(3):
+            lo, hi = e[2 * i], e[2 * i + 1]
+            if grid_size[i] == 1:
+                lo, hi = 1, 1
+            if lo < 0:
+                lo += grid_size[i] + 1
+            if hi < 0:
+                hi += grid_size[i] + 1
+            out += [lo, hi]
+        return tuple(out)
+
+
+@dataclass
+class AcousticSource:
+    location: tuple
+    amplitude: float
+    frequency: float
+    radius: float
+    phase: float = 0.0
+
+    def to_c(self) -> capi.AcousticSource:
+        s = capi.AcousticSource()
+        for i in range(3):
+            s.location[i] = self.location[i] if i < len(self.location) else 0.0
+        s.amplitude, s.frequency, s.radius, s.phase = (
+            self.amplitude, self.frequency, self.radius, self.phase)
+        return s
+
+
+@dataclass
+class Block:
+    grid_size: tuple  # (Nx, Ny, Nz), Nz = 1 in 2D
+    coordinates: np.ndarray  # (nD, N)
+    iblank: Optional[np.ndarray] = None  # (N,) int32
+    periodicity_type: tuple = (0, 0, 0)
+    periodic_length: tuple = (0.0, 0.0, 0.0)
+    initial_state: Optional[np.ndarray] = None  # (nU, N)
+    target_state: Optional[np.ndarray] = None  # (nU, N)
+    control_mollifier: Optional[np.ndarray] = None  # (N,)
+    target_mollifier: Optional[np.ndarray] = None  # (N,)
+    mean_pressure: Optional[np.ndarray] = None  # (N,)
+
+    @property
+    def n_points(self) -> int:
+        return int(np.prod(self.grid_size))
+
+    def desc(self) -> capi.BlockDesc:
+        d = capi.BlockDesc()
+        for i in range(3):
+            d.grid_size[i] = int(self.grid_size[i])
+            d.periodicity_type[i] = int(self.periodicity_type[i])
+            d.periodic_length[i] = float(self.periodic_length[i])
+        return d
+
+    def iblank_array(self) -> np.ndarray:
+        if self.iblank is None:
+            return np.ones(self.n_points, dtype=np.int32)
+        return np.ascontiguousarray(self.iblank, dtype=np.int32)
+
+
+@dataclass
+class Problem:
+    options: Options
+    blocks: List[Block] = field(default_factory=list)
+    patches: List[Patch] = field(default_factory=list)
+    sources: List[AcousticSource] = field(default_factory=list)
+    n_steps: int = 0
+    save_interval: int = 10
+
+    @property
+    def n_unknowns(self) -> int:
+        return self.options.n_dimensions + 2
+
+    def actuator_points(self) -> int:
+        n = 0
+        for p in self.patches:
+            if p.type == "ACTUATOR":
+                e = p.resolved_extent(self.blocks[p.grid_index - 1].grid_size)
+                n += (e[1] - e[0] + 1) * (e[3] - e[2] + 1) * (e[5] - e[4] + 1)
+        return n
+
+
+def quiescent_state(n_points: int, n_dimensions: int, gamma: float) -> np.ndarray:
+    """State%makeQuiescent (src/StateImpl.f90:434-459): rho = 1, u = 0, p = 1/gamma."""
+    q = np.zeros((n_dimensions + 2, n_points))
+    q[0] = 1.0
+    q[n_dimensions + 1] = 1.0 / gamma / (gamma - 1.0)
+    return q

@@ -1,0 +1,184 @@
+"""Python front end of the CUDA library (the counterpart of magudi's
+Region/Solver driving, for users and tests). Every call goes through the C
+ABI of include/magudi_gb300.h; there is no CPU path. If the library cannot be
+loaded the constructor raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import capi
+
+_lib = None
+
+
+class MagudiError(RuntimeError):
+    pass
+
+
+def library_path():
+    from .build import LIB_PATH
+    return LIB_PATH
+
+
+def load_library(build_if_missing=True):
+    """Loads libmagudi_gb300.so (building it first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise MagudiError(f"{path} is missing; run magudi_gb300.build.build()")
+        from .build import build
+        build()
+    L = C.CDLL(path)
+    ctx = C.c_void_p
+    L.mgd_last_error.restype = C.c_char_p
+    L.mgd_last_error.argtypes = [ctx]
+    L.mgd_create.argtypes = [C.POINTER(capi.Options), C.POINTER(ctx)]
+    L.mgd_destroy.argtypes = [ctx]
+    L.mgd_add_block.argtypes = [ctx, C.POINTER(capi.BlockDesc), C.POINTER(C.c_double), C.POINTER(C.c_int)]
+    L.mgd_add_patch.argtypes = [ctx, C.POINTER(capi.PatchDesc)]
+    L.mgd_add_acoustic_source.argtypes = [ctx, C.POINTER(capi.AcousticSource)]
+    L.mgd_set_field.argtypes = [ctx, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    L.mgd_get_field.argtypes = [ctx, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    L.mgd_finalize_setup.argtypes = [ctx]
+    L.mgd_update_state.argtypes = [ctx]
+    L.mgd_compute_rhs.argtypes = [ctx, C.c_int, C.c_double, C.c_double]
+    L.mgd_update_adjoint_forcing.argtypes = [ctx, C.c_int]
+    L.mgd_compute_functional.argtypes = [ctx, C.POINTER(C.c_double)]
+    L.mgd_compute_sensitivity.argtypes = [ctx, C.POINTER(C.c_double)]
+    L.mgd_rk4_substep.argtypes = [ctx, C.c_int, C.POINTER(C.c_double), C.c_double, C.c_int]
+    L.mgd_set_control_forcing.argtypes = [ctx, C.POINTER(C.c_double), C.c_longlong]
+    L.mgd_actuator_patch_size.argtypes = [ctx, C.POINTER(C.c_longlong)]
+    L.mgd_run_forward.argtypes = [ctx, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_double)]
+    L.mgd_run_adjoint.argtypes = [ctx, C.POINTER(C.c_double)]
+    L.mgd_get_gradient.argtypes = [ctx, C.POINTER(C.c_double), C.c_longlong]
+    L.mgd_stream.restype = C.c_void_p
+    L.mgd_stream.argtypes = [ctx]
+    L.mgd_kernel_launches.restype = C.c_longlong
+    L.mgd_kernel_launches.argtypes = [ctx, C.c_int]
+    _lib = L
+    return L
+
+
+class Solver:
+    """One region on the current CUDA device, built from a Problem."""
+
+    def __init__(self, problem, finalize=True):
+        self.L = load_library()
+        self.problem = problem
+        self.nU = problem.n_unknowns
+        self._opts = problem.options.to_c()
+        h = C.c_void_p()
+        if self.L.mgd_create(C.byref(self._opts), C.byref(h)):
+            raise MagudiError(self.L.mgd_last_error(None).decode())
+        self.h = h
+        for blk in problem.blocks:
+            coords = np.ascontiguousarray(blk.coordinates, dtype=np.float64)
+            ib = blk.iblank_array()
+            d = blk.desc()
+            self._check(self.L.mgd_add_block(self.h, C.byref(d), capi.dptr(coords), capi.iptr(ib)))
+        for p in problem.patches:
+            pd = p.to_c()
+            self._check(self.L.mgd_add_patch(self.h, C.byref(pd)))
+        for s in problem.sources:
+            sd = s.to_c()
+            self._check(self.L.mgd_add_acoustic_source(self.h, C.byref(sd)))
+        for bi, blk in enumerate(problem.blocks, start=1):
+            if blk.target_state is not None:
+                self.set_field(bi, capi.FIELD_TARGET, blk.target_state)
+            if blk.control_mollifier is not None:
+                self.set_field(bi, capi.FIELD_CONTROL_MOLLIFIER, blk.control_mollifier)
+            if blk.target_mollifier is not None:
+                self.set_field(bi, capi.FIELD_TARGET_MOLLIFIER, blk.target_mollifier)
+            if blk.mean_pressure is not None:
+                self.set_field(bi, capi.FIELD_MEAN_PRESSURE, blk.mean_pressure)
+            if blk.initial_state is not None:
+                self.set_field(bi, capi.FIELD_CONSERVED, blk.initial_state)
+        if finalize:
+            self._check(self.L.mgd_finalize_setup(self.h))
+
+    def _check(self, rc):
+        if rc:
+            raise MagudiError(self.L.mgd_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mgd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _ncomp(self, field):
+        nD = self.problem.options.n_dimensions
+        return {capi.FIELD_CONSERVED: self.nU, capi.FIELD_ADJOINT: self.nU, capi.FIELD_TARGET: self.nU,
+                capi.FIELD_RHS: self.nU, capi.FIELD_METRICS: nD * nD,
+                capi.FIELD_ARC_LENGTHS: nD}.get(field, 1)
+
+    def set_field(self, block, field, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        self._check(self.L.mgd_set_field(self.h, block, field, capi.dptr(a)))
+
+    def get_field(self, block, field):
+        n = self.problem.blocks[block - 1].n_points
+        nc = self._ncomp(field)
+        out = np.zeros((nc, n)) if nc > 1 else np.zeros(n)
+        self._check(self.L.mgd_get_field(self.h, block, field, capi.dptr(out)))
+        return out
+
+    def update_state(self):
+        self._check(self.L.mgd_update_state(self.h))
+
+    def compute_rhs(self, mode, time=0.0, adjoint_forcing_factor=1.0):
+        self._check(self.L.mgd_compute_rhs(self.h, mode, time, adjoint_forcing_factor))
+
+    def update_adjoint_forcing(self, no_forcing=False):
+        self._check(self.L.mgd_update_adjoint_forcing(self.h, int(no_forcing)))
+
+    def functional(self):
+        v = C.c_double()
+        self._check(self.L.mgd_compute_functional(self.h, C.byref(v)))
+        return v.value
+
+    def sensitivity(self):
+        v = C.c_double()
+        self._check(self.L.mgd_compute_sensitivity(self.h, C.byref(v)))
+        return v.value
+
+    def rk4_substep(self, mode, time, dt, stage):
+        t = C.c_double(time)
+        self._check(self.L.mgd_rk4_substep(self.h, mode, C.byref(t), dt, stage))
+        return t.value
+
+    def actuator_points(self):
+        n = C.c_longlong()
+        self._check(self.L.mgd_actuator_patch_size(self.h, C.byref(n)))
+        return n.value
+
+    def set_control_forcing(self, entries):
+        a = np.ascontiguousarray(entries, dtype=np.float64)
+        n = a.size // max(1, self.actuator_points())
+        self._check(self.L.mgd_set_control_forcing(self.h, capi.dptr(a), n))
+
+    def run_forward(self, n_steps, save_interval=10, t0=0.0):
+        v = C.c_double()
+        self._check(self.L.mgd_run_forward(self.h, n_steps, save_interval, t0, C.byref(v)))
+        return v.value
+
+    def run_adjoint(self):
+        v = C.c_double()
+        self._check(self.L.mgd_run_adjoint(self.h, C.byref(v)))
+        return v.value
+
+    def gradient(self, n_entries):
+        P = self.actuator_points()
+        out = np.zeros(n_entries * P)
+        self._check(self.L.mgd_get_gradient(self.h, capi.dptr(out), n_entries))
+        return out.reshape(n_entries, P)
+
+    def kernel_launches(self, reset=False):
+        return self.L.mgd_kernel_launches(self.h, int(reset))

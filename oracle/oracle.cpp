@@ -1,0 +1,1763 @@
+// oracle.cpp -- CPU restatement of magudi's forward and discrete-adjoint RHS,
+// RK4 integrator, acoustic-noise functional and thermal-actuator gradient.
+//
+// TEST INFRASTRUCTURE ONLY. This file is the parity oracle for the CUDA path
+// and the timed CPU baseline. It is never linked into, loaded by or called
+// from the product library; only tests/, __graft_entry__.smoke() and the
+// cpu_baseline / --impl reference legs of bench.py use it, as the checker.
+//
+// Every routine restates the reference routine cited beside it (paths are
+// relative to the magudi source tree). Loop orders, the order of operations
+// inside sums and the placement of the 1/det multiply follow the reference,
+// so that results agree to rounding. The reference compiles with
+// -ffast-math; it is therefore not a bit-exact target and parity is defined
+// norm-wise.
+//
+// Parity status: the SBP 4-8 first-derivative operator is pinned against
+// the reference's own Python implementation (tests/golden/); the remaining
+// routines are pinned by the reference's property tests restated in tests/
+// (SBP identity, convergence order, adjoint dual consistency, RK4 adjoint
+// exactness, gradient finite-difference sweep).
+
+#include "../include/magudi_gb300.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+
+enum { SYMMETRIC = 0, SKEW_SYMMETRIC = 1 };
+
+// t_StencilOperator (include/StencilOperator.f90:12-29). rhsBoundary1(k,m):
+// k = column inside the boundary window, m = output row; stored column-major
+// as in Fortran.
+struct StencilOp {
+  int symmetryType = SYMMETRIC;
+  int interiorWidth = 0, boundaryWidth = 0, boundaryDepth = 0;
+  std::vector<double> interior;  // rhsInterior(-w/2 : w/2)
+  std::vector<double> rb1, rb2;  // rhsBoundary1/2(boundaryWidth, boundaryDepth)
+  std::vector<double> normBoundary;
+  int nGhost[2] = {0, 0};
+  int periodicOffset[2] = {0, 0};
+  bool hasDomainBoundary[2] = {true, true};
+
+  void allocate() {  // allocateData, src/StencilOperatorImpl.f90:15-33
+    interior.assign(interiorWidth, 0.0);
+    rb1.assign(boundaryWidth * boundaryDepth, 0.0);
+    rb2.assign(boundaryWidth * boundaryDepth, 0.0);
+    normBoundary.assign(boundaryDepth, 1.0);
+  }
+  double& in(int j) { return interior[j + interiorWidth / 2]; }
+  double in(int j) const { return interior[j + interiorWidth / 2]; }
+  double& b1(int k, int m) { return rb1[(k - 1) + boundaryWidth * (m - 1)]; }
+  double b1(int k, int m) const { return rb1[(k - 1) + boundaryWidth * (m - 1)]; }
+  double& b2(int k, int m) { return rb2[(k - 1) + boundaryWidth * (m - 1)]; }
+  double b2(int k, int m) const { return rb2[(k - 1) + boundaryWidth * (m - 1)]; }
+
+  void fillRightBoundary() {  // src/StencilOperatorImpl.f90:2181-2191
+    for (int m = 1; m <= boundaryDepth; ++m)
+      for (int k = 1; k <= boundaryWidth; ++k)
+        b2(k, m) = (symmetryType == SYMMETRIC ? 1.0 : -1.0) * b1(boundaryWidth + 1 - k, m);
+  }
+};
+
+// setupOperator "SBP 4-8 first derivative", src/StencilOperatorImpl.f90:1586-1743.
+StencilOp sbp48FirstDerivative() {
+  StencilOp op;
+  op.symmetryType = SKEW_SYMMETRIC;
+  op.interiorWidth = 9;
+  op.boundaryWidth = 12;
+  op.boundaryDepth = 8;
+  op.allocate();
+  op.in(1) = 4.0 / 5.0;
+  op.in(2) = -1.0 / 5.0;
+  op.in(3) = 4.0 / 105.0;
+  op.in(4) = -1.0 / 280.0;
+  for (int j = 1; j <= 4; ++j) op.in(-j) = -op.in(j);
+  const double nb[8] = {1498139.0 / 5080320.0, 1107307.0 / 725760.0, 20761.0 / 80640.0,
+                        1304999.0 / 725760.0,  299527.0 / 725760.0,  103097.0 / 80640.0,
+                        670091.0 / 725760.0,   5127739.0 / 5080320.0};
+  for (int i = 0; i < 8; ++i) op.normBoundary[i] = nb[i];
+  const double x1 = 541.0 / 1000.0, x2 = -27.0 / 400.0, x3 = 187.0 / 250.0;
+  auto& b = op;
+  b.b1(1, 1) = -2540160.0 / 1498139.0;
+  b.b1(2, 1) = 9.0 * (2257920.0 * x1 + 11289600.0 * x2 + 22579200.0 * x3 - 15849163.0) / 5992556.0;
+  b.b1(3, 1) = 3.0 * (-33868800.0 * x1 - 162570240.0 * x2 - 304819200.0 * x3 + 235236677.0) / 5992556.0;
+  b.b1(4, 1) = (609638400.0 * x1 + 2743372800.0 * x2 + 4572288000.0 * x3 - 3577778591.0) / 17977668.0;
+  b.b1(5, 1) = 3.0 * (-16934400 * x1 - 67737600.0 * x2 - 84672000.0 * x3 + 67906303.0) / 1498139.0;
+  b.b1(6, 1) = 105.0 * (967680.0 * x1 + 2903040.0 * x2 - 305821.0) / 5992556.0;
+  b.b1(7, 1) = 49.0 * (-1244160.0 * x1 + 18662400.0 * x3 - 13322233.0) / 17977668.0;
+  b.b1(8, 1) = 3.0 * (-6773760.0 * x2 - 33868800.0 * x3 + 24839327.0) / 5992556.0;
+
+  b.b1(1, 2) = 9.0 * (-2257920.0 * x1 - 11289600.0 * x2 - 22579200.0 * x3 + 15849163.0) / 31004596.0;
+  b.b1(2, 2) = 0.0;
+  b.b1(3, 2) = 3.0 * (7257600.0 * x1 + 33868800.0 * x2 + 60963840.0 * x3 - 47167457.0) / 2214614.0;
+  b.b1(4, 2) = 3.0 * (-9676800.0 * x1 - 42336000.0 * x2 - 67737600.0 * x3 + 53224573.0) / 1107307.0;
+  b.b1(5, 2) = 7.0 * (55987200.0 * x1 + 217728000.0 * x2 + 261273600.0 * x3 - 211102099.0) / 13287684.0;
+  b.b1(6, 2) = 3.0 * (-11612160.0 * x1 - 33868800.0 * x2 + 3884117.0) / 2214614.0;
+  b.b1(7, 2) = 150.0 * (24192.0 * x1 - 338688.0 * x3 + 240463.0) / 1107307.0;
+  b.b1(8, 2) = (152409600.0 * x2 + 731566080.0 * x3 - 536324953.0) / 46506894.0;
+
+  b.b1(1, 3) = (33868800.0 * x1 + 162570240.0 * x2 + 304819200.0 * x3 - 235236677.0) / 1743924.0;
+  b.b1(2, 3) = (-7257600.0 * x1 - 33868800.0 * x2 - 60963840.0 * x3 + 47167457.0) / 124566.0;
+  b.b1(3, 3) = 0.0;
+  b.b1(4, 3) = (24192000.0 * x1 + 101606400.0 * x2 + 152409600.0 * x3 - 120219461.0) / 124566.0;
+  b.b1(5, 3) = (-72576000.0 * x1 - 270950400.0 * x2 - 304819200.0 * x3 + 249289259.0) / 249132.0;
+  b.b1(6, 3) = 9.0 * (806400.0 * x1 + 2257920.0 * x2 - 290167.0) / 41522.0;
+  b.b1(7, 3) = 6.0 * (-134400.0 * x1 + 1693440.0 * x3 - 1191611.0) / 20761.0;
+  b.b1(8, 3) = 5.0 * (-2257920.0 * x2 - 10160640.0 * x3 + 7439833.0) / 290654.0;
+
+  b.b1(1, 4) = (-609638400.0 * x1 - 2743372800.0 * x2 - 4572288000.0 * x3 + 3577778591.0) / 109619916.0;
+  b.b1(2, 4) = 3.0 * (9676800.0 * x1 + 42336000.0 * x2 + 67737600.0 * x3 - 53224573.0) / 1304999.0;
+  b.b1(3, 4) = 3.0 * (-24192000.0 * x1 - 101606400.0 * x2 - 152409600.0 * x3 + 120219461.0) / 2609998.0;
+  b.b1(4, 4) = 0.0;
+  b.b1(5, 4) = 9.0 * (16128000.0 * x1 + 56448000.0 * x2 + 56448000.0 * x3 - 47206049.0) / 5219996.0;
+  b.b1(6, 4) = 3.0 * (-19353600.0 * x1 - 50803200.0 * x2 + 7628371.0) / 2609998.0;
+  b.b1(7, 4) = 2.0 * (10886400.0 * x1 - 114307200.0 * x3 + 79048289.0) / 3914997.0;
+  b.b1(8, 4) = 75.0 * (1354752.0 * x2 + 5419008.0 * x3 - 3952831.0) / 18269986.0;
+
+  b.b1(1, 5) = 3.0 * (16934400.0 * x1 + 67737600.0 * x2 + 84672000.0 * x3 - 67906303.0) / 2096689.0;
+  b.b1(2, 5) = 7.0 * (-55987200.0 * x1 - 217728000.0 * x2 - 261273600.0 * x3 + 211102099.0) / 3594324.0;
+  b.b1(3, 5) = 3.0 * (72576000.0 * x1 + 270950400.0 * x2 + 304819200.0 * x3 - 249289259.0) / 1198108.0;
+  b.b1(4, 5) = 9.0 * (-16128000.0 * x1 - 56448000.0 * x2 - 56448000.0 * x3 + 47206049.0) / 1198108.0;
+  b.b1(5, 5) = 0.0;
+  b.b1(6, 5) = 105.0 * (414720.0 * x1 + 967680.0 * x2 - 165527.0) / 1198108.0;
+  b.b1(7, 5) = 15.0 * (-967680.0 * x1 + 6773760.0 * x3 - 4472029.0) / 1198108.0;
+  b.b1(8, 5) = (-304819200.0 * x2 - 914457600.0 * x3 + 657798011.0) / 25160268.0;
+  b.b1(9, 5) = -2592.0 / 299527.0;
+
+  b.b1(1, 6) = 5.0 * (-967680.0 * x1 - 2903040.0 * x2 + 305821.0) / 1237164.0;
+  b.b1(2, 6) = (11612160.0 * x1 + 33868800.0 * x2 - 3884117.0) / 618582.0;
+  b.b1(3, 6) = 9.0 * (-806400.0 * x1 - 2257920.0 * x2 + 290167.0) / 206194.0;
+  b.b1(4, 6) = (19353600.0 * x1 + 50803200.0 * x2 - 7628371.0) / 618582.0;
+  b.b1(5, 6) = 35.0 * (-414720.0 * x1 - 967680.0 * x2 + 165527.0) / 1237164.0;
+  b.b1(6, 6) = 0.0;
+  b.b1(7, 6) = 80640.0 * x1 / 103097.0;
+  b.b1(8, 6) = 80640.0 * x2 / 103097.0;
+  b.b1(9, 6) = 3072.0 / 103097.0;
+  b.b1(10, 6) = -288.0 / 103097.0;
+
+  b.b1(1, 7) = 7.0 * (1244160.0 * x1 - 18662400.0 * x3 + 13322233.0) / 8041092.0;
+  b.b1(2, 7) = 150.0 * (-24192.0 * x1 + 338688.0 * x3 - 240463.0) / 670091.0;
+  b.b1(3, 7) = 54.0 * (134400.0 * x1 - 1693440.0 * x3 + 1191611.0) / 670091.0;
+  b.b1(4, 7) = 2.0 * (-10886400.0 * x1 + 114307200.0 * x3 - 79048289.0) / 2010273.0;
+  b.b1(5, 7) = 15.0 * (967680.0 * x1 - 6773760.0 * x3 + 4472029.0) / 2680364.0;
+  b.b1(6, 7) = -725760.0 * x1 / 670091.0;
+  b.b1(7, 7) = 0.0;
+  b.b1(8, 7) = 725760.0 * x3 / 670091.0;
+  b.b1(9, 7) = -145152.0 / 670091.0;
+  b.b1(10, 7) = 27648.0 / 670091.0;
+  b.b1(11, 7) = -2592.0 / 670091.0;
+
+  b.b1(1, 8) = 3.0 * (6773760.0 * x2 + 33868800.0 * x3 - 24839327.0) / 20510956.0;
+  b.b1(2, 8) = (-152409600.0 * x2 - 731566080.0 * x3 + 536324953.0) / 30766434.0;
+  b.b1(3, 8) = 45.0 * (2257920.0 * x2 + 10160640.0 * x3 - 7439833.0) / 10255478.0;
+  b.b1(4, 8) = 75.0 * (-1354752.0 * x2 - 5419008.0 * x3 + 3952831.0) / 10255478.0;
+  b.b1(5, 8) = (304819200.0 * x2 + 914457600.0 * x3 - 657798011.0) / 61532868.0;
+  b.b1(6, 8) = -5080320.0 * x2 / 5127739.0;
+  b.b1(7, 8) = -5080320.0 * x3 / 5127739.0;
+  b.b1(8, 8) = 0.0;
+  b.b1(9, 8) = 4064256.0 / 5127739.0;
+  b.b1(10, 8) = -1016064.0 / 5127739.0;
+  b.b1(11, 8) = 193536.0 / 5127739.0;
+  b.b1(12, 8) = -18144.0 / 5127739.0;
+  op.fillRightBoundary();
+  return op;
+}
+
+// "SBP 4-8 dissipation", src/StencilOperatorImpl.f90:1928-1941.
+StencilOp sbp48Dissipation() {
+  StencilOp op;
+  op.symmetryType = SYMMETRIC;
+  op.interiorWidth = 5;
+  op.boundaryWidth = 5;
+  op.boundaryDepth = 2;
+  op.allocate();
+  op.in(0) = 6.0;
+  op.in(1) = -4.0;
+  op.in(2) = 1.0;
+  op.in(-1) = op.in(1);
+  op.in(-2) = op.in(2);
+  for (int m = 1; m <= 2; ++m)
+    for (int k = 1; k <= 5; ++k) op.b1(k, m) = op.in(k - 3);
+  op.fillRightBoundary();
+  return op;
+}
+
+// "SBP 4-8 dissipation transpose", src/StencilOperatorImpl.f90:1942-1960.
+StencilOp sbp48DissipationTranspose() {
+  StencilOp op;
+  op.symmetryType = SYMMETRIC;
+  op.interiorWidth = 5;
+  op.boundaryWidth = 7;
+  op.boundaryDepth = 5;
+  op.allocate();
+  op.in(0) = 6.0;
+  op.in(1) = -4.0;
+  op.in(2) = 1.0;
+  op.in(-1) = op.in(1);
+  op.in(-2) = op.in(2);
+  for (int r = 1; r <= 3; ++r)
+    for (int m = 1; m <= 5; ++m) op.b1(r, m) = op.in(m - 3);
+  for (int m = 2; m <= 5; ++m) op.b1(4, m) = op.in(m - 4);
+  for (int m = 3; m <= 5; ++m) op.b1(5, m) = op.in(m - 5);
+  for (int m = 4; m <= 5; ++m) op.b1(6, m) = op.in(m - 6);
+  op.b1(7, 5) = op.in(-2);
+  op.fillRightBoundary();
+  return op;
+}
+
+// getAdjointOperator, src/StencilOperatorImpl.f90:2285-2372: H^-1 D^T H.
+StencilOp adjointOf(const StencilOp& d) {
+  StencilOp a;
+  a.symmetryType = d.symmetryType;
+  a.interiorWidth = d.interiorWidth;
+  a.boundaryDepth = d.boundaryWidth;
+  a.boundaryWidth = d.boundaryWidth + d.interiorWidth / 2;
+  a.allocate();
+  const int h = d.interiorWidth / 2;
+  for (int i = -h; i <= h; ++i) a.in(i) = d.in(-i);
+  a.normBoundary = d.normBoundary;
+  for (int k = 1; k <= d.boundaryWidth; ++k)
+    for (int m = 1; m <= d.boundaryDepth; ++m) a.b1(m, k) = d.b1(k, m);
+  for (int i = d.boundaryDepth + 1; i <= d.boundaryWidth + h; ++i)
+    for (int j = -h; j <= h; ++j) {
+      if (i + j > d.boundaryWidth) break;
+      a.b1(i, i + j) = d.in(j);
+    }
+  const int nn = (int)a.normBoundary.size();
+  for (int i = 1; i <= a.boundaryWidth; ++i)
+    for (int m = 1; m <= nn; ++m) a.b1(i, m) = a.b1(i, m) / a.normBoundary[m - 1];
+  for (int i = 1; i <= a.boundaryDepth; ++i)
+    for (int k = 1; k <= nn; ++k) a.b1(k, i) = a.b1(k, i) * a.normBoundary[k - 1];
+  a.fillRightBoundary();
+  return a;
+}
+
+// updateOperator, src/StencilOperatorImpl.f90:2195-2256, for one process.
+void updateOperator(StencilOp& op, int periodicityType) {
+  const bool periodic = periodicityType != MGD_PERIODIC_NONE;
+  op.hasDomainBoundary[0] = op.hasDomainBoundary[1] = !periodic;
+  op.nGhost[0] = op.nGhost[1] = periodic ? op.interiorWidth / 2 : 0;
+  op.periodicOffset[0] = op.periodicOffset[1] = 0;
+  if (periodicityType == MGD_PERIODIC_OVERLAP) op.periodicOffset[0] = op.periodicOffset[1] = 1;
+}
+
+// Strides of a block: point (i,j,k) 0-based is at i + n0*(j + n1*k).
+struct Lines {
+  long long n, stride, nLines;
+  int gs[3], dir;
+  Lines(const int g[3], int d) {
+    gs[0] = g[0]; gs[1] = g[1]; gs[2] = g[2]; dir = d;
+    n = g[d];
+    stride = d == 0 ? 1 : (d == 1 ? g[0] : (long long)g[0] * g[1]);
+    nLines = (long long)g[0] * g[1] * g[2] / n;
+  }
+  long long base(long long line) const {  // first point of the line-th pencil
+    if (dir == 0) return line * n;
+    if (dir == 1) {
+      long long i = line % gs[0], k = line / gs[0];
+      return i + (long long)gs[0] * gs[1] * k;
+    }
+    return line;
+  }
+};
+
+// applyOperator_{1,2,3} + applyOperatorAtInteriorPoints_{1,2,3} for one
+// process, src/StencilOperatorImpl.f90:35-457. x is (N, ncomp), in place.
+void apply(const StencilOp& op, double* x, int ncomp, const int gs[3], int dir) {
+  Lines L(gs, dir);
+  const long long N = (long long)gs[0] * gs[1] * gs[2];
+  const int n = (int)L.n, h = op.interiorWidth / 2;
+  const int g0 = op.nGhost[0], g1 = op.nGhost[1];
+  for (int c = 0; c < ncomp; ++c) {
+    double* xc = x + N * c;
+#pragma omp parallel for schedule(static)
+    for (long long line = 0; line < L.nLines; ++line) {
+      std::vector<double> xg(n + g0 + g1);
+      const long long b = L.base(line);
+      for (int i = 0; i < n; ++i) xg[g0 + i] = xc[b + i * L.stride];
+      // fillGhostPoints for a single process, src/MPIHelperImpl.f90:113-390.
+      for (int i = 1; i <= g0; ++i) xg[g0 - i] = xg[g0 + n - i - op.periodicOffset[0]];
+      for (int i = 1; i <= g1; ++i) xg[g0 + n - 1 + i] = xg[g0 + i - 1 + op.periodicOffset[1]];
+      int is = 0, ie = n - 1;
+      if (g0 == 0) is += op.boundaryDepth;
+      if (g1 == 0) ie -= op.boundaryDepth;
+      for (int i = is; i <= ie; ++i) {
+        const double* p = &xg[g0 + i];
+        double s;
+        if (op.symmetryType == SKEW_SYMMETRIC) {
+          s = op.in(1) * (p[1] - p[-1]);
+          for (int j = 2; j <= h; ++j) s += op.in(j) * (p[j] - p[-j]);
+        } else {
+          s = op.in(1) * (p[1] + p[-1]);
+          for (int j = 2; j <= h; ++j) s += op.in(j) * (p[j] + p[-j]);
+          s += op.in(0) * p[0];
+        }
+        xc[b + i * L.stride] = s;
+      }
+      const int w = op.boundaryWidth;
+      if (op.hasDomainBoundary[0])
+        for (int m = 1; m <= op.boundaryDepth; ++m) {
+          double s = op.b1(1, m) * xg[0];
+          for (int k = 2; k <= w; ++k) s += op.b1(k, m) * xg[k - 1];
+          xc[b + (m - 1) * L.stride] = s;
+        }
+      if (op.hasDomainBoundary[1])
+        for (int m = 1; m <= op.boundaryDepth; ++m) {
+          double s = op.b2(1, m) * xg[n - w];
+          for (int k = 2; k <= w; ++k) s += op.b2(k, m) * xg[n - w + k - 1];
+          xc[b + (n - m) * L.stride] = s;
+        }
+    }
+  }
+}
+
+// applyOperatorNorm / applyOperatorNormInverse, src/StencilOperatorImpl.f90:838-1107.
+void applyNorm(const StencilOp& op, double* x, int ncomp, const int gs[3], int dir, bool inverse) {
+  Lines L(gs, dir);
+  const long long N = (long long)gs[0] * gs[1] * gs[2];
+  const int n = (int)L.n, d = op.boundaryDepth;
+  for (int c = 0; c < ncomp; ++c)
+    for (long long line = 0; line < L.nLines; ++line) {
+      double* xc = x + N * c + L.base(line);
+      if (op.hasDomainBoundary[0])
+        for (int i = 1; i <= d; ++i) {
+          double& v = xc[(i - 1) * L.stride];
+          v = inverse ? v / op.normBoundary[i - 1] : op.normBoundary[i - 1] * v;
+        }
+      if (op.hasDomainBoundary[1])
+        for (int i = n + 1 - d; i <= n; ++i) {
+          double& v = xc[(i - 1) * L.stride];
+          v = inverse ? v / op.normBoundary[n - i] : op.normBoundary[n - i] * v;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pointwise gas dynamics, src/CNSHelperImpl.f90.
+// ---------------------------------------------------------------------------
+
+// computeJacobianOfInviscidFlux{2D,3D}, src/CNSHelperImpl.f90:1098-1445.
+// A(i,j) is stored at A[i + nU*j] (0-based, column-major).
+void inviscidJacobian(int nD, const double* cv, const double* m, double g, double* A,
+                      double v, const double* u, double T) {
+  const int nU = nD + 2;
+  double U = 0.0, u2 = 0.0;
+  for (int d = 0; d < nD; ++d) U += m[d] * u[d];
+  for (int d = 0; d < nD; ++d) u2 += u[d] * u[d];
+  (void)cv; (void)v;
+  const double phi2 = 0.5 * (g - 1.0) * u2;
+  auto a = [&](int i, int j) -> double& { return A[(i - 1) + nU * (j - 1)]; };
+  const int E = nU;
+  a(1, 1) = 0.0;
+  for (int d = 1; d <= nD; ++d) a(1 + d, 1) = phi2 * m[d - 1] - U * u[d - 1];
+  a(E, 1) = U * ((g - 2.0) / (g - 1.0) * phi2 - T);
+  for (int c = 1; c <= nD; ++c) {
+    a(1, 1 + c) = m[c - 1];
+    for (int d = 1; d <= nD; ++d) {
+      if (d == c) a(1 + d, 1 + c) = U - (g - 2.0) * u[c - 1] * m[c - 1];
+      else a(1 + d, 1 + c) = u[d - 1] * m[c - 1] - (g - 1.0) * u[c - 1] * m[d - 1];
+    }
+    a(E, 1 + c) = (T + phi2 / (g - 1.0)) * m[c - 1] - (g - 1.0) * U * u[c - 1];
+  }
+  a(1, E) = 0.0;
+  for (int d = 1; d <= nD; ++d) a(1 + d, E) = (g - 1.0) * m[d - 1];
+  a(E, E) = g * U;
+}
+
+// computeIncomingJacobianOfInviscidFlux{2D,3D}, src/CNSHelperImpl.f90:1669-2343
+// (without the variations). The state is passed as conserved variables only.
+void incomingJacobian(int nD, const double* cv, const double* metrics, double g,
+                      int incomingDirection, double* out) {
+  const int nU = nD + 2;
+  double arc = 0.0;
+  for (int d = 0; d < nD; ++d) arc += metrics[d] * metrics[d];
+  arc = std::sqrt(arc);
+  double nm[3];
+  for (int d = 0; d < nD; ++d) nm[d] = metrics[d] / arc;
+  const double v = 1.0 / cv[0];
+  double u[3], u2 = 0.0;
+  for (int d = 0; d < nD; ++d) u[d] = v * cv[d + 1];
+  for (int d = 0; d < nD; ++d) u2 += u[d] * u[d];
+  const double T = g * (v * cv[nD + 1] - 0.5 * u2);
+  double U = 0.0;
+  for (int d = 0; d < nD; ++d) U += nm[d] * u[d];
+  const double c = std::sqrt((g - 1.0) * T);
+  const double phi2 = 0.5 * (g - 1.0) * u2;
+  double R[25], Lt[25], lam[5];
+  auto r = [&](int i, int j) -> double& { return R[(i - 1) + nU * (j - 1)]; };
+  auto l = [&](int i, int j) -> double& { return Lt[(i - 1) + nU * (j - 1)]; };
+  const double rho = cv[0];
+  if (nD == 2) {
+    lam[0] = U; lam[1] = U; lam[2] = U + c; lam[3] = U - c;
+    for (int i = 0; i < 4; ++i) lam[i] = arc * lam[i];
+    for (int i = 0; i < 4; ++i) if (incomingDirection * lam[i] < 0.0) lam[i] = 0.0;
+    r(1, 1) = 1.0; r(2, 1) = u[0]; r(3, 1) = u[1]; r(4, 1) = phi2 / (g - 1.0);
+    r(1, 2) = 0.0; r(2, 2) = nm[1] * rho; r(3, 2) = -nm[0] * rho;
+    r(4, 2) = rho * (nm[1] * u[0] - nm[0] * u[1]);
+    r(1, 3) = 1.0; r(2, 3) = u[0] + nm[0] * c; r(3, 3) = u[1] + nm[1] * c;
+    r(4, 3) = T + phi2 / (g - 1.0) + c * U;
+    r(1, 4) = 1.0; r(2, 4) = u[0] - nm[0] * c; r(3, 4) = u[1] - nm[1] * c;
+    r(4, 4) = T + phi2 / (g - 1.0) - c * U;
+    l(1, 1) = 1.0 - phi2 / (c * c);
+    l(2, 1) = -v * (nm[1] * u[0] - nm[0] * u[1]);
+    l(3, 1) = 0.5 * (phi2 / (c * c) - U / c);
+    l(4, 1) = 0.5 * (phi2 / (c * c) + U / c);
+    l(1, 2) = u[0] / T; l(2, 2) = v * nm[1];
+    l(3, 2) = -0.5 * (u[0] / T - nm[0] / c); l(4, 2) = -0.5 * (u[0] / T + nm[0] / c);
+    l(1, 3) = u[1] / T; l(2, 3) = -v * nm[0];
+    l(3, 3) = -0.5 * (u[1] / T - nm[1] / c); l(4, 3) = -0.5 * (u[1] / T + nm[1] / c);
+    l(1, 4) = -1.0 / T; l(2, 4) = 0.0; l(3, 4) = 0.5 / T; l(4, 4) = 0.5 / T;
+  } else {
+    lam[0] = U; lam[1] = U; lam[2] = U; lam[3] = U + c; lam[4] = U - c;
+    for (int i = 0; i < 5; ++i) lam[i] = arc * lam[i];
+    for (int i = 0; i < 5; ++i) if (incomingDirection * lam[i] < 0.0) lam[i] = 0.0;
+    const double h0 = phi2 / (g - 1.0);
+    r(1, 1) = nm[0]; r(2, 1) = nm[0] * u[0]; r(3, 1) = nm[0] * u[1] + rho * nm[2];
+    r(4, 1) = nm[0] * u[2] - rho * nm[1];
+    r(5, 1) = rho * (nm[2] * u[1] - nm[1] * u[2]) + h0 * nm[0];
+    r(1, 2) = nm[1]; r(2, 2) = nm[1] * u[0] - rho * nm[2]; r(3, 2) = nm[1] * u[1];
+    r(4, 2) = nm[1] * u[2] + rho * nm[0];
+    r(5, 2) = rho * (nm[0] * u[2] - nm[2] * u[0]) + h0 * nm[1];
+    r(1, 3) = nm[2]; r(2, 3) = nm[2] * u[0] + rho * nm[1]; r(3, 3) = nm[2] * u[1] - rho * nm[0];
+    r(4, 3) = nm[2] * u[2];
+    r(5, 3) = rho * (nm[1] * u[0] - nm[0] * u[1]) + h0 * nm[2];
+    r(1, 4) = 1.0; r(2, 4) = u[0] + nm[0] * c; r(3, 4) = u[1] + nm[1] * c;
+    r(4, 4) = u[2] + nm[2] * c; r(5, 4) = T + h0 + c * U;
+    r(1, 5) = 1.0; r(2, 5) = u[0] - nm[0] * c; r(3, 5) = u[1] - nm[1] * c;
+    r(4, 5) = u[2] - nm[2] * c; r(5, 5) = T + h0 - c * U;
+    const double q = 1.0 - phi2 / (c * c);
+    l(1, 1) = nm[0] * q - v * (nm[2] * u[1] - nm[1] * u[2]);
+    l(2, 1) = nm[1] * q - v * (nm[0] * u[2] - nm[2] * u[0]);
+    l(3, 1) = nm[2] * q - v * (nm[1] * u[0] - nm[0] * u[1]);
+    l(4, 1) = 0.5 * (phi2 / (c * c) - U / c);
+    l(5, 1) = 0.5 * (phi2 / (c * c) + U / c);
+    l(1, 2) = nm[0] * u[0] / T; l(2, 2) = nm[1] * u[0] / T - v * nm[2];
+    l(3, 2) = nm[2] * u[0] / T + v * nm[1];
+    l(4, 2) = -0.5 * (u[0] / T - nm[0] / c); l(5, 2) = -0.5 * (u[0] / T + nm[0] / c);
+    l(1, 3) = nm[0] * u[1] / T + v * nm[2]; l(2, 3) = nm[1] * u[1] / T;
+    l(3, 3) = nm[2] * u[1] / T - v * nm[0];
+    l(4, 3) = -0.5 * (u[1] / T - nm[1] / c); l(5, 3) = -0.5 * (u[1] / T + nm[1] / c);
+    l(1, 4) = nm[0] * u[2] / T - v * nm[1]; l(2, 4) = nm[1] * u[2] / T + v * nm[0];
+    l(3, 4) = nm[2] * u[2] / T;
+    l(4, 4) = -0.5 * (u[2] / T - nm[2] / c); l(5, 4) = -0.5 * (u[2] / T + nm[2] / c);
+    l(1, 5) = -nm[0] / T; l(2, 5) = -nm[1] / T; l(3, 5) = -nm[2] / T;
+    l(4, 5) = 0.5 / T; l(5, 5) = 0.5 / T;
+  }
+  for (int j = 1; j <= nU; ++j)
+    for (int i = 1; i <= nU; ++i) {
+      double s = r(i, 1) * lam[0] * l(1, j);
+      for (int k = 2; k <= nU; ++k) s += r(i, k) * lam[k - 1] * l(k, j);
+      out[(i - 1) + nU * (j - 1)] = s;
+    }
+}
+
+// computeFirstPartialViscousJacobian{2D,3D}, src/CNSHelperImpl.f90:2412-2601.
+void firstPartialViscousJacobian(int nD, const double* m, const double* tau, const double* hf,
+                                 double n, double g, double v, const double* u, double T,
+                                 double* B) {
+  const int nU = nD + 2;
+  auto b = [&](int i, int j) -> double& { return B[(i - 1) + nU * (j - 1)]; };
+  double u2 = 0.0;
+  for (int d = 0; d < nD; ++d) u2 += u[d] * u[d];
+  const double phi2 = 0.5 * (g - 1.0) * u2;
+  double ct[3], cq = 0.0;
+  for (int a = 0; a < nD; ++a) {
+    ct[a] = m[0] * tau[nD * a + 0];
+    for (int d = 1; d < nD; ++d) ct[a] += m[d] * tau[nD * a + d];
+  }
+  cq = m[0] * hf[0];
+  for (int d = 1; d < nD; ++d) cq += m[d] * hf[d];
+  double t1 = u[0] * ct[0];
+  for (int d = 1; d < nD; ++d) t1 += u[d] * ct[d];
+  double uct = t1;
+  t1 = t1 - cq;
+  const int E = nU;
+  double t2 = n * g * v / T * (phi2 / (g - 1.0) - T / g);
+  b(1, 1) = 0.0;
+  for (int d = 1; d <= nD; ++d) b(1 + d, 1) = t2 * ct[d - 1];
+  b(E, 1) = t2 * t1 - v * uct;
+  for (int c = 1; c <= nD; ++c) {
+    t2 = -n * g * v / T * u[c - 1];
+    b(1, 1 + c) = 0.0;
+    for (int d = 1; d <= nD; ++d) b(1 + d, 1 + c) = t2 * ct[d - 1];
+    b(E, 1 + c) = t2 * t1 + v * ct[c - 1];
+  }
+  t2 = n * g * v / T;
+  b(1, E) = 0.0;
+  for (int d = 1; d <= nD; ++d) b(1 + d, E) = t2 * ct[d - 1];
+  b(E, E) = t2 * t1;
+}
+
+// computeSecondPartialViscousJacobian{2D,3D}, src/CNSHelperImpl.f90:2636-2757.
+// Output (nD+1)x(nD+1), column-major.
+void secondPartialViscousJacobian(int nD, const double* u, double mu, double lambda, double k,
+                                  double jac, const double* m1, const double* m2, double* B) {
+  const int n = nD + 1;
+  auto b = [&](int i, int j) -> double& { return B[(i - 1) + n * (j - 1)]; };
+  double t1 = m1[0] * m2[0], t2 = m2[0] * u[0], t3 = m1[0] * u[0];
+  for (int d = 1; d < nD; ++d) {
+    t1 += m1[d] * m2[d];
+    t2 += m2[d] * u[d];
+    t3 += m1[d] * u[d];
+  }
+  t2 = mu * t2;
+  t3 = lambda * t3;
+  for (int c = 1; c <= nD; ++c) {
+    for (int r = 1; r <= nD; ++r) {
+      if (r == c) b(r, c) = mu * t1 + (mu + lambda) * m1[c - 1] * m2[c - 1];
+      else b(r, c) = mu * m1[c - 1] * m2[r - 1] + lambda * m1[r - 1] * m2[c - 1];
+    }
+    b(n, c) = mu * t1 * u[c - 1] + m1[c - 1] * t2 + m2[c - 1] * t3;
+  }
+  for (int r = 1; r <= nD; ++r) b(r, n) = 0.0;
+  b(n, n) = k * t1;
+  for (int i = 0; i < n * n; ++i) B[i] = jac * B[i];
+}
+
+// ---------------------------------------------------------------------------
+// Region: grid, state, patches (single process, one or more blocks).
+// ---------------------------------------------------------------------------
+
+struct Patch {
+  mgd_patch_desc d;
+  int extent[6] = {0, 0, 0, 0, 0, 0};
+  long long offset[3] = {0, 0, 0}, localSize[3] = {0, 0, 0}, nPatchPoints = 0;
+  double inviscidPenaltyAmount = 0, viscousPenaltyAmount = 0;
+  std::vector<double> spongeStrength;       // (nPatchPoints)
+  std::vector<double> viscousFluxes;        // (nPatchPoints, nU, nD)
+  std::vector<double> targetViscousFluxes;  // (nPatchPoints, nU, nD)
+  std::vector<double> adjointForcing;       // (nPatchPoints, nU)
+  std::vector<double> controlForcing;       // (nPatchPoints, nU)
+};
+
+struct Block {
+  mgd_block_desc d;
+  int gs[3];
+  long long N;
+  bool isCurvilinear;
+  std::vector<double> coordinates, metrics, jacobian, norm, arcLengths;
+  std::vector<int> iblank;
+  std::vector<StencilOp> firstDerivative, adjointFirstDerivative, dissipation, dissipationTranspose;
+  // t_State, include/State.f90:51-87.
+  std::vector<double> conservedVariables, adjointVariables, targetState, rightHandSide;
+  std::vector<double> specificVolume, velocity, pressure, temperature, dynamicViscosity,
+      secondCoefficientOfViscosity, thermalDiffusivity, stressTensor, heatFlux;
+  std::vector<double> controlMollifier, targetMollifier, meanPressure;
+  std::vector<double> buffer1, buffer2;  // RK4 data_(i)%buffer1/2
+};
+
+struct Region {
+  mgd_options o;
+  int nD, nU;
+  double reInv = 0, prInv = 0, powerLawExponent = 0, bulkViscosityRatio = 0;
+  std::vector<Block> blocks;
+  std::vector<Patch> patches;
+  std::vector<mgd_acoustic_source> sources;
+  std::string error;
+  // run state
+  std::vector<double> forcingEntries;  // control forcing, file order
+  long long nForcingEntries = 0;
+  std::vector<double> gradientEntries;
+  int nSteps = 0;
+  double t0 = 0.0;
+  std::vector<std::vector<double>> stageStates;  // forward stage inputs per block
+  std::vector<double> stageTimes;
+  double finalTime = 0.0;
+};
+
+static long long patchGridIndex(const Block& b, long long i, long long j, long long k) {
+  return (i - 1) + b.gs[0] * ((j - 1) + (long long)b.gs[1] * (k - 1));
+}
+
+template <class F>
+static void forPatchPoints(const Patch& p, const Block& b, F f) {
+  long long pi = 0;
+  for (long long k = p.offset[2] + 1; k <= p.offset[2] + p.localSize[2]; ++k)
+    for (long long j = p.offset[1] + 1; j <= p.offset[1] + p.localSize[1]; ++j)
+      for (long long i = p.offset[0] + 1; i <= p.offset[0] + p.localSize[0]; ++i, ++pi)
+        f(patchGridIndex(b, i, j, k), pi);
+}
+
+// computeCoordinateDerivatives, src/GridImpl.f90:621-745.
+static void coordinateDerivatives(Region& R, Block& b, int dir, double* out) {
+  const int nD = R.nD;
+  const long long N = b.N;
+  if (b.d.periodicity_type[dir] != MGD_PERIODIC_PLANE) {
+    std::copy(b.coordinates.begin(), b.coordinates.end(), out);
+    apply(b.firstDerivative[dir], out, nD, b.gs, dir);
+    return;
+  }
+  const StencilOp& op = b.firstDerivative[dir];
+  Lines L(b.gs, dir);
+  const int n = (int)L.n, g0 = op.nGhost[0], g1 = op.nGhost[1], h = op.interiorWidth / 2;
+  for (int c = 0; c < nD; ++c)
+    for (long long line = 0; line < L.nLines; ++line) {
+      std::vector<double> xg(n + g0 + g1);
+      const long long base = L.base(line);
+      for (int i = 0; i < n; ++i) xg[g0 + i] = b.coordinates[N * c + base + i * L.stride];
+      for (int i = 1; i <= g0; ++i) xg[g0 - i] = xg[g0 + n - i - op.periodicOffset[0]];
+      for (int i = 1; i <= g1; ++i) xg[g0 + n - 1 + i] = xg[g0 + i - 1 + op.periodicOffset[1]];
+      if (c == dir) {
+        for (int i = 0; i < g0; ++i) xg[i] = xg[i] - b.d.periodic_length[dir];
+        for (int i = 0; i < g1; ++i) xg[g0 + n + i] = xg[g0 + n + i] + b.d.periodic_length[dir];
+      }
+      for (int i = 0; i < n; ++i) {
+        const double* p = &xg[g0 + i];
+        double s = op.in(1) * (p[1] - p[-1]);
+        for (int j = 2; j <= h; ++j) s += op.in(j) * (p[j] - p[-j]);
+        out[N * c + base + i * L.stride] = s;
+      }
+    }
+}
+
+// updateGrid, src/GridImpl.f90:746-1066.
+static void updateGrid(Region& R, Block& b) {
+  const int nD = R.nD;
+  const long long N = b.N;
+  std::vector<double> jmi(N * nD * nD);
+  for (int j = 0; j < nD; ++j) coordinateDerivatives(R, b, j, &jmi[N * nD * j]);
+  for (int i = 0; i < nD * nD; ++i)
+    for (long long p = 0; p < N; ++p)
+      if (b.iblank[p] == 0) jmi[N * i + p] = 0.0;
+  auto J = [&](int c, long long p) { return jmi[N * (c - 1) + p]; };
+  b.metrics.assign(N * nD * nD, 0.0);
+  b.jacobian.assign(N, 0.0);
+  b.arcLengths.assign(N * nD, 0.0);
+  auto M = [&](int c, long long p) -> double& { return b.metrics[N * (c - 1) + p]; };
+  if (nD == 2) {
+    for (long long p = 0; p < N; ++p) {
+      if (b.isCurvilinear) {
+        b.jacobian[p] = (J(1, p) * J(4, p) - J(2, p) * J(3, p));
+        M(1, p) = J(4, p); M(2, p) = -J(3, p); M(3, p) = -J(2, p); M(4, p) = J(1, p);
+        b.arcLengths[p] = std::sqrt(M(1, p) * M(1, p) + M(2, p) * M(2, p));
+        b.arcLengths[N + p] = std::sqrt(M(3, p) * M(3, p) + M(4, p) * M(4, p));
+      } else {
+        b.jacobian[p] = J(1, p) * J(4, p);
+        M(1, p) = J(4, p); M(2, p) = 0.0; M(3, p) = 0.0; M(4, p) = J(1, p);
+        b.arcLengths[p] = std::fabs(M(1, p));
+        b.arcLengths[N + p] = std::fabs(M(4, p));
+      }
+    }
+  } else {
+    bool anyPlane = false;
+    for (int d = 0; d < 3; ++d) anyPlane = anyPlane || b.d.periodicity_type[d] == MGD_PERIODIC_PLANE;
+    for (long long p = 0; p < N; ++p) {
+      if (b.isCurvilinear)
+        b.jacobian[p] = J(1, p) * (J(5, p) * J(9, p) - J(8, p) * J(6, p)) +
+                        J(4, p) * (J(8, p) * J(3, p) - J(2, p) * J(9, p)) +
+                        J(7, p) * (J(2, p) * J(6, p) - J(5, p) * J(3, p));
+      else
+        b.jacobian[p] = J(1, p) * J(5, p) * J(9, p);
+    }
+    if (anyPlane) {
+      for (long long p = 0; p < N; ++p) {
+        if (b.isCurvilinear) {
+          M(1, p) = J(5, p) * J(9, p) - J(8, p) * J(6, p);
+          M(2, p) = J(7, p) * J(6, p) - J(4, p) * J(9, p);
+          M(3, p) = J(4, p) * J(8, p) - J(7, p) * J(5, p);
+          M(4, p) = J(8, p) * J(3, p) - J(2, p) * J(9, p);
+          M(5, p) = J(1, p) * J(9, p) - J(7, p) * J(3, p);
+          M(6, p) = J(7, p) * J(2, p) - J(1, p) * J(8, p);
+          M(7, p) = J(2, p) * J(6, p) - J(5, p) * J(3, p);
+          M(8, p) = J(4, p) * J(3, p) - J(1, p) * J(6, p);
+          M(9, p) = J(1, p) * J(5, p) - J(4, p) * J(2, p);
+        } else {
+          M(1, p) = J(5, p) * J(9, p);
+          M(5, p) = J(1, p) * J(9, p);
+          M(9, p) = J(1, p) * J(5, p);
+        }
+      }
+    } else {
+      // Conservative metric form through derivatives of products.
+      std::vector<double> F(N);
+      auto term = [&](int jc, int coord, int dir) {
+        for (long long p = 0; p < N; ++p) F[p] = J(jc, p) * b.coordinates[N * (coord - 1) + p];
+        apply(b.firstDerivative[dir - 1], F.data(), 1, b.gs, dir - 1);
+      };
+      // metric(c) = D_a(jmi(x) * coord) - D_b(jmi(y) * coord), src/GridImpl.f90:902-1012.
+      struct T { int c, ja, coa, da, jb, cob, db; bool always; };
+      const T table[9] = {{1, 5, 3, 3, 8, 3, 2, true},  {2, 6, 1, 3, 9, 1, 2, false},
+                          {3, 4, 2, 3, 7, 2, 2, false}, {4, 8, 3, 1, 2, 3, 3, false},
+                          {5, 9, 1, 1, 3, 1, 3, true},  {6, 7, 2, 1, 1, 2, 3, false},
+                          {7, 2, 3, 2, 5, 3, 1, false}, {8, 3, 1, 2, 6, 1, 1, false},
+                          {9, 1, 2, 2, 4, 2, 1, true}};
+      for (const T& t : table) {
+        if (!t.always && !b.isCurvilinear) {
+          for (long long p = 0; p < N; ++p) M(t.c, p) = 0.0;
+          continue;
+        }
+        term(t.ja, t.coa, t.da);
+        for (long long p = 0; p < N; ++p) M(t.c, p) = F[p];
+        if (b.isCurvilinear) {
+          term(t.jb, t.cob, t.db);
+          for (long long p = 0; p < N; ++p) M(t.c, p) = M(t.c, p) - F[p];
+        }
+      }
+      for (int i = 1; i <= 9; ++i)
+        for (long long p = 0; p < N; ++p)
+          if (b.iblank[p] == 0) M(i, p) = 0.0;
+    }
+    for (long long p = 0; p < N; ++p) {
+      for (int d = 0; d < 3; ++d) {
+        if (b.isCurvilinear)
+          b.arcLengths[N * d + p] = std::sqrt(M(3 * d + 1, p) * M(3 * d + 1, p) +
+                                              M(3 * d + 2, p) * M(3 * d + 2, p) +
+                                              M(3 * d + 3, p) * M(3 * d + 3, p));
+        else
+          b.arcLengths[N * d + p] = std::fabs(M(4 * d + 1, p));
+      }
+    }
+  }
+  for (long long p = 0; p < N; ++p)
+    if (b.iblank[p] == 0) b.jacobian[p] = 1.0;
+  for (long long p = 0; p < N; ++p)
+    if (!(b.jacobian[p] > 0.0)) {
+      char msg[160];
+      std::snprintf(msg, sizeof msg, "Jacobian at point %lld is non-positive!", p);
+      R.error = msg;
+      return;
+    }
+  b.norm.assign(N, 1.0);
+  for (int d = 0; d < nD; ++d) applyNorm(b.firstDerivative[d], b.norm.data(), 1, b.gs, d, false);
+  for (long long p = 0; p < N; ++p) b.norm[p] = b.norm[p] * b.jacobian[p];
+  for (long long p = 0; p < N; ++p) b.jacobian[p] = 1.0 / b.jacobian[p];
+}
+
+// computeGradientOfScalar / computeGradientOfVector, src/GridImpl.f90:1172-1421:
+// grad(:, (c-1)*nD + d) = d f_c / d x_d.
+static void computeGradient(Region& R, Block& b, const double* f, int ncomp, double* grad) {
+  const int nD = R.nD;
+  const long long N = b.N;
+  std::vector<double> dxi((size_t)N * ncomp * nD);
+  for (int d = 0; d < nD; ++d) {
+    double* t = &dxi[(size_t)N * ncomp * d];
+    std::copy(f, f + N * ncomp, t);
+    apply(b.firstDerivative[d], t, ncomp, b.gs, d);
+  }
+  // dxi[N*(ncomp*d + c) + p] = d f_c / d xi_d
+  auto D = [&](int c, int d, long long p) { return dxi[N * (ncomp * d + c) + p]; };
+  auto M = [&](int c, long long p) { return b.metrics[N * (c - 1) + p]; };
+#pragma omp parallel for schedule(static)
+  for (long long p = 0; p < N; ++p) {
+    const double jac = b.jacobian[p];
+    for (int c = 0; c < ncomp; ++c)
+      for (int x = 0; x < nD; ++x) {
+        double s;
+        if (b.isCurvilinear) {
+          // jacobian * sum_d metrics(d, x) * df/dxi_d, metric of direction d component x
+          s = M(x + 1, p) * D(c, 0, p);
+          for (int d = 1; d < nD; ++d) s += M(nD * d + x + 1, p) * D(c, d, p);
+          s = jac * s;
+        } else {
+          s = jac * M(nD * x + x + 1, p) * D(c, x, p);
+        }
+        grad[N * (nD * c + x) + p] = s;
+      }
+  }
+}
+
+// updateState, src/StateImpl.f90:466-537, with computeDependentVariables
+// (src/CNSHelperImpl.f90:3-87), computeTransportVariables (:89-177) and
+// computeStressTensor (:353-458).
+static void updateState(Region& R, Block& b, const double* q) {
+  const int nD = R.nD;
+  const long long N = b.N;
+  const double g = R.o.ratio_of_specific_heats;
+#pragma omp parallel for schedule(static)
+  for (long long p = 0; p < N; ++p) {
+    const double v = 1.0 / q[p];
+    b.specificVolume[p] = v;
+    double u2 = 0.0;
+    for (int d = 0; d < nD; ++d) {
+      const double u = v * q[N * (d + 1) + p];
+      b.velocity[N * d + p] = u;
+    }
+    for (int d = 0; d < nD; ++d) u2 += b.velocity[N * d + p] * b.velocity[N * d + p];
+    const double pr = (g - 1.0) * (q[N * (nD + 1) + p] - 0.5 * q[p] * u2);
+    b.pressure[p] = pr;
+    b.temperature[p] = g * pr / (g - 1.0) * v;
+  }
+  if (!R.o.viscous) return;
+#pragma omp parallel for schedule(static)
+  for (long long p = 0; p < N; ++p) {
+    if (R.powerLawExponent <= 0.0) {
+      b.dynamicViscosity[p] = R.reInv;
+      b.secondCoefficientOfViscosity[p] = (R.bulkViscosityRatio - 2.0 / 3.0) * R.reInv;
+      b.thermalDiffusivity[p] = R.reInv * R.prInv;
+    } else {
+      const double mu = std::pow((g - 1.0) * b.temperature[p], R.powerLawExponent) * R.reInv;
+      b.dynamicViscosity[p] = mu;
+      b.secondCoefficientOfViscosity[p] = (R.bulkViscosityRatio - 2.0 / 3.0) * mu;
+      b.thermalDiffusivity[p] = mu * R.prInv;
+    }
+  }
+  computeGradient(R, b, b.velocity.data(), nD, b.stressTensor.data());
+  // in-place stress, src/CNSHelperImpl.f90:405-455
+#pragma omp parallel for schedule(static)
+  for (long long p = 0; p < N; ++p) {
+    double* s = b.stressTensor.data();
+    const double mu = b.dynamicViscosity[p], la = b.secondCoefficientOfViscosity[p];
+    auto S = [&](int c) -> double& { return s[N * (c - 1) + p]; };
+    if (nD == 2) {
+      const double div = la * (S(1) + S(4));
+      S(1) = 2.0 * mu * S(1) + div;
+      S(2) = mu * (S(2) + S(3));
+      S(3) = S(2);
+      S(4) = 2.0 * mu * S(4) + div;
+    } else {
+      const double div = la * (S(1) + S(5) + S(9));
+      S(1) = 2.0 * mu * S(1) + div;
+      S(2) = mu * (S(2) + S(4));
+      S(3) = mu * (S(3) + S(7));
+      S(4) = S(2);
+      S(5) = 2.0 * mu * S(5) + div;
+      S(6) = mu * (S(6) + S(8));
+      S(7) = S(3);
+      S(8) = S(6);
+      S(9) = 2.0 * mu * S(9) + div;
+    }
+  }
+  computeGradient(R, b, b.temperature.data(), 1, b.heatFlux.data());
+  for (int d = 0; d < nD; ++d)
+    for (long long p = 0; p < N; ++p)
+      b.heatFlux[N * d + p] = -b.thermalDiffusivity[p] * b.heatFlux[N * d + p];
+}
+
+// computeCartesianInviscidFluxes / computeCartesianViscousFluxes,
+// src/CNSHelperImpl.f90:563-689. flux layout (N, nU, nD).
+static void cartesianFluxes(Region& R, Block& b, const double* q, double* fInv, double* fVisc) {
+  const int nD = R.nD, nU = R.nU;
+  const long long N = b.N;
+#pragma omp parallel for schedule(static)
+  for (long long p = 0; p < N; ++p) {
+    auto F = [&](double* f, int c, int d) -> double& { return f[N * ((c - 1) + nU * (d - 1)) + p]; };
+    const double pr = b.pressure[p];
+    for (int d = 1; d <= nD; ++d) {
+      const double ud = b.velocity[N * (d - 1) + p];
+      F(fInv, 1, d) = q[N * d + p];
+      for (int c = 1; c <= nD; ++c) {
+        // the reference fills the upper triangle by copying the lower one
+        double v = c < d ? q[N * c + p] * b.velocity[N * (d - 1) + p]
+                         : q[N * d + p] * b.velocity[N * (c - 1) + p];
+        if (c == d) v = v + pr;
+        F(fInv, c + 1, d) = v;
+      }
+      F(fInv, nU, d) = ud * (q[N * (nD + 1) + p] + pr);
+    }
+    if (fVisc) {
+      const double* s = b.stressTensor.data();
+      for (int d = 1; d <= nD; ++d) {
+        F(fVisc, 1, d) = 0.0;
+        for (int c = 1; c <= nD; ++c) F(fVisc, c + 1, d) = s[N * (nD * (c - 1) + d - 1) + p];
+        double e = b.velocity[p] * s[N * (d - 1) + p];
+        for (int c = 2; c <= nD; ++c) e += b.velocity[N * (c - 1) + p] * s[N * (nD * (c - 1) + d - 1) + p];
+        F(fVisc, nU, d) = e - b.heatFlux[N * (d - 1) + p];
+      }
+    }
+  }
+}
+
+// Far-field patch setup, src/FarFieldPatchImpl.f90:3-74; sponge strengths,
+// src/PatchFactoryImpl.f90:161-374; updatePatchFactories (:446-574).
+static int setupPatches(Region& R) {
+  for (Patch& p : R.patches) {
+    Block& b = R.blocks[p.d.grid_index - 1];
+    // negative extents count from the end, src/PatchDescriptorImpl.f90:57-63
+    for (int i = 0; i < 3; ++i) {
+      int lo = p.d.extent[2 * i], hi = p.d.extent[2 * i + 1];
+      if (i >= R.nD) { lo = hi = 1; }
+      if (lo < 0) lo += b.gs[i] + 1;
+      if (hi < 0) hi += b.gs[i] + 1;
+      p.extent[2 * i] = lo;
+      p.extent[2 * i + 1] = hi;
+      p.offset[i] = lo - 1;
+      p.localSize[i] = hi - lo + 1;
+    }
+    p.nPatchPoints = p.localSize[0] * p.localSize[1] * p.localSize[2];
+    const int dir = std::abs(p.d.normal_direction);
+    if (p.d.type == MGD_PATCH_SAT_FAR_FIELD) {
+      const double nb = b.firstDerivative[dir - 1].normBoundary[0];
+      p.inviscidPenaltyAmount = std::copysign(p.d.inviscid_penalty_amount, (double)p.d.normal_direction) / nb;
+      p.viscousPenaltyAmount = R.o.viscous ? std::copysign(p.d.viscous_penalty_amount, (double)p.d.normal_direction) / nb : 0.0;
+      if (R.o.viscous) {
+        p.viscousFluxes.assign(p.nPatchPoints * R.nU * R.nD, 0.0);
+        p.targetViscousFluxes.assign(p.nPatchPoints * R.nU * R.nD, 0.0);
+      }
+    }
+    if (p.d.type == MGD_PATCH_COST_TARGET) p.adjointForcing.assign(p.nPatchPoints * R.nU, 0.0);
+    if (p.d.type == MGD_PATCH_ACTUATOR) p.controlForcing.assign(p.nPatchPoints * R.nU, 0.0);
+    if (p.d.type == MGD_PATCH_SPONGE) p.spongeStrength.assign(p.nPatchPoints, 0.0);
+  }
+  // computeSpongeStrengths
+  for (size_t bi = 0; bi < R.blocks.size(); ++bi) {
+    Block& b = R.blocks[bi];
+    for (int dir = 0; dir < R.nD; ++dir) {
+      bool any = false;
+      for (Patch& p : R.patches)
+        any = any || (p.d.type == MGD_PATCH_SPONGE && p.d.grid_index == (int)bi + 1 &&
+                      std::abs(p.d.normal_direction) == dir + 1);
+      if (!any) continue;
+      std::vector<double> cd(b.N * R.nD), arc(b.N);
+      coordinateDerivatives(R, b, dir, cd.data());
+      for (long long q = 0; q < b.N; ++q) {
+        double s = 0.0;
+        for (int c = 0; c < R.nD; ++c) s += cd[b.N * c + q] * cd[b.N * c + q];
+        arc[q] = std::sqrt(s);
+      }
+      for (Patch& p : R.patches) {
+        if (p.d.type != MGD_PATCH_SPONGE || p.d.grid_index != (int)bi + 1 ||
+            std::abs(p.d.normal_direction) != dir + 1 || p.nPatchPoints <= 0)
+          continue;
+        const int lo = p.extent[2 * dir], hi = p.extent[2 * dir + 1];
+        const long long stride = dir == 0 ? 1 : (dir == 1 ? b.gs[0] : (long long)b.gs[0] * b.gs[1]);
+        forPatchPoints(p, b, [&](long long gi, long long pi) {
+          long long idx[3] = {gi % b.gs[0], (gi / b.gs[0]) % b.gs[1], gi / ((long long)b.gs[0] * b.gs[1])};
+          const long long line0 = gi - idx[dir] * stride;
+          auto curve = [&](int i1) { return arc[line0 + (i1 - 1) * stride]; };
+          const int i = (int)idx[dir] + 1;
+          double num = 0.0, den = 0.0;
+          if (p.d.normal_direction > 0) {
+            for (int t = lo; t <= i - 1; ++t) num += curve(t);
+            for (int t = lo; t <= hi - 1; ++t) den += curve(t);
+          } else {
+            for (int t = i + 1; t <= hi; ++t) num += curve(t);
+            for (int t = lo + 1; t <= hi; ++t) den += curve(t);
+          }
+          p.spongeStrength[pi] = num / den;
+        });
+        for (auto& s : p.spongeStrength)
+          s = p.d.sponge_amount * std::pow(1.0 - s, (double)p.d.sponge_exponent);
+      }
+    }
+  }
+  // target viscous fluxes on far-field patches (updatePatchFactories)
+  if (R.o.viscous) {
+    for (size_t bi = 0; bi < R.blocks.size(); ++bi) {
+      Block& b = R.blocks[bi];
+      bool any = false;
+      for (Patch& p : R.patches) any = any || (p.d.type == MGD_PATCH_SAT_FAR_FIELD && p.d.grid_index == (int)bi + 1);
+      if (!any) continue;
+      updateState(R, b, b.targetState.data());
+      std::vector<double> fInv(b.N * R.nU * R.nD), fVisc(b.N * R.nU * R.nD);
+      cartesianFluxes(R, b, b.targetState.data(), fInv.data(), fVisc.data());
+      for (Patch& p : R.patches) {
+        if (p.d.type != MGD_PATCH_SAT_FAR_FIELD || p.d.grid_index != (int)bi + 1) continue;
+        for (int c = 0; c < R.nU * R.nD; ++c)
+          forPatchPoints(p, b, [&](long long gi, long long pi) {
+            p.targetViscousFluxes[p.nPatchPoints * c + pi] = fVisc[b.N * c + gi];
+          });
+      }
+    }
+  }
+  return 0;
+}
+
+// computeQuadratureOnPatches, src/PatchFactoryImpl.f90:376-444.
+static double quadratureOnPatches(Region& R, Block& b, int bi, int type, const double* f) {
+  std::vector<double> mask(b.N, 0.0);
+  for (Patch& p : R.patches) {
+    if (p.d.type != type || p.d.grid_index != bi + 1) continue;
+    forPatchPoints(p, b, [&](long long gi, long long) { mask[gi] = 1.0; });
+  }
+  for (long long q = 0; q < b.N; ++q)
+    if (b.iblank[q] == 0) mask[q] = 0.0;
+  double s = 0.0;
+  for (long long q = 0; q < b.N; ++q) s += mask[q] * b.norm[q] * f[q];
+  return s;
+}
+
+// normalizeControlMollifier / normalizeTargetMollifier (L1), src/RegionImpl.f90:459-603.
+static void normalizeMollifiers(Region& R) {
+  if (R.o.enable_controller) {
+    double s = 0.0;
+    for (size_t bi = 0; bi < R.blocks.size(); ++bi)
+      s += quadratureOnPatches(R, R.blocks[bi], (int)bi, MGD_PATCH_ACTUATOR, R.blocks[bi].controlMollifier.data());
+    for (auto& b : R.blocks)
+      for (auto& v : b.controlMollifier) v = v / s;
+  }
+  if (R.o.enable_functional) {
+    double s = 0.0;
+    for (size_t bi = 0; bi < R.blocks.size(); ++bi)
+      s += quadratureOnPatches(R, R.blocks[bi], (int)bi, MGD_PATCH_COST_TARGET, R.blocks[bi].targetMollifier.data());
+    for (auto& b : R.blocks)
+      for (auto& v : b.targetMollifier) v = v / s;
+  }
+}
+
+// addDissipation, src/RhsHelperImpl.f90:10-87 (non-composite path).
+static void addDissipation(Region& R, Block& b, int mode) {
+  const int nD = R.nD, nU = R.nU;
+  const long long N = b.N;
+  const double amount = mode == MGD_FORWARD ? R.o.dissipation_amount : -R.o.dissipation_amount;
+  std::vector<double> d(N * nU);
+  for (int i = 0; i < nD; ++i) {
+    const std::vector<double>& src = mode == MGD_FORWARD ? b.conservedVariables : b.adjointVariables;
+    std::copy(src.begin(), src.end(), d.begin());
+    apply(b.dissipation[i], d.data(), nU, b.gs, i);
+    for (int j = 0; j < nU; ++j)
+      for (long long p = 0; p < N; ++p) d[N * j + p] = -b.arcLengths[N * i + p] * d[N * j + p];
+    apply(b.dissipationTranspose[i], d.data(), nU, b.gs, i);
+    applyNorm(b.firstDerivative[i], d.data(), nU, b.gs, i, true);
+    for (long long k = 0; k < N * nU; ++k) b.rightHandSide[k] = b.rightHandSide[k] + amount * d[k];
+  }
+}
+
+// computeRhsForward, src/RhsHelperImpl.f90:254-354.
+static void computeRhsForward(Region& R, Block& b, int bi) {
+  const int nD = R.nD, nU = R.nU;
+  const long long N = b.N;
+  std::vector<double> f1(N * nU * nD), f2(N * nU * nD);
+  std::fill(b.rightHandSide.begin(), b.rightHandSide.end(), 0.0);
+  cartesianFluxes(R, b, b.conservedVariables.data(), f1.data(), R.o.viscous ? f2.data() : nullptr);
+  if (R.o.viscous)
+    for (long long k = 0; k < N * nU * nD; ++k) f1[k] = f1[k] - f2[k];
+  if (R.o.viscous)
+    for (Patch& p : R.patches) {
+      if (p.d.grid_index != bi + 1 || p.nPatchPoints <= 0 || p.d.type != MGD_PATCH_SAT_FAR_FIELD) continue;
+      for (int c = 0; c < nU * nD; ++c)
+        forPatchPoints(p, b, [&](long long gi, long long pi) { p.viscousFluxes[p.nPatchPoints * c + pi] = f2[N * c + gi]; });
+    }
+  // transformFluxes, src/CNSHelperImpl.f90:772-840
+  auto M = [&](int c, long long p) { return b.metrics[N * (c - 1) + p]; };
+#pragma omp parallel for schedule(static)
+  for (long long p = 0; p < N; ++p)
+    for (int c = 0; c < nU; ++c)
+      for (int i = 0; i < nD; ++i) {
+        double s;
+        if (b.isCurvilinear || nD == 1) {
+          s = M(nD * i + 1, p) * f1[N * (c + nU * 0) + p];
+          for (int d = 1; d < nD; ++d) s += M(nD * i + d + 1, p) * f1[N * (c + nU * d) + p];
+        } else {
+          s = M(nD * i + i + 1, p) * f1[N * (c + nU * i) + p];
+        }
+        f2[N * (c + nU * i) + p] = s;
+      }
+  for (int i = 0; i < nD; ++i) apply(b.firstDerivative[i], &f2[N * nU * i], nU, b.gs, i);
+  for (int c = 0; c < nU; ++c)
+    for (long long p = 0; p < N; ++p) {
+      double s = f2[N * c + p];
+      for (int i = 1; i < nD; ++i) s += f2[N * (c + nU * i) + p];
+      b.rightHandSide[N * c + p] = b.rightHandSide[N * c + p] - s;
+    }
+  if (R.o.dissipation) addDissipation(R, b, MGD_FORWARD);
+}
+
+// addFarFieldAdjointPenalty, src/RhsHelperImpl.f90:89-250.
+static void addFarFieldAdjointPenalty(Region& R, Block& b, int bi) {
+  const int nD = R.nD, nU = R.nU;
+  const long long N = b.N;
+  bool any = false;
+  for (Patch& p : R.patches) any = any || (p.d.type == MGD_PATCH_SAT_FAR_FIELD && p.d.grid_index == bi + 1);
+  if (!any) return;
+  std::vector<double> temp1(N * (nU - 1) * nD, 0.0), temp2(N * (nU - 1));
+  double B[16];
+  for (Patch& p : R.patches) {
+    if (p.d.type != MGD_PATCH_SAT_FAR_FIELD || p.d.grid_index != bi + 1 || p.nPatchPoints <= 0) continue;
+    const int dir = std::abs(p.d.normal_direction);
+    forPatchPoints(p, b, [&](long long gi, long long) {
+      if (b.iblank[gi] == 0) return;
+      double u[3], m1[3], m2[3];
+      for (int d = 0; d < nD; ++d) {
+        u[d] = b.velocity[N * d + gi];
+        m1[d] = b.metrics[N * (nD * (dir - 1) + d) + gi];
+      }
+      for (int l = 0; l < nD; ++l) {
+        for (int d = 0; d < nD; ++d) m2[d] = b.metrics[N * (nD * l + d) + gi];
+        secondPartialViscousJacobian(nD, u, b.dynamicViscosity[gi], b.secondCoefficientOfViscosity[gi],
+                                     b.thermalDiffusivity[gi], b.jacobian[gi], m1, m2, B);
+        for (int r = 0; r < nU - 1; ++r) {
+          double s = B[0 + (nU - 1) * r] * b.adjointVariables[N * 1 + gi];
+          for (int k = 1; k < nU - 1; ++k) s += B[k + (nU - 1) * r] * b.adjointVariables[N * (k + 1) + gi];
+          temp1[N * (r + (nU - 1) * l) + gi] = temp1[N * (r + (nU - 1) * l) + gi] - p.viscousPenaltyAmount * s;
+        }
+      }
+    });
+  }
+  for (int i = 0; i < nD; ++i) apply(b.adjointFirstDerivative[i], &temp1[N * (nU - 1) * i], nU - 1, b.gs, i);
+  for (int c = 0; c < nU - 1; ++c)
+    for (long long q = 0; q < N; ++q) {
+      double s = temp1[N * c + q];
+      for (int i = 1; i < nD; ++i) s += temp1[N * (c + (nU - 1) * i) + q];
+      temp2[N * c + q] = s;
+    }
+  const double g = R.o.ratio_of_specific_heats;
+  for (long long q = 0; q < N; ++q) {
+    const double v = b.specificVolume[q];
+    temp2[N * nD + q] = g * v * temp2[N * nD + q];
+    for (int i = 0; i < nD; ++i) temp2[N * i + q] = v * temp2[N * i + q] - b.velocity[N * i + q] * temp2[N * nD + q];
+    for (int c = 1; c < nU; ++c) b.rightHandSide[N * c + q] = b.rightHandSide[N * c + q] + temp2[N * (c - 1) + q];
+    double su = b.velocity[q] * temp2[q];
+    for (int i = 1; i < nD; ++i) su += b.velocity[N * i + q] * temp2[N * i + q];
+    b.rightHandSide[q] = b.rightHandSide[q] - v * b.conservedVariables[N * (nD + 1) + q] * temp2[N * nD + q] - su;
+  }
+}
+
+// computeRhsAdjoint, src/RhsHelperImpl.f90:356-596.
+static void computeRhsAdjoint(Region& R, Block& b, int bi) {
+  const int nD = R.nD, nU = R.nU;
+  const long long N = b.N;
+  const double g = R.o.ratio_of_specific_heats;
+  std::vector<double> temp1(N * nU * nD);
+  std::fill(b.rightHandSide.begin(), b.rightHandSide.end(), 0.0);
+  for (int i = 0; i < nD; ++i) {
+    std::copy(b.adjointVariables.begin(), b.adjointVariables.end(), temp1.begin() + N * nU * i);
+    apply(b.adjointFirstDerivative[i], &temp1[N * nU * i], nU, b.gs, i);
+  }
+#pragma omp parallel for schedule(static)
+  for (long long j = 0; j < N; ++j) {
+    double cv[5], u[3], m[3], tau[9], hf[3], A[25], B1[25];
+    for (int c = 0; c < nU; ++c) cv[c] = b.conservedVariables[N * c + j];
+    for (int d = 0; d < nD; ++d) u[d] = b.velocity[N * d + j];
+    if (R.o.viscous) {
+      for (int c = 0; c < nD * nD; ++c) tau[c] = b.stressTensor[N * c + j];
+      for (int d = 0; d < nD; ++d) hf[d] = b.heatFlux[N * d + j];
+    }
+    for (int i = 0; i < nD; ++i) {
+      for (int d = 0; d < nD; ++d) m[d] = b.metrics[N * (nD * i + d) + j];
+      inviscidJacobian(nD, cv, m, g, A, b.specificVolume[j], u, b.temperature[j]);
+      if (R.o.viscous) {
+        firstPartialViscousJacobian(nD, m, tau, hf, R.powerLawExponent, g, b.specificVolume[j], u,
+                                    b.temperature[j], B1);
+        for (int k = 0; k < nU * nU; ++k) A[k] = A[k] - B1[k];
+      }
+      for (int r = 0; r < nU; ++r) {
+        double s = A[0 + nU * r] * temp1[N * (0 + nU * i) + j];
+        for (int k = 1; k < nU; ++k) s += A[k + nU * r] * temp1[N * (k + nU * i) + j];
+        b.rightHandSide[N * r + j] = b.rightHandSide[N * r + j] + s;
+      }
+    }
+  }
+  if (R.o.viscous) {
+    std::vector<double> temp2(N * (nU - 1));
+#pragma omp parallel for schedule(static)
+    for (long long k = 0; k < N; ++k) {
+      double u[3], m1[3], m2[3], B2[16], ad[4 * 3];
+      for (int d = 0; d < nD; ++d) u[d] = b.velocity[N * d + k];
+      for (int t = 0; t < (nU - 1) * nD; ++t) ad[t] = 0.0;
+      for (int jj = 0; jj < nD; ++jj) {
+        for (int d = 0; d < nD; ++d) m2[d] = b.metrics[N * (nD * jj + d) + k];
+        for (int i = 0; i < nD; ++i) {
+          for (int d = 0; d < nD; ++d) m1[d] = b.metrics[N * (nD * i + d) + k];
+          secondPartialViscousJacobian(nD, u, b.dynamicViscosity[k], b.secondCoefficientOfViscosity[k],
+                                       b.thermalDiffusivity[k], b.jacobian[k], m1, m2, B2);
+          for (int r = 0; r < nU - 1; ++r) {
+            double s = B2[0 + (nU - 1) * r] * temp1[N * (1 + nU * i) + k];
+            for (int c = 1; c < nU - 1; ++c) s += B2[c + (nU - 1) * r] * temp1[N * (c + 1 + nU * i) + k];
+            ad[r + (nU - 1) * jj] = ad[r + (nU - 1) * jj] + s;
+          }
+        }
+      }
+      for (int jj = 0; jj < nD; ++jj)
+        for (int r = 0; r < nU - 1; ++r) temp1[N * (r + 1 + nU * jj) + k] = ad[r + (nU - 1) * jj];
+    }
+    for (int jj = 0; jj < nD; ++jj) apply(b.adjointFirstDerivative[jj], &temp1[N * (1 + nU * jj)], nU - 1, b.gs, jj);
+    for (int c = 0; c < nU - 1; ++c)
+      for (long long k = 0; k < N; ++k) {
+        double s = temp1[N * (c + 1) + k];
+        for (int jj = 1; jj < nD; ++jj) s += temp1[N * (c + 1 + nU * jj) + k];
+        temp2[N * c + k] = s;
+      }
+    for (long long k = 0; k < N; ++k) {
+      const double v = b.specificVolume[k];
+      temp2[N * nD + k] = g * v * temp2[N * nD + k];
+      for (int i = 0; i < nD; ++i) temp2[N * i + k] = v * temp2[N * i + k] - b.velocity[N * i + k] * temp2[N * nD + k];
+      for (int c = 1; c < nU; ++c) b.rightHandSide[N * c + k] = b.rightHandSide[N * c + k] - temp2[N * (c - 1) + k];
+      double su = b.velocity[k] * temp2[k];
+      for (int i = 1; i < nD; ++i) su += b.velocity[N * i + k] * temp2[N * i + k];
+      b.rightHandSide[k] = b.rightHandSide[k] + v * b.conservedVariables[N * (nD + 1) + k] * temp2[N * nD + k] + su;
+    }
+  }
+  if (R.o.dissipation) addDissipation(R, b, MGD_ADJOINT);
+  if (R.o.viscous) addFarFieldAdjointPenalty(R, b, bi);
+}
+
+// Patch%updateRhs for the implemented patch types (src/FarFieldPatchImpl.f90:93-286,
+// src/SpongePatchImpl.f90:65-165, src/ActuatorPatchImpl.f90:108-181,
+// src/CostTargetPatchImpl.f90:72-136).
+static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjointForcingFactor) {
+  const int nD = R.nD, nU = R.nU;
+  const long long N = b.N;
+  const double g = R.o.ratio_of_specific_heats;
+  if (p.nPatchPoints <= 0) return;
+  switch (p.d.type) {
+    case MGD_PATCH_SAT_FAR_FIELD: {
+      const int dir = std::abs(p.d.normal_direction);
+      const int incoming = p.d.normal_direction;
+      forPatchPoints(p, b, [&](long long gi, long long pi) {
+        if (b.iblank[gi] == 0) return;
+        double qt[5], m[3], Ain[25], B1[25];
+        for (int c = 0; c < nU; ++c) qt[c] = b.targetState[N * c + gi];
+        for (int d = 0; d < nD; ++d) m[d] = b.metrics[N * (nD * (dir - 1) + d) + gi];
+        incomingJacobian(nD, qt, m, g, incoming, Ain);
+        const double jac = b.jacobian[gi];
+        if (mode == MGD_FORWARD) {
+          for (int r = 0; r < nU; ++r) {
+            double s = Ain[r] * (b.conservedVariables[gi] - qt[0]);
+            for (int c = 1; c < nU; ++c) s += Ain[r + nU * c] * (b.conservedVariables[N * c + gi] - qt[c]);
+            b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] - p.inviscidPenaltyAmount * jac * s;
+          }
+          if (R.o.viscous)
+            for (int r = 0; r < nU; ++r) {
+              double s = 0.0;
+              for (int d = 0; d < nD; ++d) {
+                const long long idx = p.nPatchPoints * (r + nU * d) + pi;
+                const double t = (p.viscousFluxes[idx] - p.targetViscousFluxes[idx]) * m[d];
+                s = d == 0 ? t : s + t;
+              }
+              b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] + p.viscousPenaltyAmount * jac * s;
+            }
+        } else {
+          for (int r = 0; r < nU; ++r) {
+            double s = Ain[0 + nU * r] * b.adjointVariables[gi];
+            for (int c = 1; c < nU; ++c) s += Ain[c + nU * r] * b.adjointVariables[N * c + gi];
+            b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] + p.inviscidPenaltyAmount * jac * s;
+          }
+          if (R.o.viscous) {
+            double cv[5], u[3], tau[9], hf[3];
+            for (int c = 0; c < nU; ++c) cv[c] = b.conservedVariables[N * c + gi];
+            for (int d = 0; d < nD; ++d) u[d] = b.velocity[N * d + gi];
+            for (int c = 0; c < nD * nD; ++c) tau[c] = b.stressTensor[N * c + gi];
+            for (int d = 0; d < nD; ++d) hf[d] = b.heatFlux[N * d + gi];
+            (void)cv;
+            firstPartialViscousJacobian(nD, m, tau, hf, R.powerLawExponent, g, b.specificVolume[gi], u,
+                                        b.temperature[gi], B1);
+            for (int r = 0; r < nU; ++r) {
+              double s = B1[0 + nU * r] * b.adjointVariables[gi];
+              for (int c = 1; c < nU; ++c) s += B1[c + nU * r] * b.adjointVariables[N * c + gi];
+              b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] - p.viscousPenaltyAmount * jac * s;
+            }
+          }
+        }
+      });
+      break;
+    }
+    case MGD_PATCH_SPONGE:
+      for (int l = 0; l < nU; ++l)
+        forPatchPoints(p, b, [&](long long gi, long long pi) {
+          if (b.iblank[gi] == 0) return;
+          double& r = b.rightHandSide[N * l + gi];
+          if (mode == MGD_FORWARD)
+            r = r - p.spongeStrength[pi] * (b.conservedVariables[N * l + gi] - b.targetState[N * l + gi]);
+          else
+            r = r + p.spongeStrength[pi] * b.adjointVariables[N * l + gi];
+        });
+      break;
+    case MGD_PATCH_ACTUATOR:
+      if (mode != MGD_FORWARD || !R.o.controller_switch) break;
+      for (int l = 0; l < nU; ++l)
+        forPatchPoints(p, b, [&](long long gi, long long pi) {
+          if (b.iblank[gi] == 0) return;
+          const double t = b.controlMollifier[gi] * p.controlForcing[p.nPatchPoints * l + pi];
+          b.rightHandSide[N * l + gi] = b.rightHandSide[N * l + gi] + t;
+        });
+      break;
+    case MGD_PATCH_COST_TARGET:
+      if (mode == MGD_FORWARD) break;
+      for (int l = 0; l < nU; ++l)
+        forPatchPoints(p, b, [&](long long gi, long long pi) {
+          if (b.iblank[gi] == 0) return;
+          b.rightHandSide[N * l + gi] = b.rightHandSide[N * l + gi] + adjointForcingFactor * p.adjointForcing[p.nPatchPoints * l + pi];
+        });
+      break;
+  }
+}
+
+// Region%computeRhs, src/RegionImpl.f90:1877-2027 (single block sets, no interfaces).
+static void computeRhs(Region& R, int mode, double time, double adjointForcingFactor) {
+  for (size_t bi = 0; bi < R.blocks.size(); ++bi) {
+    if (mode == MGD_FORWARD) computeRhsForward(R, R.blocks[bi], (int)bi);
+    else computeRhsAdjoint(R, R.blocks[bi], (int)bi);
+  }
+  for (Block& b : R.blocks)
+    for (int j = 0; j < R.nU; ++j)
+      for (long long p = 0; p < b.N; ++p) b.rightHandSide[b.N * j + p] = b.rightHandSide[b.N * j + p] * b.jacobian[p];
+  for (Patch& p : R.patches) patchUpdateRhs(R, p, R.blocks[p.d.grid_index - 1], mode, adjointForcingFactor);
+  // State%addSources -> AcousticSource%add, src/StateImpl.f90:672-705, src/AcousticSourceImpl.f90:34-64
+  if (mode == MGD_FORWARD)
+    for (const mgd_acoustic_source& s : R.sources) {
+      const double pi = 4.0 * std::atan(1.0);
+      const double w = 2.0 * pi * s.frequency, gf = 9.0 / (2.0 * s.radius * s.radius);
+      const double a = s.amplitude * std::cos(w * time + s.phase);
+      for (Block& b : R.blocks)
+        for (long long p = 0; p < b.N; ++p) {
+          if (b.iblank[p] == 0) continue;
+          double r = 0.0;
+          for (int d = 0; d < R.nD; ++d) {
+            const double x = b.coordinates[b.N * d + p] - s.location[d];
+            r += x * x;
+          }
+          b.rightHandSide[b.N * (R.nD + 1) + p] = b.rightHandSide[b.N * (R.nD + 1) + p] + a * std::exp(-gf * r);
+        }
+    }
+  for (Block& b : R.blocks)
+    for (int j = 0; j < R.nU; ++j)
+      for (long long p = 0; p < b.N; ++p)
+        if (b.iblank[p] == 0) b.rightHandSide[b.N * j + p] = 0.0;
+}
+
+static void updateAll(Region& R) {
+  for (Block& b : R.blocks) updateState(R, b, b.conservedVariables.data());
+}
+
+// AcousticNoise%compute, src/AcousticNoiseImpl.f90:123-206.
+static double computeFunctional(Region& R) {
+  double J = 0.0;
+  for (size_t bi = 0; bi < R.blocks.size(); ++bi) {
+    Block& b = R.blocks[bi];
+    std::vector<double> f(b.N);
+    for (long long p = 0; p < b.N; ++p) {
+      const double F = b.pressure[p] - b.meanPressure[p];
+      f[p] = F * F * b.targetMollifier[p];
+    }
+    J += quadratureOnPatches(R, b, (int)bi, MGD_PATCH_COST_TARGET, f.data());
+  }
+  return J;
+}
+
+// computeAcousticNoiseAdjointForcing, src/AcousticNoiseImpl.f90:208-280 via
+// Functional%updateAdjointForcing, src/FunctionalImpl.f90:26-72.
+static void updateAdjointForcing(Region& R, bool noForcing) {
+  const int nD = R.nD, nU = R.nU;
+  const double g = R.o.ratio_of_specific_heats;
+  for (Patch& p : R.patches) {
+    if (p.d.type != MGD_PATCH_COST_TARGET || p.nPatchPoints <= 0) continue;
+    Block& b = R.blocks[p.d.grid_index - 1];
+    if (noForcing) {
+      std::fill(p.adjointForcing.begin(), p.adjointForcing.end(), 0.0);
+      continue;
+    }
+    const long long N = b.N, P = p.nPatchPoints;
+    forPatchPoints(p, b, [&](long long gi, long long pi) {
+      if (b.iblank[gi] == 0) return;
+      const double F = -2.0 * b.targetMollifier[gi] * 1.0 * (g - 1.0) * (b.pressure[gi] - b.meanPressure[gi]);
+      p.adjointForcing[P * (nD + 1) + pi] = F;
+      double u2 = 0.0;
+      for (int d = 0; d < nD; ++d) {
+        p.adjointForcing[P * (d + 1) + pi] = -b.velocity[N * d + gi] * F;
+        u2 += b.velocity[N * d + gi] * b.velocity[N * d + gi];
+      }
+      p.adjointForcing[pi] = 0.5 * u2 * F;
+    });
+    (void)nU;
+  }
+}
+
+// ThermalActuator%computeSensitivity, src/ThermalActuatorImpl.f90:83-159.
+static double computeSensitivity(Region& R) {
+  double s = 0.0;
+  for (size_t bi = 0; bi < R.blocks.size(); ++bi) {
+    Block& b = R.blocks[bi];
+    std::vector<double> f(b.N);
+    for (long long p = 0; p < b.N; ++p) {
+      const double F = b.adjointVariables[b.N * (R.nD + 1) + p] * b.controlMollifier[p] * 1.0;
+      f[p] = F * F;
+    }
+    s += quadratureOnPatches(R, b, (int)bi, MGD_PATCH_ACTUATOR, f.data());
+  }
+  return s;
+}
+
+static long long actuatorPoints(Region& R) {
+  long long n = 0;
+  for (Patch& p : R.patches)
+    if (p.d.type == MGD_PATCH_ACTUATOR) n += p.nPatchPoints;
+  return n;
+}
+
+// ThermalActuator%updateGradient, src/ThermalActuatorImpl.f90:383-443
+// (appends one entry, patches in bc.dat order).
+static void appendGradient(Region& R) {
+  for (Patch& p : R.patches) {
+    if (p.d.type != MGD_PATCH_ACTUATOR || p.nPatchPoints <= 0) continue;
+    Block& b = R.blocks[p.d.grid_index - 1];
+    forPatchPoints(p, b, [&](long long gi, long long) {
+      R.gradientEntries.push_back(b.adjointVariables[b.N * (R.nD + 1) + gi] * (b.controlMollifier[gi] * 1.0));
+    });
+  }
+}
+
+// controller%cleanupForcing + updateForcing / migrateToForcing for forward
+// stage (step, stage) of a run of nSteps, src/ThermalActuatorImpl.f90:161-381.
+static void loadForcing(Region& R, int step, int stage) {
+  const long long P = actuatorPoints(R);
+  const long long e = (long long)(R.nSteps - step) * 4 + (4 - stage);
+  long long off = 0;
+  for (Patch& p : R.patches) {
+    if (p.d.type != MGD_PATCH_ACTUATOR || p.nPatchPoints <= 0) continue;
+    std::fill(p.controlForcing.begin(), p.controlForcing.end(), 0.0);
+    if (e < R.nForcingEntries)
+      for (long long i = 0; i < p.nPatchPoints; ++i)
+        p.controlForcing[p.nPatchPoints * (R.nD + 1) + i] = 0.0 + 1.0 * R.forcingEntries[P * e + off + i];
+    off += p.nPatchPoints;
+  }
+}
+
+// substepForwardRK4 / substepAdjointRK4, src/RK4IntegratorImpl.f90:65-270.
+static void substep(Region& R, int mode, double& time, double dt, int stage, bool updateAfter) {
+  if (mode == MGD_FORWARD) {
+    if (stage == 1) for (Block& b : R.blocks) b.buffer1 = b.conservedVariables;
+    if (stage == 2 || stage == 4) time = time + dt / 2.0;
+    computeRhs(R, MGD_FORWARD, time, 1.0);
+    for (Block& b : R.blocks) {
+      const long long n = b.N * R.nU;
+      for (long long k = 0; k < n; ++k) {
+        const double r = b.rightHandSide[k];
+        switch (stage) {
+          case 1: b.buffer2[k] = b.conservedVariables[k] + dt * r / 6.0;
+                  b.conservedVariables[k] = b.buffer1[k] + dt * r / 2.0; break;
+          case 2: b.buffer2[k] = b.buffer2[k] + dt * r / 3.0;
+                  b.conservedVariables[k] = b.buffer1[k] + dt * r / 2.0; break;
+          case 3: b.buffer2[k] = b.buffer2[k] + dt * r / 3.0;
+                  b.conservedVariables[k] = b.buffer1[k] + dt * r; break;
+          case 4: b.conservedVariables[k] = b.buffer2[k] + dt * r / 6.0; break;
+        }
+      }
+    }
+    if (updateAfter) updateAll(R);
+  } else {
+    if (stage == 4) for (Block& b : R.blocks) b.buffer1 = b.adjointVariables;
+    const double factor = stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0);
+    computeRhs(R, MGD_ADJOINT, time, factor);
+    for (Block& b : R.blocks) {
+      const long long n = b.N * R.nU;
+      for (long long k = 0; k < n; ++k) {
+        const double r = b.rightHandSide[k];
+        switch (stage) {
+          case 4: b.buffer2[k] = b.adjointVariables[k] - dt * r / 6.0;
+                  b.adjointVariables[k] = b.buffer1[k] - dt * r / 2.0; break;
+          case 3: b.buffer2[k] = b.buffer2[k] - dt * r / 3.0;
+                  b.adjointVariables[k] = b.buffer1[k] - dt * r / 2.0; break;
+          case 2: b.buffer2[k] = b.buffer2[k] - dt * r / 3.0;
+                  b.adjointVariables[k] = b.buffer1[k] - dt * r; break;
+          case 1: b.adjointVariables[k] = b.buffer2[k] - dt * r / 6.0; break;
+        }
+      }
+    }
+    if (stage == 3 || stage == 1) time = time - dt / 2.0;
+  }
+}
+
+static const double kRkNorm[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
+
+// Solver%runForward, src/SolverImpl.f90:672-912 (functional on, constant dt).
+// Stage inputs are kept in memory for the adjoint run; that matches
+// UniformCheckpointer's recomputation exactly because the forward is deterministic.
+static double runForward(Region& R, int nSteps, double t0, bool keepStages) {
+  R.nSteps = nSteps;
+  R.t0 = t0;
+  const double dt = R.o.time_step_size;
+  double time = t0, J = 0.0;
+  updateAll(R);
+  R.stageStates.clear();
+  R.stageTimes.clear();
+  for (int step = 1; step <= nSteps; ++step) {
+    for (int i = 1; i <= 4; ++i) {
+      if (keepStages) {
+        std::vector<double> all;
+        for (Block& b : R.blocks) all.insert(all.end(), b.conservedVariables.begin(), b.conservedVariables.end());
+        R.stageStates.push_back(std::move(all));
+        R.stageTimes.push_back(time);
+      }
+      if (R.o.enable_controller && R.o.controller_switch) loadForcing(R, step, i);
+      substep(R, MGD_FORWARD, time, dt, i, true);
+      if (R.o.enable_functional) J = J + kRkNorm[i - 1] * dt * computeFunctional(R);
+    }
+  }
+  R.finalTime = time;
+  return J;
+}
+
+static void setForwardState(Region& R, const std::vector<double>& all) {
+  size_t off = 0;
+  for (Block& b : R.blocks) {
+    std::copy(all.begin() + off, all.begin() + off + b.conservedVariables.size(), b.conservedVariables.begin());
+    off += b.conservedVariables.size();
+  }
+  updateAll(R);
+}
+
+// Solver%runAdjoint, src/SolverImpl.f90:914-1245, and the adjoint initial
+// condition of loadInitialCondition, :368-427.
+static double runAdjoint(Region& R) {
+  const double dt = R.o.time_step_size;
+  // final forward state is the current state
+  updateAll(R);
+  for (Block& b : R.blocks) std::fill(b.adjointVariables.begin(), b.adjointVariables.end(), 0.0);
+  updateAdjointForcing(R, !R.o.adjoint_forcing_switch);
+  for (Block& b : R.blocks) std::fill(b.rightHandSide.begin(), b.rightHandSide.end(), 0.0);
+  for (Patch& p : R.patches)
+    if (p.d.type == MGD_PATCH_COST_TARGET) patchUpdateRhs(R, p, R.blocks[p.d.grid_index - 1], MGD_ADJOINT, -dt / 6.0);
+  for (Block& b : R.blocks)
+    for (size_t k = 0; k < b.adjointVariables.size(); ++k) b.adjointVariables[k] = b.adjointVariables[k] + b.rightHandSide[k];
+  R.gradientEntries.clear();
+  double time = R.finalTime - 0.5 * dt, s = 0.0;
+  for (int step = R.nSteps; step >= 1; --step) {
+    for (int i = 4; i >= 1; --i) {
+      setForwardState(R, R.stageStates[(size_t)(step - 1) * 4 + (i - 1)]);
+      appendGradient(R);
+      s = s + kRkNorm[i - 1] * dt * computeSensitivity(R);
+      const bool finalStage = (step == 1 && i == 1);
+      updateAdjointForcing(R, !R.o.adjoint_forcing_switch || finalStage);
+      substep(R, MGD_ADJOINT, time, dt, i, false);
+    }
+  }
+  return s;
+}
+
+}  // namespace orc
+
+// ---------------------------------------------------------------------------
+// C interface of the oracle (loaded by the tests through ctypes).
+// ---------------------------------------------------------------------------
+using orc::Region;
+
+extern "C" {
+
+void* orc_create(const mgd_options* o) {
+  Region* R = new Region();
+  R->o = *o;
+  R->nD = o->n_dimensions;
+  R->nU = o->n_dimensions + 2;
+  if (o->viscous) {
+    // src/SolverOptionsImpl.f90:56-71
+    double re = std::max(0.0, o->reynolds_number), pr = std::max(0.0, o->prandtl_number);
+    if (re <= 0.0 || pr <= 0.0) {
+      R->reInv = re; R->prInv = pr; R->powerLawExponent = 0.0; R->bulkViscosityRatio = 0.0;
+    } else {
+      R->reInv = 1.0 / re; R->prInv = 1.0 / pr;
+      R->powerLawExponent = o->viscosity_power_law_exponent;
+      R->bulkViscosityRatio = o->bulk_viscosity_ratio;
+    }
+  }
+  return R;
+}
+
+void orc_destroy(void* h) { delete (Region*)h; }
+
+const char* orc_last_error(void* h) { return ((Region*)h)->error.c_str(); }
+
+int orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
+
+int orc_add_block(void* h, const mgd_block_desc* d, const double* coords, const int* iblank) {
+  Region& R = *(Region*)h;
+  orc::Block b;
+  b.d = *d;
+  for (int i = 0; i < 3; ++i) b.gs[i] = i < R.nD ? d->grid_size[i] : 1;
+  b.N = (long long)b.gs[0] * b.gs[1] * b.gs[2];
+  b.isCurvilinear = R.o.curvilinear != 0;
+  b.coordinates.assign(coords, coords + b.N * R.nD);
+  b.iblank.assign(iblank, iblank + b.N);
+  auto d1 = orc::sbp48FirstDerivative();
+  auto diss = orc::sbp48Dissipation();
+  auto dissT = orc::sbp48DissipationTranspose();
+  for (int i = 0; i < R.nD; ++i) {
+    orc::StencilOp a = d1, ad = orc::adjointOf(d1), di = diss, dt = dissT;
+    orc::updateOperator(a, d->periodicity_type[i]);
+    orc::updateOperator(ad, d->periodicity_type[i]);
+    orc::updateOperator(di, d->periodicity_type[i]);
+    orc::updateOperator(dt, d->periodicity_type[i]);
+    b.firstDerivative.push_back(a);
+    b.adjointFirstDerivative.push_back(ad);
+    b.dissipation.push_back(di);
+    b.dissipationTranspose.push_back(dt);
+  }
+  const long long N = b.N;
+  const int nU = R.nU, nD = R.nD;
+  b.conservedVariables.assign(N * nU, 0.0);
+  b.adjointVariables.assign(N * nU, 0.0);
+  b.targetState.assign(N * nU, 0.0);
+  b.rightHandSide.assign(N * nU, 0.0);
+  b.buffer1.assign(N * nU, 0.0);
+  b.buffer2.assign(N * nU, 0.0);
+  b.specificVolume.assign(N, 0.0);
+  b.velocity.assign(N * nD, 0.0);
+  b.pressure.assign(N, 0.0);
+  b.temperature.assign(N, 0.0);
+  b.dynamicViscosity.assign(N, 0.0);
+  b.secondCoefficientOfViscosity.assign(N, 0.0);
+  b.thermalDiffusivity.assign(N, 0.0);
+  b.stressTensor.assign(N * nD * nD, 0.0);
+  b.heatFlux.assign(N * nD, 0.0);
+  b.controlMollifier.assign(N, 1.0);
+  b.targetMollifier.assign(N, 1.0);
+  b.meanPressure.assign(N, 1.0 / R.o.ratio_of_specific_heats);
+  // makeQuiescent target state, src/StateImpl.f90:434-459
+  for (long long p = 0; p < N; ++p) {
+    b.targetState[p] = 1.0;
+    b.targetState[N * (nD + 1) + p] = 1.0 / R.o.ratio_of_specific_heats / (R.o.ratio_of_specific_heats - 1.0);
+  }
+  R.blocks.push_back(std::move(b));
+  orc::updateGrid(R, R.blocks.back());
+  return R.error.empty() ? 0 : 1;
+}
+
+int orc_add_patch(void* h, const mgd_patch_desc* p) {
+  Region& R = *(Region*)h;
+  orc::Patch q;
+  q.d = *p;
+  R.patches.push_back(q);
+  return 0;
+}
+
+int orc_add_source(void* h, const mgd_acoustic_source* s) {
+  ((Region*)h)->sources.push_back(*s);
+  return 0;
+}
+
+static std::vector<double>* fieldOf(Region& R, orc::Block& b, int field, int* ncomp) {
+  *ncomp = 1;
+  switch (field) {
+    case MGD_FIELD_CONSERVED: *ncomp = R.nU; return &b.conservedVariables;
+    case MGD_FIELD_ADJOINT: *ncomp = R.nU; return &b.adjointVariables;
+    case MGD_FIELD_TARGET: *ncomp = R.nU; return &b.targetState;
+    case MGD_FIELD_RHS: *ncomp = R.nU; return &b.rightHandSide;
+    case MGD_FIELD_CONTROL_MOLLIFIER: return &b.controlMollifier;
+    case MGD_FIELD_TARGET_MOLLIFIER: return &b.targetMollifier;
+    case MGD_FIELD_MEAN_PRESSURE: return &b.meanPressure;
+    case MGD_FIELD_METRICS: *ncomp = R.nD * R.nD; return &b.metrics;
+    case MGD_FIELD_JACOBIAN: return &b.jacobian;
+    case MGD_FIELD_NORM: return &b.norm;
+    case MGD_FIELD_PRESSURE: return &b.pressure;
+    case MGD_FIELD_TEMPERATURE: return &b.temperature;
+    case MGD_FIELD_ARC_LENGTHS: *ncomp = R.nD; return &b.arcLengths;
+  }
+  return nullptr;
+}
+
+int orc_set_field(void* h, int block, int field, const double* src) {
+  Region& R = *(Region*)h;
+  int nc;
+  auto* v = fieldOf(R, R.blocks[block - 1], field, &nc);
+  if (!v) return 1;
+  std::copy(src, src + v->size(), v->begin());
+  return 0;
+}
+
+int orc_get_field(void* h, int block, int field, double* dst) {
+  Region& R = *(Region*)h;
+  int nc;
+  auto* v = fieldOf(R, R.blocks[block - 1], field, &nc);
+  if (!v) return 1;
+  std::copy(v->begin(), v->end(), dst);
+  return 0;
+}
+
+int orc_finalize_setup(void* h) {
+  Region& R = *(Region*)h;
+  orc::setupPatches(R);
+  orc::normalizeMollifiers(R);
+  return R.error.empty() ? 0 : 1;
+}
+
+int orc_update_state(void* h) {
+  orc::updateAll(*(Region*)h);
+  return 0;
+}
+
+int orc_compute_rhs(void* h, int mode, double time, double factor) {
+  orc::computeRhs(*(Region*)h, mode, time, factor);
+  return 0;
+}
+
+int orc_update_adjoint_forcing(void* h, int noForcing) {
+  orc::updateAdjointForcing(*(Region*)h, noForcing != 0);
+  return 0;
+}
+
+int orc_compute_functional(void* h, double* v) {
+  *v = orc::computeFunctional(*(Region*)h);
+  return 0;
+}
+
+int orc_compute_sensitivity(void* h, double* v) {
+  *v = orc::computeSensitivity(*(Region*)h);
+  return 0;
+}
+
+int orc_rk4_substep(void* h, int mode, double* time, double dt, int stage) {
+  orc::substep(*(Region*)h, mode, *time, dt, stage, mode == MGD_FORWARD);
+  return 0;
+}
+
+int orc_set_control_forcing(void* h, const double* src, long long nEntries) {
+  Region& R = *(Region*)h;
+  const long long P = orc::actuatorPoints(R);
+  R.forcingEntries.assign(src, src + P * nEntries);
+  R.nForcingEntries = nEntries;
+  return 0;
+}
+
+int orc_actuator_patch_size(void* h, long long* n) {
+  *n = orc::actuatorPoints(*(Region*)h);
+  return 0;
+}
+
+int orc_run_forward(void* h, int nSteps, int saveInterval, double t0, double* cost) {
+  (void)saveInterval;
+  *cost = orc::runForward(*(Region*)h, nSteps, t0, true);
+  return 0;
+}
+
+int orc_run_forward_nostore(void* h, int nSteps, double t0, double* cost) {
+  *cost = orc::runForward(*(Region*)h, nSteps, t0, false);
+  return 0;
+}
+
+int orc_run_adjoint(void* h, double* s) {
+  *s = orc::runAdjoint(*(Region*)h);
+  return 0;
+}
+
+int orc_get_gradient(void* h, double* dst, long long nEntries) {
+  Region& R = *(Region*)h;
+  const long long P = orc::actuatorPoints(R);
+  const long long n = std::min<long long>(nEntries * P, (long long)R.gradientEntries.size());
+  std::copy(R.gradientEntries.begin(), R.gradientEntries.begin() + n, dst);
+  return 0;
+}
+
+// Operator tables for the coefficient tests: which = 0 first derivative,
+// 1 adjoint first derivative, 2 dissipation, 3 dissipation transpose.
+int orc_operator_info(int which, int* dims /* symmetry, iw, bw, bd */, double* interior,
+                      double* rb1, double* norm) {
+  orc::StencilOp d1 = orc::sbp48FirstDerivative();
+  orc::StencilOp op = which == 0 ? d1 : which == 1 ? orc::adjointOf(d1)
+                      : which == 2 ? orc::sbp48Dissipation() : orc::sbp48DissipationTranspose();
+  dims[0] = op.symmetryType; dims[1] = op.interiorWidth; dims[2] = op.boundaryWidth; dims[3] = op.boundaryDepth;
+  if (interior) std::copy(op.interior.begin(), op.interior.end(), interior);
+  if (rb1) std::copy(op.rb1.begin(), op.rb1.end(), rb1);
+  if (norm) std::copy(op.normBoundary.begin(), op.normBoundary.end(), norm);
+  return (int)op.normBoundary.size();
+}
+
+// Applies one operator along direction dir of an (n0,n1,n2) array in place.
+int orc_apply_operator(int which, int periodicity, double* x, int ncomp, const int* gs, int dir) {
+  orc::StencilOp d1 = orc::sbp48FirstDerivative();
+  orc::StencilOp op = which == 0 ? d1 : which == 1 ? orc::adjointOf(d1)
+                      : which == 2 ? orc::sbp48Dissipation() : orc::sbp48DissipationTranspose();
+  orc::updateOperator(op, periodicity);
+  int g[3] = {gs[0], gs[1], gs[2]};
+  orc::apply(op, x, ncomp, g, dir);
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,200 @@
+"""ctypes front end of the CPU oracle (oracle/oracle.cpp) for the tests.
+
+The oracle is the checker: tests compare the CUDA library against it. It is
+built by oracle/build.sh into oracle/_build/liboracle.so.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from magudi_gb300 import capi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+
+_lib = None
+
+
+def build():
+    subprocess.check_call(["bash", os.path.join(ROOT, "oracle", "build.sh")])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.orc_create.restype = C.c_void_p
+        L.orc_create.argtypes = [C.POINTER(capi.Options)]
+        L.orc_destroy.argtypes = [C.c_void_p]
+        L.orc_last_error.restype = C.c_char_p
+        L.orc_last_error.argtypes = [C.c_void_p]
+        L.orc_add_block.argtypes = [C.c_void_p, C.POINTER(capi.BlockDesc), C.POINTER(C.c_double), C.POINTER(C.c_int)]
+        L.orc_add_patch.argtypes = [C.c_void_p, C.POINTER(capi.PatchDesc)]
+        L.orc_add_source.argtypes = [C.c_void_p, C.POINTER(capi.AcousticSource)]
+        for f in ("orc_set_field", "orc_get_field"):
+            getattr(L, f).argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double)]
+        L.orc_finalize_setup.argtypes = [C.c_void_p]
+        L.orc_update_state.argtypes = [C.c_void_p]
+        L.orc_compute_rhs.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double]
+        L.orc_update_adjoint_forcing.argtypes = [C.c_void_p, C.c_int]
+        L.orc_compute_functional.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.orc_compute_sensitivity.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.orc_rk4_substep.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.c_double, C.c_int]
+        L.orc_set_control_forcing.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_longlong]
+        L.orc_actuator_patch_size.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
+        L.orc_run_forward.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_double)]
+        L.orc_run_forward_nostore.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double)]
+        L.orc_run_adjoint.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.orc_get_gradient.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_longlong]
+        L.orc_operator_info.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_apply_operator.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.c_int,
+                                         C.POINTER(C.c_int), C.c_int]
+        L.orc_set_threads.argtypes = [C.c_int]
+        _lib = L
+    return _lib
+
+
+def set_threads(n):
+    return lib().orc_set_threads(n)
+
+
+def operator(which):
+    """(symmetry, interior, rhsBoundary1 (width, depth) array, normBoundary)."""
+    L = lib()
+    dims = (C.c_int * 4)()
+    L.orc_operator_info(which, dims, None, None, None)
+    sym, iw, bw, bd = list(dims)
+    interior = np.zeros(iw)
+    rb1 = np.zeros(bw * bd)
+    norm = np.zeros(max(bd, 12))
+    nn = L.orc_operator_info(which, dims, capi.dptr(interior), capi.dptr(rb1), capi.dptr(norm))
+    return sym, interior, rb1.reshape(bd, bw).T, norm[:nn]
+
+
+def apply_operator(which, x, grid_size, direction, periodicity=0):
+    """Applies operator `which` (0 D, 1 D-adjoint, 2 dissipation, 3 its transpose)
+    along `direction` (0-based) to x of shape (nc, N); returns a new array."""
+    y = np.ascontiguousarray(x, dtype=np.float64).copy()
+    gs = (C.c_int * 3)(*grid_size)
+    nc = y.shape[0] if y.ndim == 2 else 1
+    lib().orc_apply_operator(which, periodicity, capi.dptr(y), nc, gs, direction)
+    return y
+
+
+class Oracle:
+    """One oracle region built from a magudi_gb300.problem.Problem."""
+
+    def __init__(self, problem, finalize=True):
+        L = lib()
+        self.L = L
+        self.problem = problem
+        self._opts = problem.options.to_c()
+        self.h = L.orc_create(C.byref(self._opts))
+        self.nU = problem.n_unknowns
+        for blk in problem.blocks:
+            coords = np.ascontiguousarray(blk.coordinates, dtype=np.float64)
+            ib = blk.iblank_array()
+            d = blk.desc()
+            rc = L.orc_add_block(self.h, C.byref(d), capi.dptr(coords), capi.iptr(ib))
+            if rc:
+                raise RuntimeError(L.orc_last_error(self.h).decode())
+        for p in problem.patches:
+            pd = p.to_c()
+            L.orc_add_patch(self.h, C.byref(pd))
+        for s in problem.sources:
+            sd = s.to_c()
+            L.orc_add_source(self.h, C.byref(sd))
+        for bi, blk in enumerate(problem.blocks, start=1):
+            if blk.target_state is not None:
+                self.set_field(bi, capi.FIELD_TARGET, blk.target_state)
+            if blk.control_mollifier is not None:
+                self.set_field(bi, capi.FIELD_CONTROL_MOLLIFIER, blk.control_mollifier)
+            if blk.target_mollifier is not None:
+                self.set_field(bi, capi.FIELD_TARGET_MOLLIFIER, blk.target_mollifier)
+            if blk.mean_pressure is not None:
+                self.set_field(bi, capi.FIELD_MEAN_PRESSURE, blk.mean_pressure)
+            if blk.initial_state is not None:
+                self.set_field(bi, capi.FIELD_CONSERVED, blk.initial_state)
+        if finalize:
+            if L.orc_finalize_setup(self.h):
+                raise RuntimeError(L.orc_last_error(self.h).decode())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.orc_destroy(self.h)
+            self.h = None
+
+    def _ncomp(self, field):
+        nD = self.problem.options.n_dimensions
+        return {capi.FIELD_CONSERVED: self.nU, capi.FIELD_ADJOINT: self.nU, capi.FIELD_TARGET: self.nU,
+                capi.FIELD_RHS: self.nU, capi.FIELD_METRICS: nD * nD,
+                capi.FIELD_ARC_LENGTHS: nD}.get(field, 1)
+
+    def set_field(self, block, field, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        self.L.orc_set_field(self.h, block, field, capi.dptr(a))
+
+    def get_field(self, block, field):
+        n = self.problem.blocks[block - 1].n_points
+        nc = self._ncomp(field)
+        out = np.zeros((nc, n)) if nc > 1 else np.zeros(n)
+        self.L.orc_get_field(self.h, block, field, capi.dptr(out))
+        return out
+
+    def update_state(self):
+        self.L.orc_update_state(self.h)
+
+    def compute_rhs(self, mode, time=0.0, adjoint_forcing_factor=1.0):
+        self.L.orc_compute_rhs(self.h, mode, time, adjoint_forcing_factor)
+
+    def update_adjoint_forcing(self, no_forcing=False):
+        self.L.orc_update_adjoint_forcing(self.h, int(no_forcing))
+
+    def functional(self):
+        v = C.c_double()
+        self.L.orc_compute_functional(self.h, C.byref(v))
+        return v.value
+
+    def sensitivity(self):
+        v = C.c_double()
+        self.L.orc_compute_sensitivity(self.h, C.byref(v))
+        return v.value
+
+    def rk4_substep(self, mode, time, dt, stage):
+        t = C.c_double(time)
+        self.L.orc_rk4_substep(self.h, mode, C.byref(t), dt, stage)
+        return t.value
+
+    def actuator_points(self):
+        n = C.c_longlong()
+        self.L.orc_actuator_patch_size(self.h, C.byref(n))
+        return n.value
+
+    def set_control_forcing(self, entries):
+        a = np.ascontiguousarray(entries, dtype=np.float64)
+        n = a.size // max(1, self.actuator_points())
+        self.L.orc_set_control_forcing(self.h, capi.dptr(a), n)
+
+    def run_forward(self, n_steps, save_interval=10, t0=0.0, keep_stages=True):
+        v = C.c_double()
+        if keep_stages:
+            self.L.orc_run_forward(self.h, n_steps, save_interval, t0, C.byref(v))
+        else:
+            self.L.orc_run_forward_nostore(self.h, n_steps, t0, C.byref(v))
+        return v.value
+
+    def run_adjoint(self):
+        v = C.c_double()
+        self.L.orc_run_adjoint(self.h, C.byref(v))
+        return v.value
+
+    def gradient(self, n_entries):
+        P = self.actuator_points()
+        out = np.zeros(n_entries * P)
+        self.L.orc_get_gradient(self.h, capi.dptr(out), n_entries)
+        return out.reshape(n_entries, P)

@@ -1,0 +1,178 @@
+"""The CPU oracle against the reference's golden vectors and property tests
+(CPU only). These pin the oracle before it is trusted as the checker:
+
+- SBP 4-8 first derivative vs the reference's own Python implementation
+  (tests/golden/sbp48_first_derivative.npz, made by make_sbp_golden.py);
+- SBP identity H D + (H D)^T = diag(-1, 0, ..., 0, 1) (test/SBP_property.f90:108-109);
+- interior order 8 / boundary order 4 (test/operator_convergence.f90:86-130);
+- adjoint operator: <A x, y>_H = <x, D y>_H (getAdjointOperator);
+- dissipation self-adjointness (test/dissipation_self_adjoint.f90);
+- full-RHS dual consistency, FD order >= 0.9 (test/adjoint_relation/full_rhs.f90:220-454);
+- gradient finite-difference sweep J(eps) (README gradient-accuracy procedure).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_lib
+from helpers import fd_order, random_full_rhs_state, small_monopole
+from magudi_gb300 import capi, configs
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "sbp48_first_derivative.npz")
+
+
+def dense(which, n):
+    """Dense matrix of operator `which` on a non-periodic line of n points."""
+    M = np.zeros((n, n))
+    for k in range(n):
+        e = np.zeros((1, n))
+        e[0, k] = 1.0
+        M[:, k] = oracle_lib.apply_operator(which, e, (n, 1, 1), 0)[0]
+    return M
+
+
+def norm_diag(n):
+    _, _, _, h = oracle_lib.operator(0)
+    H = np.ones(n)
+    H[: len(h)] = h
+    H[n - len(h):] = h[::-1]
+    return H
+
+
+def test_first_derivative_matches_reference_python():
+    g = np.load(GOLDEN)
+    for n in (24, 37, 64):
+        x, d = g[f"x_{n}"], g[f"dx_{n}"]
+        y = oracle_lib.apply_operator(0, x.T.copy(), (n, 1, 1), 0)
+        assert np.max(np.abs(y - d.T)) <= 1e-14 * max(1.0, np.max(np.abs(d)))
+    y = oracle_lib.apply_operator(0, g["x_sin"].T.copy(), (50, 1, 1), 0)
+    assert np.max(np.abs(y - g["dx_sin"].T)) <= 1e-15
+
+
+@pytest.mark.parametrize("n", [25, 40, 57])
+def test_sbp_identity(n):
+    D = dense(0, n)
+    H = np.diag(norm_diag(n))
+    Q = H @ D
+    B = np.zeros((n, n))
+    B[0, 0], B[-1, -1] = -1.0, 1.0
+    assert np.max(np.abs(Q + Q.T - B)) < 10 * np.finfo(float).eps * n
+
+
+def test_convergence_order():
+    errs_int, errs_bnd, hs = [], [], []
+    w = 10.0
+    for n in (41, 61, 81, 121):
+        x = np.linspace(0.0, 1.0, n)
+        h = x[1] - x[0]
+        f = np.sin(w * x + 0.3)
+        d = oracle_lib.apply_operator(0, f[None, :], (n, 1, 1), 0)[0] / h
+        e = np.abs(d - w * np.cos(w * x + 0.3))
+        errs_int.append(e[12:-12].max())
+        errs_bnd.append(e[:8].max())
+        hs.append(h)
+    o_int = fd_order(hs, errs_int)
+    o_bnd = fd_order(hs, errs_bnd)
+    assert np.all(o_int > 7.9), o_int
+    assert o_bnd[-1] > 3.8 and np.all(np.diff(o_bnd) > 0), o_bnd
+
+
+@pytest.mark.parametrize("n", [30, 45])
+def test_adjoint_operator_is_h_adjoint(n):
+    D, A = dense(0, n), dense(1, n)
+    H = np.diag(norm_diag(n))
+    assert np.max(np.abs(H @ A - (H @ D).T)) < 1e-13
+
+
+def test_dissipation_self_adjoint():
+    n = 40
+    Dd, Dt = dense(2, n), dense(3, n)
+    assert np.max(np.abs(Dt - Dd.T)) == 0.0
+    H = norm_diag(n)
+    arc = np.linspace(0.5, 1.5, n)
+    M = np.diag(1.0 / H) @ Dt @ np.diag(-arc) @ Dd
+    HM = np.diag(H) @ M
+    assert np.max(np.abs(HM - HM.T)) < 1e-12
+
+
+def _dual_consistency(P, seed=1):
+    rng = np.random.default_rng(seed)
+    q0, lam = random_full_rhs_state(P, seed)
+    N = P.blocks[0].n_points
+    nD = P.options.n_dimensions
+    nU = nD + 2
+    g = P.options.ratio_of_specific_heats
+    dprim = rng.uniform(-1.0, 1.0, (nU, N))
+    dq = np.zeros_like(q0)
+    dq[0] = dprim[0]
+    for j in range(nD):
+        dq[1 + j] = q0[1 + j] / q0[0] * dprim[0] + q0[0] * dprim[1 + j]
+    dq[nU - 1] = (q0[nU - 1] / q0[0] * dprim[0] + np.sum(q0[1:1 + nD] * dprim[1:1 + nD], axis=0)
+                  + q0[0] / g * dprim[nU - 1])
+    o = oracle_lib.Oracle(P)
+    o.set_field(1, capi.FIELD_CONSERVED, q0)
+    o.update_state()
+    o.set_field(1, capi.FIELD_ADJOINT, lam)
+    o.update_adjoint_forcing(True)
+    o.compute_rhs(capi.FORWARD, 0.3)
+    r0 = o.get_field(1, capi.FIELD_RHS)
+    o.compute_rhs(capi.ADJOINT, 0.3, 1.0)
+    ra = o.get_field(1, capi.FIELD_RHS)
+    norm = o.get_field(1, capi.FIELD_NORM)
+    s1 = np.sum(ra * norm * dq)
+    hs, errs = [], []
+    h = 1e-3
+    for _ in range(12):
+        o.set_field(1, capi.FIELD_CONSERVED, q0 + h * dq)
+        o.update_state()
+        o.compute_rhs(capi.FORWARD, 0.3)
+        s2 = np.sum(lam * norm * (o.get_field(1, capi.FIELD_RHS) - r0))
+        hs.append(h)
+        errs.append(abs((s2 / h + s1) / s1))
+        h *= 10 ** -0.25
+    order = fd_order(hs, errs)
+    order = np.sort(order)[1:-1]  # trimmed mean, as full_rhs.f90:443-451
+    return order.mean()
+
+
+def test_full_rhs_dual_consistency_2d():
+    P = small_monopole(n=31, ny=29, sponge_points=5)
+    assert _dual_consistency(P) >= 0.9
+
+
+def test_full_rhs_dual_consistency_2d_curvilinear_inviscid_penalty_only():
+    P = small_monopole(n=29, ny=31, sponge_points=4)
+    P.options.curvilinear = True
+    x, y = P.blocks[0].coordinates
+    P.blocks[0].coordinates = np.ascontiguousarray(np.stack([x + 0.1 * np.sin(0.4 * y), y + 0.05 * np.sin(0.3 * x)]))
+    for p in P.patches:
+        if p.type == "SAT_FAR_FIELD":
+            p.viscous_penalty_amount = 0.0
+    assert _dual_consistency(P, 3) >= 0.9
+
+
+def test_full_rhs_dual_consistency_3d_periodic():
+    P = configs.taylor_green_3d(n=12)
+    P.options.use_constant_cfl = False
+    P.options.time_step_size = 0.01
+    assert _dual_consistency(P, 2) >= 0.9
+
+
+def test_gradient_finite_difference_sweep():
+    P = small_monopole(n=33, ny=33, n_steps=24, save_interval=6)
+    o = oracle_lib.Oracle(P)
+    J0 = o.run_forward(P.n_steps)
+    G0 = o.run_adjoint()
+    grad = o.gradient(4 * P.n_steps)
+    assert J0 > 0 and G0 > 0
+    P.options.controller_switch = True
+    best = 1.0
+    for k in (0, 2, 4):
+        eps = 10 ** (-2 - 0.25 * k)
+        o2 = oracle_lib.Oracle(P)
+        o2.set_control_forcing(eps * grad)
+        J1 = o2.run_forward(P.n_steps, keep_stages=False)
+        best = min(best, abs((J1 - J0) / eps - G0) / G0)
+    # the error grows as eps shrinks (roundoff in J1 - J0); its minimum bounds the adjoint error
+    assert best < 1e-5
