@@ -1,0 +1,325 @@
+"""Benchmark of the magudi hot path on one GB300.
+
+Workload (one "step"): the 2D acoustic monopole, 201x201 grid on [-14,14]^2,
+FP64 viscous Navier-Stokes with SBP 4-8 derivatives and dissipation,
+far-field SATs, 20-point sponges, a Gaussian cost target and control
+mollifier; 960 RK4 steps forward (dt = 0.05) with a snapshot every 10 steps,
+then the discrete adjoint over the same horizon with uniform checkpointing
+(forward recomputed on the device between snapshots) -- one complete
+forward + adjoint gradient evaluation.
+
+Metric: FP64 Mpt-RHS/s = grid points x (forward + adjoint RHS evaluations)
+/ seconds / 1e6 (the forward recomputation of checkpointing is not counted).
+`value` is device-timed (CUDA events on the library's stream) with the
+initial state already in HBM; `e2e` is the same metric through the C ABI
+with the initial state uploaded from pinned host memory and the gradient
+vector, J and Grad0 read back each step.
+
+--impl reference times the CPU restatement of the reference (oracle/) on the
+host cores (the Fortran reference cannot be built: it needs an MPI Fortran
+toolchain and CMake-generated headers) on a bounded sample of the same
+workload (fewer RK steps of the same grid), scaled to the same metric.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GRID = 201
+N_STEPS = 960
+SAVE_INTERVAL = 10
+WORKLOAD = ("2D acoustic monopole 201x201, FP64 viscous NS, SBP 4-8 + dissipation 0.01, far-field SAT + "
+            "20-pt sponge, forward 960 RK4 steps (dt 0.05) + discrete adjoint, uniform checkpointing "
+            "every 10 steps on the device")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-sample-steps", type=int, default=40)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--rk-steps", type=int, default=N_STEPS,
+                    help="RK4 steps per gradient evaluation (profiling runs use a few)")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="run the gradient evaluations and exit (for ncu captures; prints no bench line)")
+    return ap.parse_args()
+
+
+def rank_info():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def problem(n_steps=N_STEPS):
+    from magudi_gb300 import configs
+    return configs.monopole_2d(n=GRID, n_steps=n_steps, save_interval=SAVE_INTERVAL)
+
+
+def cpu_sample(sample_steps, threads=None):
+    """Times the oracle on the full grid for `sample_steps` RK steps forward +
+    adjoint; returns (Mpt-RHS/s, seconds, cores)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    cores = threads or os.cpu_count()
+    oracle_lib.set_threads(cores)
+    P = problem()
+    o = oracle_lib.Oracle(P)
+    t = time.perf_counter()
+    o.run_forward(sample_steps)
+    o.run_adjoint()
+    dt = time.perf_counter() - t
+    pts = P.blocks[0].n_points
+    return pts * 8 * sample_steps / dt / 1e6, dt, cores
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/mgd_clocks.csv"
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp64_peak_tflops(torch):
+    """Measured FP64 rate of this GPU: cuBLAS DGEMM 4096^3, best of 3."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        return json.load(open(path)), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+# Algorithmic units of the dominant kernels, per grid point (2D), from their
+# compulsory array traffic (each array touched once) and the FP64 operation
+# counts of the kernel code (adds, multiplies and FMAs counted as 1 and 2 flops).
+KERNEL_UNITS = {
+    "adjoint_part_a": {"bytes": 8 * (4 + 4 + 3 + 4 + 3 + 8 + 4 + 6 + 8 + 2) + 16, "flops": 620},
+    "forward_divergence_rk": {"bytes": 8 * (8 + 8 + 1 + 4 + 1 + 8 + 4 + 8 + 4) + 20, "flops": 330},
+    "forward_gradient_flux": {"bytes": 8 * (6 + 4 + 3 + 2 + 8 + 8) + 12, "flops": 290},
+    "adjoint_part_b": {"bytes": 8 * (4 + 6 + 8 + 4 + 4 + 8 + 4 + 1) + 20, "flops": 260},
+}
+
+
+def run_reference(args):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    per_step = []
+    mpts = None
+    for i in range(args.warmup + args.steps):
+        v, dt, cores = cpu_sample(args.cpu_sample_steps)
+        if i >= args.warmup:
+            per_step.append(v)
+            mpts = v
+    value = statistics.mean(per_step)
+    pts = GRID * GRID
+    ms = pts * 8 * N_STEPS / (value * 1e6) * 1e3
+    line = {
+        "impl": "reference", "metric": "FP64 Mpt-RHS/s", "value": value, "unit": "Mpt-RHS/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": "201x201", "rk4_steps": N_STEPS, "save_interval": SAVE_INTERVAL,
+                   "sample": f"{args.cpu_sample_steps} RK4 steps forward + adjoint per timed step, scaled to 960"},
+        "cpu_baseline": {"value": value, "unit": "Mpt-RHS/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"oracle (C++ restatement, OpenMP) on the 201x201 grid, {args.cpu_sample_steps} "
+                                   f"RK4 steps forward + adjoint"},
+        "e2e": {"value": value, "unit": "Mpt-RHS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    rank, world, local = rank_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from magudi_gb300 import capi
+    from magudi_gb300.solver import Solver
+
+    n_steps = args.rk_steps
+    P = problem(n_steps)
+    blk = P.blocks[0]
+    pts = blk.n_points
+    nU = P.n_unknowns
+    s = Solver(P)
+    stream = torch.cuda.ExternalStream(s.stream_handle())
+    n_entries = 4 * n_steps
+    Pact = s.actuator_points()
+    # device-resident initial state for the device-timed metric
+    q0_dev = torch.from_numpy(np.ascontiguousarray(blk.initial_state)).cuda()
+    # pinned host buffers for the end-to-end metric
+    q0_host = torch.from_numpy(np.ascontiguousarray(blk.initial_state)).pin_memory()
+    grad_host = torch.empty(n_entries * Pact, dtype=torch.float64).pin_memory()
+    flush = torch.empty(512 * 1024 * 1024 // 8, dtype=torch.float64, device="cuda")
+
+    def set_q(ptr):
+        s._check(s.L.mgd_set_field(s.h, 1, capi.FIELD_CONSERVED, capi.C.cast(ptr, capi.C.POINTER(capi.C.c_double))))
+
+    def gradient_step(ptr_q):
+        set_q(ptr_q)
+        J = s.run_forward(n_steps, SAVE_INTERVAL)
+        G = s.run_adjoint()
+        return J, G
+
+    for _ in range(args.warmup):
+        gradient_step(q0_dev.data_ptr())
+    torch.cuda.synchronize()
+    if args.profile_only:
+        for _ in range(args.steps):
+            J, G = gradient_step(q0_dev.data_ptr())
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_only": True, "rk_steps": n_steps, "J": J, "grad0": G}), flush=True)
+        return
+    s.kernel_launches(reset=True)
+    clocks = ClockSampler()
+    clocks.start()
+    times = []
+    J = G = None
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if world > 1:
+            torch.distributed.barrier()
+        e0.record(stream)
+        J, G = gradient_step(q0_dev.data_ptr())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    launches = s.kernel_launches(reset=True) // args.steps
+    # end to end through the C ABI with host buffers
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        gradient_step(q0_host.data_ptr())
+        s._check(s.L.mgd_get_gradient(s.h, capi.C.cast(grad_host.data_ptr(), capi.C.POINTER(capi.C.c_double)), n_entries))
+        torch.cuda.synchronize()
+        e2e_times.append((time.perf_counter() - t) * 1e3)
+    clk = clocks.stop()
+    ms = statistics.mean(times)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    rhs_evals = 8 * n_steps
+    value = world * pts * rhs_evals / (ms / 1e3) / 1e6
+    e2e_ms = statistics.mean(e2e_times)
+    e2e = world * pts * rhs_evals / (e2e_ms / 1e3) / 1e6
+    # per-kernel timing for the roofline (separate short loops on the same stream)
+    fwd = s.profile_stage_kernels(capi.FORWARD, 30)
+    adj = s.profile_stage_kernels(capi.ADJOINT, 30)
+    kern = {"forward_gradient_flux": fwd[0], "forward_divergence_rk": fwd[1],
+            "adjoint_part_a": adj[2], "adjoint_part_b": adj[3]}
+    dominant = max(kern, key=kern.get)
+    peaks, peak_kind = measured_peaks()
+    units = KERNEL_UNITS[dominant]
+    t_launch = kern[dominant] / 1e3
+    achieved_gbs = units["bytes"] * pts / t_launch / 1e9
+    achieved_tf = units["flops"] * pts / t_launch / 1e12
+    fp64_peak = fp64_peak_tflops(torch)
+    line = {
+        "metric": "FP64 Mpt-RHS/s", "value": value, "unit": "Mpt-RHS/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (quiescent monopole initial state generated in-process)",
+        "config": {"workload": WORKLOAD, "grid": "201x201", "rk4_steps": N_STEPS, "save_interval": SAVE_INTERVAL,
+                   "l2": "512 MB buffer written between timed steps (working set fits in L2)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "adjoint_gradient_s": ms / 1e3,
+        "J": J, "grad0": G,
+        "e2e": {"value": e2e, "unit": "Mpt-RHS/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": pts * nU * 8, "d2h_bytes_per_step": n_entries * Pact * 8 + 16},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "kernels_ms_per_launch": kern,
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved_gbs,
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
+                     "traffic": None, "peak_source": peak_kind,
+                     "fp64": {"achieved_tflops": achieved_tf, "peak_tflops": fp64_peak,
+                              "frac": achieved_tf / fp64_peak, "peak_source": "measured: cuBLAS DGEMM 4096^3"}},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, dt, cores = cpu_sample(args.cpu_sample_steps)
+        line["cpu_baseline"] = {"value": v, "unit": "Mpt-RHS/s", "cores": cores, "kind": "port",
+                                "sample": f"oracle (C++ restatement of the reference, OpenMP) on the 201x201 grid, "
+                                          f"{args.cpu_sample_steps} RK4 steps forward + adjoint ({dt:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -64,7 +64,7 @@ typedef struct {
   int n_dimensions;                  /* 2 or 3 */
   int viscous;                       /* include_viscous_terms */
   int dissipation;                   /* add_dissipation */
-  int composite_dissipation;         /* composite_dissipation (only 0 supported) */
+  int composite_dissipation;         /* composite_dissipation */
   int curvilinear;                   /* curvilinear_domain */
   int use_constant_cfl;              /* use_constant_CFL_mode */
   int enable_controller;             /* enable_controller */
@@ -134,7 +134,8 @@ int mgd_add_patch(mgd_ctx* ctx, const mgd_patch_desc* patch);
 /* State%setup acoustic sources (src/StateImpl.f90:135-150). */
 int mgd_add_acoustic_source(mgd_ctx* ctx, const mgd_acoustic_source* source);
 
-/* Region%loadData / saveData for one field of one block (src/RegionImpl.f90:1489). */
+/* Region%loadData / saveData for one field of one block (src/RegionImpl.f90:1489).
+ * The pointer may be host or device memory (unified addressing). */
 int mgd_set_field(mgd_ctx* ctx, int block, int field, const double* host);
 int mgd_get_field(mgd_ctx* ctx, int block, int field, double* host);
 
@@ -194,6 +195,18 @@ int mgd_run_adjoint(mgd_ctx* ctx, double* sensitivity);
  * writes <prefix>.gradient_<patch>.dat (ThermalActuator%updateGradient,
  * src/ThermalActuatorImpl.f90:383-443): 4*n_steps entries of nPatchPoints. */
 int mgd_get_gradient(mgd_ctx* ctx, double* host, long long n_entries);
+
+/* Measurement hook (no reference counterpart): times each kernel of one RK
+ * stage separately with CUDA events on the context stream; forward gives 2
+ * durations [gradient/flux, divergence+RK], adjoint 4 [primitives, stress,
+ * part A, part B], in milliseconds per launch averaged over reps launches.
+ * Needs a preceding mgd_run_forward; leaves the state changed. */
+int mgd_profile_stage_kernels(mgd_ctx* ctx, int mode, int reps, double* avg_ms, int* n_kernels);
+
+/* Self-test (no reference counterpart): evaluates x[i]^e on the current
+ * device with the library's table-driven power function (fast) and with
+ * CUDA's pow (ref), for checking the viscosity law's error bound. */
+int mgd_selftest_pow(const double* x, int n, double e, double* fast, double* ref);
 
 /* CUDA stream the context launches on (cudaStream_t as void*). */
 void* mgd_stream(mgd_ctx* ctx);

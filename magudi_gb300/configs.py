@@ -31,16 +31,18 @@ def monopole_2d(n=201, ny=None, dt=0.05, n_steps=960, sponge_points=20, sponge_a
                 dissipation_amount=0.01, reynolds=200.0, prandtl=0.72,
                 power_law=0.666, bulk_viscosity_ratio=0.6, save_interval=10,
                 controller_switch=False, half_width=14.0, target_center=(0.0, 10.0),
-                control_center=(0.0, 0.0), mollifier_sigma=1.0):
+                control_center=(0.0, 0.0), mollifier_sigma=1.0, composite_dissipation=True):
     """Acoustic monopole: quiescent ambient rho = 1, u = 0, p = 1/gamma; pressure
     source 0.01 sin(2 pi 0.2 t) with a Gaussian of sigma 0.5 at the origin.
     magudi's source is A cos(w t + phase) exp(-9/(2 R^2) r^2)
     (src/AcousticSourceImpl.f90:27,55-62), so sin -> phase = -pi/2 and
-    sigma = 0.5 -> R = 3 sigma = 1.5."""
+    sigma = 0.5 -> R = 3 sigma = 1.5. The dissipation is magudi's default
+    composite operator: the non-composite one at amount 0.01 is unstable at
+    dt = 0.05 on this grid."""
     ny = ny or n
     gamma = 1.4
     opts = Options(
-        n_dimensions=2, viscous=True, dissipation=True, composite_dissipation=False,
+        n_dimensions=2, viscous=True, dissipation=True, composite_dissipation=composite_dissipation,
         curvilinear=False, use_constant_cfl=False, enable_controller=True,
         enable_functional=True, controller_switch=controller_switch,
         ratio_of_specific_heats=gamma, reynolds_number=reynolds, prandtl_number=prandtl,
@@ -133,7 +135,7 @@ def taylor_green_3d(n=256, mach=0.1, reynolds=1600.0, cfl=0.5, n_steps=2000,
     q[1], q[2], q[3] = u, v, w
     q[4] = p / (gamma - 1.0) + 0.5 * (u ** 2 + v ** 2 + w ** 2)
     opts = Options(
-        n_dimensions=3, viscous=True, dissipation=True, composite_dissipation=False,
+        n_dimensions=3, viscous=True, dissipation=True, composite_dissipation=True,
         curvilinear=False, use_constant_cfl=True, cfl=cfl, enable_controller=False,
         enable_functional=False, ratio_of_specific_heats=gamma, reynolds_number=reynolds,
         prandtl_number=0.72, viscosity_power_law_exponent=power_law,

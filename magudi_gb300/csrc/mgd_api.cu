@@ -5,6 +5,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
+#include <map>
+#include <tuple>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -81,10 +84,6 @@ int mgd_create(const mgd_options* o, mgd_ctx** out) {
     g_createError = "n_dimensions must be 2 or 3";
     return 1;
   }
-  if (o->composite_dissipation) {
-    g_createError = "composite_dissipation = true is not supported (pin composite_dissipation = false)";
-    return 1;
-  }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     g_createError = "no CUDA device available";
@@ -103,6 +102,8 @@ int mgd_create(const mgd_options* o, mgd_ctx** out) {
   P.gOverGm1 = P.g / P.gm1;
   P.viscous = o->viscous;
   P.dissipation = o->dissipation;
+  P.composite = o->composite_dissipation;
+  P.dissipationAmount = o->dissipation_amount;
   P.reInv = 0.0; P.prInv = 0.0; P.powerLawExponent = 0.0; P.laFactor = 0.0;
   if (o->viscous) {
     const double re = std::max(0.0, o->reynolds_number), pr = std::max(0.0, o->prandtl_number);
@@ -315,6 +316,7 @@ int mgd_add_block(mgd_ctx* h, const mgd_block_desc* desc, const double* coordina
     v.ax[i].stride = i == 0 ? 1 : (i == 1 ? v.gs[0] : (long long)v.gs[0] * v.gs[1]);
   }
   v.curvilinear = c.opts.curvilinear;
+  b.tGrad = b.tRhs = b.tAdjA = b.tAdjB = c.nD == 2 ? makeTile(b, 32, 4, 1) : makeTile(b, 32, 2, 2);
   const long long N = v.N;
   const int nD = c.nD, nU = c.nU;
   PrimLayout L{nD};
@@ -341,6 +343,7 @@ int mgd_add_block(mgd_ctx* h, const mgd_block_desc* desc, const double* coordina
   chk(devAlloc(b, &v.dq, N * nD * nU));
   chk(devAlloc(b, &v.rcore, N * nU));
   chk(devAlloc(b, &v.ad, N * nD * (nU - 1)));
+  chk(devAlloc(b, &v.adjF, N * nU));
   chk(devAlloc(b, &sponge, N));
   chk(devAlloc(b, &mc, N));
   chk(devAlloc(b, &mt, N));
@@ -428,7 +431,7 @@ int mgd_set_field(mgd_ctx* h, int block, int field, const double* host) {
     return fail(c, "target state and mollifiers must be set before mgd_finalize_setup");
   double* d = fieldPtr(c, b, field, true);
   if (!d) return fail(c, "field is read-only or unknown");
-  CUDA_TRY(c, cudaMemcpyAsync(d, host, (size_t)b.v.N * ncompOf(c, field) * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+  CUDA_TRY(c, cudaMemcpyAsync(d, host, (size_t)b.v.N * ncompOf(c, field) * sizeof(double), cudaMemcpyDefault, c.stream));
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   return 0;
 }
@@ -448,7 +451,7 @@ int mgd_get_field(mgd_ctx* h, int block, int field, double* host) {
   }
   double* d = fieldPtr(c, b, field, false);
   if (!d) return fail(c, "unknown field");
-  CUDA_TRY(c, cudaMemcpyAsync(host, d, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  CUDA_TRY(c, cudaMemcpyAsync(host, d, n * sizeof(double), cudaMemcpyDefault, c.stream));
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   return 0;
 }
@@ -473,6 +476,80 @@ static void forExtent(const int ext[6], const int gs[3], F f) {
     for (int j = ext[2]; j <= ext[3]; ++j)
       for (int i = ext[0]; i <= ext[1]; ++i, ++pi)
         f((long long)(i - 1) + (long long)gs[0] * ((j - 1) + (long long)gs[1] * (k - 1)), pi);
+}
+
+// Tile-shape autotuner: times each stage kernel of one RK stage under
+// candidate thread-block tilings on the current state and keeps the fastest
+// per kernel. Results are cached per grid shape and physics flags for the
+// lifetime of the process.
+static RunScalars apiScalars(Context& c);
+static int setApiTime(Context& c, double time);
+
+struct TuneKey {
+  int nD, gs[3], curv, visc, diss, comp;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(nD, gs[0], gs[1], gs[2], curv, visc, diss, comp) <
+           std::tie(o.nD, o.gs[0], o.gs[1], o.gs[2], o.curv, o.visc, o.diss, o.comp);
+  }
+};
+
+static int autotune(Context& c, DevBlock& b) {
+  static std::map<TuneKey, std::array<Tile, 4>> cache;
+  TuneKey key{c.nD, {b.v.gs[0], b.v.gs[1], b.v.gs[2]}, b.v.curvilinear, c.phys.viscous, c.phys.dissipation,
+              c.phys.composite};
+  auto it = cache.find(key);
+  if (it != cache.end()) {
+    b.tGrad = it->second[0]; b.tRhs = it->second[1]; b.tAdjA = it->second[2]; b.tAdjB = it->second[3];
+    return 0;
+  }
+  std::vector<std::array<int, 3>> cands;
+  if (c.nD == 2)
+    cands = {{32, 1, 1}, {64, 1, 1}, {128, 1, 1}, {32, 2, 1}, {32, 4, 1}, {16, 4, 1}, {16, 8, 1},
+             {32, 8, 1}, {64, 2, 1}, {8, 8, 1}, {16, 2, 1}};
+  else
+    cands = {{32, 2, 2}, {32, 4, 1}, {16, 4, 2}, {16, 8, 1}, {8, 8, 2}, {32, 1, 4}, {64, 2, 1},
+             {32, 2, 1}, {16, 2, 2}, {8, 4, 4}, {32, 4, 2}};
+  RunScalars rs = apiScalars(c);
+  if (setApiTime(c, 0.0)) return 1;
+  launchPrims(c, b, b.v.q, false);
+  if (c.phys.viscous) launchGradFlux(c, b, false, false, true, &rs, 1, false);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto timeIt = [&](auto fn) {
+    fn();
+    cudaEventRecord(e0, c.stream);
+    for (int r = 0; r < 3; ++r) fn();
+    cudaEventRecord(e1, c.stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return ms;
+  };
+  Tile* slots[4] = {&b.tGrad, &b.tRhs, &b.tAdjA, &b.tAdjB};
+  const long long saved = c.launches;
+  for (int k = 0; k < 4; ++k) {
+    float best = 1e30f;
+    Tile bestTile = *slots[k];
+    for (const auto& cd : cands) {
+      *slots[k] = makeTile(b, cd[0], cd[1], cd[2]);
+      float ms;
+      switch (k) {
+        case 0: ms = timeIt([&] { launchGradFlux(c, b, true, true, false, &rs, 1, false); }); break;
+        case 1: ms = timeIt([&] { launchForwardRhs(c, b, 0, rs, true, false, false); }); break;
+        case 2: ms = timeIt([&] { launchAdjointA(c, b, rs, 1, false); }); break;
+        default: ms = timeIt([&] { launchAdjointB(c, b, 0, rs, 1, 0.0, true); }); break;
+      }
+      if (ms < best) { best = ms; bestTile = *slots[k]; }
+    }
+    *slots[k] = bestTile;
+  }
+  c.launches = saved;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (checkLaunch(c)) return 1;
+  cache[key] = {b.tGrad, b.tRhs, b.tAdjA, b.tAdjB};
+  return 0;
 }
 
 int mgd_finalize_setup(mgd_ctx* h) {
@@ -683,6 +760,8 @@ int mgd_finalize_setup(mgd_ctx* h) {
     CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   }
   c.finalized = true;
+  if (autotune(c, b)) return 1;
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   return 0;
 }
 
@@ -748,21 +827,26 @@ int mgd_compute_rhs(mgd_ctx* h, int mode, double time, double adjoint_forcing_fa
 }
 
 int mgd_update_adjoint_forcing(mgd_ctx* h, int no_adjoint_forcing) {
-  // The adjoint forcing is evaluated inside the adjoint RHS from the current
-  // forward state; this call only records whether it is switched off.
+  // Stores the cost-target adjoint forcing of the current forward state for
+  // the per-call RHS (inside runs it is evaluated in the adjoint kernel).
   Context& c = h->c;
-  c.opts.adjoint_forcing_switch = no_adjoint_forcing ? 0 : 1;
+  if (requireReady(c)) return 1;
+  DevBlock& b = c.blocks[0];
+  launchPrims(c, b, b.v.q, false);
+  launchStoreAdjointForcing(c, b, no_adjoint_forcing != 0);
+  if (checkLaunch(c)) return 1;
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   return 0;
 }
 
-static int reduceToHost(Context& c, int nSlots, std::vector<double>& out) {
+static int reduceToHost(Context& c, int nSlots, int count, std::vector<double>& out) {
   const int nb = stageBlocks(c.blocks[0]);
   if (c.stageValueCapacity < nSlots) {
     cudaFree(c.dStageValues);
     CUDA_TRY(c, cudaMalloc((void**)&c.dStageValues, (size_t)std::max(1, nSlots) * sizeof(double)));
     c.stageValueCapacity = nSlots;
   }
-  launchReducePartials(c, c.dPartials, nb, nSlots, c.dStageValues);
+  launchReducePartials(c, c.dPartials, nb, count, nSlots, c.dStageValues);
   out.resize(nSlots);
   if (nSlots > 0)
     CUDA_TRY(c, cudaMemcpyAsync(out.data(), c.dStageValues, (size_t)nSlots * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
@@ -831,7 +915,7 @@ int mgd_rk4_substep(mgd_ctx* h, int mode, double* time, double dt, int stage) {
     launchGradFlux(c, b, true, true, false, &rs, 1, false);
     launchForwardRhs(c, b, stage, rs, true, false, false);
   } else if (mode == MGD_ADJOINT) {
-    const double factor = c.opts.adjoint_forcing_switch ? (stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0)) : 0.0;
+    const double factor = stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0);
     launchPrims(c, b, b.v.q, false);
     if (c.phys.viscous) launchGradFlux(c, b, false, false, true, &rs, 1, false);
     launchAdjointA(c, b, rs, 1, false);
@@ -893,16 +977,20 @@ static int setCounters(Context& c, int step, int segBase) {
 }
 
 // Captures `body` into an executable graph on the context stream.
+// The kernels recorded during capture are counted per graph launch instead.
 template <class F>
-static int capture(Context& c, cudaGraphExec_t* exec, F body) {
+static int capture(Context& c, cudaGraphExec_t* exec, long long* nodes, F body) {
   if (*exec) {
     cudaGraphExecDestroy(*exec);
     *exec = nullptr;
   }
   cudaGraph_t g = nullptr;
+  const long long before = c.launches;
   CUDA_TRY(c, cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
   body();
   CUDA_TRY(c, cudaStreamEndCapture(c.stream, &g));
+  *nodes = c.launches - before;
+  c.launches = before;
   CUDA_TRY(c, cudaGraphInstantiate(exec, g, 0));
   cudaGraphDestroy(g);
   return 0;
@@ -966,7 +1054,7 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
   launchPrims(c, b, b.v.q, false);
   launchSnapshot(c, b, c.dSnapshots, save_interval, true);
   if (setCounters(c, 1, 0)) return 1;
-  if (capture(c, &c.gForward, [&]() {
+  if (capture(c, &c.gForward, &c.nodesForward, [&]() {
         for (int i = 1; i <= 4; ++i) {
           launchGradFlux(c, b, true, true, false, &rs, i, false);
           launchForwardRhs(c, b, i, rs, false, functional, controller);
@@ -975,15 +1063,13 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
         launchStepAdvance(c, 1);
       }))
     return 1;
-  const long long before = c.launches;
-  const long long perStep = before;  // launches recorded during capture
-  (void)perStep;
   for (int s = 0; s < n_steps; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gForward, c.stream));
+  c.launches += (long long)n_steps * c.nodesForward;
   if (checkLaunch(c)) return 1;
   double J = 0.0;
   if (functional) {
     std::vector<double> vals;
-    if (reduceToHost(c, 4 * n_steps, vals)) return 1;
+    if (reduceToHost(c, 4 * n_steps, b.tRhs.blocks(), vals)) return 1;
     for (int s = 0; s < n_steps; ++s)
       for (int i = 0; i < 4; ++i) J = J + kRkNorm[i] * dt * vals[(size_t)4 * s + i];
   } else {
@@ -1012,7 +1098,7 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   // adjoint initial condition at the final state (its primitives are current)
   launchPrims(c, b, b.v.q, false);
   launchAdjointInitial(c, b, c.opts.adjoint_forcing_switch ? -dt / 6.0 : 0.0);
-  if (capture(c, &c.gRecompute, [&]() {
+  if (capture(c, &c.gRecompute, &c.nodesRecompute, [&]() {
         for (int i = 1; i <= 4; ++i) {
           launchGradFlux(c, b, true, true, false, &rs, i, true);
           launchForwardRhs(c, b, i, rs, false, false, controller);
@@ -1020,7 +1106,7 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
         launchStepAdvance(c, 1);
       }))
     return 1;
-  if (capture(c, &c.gAdjoint, [&]() {
+  if (capture(c, &c.gAdjoint, &c.nodesAdjoint, [&]() {
         for (int i = 4; i >= 1; --i) {
           launchPrims(c, b, nullptr, true, &rs, i);
           if (c.phys.viscous) launchGradFlux(c, b, false, false, true, &rs, i, false);
@@ -1041,10 +1127,11 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
     for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gRecompute, c.stream));
     if (setCounters(c, end, L)) return 1;
     for (int s = end; s >= L + 1; --s) CUDA_TRY(c, cudaGraphLaunch(c.gAdjoint, c.stream));
+    c.launches += (long long)(end - L) * (c.nodesRecompute + c.nodesAdjoint);
   }
   if (checkLaunch(c)) return 1;
   std::vector<double> vals;
-  if (reduceToHost(c, 4 * T, vals)) return 1;
+  if (reduceToHost(c, 4 * T, b.tAdjA.blocks(), vals)) return 1;
   double sum = 0.0;
   for (int n = T; n >= 1; --n)
     for (int i = 4; i >= 1; --i) {
@@ -1065,3 +1152,74 @@ int mgd_get_gradient(mgd_ctx* h, double* host, long long n_entries) {
   return 0;
 }
 
+
+// Times each kernel of one RK stage separately with CUDA events on the
+// context stream: forward -> [K2 gradient/flux, K3 divergence+RK];
+// adjoint -> [primitives, stress, part A, part B]. avg_ms receives the mean
+// duration per launch over `reps` launches of each kernel. The state is
+// left changed (the RK updates run); use it on a scratch context state.
+int mgd_profile_stage_kernels(mgd_ctx* h, int mode, int reps, double* avg_ms, int* n_kernels) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  if (c.runSteps < 1) return fail(c, "mgd_profile_stage_kernels needs a preceding mgd_run_forward");
+  DevBlock& b = c.blocks[0];
+  RunScalars rs = runScalars(c);
+  const long long needStage = 4LL * std::max(1, c.saveInterval) * c.nU * b.v.N;
+  if (c.stageBufCapacity < needStage) {
+    cudaFree(c.dStageBuf);
+    CUDA_TRY(c, cudaMalloc((void**)&c.dStageBuf, needStage * sizeof(double)));
+    c.stageBufCapacity = needStage;
+    rs.stageBuf = c.dStageBuf;
+  }
+  if (setCounters(c, 1, 0)) return 1;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
+  auto timeIt = [&](auto fn) {
+    fn();  // warm
+    cudaEventRecord(e0, c.stream);
+    for (int r = 0; r < reps; ++r) fn();
+    cudaEventRecord(e1, c.stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return (double)ms / reps;
+  };
+  launchPrims(c, b, b.v.q, false);
+  if (mode == MGD_FORWARD) {
+    avg_ms[0] = timeIt([&] { launchGradFlux(c, b, true, true, false, &rs, 2, false); });
+    avg_ms[1] = timeIt([&] { launchForwardRhs(c, b, 2, rs, false, c.opts.enable_functional != 0, controller); });
+    *n_kernels = 2;
+  } else {
+    // the stage slot (step 1, stage 1) of the stage buffer holds a valid state
+    CUDA_TRY(c, cudaMemcpyAsync(c.dStageBuf, b.v.q, (size_t)c.nU * b.v.N * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    avg_ms[0] = timeIt([&] { launchPrims(c, b, nullptr, true, &rs, 1); });
+    avg_ms[1] = c.phys.viscous ? timeIt([&] { launchGradFlux(c, b, false, false, true, &rs, 1, false); }) : 0.0;
+    avg_ms[2] = timeIt([&] { launchAdjointA(c, b, rs, 1, true); });
+    avg_ms[3] = timeIt([&] { launchAdjointB(c, b, 3, rs, 3, 0.0, false); });
+    *n_kernels = 4;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (checkLaunch(c)) return 1;
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  return 0;
+}
+
+// Self-test of the table-driven power function used by the viscosity law:
+// evaluates x[i]^e with it (fast) and with CUDA's pow (ref) on the current device.
+int mgd_selftest_pow(const double* x, int n, double e, double* fast, double* ref) {
+  if (n <= 0) return 0;
+  double *dx = nullptr, *df = nullptr, *dr = nullptr;
+  if (cudaMalloc((void**)&dx, n * sizeof(double)) != cudaSuccess) return 1;
+  cudaMalloc((void**)&df, n * sizeof(double));
+  cudaMalloc((void**)&dr, n * sizeof(double));
+  cudaMemcpy(dx, x, n * sizeof(double), cudaMemcpyHostToDevice);
+  launchPowSelfTest(dx, n, e, df, dr);
+  cudaMemcpy(fast, df, n * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaMemcpy(ref, dr, n * sizeof(double), cudaMemcpyDeviceToHost);
+  const cudaError_t err = cudaGetLastError();
+  cudaFree(dx); cudaFree(df); cudaFree(dr);
+  return err == cudaSuccess ? 0 : 1;
+}

@@ -12,7 +12,7 @@
 
 namespace mgd {
 
-enum OpId { OP_D1 = 0, OP_D1ADJ = 1, OP_DISS = 2, OP_DISST = 3, OP_COUNT = 4 };
+enum OpId { OP_D1 = 0, OP_D1ADJ = 1, OP_DISS = 2, OP_DISST = 3, OP_DCOMP = 4, OP_COUNT = 5 };
 
 // Compile-time shape of each operator's boundary block.
 template <int OP> struct OpShape;
@@ -20,6 +20,7 @@ template <> struct OpShape<OP_D1> { static constexpr int depth = 8, width = 12, 
 template <> struct OpShape<OP_D1ADJ> { static constexpr int depth = 12, width = 16, half = 4; static constexpr bool skew = true; };
 template <> struct OpShape<OP_DISS> { static constexpr int depth = 2, width = 5, half = 2; static constexpr bool skew = false; };
 template <> struct OpShape<OP_DISST> { static constexpr int depth = 8, width = 10, half = 2; static constexpr bool skew = false; };
+template <> struct OpShape<OP_DCOMP> { static constexpr int depth = 8, width = 12, half = 4; static constexpr bool skew = false; };
 
 struct OpTables {
   double interior[OP_COUNT][9];         // offsets -half..half
@@ -56,9 +57,10 @@ __device__ __forceinline__ double applyOp(const double* __restrict__ line, int i
   const long long st = ax.stride;
   if (ax.per == 0) {
     if (i < S::depth) {
+      // boundary closure rows are rare: keep them compact (few registers)
       const double* __restrict__ row = &c_ops.left[OP][i * S::width];
       double s = row[0] * __ldg(line);
-#pragma unroll
+#pragma unroll 1
       for (int k = 1; k < S::width; ++k) s += row[k] * __ldg(line + k * st);
       return s;
     }
@@ -68,7 +70,7 @@ __device__ __forceinline__ double applyOp(const double* __restrict__ line, int i
       const double* __restrict__ end = line + (long long)(ax.n - S::width) * st;
       // right block = reflection of the left block, negated for skew operators
       double s = row[S::width - 1] * __ldg(end);
-#pragma unroll
+#pragma unroll 1
       for (int k = 1; k < S::width; ++k) s += row[S::width - 1 - k] * __ldg(end + k * st);
       return S::skew ? -s : s;
     }
@@ -98,6 +100,67 @@ __device__ __forceinline__ double applyOp(const double* __restrict__ line, int i
     for (int j = 2; j <= S::half; ++j) s += cin[S::half + j] * (at(j) + at(-j));
     return s + cin[S::half] * at(0);
   }
+}
+
+// ---------------------------------------------------------------------------
+// x^n for x > 0 in FP64 with few FP64 operations, after P. T. P. Tang's
+// table-driven logarithm and exponential (ACM TOMS 15(2), 1989; 16(4), 1990):
+//   log x = e ln2 + log(F) + log1p(m/F - 1), F from a 128-entry table
+//   exp y = 2^(k/64) exp(r), |r| <= ln2/128, 2^(j/64) from a 64-entry table.
+// Exponent and mantissa are split with integer operations, which do not
+// occupy the FP64 pipe. Non-positive or non-finite x falls back to pow().
+// ---------------------------------------------------------------------------
+struct PowTables {
+  double invF[128];   // G_j = 1 / F_j rounded, F_j = 1 + (j + 1/2)/128
+  double logFhi[128]; // -log G_j, high part
+  double logFlo[128]; // -log G_j, low part
+  double exp2j[64];   // 2^(j/64)
+};
+
+__device__ __forceinline__ double fastPowPositive(double x, double n, const PowTables* __restrict__ tab) {
+  const long long bits = __double_as_longlong(x);
+  const int be = (int)((bits >> 52) & 0x7FF);
+  if (!(x > 0.0) || be == 0 || be == 0x7FF) return pow(x, n);
+  const int e = be - 1023;
+  const int j = (int)((bits >> 45) & 0x7F);
+  const double m = __longlong_as_double((bits & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
+  const double t = fma(m, __ldg(&tab->invF[j]), -1.0);  // |t| < 2^-8
+  // log1p(t) - t = t^2 (-1/2 + t/3 - t^2/4 + ... - t^6/8)
+  double q = -1.0 / 8.0;
+  q = fma(q, t, 1.0 / 7.0);
+  q = fma(q, t, -1.0 / 6.0);
+  q = fma(q, t, 1.0 / 5.0);
+  q = fma(q, t, -1.0 / 4.0);
+  q = fma(q, t, 1.0 / 3.0);
+  q = fma(q, t, -0.5);
+  const double t2 = t * t;
+  const double ln2hi = 6.93147180369123816490e-01, ln2lo = 1.90821492927058770002e-10;
+  const double ed = (double)e;
+  const double lo = fma(t2, q, fma(ed, ln2lo, __ldg(&tab->logFlo[j])));
+  const double hi = fma(ed, ln2hi, __ldg(&tab->logFhi[j]));
+  const double logx = hi + (t + lo);
+  const double y = n * logx;
+  // exp(y): y = k ln2/64 + r
+  const double inv = 92.332482616893656877;  // 64 / ln 2
+  const double shifter = 6755399441055744.0;   // 1.5 * 2^52: rounds to an integer
+  const double kd_s = fma(y, inv, shifter);
+  const long long kbits = __double_as_longlong(kd_s);
+  const double kd = kd_s - shifter;
+  const double l64hi = 0.01083042469326756, l64lo = 2.9815858269852933e-12;  // ln2/64 = hi + lo, hi*k exact
+  double r = fma(-kd, l64hi, y);
+  r = fma(-kd, l64lo, r);
+  double pe = 1.0 / 720.0;
+  pe = fma(pe, r, 1.0 / 120.0);
+  pe = fma(pe, r, 1.0 / 24.0);
+  pe = fma(pe, r, 1.0 / 6.0);
+  pe = fma(pe, r, 0.5);
+  pe = fma(pe * r, r, r);                      // exp(r) - 1
+  const int k = (int)(kbits & 0xFFFFFFFFLL);
+  const int jj = k & 63, kk = k >> 6;
+  const double tj = __ldg(&tab->exp2j[jj]);
+  const double res = fma(tj, pe, tj);
+  // scale by 2^kk through the exponent field (result stays normal here)
+  return __longlong_as_double(__double_as_longlong(res) + ((long long)kk << 52));
 }
 
 // ---------------------------------------------------------------------------

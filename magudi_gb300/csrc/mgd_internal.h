@@ -61,9 +61,10 @@ struct BlockView {
   double* tau;
   double* hf;
   double* fhat;   // nD x nU
-  double* dq;     // nD x nU
+  double* dq;     // nD x nU (composite dissipation: nU, already scaled)
   double* rcore;  // nU
   double* ad;     // nD x (nU-1)
+  double* adjF;   // nU: stored cost-target adjoint forcing (per-call API path)
   // patches
   const double* sponge;   // summed sponge strength
   const double* mc;       // control mollifier (normalized)
@@ -79,10 +80,20 @@ struct BlockView {
   FarFieldEntries ff;
 };
 
+// Thread-block tiling of a block's points: blocks of t[0] x t[1] x t[2]
+// threads cover n[0] x n[1] x n[2] tiles of the grid.
+struct Tile {
+  int t[3];
+  int n[3];
+  int threads() const { return t[0] * t[1] * t[2]; }
+  int blocks() const { return n[0] * n[1] * n[2]; }
+};
+
 // Constants of the physics and of the run.
 struct Physics {
   double g, gm1, gOverGm1, reInv, prInv, powerLawExponent, laFactor;
-  int viscous, dissipation;
+  double dissipationAmount;
+  int viscous, dissipation, composite;
 };
 
 struct RunScalars {
@@ -105,6 +116,8 @@ struct RunScalars {
 struct DevBlock {
   mgd_block_desc desc;
   BlockView v;
+  // tile shapes of the stage kernels, chosen by the autotuner
+  Tile tGrad{}, tRhs{}, tAdjA{}, tAdjB{};
   std::vector<void*> allocations;
   int nStagePartialBlocks = 0;
   // host copies kept for setup
@@ -151,6 +164,7 @@ struct Context {
   double* dStageBuf = nullptr;
   long long stageBufCapacity = 0;
   cudaGraphExec_t gForward = nullptr, gRecompute = nullptr, gAdjoint = nullptr;
+  long long nodesForward = 0, nodesRecompute = 0, nodesAdjoint = 0;
 };
 
 // ----- launchers (mgd_kernels.cu) -----
@@ -170,13 +184,19 @@ void launchAdjointA(Context& c, DevBlock& b, const RunScalars& rs, int stage, bo
 void launchAdjointB(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage,
                     double apiFactor, bool api);
 void launchAdjointInitial(Context& c, DevBlock& b, double factor);
+// Functional%updateAdjointForcing for the per-call API: stores the forcing of
+// the current state (or zeros) in adjF.
+void launchStoreAdjointForcing(Context& c, DevBlock& b, bool zero);
 void launchSnapshot(Context& c, DevBlock& b, double* snapshots, int saveInterval, bool initial);
 void launchStepAdvance(Context& c, int delta);
-void launchReducePartials(Context& c, const double* partials, int nBlocks, int nSlots, double* out);
+void launchReducePartials(Context& c, const double* partials, int stride, int count, int nSlots, double* out);
 void launchCoordinateDerivative(Context& c, DevBlock& b, int dir, double* out);
 void launchApplyD1(Context& c, DevBlock& b, int dir, const double* in, double* out, int ncomp);
 void launchFarFieldMatricesWith(Context& c, DevBlock& b, const double* sigInv, const int* signedNormal);
 void launchFarFieldTargetVisc(Context& c, DevBlock& b);
 int stageBlocks(const DevBlock& b);
+void launchPowSelfTest(const double* x, int n, double e, double* fast, double* ref);
+Tile makeTile(const DevBlock& b, int tx, int ty, int tz);
+int maxTileBlocks(const DevBlock& b);
 
 }  // namespace mgd

@@ -9,6 +9,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "mgd_internal.h"
@@ -18,12 +20,41 @@ namespace mgd {
 
 
 __constant__ double c_norm[8];
+__device__ PowTables g_powTables;
 
-constexpr int kBlock = 128;
+static void uploadPowTables() {
+  PowTables t;
+  for (int j = 0; j < 128; ++j) {
+    const long double F = 1.0L + (j + 0.5L) / 128.0L;
+    t.invF[j] = (double)(1.0L / F);
+    const long double L = -logl((long double)t.invF[j]);
+    t.logFhi[j] = (double)L;
+    t.logFlo[j] = (double)(L - (long double)t.logFhi[j]);
+  }
+  for (int j = 0; j < 64; ++j) t.exp2j[j] = (double)exp2l(j / 64.0L);
+  cudaMemcpyToSymbol(g_powTables, &t, sizeof t);
+}
+
+constexpr int kBlock = 128;      // pointwise kernels
+constexpr int kMaxTile = 256;    // largest stage-kernel tile
 
 static inline int gridFor(long long n) { return (int)((n + kBlock - 1) / kBlock); }
 
-int stageBlocks(const DevBlock& b) { return gridFor(b.v.N); }
+Tile makeTile(const DevBlock& b, int tx, int ty, int tz) {
+  Tile t;
+  t.t[0] = tx; t.t[1] = b.v.nD >= 2 ? ty : 1; t.t[2] = b.v.nD >= 3 ? tz : 1;
+  for (int d = 0; d < 3; ++d) t.n[d] = (b.v.gs[d] + t.t[d] - 1) / t.t[d];
+  return t;
+}
+
+// Partial sums are laid out per stage slot with room for the largest tiling.
+int maxTileBlocks(const DevBlock& b) {
+  int m = 0;
+  for (const Tile* t : {&b.tGrad, &b.tRhs, &b.tAdjA, &b.tAdjB}) m = std::max(m, t->blocks());
+  return std::max(m, 1);
+}
+
+int stageBlocks(const DevBlock& b) { return maxTileBlocks(b); }
 
 void uploadOperatorTables() {
   static bool done[64] = {false};
@@ -36,13 +67,15 @@ void uploadOperatorTables() {
   const HostOp ad = makeAdjoint(d1);
   const HostOp di = makeDissipation48();
   const HostOp dt = makeDissipationTransposeNormInverse48(d1);
-  const HostOp* ops[OP_COUNT] = {&d1, &ad, &di, &dt};
+  const HostOp dc = makeCompositeDissipation48();
+  const HostOp* ops[OP_COUNT] = {&d1, &ad, &di, &dt, &dc};
   for (int o = 0; o < OP_COUNT; ++o) {
     for (size_t j = 0; j < ops[o]->interior.size(); ++j) t.interior[o][j] = ops[o]->interior[j];
     for (size_t j = 0; j < ops[o]->left.size(); ++j) t.left[o][j] = ops[o]->left[j];
   }
   cudaMemcpyToSymbol(c_ops, &t, sizeof t);
   cudaMemcpyToSymbol(c_norm, d1.norm.data(), 8 * sizeof(double));
+  uploadPowTables();
   if (dev < 64) done[dev] = true;
 }
 
@@ -64,6 +97,20 @@ __device__ __forceinline__ PointIndex pointIndex(const BlockView& B, long long p
   return r;
 }
 
+// Grid point of this thread under tiling T; false when the tile overhangs the grid.
+__device__ __forceinline__ bool locate(const BlockView& B, const Tile& T, long long& p, PointIndex& r) {
+  const int t = threadIdx.x, b = blockIdx.x;
+  const int lx = t % T.t[0], ly = (t / T.t[0]) % T.t[1], lz = t / (T.t[0] * T.t[1]);
+  const int bx = b % T.n[0], by = (b / T.n[0]) % T.n[1], bz = b / (T.n[0] * T.n[1]);
+  r.idx[0] = bx * T.t[0] + lx;
+  r.idx[1] = by * T.t[1] + ly;
+  r.idx[2] = bz * T.t[2] + lz;
+  if (r.idx[0] >= B.gs[0] || r.idx[1] >= B.gs[1] || r.idx[2] >= B.gs[2]) return false;
+  p = r.idx[0] + (long long)B.gs[0] * (r.idx[1] + (long long)B.gs[1] * r.idx[2]);
+  for (int d = 0; d < 3; ++d) r.base[d] = p - (long long)r.idx[d] * B.ax[d].stride;
+  return true;
+}
+
 // Primitive variables of one state (computeDependentVariables +
 // computeTransportVariables, src/CNSHelperImpl.f90:3-177).
 template <int ND>
@@ -81,7 +128,7 @@ __device__ __forceinline__ void primitives(const double* q, const Physics& P, do
   out[1 + ND] = pr;
   out[2 + ND] = T;
   double mu = P.reInv;
-  if (P.powerLawExponent > 0.0) mu = pow(P.gm1 * T, P.powerLawExponent) * P.reInv;
+  if (P.powerLawExponent > 0.0) mu = fastPowPositive(P.gm1 * T, P.powerLawExponent, &g_powTables) * P.reInv;
   out[3 + ND] = mu;
   out[4 + ND] = P.laFactor * mu;
   out[5 + ND] = mu * P.prInv;
@@ -89,14 +136,14 @@ __device__ __forceinline__ void primitives(const double* q, const Physics& P, do
 
 // Deterministic block sum of one value per thread; thread 0 gets the result.
 __device__ __forceinline__ double blockSum(double v) {
-  __shared__ double warpSums[kBlock / 32];
+  __shared__ double warpSums[32];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (lane == 0) warpSums[w] = v;
   __syncthreads();
   double s = 0.0;
   if (threadIdx.x == 0)
-    for (int i = 0; i < kBlock / 32; ++i) s += warpSums[i];
+    for (int i = 0; i < (int)((blockDim.x + 31) / 32); ++i) s += warpSums[i];
   return s;
 }
 
@@ -131,13 +178,13 @@ __global__ void __launch_bounds__(kBlock) kPrims(BlockView B, Physics P, const d
 enum { GF_FLUX = 1, GF_DISS = 2, GF_STRESS = 4, GF_STORE = 8 };
 
 template <int ND, bool CURV, bool VISC>
-__global__ void __launch_bounds__(kBlock) kGradFlux(BlockView B, Physics P, RunScalars rs, int flags,
-                                                    int stage) {
-  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
-  if (p >= B.N) return;
+__global__ void __launch_bounds__(kMaxTile) kGradFlux(BlockView B, Physics P, RunScalars rs, int flags,
+                                                      int stage, Tile T) {
+  long long p;
+  PointIndex I;
+  if (!locate(B, T, p, I)) return;
   constexpr int nU = ND + 2, E = ND + 1;
   const long long N = B.N;
-  const PointIndex I = pointIndex(B, p);
   const PrimLayout L{ND};
   double q[nU];
   for (int c = 0; c < nU; ++c) q[c] = B.q[p + N * c];
@@ -240,10 +287,19 @@ __global__ void __launch_bounds__(kBlock) kGradFlux(BlockView B, Physics P, RunS
       }
   }
   if (flags & GF_DISS) {
-    for (int d = 0; d < ND; ++d) {
-      const double a = B.arcA[p + N * d];
-      for (int c = 0; c < nU; ++c)
-        B.dq[p + N * (d * nU + c)] = a * applyOp<OP_DISS>(B.q + N * c + I.base[d], I.idx[d], B.ax[d]);
+    if (P.composite) {
+      // addDissipation composite path: amount * sum_i D_comp,i q
+      for (int c = 0; c < nU; ++c) {
+        double s = applyOp<OP_DCOMP>(B.q + N * c + I.base[0], I.idx[0], B.ax[0]);
+        for (int d = 1; d < ND; ++d) s += applyOp<OP_DCOMP>(B.q + N * c + I.base[d], I.idx[d], B.ax[d]);
+        B.dq[p + N * c] = P.dissipationAmount * s;
+      }
+    } else {
+      for (int d = 0; d < ND; ++d) {
+        const double a = B.arcA[p + N * d];
+        for (int c = 0; c < nU; ++c)
+          B.dq[p + N * (d * nU + c)] = a * applyOp<OP_DISS>(B.q + N * c + I.base[d], I.idx[d], B.ax[d]);
+      }
     }
   }
 }
@@ -255,25 +311,30 @@ __global__ void __launch_bounds__(kBlock) kGradFlux(BlockView B, Physics P, RunS
 // primitive variables of the new state and the functional's partial sums.
 // ---------------------------------------------------------------------------
 template <int ND>
-__global__ void __launch_bounds__(kBlock) kForwardRhs(BlockView B, Physics P, RunScalars rs, int rkStage,
-                                                      int stage, int accumulate, int controller) {
-  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
-  const bool active = p < B.N;
+__global__ void __launch_bounds__(kMaxTile) kForwardRhs(BlockView B, Physics P, RunScalars rs, int rkStage,
+                                                        int stage, int accumulate, int controller, Tile T) {
+  long long p = 0;
+  PointIndex I;
+  const bool active = locate(B, T, p, I);
   constexpr int nU = ND + 2, E = ND + 1;
   const long long N = B.N;
   double fval = 0.0;
   if (active) {
-    const PointIndex I = pointIndex(B, p);
     double r[nU];
     for (int c = 0; c < nU; ++c) {
       double s = applyOp<OP_D1>(B.fhat + N * c + I.base[0], I.idx[0], B.ax[0]);
       for (int i = 1; i < ND; ++i) s += applyOp<OP_D1>(B.fhat + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
       r[c] = -s;
     }
-    if (P.dissipation)
-      for (int c = 0; c < nU; ++c)
-        for (int i = 0; i < ND; ++i)
-          r[c] += applyOp<OP_DISST>(B.dq + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
+    if (P.dissipation) {
+      if (P.composite) {
+        for (int c = 0; c < nU; ++c) r[c] += B.dq[p + N * c];
+      } else {
+        for (int c = 0; c < nU; ++c)
+          for (int i = 0; i < ND; ++i)
+            r[c] += applyOp<OP_DISST>(B.dq + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
+      }
+    }
     const double jac = B.jac[p];
     for (int c = 0; c < nU; ++c) r[c] = r[c] * jac;
     double q[nU];
@@ -374,16 +435,16 @@ __global__ void __launch_bounds__(kBlock) kForwardRhs(BlockView B, Physics P, Ru
 // (src/ThermalActuatorImpl.f90:83-159, 383-443).
 // ---------------------------------------------------------------------------
 template <int ND, bool VISC>
-__global__ void __launch_bounds__(kBlock) kAdjointA(BlockView B, Physics P, RunScalars rs, int stage,
-                                                    int record) {
-  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
-  const bool active = p < B.N;
+__global__ void __launch_bounds__(kMaxTile) kAdjointA(BlockView B, Physics P, RunScalars rs, int stage,
+                                                      int record, Tile T) {
+  long long p = 0;
+  PointIndex I;
+  const bool active = locate(B, T, p, I);
   constexpr int nU = ND + 2, E = ND + 1, nV = ND + 1;
   const long long N = B.N;
   const PrimLayout L{ND};
   double sval = 0.0;
   if (active) {
-    const PointIndex I = pointIndex(B, p);
     double w[ND][nU];
     for (int i = 0; i < ND; ++i)
       for (int c = 0; c < nU; ++c) w[i][c] = applyOp<OP_D1ADJ>(B.lam + N * c + I.base[i], I.idx[i], B.ax[i]);
@@ -428,12 +489,21 @@ __global__ void __launch_bounds__(kBlock) kAdjointA(BlockView B, Physics P, RunS
       for (int j = 0; j < ND; ++j)
         for (int c = 0; c < nV; ++c) B.ad[p + N * (j * nV + c)] = ad[j][c];
     }
-    if (P.dissipation)
-      for (int d = 0; d < ND; ++d) {
-        const double a = -B.arcA[p + N * d];
-        for (int c = 0; c < nU; ++c)
-          B.dq[p + N * (d * nU + c)] = a * applyOp<OP_DISS>(B.lam + N * c + I.base[d], I.idx[d], B.ax[d]);
+    if (P.dissipation) {
+      if (P.composite) {
+        for (int c = 0; c < nU; ++c) {
+          double s = applyOp<OP_DCOMP>(B.lam + N * c + I.base[0], I.idx[0], B.ax[0]);
+          for (int d = 1; d < ND; ++d) s += applyOp<OP_DCOMP>(B.lam + N * c + I.base[d], I.idx[d], B.ax[d]);
+          B.dq[p + N * c] = -P.dissipationAmount * s;
+        }
+      } else {
+        for (int d = 0; d < ND; ++d) {
+          const double a = -B.arcA[p + N * d];
+          for (int c = 0; c < nU; ++c)
+            B.dq[p + N * (d * nU + c)] = a * applyOp<OP_DISS>(B.lam + N * c + I.base[d], I.idx[d], B.ax[d]);
+        }
       }
+    }
     if (record) {
       const long long entry = (long long)(rs.nSteps - *rs.step) * 4 + (4 - stage);
       const double g = lp[E] * B.mc[p];
@@ -462,14 +532,14 @@ __global__ void __launch_bounds__(kBlock) kAdjointA(BlockView B, Physics P, RunS
 // (src/RK4IntegratorImpl.f90:203-266).
 // ---------------------------------------------------------------------------
 template <int ND, bool VISC>
-__global__ void __launch_bounds__(kBlock) kAdjointB(BlockView B, Physics P, RunScalars rs, int rkStage,
-                                                    int stage, double apiFactor, int api) {
-  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
-  if (p >= B.N) return;
+__global__ void __launch_bounds__(kMaxTile) kAdjointB(BlockView B, Physics P, RunScalars rs, int rkStage,
+                                                      int stage, double apiFactor, int api, Tile T) {
+  long long p;
+  PointIndex I;
+  if (!locate(B, T, p, I)) return;
   constexpr int nU = ND + 2, E = ND + 1, nV = ND + 1;
   const long long N = B.N;
   const PrimLayout L{ND};
-  const PointIndex I = pointIndex(B, p);
   double r[nU];
   for (int c = 0; c < nU; ++c) r[c] = B.rcore[p + N * c];
   double u[ND];
@@ -491,10 +561,15 @@ __global__ void __launch_bounds__(kBlock) kAdjointB(BlockView B, Physics P, RunS
     for (int d = 1; d < ND; ++d) su += u[d] * x[d];
     r[0] += v * B.q[p + N * E] * xE + su;
   }
-  if (P.dissipation)
-    for (int c = 0; c < nU; ++c)
-      for (int i = 0; i < ND; ++i)
-        r[c] += applyOp<OP_DISST>(B.dq + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
+  if (P.dissipation) {
+    if (P.composite) {
+      for (int c = 0; c < nU; ++c) r[c] += B.dq[p + N * c];
+    } else {
+      for (int c = 0; c < nU; ++c)
+        for (int i = 0; i < ND; ++i)
+          r[c] += applyOp<OP_DISST>(B.dq + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
+    }
+  }
   const double jac = B.jac[p];
   for (int c = 0; c < nU; ++c) r[c] = r[c] * jac;
   double lp[nU];
@@ -524,11 +599,13 @@ __global__ void __launch_bounds__(kBlock) kAdjointB(BlockView B, Physics P, RunS
   if (S != 0.0)
     for (int c = 0; c < nU; ++c) r[c] += S * lp[c];
   const double cnt = B.tgtCount[p];
-  if (cnt != 0.0) {
+  if (api) {
+    // per-call path: the forcing stored by the last updateAdjointForcing
+    if (cnt != 0.0 && apiFactor != 0.0)
+      for (int c = 0; c < nU; ++c) r[c] += apiFactor * B.adjF[p + N * c];
+  } else if (cnt != 0.0) {
     double factor;
-    if (api) {
-      factor = apiFactor;
-    } else {
+    {
       const bool finalStage = (*rs.step == 1 && stage == 1);
       factor = (!rs.adjointForcingSwitch || finalStage) ? 0.0
                : (stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0));
@@ -601,6 +678,31 @@ __global__ void __launch_bounds__(kBlock) kAdjointInitial(BlockView B, Physics P
   for (int c = 0; c < nU; ++c) B.lam[p + N * c] = r[c];
 }
 
+template <int ND>
+__global__ void __launch_bounds__(kBlock) kStoreAdjointForcing(BlockView B, Physics P, int zero) {
+  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
+  if (p >= B.N) return;
+  constexpr int nU = ND + 2, E = ND + 1;
+  const long long N = B.N;
+  const PrimLayout L{ND};
+  double r[nU];
+  for (int c = 0; c < nU; ++c) r[c] = 0.0;
+  const double cnt = B.tgtCount[p];
+  if (!zero && cnt != 0.0) {
+    double u[ND];
+    for (int d = 0; d < ND; ++d) u[d] = B.prim[p + N * L.u(d)];
+    const double F = -2.0 * B.mt[p] * P.gm1 * (B.prim[p + N * L.p()] - B.meanP[p]);
+    double u2 = u[0] * u[0];
+    for (int d = 1; d < ND; ++d) u2 += u[d] * u[d];
+    for (int k = 0; k < (int)cnt; ++k) {
+      r[E] += F;
+      for (int d = 0; d < ND; ++d) r[1 + d] += -u[d] * F;
+      r[0] += 0.5 * u2 * F;
+    }
+  }
+  for (int c = 0; c < nU; ++c) B.adjF[p + N * c] = r[c];
+}
+
 // Snapshot of the conserved variables after a completed forward step.
 __global__ void kSnapshot(double* __restrict__ snap, const double* __restrict__ q, long long n,
                           const int* __restrict__ step, int saveInterval, int initial) {
@@ -614,13 +716,14 @@ __global__ void kStepAdvance(int* counters, int delta) {
   if (threadIdx.x == 0 && blockIdx.x == 0) counters[0] += delta;
 }
 
-// out[s] = sum over blocks of partials[s * nBlocks + b], fixed order.
-__global__ void kReducePartials(const double* __restrict__ partials, int nBlocks, int nSlots,
+// out[s] = sum over the first `count` block partials of slot s (row stride
+// `stride`), in a fixed order.
+__global__ void kReducePartials(const double* __restrict__ partials, int stride, int count, int nSlots,
                                 double* __restrict__ out) {
   const int s = blockIdx.x;
   if (s >= nSlots) return;
   double v = 0.0;
-  for (int b = threadIdx.x; b < nBlocks; b += kBlock) v += partials[(long long)s * nBlocks + b];
+  for (int b = threadIdx.x; b < count; b += blockDim.x) v += partials[(long long)s * stride + b];
   const double t = blockSum(v);
   if (threadIdx.x == 0) out[s] = t;
 }
@@ -716,6 +819,19 @@ __global__ void kFarFieldTargetVisc(BlockView B) {
   }
 }
 
+__global__ void kPowSelfTest(const double* __restrict__ x, int n, double e, double* __restrict__ fast,
+                             double* __restrict__ ref) {
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  if (i >= n) return;
+  fast[i] = fastPowPositive(x[i], e, &g_powTables);
+  ref[i] = pow(x[i], e);
+}
+
+void launchPowSelfTest(const double* x, int n, double e, double* fast, double* ref) {
+  uploadOperatorTables();
+  kPowSelfTest<<<(n + kBlock - 1) / kBlock, kBlock>>>(x, n, e, fast, ref);
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
@@ -735,10 +851,10 @@ void launchGradFlux(Context& c, DevBlock& b, bool writeFlux, bool writeDiss, boo
               (writeStress ? GF_STRESS : 0) | (storeStage ? GF_STORE : 0);
   RunScalars r{};
   if (rs) r = *rs;
-  const int G = gridFor(b.v.N);
+  const Tile T = b.tGrad;
   const bool curv = b.v.curvilinear != 0, visc = c.phys.viscous != 0;
   MGD_LAUNCH(c);
-#define GF(ND, CU, VI) kGradFlux<ND, CU, VI><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, r, flags, stage)
+#define GF(ND, CU, VI) kGradFlux<ND, CU, VI><<<T.blocks(), T.threads(), 0, c.stream>>>(b.v, c.phys, r, flags, stage, T)
   if (c.nD == 2) {
     if (curv) { if (visc) GF(2, true, true); else GF(2, true, false); }
     else { if (visc) GF(2, false, true); else GF(2, false, false); }
@@ -752,35 +868,38 @@ void launchGradFlux(Context& c, DevBlock& b, bool writeFlux, bool writeDiss, boo
 void launchForwardRhs(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bool api,
                       bool accumulate, bool controller) {
   const int stage = api ? 1 : rkStage;
+  const Tile T = b.tRhs;
   MGD_LAUNCH(c);
   if (c.nD == 2)
-    kForwardRhs<2><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, accumulate, controller);
+    kForwardRhs<2><<<T.blocks(), T.threads(), 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, accumulate, controller, T);
   else
-    kForwardRhs<3><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, accumulate, controller);
+    kForwardRhs<3><<<T.blocks(), T.threads(), 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, accumulate, controller, T);
 }
 
 void launchAdjointA(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool record) {
-  const int G = gridFor(b.v.N);
+  const Tile T = b.tAdjA;
+  const int G = T.blocks(), W = T.threads();
   MGD_LAUNCH(c);
   if (c.nD == 2) {
-    if (c.phys.viscous) kAdjointA<2, true><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, stage, record);
-    else kAdjointA<2, false><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, stage, record);
+    if (c.phys.viscous) kAdjointA<2, true><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, stage, record, T);
+    else kAdjointA<2, false><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, stage, record, T);
   } else {
-    if (c.phys.viscous) kAdjointA<3, true><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, stage, record);
-    else kAdjointA<3, false><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, stage, record);
+    if (c.phys.viscous) kAdjointA<3, true><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, stage, record, T);
+    else kAdjointA<3, false><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, stage, record, T);
   }
 }
 
 void launchAdjointB(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage, double apiFactor,
                     bool api) {
-  const int G = gridFor(b.v.N);
+  const Tile T = b.tAdjB;
+  const int G = T.blocks(), W = T.threads();
   MGD_LAUNCH(c);
   if (c.nD == 2) {
-    if (c.phys.viscous) kAdjointB<2, true><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api);
-    else kAdjointB<2, false><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api);
+    if (c.phys.viscous) kAdjointB<2, true><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api, T);
+    else kAdjointB<2, false><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api, T);
   } else {
-    if (c.phys.viscous) kAdjointB<3, true><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api);
-    else kAdjointB<3, false><<<G, kBlock, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api);
+    if (c.phys.viscous) kAdjointB<3, true><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api, T);
+    else kAdjointB<3, false><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api, T);
   }
 }
 
@@ -788,6 +907,12 @@ void launchAdjointInitial(Context& c, DevBlock& b, double factor) {
   MGD_LAUNCH(c);
   if (c.nD == 2) kAdjointInitial<2><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, factor);
   else kAdjointInitial<3><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, factor);
+}
+
+void launchStoreAdjointForcing(Context& c, DevBlock& b, bool zero) {
+  MGD_LAUNCH(c);
+  if (c.nD == 2) kStoreAdjointForcing<2><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, zero);
+  else kStoreAdjointForcing<3><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, zero);
 }
 
 void launchSnapshot(Context& c, DevBlock& b, double* snapshots, int saveInterval, bool initial) {
@@ -801,10 +926,10 @@ void launchStepAdvance(Context& c, int delta) {
   kStepAdvance<<<1, 32, 0, c.stream>>>(c.dCounters, delta);
 }
 
-void launchReducePartials(Context& c, const double* partials, int nBlocks, int nSlots, double* out) {
+void launchReducePartials(Context& c, const double* partials, int stride, int count, int nSlots, double* out) {
   if (nSlots <= 0) return;
   MGD_LAUNCH(c);
-  kReducePartials<<<nSlots, kBlock, 0, c.stream>>>(partials, nBlocks, nSlots, out);
+  kReducePartials<<<nSlots, kBlock, 0, c.stream>>>(partials, stride, count, nSlots, out);
 }
 
 void launchCoordinateDerivative(Context& c, DevBlock& b, int dir, double* out) {

@@ -187,4 +187,34 @@ inline HostOp makeDissipationTransposeNormInverse48(const HostOp& d1) {
   return t;
 }
 
+// Composite dissipation: one symmetric 8th-difference operator with
+// boundary closure (interior (-1, 8, -28, 56, -70, 56, -28, 8, -1)/256),
+// H-self-adjoint, applied as rhs += amount * D q with no arc-length scaling
+// (magudi's default composite_dissipation = true path).
+inline HostOp makeCompositeDissipation48() {
+  HostOp d;
+  d.depth = 8; d.width = 12; d.half = 4; d.skew = false;
+  d.interior = {-1.0, 8.0, -28.0, 56.0, -70.0, 56.0, -28.0, 8.0, -1.0};
+  for (double& v : d.interior) v = v / 256.0;
+  d.left.assign(8 * 12, 0.0);
+  struct Row { int first, count; double num[9]; double den; };
+  const Row rows[8] = {
+      {0, 5, {-15240960.0, 60963840.0, -91445760.0, 60963840.0, -15240960.0}, 1498139.0},
+      {0, 6, {8709120.0, -35562240.0, 55157760.0, -39191040.0, 11612160.0, -725760.0}, 1107307.0},
+      {0, 7, {-1451520.0, 6128640.0, -10080000.0, 8064000.0, -3225600.0, 645120.0, -80640.0}, 20761.0},
+      {0, 8, {8709120.0, -39191040.0, 72576000.0, -73301760.0, 46448640.0, -20321280.0, 5806080.0, -725760.0},
+       1304999.0},
+      {0, 9, {-2177280.0, 11612160.0, -29030400.0, 46448640.0, -52254720.0, 40642560.0, -20321280.0, 5806080.0,
+              -725760.0}, 299527.0},
+      {1, 9, {-80640.0, 645120.0, -2257920.0, 4515840.0, -5644800.0, 4515840.0, -2257920.0, 645120.0, -80640.0},
+       103097.0},
+      {2, 9, {-725760.0, 5806080.0, -20321280.0, 40642560.0, -50803200.0, 40642560.0, -20321280.0, 5806080.0,
+              -725760.0}, 670091.0},
+      {3, 9, {-5080320.0, 40642560.0, -142248960.0, 284497920.0, -355622400.0, 284497920.0, -142248960.0,
+              40642560.0, -5080320.0}, 5127739.0}};
+  for (int m = 0; m < 8; ++m)
+    for (int t = 0; t < rows[m].count; ++t) d.L(m, rows[m].first + t) = rows[m].num[t] / rows[m].den / 256.0;
+  return d;
+}
+
 }  // namespace mgd

@@ -20,13 +20,12 @@ from . import capi
 @dataclass
 class Options:
     """Hot-path keys of magudi.inp (src/SimulationFlagsImpl.f90:24-45,
-    src/SolverOptionsImpl.f90:46-135). Defaults are the reference defaults,
-    except composite_dissipation, which only the non-composite path supports."""
+    src/SolverOptionsImpl.f90:46-135). Defaults are the reference defaults."""
 
     n_dimensions: int = 2
     viscous: bool = False
     dissipation: bool = False
-    composite_dissipation: bool = False
+    composite_dissipation: bool = True
     curvilinear: bool = True
     use_constant_cfl: bool = True
     enable_controller: bool = False

@@ -56,6 +56,7 @@ def load_library(build_if_missing=True):
     L.mgd_run_forward.argtypes = [ctx, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_double)]
     L.mgd_run_adjoint.argtypes = [ctx, C.POINTER(C.c_double)]
     L.mgd_get_gradient.argtypes = [ctx, C.POINTER(C.c_double), C.c_longlong]
+    L.mgd_profile_stage_kernels.argtypes = [ctx, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)]
     L.mgd_stream.restype = C.c_void_p
     L.mgd_stream.argtypes = [ctx]
     L.mgd_kernel_launches.restype = C.c_longlong
@@ -179,6 +180,16 @@ class Solver:
         out = np.zeros(n_entries * P)
         self._check(self.L.mgd_get_gradient(self.h, capi.dptr(out), n_entries))
         return out.reshape(n_entries, P)
+
+    def profile_stage_kernels(self, mode, reps=20):
+        """Mean per-launch milliseconds of each kernel of one RK stage."""
+        out = (C.c_double * 8)()
+        n = C.c_int()
+        self._check(self.L.mgd_profile_stage_kernels(self.h, mode, reps, out, C.byref(n)))
+        return list(out)[: n.value]
+
+    def stream_handle(self):
+        return self.L.mgd_stream(self.h)
 
     def kernel_launches(self, reset=False):
         return self.L.mgd_kernel_launches(self.h, int(reset))

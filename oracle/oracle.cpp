@@ -193,6 +193,39 @@ StencilOp sbp48Dissipation() {
   return op;
 }
 
+// "SBP 4-8 composite dissipation", src/StencilOperatorImpl.f90:1842-1927.
+StencilOp sbp48CompositeDissipation() {
+  StencilOp op;
+  op.symmetryType = SYMMETRIC;
+  op.interiorWidth = 9;
+  op.boundaryWidth = 12;
+  op.boundaryDepth = 8;
+  op.allocate();
+  const double in[5] = {-70.0, 56.0, -28.0, 8.0, -1.0};
+  for (int j = 0; j <= 4; ++j) op.in(j) = in[j];
+  for (int j = 1; j <= 4; ++j) op.in(-j) = op.in(j);
+  for (double& v : op.interior) v = v / 256.0;
+  const double nb[8] = {1498139.0 / 5080320.0, 1107307.0 / 725760.0, 20761.0 / 80640.0,
+                        1304999.0 / 725760.0,  299527.0 / 725760.0,  103097.0 / 80640.0,
+                        670091.0 / 725760.0,   5127739.0 / 5080320.0};
+  for (int i = 0; i < 8; ++i) op.normBoundary[i] = nb[i];
+  struct Row { int m, k0, n; double num[9]; double den; };
+  const Row rows[8] = {
+      {1, 1, 5, {-15240960.0, 60963840.0, -91445760.0, 60963840.0, -15240960.0}, 1498139.0},
+      {2, 1, 6, {8709120.0, -35562240.0, 55157760.0, -39191040.0, 11612160.0, -725760.0}, 1107307.0},
+      {3, 1, 7, {-1451520.0, 6128640.0, -10080000.0, 8064000.0, -3225600.0, 645120.0, -80640.0}, 20761.0},
+      {4, 1, 8, {8709120.0, -39191040.0, 72576000.0, -73301760.0, 46448640.0, -20321280.0, 5806080.0, -725760.0}, 1304999.0},
+      {5, 1, 9, {-2177280.0, 11612160.0, -29030400.0, 46448640.0, -52254720.0, 40642560.0, -20321280.0, 5806080.0, -725760.0}, 299527.0},
+      {6, 2, 9, {-80640.0, 645120.0, -2257920.0, 4515840.0, -5644800.0, 4515840.0, -2257920.0, 645120.0, -80640.0}, 103097.0},
+      {7, 3, 9, {-725760.0, 5806080.0, -20321280.0, 40642560.0, -50803200.0, 40642560.0, -20321280.0, 5806080.0, -725760.0}, 670091.0},
+      {8, 4, 9, {-5080320.0, 40642560.0, -142248960.0, 284497920.0, -355622400.0, 284497920.0, -142248960.0, 40642560.0, -5080320.0}, 5127739.0}};
+  for (const Row& r : rows)
+    for (int t = 0; t < r.n; ++t) op.b1(r.k0 + t, r.m) = r.num[t] / r.den;
+  for (double& v : op.rb1) v = v / 256.0;
+  op.fillRightBoundary();
+  return op;
+}
+
 // "SBP 4-8 dissipation transpose", src/StencilOperatorImpl.f90:1942-1960.
 StencilOp sbp48DissipationTranspose() {
   StencilOp op;
@@ -995,7 +1028,7 @@ static void normalizeMollifiers(Region& R) {
   }
 }
 
-// addDissipation, src/RhsHelperImpl.f90:10-87 (non-composite path).
+// addDissipation, src/RhsHelperImpl.f90:10-87 (composite and non-composite paths).
 static void addDissipation(Region& R, Block& b, int mode) {
   const int nD = R.nD, nU = R.nU;
   const long long N = b.N;
@@ -1005,10 +1038,12 @@ static void addDissipation(Region& R, Block& b, int mode) {
     const std::vector<double>& src = mode == MGD_FORWARD ? b.conservedVariables : b.adjointVariables;
     std::copy(src.begin(), src.end(), d.begin());
     apply(b.dissipation[i], d.data(), nU, b.gs, i);
-    for (int j = 0; j < nU; ++j)
-      for (long long p = 0; p < N; ++p) d[N * j + p] = -b.arcLengths[N * i + p] * d[N * j + p];
-    apply(b.dissipationTranspose[i], d.data(), nU, b.gs, i);
-    applyNorm(b.firstDerivative[i], d.data(), nU, b.gs, i, true);
+    if (!R.o.composite_dissipation) {
+      for (int j = 0; j < nU; ++j)
+        for (long long p = 0; p < N; ++p) d[N * j + p] = -b.arcLengths[N * i + p] * d[N * j + p];
+      apply(b.dissipationTranspose[i], d.data(), nU, b.gs, i);
+      applyNorm(b.firstDerivative[i], d.data(), nU, b.gs, i, true);
+    }
     for (long long k = 0; k < N * nU; ++k) b.rightHandSide[k] = b.rightHandSide[k] + amount * d[k];
   }
 }
@@ -1567,7 +1602,7 @@ int orc_add_block(void* h, const mgd_block_desc* d, const double* coords, const 
   b.coordinates.assign(coords, coords + b.N * R.nD);
   b.iblank.assign(iblank, iblank + b.N);
   auto d1 = orc::sbp48FirstDerivative();
-  auto diss = orc::sbp48Dissipation();
+  auto diss = R.o.composite_dissipation ? orc::sbp48CompositeDissipation() : orc::sbp48Dissipation();
   auto dissT = orc::sbp48DissipationTranspose();
   for (int i = 0; i < R.nD; ++i) {
     orc::StencilOp a = d1, ad = orc::adjointOf(d1), di = diss, dt = dissT;
@@ -1736,12 +1771,14 @@ int orc_get_gradient(void* h, double* dst, long long nEntries) {
 }
 
 // Operator tables for the coefficient tests: which = 0 first derivative,
-// 1 adjoint first derivative, 2 dissipation, 3 dissipation transpose.
+// 1 adjoint first derivative, 2 dissipation, 3 dissipation transpose,
+// 4 composite dissipation.
 int orc_operator_info(int which, int* dims /* symmetry, iw, bw, bd */, double* interior,
                       double* rb1, double* norm) {
   orc::StencilOp d1 = orc::sbp48FirstDerivative();
   orc::StencilOp op = which == 0 ? d1 : which == 1 ? orc::adjointOf(d1)
-                      : which == 2 ? orc::sbp48Dissipation() : orc::sbp48DissipationTranspose();
+                      : which == 2 ? orc::sbp48Dissipation()
+                      : which == 3 ? orc::sbp48DissipationTranspose() : orc::sbp48CompositeDissipation();
   dims[0] = op.symmetryType; dims[1] = op.interiorWidth; dims[2] = op.boundaryWidth; dims[3] = op.boundaryDepth;
   if (interior) std::copy(op.interior.begin(), op.interior.end(), interior);
   if (rb1) std::copy(op.rb1.begin(), op.rb1.end(), rb1);
@@ -1753,7 +1790,8 @@ int orc_operator_info(int which, int* dims /* symmetry, iw, bw, bd */, double* i
 int orc_apply_operator(int which, int periodicity, double* x, int ncomp, const int* gs, int dir) {
   orc::StencilOp d1 = orc::sbp48FirstDerivative();
   orc::StencilOp op = which == 0 ? d1 : which == 1 ? orc::adjointOf(d1)
-                      : which == 2 ? orc::sbp48Dissipation() : orc::sbp48DissipationTranspose();
+                      : which == 2 ? orc::sbp48Dissipation()
+                      : which == 3 ? orc::sbp48DissipationTranspose() : orc::sbp48CompositeDissipation();
   orc::updateOperator(op, periodicity);
   int g[3] = {gs[0], gs[1], gs[2]};
   orc::apply(op, x, ncomp, g, dir);

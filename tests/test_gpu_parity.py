@@ -75,6 +75,24 @@ def test_adjoint_rhs_random_state(seed):
     assert rel_err(g, r) < RHS_TOL
 
 
+@pytest.mark.parametrize("composite", [True, False])
+def test_rhs_dissipation_variants(composite):
+    P = small_monopole()
+    P.options.composite_dissipation = composite
+    q, lam = random_full_rhs_state(P, 21)
+    pair = _pair(P)
+    _set_both(pair, capi.FIELD_CONSERVED, q)
+    _set_both(pair, capi.FIELD_ADJOINT, lam)
+    for s in pair:
+        s.update_state()
+        s.update_adjoint_forcing(False)
+        s.compute_rhs(capi.FORWARD, 0.1)
+    assert rel_err(pair[0].get_field(1, capi.FIELD_RHS), pair[1].get_field(1, capi.FIELD_RHS)) < RHS_TOL
+    for s in pair:
+        s.compute_rhs(capi.ADJOINT, 0.0, 0.5)
+    assert rel_err(pair[0].get_field(1, capi.FIELD_RHS), pair[1].get_field(1, capi.FIELD_RHS)) < RHS_TOL
+
+
 def test_rhs_inviscid_no_dissipation():
     P = small_monopole()
     P.options.viscous = False

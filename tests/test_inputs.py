@@ -1,0 +1,71 @@
+"""magudi.inp / bc.dat front end (CPU)."""
+import pytest
+
+from magudi_gb300 import inputs
+from magudi_gb300.capi import PERIODIC_PLANE
+
+INP = """# comment line
+output_prefix = "AcousticMonopole"
+include_viscous_terms = true
+use_constant_CFL_mode = false
+curvilinear_domain = false
+Reynolds_number = 200.
+Prandtl_number = 0.72   # trailing comment
+add_dissipation = true
+dissipation_amount = 0.01
+time_step_size = 0.05
+defaults/sponge_amount = 0.2
+patches/farField.E/viscous_penalty_amount = 0.5
+number_of_acoustic_sources = 1
+acoustic_source01/amplitude = 0.01
+acoustic_source01/x = -3.
+grid001/dir1/periodicity_type = "PLANE"
+grid001/dir1/periodic_length = 6.283185307179586
+"""
+
+BC = """# Name                 Type                  Grid normDir iMin iMax jMin jMax kMin kMax
+  farField.E           SAT_FAR_FIELD            1       1    1    1    1   -1    1   -1
+  sponge.E             SPONGE                   1       1    1   29    1   -1    1   -1
+  controlRegion        ACTUATOR                 1       0  108  137   86  116    1   -1
+"""
+
+
+def test_parse_and_map(tmp_path):
+    (tmp_path / "magudi.inp").write_text(INP)
+    (tmp_path / "bc.dat").write_text(BC)
+    d = inputs.parse_input_file(tmp_path / "magudi.inp")
+    assert d.get_str("output_prefix") == "AcousticMonopole"
+    o = inputs.options_from_inputs(d, 2)
+    assert o.viscous and o.dissipation and not o.curvilinear and not o.use_constant_cfl
+    assert o.reynolds_number == 200.0 and o.prandtl_number == 0.72
+    assert o.composite_dissipation  # reference default
+    assert o.viscosity_power_law_exponent == 0.666 and o.bulk_viscosity_ratio == 0.6
+    rows = inputs.read_bc_dat(tmp_path / "bc.dat")
+    ps = inputs.patches_from_bc(d, rows)
+    assert [p.type for p in ps] == ["SAT_FAR_FIELD", "SPONGE", "ACTUATOR"]
+    assert ps[0].viscous_penalty_amount == 0.5 and ps[0].inviscid_penalty_amount == 1.0
+    assert ps[1].sponge_amount == 0.2 and ps[1].sponge_exponent == 2
+    src = inputs.sources_from_inputs(d, 2)
+    assert len(src) == 1 and src[0].location[0] == -3.0 and src[0].amplitude == 0.01
+    types, lengths = inputs.block_periodicity(d, 1, 2)
+    assert types[0] == PERIODIC_PLANE and abs(lengths[0] - 6.283185307179586) < 1e-15
+
+
+def test_errors(tmp_path):
+    (tmp_path / "bad.inp").write_text("a = b = c\n")
+    with pytest.raises(inputs.InputError):
+        inputs.parse_input_file(tmp_path / "bad.inp")
+    (tmp_path / "dup.dat").write_text(BC + "  farField.E SAT_FAR_FIELD 1 1 1 1 1 -1 1 -1\n")
+    with pytest.raises(inputs.InputError):
+        inputs.read_bc_dat(tmp_path / "dup.dat")
+    (tmp_path / "m.inp").write_text("add_dissipation = true\n")
+    with pytest.raises(inputs.InputError):
+        inputs.options_from_inputs(inputs.parse_input_file(tmp_path / "m.inp"), 2)
+
+
+def test_round_trip(tmp_path):
+    from magudi_gb300 import configs
+    P = configs.monopole_2d(n=41)
+    inputs.write_bc_dat(tmp_path / "bc.dat", P.patches)
+    rows = inputs.read_bc_dat(tmp_path / "bc.dat")
+    assert [r[4] for r in rows] == [tuple(p.extent) for p in P.patches]

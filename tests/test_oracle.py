@@ -136,8 +136,9 @@ def _dual_consistency(P, seed=1):
     return order.mean()
 
 
-def test_full_rhs_dual_consistency_2d():
-    P = small_monopole(n=31, ny=29, sponge_points=5)
+@pytest.mark.parametrize("composite", [True, False])
+def test_full_rhs_dual_consistency_2d(composite):
+    P = small_monopole(n=31, ny=29, sponge_points=5, composite_dissipation=composite)
     assert _dual_consistency(P) >= 0.9
 
 
