@@ -208,6 +208,21 @@ int mgd_profile_stage_kernels(mgd_ctx* ctx, int mode, int reps, double* avg_ms, 
  * CUDA's pow (ref), for checking the viscosity law's error bound. */
 int mgd_selftest_pow(const double* x, int n, double e, double* fast, double* ref);
 
+/* Forward RHS without any device allocation (no counterpart in the
+ * reference). For callers that must not allocate device memory when they
+ * evaluate an RHS -- a host that reserved its device-memory budget up front
+ * with its own pool, or a loop that cannot take cudaMalloc's implicit device
+ * synchronisation. q (N, nU) and rhs (N, nU) are the caller's device
+ * buffers; time is state%time. Grid and patch data come from the context,
+ * which must have been finalized; all intermediates live in one fixed
+ * 16 MiB array in device memory that every GPU loading the library holds
+ * until exit, so blocks above about 100k points (2D) / 55k points (3D) are
+ * rejected with an error. The first call on a device looks up that array's
+ * device address, so make it before any stream capture. Calls share the
+ * array: calls that overlap on the GPU (from different contexts or host
+ * threads) race and must be serialised by the caller. */
+int mgd_forward_rhs_noalloc(mgd_ctx* ctx, const double* q, double time, double* rhs);
+
 /* CUDA stream the context launches on (cudaStream_t as void*). */
 void* mgd_stream(mgd_ctx* ctx);
 

@@ -19,9 +19,6 @@
 
 using namespace mgd;
 
-struct mgd_ctx {
-  Context c;
-};
 
 static std::string g_createError;
 

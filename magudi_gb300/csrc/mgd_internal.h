@@ -200,3 +200,8 @@ Tile makeTile(const DevBlock& b, int tx, int ty, int tz);
 int maxTileBlocks(const DevBlock& b);
 
 }  // namespace mgd
+
+// The opaque handle of the C ABI.
+struct mgd_ctx {
+  mgd::Context c;
+};
