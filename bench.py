@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-sample-steps", type=int, default=40)
+    ap.add_argument("--cpu-sample-steps", type=int, default=400)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rk-steps", type=int, default=N_STEPS,
                     help="RK4 steps per gradient evaluation (profiling runs use a few)")
@@ -147,15 +147,34 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-# Algorithmic units of the dominant kernels, per grid point (2D), from their
-# compulsory array traffic (each array touched once) and the FP64 operation
-# counts of the kernel code (adds, multiplies and FMAs counted as 1 and 2 flops).
+# Algorithmic traffic and FP64 operations per grid point of each stage kernel
+# on the 2D viscous Cartesian workload (each array element that the kernel
+# needs read or written once; stencil neighbours are re-reads, not counted).
+# bytes: doubles x 8 plus int32 index words x 4; flops: adds and multiplies
+# count 1, FMAs 2.
 KERNEL_UNITS = {
-    "adjoint_part_a": {"bytes": 8 * (4 + 4 + 3 + 4 + 3 + 8 + 4 + 6 + 8 + 2) + 16, "flops": 620},
-    "forward_divergence_rk": {"bytes": 8 * (8 + 8 + 1 + 4 + 1 + 8 + 4 + 8 + 4) + 20, "flops": 330},
-    "forward_gradient_flux": {"bytes": 8 * (6 + 4 + 3 + 2 + 8 + 8) + 12, "flops": 290},
-    "adjoint_part_b": {"bytes": 8 * (4 + 6 + 8 + 4 + 4 + 8 + 4 + 1) + 20, "flops": 260},
+    # q 4, prim (u 2, p, T, mu, la, k) 7, metric diagonal 2, jac 1; writes fhat 8; ffOfPoint 3 ints
+    "forward_gradient_flux": {"bytes": 8 * (4 + 7 + 2 + 1 + 8) + 4 * 3, "flops": 130},
+    # q 4 read, dq 4 written
+    "forward_dissipation": {"bytes": 8 * (4 + 4), "flops": 80},
+    # fhat 8, dq 4, jac 1, q 4, qt 4, sponge 1, srcG 1, b1 4, b2 4 read; b2 4, q 4 written; ffOfPoint 3 + iblank 1 ints
+    "forward_divergence_rk": {"bytes": 8 * (8 + 4 + 1 + 4 + 4 + 1 + 1 + 4 + 4 + 4 + 4) + 4 * 4, "flops": 90},
+    # q 4 read, prim 8 written
+    "forward_primitives": {"bytes": 8 * (4 + 8), "flops": 55},
+    # lambda 4, metric diagonal 2, prim (u 2, v, T, mu, la, k) 7, tau 4, hf 2, jac 1 read; rcore 4, ad 6 written
+    "adjoint_core": {"bytes": 8 * (4 + 2 + 7 + 4 + 2 + 1 + 4 + 6) + 4 * 3, "flops": 370},
+    # lambda 4 read, dq 4 written
+    "adjoint_dissipation": {"bytes": 8 * (4 + 4), "flops": 80},
+    # ad 6 read, t2 3 written
+    "adjoint_diffusion": {"bytes": 8 * (6 + 3), "flops": 48},
+    # rcore 4, prim (v, u 2) 3, q_E 1, t2 3, dq 4, jac 1, lambda 4, sponge 1, tgtCount 1, b1 4, b2 4 read;
+    # b2 4, lambda 4 written; ffOfPoint 3 + iblank 1 ints
+    "adjoint_assemble_rk": {"bytes": 8 * (4 + 3 + 1 + 3 + 4 + 1 + 4 + 1 + 1 + 4 + 4 + 4 + 4) + 4 * 4, "flops": 60},
 }
+FORWARD_KERNELS = ["forward_gradient_flux", "forward_dissipation", "forward_divergence_rk", "forward_primitives",
+                   "forward_functional"]
+ADJOINT_KERNELS = ["adjoint_core", "adjoint_dissipation", "adjoint_diffusion", "adjoint_assemble_rk",
+                   "adjoint_gradient_sensitivity"]
 
 
 def run_reference(args):
@@ -272,9 +291,16 @@ def run_ours(args):
     # per-kernel timing for the roofline (separate short loops on the same stream)
     fwd = s.profile_stage_kernels(capi.FORWARD, 30)
     adj = s.profile_stage_kernels(capi.ADJOINT, 30)
-    kern = {"forward_gradient_flux": fwd[0], "forward_divergence_rk": fwd[1],
-            "adjoint_part_a": adj[2], "adjoint_part_b": adj[3]}
-    dominant = max(kern, key=kern.get)
+    kern = dict(zip(FORWARD_KERNELS, fwd))
+    kern.update(zip(ADJOINT_KERNELS, adj))
+    # launches per gradient evaluation: forward stage kernels run in the forward
+    # pass and again in the checkpoint recomputation, the functional only in the
+    # forward pass, adjoint kernels once
+    per_grad = {k: 8 * n_steps for k in FORWARD_KERNELS}
+    per_grad["forward_functional"] = 4 * n_steps
+    per_grad.update({k: 4 * n_steps for k in ADJOINT_KERNELS})
+    share = {k: kern[k] * per_grad[k] for k in kern}
+    dominant = max((k for k in share if k in KERNEL_UNITS), key=share.get)
     peaks, peak_kind = measured_peaks()
     units = KERNEL_UNITS[dominant]
     t_launch = kern[dominant] / 1e3
@@ -296,6 +322,7 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk,
         "kernels_ms_per_launch": kern,
+        "kernel_time_share": {k: share[k] / sum(share.values()) for k in share},
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved_gbs,
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
                      "traffic": None, "peak_source": peak_kind,

@@ -118,6 +118,16 @@ int mgd_create(const mgd_options* o, mgd_ctx** out) {
     delete h;
     return 1;
   }
+  if (cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking) != cudaSuccess) {
+    g_createError = "cudaStreamCreate failed";
+    cudaStreamDestroy(c.stream);
+    delete h;
+    return 1;
+  }
+  for (int k = 0; k < 8; ++k) {
+    cudaEventCreateWithFlags(&c.evFork[k], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c.evJoin[k], cudaEventDisableTiming);
+  }
   uploadOperatorTables();
   cudaMalloc((void**)&c.dCounters, 4 * sizeof(int));
   const int init[4] = {1, 0, 1, 0};
@@ -144,6 +154,11 @@ int mgd_destroy(mgd_ctx* h) {
   if (c.gForward) cudaGraphExecDestroy(c.gForward);
   if (c.gRecompute) cudaGraphExecDestroy(c.gRecompute);
   if (c.gAdjoint) cudaGraphExecDestroy(c.gAdjoint);
+  for (int k = 0; k < 8; ++k) {
+    cudaEventDestroy(c.evFork[k]);
+    cudaEventDestroy(c.evJoin[k]);
+  }
+  cudaStreamDestroy(c.side);
   cudaStreamDestroy(c.stream);
   delete h;
   return 0;
@@ -313,7 +328,7 @@ int mgd_add_block(mgd_ctx* h, const mgd_block_desc* desc, const double* coordina
     v.ax[i].stride = i == 0 ? 1 : (i == 1 ? v.gs[0] : (long long)v.gs[0] * v.gs[1]);
   }
   v.curvilinear = c.opts.curvilinear;
-  b.tGrad = b.tRhs = b.tAdjA = b.tAdjB = c.nD == 2 ? makeTile(b, 32, 4, 1) : makeTile(b, 32, 2, 2);
+  b.tGrad = b.tDiss = b.tRhs = b.tAdjA = b.tAdjD = b.tAdjB = c.nD == 2 ? makeTile(b, 32, 4, 1) : makeTile(b, 32, 2, 2);
   const long long N = v.N;
   const int nD = c.nD, nU = c.nU;
   PrimLayout L{nD};
@@ -340,6 +355,7 @@ int mgd_add_block(mgd_ctx* h, const mgd_block_desc* desc, const double* coordina
   chk(devAlloc(b, &v.dq, N * nD * nU));
   chk(devAlloc(b, &v.rcore, N * nU));
   chk(devAlloc(b, &v.ad, N * nD * (nU - 1)));
+  chk(devAlloc(b, &v.t2, N * (nU - 1)));
   chk(devAlloc(b, &v.adjF, N * nU));
   chk(devAlloc(b, &sponge, N));
   chk(devAlloc(b, &mc, N));
@@ -491,12 +507,13 @@ struct TuneKey {
 };
 
 static int autotune(Context& c, DevBlock& b) {
-  static std::map<TuneKey, std::array<Tile, 4>> cache;
+  static std::map<TuneKey, std::array<Tile, 6>> cache;
   TuneKey key{c.nD, {b.v.gs[0], b.v.gs[1], b.v.gs[2]}, b.v.curvilinear, c.phys.viscous, c.phys.dissipation,
               c.phys.composite};
+  Tile* slots[6] = {&b.tGrad, &b.tDiss, &b.tRhs, &b.tAdjA, &b.tAdjD, &b.tAdjB};
   auto it = cache.find(key);
   if (it != cache.end()) {
-    b.tGrad = it->second[0]; b.tRhs = it->second[1]; b.tAdjA = it->second[2]; b.tAdjB = it->second[3];
+    for (int k = 0; k < 6; ++k) *slots[k] = it->second[k];
     return 0;
   }
   std::vector<std::array<int, 3>> cands;
@@ -509,7 +526,7 @@ static int autotune(Context& c, DevBlock& b) {
   RunScalars rs = apiScalars(c);
   if (setApiTime(c, 0.0)) return 1;
   launchPrims(c, b, b.v.q, false);
-  if (c.phys.viscous) launchGradFlux(c, b, false, false, true, &rs, 1, false);
+  if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs, 1, false);
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -523,19 +540,21 @@ static int autotune(Context& c, DevBlock& b) {
     cudaEventElapsedTime(&ms, e0, e1);
     return ms;
   };
-  Tile* slots[4] = {&b.tGrad, &b.tRhs, &b.tAdjA, &b.tAdjB};
   const long long saved = c.launches;
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < 6; ++k) {
+    if ((k == 1 && !c.phys.dissipation) || (k == 4 && !c.phys.viscous)) continue;
     float best = 1e30f;
     Tile bestTile = *slots[k];
     for (const auto& cd : cands) {
       *slots[k] = makeTile(b, cd[0], cd[1], cd[2]);
       float ms;
       switch (k) {
-        case 0: ms = timeIt([&] { launchGradFlux(c, b, true, true, false, &rs, 1, false); }); break;
-        case 1: ms = timeIt([&] { launchForwardRhs(c, b, 0, rs, true, false, false); }); break;
-        case 2: ms = timeIt([&] { launchAdjointA(c, b, rs, 1, false); }); break;
-        default: ms = timeIt([&] { launchAdjointB(c, b, 0, rs, 1, 0.0, true); }); break;
+        case 0: ms = timeIt([&] { launchGradFlux(c, b, true, false, &rs, 1, false); }); break;
+        case 1: ms = timeIt([&] { launchDissipation(c, b, b.v.q, 1.0); }); break;
+        case 2: ms = timeIt([&] { launchForwardDivergence(c, b, 0, rs, true, false); }); break;
+        case 3: ms = timeIt([&] { launchAdjointCore(c, b, rs, 1, false); }); break;
+        case 4: ms = timeIt([&] { launchAdjointDiffusion(c, b); }); break;
+        default: ms = timeIt([&] { launchAdjointAssemble(c, b, 0, rs, 1, 0.0, true, false); }); break;
       }
       if (ms < best) { best = ms; bestTile = *slots[k]; }
     }
@@ -545,7 +564,9 @@ static int autotune(Context& c, DevBlock& b) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (checkLaunch(c)) return 1;
-  cache[key] = {b.tGrad, b.tRhs, b.tAdjA, b.tAdjB};
+  std::array<Tile, 6> entry;
+  for (int k = 0; k < 6; ++k) entry[k] = *slots[k];
+  cache[key] = entry;
   return 0;
 }
 
@@ -667,6 +688,9 @@ int mgd_finalize_setup(mgd_ctx* h) {
     }
   }
   c.actuatorPoints = actOffset;
+  std::vector<int> actPts((size_t)std::max(1LL, actOffset), 0);
+  for (long long p = 0; p < N; ++p)
+    if (actIdx[p] >= 0) actPts[actIdx[p]] = (int)p;
   for (long long p = 0; p < N; ++p)
     if (b.hostIblank[p] == 0) { maskT[p] = 0.0; maskA[p] = 0.0; }
   // mollifier normalization (src/RegionImpl.f90:459-603, L1 norm)
@@ -705,6 +729,23 @@ int mgd_finalize_setup(mgd_ctx* h) {
   }
   BlockView& v = b.v;
   v.nSources = (int)c.sources.size();
+  std::vector<int> tgtPts;
+  for (long long p = 0; p < N; ++p)
+    if (wT[p] != 0.0) tgtPts.push_back((int)p);
+  {
+    int* dT = nullptr;
+    int* dA = nullptr;
+    if (devAlloc(b, &dT, std::max<size_t>(1, tgtPts.size())) != cudaSuccess ||
+        devAlloc(b, &dA, actPts.size()) != cudaSuccess)
+      return fail(c, "device allocation failed for patch point lists");
+    if (!tgtPts.empty())
+      CUDA_TRY(c, cudaMemcpy(dT, tgtPts.data(), tgtPts.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(dA, actPts.data(), actPts.size() * sizeof(int), cudaMemcpyHostToDevice));
+    v.tgtPts = dT;
+    v.nTgt = (int)tgtPts.size();
+    v.actPts = dA;
+    v.nAct = (int)actOffset;
+  }
   CUDA_TRY(c, cudaMemcpy((void*)v.sponge, sponge.data(), N * sizeof(double), cudaMemcpyHostToDevice));
   CUDA_TRY(c, cudaMemcpy((void*)v.mc, mcH.data(), N * sizeof(double), cudaMemcpyHostToDevice));
   CUDA_TRY(c, cudaMemcpy((void*)v.mt, mtH.data(), N * sizeof(double), cudaMemcpyHostToDevice));
@@ -749,7 +790,7 @@ int mgd_finalize_setup(mgd_ctx* h) {
       launchPrims(c, b, v.qt, false);
       double* qSave = v.q;
       v.q = (double*)v.qt;
-      launchGradFlux(c, b, false, false, true, nullptr, 0, false);
+      launchGradFlux(c, b, false, true, nullptr, 0, false);
       v.q = qSave;
       launchFarFieldTargetVisc(c, b);
     }
@@ -769,7 +810,7 @@ static RunScalars apiScalars(Context& c) {
   r.amp = c.dApiAmp;
   r.dt = c.opts.time_step_size;
   r.adjointForcingSwitch = c.opts.adjoint_forcing_switch;
-  r.nPartialBlocks = stageBlocks(c.blocks[0]);
+  r.nPartialBlocks = reductionBlocks(c.blocks[0]);
   return r;
 }
 
@@ -789,12 +830,56 @@ static int requireReady(Context& c) {
   return 0;
 }
 
+namespace mgd {
+
+// One forward RK stage (rkStage 1..4) or the forward RHS alone (rkStage 0).
+// The dissipation kernel runs on the side stream beside the flux kernel; both
+// only read q and join before the divergence kernel updates it.
+void forwardStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bool api, bool controller, bool store,
+                  bool functional) {
+  const int stage = api ? 1 : rkStage;
+  const bool diss = c.phys.dissipation != 0;
+  if (diss) {
+    cudaEventRecord(c.evFork[0], c.stream);
+    cudaStreamWaitEvent(c.side, c.evFork[0], 0);
+    launchDissipation(c, b, b.v.q, 1.0, c.side);
+    cudaEventRecord(c.evJoin[0], c.side);
+  }
+  launchGradFlux(c, b, true, false, &rs, stage, store);
+  if (diss) cudaStreamWaitEvent(c.stream, c.evJoin[0], 0);
+  launchForwardDivergence(c, b, rkStage, rs, api, controller);
+  if (rkStage > 0) launchPrims(c, b, b.v.q, false);
+  if (functional) launchFunctional(c, b, rs, stage);
+}
+
+// One adjoint RK stage (rkStage 4..1) or the adjoint RHS alone (rkStage 0).
+// The adjoint dissipation and, when recording, the gradient/sensitivity
+// kernel read lambda on the side stream beside the core and diffusion
+// kernels; all join before the assembly kernel updates lambda.
+void adjointStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage, double apiFactor, bool api,
+                  bool fromSlot, bool record) {
+  const bool side = c.phys.dissipation != 0 || record;
+  if (side) {
+    cudaEventRecord(c.evFork[1], c.stream);
+    cudaStreamWaitEvent(c.side, c.evFork[1], 0);
+    launchDissipation(c, b, b.v.lam, -1.0, c.side);
+    if (record) launchGradientSensitivity(c, b, rs, stage, c.side);
+    cudaEventRecord(c.evJoin[1], c.side);
+  }
+  launchAdjointCore(c, b, rs, stage, fromSlot);
+  launchAdjointDiffusion(c, b);
+  if (side) cudaStreamWaitEvent(c.stream, c.evJoin[1], 0);
+  launchAdjointAssemble(c, b, rkStage, rs, stage, apiFactor, api, fromSlot);
+}
+
+}  // namespace mgd
+
 int mgd_update_state(mgd_ctx* h) {
   Context& c = h->c;
   if (requireReady(c)) return 1;
   DevBlock& b = c.blocks[0];
   launchPrims(c, b, b.v.q, false);
-  if (c.phys.viscous) launchGradFlux(c, b, false, false, true, nullptr, 0, false);
+  if (c.phys.viscous) launchGradFlux(c, b, false, true, nullptr, 0, false);
   if (checkLaunch(c)) return 1;
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   return 0;
@@ -808,13 +893,11 @@ int mgd_compute_rhs(mgd_ctx* h, int mode, double time, double adjoint_forcing_fa
   if (mode == MGD_FORWARD) {
     if (setApiTime(c, time)) return 1;
     launchPrims(c, b, b.v.q, false);
-    launchGradFlux(c, b, true, true, false, &rs, 1, false);
-    launchForwardRhs(c, b, 0, rs, true, false, false);
+    forwardStage(c, b, 0, rs, true, false, false, false);
   } else if (mode == MGD_ADJOINT) {
     launchPrims(c, b, b.v.q, false);
-    if (c.phys.viscous) launchGradFlux(c, b, false, false, true, &rs, 1, false);
-    launchAdjointA(c, b, rs, 1, false);
-    launchAdjointB(c, b, 0, rs, 1, adjoint_forcing_factor, true);
+    if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs, 1, false);
+    adjointStage(c, b, 0, rs, 1, adjoint_forcing_factor, true, false, false);
   } else {
     return fail(c, "mode must be MGD_FORWARD or MGD_ADJOINT");
   }
@@ -836,14 +919,14 @@ int mgd_update_adjoint_forcing(mgd_ctx* h, int no_adjoint_forcing) {
   return 0;
 }
 
-static int reduceToHost(Context& c, int nSlots, int count, std::vector<double>& out) {
-  const int nb = stageBlocks(c.blocks[0]);
+static int reduceToHost(Context& c, int nSlots, std::vector<double>& out) {
+  const int nb = reductionBlocks(c.blocks[0]);
   if (c.stageValueCapacity < nSlots) {
     cudaFree(c.dStageValues);
     CUDA_TRY(c, cudaMalloc((void**)&c.dStageValues, (size_t)std::max(1, nSlots) * sizeof(double)));
     c.stageValueCapacity = nSlots;
   }
-  launchReducePartials(c, c.dPartials, nb, count, nSlots, c.dStageValues);
+  launchReducePartials(c, c.dPartials, nb, nb, nSlots, c.dStageValues);
   out.resize(nSlots);
   if (nSlots > 0)
     CUDA_TRY(c, cudaMemcpyAsync(out.data(), c.dStageValues, (size_t)nSlots * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
@@ -852,7 +935,7 @@ static int reduceToHost(Context& c, int nSlots, int count, std::vector<double>& 
 }
 
 static int ensurePartials(Context& c, long long nSlots) {
-  const long long need = nSlots * stageBlocks(c.blocks[0]);
+  const long long need = nSlots * reductionBlocks(c.blocks[0]);
   if (c.partialCapacity < need) {
     cudaFree(c.dPartials);
     CUDA_TRY(c, cudaMalloc((void**)&c.dPartials, (size_t)std::max(1LL, need) * sizeof(double)));
@@ -909,14 +992,12 @@ int mgd_rk4_substep(mgd_ctx* h, int mode, double* time, double dt, int stage) {
     if (stage == 2 || stage == 4) *time = *time + dt / 2.0;
     if (setApiTime(c, *time)) return 1;
     launchPrims(c, b, b.v.q, false);
-    launchGradFlux(c, b, true, true, false, &rs, 1, false);
-    launchForwardRhs(c, b, stage, rs, true, false, false);
+    forwardStage(c, b, stage, rs, true, false, false, false);
   } else if (mode == MGD_ADJOINT) {
     const double factor = stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0);
     launchPrims(c, b, b.v.q, false);
-    if (c.phys.viscous) launchGradFlux(c, b, false, false, true, &rs, 1, false);
-    launchAdjointA(c, b, rs, 1, false);
-    launchAdjointB(c, b, stage, rs, 1, factor, true);
+    if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs, 1, false);
+    adjointStage(c, b, stage, rs, 1, factor, true, false, false);
     if (stage == 3 || stage == 1) *time = *time - dt / 2.0;
   } else {
     return fail(c, "mode must be MGD_FORWARD or MGD_ADJOINT");
@@ -960,8 +1041,10 @@ static RunScalars runScalars(Context& c) {
   r.P = c.actuatorPoints;
   r.gradient = c.dGradient;
   r.partials = c.dPartials;
-  r.nPartialBlocks = stageBlocks(c.blocks[0]);
+  r.nPartialBlocks = reductionBlocks(c.blocks[0]);
   r.stageBuf = c.dStageBuf;
+  r.slotStride = c.slotStride;
+  r.slotFull = c.slotFull;
   r.dt = c.opts.time_step_size;
   r.adjointForcingSwitch = c.opts.adjoint_forcing_switch;
   return r;
@@ -990,6 +1073,34 @@ static int capture(Context& c, cudaGraphExec_t* exec, long long* nodes, F body) 
   c.launches = before;
   CUDA_TRY(c, cudaGraphInstantiate(exec, g, 0));
   cudaGraphDestroy(g);
+  return 0;
+}
+
+// Stage buffer of one checkpoint segment: 4*S slots. A slot holds the stage's
+// input state q and, when memory allows, also its primitive variables, stress
+// and heat flux, so the adjoint stages read them instead of recomputing them.
+static int ensureStageBuffer(Context& c, DevBlock& b, int S) {
+  const long long N = b.v.N;
+  const int nD = c.nD, nU = c.nU;
+  const long long qOnly = (long long)nU * N;
+  const long long full = (long long)(nU + PrimLayout{nD}.count() + nD * nD + nD) * N;
+  const long long needFull = 4LL * S * full;
+  if (c.stageBufCapacity >= needFull) {
+    c.slotStride = full;
+    c.slotFull = 1;
+    return 0;
+  }
+  cudaFree(c.dStageBuf);
+  c.dStageBuf = nullptr;
+  c.stageBufCapacity = 0;
+  size_t freeB = 0, totalB = 0;
+  CUDA_TRY(c, cudaMemGetInfo(&freeB, &totalB));
+  const bool useFull = (double)needFull * sizeof(double) <= 0.5 * (double)freeB;
+  const long long need = useFull ? needFull : 4LL * S * qOnly;
+  CUDA_TRY(c, cudaMalloc((void**)&c.dStageBuf, (size_t)need * sizeof(double)));
+  c.stageBufCapacity = need;
+  c.slotStride = useFull ? full : qOnly;
+  c.slotFull = useFull ? 1 : 0;
   return 0;
 }
 
@@ -1052,10 +1163,7 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
   launchSnapshot(c, b, c.dSnapshots, save_interval, true);
   if (setCounters(c, 1, 0)) return 1;
   if (capture(c, &c.gForward, &c.nodesForward, [&]() {
-        for (int i = 1; i <= 4; ++i) {
-          launchGradFlux(c, b, true, true, false, &rs, i, false);
-          launchForwardRhs(c, b, i, rs, false, functional, controller);
-        }
+        for (int i = 1; i <= 4; ++i) forwardStage(c, b, i, rs, false, controller, false, functional);
         launchSnapshot(c, b, c.dSnapshots, save_interval, false);
         launchStepAdvance(c, 1);
       }))
@@ -1066,7 +1174,7 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
   double J = 0.0;
   if (functional) {
     std::vector<double> vals;
-    if (reduceToHost(c, 4 * n_steps, b.tRhs.blocks(), vals)) return 1;
+    if (reduceToHost(c, 4 * n_steps, vals)) return 1;
     for (int s = 0; s < n_steps; ++s)
       for (int i = 0; i < 4; ++i) J = J + kRkNorm[i] * dt * vals[(size_t)4 * s + i];
   } else {
@@ -1084,31 +1192,26 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   const long long N = b.v.N;
   const int nU = c.nU, T = c.runSteps, S = c.saveInterval;
   const double dt = c.opts.time_step_size;
-  const long long needStage = 4LL * S * nU * N;
-  if (c.stageBufCapacity < needStage) {
-    cudaFree(c.dStageBuf);
-    CUDA_TRY(c, cudaMalloc((void**)&c.dStageBuf, needStage * sizeof(double)));
-    c.stageBufCapacity = needStage;
-  }
+  if (ensureStageBuffer(c, b, S)) return 1;
   const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
   RunScalars rs = runScalars(c);
+  const bool full = c.slotFull != 0;
   // adjoint initial condition at the final state (its primitives are current)
   launchPrims(c, b, b.v.q, false);
   launchAdjointInitial(c, b, c.opts.adjoint_forcing_switch ? -dt / 6.0 : 0.0);
   if (capture(c, &c.gRecompute, &c.nodesRecompute, [&]() {
-        for (int i = 1; i <= 4; ++i) {
-          launchGradFlux(c, b, true, true, false, &rs, i, true);
-          launchForwardRhs(c, b, i, rs, false, false, controller);
-        }
+        for (int i = 1; i <= 4; ++i) forwardStage(c, b, i, rs, false, controller, true, false);
         launchStepAdvance(c, 1);
       }))
     return 1;
   if (capture(c, &c.gAdjoint, &c.nodesAdjoint, [&]() {
         for (int i = 4; i >= 1; --i) {
-          launchPrims(c, b, nullptr, true, &rs, i);
-          if (c.phys.viscous) launchGradFlux(c, b, false, false, true, &rs, i, false);
-          launchAdjointA(c, b, rs, i, true);
-          launchAdjointB(c, b, i, rs, i, 0.0, false);
+          if (!full) {
+            // restore the forward state of this stage from its slot
+            launchPrims(c, b, nullptr, true, &rs, i);
+            if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs, i, false);
+          }
+          adjointStage(c, b, i, rs, i, 0.0, false, full, true);
         }
         launchStepAdvance(c, -1);
       }))
@@ -1128,7 +1231,7 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   }
   if (checkLaunch(c)) return 1;
   std::vector<double> vals;
-  if (reduceToHost(c, 4 * T, b.tAdjA.blocks(), vals)) return 1;
+  if (reduceToHost(c, 4 * T, vals)) return 1;
   double sum = 0.0;
   for (int n = T; n >= 1; --n)
     for (int i = 4; i >= 1; --i) {
@@ -1151,23 +1254,16 @@ int mgd_get_gradient(mgd_ctx* h, double* host, long long n_entries) {
 
 
 // Times each kernel of one RK stage separately with CUDA events on the
-// context stream: forward -> [K2 gradient/flux, K3 divergence+RK];
-// adjoint -> [primitives, stress, part A, part B]. avg_ms receives the mean
-// duration per launch over `reps` launches of each kernel. The state is
-// left changed (the RK updates run); use it on a scratch context state.
+// context stream, avg_ms receiving the mean duration per launch over `reps`
+// launches. Forward: [gradient/flux, dissipation, divergence+RK, primitives,
+// functional]; adjoint: [core, dissipation, diffusion, assembly+RK,
+// gradient/sensitivity]. The state is left changed (the RK updates run).
 int mgd_profile_stage_kernels(mgd_ctx* h, int mode, int reps, double* avg_ms, int* n_kernels) {
   Context& c = h->c;
   if (requireReady(c)) return 1;
   if (c.runSteps < 1) return fail(c, "mgd_profile_stage_kernels needs a preceding mgd_run_forward");
   DevBlock& b = c.blocks[0];
   RunScalars rs = runScalars(c);
-  const long long needStage = 4LL * std::max(1, c.saveInterval) * c.nU * b.v.N;
-  if (c.stageBufCapacity < needStage) {
-    cudaFree(c.dStageBuf);
-    CUDA_TRY(c, cudaMalloc((void**)&c.dStageBuf, needStage * sizeof(double)));
-    c.stageBufCapacity = needStage;
-    rs.stageBuf = c.dStageBuf;
-  }
   if (setCounters(c, 1, 0)) return 1;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -1185,18 +1281,20 @@ int mgd_profile_stage_kernels(mgd_ctx* h, int mode, int reps, double* avg_ms, in
   };
   launchPrims(c, b, b.v.q, false);
   if (mode == MGD_FORWARD) {
-    avg_ms[0] = timeIt([&] { launchGradFlux(c, b, true, true, false, &rs, 2, false); });
-    avg_ms[1] = timeIt([&] { launchForwardRhs(c, b, 2, rs, false, c.opts.enable_functional != 0, controller); });
-    *n_kernels = 2;
+    avg_ms[0] = timeIt([&] { launchGradFlux(c, b, true, false, &rs, 2, false); });
+    avg_ms[1] = c.phys.dissipation ? timeIt([&] { launchDissipation(c, b, b.v.q, 1.0); }) : 0.0;
+    avg_ms[2] = timeIt([&] { launchForwardDivergence(c, b, 2, rs, false, controller); });
+    avg_ms[3] = timeIt([&] { launchPrims(c, b, b.v.q, false); });
+    avg_ms[4] = c.opts.enable_functional ? timeIt([&] { launchFunctional(c, b, rs, 2); }) : 0.0;
   } else {
-    // the stage slot (step 1, stage 1) of the stage buffer holds a valid state
-    CUDA_TRY(c, cudaMemcpyAsync(c.dStageBuf, b.v.q, (size_t)c.nU * b.v.N * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
-    avg_ms[0] = timeIt([&] { launchPrims(c, b, nullptr, true, &rs, 1); });
-    avg_ms[1] = c.phys.viscous ? timeIt([&] { launchGradFlux(c, b, false, false, true, &rs, 1, false); }) : 0.0;
-    avg_ms[2] = timeIt([&] { launchAdjointA(c, b, rs, 1, true); });
-    avg_ms[3] = timeIt([&] { launchAdjointB(c, b, 3, rs, 3, 0.0, false); });
-    *n_kernels = 4;
+    if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs, 1, false);
+    avg_ms[0] = timeIt([&] { launchAdjointCore(c, b, rs, 3, false); });
+    avg_ms[1] = c.phys.dissipation ? timeIt([&] { launchDissipation(c, b, b.v.lam, -1.0); }) : 0.0;
+    avg_ms[2] = c.phys.viscous ? timeIt([&] { launchAdjointDiffusion(c, b); }) : 0.0;
+    avg_ms[3] = timeIt([&] { launchAdjointAssemble(c, b, 3, rs, 3, 0.0, false, false); });
+    avg_ms[4] = timeIt([&] { launchGradientSensitivity(c, b, rs, 3); });
   }
+  *n_kernels = 5;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (checkLaunch(c)) return 1;

@@ -27,8 +27,12 @@ struct OpTables {
   double left[OP_COUNT][16 * 12];       // depth x width row-major
 };
 
-// One copy per translation unit; only mgd_kernels.cu launches kernels and fills it.
+// One copy per translation unit; only mgd_kernels.cu launches kernels and
+// fills them. Interior coefficients are uniform across a warp and live in
+// constant memory; boundary-closure rows differ between lanes and are read
+// from global memory through L1, which serves divergent addresses at once.
 static __constant__ OpTables c_ops;
+static __device__ double g_opLeft[OP_COUNT][16 * 12];
 
 // One direction of a block: n points along it, memory stride, periodicity.
 struct Axis {
@@ -58,20 +62,20 @@ __device__ __forceinline__ double applyOp(const double* __restrict__ line, int i
   if (ax.per == 0) {
     if (i < S::depth) {
       // boundary closure rows are rare: keep them compact (few registers)
-      const double* __restrict__ row = &c_ops.left[OP][i * S::width];
-      double s = row[0] * __ldg(line);
+      const double* __restrict__ row = &g_opLeft[OP][i * S::width];
+      double s = __ldg(row) * __ldg(line);
 #pragma unroll 1
-      for (int k = 1; k < S::width; ++k) s += row[k] * __ldg(line + k * st);
+      for (int k = 1; k < S::width; ++k) s += __ldg(row + k) * __ldg(line + k * st);
       return s;
     }
     if (i >= ax.n - S::depth) {
       const int m = ax.n - 1 - i;
-      const double* __restrict__ row = &c_ops.left[OP][m * S::width];
+      const double* __restrict__ row = &g_opLeft[OP][m * S::width];
       const double* __restrict__ end = line + (long long)(ax.n - S::width) * st;
       // right block = reflection of the left block, negated for skew operators
-      double s = row[S::width - 1] * __ldg(end);
+      double s = __ldg(row + S::width - 1) * __ldg(end);
 #pragma unroll 1
-      for (int k = 1; k < S::width; ++k) s += row[S::width - 1 - k] * __ldg(end + k * st);
+      for (int k = 1; k < S::width; ++k) s += __ldg(row + S::width - 1 - k) * __ldg(end + k * st);
       return S::skew ? -s : s;
     }
     const double* __restrict__ c = line + (long long)i * st;

@@ -34,7 +34,7 @@ struct FarFieldEntries {
   double* M = nullptr;       // nU*nU: inviscidPenaltyAmount * jacobian * A+(target), column-major
   double* sigV = nullptr;    // viscousPenaltyAmount * jacobian
   double* sigVRaw = nullptr; // viscousPenaltyAmount
-  double* visc = nullptr;    // nU: viscous flux contracted with the normal metric (current state)
+  double* visc = nullptr;    // nU: SAT vector of the entry at the current stage (forward or adjoint)
   double* viscT = nullptr;   // nU: the same for the target state
 };
 
@@ -64,6 +64,7 @@ struct BlockView {
   double* dq;     // nD x nU (composite dissipation: nU, already scaled)
   double* rcore;  // nU
   double* ad;     // nD x (nU-1)
+  double* t2;     // nU-1: divergence of the adjoint viscous diffusion
   double* adjF;   // nU: stored cost-target adjoint forcing (per-call API path)
   // patches
   const double* sponge;   // summed sponge strength
@@ -77,6 +78,10 @@ struct BlockView {
   const int* ffOfPoint;   // 3 far-field entry indices per point, -1 if none
   const double* srcG;     // nSources x N: exp(-gaussianFactor r^2), 0 on holes
   int nSources;
+  const int* tgtPts;      // points with a cost-target quadrature weight
+  int nTgt;
+  const int* actPts;      // grid point of each actuator-patch point, patch order
+  int nAct;
   FarFieldEntries ff;
 };
 
@@ -108,7 +113,9 @@ struct RunScalars {
   double* gradient;       // gradient entries, P each (file order)
   double* partials;       // block partial sums per stage slot
   int nPartialBlocks;
-  double* stageBuf;       // stage inputs of the current segment (4*S slots of nU*N)
+  double* stageBuf;       // stage inputs of the current segment (4*S slots)
+  long long slotStride;   // doubles per stage slot
+  int slotFull;           // slots hold q, primitives, stress and heat flux (else q only)
   double dt;
   int adjointForcingSwitch;
 };
@@ -117,7 +124,7 @@ struct DevBlock {
   mgd_block_desc desc;
   BlockView v;
   // tile shapes of the stage kernels, chosen by the autotuner
-  Tile tGrad{}, tRhs{}, tAdjA{}, tAdjB{};
+  Tile tGrad{}, tDiss{}, tRhs{}, tAdjA{}, tAdjD{}, tAdjB{};
   std::vector<void*> allocations;
   int nStagePartialBlocks = 0;
   // host copies kept for setup
@@ -134,6 +141,8 @@ struct Context {
   Physics phys;
   int nD = 2, nU = 4;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;          // second stream for concurrent graph branches
+  cudaEvent_t evFork[8] = {}, evJoin[8] = {};
   int device = 0;
   std::string error;
   std::vector<DevBlock> blocks;
@@ -163,41 +172,61 @@ struct Context {
   long long snapshotCapacity = 0;
   double* dStageBuf = nullptr;
   long long stageBufCapacity = 0;
+  long long slotStride = 0;         // doubles per stage slot of dStageBuf
+  int slotFull = 0;                 // slots also hold primitives, stress and heat flux
   cudaGraphExec_t gForward = nullptr, gRecompute = nullptr, gAdjoint = nullptr;
   long long nodesForward = 0, nodesRecompute = 0, nodesAdjoint = 0;
 };
 
+// ----- stage orchestration (mgd_api.cu) -----
+void forwardStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bool api, bool controller, bool store,
+                  bool functional);
+void adjointStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage, double apiFactor, bool api,
+                  bool fromSlot, bool record);
+
 // ----- launchers (mgd_kernels.cu) -----
+// Every launcher takes the stream it launches on; the context stream when 0.
 void uploadOperatorTables();
-// K1: primitive variables of qSrc (or, when fromStage, of the stage-buffer slot
-// of the current step/stage); copyToQ also stores that state as the conserved variables.
+// Primitive variables of qSrc (or, when stage > 0, of the stage-buffer slot
+// of the current step and stage); copyToQ also stores that state as q.
 void launchPrims(Context& c, DevBlock& b, const double* qSrc, bool copyToQ, const RunScalars* rs = nullptr,
-                 int stage = 0);
-// K2: gradient, stress, fluxes, dissipation stage 1
-void launchGradFlux(Context& c, DevBlock& b, bool writeFlux, bool writeDiss, bool writeStress,
-                    const RunScalars* rs, int stage, bool storeStage);
-// K3: divergence, dissipation stage 2, patches, then either write rhs (rkStage = 0)
-// or fuse the RK4 forward update of stage rkStage
-void launchForwardRhs(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bool api,
-                      bool accumulateFunctional, bool controller);
-void launchAdjointA(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool record);
-void launchAdjointB(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage,
-                    double apiFactor, bool api);
+                 int stage = 0, cudaStream_t s = 0);
+// Gradients, stress, heat flux and contravariant fluxes (flags GF_*).
+void launchGradFlux(Context& c, DevBlock& b, bool writeFlux, bool writeStress, const RunScalars* rs, int stage,
+                    bool storeStage, cudaStream_t s = 0);
+// Artificial dissipation of src (q forward, lambda adjoint) into b.v.dq,
+// scaled by sign (+1 forward, -1 adjoint).
+void launchDissipation(Context& c, DevBlock& b, const double* src, double sign, cudaStream_t s = 0);
+// Flux divergence, dissipation, 1/det, SATs, sources, then the RK4 forward
+// update of rkStage (or, for rkStage = 0, the RHS into b.v.rhs).
+void launchForwardDivergence(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bool api, bool controller,
+                             cudaStream_t s = 0);
+// Functional partial sums of the state just produced (stage slot of step/stage).
+void launchFunctional(Context& c, DevBlock& b, const RunScalars& rs, int stage, cudaStream_t s = 0);
+// Adjoint: inviscid/viscous Jacobian-transpose products and viscous diffusion.
+void launchAdjointCore(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool fromSlot, cudaStream_t s = 0);
+// Adjoint: divergence of the viscous diffusion (per component).
+void launchAdjointDiffusion(Context& c, DevBlock& b, cudaStream_t s = 0);
+// Adjoint: final assembly, SATs, cost-target forcing and the RK4 adjoint update.
+void launchAdjointAssemble(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage, double apiFactor,
+                           bool api, bool fromSlot, cudaStream_t s = 0);
+// Gradient entry and sensitivity partial sums of the adjoint state at a stage.
+void launchGradientSensitivity(Context& c, DevBlock& b, const RunScalars& rs, int stage, cudaStream_t s = 0);
 void launchAdjointInitial(Context& c, DevBlock& b, double factor);
 // Functional%updateAdjointForcing for the per-call API: stores the forcing of
 // the current state (or zeros) in adjF.
 void launchStoreAdjointForcing(Context& c, DevBlock& b, bool zero);
-void launchSnapshot(Context& c, DevBlock& b, double* snapshots, int saveInterval, bool initial);
-void launchStepAdvance(Context& c, int delta);
+void launchSnapshot(Context& c, DevBlock& b, double* snapshots, int saveInterval, bool initial, cudaStream_t s = 0);
+void launchStepAdvance(Context& c, int delta, cudaStream_t s = 0);
 void launchReducePartials(Context& c, const double* partials, int stride, int count, int nSlots, double* out);
 void launchCoordinateDerivative(Context& c, DevBlock& b, int dir, double* out);
 void launchApplyD1(Context& c, DevBlock& b, int dir, const double* in, double* out, int ncomp);
 void launchFarFieldMatricesWith(Context& c, DevBlock& b, const double* sigInv, const int* signedNormal);
 void launchFarFieldTargetVisc(Context& c, DevBlock& b);
-int stageBlocks(const DevBlock& b);
+// Blocks of the fixed-layout reductions (functional, sensitivity).
+int reductionBlocks(const DevBlock& b);
 void launchPowSelfTest(const double* x, int n, double e, double* fast, double* ref);
 Tile makeTile(const DevBlock& b, int tx, int ty, int tz);
-int maxTileBlocks(const DevBlock& b);
 
 }  // namespace mgd
 

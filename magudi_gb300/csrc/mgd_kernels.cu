@@ -1,11 +1,16 @@
 // mgd_kernels.cu -- FP64 kernels of the forward and discrete-adjoint RHS and
 // the RK4 stage updates, plus the setup kernels (grid metrics, far-field SAT
-// matrices). One thread per grid point; stencil taps are read through the
-// read-only cache. Each RK stage is two kernels forward (K2: gradients,
-// stress, fluxes, first dissipation sweep; K3: flux divergence, second
-// dissipation sweep, SATs, sources, RK update, primitive variables of the new
-// state, functional partial sums) and four adjoint (forward-state update x2,
-// adjoint part A, adjoint part B with the RK update).
+// matrices). Stencil taps are read through the read-only cache.
+//
+// Forward RK stage: kGradFlux (one thread per point: gradients, stress,
+// contravariant fluxes, far-field SAT vector) runs beside kDissipation (one
+// thread per point and component); kForwardDivergence (one thread per point
+// and component) adds the flux divergence, dissipation, SATs and sources and
+// applies the RK update; kPrims refreshes the primitive variables and
+// kFunctional sums the cost functional over the cost-target points.
+// Adjoint RK stage: kAdjointCore (per point) beside kDissipation and
+// kGradientSensitivity; kAdjointDiffusion and kAdjointAssemble (per point and
+// component) finish the adjoint RHS and its RK update.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -47,14 +52,6 @@ Tile makeTile(const DevBlock& b, int tx, int ty, int tz) {
   return t;
 }
 
-// Partial sums are laid out per stage slot with room for the largest tiling.
-int maxTileBlocks(const DevBlock& b) {
-  int m = 0;
-  for (const Tile* t : {&b.tGrad, &b.tRhs, &b.tAdjA, &b.tAdjB}) m = std::max(m, t->blocks());
-  return std::max(m, 1);
-}
-
-int stageBlocks(const DevBlock& b) { return maxTileBlocks(b); }
 
 void uploadOperatorTables() {
   static bool done[64] = {false};
@@ -74,6 +71,7 @@ void uploadOperatorTables() {
     for (size_t j = 0; j < ops[o]->left.size(); ++j) t.left[o][j] = ops[o]->left[j];
   }
   cudaMemcpyToSymbol(c_ops, &t, sizeof t);
+  cudaMemcpyToSymbol(g_opLeft, t.left, sizeof t.left);
   cudaMemcpyToSymbol(c_norm, d1.norm.data(), 8 * sizeof(double));
   uploadPowTables();
   if (dev < 64) done[dev] = true;
@@ -148,7 +146,7 @@ __device__ __forceinline__ double blockSum(double v) {
 }
 
 // ---------------------------------------------------------------------------
-// K1: primitive variables (State%update pointwise part, src/StateImpl.f90:466-492)
+// Primitive variables (State%update pointwise part, src/StateImpl.f90:466-492)
 // ---------------------------------------------------------------------------
 template <int ND>
 __global__ void __launch_bounds__(kBlock) kPrims(BlockView B, Physics P, const double* __restrict__ qSrc,
@@ -158,7 +156,7 @@ __global__ void __launch_bounds__(kBlock) kPrims(BlockView B, Physics P, const d
   constexpr int nU = ND + 2;
   if (stage > 0) {
     const int slot = ((*rs.step) - (*rs.segBase) - 1) * 4 + stage - 1;
-    qSrc = rs.stageBuf + (long long)slot * nU * B.N;
+    qSrc = rs.stageBuf + (long long)slot * rs.slotStride;
   }
   double q[nU], pr[6 + ND];
   for (int c = 0; c < nU; ++c) q[c] = qSrc[p + B.N * c];
@@ -168,14 +166,35 @@ __global__ void __launch_bounds__(kBlock) kPrims(BlockView B, Physics P, const d
   for (int c = 0; c < 6 + ND; ++c) B.prim[p + B.N * c] = pr[c];
 }
 
+// Forward-state arrays seen by the adjoint kernels: the block's own arrays, or
+// the stage-buffer slot of the current step and stage when the checkpoint
+// recomputation stored primitives, stress and heat flux with the state.
+struct FwdState {
+  const double* q;
+  const double* prim;
+  const double* tau;
+  const double* hf;
+};
+
+template <int ND>
+__device__ __forceinline__ FwdState forwardState(const BlockView& B, const RunScalars& rs, int stage, bool fromSlot) {
+  if (!fromSlot) return {B.q, B.prim, B.tau, B.hf};
+  const int slot = ((*rs.step) - (*rs.segBase) - 1) * 4 + stage - 1;
+  const double* base = rs.stageBuf + (long long)slot * rs.slotStride;
+  const long long N = B.N;
+  const double* prim = base + (ND + 2) * N;
+  const double* tau = prim + (6 + ND) * N;
+  return {base, prim, tau, tau + ND * ND * N};
+}
+
 // ---------------------------------------------------------------------------
-// K2: velocity and temperature gradients, stress and heat flux (State%update,
+// Velocity and temperature gradients, stress and heat flux (State%update,
 // src/StateImpl.f90:494-533 with Grid%computeGradient, src/GridImpl.f90:1172-1421),
 // Cartesian inviscid and viscous fluxes transformed to contravariant form
-// (computeRhsForward, src/RhsHelperImpl.f90:295-339) and the first sweep of
-// the artificial dissipation (addDissipation, src/RhsHelperImpl.f90:54-66).
+// (computeRhsForward, src/RhsHelperImpl.f90:295-339), and the complete
+// far-field SAT vector of each boundary point (src/FarFieldPatchImpl.f90:227-235).
 // ---------------------------------------------------------------------------
-enum { GF_FLUX = 1, GF_DISS = 2, GF_STRESS = 4, GF_STORE = 8 };
+enum { GF_FLUX = 1, GF_STRESS = 4, GF_STORE = 8 };
 
 template <int ND, bool CURV, bool VISC>
 __global__ void __launch_bounds__(kMaxTile) kGradFlux(BlockView B, Physics P, RunScalars rs, int flags,
@@ -188,10 +207,13 @@ __global__ void __launch_bounds__(kMaxTile) kGradFlux(BlockView B, Physics P, Ru
   const PrimLayout L{ND};
   double q[nU];
   for (int c = 0; c < nU; ++c) q[c] = B.q[p + N * c];
+  double* slot = nullptr;
   if (flags & GF_STORE) {
-    const int slot = ((*rs.step) - (*rs.segBase) - 1) * 4 + stage - 1;
-    double* dst = rs.stageBuf + (long long)slot * nU * N;
-    for (int c = 0; c < nU; ++c) dst[p + N * c] = q[c];
+    const int s = ((*rs.step) - (*rs.segBase) - 1) * 4 + stage - 1;
+    slot = rs.stageBuf + (long long)s * rs.slotStride;
+    for (int c = 0; c < nU; ++c) slot[p + N * c] = q[c];
+    if (rs.slotFull)
+      for (int c = 0; c < 6 + ND; ++c) slot[p + N * (nU + c)] = B.prim[p + N * c];
   }
   double m[ND * ND];
   for (int c = 0; c < ND * ND; ++c) m[c] = (CURV || (c % (ND + 1)) == 0) ? B.metrics[p + N * c] : 0.0;
@@ -201,7 +223,9 @@ __global__ void __launch_bounds__(kMaxTile) kGradFlux(BlockView B, Physics P, Ru
   if (VISC && (flags & (GF_FLUX | GF_STRESS))) {
     const double jac = B.jac[p];
     double du[ND][ND], dT[ND];
+#pragma unroll
     for (int d = 0; d < ND; ++d) {
+#pragma unroll
       for (int c = 0; c < ND; ++c) du[c][d] = applyOp<OP_D1>(B.prim + N * L.u(c) + I.base[d], I.idx[d], B.ax[d]);
       dT[d] = applyOp<OP_D1>(B.prim + N * L.T() + I.base[d], I.idx[d], B.ax[d]);
     }
@@ -239,6 +263,11 @@ __global__ void __launch_bounds__(kMaxTile) kGradFlux(BlockView B, Physics P, Ru
       for (int c = 0; c < ND * ND; ++c) B.tau[p + N * c] = tau[c];
       for (int x = 0; x < ND; ++x) B.hf[p + N * x] = hf[x];
     }
+    if (slot && rs.slotFull) {
+      double* st = slot + N * (nU + 6 + ND);
+      for (int c = 0; c < ND * ND; ++c) st[p + N * c] = tau[c];
+      for (int x = 0; x < ND; ++x) st[p + N * (ND * ND + x)] = hf[x];
+    }
   }
   if (flags & GF_FLUX) {
     const double pr = B.prim[p + N * L.p()];
@@ -252,8 +281,8 @@ __global__ void __launch_bounds__(kMaxTile) kGradFlux(BlockView B, Physics P, Ru
       }
       F[E][d] = u[d] * (q[E] + pr);
     }
+    double Fv[nU][ND];
     if (VISC) {
-      double Fv[nU][ND];
       for (int d = 0; d < ND; ++d) {
         Fv[0][d] = 0.0;
         for (int c = 0; c < ND; ++c) Fv[1 + c][d] = tau[ND * c + d];
@@ -261,19 +290,31 @@ __global__ void __launch_bounds__(kMaxTile) kGradFlux(BlockView B, Physics P, Ru
         for (int c = 1; c < ND; ++c) e += u[c] * tau[ND * c + d];
         Fv[E][d] = e - hf[d];
       }
-      for (int s = 0; s < 3; ++s) {
-        const int e = B.ffOfPoint[3 * p + s];
-        if (e < 0) continue;
-        const double* mn = m + ND * (B.ff.normalDir[e] - 1);
-        for (int r = 0; r < nU; ++r) {
-          double t = Fv[r][0] * mn[0];
-          for (int d = 1; d < ND; ++d) t += Fv[r][d] * mn[d];
-          B.ff.visc[(long long)e * nU + r] = t;
+    }
+    for (int s = 0; s < 3; ++s) {
+      const int e = B.ffOfPoint[3 * p + s];
+      if (e < 0) continue;
+      // sat = -sigma_inv J A+ (q - q_target) + sigma_visc J (F_v - F_v,target) . m
+      const double* M = B.ff.M + (long long)e * nU * nU;
+      double dqv[nU];
+      for (int c = 0; c < nU; ++c) dqv[c] = q[c] - B.qt[p + N * c];
+      double mn[ND];  // metric row of the normal direction, read from memory (no dynamic register index)
+      for (int d = 0; d < ND; ++d) mn[d] = B.metrics[p + N * (ND * (B.ff.normalDir[e] - 1) + d)];
+      for (int r = 0; r < nU; ++r) {
+        double t = M[r] * dqv[0];
+        for (int c = 1; c < nU; ++c) t += M[r + nU * c] * dqv[c];
+        double sat = -t;
+        if (VISC) {
+          double f = Fv[r][0] * mn[0];
+          for (int d = 1; d < ND; ++d) f += Fv[r][d] * mn[d];
+          sat += B.ff.sigV[e] * (f - B.ff.viscT[(long long)e * nU + r]);
         }
+        B.ff.visc[(long long)e * nU + r] = sat;
       }
+    }
+    if (VISC)
       for (int r = 1; r < nU; ++r)
         for (int d = 0; d < ND; ++d) F[r][d] = F[r][d] - Fv[r][d];
-    }
     for (int i = 0; i < ND; ++i)
       for (int c = 0; c < nU; ++c) {
         double s;
@@ -286,368 +327,346 @@ __global__ void __launch_bounds__(kMaxTile) kGradFlux(BlockView B, Physics P, Ru
         B.fhat[p + N * (i * nU + c)] = s;
       }
   }
-  if (flags & GF_DISS) {
-    if (P.composite) {
-      // addDissipation composite path: amount * sum_i D_comp,i q
-      for (int c = 0; c < nU; ++c) {
-        double s = applyOp<OP_DCOMP>(B.q + N * c + I.base[0], I.idx[0], B.ax[0]);
-        for (int d = 1; d < ND; ++d) s += applyOp<OP_DCOMP>(B.q + N * c + I.base[d], I.idx[d], B.ax[d]);
-        B.dq[p + N * c] = P.dissipationAmount * s;
-      }
-    } else {
-      for (int d = 0; d < ND; ++d) {
-        const double a = B.arcA[p + N * d];
-        for (int c = 0; c < nU; ++c)
-          B.dq[p + N * (d * nU + c)] = a * applyOp<OP_DISS>(B.q + N * c + I.base[d], I.idx[d], B.ax[d]);
-      }
-    }
-  }
 }
 
 // ---------------------------------------------------------------------------
-// K3: forward RHS (computeRhsForward + Region%computeRhs,
-// src/RhsHelperImpl.f90:330-351, src/RegionImpl.f90:1968-2023) fused with the
-// RK4 forward stage update (src/RK4IntegratorImpl.f90:104-158), the
-// primitive variables of the new state and the functional's partial sums.
+// Artificial dissipation (addDissipation, src/RhsHelperImpl.f90:10-87), one
+// thread per point and component. Composite: dq_c = sign * amount * sum_i
+// Dc_i src_c. Non-composite, first sweep: dq_{i,c} = sign * (-amount arc_i) D_i src_c.
 // ---------------------------------------------------------------------------
 template <int ND>
-__global__ void __launch_bounds__(kMaxTile) kForwardRhs(BlockView B, Physics P, RunScalars rs, int rkStage,
-                                                        int stage, int accumulate, int controller, Tile T) {
-  long long p = 0;
+__global__ void __launch_bounds__(kMaxTile) kDissipation(BlockView B, Physics P, const double* __restrict__ src,
+                                                         double sign, Tile T) {
+  long long p;
   PointIndex I;
-  const bool active = locate(B, T, p, I);
-  constexpr int nU = ND + 2, E = ND + 1;
+  if (!locate(B, T, p, I)) return;
+  constexpr int nU = ND + 2;
+  const int c = blockIdx.y;
   const long long N = B.N;
-  double fval = 0.0;
-  if (active) {
-    double r[nU];
-    for (int c = 0; c < nU; ++c) {
-      double s = applyOp<OP_D1>(B.fhat + N * c + I.base[0], I.idx[0], B.ax[0]);
-      for (int i = 1; i < ND; ++i) s += applyOp<OP_D1>(B.fhat + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
-      r[c] = -s;
-    }
-    if (P.dissipation) {
-      if (P.composite) {
-        for (int c = 0; c < nU; ++c) r[c] += B.dq[p + N * c];
-      } else {
-        for (int c = 0; c < nU; ++c)
-          for (int i = 0; i < ND; ++i)
-            r[c] += applyOp<OP_DISST>(B.dq + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
-      }
-    }
-    const double jac = B.jac[p];
-    for (int c = 0; c < nU; ++c) r[c] = r[c] * jac;
-    double q[nU];
-    for (int c = 0; c < nU; ++c) q[c] = B.q[p + N * c];
-    // far-field SAT (addFarFieldPenalty FORWARD, src/FarFieldPatchImpl.f90:227-235)
-    for (int s = 0; s < 3; ++s) {
-      const int e = B.ffOfPoint[3 * p + s];
-      if (e < 0) continue;
-      const double* M = B.ff.M + (long long)e * nU * nU;
-      double dqv[nU];
-      for (int c = 0; c < nU; ++c) dqv[c] = q[c] - B.qt[p + N * c];
-      for (int row = 0; row < nU; ++row) {
-        double t = M[row] * dqv[0];
-        for (int c = 1; c < nU; ++c) t += M[row + nU * c] * dqv[c];
-        r[row] -= t;
-      }
-      if (P.viscous) {
-        const double sv = B.ff.sigV[e];
-        for (int row = 0; row < nU; ++row)
-          r[row] += sv * (B.ff.visc[(long long)e * nU + row] - B.ff.viscT[(long long)e * nU + row]);
-      }
-    }
-    // sponge (addDamping FORWARD, src/SpongePatchImpl.f90:86-104)
-    const double S = B.sponge[p];
-    if (S != 0.0)
-      for (int c = 0; c < nU; ++c) r[c] -= S * (q[c] - B.qt[p + N * c]);
+  const double* x = src + N * c;
+  if (P.composite) {
+    double s = applyOp<OP_DCOMP>(x + I.base[0], I.idx[0], B.ax[0]);
+    for (int d = 1; d < ND; ++d) s += applyOp<OP_DCOMP>(x + I.base[d], I.idx[d], B.ax[d]);
+    B.dq[p + N * c] = (sign * P.dissipationAmount) * s;
+  } else {
+    for (int d = 0; d < ND; ++d)
+      B.dq[p + N * (d * nU + c)] = (sign * B.arcA[p + N * d]) * applyOp<OP_DISS>(x + I.base[d], I.idx[d], B.ax[d]);
+  }
+}
+
+template <int ND>
+__device__ __forceinline__ double dissipationTerm(const BlockView& B, const Physics& P, const PointIndex& I,
+                                                  long long p, int c) {
+  constexpr int nU = ND + 2;
+  const long long N = B.N;
+  if (P.composite) return B.dq[p + N * c];
+  double s = applyOp<OP_DISST>(B.dq + N * c + I.base[0], I.idx[0], B.ax[0]);
+  for (int i = 1; i < ND; ++i) s += applyOp<OP_DISST>(B.dq + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Forward RHS of one component (computeRhsForward + Region%computeRhs,
+// src/RhsHelperImpl.f90:330-351, src/RegionImpl.f90:1968-2023) fused with
+// that component's RK4 forward stage update (src/RK4IntegratorImpl.f90:104-158).
+// ---------------------------------------------------------------------------
+template <int ND>
+__global__ void __launch_bounds__(kMaxTile) kForwardDivergence(BlockView B, Physics P, RunScalars rs, int rkStage,
+                                                               int stage, int controller, Tile T) {
+  long long p;
+  PointIndex I;
+  if (!locate(B, T, p, I)) return;
+  constexpr int nU = ND + 2, E = ND + 1;
+  const int c = blockIdx.y;
+  const long long N = B.N;
+  double s = applyOp<OP_D1>(B.fhat + N * c + I.base[0], I.idx[0], B.ax[0]);
+  for (int i = 1; i < ND; ++i) s += applyOp<OP_D1>(B.fhat + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
+  double r = -s;
+  if (P.dissipation) r += dissipationTerm<ND>(B, P, I, p, c);
+  r = r * B.jac[p];
+  for (int k = 0; k < 3; ++k) {
+    const int e = B.ffOfPoint[3 * p + k];
+    if (e >= 0) r += B.ff.visc[(long long)e * nU + c];
+  }
+  const long long kc = p + N * c;
+  const double q = B.q[kc];
+  const double S = B.sponge[p];
+  if (S != 0.0) r -= S * (q - B.qt[kc]);
+  if (c == E) {
     const int step = *rs.step;
-    // actuator (updateActuatorPatch FORWARD, src/ActuatorPatchImpl.f90:134-168)
     if (controller) {
       const int ai = B.actIdx[p];
       if (ai >= 0) {
         const long long e = (long long)(rs.nSteps - step) * 4 + (4 - stage);
-        if (e >= 0 && e < rs.nForcingEntries) r[E] += B.mc[p] * rs.forcing[e * rs.P + ai];
+        if (e >= 0 && e < rs.nForcingEntries) r += B.mc[p] * rs.forcing[e * rs.P + ai];
       }
     }
-    // acoustic sources (AcousticSource%add, src/AcousticSourceImpl.f90:34-64)
     if (B.nSources > 0) {
       const double* amp = rs.amp + ((long long)(step - 1) * 4 + (stage - 1)) * B.nSources;
-      for (int s = 0; s < B.nSources; ++s) r[E] += amp[s] * B.srcG[p + N * s];
-    }
-    if (B.iblank[p] == 0)
-      for (int c = 0; c < nU; ++c) r[c] = 0.0;
-    if (rkStage == 0) {
-      for (int c = 0; c < nU; ++c) B.rhs[p + N * c] = r[c];
-    } else {
-      const double h6 = rs.dt / 6.0, h3 = rs.dt / 3.0, h2 = rs.dt / 2.0;
-      double qn[nU];
-      for (int c = 0; c < nU; ++c) {
-        const long long k = p + N * c;
-        switch (rkStage) {
-          case 1:
-            B.b1[k] = q[c];
-            B.b2[k] = q[c] + h6 * r[c];
-            qn[c] = q[c] + h2 * r[c];
-            break;
-          case 2:
-            B.b2[k] = B.b2[k] + h3 * r[c];
-            qn[c] = B.b1[k] + h2 * r[c];
-            break;
-          case 3:
-            B.b2[k] = B.b2[k] + h3 * r[c];
-            qn[c] = B.b1[k] + rs.dt * r[c];
-            break;
-          default:
-            qn[c] = B.b2[k] + h6 * r[c];
-            break;
-        }
-        B.q[k] = qn[c];
-      }
-      double pr[6 + ND];
-      primitives<ND>(qn, P, pr);
-      for (int c = 0; c < 6 + ND; ++c) B.prim[p + N * c] = pr[c];
-      if (accumulate) {
-        const double w = B.wT[p];
-        if (w != 0.0) {
-          const double F = pr[1 + ND] - B.meanP[p];
-          fval = w * (F * F * B.mt[p]);
-        }
-      }
+      for (int k = 0; k < B.nSources; ++k) r += amp[k] * B.srcG[p + N * k];
     }
   }
-  if (accumulate) {
-    const double s = blockSum(fval);
-    if (threadIdx.x == 0) {
-      const int slot = ((*rs.step) - 1) * 4 + (stage - 1);
-      rs.partials[(long long)slot * rs.nPartialBlocks + blockIdx.x] = s;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Adjoint part A (computeRhsAdjoint, src/RhsHelperImpl.f90:398-560, first half):
-// adjoint derivatives of lambda, inviscid minus first-partial viscous
-// Jacobian-transpose products, second-partial viscous products (plus the
-// far-field viscous adjoint penalty of src/RhsHelperImpl.f90:89-250 folded
-// into the same adjoint sweep), the first adjoint dissipation sweep, the
-// gradient entry and the sensitivity partial sums of this stage
-// (src/ThermalActuatorImpl.f90:83-159, 383-443).
-// ---------------------------------------------------------------------------
-template <int ND, bool VISC>
-__global__ void __launch_bounds__(kMaxTile) kAdjointA(BlockView B, Physics P, RunScalars rs, int stage,
-                                                      int record, Tile T) {
-  long long p = 0;
-  PointIndex I;
-  const bool active = locate(B, T, p, I);
-  constexpr int nU = ND + 2, E = ND + 1, nV = ND + 1;
-  const long long N = B.N;
-  const PrimLayout L{ND};
-  double sval = 0.0;
-  if (active) {
-    double w[ND][nU];
-    for (int i = 0; i < ND; ++i)
-      for (int c = 0; c < nU; ++c) w[i][c] = applyOp<OP_D1ADJ>(B.lam + N * c + I.base[i], I.idx[i], B.ax[i]);
-    double m[ND * ND];
-    for (int c = 0; c < ND * ND; ++c) m[c] = B.metrics[p + N * c];
-    double u[ND];
-    for (int d = 0; d < ND; ++d) u[d] = B.prim[p + N * L.u(d)];
-    const double v = B.prim[p + N * L.v()], T = B.prim[p + N * L.T()];
-    double tau[ND * ND], hf[ND];
-    if (VISC) {
-      for (int c = 0; c < ND * ND; ++c) tau[c] = B.tau[p + N * c];
-      for (int d = 0; d < ND; ++d) hf[d] = B.hf[p + N * d];
-    }
-    double y[nU];
-    for (int c = 0; c < nU; ++c) y[c] = 0.0;
-    for (int i = 0; i < ND; ++i)
-      addFluxJacobianTransposeProduct<ND, VISC>(m + ND * i, u, T, v, P.g, P.powerLawExponent, tau, hf, w[i], y);
-    for (int c = 0; c < nU; ++c) B.rcore[p + N * c] = y[c];
-    double lp[nU];
-    for (int c = 0; c < nU; ++c) lp[c] = B.lam[p + N * c];
-    if (VISC) {
-      const double mu = B.prim[p + N * L.mu()], la = B.prim[p + N * L.la()], kd = B.prim[p + N * L.k()];
-      const double jac = B.jac[p];
-      double ad[ND][nV];
-      for (int j = 0; j < ND; ++j) {
-        for (int c = 0; c < nV; ++c) ad[j][c] = 0.0;
-        for (int i = 0; i < ND; ++i)
-          secondPartialViscousTransposeProduct<ND>(u, mu, la, kd, jac, m + ND * i, m + ND * j, &w[i][1], ad[j]);
-      }
-      for (int s = 0; s < 3; ++s) {
-        const int e = B.ffOfPoint[3 * p + s];
-        if (e < 0) continue;
-        const double* mn = m + ND * (B.ff.normalDir[e] - 1);
-        const double sv = B.ff.sigVRaw[e];
-        for (int l = 0; l < ND; ++l) {
-          double t[nV];
-          for (int c = 0; c < nV; ++c) t[c] = 0.0;
-          secondPartialViscousTransposeProduct<ND>(u, mu, la, kd, jac, mn, m + ND * l, &lp[1], t);
-          for (int c = 0; c < nV; ++c) ad[l][c] += sv * t[c];
-        }
-      }
-      for (int j = 0; j < ND; ++j)
-        for (int c = 0; c < nV; ++c) B.ad[p + N * (j * nV + c)] = ad[j][c];
-    }
-    if (P.dissipation) {
-      if (P.composite) {
-        for (int c = 0; c < nU; ++c) {
-          double s = applyOp<OP_DCOMP>(B.lam + N * c + I.base[0], I.idx[0], B.ax[0]);
-          for (int d = 1; d < ND; ++d) s += applyOp<OP_DCOMP>(B.lam + N * c + I.base[d], I.idx[d], B.ax[d]);
-          B.dq[p + N * c] = -P.dissipationAmount * s;
-        }
-      } else {
-        for (int d = 0; d < ND; ++d) {
-          const double a = -B.arcA[p + N * d];
-          for (int c = 0; c < nU; ++c)
-            B.dq[p + N * (d * nU + c)] = a * applyOp<OP_DISS>(B.lam + N * c + I.base[d], I.idx[d], B.ax[d]);
-        }
-      }
-    }
-    if (record) {
-      const long long entry = (long long)(rs.nSteps - *rs.step) * 4 + (4 - stage);
-      const double g = lp[E] * B.mc[p];
-      const int ai = B.actIdx[p];
-      if (ai >= 0) rs.gradient[entry * rs.P + ai] = g;
-      const double wA = B.wA[p];
-      if (wA != 0.0) sval = wA * (g * g);
-    }
-  }
-  if (record) {
-    const double s = blockSum(sval);
-    if (threadIdx.x == 0) {
-      const long long entry = (long long)(rs.nSteps - *rs.step) * 4 + (4 - stage);
-      rs.partials[entry * rs.nPartialBlocks + blockIdx.x] = s;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Adjoint part B: adjoint divergence of the viscous diffusion term and its
-// primitive-to-conservative map (src/RhsHelperImpl.f90:562-582), the second
-// adjoint dissipation sweep, 1/det, the far-field / sponge / cost-target
-// adjoint terms (src/FarFieldPatchImpl.f90:237-257, src/SpongePatchImpl.f90:
-// 106-124, src/CostTargetPatchImpl.f90:72-136 with the AcousticNoise forcing
-// of src/AcousticNoiseImpl.f90:208-280) and the RK4 adjoint stage update
-// (src/RK4IntegratorImpl.f90:203-266).
-// ---------------------------------------------------------------------------
-template <int ND, bool VISC>
-__global__ void __launch_bounds__(kMaxTile) kAdjointB(BlockView B, Physics P, RunScalars rs, int rkStage,
-                                                      int stage, double apiFactor, int api, Tile T) {
-  long long p;
-  PointIndex I;
-  if (!locate(B, T, p, I)) return;
-  constexpr int nU = ND + 2, E = ND + 1, nV = ND + 1;
-  const long long N = B.N;
-  const PrimLayout L{ND};
-  double r[nU];
-  for (int c = 0; c < nU; ++c) r[c] = B.rcore[p + N * c];
-  double u[ND];
-  for (int d = 0; d < ND; ++d) u[d] = B.prim[p + N * L.u(d)];
-  const double v = B.prim[p + N * L.v()];
-  if (VISC) {
-    double t2[nV];
-    for (int c = 0; c < nV; ++c) {
-      double s = applyOp<OP_D1ADJ>(B.ad + N * c + I.base[0], I.idx[0], B.ax[0]);
-      for (int j = 1; j < ND; ++j) s += applyOp<OP_D1ADJ>(B.ad + N * (j * nV + c) + I.base[j], I.idx[j], B.ax[j]);
-      t2[c] = s;
-    }
-    const double xE = P.g * v * t2[ND];
-    double x[ND];
-    for (int d = 0; d < ND; ++d) x[d] = v * t2[d] - u[d] * xE;
-    for (int d = 0; d < ND; ++d) r[1 + d] -= x[d];
-    r[E] -= xE;
-    double su = u[0] * x[0];
-    for (int d = 1; d < ND; ++d) su += u[d] * x[d];
-    r[0] += v * B.q[p + N * E] * xE + su;
-  }
-  if (P.dissipation) {
-    if (P.composite) {
-      for (int c = 0; c < nU; ++c) r[c] += B.dq[p + N * c];
-    } else {
-      for (int c = 0; c < nU; ++c)
-        for (int i = 0; i < ND; ++i)
-          r[c] += applyOp<OP_DISST>(B.dq + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
-    }
-  }
-  const double jac = B.jac[p];
-  for (int c = 0; c < nU; ++c) r[c] = r[c] * jac;
-  double lp[nU];
-  for (int c = 0; c < nU; ++c) lp[c] = B.lam[p + N * c];
-  for (int s = 0; s < 3; ++s) {
-    const int e = B.ffOfPoint[3 * p + s];
-    if (e < 0) continue;
-    const double* M = B.ff.M + (long long)e * nU * nU;
-    for (int row = 0; row < nU; ++row) {
-      double t = M[nU * row] * lp[0];
-      for (int c = 1; c < nU; ++c) t += M[c + nU * row] * lp[c];
-      r[row] += t;
-    }
-    if (VISC) {
-      double m[ND], tau[ND * ND], hf[ND], y[nU];
-      const int nd = B.ff.normalDir[e] - 1;
-      for (int d = 0; d < ND; ++d) m[d] = B.metrics[p + N * (ND * nd + d)];
-      for (int c = 0; c < ND * ND; ++c) tau[c] = B.tau[p + N * c];
-      for (int d = 0; d < ND; ++d) hf[d] = B.hf[p + N * d];
-      for (int c = 0; c < nU; ++c) y[c] = 0.0;
-      firstPartialViscousTransposeProduct<ND>(m, u, B.prim[p + N * L.T()], v, P.g, P.powerLawExponent, tau, hf, lp, y);
-      const double sv = B.ff.sigV[e];
-      for (int c = 0; c < nU; ++c) r[c] -= sv * y[c];
-    }
-  }
-  const double S = B.sponge[p];
-  if (S != 0.0)
-    for (int c = 0; c < nU; ++c) r[c] += S * lp[c];
-  const double cnt = B.tgtCount[p];
-  if (api) {
-    // per-call path: the forcing stored by the last updateAdjointForcing
-    if (cnt != 0.0 && apiFactor != 0.0)
-      for (int c = 0; c < nU; ++c) r[c] += apiFactor * B.adjF[p + N * c];
-  } else if (cnt != 0.0) {
-    double factor;
-    {
-      const bool finalStage = (*rs.step == 1 && stage == 1);
-      factor = (!rs.adjointForcingSwitch || finalStage) ? 0.0
-               : (stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0));
-    }
-    if (factor != 0.0) {
-      const double F = -2.0 * B.mt[p] * P.gm1 * (B.prim[p + N * L.p()] - B.meanP[p]);
-      double u2 = u[0] * u[0];
-      for (int d = 1; d < ND; ++d) u2 += u[d] * u[d];
-      for (int k = 0; k < (int)cnt; ++k) {
-        r[E] += factor * F;
-        for (int d = 0; d < ND; ++d) r[1 + d] += factor * (-u[d] * F);
-        r[0] += factor * (0.5 * u2 * F);
-      }
-    }
-  }
-  if (B.iblank[p] == 0)
-    for (int c = 0; c < nU; ++c) r[c] = 0.0;
+  if (B.iblank[p] == 0) r = 0.0;
   if (rkStage == 0) {
-    for (int c = 0; c < nU; ++c) B.rhs[p + N * c] = r[c];
+    B.rhs[kc] = r;
     return;
   }
   const double h6 = rs.dt / 6.0, h3 = rs.dt / 3.0, h2 = rs.dt / 2.0;
-  for (int c = 0; c < nU; ++c) {
-    const long long k = p + N * c;
-    switch (rkStage) {
-      case 4:
-        B.b1[k] = lp[c];
-        B.b2[k] = lp[c] - h6 * r[c];
-        B.lam[k] = lp[c] - h2 * r[c];
-        break;
-      case 3:
-        B.b2[k] = B.b2[k] - h3 * r[c];
-        B.lam[k] = B.b1[k] - h2 * r[c];
-        break;
-      case 2:
-        B.b2[k] = B.b2[k] - h3 * r[c];
-        B.lam[k] = B.b1[k] - rs.dt * r[c];
-        break;
-      default:
-        B.lam[k] = B.b2[k] - h6 * r[c];
-        break;
+  switch (rkStage) {
+    case 1:
+      B.b1[kc] = q;
+      B.b2[kc] = q + h6 * r;
+      B.q[kc] = q + h2 * r;
+      break;
+    case 2:
+      B.b2[kc] = B.b2[kc] + h3 * r;
+      B.q[kc] = B.b1[kc] + h2 * r;
+      break;
+    case 3:
+      B.b2[kc] = B.b2[kc] + h3 * r;
+      B.q[kc] = B.b1[kc] + rs.dt * r;
+      break;
+    default:
+      B.q[kc] = B.b2[kc] + h6 * r;
+      break;
+  }
+}
+
+// Functional (AcousticNoise%compute, src/AcousticNoiseImpl.f90:123-206) of the
+// state whose primitives are current: partial sums over the cost-target points,
+// fixed block layout, into the slot of (step, stage).
+__global__ void __launch_bounds__(kBlock) kFunctional(BlockView B, RunScalars rs, int stage, int pressureComp) {
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  double v = 0.0;
+  if (i < B.nTgt) {
+    const long long p = B.tgtPts[i];
+    const double F = B.prim[p + B.N * pressureComp] - B.meanP[p];
+    v = B.wT[p] * (F * F * B.mt[p]);
+  }
+  const double s = blockSum(v);
+  if (threadIdx.x == 0) {
+    const int slot = ((*rs.step) - 1) * 4 + (stage - 1);
+    rs.partials[(long long)slot * rs.nPartialBlocks + blockIdx.x] = s;
+  }
+}
+
+// Gradient entry and sensitivity partial sums of lambda at an adjoint stage
+// (ThermalActuator%updateGradient / computeSensitivity,
+// src/ThermalActuatorImpl.f90:83-159, 383-443), over the actuator points.
+__global__ void __launch_bounds__(kBlock) kGradientSensitivity(BlockView B, RunScalars rs, int stage, int energyComp) {
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  const long long entry = (long long)(rs.nSteps - *rs.step) * 4 + (4 - stage);
+  double v = 0.0;
+  if (i < B.nAct) {
+    const long long p = B.actPts[i];
+    const double g = B.lam[p + B.N * energyComp] * B.mc[p];
+    rs.gradient[entry * rs.P + i] = g;
+    v = B.wA[p] * (g * g);
+  }
+  const double s = blockSum(v);
+  if (threadIdx.x == 0) rs.partials[entry * rs.nPartialBlocks + blockIdx.x] = s;
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint core (computeRhsAdjoint, src/RhsHelperImpl.f90:398-560): adjoint
+// derivatives of lambda, (A - B1)^T products formed column by column, the
+// second-partial viscous diffusion B2^T with the far-field viscous adjoint
+// penalty (src/RhsHelperImpl.f90:89-250) folded into the same sweep, and
+// the complete far-field adjoint SAT vector (src/FarFieldPatchImpl.f90:237-257).
+// ---------------------------------------------------------------------------
+template <int ND, bool VISC>
+__global__ void __launch_bounds__(kMaxTile) kAdjointCore(BlockView B, Physics P, RunScalars rs, int stage,
+                                                         int fromSlot, Tile T) {
+  long long p;
+  PointIndex I;
+  if (!locate(B, T, p, I)) return;
+  constexpr int nU = ND + 2, nV = ND + 1;
+  const long long N = B.N;
+  const PrimLayout L{ND};
+  const FwdState fs = forwardState<ND>(B, rs, stage, fromSlot != 0);
+  double w[ND][nU];
+#pragma unroll
+  for (int i = 0; i < ND; ++i)
+#pragma unroll
+    for (int c = 0; c < nU; ++c) w[i][c] = applyOp<OP_D1ADJ>(B.lam + N * c + I.base[i], I.idx[i], B.ax[i]);
+  double m[ND * ND];
+  for (int c = 0; c < ND * ND; ++c) m[c] = B.metrics[p + N * c];
+  double u[ND];
+  for (int d = 0; d < ND; ++d) u[d] = fs.prim[p + N * L.u(d)];
+  const double v = fs.prim[p + N * L.v()], Tm = fs.prim[p + N * L.T()];
+  double tau[ND * ND], hf[ND];
+  if (VISC) {
+    for (int c = 0; c < ND * ND; ++c) tau[c] = fs.tau[p + N * c];
+    for (int d = 0; d < ND; ++d) hf[d] = fs.hf[p + N * d];
+  }
+  double y[nU];
+  for (int c = 0; c < nU; ++c) y[c] = 0.0;
+#pragma unroll
+  for (int i = 0; i < ND; ++i)
+    addFluxJacobianTransposeProduct<ND, VISC>(m + ND * i, u, Tm, v, P.g, P.powerLawExponent, tau, hf, w[i], y);
+  for (int c = 0; c < nU; ++c) B.rcore[p + N * c] = y[c];
+  double lp[nU];
+  for (int c = 0; c < nU; ++c) lp[c] = B.lam[p + N * c];
+  double mu = 0.0, la = 0.0, kd = 0.0;
+  const double jac = B.jac[p];
+  if (VISC) {
+    mu = fs.prim[p + N * L.mu()];
+    la = fs.prim[p + N * L.la()];
+    kd = fs.prim[p + N * L.k()];
+    double ad[ND][nV];
+    for (int j = 0; j < ND; ++j) {
+      for (int c = 0; c < nV; ++c) ad[j][c] = 0.0;
+#pragma unroll
+      for (int i = 0; i < ND; ++i)
+        secondPartialViscousTransposeProduct<ND>(u, mu, la, kd, jac, m + ND * i, m + ND * j, &w[i][1], ad[j]);
     }
+    for (int k = 0; k < 3; ++k) {
+      const int e = B.ffOfPoint[3 * p + k];
+      if (e < 0) continue;
+      double mn[ND];  // metric row of the normal direction, read from memory (no dynamic register index)
+      for (int d = 0; d < ND; ++d) mn[d] = B.metrics[p + N * (ND * (B.ff.normalDir[e] - 1) + d)];
+      const double sv = B.ff.sigVRaw[e];
+      for (int l = 0; l < ND; ++l) {
+        double t[nV];
+        for (int c = 0; c < nV; ++c) t[c] = 0.0;
+        secondPartialViscousTransposeProduct<ND>(u, mu, la, kd, jac, mn, m + ND * l, &lp[1], t);
+        for (int c = 0; c < nV; ++c) ad[l][c] += sv * t[c];
+      }
+    }
+    for (int j = 0; j < ND; ++j)
+      for (int c = 0; c < nV; ++c) B.ad[p + N * (j * nV + c)] = ad[j][c];
+  }
+  for (int k = 0; k < 3; ++k) {
+    const int e = B.ffOfPoint[3 * p + k];
+    if (e < 0) continue;
+    const double* M = B.ff.M + (long long)e * nU * nU;
+    double z[nU];
+    for (int c = 0; c < nU; ++c) z[c] = 0.0;
+    if (VISC) {
+      double mn[ND];  // metric row of the normal direction, read from memory (no dynamic register index)
+      for (int d = 0; d < ND; ++d) mn[d] = B.metrics[p + N * (ND * (B.ff.normalDir[e] - 1) + d)];
+      firstPartialViscousTransposeProduct<ND>(mn, u, Tm, v, P.g, P.powerLawExponent, tau, hf, lp, z);
+    }
+    const double sv = B.ff.sigV[e];
+    for (int row = 0; row < nU; ++row) {
+      double t = M[nU * row] * lp[0];
+      for (int c = 1; c < nU; ++c) t += M[c + nU * row] * lp[c];
+      B.ff.visc[(long long)e * nU + row] = VISC ? t - sv * z[row] : t;
+    }
+  }
+}
+
+// Divergence of the adjoint viscous diffusion, one thread per point and
+// momentum/energy component: t2_c = sum_j D+_j ad_{j,c} (src/RhsHelperImpl.f90:562-564).
+template <int ND>
+__global__ void __launch_bounds__(kMaxTile) kAdjointDiffusion(BlockView B, Tile T) {
+  long long p;
+  PointIndex I;
+  if (!locate(B, T, p, I)) return;
+  constexpr int nV = ND + 1;
+  const int c = blockIdx.y;
+  const long long N = B.N;
+  double s = applyOp<OP_D1ADJ>(B.ad + N * c + I.base[0], I.idx[0], B.ax[0]);
+  for (int j = 1; j < ND; ++j) s += applyOp<OP_D1ADJ>(B.ad + N * (j * nV + c) + I.base[j], I.idx[j], B.ax[j]);
+  B.t2[p + N * c] = s;
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint assembly of one component: the viscous primitive-to-conservative
+// map (src/RhsHelperImpl.f90:566-582), dissipation, 1/det, far-field /
+// sponge / cost-target terms (src/FarFieldPatchImpl.f90:237-257,
+// src/SpongePatchImpl.f90:106-124, src/CostTargetPatchImpl.f90:72-136 with
+// src/AcousticNoiseImpl.f90:208-280) and the RK4 adjoint stage update of
+// that component (src/RK4IntegratorImpl.f90:203-266).
+// ---------------------------------------------------------------------------
+template <int ND, bool VISC>
+__global__ void __launch_bounds__(kMaxTile) kAdjointAssemble(BlockView B, Physics P, RunScalars rs, int rkStage,
+                                                             int stage, double apiFactor, int api, int fromSlot,
+                                                             Tile T) {
+  long long p;
+  PointIndex I;
+  if (!locate(B, T, p, I)) return;
+  constexpr int nU = ND + 2, E = ND + 1;
+  const int c = blockIdx.y;
+  const long long N = B.N;
+  const PrimLayout L{ND};
+  const FwdState fs = forwardState<ND>(B, rs, stage, fromSlot != 0);
+  double r = B.rcore[p + N * c];
+  const double v = fs.prim[p + N * L.v()];
+  if (VISC) {
+    const double xE = P.g * v * B.t2[p + N * ND];
+    if (c == E) {
+      r -= xE;
+    } else if (c > 0) {
+      r -= v * B.t2[p + N * (c - 1)] - fs.prim[p + N * L.u(c - 1)] * xE;
+    } else {
+      double su = 0.0;
+      for (int d = 0; d < ND; ++d) {
+        const double ud = fs.prim[p + N * L.u(d)];
+        const double xd = v * B.t2[p + N * d] - ud * xE;
+        su = d == 0 ? ud * xd : su + ud * xd;
+      }
+      r += v * fs.q[p + N * E] * xE + su;
+    }
+  }
+  if (P.dissipation) r += dissipationTerm<ND>(B, P, I, p, c);
+  r = r * B.jac[p];
+  for (int k = 0; k < 3; ++k) {
+    const int e = B.ffOfPoint[3 * p + k];
+    if (e >= 0) r += B.ff.visc[(long long)e * nU + c];
+  }
+  const long long kc = p + N * c;
+  const double lam = B.lam[kc];
+  const double S = B.sponge[p];
+  if (S != 0.0) r += S * lam;
+  const double cnt = B.tgtCount[p];
+  if (api) {
+    if (cnt != 0.0 && apiFactor != 0.0) r += apiFactor * B.adjF[kc];
+  } else if (cnt != 0.0) {
+    const bool finalStage = (*rs.step == 1 && stage == 1);
+    const double factor = (!rs.adjointForcingSwitch || finalStage) ? 0.0
+                          : (stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0));
+    if (factor != 0.0) {
+      const double F = -2.0 * B.mt[p] * P.gm1 * (fs.prim[p + N * L.p()] - B.meanP[p]);
+      double f;
+      if (c == E) {
+        f = F;
+      } else if (c > 0) {
+        f = -fs.prim[p + N * L.u(c - 1)] * F;
+      } else {
+        double u2 = 0.0;
+        for (int d = 0; d < ND; ++d) {
+          const double ud = fs.prim[p + N * L.u(d)];
+          u2 = d == 0 ? ud * ud : u2 + ud * ud;
+        }
+        f = 0.5 * u2 * F;
+      }
+      for (int k = 0; k < (int)cnt; ++k) r += factor * f;
+    }
+  }
+  if (B.iblank[p] == 0) r = 0.0;
+  if (rkStage == 0) {
+    B.rhs[kc] = r;
+    return;
+  }
+  const double h6 = rs.dt / 6.0, h3 = rs.dt / 3.0, h2 = rs.dt / 2.0;
+  switch (rkStage) {
+    case 4:
+      B.b1[kc] = lam;
+      B.b2[kc] = lam - h6 * r;
+      B.lam[kc] = lam - h2 * r;
+      break;
+    case 3:
+      B.b2[kc] = B.b2[kc] - h3 * r;
+      B.lam[kc] = B.b1[kc] - h2 * r;
+      break;
+    case 2:
+      B.b2[kc] = B.b2[kc] - h3 * r;
+      B.lam[kc] = B.b1[kc] - rs.dt * r;
+      break;
+    default:
+      B.lam[kc] = B.b2[kc] - h6 * r;
+      break;
   }
 }
 
@@ -837,24 +856,33 @@ void launchPowSelfTest(const double* x, int n, double e, double* fast, double* r
 // ---------------------------------------------------------------------------
 #define MGD_LAUNCH(c) (++(c).launches)
 
-void launchPrims(Context& c, DevBlock& b, const double* qSrc, bool copyToQ, const RunScalars* rs, int stage) {
+static inline cudaStream_t on(const Context& c, cudaStream_t s) { return s ? s : c.stream; }
+
+// Blocks of the fixed-layout reductions: one partial sum per block of the
+// cost-target (functional) and actuator (sensitivity) point lists.
+int reductionBlocks(const DevBlock& b) {
+  return std::max({1, (b.v.nTgt + kBlock - 1) / kBlock, (b.v.nAct + kBlock - 1) / kBlock});
+}
+
+void launchPrims(Context& c, DevBlock& b, const double* qSrc, bool copyToQ, const RunScalars* rs, int stage,
+                 cudaStream_t s) {
   RunScalars r{};
   if (rs) r = *rs;
   MGD_LAUNCH(c);
-  if (c.nD == 2) kPrims<2><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, qSrc, copyToQ, r, stage);
-  else kPrims<3><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, qSrc, copyToQ, r, stage);
+  if (c.nD == 2) kPrims<2><<<gridFor(b.v.N), kBlock, 0, on(c, s)>>>(b.v, c.phys, qSrc, copyToQ, r, stage);
+  else kPrims<3><<<gridFor(b.v.N), kBlock, 0, on(c, s)>>>(b.v, c.phys, qSrc, copyToQ, r, stage);
 }
 
-void launchGradFlux(Context& c, DevBlock& b, bool writeFlux, bool writeDiss, bool writeStress,
-                    const RunScalars* rs, int stage, bool storeStage) {
-  int flags = (writeFlux ? GF_FLUX : 0) | (writeDiss && c.phys.dissipation ? GF_DISS : 0) |
-              (writeStress ? GF_STRESS : 0) | (storeStage ? GF_STORE : 0);
+void launchGradFlux(Context& c, DevBlock& b, bool writeFlux, bool writeStress, const RunScalars* rs, int stage,
+                    bool storeStage, cudaStream_t s) {
+  const int flags = (writeFlux ? GF_FLUX : 0) | (writeStress ? GF_STRESS : 0) | (storeStage ? GF_STORE : 0);
   RunScalars r{};
   if (rs) r = *rs;
   const Tile T = b.tGrad;
   const bool curv = b.v.curvilinear != 0, visc = c.phys.viscous != 0;
   MGD_LAUNCH(c);
-#define GF(ND, CU, VI) kGradFlux<ND, CU, VI><<<T.blocks(), T.threads(), 0, c.stream>>>(b.v, c.phys, r, flags, stage, T)
+#define GF(ND, CU, VI) \
+  kGradFlux<ND, CU, VI><<<T.blocks(), T.threads(), 0, on(c, s)>>>(b.v, c.phys, r, flags, stage, T)
   if (c.nD == 2) {
     if (curv) { if (visc) GF(2, true, true); else GF(2, true, false); }
     else { if (visc) GF(2, false, true); else GF(2, false, false); }
@@ -865,42 +893,75 @@ void launchGradFlux(Context& c, DevBlock& b, bool writeFlux, bool writeDiss, boo
 #undef GF
 }
 
-void launchForwardRhs(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bool api,
-                      bool accumulate, bool controller) {
+void launchDissipation(Context& c, DevBlock& b, const double* src, double sign, cudaStream_t s) {
+  if (!c.phys.dissipation) return;
+  const Tile T = b.tDiss;
+  const dim3 grid(T.blocks(), c.nU);
+  MGD_LAUNCH(c);
+  if (c.nD == 2) kDissipation<2><<<grid, T.threads(), 0, on(c, s)>>>(b.v, c.phys, src, sign, T);
+  else kDissipation<3><<<grid, T.threads(), 0, on(c, s)>>>(b.v, c.phys, src, sign, T);
+}
+
+void launchForwardDivergence(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bool api, bool controller,
+                             cudaStream_t s) {
   const int stage = api ? 1 : rkStage;
   const Tile T = b.tRhs;
+  const dim3 grid(T.blocks(), c.nU);
   MGD_LAUNCH(c);
   if (c.nD == 2)
-    kForwardRhs<2><<<T.blocks(), T.threads(), 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, accumulate, controller, T);
+    kForwardDivergence<2><<<grid, T.threads(), 0, on(c, s)>>>(b.v, c.phys, rs, rkStage, stage, controller, T);
   else
-    kForwardRhs<3><<<T.blocks(), T.threads(), 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, accumulate, controller, T);
+    kForwardDivergence<3><<<grid, T.threads(), 0, on(c, s)>>>(b.v, c.phys, rs, rkStage, stage, controller, T);
 }
 
-void launchAdjointA(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool record) {
+void launchFunctional(Context& c, DevBlock& b, const RunScalars& rs, int stage, cudaStream_t s) {
+  MGD_LAUNCH(c);
+  kFunctional<<<reductionBlocks(b), kBlock, 0, on(c, s)>>>(b.v, rs, stage, PrimLayout{c.nD}.p());
+}
+
+void launchGradientSensitivity(Context& c, DevBlock& b, const RunScalars& rs, int stage, cudaStream_t s) {
+  MGD_LAUNCH(c);
+  kGradientSensitivity<<<reductionBlocks(b), kBlock, 0, on(c, s)>>>(b.v, rs, stage, c.nD + 1);
+}
+
+void launchAdjointCore(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool fromSlot, cudaStream_t s) {
   const Tile T = b.tAdjA;
   const int G = T.blocks(), W = T.threads();
+  cudaStream_t st = on(c, s);
   MGD_LAUNCH(c);
   if (c.nD == 2) {
-    if (c.phys.viscous) kAdjointA<2, true><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, stage, record, T);
-    else kAdjointA<2, false><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, stage, record, T);
+    if (c.phys.viscous) kAdjointCore<2, true><<<G, W, 0, st>>>(b.v, c.phys, rs, stage, fromSlot, T);
+    else kAdjointCore<2, false><<<G, W, 0, st>>>(b.v, c.phys, rs, stage, fromSlot, T);
   } else {
-    if (c.phys.viscous) kAdjointA<3, true><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, stage, record, T);
-    else kAdjointA<3, false><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, stage, record, T);
+    if (c.phys.viscous) kAdjointCore<3, true><<<G, W, 0, st>>>(b.v, c.phys, rs, stage, fromSlot, T);
+    else kAdjointCore<3, false><<<G, W, 0, st>>>(b.v, c.phys, rs, stage, fromSlot, T);
   }
 }
 
-void launchAdjointB(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage, double apiFactor,
-                    bool api) {
-  const Tile T = b.tAdjB;
-  const int G = T.blocks(), W = T.threads();
+void launchAdjointDiffusion(Context& c, DevBlock& b, cudaStream_t s) {
+  if (!c.phys.viscous) return;
+  const Tile T = b.tAdjD;
+  const dim3 grid(T.blocks(), c.nU - 1);
   MGD_LAUNCH(c);
+  if (c.nD == 2) kAdjointDiffusion<2><<<grid, T.threads(), 0, on(c, s)>>>(b.v, T);
+  else kAdjointDiffusion<3><<<grid, T.threads(), 0, on(c, s)>>>(b.v, T);
+}
+
+void launchAdjointAssemble(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage, double apiFactor,
+                           bool api, bool fromSlot, cudaStream_t s) {
+  const Tile T = b.tAdjB;
+  const dim3 grid(T.blocks(), c.nU);
+  const int W = T.threads();
+  cudaStream_t st = on(c, s);
+  MGD_LAUNCH(c);
+#define AA(ND, VI) \
+  kAdjointAssemble<ND, VI><<<grid, W, 0, st>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api, fromSlot, T)
   if (c.nD == 2) {
-    if (c.phys.viscous) kAdjointB<2, true><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api, T);
-    else kAdjointB<2, false><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api, T);
+    if (c.phys.viscous) AA(2, true); else AA(2, false);
   } else {
-    if (c.phys.viscous) kAdjointB<3, true><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api, T);
-    else kAdjointB<3, false><<<G, W, 0, c.stream>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api, T);
+    if (c.phys.viscous) AA(3, true); else AA(3, false);
   }
+#undef AA
 }
 
 void launchAdjointInitial(Context& c, DevBlock& b, double factor) {
@@ -915,15 +976,15 @@ void launchStoreAdjointForcing(Context& c, DevBlock& b, bool zero) {
   else kStoreAdjointForcing<3><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, zero);
 }
 
-void launchSnapshot(Context& c, DevBlock& b, double* snapshots, int saveInterval, bool initial) {
+void launchSnapshot(Context& c, DevBlock& b, double* snapshots, int saveInterval, bool initial, cudaStream_t s) {
   const long long n = b.v.N * b.v.nU;
   MGD_LAUNCH(c);
-  kSnapshot<<<gridFor(n), kBlock, 0, c.stream>>>(snapshots, b.v.q, n, c.dCounters, saveInterval, initial);
+  kSnapshot<<<gridFor(n), kBlock, 0, on(c, s)>>>(snapshots, b.v.q, n, c.dCounters, saveInterval, initial);
 }
 
-void launchStepAdvance(Context& c, int delta) {
+void launchStepAdvance(Context& c, int delta, cudaStream_t s) {
   MGD_LAUNCH(c);
-  kStepAdvance<<<1, 32, 0, c.stream>>>(c.dCounters, delta);
+  kStepAdvance<<<1, 32, 0, on(c, s)>>>(c.dCounters, delta);
 }
 
 void launchReducePartials(Context& c, const double* partials, int stride, int count, int nSlots, double* out) {

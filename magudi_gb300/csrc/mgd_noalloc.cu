@@ -121,12 +121,11 @@ int mgd_forward_rhs_noalloc(mgd_ctx* h, const double* q, double time, double* rh
   rs.amp = scratch;
   rs.dt = c.opts.time_step_size;
   rs.adjointForcingSwitch = c.opts.adjoint_forcing_switch;
-  rs.nPartialBlocks = stageBlocks(b);
+  rs.nPartialBlocks = reductionBlocks(b);
   const BlockView saved = b.v;
   b.v = view;
   launchPrims(c, b, view.q, false);
-  launchGradFlux(c, b, true, true, false, &rs, 1, false);
-  launchForwardRhs(c, b, 0, rs, true, false, false);
+  forwardStage(c, b, 0, rs, true, false, false, false);
   b.v = saved;
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
