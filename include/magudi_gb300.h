@@ -180,10 +180,22 @@ int mgd_set_control_forcing(mgd_ctx* ctx, const double* host, long long n_entrie
 int mgd_actuator_patch_size(mgd_ctx* ctx, long long* n_points);
 
 /* Solver%runForward (src/SolverImpl.f90:672-912) from the current conserved
- * variables at time t0 for n_steps RK4 steps with constant dt; keeps a
- * snapshot every save_interval steps in device memory for a following
- * mgd_run_adjoint. *cost = the time-integrated functional. */
+ * variables at time t0 for n_steps RK4 steps; keeps a snapshot every
+ * save_interval steps in device memory for a following mgd_run_adjoint.
+ * The step size is time_step_size, or in constant-CFL mode the step size of
+ * the state at the start of each step (src/SolverImpl.f90:809), evaluated on
+ * the device. *cost = the time-integrated functional. */
 int mgd_run_forward(mgd_ctx* ctx, int n_steps, int save_interval, double t0, double* cost);
+
+/* Region%getTimeStepSize (src/RegionImpl.f90:1842-1875 with
+ * computeTimeStepSize, src/CNSHelperImpl.f90:913-982): time_step_size, or in
+ * constant-CFL mode the minimum over the grid of the advective and viscous
+ * CFL bounds of the current conserved variables. */
+int mgd_time_step_size(mgd_ctx* ctx, double* dt);
+
+/* Step sizes of the steps of the last mgd_run_forward (n_steps doubles);
+ * the adjoint run uses the same ones. */
+int mgd_get_step_sizes(mgd_ctx* ctx, double* host, int n_steps);
 
 /* Solver%runAdjoint (src/SolverImpl.f90:914-1245) over the horizon of the
  * preceding mgd_run_forward, with UniformCheckpointer recomputation

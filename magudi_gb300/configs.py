@@ -31,14 +31,15 @@ def monopole_2d(n=201, ny=None, dt=0.05, n_steps=960, sponge_points=20, sponge_a
                 dissipation_amount=0.01, reynolds=200.0, prandtl=0.72,
                 power_law=0.666, bulk_viscosity_ratio=0.6, save_interval=10,
                 controller_switch=False, half_width=14.0, target_center=(0.0, 10.0),
-                control_center=(0.0, 0.0), mollifier_sigma=1.0, composite_dissipation=True):
+                control_center=(0.0, 0.0), mollifier_sigma=1.0, composite_dissipation=True, cfl=None):
     """Acoustic monopole: quiescent ambient rho = 1, u = 0, p = 1/gamma; pressure
     source 0.01 sin(2 pi 0.2 t) with a Gaussian of sigma 0.5 at the origin.
     magudi's source is A cos(w t + phase) exp(-9/(2 R^2) r^2)
     (src/AcousticSourceImpl.f90:27,55-62), so sin -> phase = -pi/2 and
     sigma = 0.5 -> R = 3 sigma = 1.5. The dissipation is magudi's default
     composite operator: the non-composite one at amount 0.01 is unstable at
-    dt = 0.05 on this grid."""
+    dt = 0.05 on this grid. With cfl set, the step size follows the
+    constant-CFL rule instead of dt."""
     ny = ny or n
     gamma = 1.4
     opts = Options(
@@ -48,6 +49,9 @@ def monopole_2d(n=201, ny=None, dt=0.05, n_steps=960, sponge_points=20, sponge_a
         ratio_of_specific_heats=gamma, reynolds_number=reynolds, prandtl_number=prandtl,
         viscosity_power_law_exponent=power_law, bulk_viscosity_ratio=bulk_viscosity_ratio,
         dissipation_amount=dissipation_amount, time_step_size=dt)
+    if cfl is not None:
+        opts.use_constant_cfl = True
+        opts.cfl = cfl
     coords, x, y = uniform_grid_2d(n, ny, -half_width, half_width)
     N = n * ny
     X, Y = coords

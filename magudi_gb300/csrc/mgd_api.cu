@@ -151,6 +151,7 @@ int mgd_destroy(mgd_ctx* h) {
   cudaFree(c.dCounters); cudaFree(c.dApiAmp); cudaFree(c.dAmp); cudaFree(c.dForcing);
   cudaFree(c.dGradient); cudaFree(c.dPartials); cudaFree(c.dStageValues);
   cudaFree(c.dSnapshots); cudaFree(c.dStageBuf);
+  cudaFree(c.dStepDt); cudaFree(c.dDtPartials); cudaFree(c.dTime);
   if (c.gForward) cudaGraphExecDestroy(c.gForward);
   if (c.gRecompute) cudaGraphExecDestroy(c.gRecompute);
   if (c.gAdjoint) cudaGraphExecDestroy(c.gAdjoint);
@@ -1045,6 +1046,7 @@ static RunScalars runScalars(Context& c) {
   r.stageBuf = c.dStageBuf;
   r.slotStride = c.slotStride;
   r.slotFull = c.slotFull;
+  r.dtStep = c.dStepDt;
   r.dt = c.opts.time_step_size;
   r.adjointForcingSwitch = c.opts.adjoint_forcing_switch;
   return r;
@@ -1073,6 +1075,26 @@ static int capture(Context& c, cudaGraphExec_t* exec, long long* nodes, F body) 
   c.launches = before;
   CUDA_TRY(c, cudaGraphInstantiate(exec, g, 0));
   cudaGraphDestroy(g);
+  return 0;
+}
+
+// Per-step step sizes of a run, the constant-CFL reduction scratch and the
+// device copy of the run time.
+static int ensureStepBuffers(Context& c, DevBlock& b, int nSteps) {
+  if (c.stepDtCapacity < nSteps) {
+    cudaFree(c.dStepDt);
+    c.dStepDt = nullptr;
+    CUDA_TRY(c, cudaMalloc((void**)&c.dStepDt, (size_t)nSteps * sizeof(double)));
+    c.stepDtCapacity = nSteps;
+  }
+  const int nb = timeStepBlocks(b);
+  if (c.dtPartialCapacity < nb) {
+    cudaFree(c.dDtPartials);
+    c.dDtPartials = nullptr;
+    CUDA_TRY(c, cudaMalloc((void**)&c.dDtPartials, (size_t)nb * sizeof(double)));
+    c.dtPartialCapacity = nb;
+  }
+  if (!c.dTime) CUDA_TRY(c, cudaMalloc((void**)&c.dTime, sizeof(double)));
   return 0;
 }
 
@@ -1112,19 +1134,14 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
   DevBlock& b = c.blocks[0];
   const long long N = b.v.N;
   const int nU = c.nU;
+  const bool cflMode = c.opts.use_constant_cfl != 0;
   const double dt = c.opts.time_step_size;
-  if (!(dt > 0.0)) return fail(c, "time_step_size must be positive (constant-CFL mode is not supported)");
+  if (!cflMode && !(dt > 0.0)) return fail(c, "time_step_size must be positive");
+  if (cflMode && !(c.opts.cfl > 0.0)) return fail(c, "cfl must be positive in constant-CFL mode");
   c.runSteps = n_steps;
   c.saveInterval = save_interval;
   c.runT0 = t0;
-  // stage times as Solver%runForward accumulates them (src/RK4IntegratorImpl.f90:95-140)
-  c.stageTimes.assign((size_t)4 * n_steps, 0.0);
-  double t = t0;
-  for (int s = 0; s < n_steps; ++s)
-    for (int i = 1; i <= 4; ++i) {
-      if (i == 2 || i == 4) t = t + dt / 2.0;
-      c.stageTimes[(size_t)4 * s + i - 1] = t;
-    }
+  if (ensureStepBuffers(c, b, n_steps)) return 1;
   const int nSrc = (int)c.sources.size();
   const long long nAmp = (long long)4 * n_steps * std::max(1, nSrc);
   if (c.ampCapacity < nAmp) {
@@ -1132,7 +1149,20 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
     CUDA_TRY(c, cudaMalloc((void**)&c.dAmp, nAmp * sizeof(double)));
     c.ampCapacity = nAmp;
   }
-  {
+  if (cflMode) {
+    // step sizes, stage times and source amplitudes are produced on the device
+    CUDA_TRY(c, cudaMemcpyAsync(c.dTime, &t0, sizeof(double), cudaMemcpyHostToDevice, c.stream));
+  } else {
+    // stage times as Solver%runForward accumulates them (src/RK4IntegratorImpl.f90:95-140)
+    c.stageTimes.assign((size_t)4 * n_steps, 0.0);
+    double t = t0;
+    for (int s = 0; s < n_steps; ++s)
+      for (int i = 1; i <= 4; ++i) {
+        if (i == 2 || i == 4) t = t + dt / 2.0;
+        c.stageTimes[(size_t)4 * s + i - 1] = t;
+      }
+    c.stepDt.assign(n_steps, dt);
+    CUDA_TRY(c, cudaMemcpy(c.dStepDt, c.stepDt.data(), n_steps * sizeof(double), cudaMemcpyHostToDevice));
     std::vector<double> amp(nAmp, 0.0);
     const double pi = 4.0 * std::atan(1.0);
     for (long long k = 0; k < 4LL * n_steps; ++k)
@@ -1163,6 +1193,7 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
   launchSnapshot(c, b, c.dSnapshots, save_interval, true);
   if (setCounters(c, 1, 0)) return 1;
   if (capture(c, &c.gForward, &c.nodesForward, [&]() {
+        if (cflMode) launchTimeStep(c, b, c.dDtPartials, c.dStepDt, c.dCounters, c.dTime, c.dAmp);
         for (int i = 1; i <= 4; ++i) forwardStage(c, b, i, rs, false, controller, false, functional);
         launchSnapshot(c, b, c.dSnapshots, save_interval, false);
         launchStepAdvance(c, 1);
@@ -1171,12 +1202,18 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
   for (int s = 0; s < n_steps; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gForward, c.stream));
   c.launches += (long long)n_steps * c.nodesForward;
   if (checkLaunch(c)) return 1;
+  if (cflMode) {
+    c.stepDt.resize(n_steps);
+    CUDA_TRY(c, cudaMemcpyAsync(c.stepDt.data(), c.dStepDt, n_steps * sizeof(double), cudaMemcpyDeviceToHost,
+                                c.stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  }
   double J = 0.0;
   if (functional) {
     std::vector<double> vals;
     if (reduceToHost(c, 4 * n_steps, vals)) return 1;
     for (int s = 0; s < n_steps; ++s)
-      for (int i = 0; i < 4; ++i) J = J + kRkNorm[i] * dt * vals[(size_t)4 * s + i];
+      for (int i = 0; i < 4; ++i) J = J + kRkNorm[i] * c.stepDt[s] * vals[(size_t)4 * s + i];
   } else {
     CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   }
@@ -1191,14 +1228,14 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   DevBlock& b = c.blocks[0];
   const long long N = b.v.N;
   const int nU = c.nU, T = c.runSteps, S = c.saveInterval;
-  const double dt = c.opts.time_step_size;
+  const double dtT = c.stepDt[T - 1];  // step size of the final forward step
   if (ensureStageBuffer(c, b, S)) return 1;
   const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
   RunScalars rs = runScalars(c);
   const bool full = c.slotFull != 0;
   // adjoint initial condition at the final state (its primitives are current)
   launchPrims(c, b, b.v.q, false);
-  launchAdjointInitial(c, b, c.opts.adjoint_forcing_switch ? -dt / 6.0 : 0.0);
+  launchAdjointInitial(c, b, c.opts.adjoint_forcing_switch ? -dtT / 6.0 : 0.0);
   if (capture(c, &c.gRecompute, &c.nodesRecompute, [&]() {
         for (int i = 1; i <= 4; ++i) forwardStage(c, b, i, rs, false, controller, true, false);
         launchStepAdvance(c, 1);
@@ -1236,9 +1273,34 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   for (int n = T; n >= 1; --n)
     for (int i = 4; i >= 1; --i) {
       const long long entry = (long long)(T - n) * 4 + (4 - i);
-      sum = sum + kRkNorm[i - 1] * dt * vals[entry];
+      sum = sum + kRkNorm[i - 1] * c.stepDt[n - 1] * vals[entry];
     }
   *sensitivity = sum;
+  return 0;
+}
+
+int mgd_time_step_size(mgd_ctx* h, double* dt) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  if (!c.opts.use_constant_cfl) {
+    *dt = c.opts.time_step_size;
+    return 0;
+  }
+  DevBlock& b = c.blocks[0];
+  if (ensureStepBuffers(c, b, std::max(1, c.runSteps))) return 1;
+  launchPrims(c, b, b.v.q, false);
+  launchTimeStep(c, b, c.dDtPartials, c.dTime, nullptr, nullptr, nullptr);
+  if (checkLaunch(c)) return 1;
+  CUDA_TRY(c, cudaMemcpyAsync(dt, c.dTime, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  return 0;
+}
+
+int mgd_get_step_sizes(mgd_ctx* h, double* host, int n_steps) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  const int n = std::min(n_steps, (int)c.stepDt.size());
+  std::copy(c.stepDt.begin(), c.stepDt.begin() + std::max(0, n), host);
   return 0;
 }
 

@@ -116,9 +116,15 @@ struct RunScalars {
   double* stageBuf;       // stage inputs of the current segment (4*S slots)
   long long slotStride;   // doubles per stage slot
   int slotFull;           // slots hold q, primitives, stress and heat flux (else q only)
-  double dt;
+  double dt;              // step size when dtStep is null
+  const double* dtStep;   // step size of each step (indexed by step - 1), or null
   int adjointForcingSwitch;
 };
+
+// Step size of the current step of a run (or the per-call step size).
+__device__ __forceinline__ double stepDt(const RunScalars& rs) {
+  return rs.dtStep ? rs.dtStep[*rs.step - 1] : rs.dt;
+}
 
 struct DevBlock {
   mgd_block_desc desc;
@@ -174,6 +180,13 @@ struct Context {
   long long stageBufCapacity = 0;
   long long slotStride = 0;         // doubles per stage slot of dStageBuf
   int slotFull = 0;                 // slots also hold primitives, stress and heat flux
+  // step sizes of the last run, constant-CFL reduction scratch and run time
+  double* dStepDt = nullptr;
+  long long stepDtCapacity = 0;
+  std::vector<double> stepDt;
+  double* dDtPartials = nullptr;
+  long long dtPartialCapacity = 0;
+  double* dTime = nullptr;
   cudaGraphExec_t gForward = nullptr, gRecompute = nullptr, gAdjoint = nullptr;
   long long nodesForward = 0, nodesRecompute = 0, nodesAdjoint = 0;
 };
@@ -219,6 +232,12 @@ void launchStoreAdjointForcing(Context& c, DevBlock& b, bool zero);
 void launchSnapshot(Context& c, DevBlock& b, double* snapshots, int saveInterval, bool initial, cudaStream_t s = 0);
 void launchStepAdvance(Context& c, int delta, cudaStream_t s = 0);
 void launchReducePartials(Context& c, const double* partials, int stride, int count, int nSlots, double* out);
+// Constant-CFL step size of the current primitives: with step == null writes
+// the step size to dtOut[0]; otherwise writes dtOut[*step - 1], advances *time
+// over the step's four stages and stores the stages' source amplitudes in amp.
+void launchTimeStep(Context& c, DevBlock& b, double* partials, double* dtOut, const int* step, double* time,
+                    double* amp, cudaStream_t s = 0);
+int timeStepBlocks(const DevBlock& b);
 void launchCoordinateDerivative(Context& c, DevBlock& b, int dir, double* out);
 void launchApplyD1(Context& c, DevBlock& b, int dir, const double* in, double* out, int ncomp);
 void launchFarFieldMatricesWith(Context& c, DevBlock& b, const double* sigInv, const int* signedNormal);

@@ -411,7 +411,8 @@ __global__ void __launch_bounds__(kMaxTile) kForwardDivergence(BlockView B, Phys
     B.rhs[kc] = r;
     return;
   }
-  const double h6 = rs.dt / 6.0, h3 = rs.dt / 3.0, h2 = rs.dt / 2.0;
+  const double dt = stepDt(rs);
+  const double h6 = dt / 6.0, h3 = dt / 3.0, h2 = dt / 2.0;
   switch (rkStage) {
     case 1:
       B.b1[kc] = q;
@@ -424,7 +425,7 @@ __global__ void __launch_bounds__(kMaxTile) kForwardDivergence(BlockView B, Phys
       break;
     case 3:
       B.b2[kc] = B.b2[kc] + h3 * r;
-      B.q[kc] = B.b1[kc] + rs.dt * r;
+      B.q[kc] = B.b1[kc] + dt * r;
       break;
     default:
       B.q[kc] = B.b2[kc] + h6 * r;
@@ -649,7 +650,8 @@ __global__ void __launch_bounds__(kMaxTile) kAdjointAssemble(BlockView B, Physic
     B.rhs[kc] = r;
     return;
   }
-  const double h6 = rs.dt / 6.0, h3 = rs.dt / 3.0, h2 = rs.dt / 2.0;
+  const double dt = stepDt(rs);
+  const double h6 = dt / 6.0, h3 = dt / 3.0, h2 = dt / 2.0;
   switch (rkStage) {
     case 4:
       B.b1[kc] = lam;
@@ -662,7 +664,7 @@ __global__ void __launch_bounds__(kMaxTile) kAdjointAssemble(BlockView B, Physic
       break;
     case 2:
       B.b2[kc] = B.b2[kc] - h3 * r;
-      B.lam[kc] = B.b1[kc] - rs.dt * r;
+      B.lam[kc] = B.b1[kc] - dt * r;
       break;
     default:
       B.lam[kc] = B.b2[kc] - h6 * r;
@@ -745,6 +747,97 @@ __global__ void kReducePartials(const double* __restrict__ partials, int stride,
   for (int b = threadIdx.x; b < count; b += blockDim.x) v += partials[(long long)s * stride + b];
   const double t = blockSum(v);
   if (threadIdx.x == 0) out[s] = t;
+}
+
+// ---------------------------------------------------------------------------
+// Constant-CFL step size (computeTimeStepSize, src/CNSHelperImpl.f90:913-982):
+// block minima of the advective and viscous bounds over the non-hole points,
+// then one block takes the minimum and, inside a run, records it for the step,
+// advances the run time over the step's stages (src/RK4IntegratorImpl.f90:95-140)
+// and evaluates the acoustic-source amplitudes of those stages
+// (src/AcousticSourceImpl.f90:34-64).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double blockMin(double v) {
+  __shared__ double warpMins[32];
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) warpMins[w] = v;
+  __syncthreads();
+  double s = warpMins[0];
+  if (threadIdx.x == 0)
+    for (int i = 1; i < (int)((blockDim.x + 31) / 32); ++i) s = fmin(s, warpMins[i]);
+  return s;
+}
+
+constexpr double kHugeStep = 1.7976931348623157e308;
+
+template <int ND>
+__global__ void __launch_bounds__(kBlock) kTimeStepPartials(BlockView B, Physics P, double cfl,
+                                                            double* __restrict__ partial) {
+  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
+  double v = kHugeStep;
+  if (p < B.N && B.iblank[p] != 0) {
+    const long long N = B.N;
+    const PrimLayout L{ND};
+    double m[ND * ND], u[ND];
+    for (int c = 0; c < ND * ND; ++c) m[c] = B.metrics[p + N * c];
+    for (int d = 0; d < ND; ++d) u[d] = B.prim[p + N * L.u(d)];
+    const double jac = B.jac[p];
+    const double a = sqrt(P.gm1 * B.prim[p + N * L.T()]);
+    double w = 0.0;
+    for (int j = 0; j < ND; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < ND; ++k) s += m[ND * j + k] * m[ND * j + k];
+      w = w + s;
+    }
+    w = a * sqrt(w);
+    for (int j = 0; j < ND; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < ND; ++k) s += u[k] * m[ND * j + k];
+      w = w + fabs(s);
+    }
+    w = jac * w;
+    v = cfl / w;
+    if (P.viscous) {
+      double s = 0.0;
+      for (int c = 0; c < ND * ND; ++c) s += m[c] * m[c];
+      const double wv = jac * jac * s * fmax(2.0 * B.prim[p + N * L.mu()], B.prim[p + N * L.k()]);
+      v = fmin(v, cfl / wv);
+    }
+  }
+  const double r = blockMin(v);
+  if (threadIdx.x == 0) partial[blockIdx.x] = r;
+}
+
+struct SourceTable {
+  int n;
+  double twoPi;
+  double amplitude[MGD_MAX_SOURCES], frequency[MGD_MAX_SOURCES], phase[MGD_MAX_SOURCES];
+};
+
+__global__ void __launch_bounds__(256) kTimeStepFinalize(const double* __restrict__ partial, int n,
+                                                         double* __restrict__ dtOut, const int* __restrict__ step,
+                                                         double* __restrict__ time, double* __restrict__ amp,
+                                                         SourceTable src) {
+  double v = kHugeStep;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) v = fmin(v, partial[i]);
+  const double dt = blockMin(v);
+  if (threadIdx.x != 0) return;
+  if (!step) {
+    dtOut[0] = dt;
+    return;
+  }
+  const int s = *step;
+  dtOut[s - 1] = dt;
+  double t = *time;
+  for (int i = 1; i <= 4; ++i) {
+    if (i == 2 || i == 4) t = t + dt / 2.0;
+    for (int k = 0; k < src.n; ++k) {
+      const double arg = __dadd_rn(__dmul_rn(__dmul_rn(src.twoPi, src.frequency[k]), t), src.phase[k]);
+      amp[((long long)(s - 1) * 4 + (i - 1)) * src.n + k] = src.amplitude[k] * cos(arg);
+    }
+  }
+  *time = t;
 }
 
 // ---------------------------------------------------------------------------
@@ -991,6 +1084,26 @@ void launchReducePartials(Context& c, const double* partials, int stride, int co
   if (nSlots <= 0) return;
   MGD_LAUNCH(c);
   kReducePartials<<<nSlots, kBlock, 0, c.stream>>>(partials, stride, count, nSlots, out);
+}
+
+int timeStepBlocks(const DevBlock& b) { return gridFor(b.v.N); }
+
+void launchTimeStep(Context& c, DevBlock& b, double* partials, double* dtOut, const int* step, double* time,
+                    double* amp, cudaStream_t s) {
+  const int nb = timeStepBlocks(b);
+  MGD_LAUNCH(c);
+  if (c.nD == 2) kTimeStepPartials<2><<<nb, kBlock, 0, on(c, s)>>>(b.v, c.phys, c.opts.cfl, partials);
+  else kTimeStepPartials<3><<<nb, kBlock, 0, on(c, s)>>>(b.v, c.phys, c.opts.cfl, partials);
+  SourceTable src{};
+  src.n = (int)c.sources.size();
+  src.twoPi = 2.0 * (4.0 * std::atan(1.0));
+  for (int k = 0; k < src.n; ++k) {
+    src.amplitude[k] = c.sources[k].amplitude;
+    src.frequency[k] = c.sources[k].frequency;
+    src.phase[k] = c.sources[k].phase;
+  }
+  MGD_LAUNCH(c);
+  kTimeStepFinalize<<<1, 256, 0, on(c, s)>>>(partials, nb, dtOut, step, time, amp, src);
 }
 
 void launchCoordinateDerivative(Context& c, DevBlock& b, int dir, double* out) {

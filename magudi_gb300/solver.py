@@ -56,6 +56,8 @@ def load_library(build_if_missing=True):
     L.mgd_run_forward.argtypes = [ctx, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_double)]
     L.mgd_run_adjoint.argtypes = [ctx, C.POINTER(C.c_double)]
     L.mgd_get_gradient.argtypes = [ctx, C.POINTER(C.c_double), C.c_longlong]
+    L.mgd_time_step_size.argtypes = [ctx, C.POINTER(C.c_double)]
+    L.mgd_get_step_sizes.argtypes = [ctx, C.POINTER(C.c_double), C.c_int]
     L.mgd_profile_stage_kernels.argtypes = [ctx, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)]
     L.mgd_stream.restype = C.c_void_p
     L.mgd_stream.argtypes = [ctx]
@@ -180,6 +182,18 @@ class Solver:
         out = np.zeros(n_entries * P)
         self._check(self.L.mgd_get_gradient(self.h, capi.dptr(out), n_entries))
         return out.reshape(n_entries, P)
+
+    def time_step_size(self):
+        """Region%getTimeStepSize of the current conserved variables."""
+        v = C.c_double()
+        self._check(self.L.mgd_time_step_size(self.h, C.byref(v)))
+        return v.value
+
+    def step_sizes(self, n_steps):
+        """Step sizes of the steps of the last run_forward."""
+        out = np.zeros(max(1, n_steps))
+        self._check(self.L.mgd_get_step_sizes(self.h, capi.dptr(out), n_steps))
+        return out[:n_steps]
 
     def profile_stage_kernels(self, mode, reps=20):
         """Mean per-launch milliseconds of each kernel of one RK stage."""

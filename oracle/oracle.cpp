@@ -25,6 +25,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <string>
 #include <vector>
@@ -606,6 +607,7 @@ struct Region {
   double t0 = 0.0;
   std::vector<std::vector<double>> stageStates;  // forward stage inputs per block
   std::vector<double> stageTimes;
+  std::vector<double> stepDt;  // time step of each forward step
   double finalTime = 0.0;
 };
 
@@ -1485,18 +1487,70 @@ static void substep(Region& R, int mode, double& time, double dt, int stage, boo
 
 static const double kRkNorm[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
 
+// computeTimeStepSize, src/CNSHelperImpl.f90:913-982, through
+// State%computeTimeStepSize (src/StateImpl.f90:605-670) and the minimum over
+// blocks of Region%getTimeStepSize (src/RegionImpl.f90:1842-1875). Uses the
+// dependent variables of the last state update.
+static double computeTimeStepSize(Region& R) {
+  if (!R.o.use_constant_cfl) return R.o.time_step_size;
+  const int nD = R.nD;
+  const double g = R.o.ratio_of_specific_heats, cfl = R.o.cfl;
+  double dt = std::numeric_limits<double>::max();
+  for (Block& b : R.blocks) {
+    const long long N = b.N;
+    for (long long i = 0; i < N; ++i) {
+      if (b.iblank[i] == 0) continue;
+      const double a = std::sqrt((g - 1.0) * b.temperature[i]);
+      double w = 0.0;
+      for (int j = 0; j < nD; ++j) {
+        double s = 0.0;
+        for (int k = 0; k < nD; ++k) {
+          const double m = b.metrics[N * (nD * j + k) + i];
+          s += m * m;
+        }
+        w = w + s;
+      }
+      w = a * std::sqrt(w);
+      for (int j = 0; j < nD; ++j) {
+        double s = 0.0;
+        for (int k = 0; k < nD; ++k) s += b.velocity[N * k + i] * b.metrics[N * (nD * j + k) + i];
+        w = w + std::abs(s);
+      }
+      w = b.jacobian[i] * w;
+      dt = std::min(dt, cfl / w);
+    }
+    if (R.o.viscous) {
+      for (long long i = 0; i < N; ++i) {
+        if (b.iblank[i] == 0) continue;
+        double s = 0.0;
+        for (int c = 0; c < nD * nD; ++c) {
+          const double m = b.metrics[N * c + i];
+          s += m * m;
+        }
+        const double w = b.jacobian[i] * b.jacobian[i] * s *
+                         std::max(2.0 * b.dynamicViscosity[i], b.thermalDiffusivity[i]);
+        dt = std::min(dt, cfl / w);
+      }
+    }
+  }
+  return dt;
+}
+
 // Solver%runForward, src/SolverImpl.f90:672-912 (functional on, constant dt).
 // Stage inputs are kept in memory for the adjoint run; that matches
 // UniformCheckpointer's recomputation exactly because the forward is deterministic.
 static double runForward(Region& R, int nSteps, double t0, bool keepStages) {
   R.nSteps = nSteps;
   R.t0 = t0;
-  const double dt = R.o.time_step_size;
   double time = t0, J = 0.0;
   updateAll(R);
   R.stageStates.clear();
   R.stageTimes.clear();
+  R.stepDt.clear();
   for (int step = 1; step <= nSteps; ++step) {
+    // src/SolverImpl.f90:809: the step size of the state at the start of the step
+    const double dt = computeTimeStepSize(R);
+    R.stepDt.push_back(dt);
     for (int i = 1; i <= 4; ++i) {
       if (keepStages) {
         std::vector<double> all;
@@ -1523,21 +1577,27 @@ static void setForwardState(Region& R, const std::vector<double>& all) {
 }
 
 // Solver%runAdjoint, src/SolverImpl.f90:914-1245, and the adjoint initial
-// condition of loadInitialCondition, :368-427.
+// condition of loadInitialCondition, :368-427. Each adjoint step uses the step
+// size of the matching forward step. (In constant-CFL mode the reference
+// re-evaluates getTimeStepSize at src/SolverImpl.f90:1139,1147 on the forward
+// state left by the last checkpoint migration, i.e. one step later; the
+// recorded step sizes make this the exact discrete adjoint of the forward run.)
 static double runAdjoint(Region& R) {
-  const double dt = R.o.time_step_size;
+  const double dtT = R.stepDt.empty() ? R.o.time_step_size : R.stepDt.back();
+  double dt = dtT;
   // final forward state is the current state
   updateAll(R);
   for (Block& b : R.blocks) std::fill(b.adjointVariables.begin(), b.adjointVariables.end(), 0.0);
   updateAdjointForcing(R, !R.o.adjoint_forcing_switch);
   for (Block& b : R.blocks) std::fill(b.rightHandSide.begin(), b.rightHandSide.end(), 0.0);
   for (Patch& p : R.patches)
-    if (p.d.type == MGD_PATCH_COST_TARGET) patchUpdateRhs(R, p, R.blocks[p.d.grid_index - 1], MGD_ADJOINT, -dt / 6.0);
+    if (p.d.type == MGD_PATCH_COST_TARGET) patchUpdateRhs(R, p, R.blocks[p.d.grid_index - 1], MGD_ADJOINT, -dtT / 6.0);
   for (Block& b : R.blocks)
     for (size_t k = 0; k < b.adjointVariables.size(); ++k) b.adjointVariables[k] = b.adjointVariables[k] + b.rightHandSide[k];
   R.gradientEntries.clear();
   double time = R.finalTime - 0.5 * dt, s = 0.0;
   for (int step = R.nSteps; step >= 1; --step) {
+    dt = R.stepDt[step - 1];
     for (int i = 4; i >= 1; --i) {
       setForwardState(R, R.stageStates[(size_t)(step - 1) * 4 + (i - 1)]);
       appendGradient(R);
@@ -1755,6 +1815,17 @@ int orc_run_forward(void* h, int nSteps, int saveInterval, double t0, double* co
 int orc_run_forward_nostore(void* h, int nSteps, double t0, double* cost) {
   *cost = orc::runForward(*(Region*)h, nSteps, t0, false);
   return 0;
+}
+
+int orc_time_step_size(void* h, double* dt) {
+  *dt = orc::computeTimeStepSize(*(Region*)h);
+  return 0;
+}
+
+int orc_step_sizes(void* h, double* out) {
+  const Region& R = *(Region*)h;
+  std::copy(R.stepDt.begin(), R.stepDt.end(), out);
+  return (int)R.stepDt.size();
 }
 
 int orc_run_adjoint(void* h, double* s) {

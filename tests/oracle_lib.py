@@ -49,6 +49,8 @@ def lib():
         L.orc_run_forward.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_double)]
         L.orc_run_forward_nostore.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double)]
         L.orc_run_adjoint.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.orc_time_step_size.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.orc_step_sizes.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.orc_get_gradient.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_longlong]
         L.orc_operator_info.argtypes = [C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                         C.POINTER(C.c_double), C.POINTER(C.c_double)]
@@ -192,6 +194,16 @@ class Oracle:
         v = C.c_double()
         self.L.orc_run_adjoint(self.h, C.byref(v))
         return v.value
+
+    def time_step_size(self):
+        v = C.c_double()
+        self.L.orc_time_step_size(self.h, C.byref(v))
+        return v.value
+
+    def step_sizes(self, n_steps):
+        out = np.zeros(max(1, n_steps))
+        n = self.L.orc_step_sizes(self.h, capi.dptr(out))
+        return out[:n]
 
     def gradient(self, n_entries):
         P = self.actuator_points()

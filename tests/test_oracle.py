@@ -177,3 +177,31 @@ def test_gradient_finite_difference_sweep():
         best = min(best, abs((J1 - J0) / eps - G0) / G0)
     # the error grows as eps shrinks (roundoff in J1 - J0); its minimum bounds the adjoint error
     assert best < 1e-5
+
+
+def test_oracle_time_step_size_restated_in_numpy():
+    """computeTimeStepSize (src/CNSHelperImpl.f90:913-982) restated with numpy
+    from the oracle's own grid and state arrays pins the oracle's CFL rule."""
+    P = small_monopole(cfl=0.7)
+    q, _ = random_full_rhs_state(P, 12)
+    o = oracle_lib.Oracle(P)
+    o.set_field(1, capi.FIELD_CONSERVED, q)
+    o.update_state()
+    opt = P.options
+    g = opt.ratio_of_specific_heats
+    nD = 2
+    N = q.shape[1]
+    m = o.get_field(1, capi.FIELD_METRICS).reshape(nD * nD, N)
+    jac = o.get_field(1, capi.FIELD_JACOBIAN)
+    T = o.get_field(1, capi.FIELD_TEMPERATURE)
+    u = q[1:1 + nD] / q[0]
+    a = np.sqrt((g - 1.0) * T)
+    rows = [m[nD * j:nD * (j + 1)] for j in range(nD)]
+    w = a * np.sqrt(sum(np.sum(r ** 2, axis=0) for r in rows))
+    w = w + sum(np.abs(np.sum(u * r, axis=0)) for r in rows)
+    dt = np.min(opt.cfl / (jac * w))
+    mu = ((g - 1.0) * T) ** opt.viscosity_power_law_exponent / opt.reynolds_number
+    k = mu / opt.prandtl_number
+    wv = jac ** 2 * np.sum(m ** 2, axis=0) * np.maximum(2.0 * mu, k)
+    dt = min(dt, np.min(opt.cfl / wv))
+    assert abs(o.time_step_size() - dt) <= 1e-13 * dt
