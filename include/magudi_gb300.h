@@ -208,6 +208,24 @@ int mgd_run_adjoint(mgd_ctx* ctx, double* sensitivity);
  * src/ThermalActuatorImpl.f90:383-443): 4*n_steps entries of nPatchPoints. */
 int mgd_get_gradient(mgd_ctx* ctx, double* host, long long n_entries);
 
+/* Batched forward runs. The reference runs its gradient-accuracy sweep as one
+ * ./forward process per control amplitude after ./zaxpy (README.md:118-165,
+ * bin/ZAXPY.f90); a batch runs many such forward solves at once. A batch
+ * groups finalized single-block contexts on one device whose options agree
+ * except for the grids (constant time_step_size). mgd_batch_run_forward
+ * advances every instance n_steps RK4 steps from its current conserved
+ * variables and control forcing (Solver%runForward, src/SolverImpl.f90:672-912,
+ * without snapshots); each stage kernel is one launch for the whole batch and
+ * each step is one CUDA graph. costs[i] receives instance i's functional;
+ * the final states stay in the instances. Tile shapes are chosen per grid
+ * size by timing candidate shapes at mgd_batch_create. */
+typedef struct mgd_batch mgd_batch;
+int mgd_batch_create(mgd_ctx* const* instances, int n_instances, mgd_batch** batch);
+int mgd_batch_run_forward(mgd_batch* batch, int n_steps, double t0, double* costs);
+int mgd_batch_destroy(mgd_batch* batch);
+const char* mgd_batch_last_error(const mgd_batch* batch);
+long long mgd_batch_kernel_launches(mgd_batch* batch, int reset);
+
 /* Measurement hook (no reference counterpart): times each kernel of one RK
  * stage separately with CUDA events on the context stream; forward gives 2
  * durations [gradient/flux, divergence+RK], adjoint 4 [primitives, stress,

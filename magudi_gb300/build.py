@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math"]
-SOURCES = ["mgd_api.cu", "mgd_kernels.cu", "mgd_noalloc.cu"]
+SOURCES = ["mgd_api.cu", "mgd_kernels.cu", "mgd_noalloc.cu", "mgd_batch.cu"]
 
 
 def nvcc():

@@ -571,6 +571,48 @@ static int autotune(Context& c, DevBlock& b) {
   return 0;
 }
 
+namespace mgd {
+
+// Fastest of nCands tile shapes for one forward stage kernel (BK_GRAD,
+// BK_DISS or BK_RHS) of block b, timed on its current state; b's own tiles
+// are left as they were.
+int autotuneTile(Context& c, DevBlock& b, int kernel, const int (*cands)[3], int nCands, Tile* best) {
+  RunScalars rs = apiScalars(c);
+  if (setApiTime(c, 0.0)) return 1;
+  launchPrims(c, b, b.v.q, false);
+  Tile* slot = kernel == BK_GRAD ? &b.tGrad : (kernel == BK_DISS ? &b.tDiss : &b.tRhs);
+  const Tile saved = *slot;
+  const long long savedLaunches = c.launches;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float bestMs = 1e30f;
+  *best = saved;
+  for (int k = 0; k < nCands; ++k) {
+    *slot = makeTile(b, cands[k][0], cands[k][1], cands[k][2]);
+    auto run = [&]() {
+      if (kernel == BK_GRAD) launchGradFlux(c, b, true, false, &rs, 1, false);
+      else if (kernel == BK_DISS) launchDissipation(c, b, b.v.q, 1.0);
+      else launchForwardDivergence(c, b, 0, rs, true, false);
+    };
+    run();
+    cudaEventRecord(e0, c.stream);
+    for (int r = 0; r < 3; ++r) run();
+    cudaEventRecord(e1, c.stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < bestMs) { bestMs = ms; *best = *slot; }
+  }
+  *slot = saved;
+  c.launches = savedLaunches;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return checkLaunch(c);
+}
+
+}  // namespace mgd
+
 int mgd_finalize_setup(mgd_ctx* h) {
   Context& c = h->c;
   if (c.finalized) return 0;
@@ -1126,11 +1168,13 @@ static int ensureStageBuffer(Context& c, DevBlock& b, int S) {
   return 0;
 }
 
-int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, double* cost) {
-  Context& c = h->c;
-  if (requireReady(c)) return 1;
-  if (n_steps < 1) return fail(c, "n_steps must be >= 1");
-  if (save_interval < 1) save_interval = n_steps;
+namespace mgd {
+
+// Run buffers and per-stage tables of a forward run of n_steps steps from t0:
+// step sizes, source amplitudes, functional partials, gradient entries and,
+// with snapshots, the checkpoint snapshots. Leaves the primitives of the
+// initial state current.
+int prepareForwardRun(Context& c, int n_steps, int save_interval, double t0, bool snapshots) {
   DevBlock& b = c.blocks[0];
   const long long N = b.v.N;
   const int nU = c.nU;
@@ -1172,11 +1216,14 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
       }
     CUDA_TRY(c, cudaMemcpy(c.dAmp, amp.data(), nAmp * sizeof(double), cudaMemcpyHostToDevice));
   }
-  const long long nSnap = n_steps / save_interval + 2;
-  if (c.snapshotCapacity < nSnap * nU * N) {
-    cudaFree(c.dSnapshots);
-    CUDA_TRY(c, cudaMalloc((void**)&c.dSnapshots, (size_t)nSnap * nU * N * sizeof(double)));
-    c.snapshotCapacity = nSnap * nU * N;
+  if (snapshots) {
+    const long long nSnap = n_steps / save_interval + 2;
+    if (c.snapshotCapacity < nSnap * nU * N) {
+      cudaFree(c.dSnapshots);
+      c.dSnapshots = nullptr;
+      CUDA_TRY(c, cudaMalloc((void**)&c.dSnapshots, (size_t)nSnap * nU * N * sizeof(double)));
+      c.snapshotCapacity = nSnap * nU * N;
+    }
   }
   if (ensurePartials(c, 4LL * n_steps)) return 1;
   const long long nGrad = 4LL * n_steps * std::max(1LL, c.actuatorPoints);
@@ -1185,12 +1232,48 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
     CUDA_TRY(c, cudaMalloc((void**)&c.dGradient, nGrad * sizeof(double)));
     c.gradientCapacity = nGrad;
   }
+  // state%update of the initial condition
+  launchPrims(c, b, b.v.q, false);
+  if (snapshots) launchSnapshot(c, b, c.dSnapshots, save_interval, true);
+  return checkLaunch(c);
+}
+
+// Step sizes back to the host and J = sum over steps and stages of
+// w_i dt_n J_{n,i} (src/SolverImpl.f90:836-841) from the stage partials.
+int finishForwardRun(Context& c, double* cost) {
+  const int n_steps = c.runSteps;
+  if (c.opts.use_constant_cfl) {
+    c.stepDt.resize(n_steps);
+    CUDA_TRY(c, cudaMemcpyAsync(c.stepDt.data(), c.dStepDt, n_steps * sizeof(double), cudaMemcpyDeviceToHost,
+                                c.stream));
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  double J = 0.0;
+  if (c.opts.enable_functional) {
+    std::vector<double> vals;
+    if (reduceToHost(c, 4 * n_steps, vals)) return 1;
+    for (int s = 0; s < n_steps; ++s)
+      for (int i = 0; i < 4; ++i) J = J + kRkNorm[i] * c.stepDt[s] * vals[(size_t)4 * s + i];
+  }
+  *cost = J;
+  return 0;
+}
+
+RunScalars runScalarsOf(Context& c) { return runScalars(c); }
+
+}  // namespace mgd
+
+int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, double* cost) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  if (n_steps < 1) return fail(c, "n_steps must be >= 1");
+  if (save_interval < 1) save_interval = n_steps;
+  DevBlock& b = c.blocks[0];
+  if (prepareForwardRun(c, n_steps, save_interval, t0, true)) return 1;
+  const bool cflMode = c.opts.use_constant_cfl != 0;
   const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
   const bool functional = c.opts.enable_functional != 0;
   RunScalars rs = runScalars(c);
-  // state%update of the initial condition, step-0 snapshot
-  launchPrims(c, b, b.v.q, false);
-  launchSnapshot(c, b, c.dSnapshots, save_interval, true);
   if (setCounters(c, 1, 0)) return 1;
   if (capture(c, &c.gForward, &c.nodesForward, [&]() {
         if (cflMode) launchTimeStep(c, b, c.dDtPartials, c.dStepDt, c.dCounters, c.dTime, c.dAmp);
@@ -1202,23 +1285,7 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
   for (int s = 0; s < n_steps; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gForward, c.stream));
   c.launches += (long long)n_steps * c.nodesForward;
   if (checkLaunch(c)) return 1;
-  if (cflMode) {
-    c.stepDt.resize(n_steps);
-    CUDA_TRY(c, cudaMemcpyAsync(c.stepDt.data(), c.dStepDt, n_steps * sizeof(double), cudaMemcpyDeviceToHost,
-                                c.stream));
-    CUDA_TRY(c, cudaStreamSynchronize(c.stream));
-  }
-  double J = 0.0;
-  if (functional) {
-    std::vector<double> vals;
-    if (reduceToHost(c, 4 * n_steps, vals)) return 1;
-    for (int s = 0; s < n_steps; ++s)
-      for (int i = 0; i < 4; ++i) J = J + kRkNorm[i] * c.stepDt[s] * vals[(size_t)4 * s + i];
-  } else {
-    CUDA_TRY(c, cudaStreamSynchronize(c.stream));
-  }
-  *cost = J;
-  return 0;
+  return finishForwardRun(c, cost);
 }
 
 int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {

@@ -191,11 +191,36 @@ struct Context {
   long long nodesForward = 0, nodesRecompute = 0, nodesAdjoint = 0;
 };
 
+// One instance of a batched launch: its block, run scalars and tile shapes.
+// All instances of a batch share the physics and the thread count of each
+// kernel; grid sizes, tiles, states and controls differ.
+struct BatchEntry {
+  BlockView v;
+  RunScalars rs;
+  Tile tGrad, tDiss, tRhs;
+  int controller;
+};
+
+// Block maps of a batched launch: entry k of a map is (instance, block within
+// the instance) for thread block k.
+enum BatchKernel { BK_GRAD = 0, BK_DISS, BK_RHS, BK_PRIMS, BK_FUNC, BK_COUNT };
+struct BatchLaunch {
+  const BatchEntry* entries = nullptr;
+  const int2* map[BK_COUNT] = {};
+  int blocks[BK_COUNT] = {};
+  int threads[BK_COUNT] = {};
+};
+
 // ----- stage orchestration (mgd_api.cu) -----
 void forwardStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bool api, bool controller, bool store,
                   bool functional);
 void adjointStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage, double apiFactor, bool api,
                   bool fromSlot, bool record);
+
+int prepareForwardRun(Context& c, int n_steps, int save_interval, double t0, bool snapshots);
+int finishForwardRun(Context& c, double* cost);
+RunScalars runScalarsOf(Context& c);
+int autotuneTile(Context& c, DevBlock& b, int kernel, const int (*cands)[3], int nCands, Tile* best);
 
 // ----- launchers (mgd_kernels.cu) -----
 // Every launcher takes the stream it launches on; the context stream when 0.
@@ -242,6 +267,16 @@ void launchCoordinateDerivative(Context& c, DevBlock& b, int dir, double* out);
 void launchApplyD1(Context& c, DevBlock& b, int dir, const double* in, double* out, int ncomp);
 void launchFarFieldMatricesWith(Context& c, DevBlock& b, const double* sigInv, const int* signedNormal);
 void launchFarFieldTargetVisc(Context& c, DevBlock& b);
+// Batched forward stage over all instances of a batch (same kernels as
+// forwardStage, one launch per kernel for the whole batch).
+void launchBatchGradFlux(Context& c, const BatchLaunch& L, int stage, cudaStream_t s);
+void launchBatchDissipation(Context& c, const BatchLaunch& L, cudaStream_t s);
+void launchBatchForwardDivergence(Context& c, const BatchLaunch& L, int rkStage, cudaStream_t s);
+void launchBatchPrims(Context& c, const BatchLaunch& L, cudaStream_t s);
+void launchBatchFunctional(Context& c, const BatchLaunch& L, int stage, cudaStream_t s);
+void launchStepAdvanceOn(int* counters, int delta, cudaStream_t s);
+constexpr int kBatchThreads = 128;
+
 // Blocks of the fixed-layout reductions (functional, sensitivity).
 int reductionBlocks(const DevBlock& b);
 void launchPowSelfTest(const double* x, int n, double e, double* fast, double* ref);

@@ -95,9 +95,10 @@ __device__ __forceinline__ PointIndex pointIndex(const BlockView& B, long long p
   return r;
 }
 
-// Grid point of this thread under tiling T; false when the tile overhangs the grid.
-__device__ __forceinline__ bool locate(const BlockView& B, const Tile& T, long long& p, PointIndex& r) {
-  const int t = threadIdx.x, b = blockIdx.x;
+// Grid point of this thread in tile-block b under tiling T; false when the
+// tile overhangs the grid.
+__device__ __forceinline__ bool locate(const BlockView& B, const Tile& T, int b, long long& p, PointIndex& r) {
+  const int t = threadIdx.x;
   const int lx = t % T.t[0], ly = (t / T.t[0]) % T.t[1], lz = t / (T.t[0] * T.t[1]);
   const int bx = b % T.n[0], by = (b / T.n[0]) % T.n[1], bz = b / (T.n[0] * T.n[1]);
   r.idx[0] = bx * T.t[0] + lx;
@@ -149,9 +150,9 @@ __device__ __forceinline__ double blockSum(double v) {
 // Primitive variables (State%update pointwise part, src/StateImpl.f90:466-492)
 // ---------------------------------------------------------------------------
 template <int ND>
-__global__ void __launch_bounds__(kBlock) kPrims(BlockView B, Physics P, const double* __restrict__ qSrc,
-                                                 int copyToQ, RunScalars rs, int stage) {
-  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
+__device__ __forceinline__ void primsPoint(const BlockView& B, const Physics& P, const double* __restrict__ qSrc,
+                                           int copyToQ, const RunScalars& rs, int stage, int blk) {
+  const long long p = (long long)blk * kBlock + threadIdx.x;
   if (p >= B.N) return;
   constexpr int nU = ND + 2;
   if (stage > 0) {
@@ -164,6 +165,12 @@ __global__ void __launch_bounds__(kBlock) kPrims(BlockView B, Physics P, const d
     for (int c = 0; c < nU; ++c) B.q[p + B.N * c] = q[c];
   primitives<ND>(q, P, pr);
   for (int c = 0; c < 6 + ND; ++c) B.prim[p + B.N * c] = pr[c];
+}
+
+template <int ND>
+__global__ void __launch_bounds__(kBlock) kPrims(BlockView B, Physics P, const double* __restrict__ qSrc,
+                                                 int copyToQ, RunScalars rs, int stage) {
+  primsPoint<ND>(B, P, qSrc, copyToQ, rs, stage, blockIdx.x);
 }
 
 // Forward-state arrays seen by the adjoint kernels: the block's own arrays, or
@@ -197,11 +204,11 @@ __device__ __forceinline__ FwdState forwardState(const BlockView& B, const RunSc
 enum { GF_FLUX = 1, GF_STRESS = 4, GF_STORE = 8 };
 
 template <int ND, bool CURV, bool VISC>
-__global__ void __launch_bounds__(kMaxTile) kGradFlux(BlockView B, Physics P, RunScalars rs, int flags,
-                                                      int stage, Tile T) {
+__device__ __forceinline__ void gradFluxPoint(const BlockView& B, const Physics& P, const RunScalars& rs, int flags,
+                                              int stage, const Tile& T, int blk) {
   long long p;
   PointIndex I;
-  if (!locate(B, T, p, I)) return;
+  if (!locate(B, T, blk, p, I)) return;
   constexpr int nU = ND + 2, E = ND + 1;
   const long long N = B.N;
   const PrimLayout L{ND};
@@ -329,17 +336,23 @@ __global__ void __launch_bounds__(kMaxTile) kGradFlux(BlockView B, Physics P, Ru
   }
 }
 
+template <int ND, bool CURV, bool VISC>
+__global__ void __launch_bounds__(kMaxTile) kGradFlux(BlockView B, Physics P, RunScalars rs, int flags,
+                                                      int stage, Tile T) {
+  gradFluxPoint<ND, CURV, VISC>(B, P, rs, flags, stage, T, blockIdx.x);
+}
+
 // ---------------------------------------------------------------------------
 // Artificial dissipation (addDissipation, src/RhsHelperImpl.f90:10-87), one
 // thread per point and component. Composite: dq_c = sign * amount * sum_i
 // Dc_i src_c. Non-composite, first sweep: dq_{i,c} = sign * (-amount arc_i) D_i src_c.
 // ---------------------------------------------------------------------------
 template <int ND>
-__global__ void __launch_bounds__(kMaxTile) kDissipation(BlockView B, Physics P, const double* __restrict__ src,
-                                                         double sign, Tile T) {
+__device__ __forceinline__ void dissipationPoint(const BlockView& B, const Physics& P, const double* __restrict__ src,
+                                                 double sign, const Tile& T, int blk) {
   long long p;
   PointIndex I;
-  if (!locate(B, T, p, I)) return;
+  if (!locate(B, T, blk, p, I)) return;
   constexpr int nU = ND + 2;
   const int c = blockIdx.y;
   const long long N = B.N;
@@ -352,6 +365,12 @@ __global__ void __launch_bounds__(kMaxTile) kDissipation(BlockView B, Physics P,
     for (int d = 0; d < ND; ++d)
       B.dq[p + N * (d * nU + c)] = (sign * B.arcA[p + N * d]) * applyOp<OP_DISS>(x + I.base[d], I.idx[d], B.ax[d]);
   }
+}
+
+template <int ND>
+__global__ void __launch_bounds__(kMaxTile) kDissipation(BlockView B, Physics P, const double* __restrict__ src,
+                                                         double sign, Tile T) {
+  dissipationPoint<ND>(B, P, src, sign, T, blockIdx.x);
 }
 
 template <int ND>
@@ -371,11 +390,12 @@ __device__ __forceinline__ double dissipationTerm(const BlockView& B, const Phys
 // that component's RK4 forward stage update (src/RK4IntegratorImpl.f90:104-158).
 // ---------------------------------------------------------------------------
 template <int ND>
-__global__ void __launch_bounds__(kMaxTile) kForwardDivergence(BlockView B, Physics P, RunScalars rs, int rkStage,
-                                                               int stage, int controller, Tile T) {
+__device__ __forceinline__ void forwardDivergencePoint(const BlockView& B, const Physics& P, const RunScalars& rs,
+                                                       int rkStage, int stage, int controller, const Tile& T,
+                                                       int blk) {
   long long p;
   PointIndex I;
-  if (!locate(B, T, p, I)) return;
+  if (!locate(B, T, blk, p, I)) return;
   constexpr int nU = ND + 2, E = ND + 1;
   const int c = blockIdx.y;
   const long long N = B.N;
@@ -433,11 +453,18 @@ __global__ void __launch_bounds__(kMaxTile) kForwardDivergence(BlockView B, Phys
   }
 }
 
+template <int ND>
+__global__ void __launch_bounds__(kMaxTile) kForwardDivergence(BlockView B, Physics P, RunScalars rs, int rkStage,
+                                                               int stage, int controller, Tile T) {
+  forwardDivergencePoint<ND>(B, P, rs, rkStage, stage, controller, T, blockIdx.x);
+}
+
 // Functional (AcousticNoise%compute, src/AcousticNoiseImpl.f90:123-206) of the
 // state whose primitives are current: partial sums over the cost-target points,
 // fixed block layout, into the slot of (step, stage).
-__global__ void __launch_bounds__(kBlock) kFunctional(BlockView B, RunScalars rs, int stage, int pressureComp) {
-  const int i = blockIdx.x * kBlock + threadIdx.x;
+__device__ __forceinline__ void functionalBlock(const BlockView& B, const RunScalars& rs, int stage,
+                                                int pressureComp, int blk) {
+  const int i = blk * kBlock + threadIdx.x;
   double v = 0.0;
   if (i < B.nTgt) {
     const long long p = B.tgtPts[i];
@@ -447,8 +474,12 @@ __global__ void __launch_bounds__(kBlock) kFunctional(BlockView B, RunScalars rs
   const double s = blockSum(v);
   if (threadIdx.x == 0) {
     const int slot = ((*rs.step) - 1) * 4 + (stage - 1);
-    rs.partials[(long long)slot * rs.nPartialBlocks + blockIdx.x] = s;
+    rs.partials[(long long)slot * rs.nPartialBlocks + blk] = s;
   }
+}
+
+__global__ void __launch_bounds__(kBlock) kFunctional(BlockView B, RunScalars rs, int stage, int pressureComp) {
+  functionalBlock(B, rs, stage, pressureComp, blockIdx.x);
 }
 
 // Gradient entry and sensitivity partial sums of lambda at an adjoint stage
@@ -476,11 +507,11 @@ __global__ void __launch_bounds__(kBlock) kGradientSensitivity(BlockView B, RunS
 // the complete far-field adjoint SAT vector (src/FarFieldPatchImpl.f90:237-257).
 // ---------------------------------------------------------------------------
 template <int ND, bool VISC>
-__global__ void __launch_bounds__(kMaxTile) kAdjointCore(BlockView B, Physics P, RunScalars rs, int stage,
-                                                         int fromSlot, Tile T) {
+__device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physics& P, const RunScalars& rs,
+                                                 int stage, int fromSlot, const Tile& T, int blk) {
   long long p;
   PointIndex I;
-  if (!locate(B, T, p, I)) return;
+  if (!locate(B, T, blk, p, I)) return;
   constexpr int nU = ND + 2, nV = ND + 1;
   const long long N = B.N;
   const PrimLayout L{ND};
@@ -557,19 +588,30 @@ __global__ void __launch_bounds__(kMaxTile) kAdjointCore(BlockView B, Physics P,
   }
 }
 
+template <int ND, bool VISC>
+__global__ void __launch_bounds__(kMaxTile) kAdjointCore(BlockView B, Physics P, RunScalars rs, int stage,
+                                                         int fromSlot, Tile T) {
+  adjointCorePoint<ND, VISC>(B, P, rs, stage, fromSlot, T, blockIdx.x);
+}
+
 // Divergence of the adjoint viscous diffusion, one thread per point and
 // momentum/energy component: t2_c = sum_j D+_j ad_{j,c} (src/RhsHelperImpl.f90:562-564).
 template <int ND>
-__global__ void __launch_bounds__(kMaxTile) kAdjointDiffusion(BlockView B, Tile T) {
+__device__ __forceinline__ void adjointDiffusionPoint(const BlockView& B, const Tile& T, int blk) {
   long long p;
   PointIndex I;
-  if (!locate(B, T, p, I)) return;
+  if (!locate(B, T, blk, p, I)) return;
   constexpr int nV = ND + 1;
   const int c = blockIdx.y;
   const long long N = B.N;
   double s = applyOp<OP_D1ADJ>(B.ad + N * c + I.base[0], I.idx[0], B.ax[0]);
   for (int j = 1; j < ND; ++j) s += applyOp<OP_D1ADJ>(B.ad + N * (j * nV + c) + I.base[j], I.idx[j], B.ax[j]);
   B.t2[p + N * c] = s;
+}
+
+template <int ND>
+__global__ void __launch_bounds__(kMaxTile) kAdjointDiffusion(BlockView B, Tile T) {
+  adjointDiffusionPoint<ND>(B, T, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -581,12 +623,12 @@ __global__ void __launch_bounds__(kMaxTile) kAdjointDiffusion(BlockView B, Tile 
 // that component (src/RK4IntegratorImpl.f90:203-266).
 // ---------------------------------------------------------------------------
 template <int ND, bool VISC>
-__global__ void __launch_bounds__(kMaxTile) kAdjointAssemble(BlockView B, Physics P, RunScalars rs, int rkStage,
-                                                             int stage, double apiFactor, int api, int fromSlot,
-                                                             Tile T) {
+__device__ __forceinline__ void adjointAssemblePoint(const BlockView& B, const Physics& P, const RunScalars& rs,
+                                                     int rkStage, int stage, double apiFactor, int api, int fromSlot,
+                                                     const Tile& T, int blk) {
   long long p;
   PointIndex I;
-  if (!locate(B, T, p, I)) return;
+  if (!locate(B, T, blk, p, I)) return;
   constexpr int nU = ND + 2, E = ND + 1;
   const int c = blockIdx.y;
   const long long N = B.N;
@@ -672,6 +714,13 @@ __global__ void __launch_bounds__(kMaxTile) kAdjointAssemble(BlockView B, Physic
   }
 }
 
+template <int ND, bool VISC>
+__global__ void __launch_bounds__(kMaxTile) kAdjointAssemble(BlockView B, Physics P, RunScalars rs, int rkStage,
+                                                             int stage, double apiFactor, int api, int fromSlot,
+                                                             Tile T) {
+  adjointAssemblePoint<ND, VISC>(B, P, rs, rkStage, stage, apiFactor, api, fromSlot, T, blockIdx.x);
+}
+
 // Adjoint initial condition lambda(T) = factor * adjointForcing(q(T)),
 // factor = -dt/6 (loadInitialCondition ADJOINT, src/SolverImpl.f90:368-427).
 template <int ND>
@@ -747,6 +796,50 @@ __global__ void kReducePartials(const double* __restrict__ partials, int stride,
   for (int b = threadIdx.x; b < count; b += blockDim.x) v += partials[(long long)s * stride + b];
   const double t = blockSum(v);
   if (threadIdx.x == 0) out[s] = t;
+}
+
+// ---------------------------------------------------------------------------
+// Batched forward stage kernels: thread block k works on block map[k].y of
+// instance map[k].x, with that instance's grid, state, run scalars and tile.
+// ---------------------------------------------------------------------------
+template <int ND, bool CURV, bool VISC>
+__global__ void __launch_bounds__(kBatchThreads) kGradFluxBatch(const BatchEntry* __restrict__ E,
+                                                                const int2* __restrict__ map, Physics P, int stage) {
+  const int2 m = map[blockIdx.x];
+  const BatchEntry& e = E[m.x];
+  gradFluxPoint<ND, CURV, VISC>(e.v, P, e.rs, GF_FLUX, stage, e.tGrad, m.y);
+}
+
+template <int ND>
+__global__ void __launch_bounds__(kBatchThreads) kDissipationBatch(const BatchEntry* __restrict__ E,
+                                                                   const int2* __restrict__ map, Physics P) {
+  const int2 m = map[blockIdx.x];
+  const BatchEntry& e = E[m.x];
+  dissipationPoint<ND>(e.v, P, e.v.q, 1.0, e.tDiss, m.y);
+}
+
+template <int ND>
+__global__ void __launch_bounds__(kBatchThreads) kForwardDivergenceBatch(const BatchEntry* __restrict__ E,
+                                                                         const int2* __restrict__ map, Physics P,
+                                                                         int rkStage) {
+  const int2 m = map[blockIdx.x];
+  const BatchEntry& e = E[m.x];
+  forwardDivergencePoint<ND>(e.v, P, e.rs, rkStage, rkStage, e.controller, e.tRhs, m.y);
+}
+
+template <int ND>
+__global__ void __launch_bounds__(kBlock) kPrimsBatch(const BatchEntry* __restrict__ E, const int2* __restrict__ map,
+                                                      Physics P) {
+  const int2 m = map[blockIdx.x];
+  const BatchEntry& e = E[m.x];
+  primsPoint<ND>(e.v, P, e.v.q, 0, e.rs, 0, m.y);
+}
+
+__global__ void __launch_bounds__(kBlock) kFunctionalBatch(const BatchEntry* __restrict__ E,
+                                                           const int2* __restrict__ map, int stage, int pressureComp) {
+  const int2 m = map[blockIdx.x];
+  const BatchEntry& e = E[m.x];
+  functionalBlock(e.v, e.rs, stage, pressureComp, m.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -1085,6 +1178,51 @@ void launchReducePartials(Context& c, const double* partials, int stride, int co
   MGD_LAUNCH(c);
   kReducePartials<<<nSlots, kBlock, 0, c.stream>>>(partials, stride, count, nSlots, out);
 }
+
+void launchBatchGradFlux(Context& c, const BatchLaunch& L, int stage, cudaStream_t s) {
+  const int G = L.blocks[BK_GRAD], W = L.threads[BK_GRAD];
+  const bool curv = c.opts.curvilinear != 0, visc = c.phys.viscous != 0;
+  MGD_LAUNCH(c);
+#define GFB(ND, CU, VI) kGradFluxBatch<ND, CU, VI><<<G, W, 0, s>>>(L.entries, L.map[BK_GRAD], c.phys, stage)
+  if (c.nD == 2) {
+    if (curv) { if (visc) GFB(2, true, true); else GFB(2, true, false); }
+    else { if (visc) GFB(2, false, true); else GFB(2, false, false); }
+  } else {
+    if (curv) { if (visc) GFB(3, true, true); else GFB(3, true, false); }
+    else { if (visc) GFB(3, false, true); else GFB(3, false, false); }
+  }
+#undef GFB
+}
+
+void launchBatchDissipation(Context& c, const BatchLaunch& L, cudaStream_t s) {
+  if (!c.phys.dissipation) return;
+  const dim3 grid(L.blocks[BK_DISS], c.nU);
+  MGD_LAUNCH(c);
+  if (c.nD == 2) kDissipationBatch<2><<<grid, L.threads[BK_DISS], 0, s>>>(L.entries, L.map[BK_DISS], c.phys);
+  else kDissipationBatch<3><<<grid, L.threads[BK_DISS], 0, s>>>(L.entries, L.map[BK_DISS], c.phys);
+}
+
+void launchBatchForwardDivergence(Context& c, const BatchLaunch& L, int rkStage, cudaStream_t s) {
+  const dim3 grid(L.blocks[BK_RHS], c.nU);
+  MGD_LAUNCH(c);
+  if (c.nD == 2)
+    kForwardDivergenceBatch<2><<<grid, L.threads[BK_RHS], 0, s>>>(L.entries, L.map[BK_RHS], c.phys, rkStage);
+  else
+    kForwardDivergenceBatch<3><<<grid, L.threads[BK_RHS], 0, s>>>(L.entries, L.map[BK_RHS], c.phys, rkStage);
+}
+
+void launchBatchPrims(Context& c, const BatchLaunch& L, cudaStream_t s) {
+  MGD_LAUNCH(c);
+  if (c.nD == 2) kPrimsBatch<2><<<L.blocks[BK_PRIMS], kBlock, 0, s>>>(L.entries, L.map[BK_PRIMS], c.phys);
+  else kPrimsBatch<3><<<L.blocks[BK_PRIMS], kBlock, 0, s>>>(L.entries, L.map[BK_PRIMS], c.phys);
+}
+
+void launchBatchFunctional(Context& c, const BatchLaunch& L, int stage, cudaStream_t s) {
+  MGD_LAUNCH(c);
+  kFunctionalBatch<<<L.blocks[BK_FUNC], kBlock, 0, s>>>(L.entries, L.map[BK_FUNC], stage, PrimLayout{c.nD}.p());
+}
+
+void launchStepAdvanceOn(int* counters, int delta, cudaStream_t s) { kStepAdvance<<<1, 32, 0, s>>>(counters, delta); }
 
 int timeStepBlocks(const DevBlock& b) { return gridFor(b.v.N); }
 

@@ -57,6 +57,13 @@ def load_library(build_if_missing=True):
     L.mgd_run_adjoint.argtypes = [ctx, C.POINTER(C.c_double)]
     L.mgd_get_gradient.argtypes = [ctx, C.POINTER(C.c_double), C.c_longlong]
     L.mgd_time_step_size.argtypes = [ctx, C.POINTER(C.c_double)]
+    L.mgd_batch_create.argtypes = [C.POINTER(ctx), C.c_int, C.POINTER(C.c_void_p)]
+    L.mgd_batch_run_forward.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double)]
+    L.mgd_batch_destroy.argtypes = [C.c_void_p]
+    L.mgd_batch_last_error.restype = C.c_char_p
+    L.mgd_batch_last_error.argtypes = [C.c_void_p]
+    L.mgd_batch_kernel_launches.restype = C.c_longlong
+    L.mgd_batch_kernel_launches.argtypes = [C.c_void_p, C.c_int]
     L.mgd_get_step_sizes.argtypes = [ctx, C.POINTER(C.c_double), C.c_int]
     L.mgd_profile_stage_kernels.argtypes = [ctx, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)]
     L.mgd_stream.restype = C.c_void_p
@@ -207,3 +214,35 @@ class Solver:
 
     def kernel_launches(self, reset=False):
         return self.L.mgd_kernel_launches(self.h, int(reset))
+
+
+class Batch:
+    """Forward runs of many Solvers at once (mgd_batch_*): one launch per
+    stage kernel for the whole batch, one CUDA graph per RK4 step. The
+    solvers keep their own grids, states and control forcings."""
+
+    def __init__(self, solvers):
+        self.L = load_library()
+        self.solvers = list(solvers)
+        arr = (C.c_void_p * len(self.solvers))(*[s.h for s in self.solvers])
+        h = C.c_void_p()
+        if self.L.mgd_batch_create(C.cast(arr, C.POINTER(C.c_void_p)), len(self.solvers), C.byref(h)):
+            raise MagudiError(self.L.mgd_batch_last_error(None).decode())
+        self.h = h
+
+    def run_forward(self, n_steps, t0=0.0):
+        costs = np.zeros(len(self.solvers))
+        if self.L.mgd_batch_run_forward(self.h, n_steps, t0, capi.dptr(costs)):
+            raise MagudiError(self.L.mgd_batch_last_error(self.h).decode())
+        return costs
+
+    def kernel_launches(self, reset=False):
+        return self.L.mgd_batch_kernel_launches(self.h, int(reset))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mgd_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

@@ -1,0 +1,69 @@
+"""Batched forward runs (mgd_batch_*) against the single-solve path and the
+oracle (-m gpu): instances of different grid sizes and control amplitudes,
+as in the reference's gradient-accuracy sweep (README.md:118-165)."""
+import numpy as np
+import pytest
+
+import oracle_lib
+from helpers import rel_err, small_monopole
+from magudi_gb300 import capi
+from magudi_gb300.solver import Batch, Solver
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [(41, 37), (33, 45), (49, 29)]
+N_STEPS = 12
+
+
+def _gradient_direction(n, ny):
+    P = small_monopole(n=n, ny=ny, n_steps=N_STEPS, save_interval=4)
+    s = Solver(P)
+    s.run_forward(N_STEPS, 4)
+    s.run_adjoint()
+    return s.gradient(4 * N_STEPS)
+
+
+def _controlled(n, ny, forcing):
+    P = small_monopole(n=n, ny=ny, n_steps=N_STEPS, controller_switch=True)
+    s = Solver(P)
+    s.set_control_forcing(forcing)
+    return P, s
+
+
+def test_batch_matches_single_solves_and_oracle():
+    grads = {sz: _gradient_direction(*sz) for sz in SIZES}
+    amps = [10.0 ** (-2.0 - 0.25 * k) for k in range(6)]
+    cases = [(SIZES[i % len(SIZES)], amps[i]) for i in range(len(amps))]
+    solvers = [_controlled(n, ny, a * grads[(n, ny)])[1] for (n, ny), a in cases]
+    batch = Batch(solvers)
+    batch.kernel_launches(reset=True)
+    costs = batch.run_forward(N_STEPS)
+    assert batch.kernel_launches() > 0
+    for i, ((n, ny), a) in enumerate(cases):
+        P, single = _controlled(n, ny, a * grads[(n, ny)])
+        J = single.run_forward(N_STEPS, N_STEPS)
+        # same kernels per point and the same fixed reduction layout: identical results
+        assert costs[i] == J
+        assert np.array_equal(solvers[i].get_field(1, capi.FIELD_CONSERVED), single.get_field(1, capi.FIELD_CONSERVED))
+        o = oracle_lib.Oracle(P)
+        o.set_control_forcing(a * grads[(n, ny)])
+        Jo = o.run_forward(N_STEPS, keep_stages=False)
+        assert abs(costs[i] - Jo) <= 1e-10 * abs(Jo)
+
+
+def test_batch_rerun_and_reuse():
+    """A batch can run again from new states; the captured graph is reused."""
+    solvers = [Solver(small_monopole(n=n, ny=ny, n_steps=N_STEPS)) for n, ny in SIZES]
+    batch = Batch(solvers)
+    c1 = batch.run_forward(N_STEPS)
+    for s in solvers:
+        s.set_field(1, capi.FIELD_CONSERVED, s.problem.blocks[0].initial_state)
+    c2 = batch.run_forward(N_STEPS)
+    assert np.array_equal(c1, c2)
+
+
+def test_batch_rejects_mismatched_options():
+    a = Solver(small_monopole())
+    b = Solver(small_monopole(dt=0.04))
+    with pytest.raises(Exception):
+        Batch([a, b])
