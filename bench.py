@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rk-steps", type=int, default=N_STEPS,
                     help="RK4 steps per gradient evaluation (profiling runs use a few)")
+    ap.add_argument("--workload", default="gradient", choices=["gradient", "sweep"],
+                    help="gradient: the forward + adjoint gradient evaluation (default); sweep: the batched "
+                         "gradient-check sweep of 64 monopole instances of mixed grid sizes")
+    ap.add_argument("--sweep-instances", type=int, default=64)
     ap.add_argument("--profile-only", action="store_true",
                     help="run the gradient evaluations and exit (for ncu captures; prints no bench line)")
     return ap.parse_args()
@@ -340,10 +344,112 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_sweep(args):
+    """Batched gradient-check sweep: every instance runs the monopole forward
+    with control forcing amplitude x (adjoint gradient of its grid size) and
+    reports its J. One step = the whole sweep through mgd_batch_run_forward;
+    the plain single-solve path (mgd_run_forward per instance) is timed once
+    beside it on the same instances."""
+    import numpy as np
+    import torch
+    from magudi_gb300 import capi, configs, sweep
+    from magudi_gb300.solver import Batch, Solver
+
+    rank, world, local = rank_info()
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    n_steps = args.rk_steps
+    cases = sweep.cases(args.sweep_instances)
+    # instances split over ranks by grid points (independent solves, no collective)
+    mine_idx = sweep.shard(cases, rank, world)
+    mine = [cases[i] for i in mine_idx]
+    grads = {}
+    for n in sorted({n for n, _ in mine}):
+        s = Solver(configs.monopole_2d(n=n, n_steps=n_steps, save_interval=SAVE_INTERVAL))
+        s.run_forward(n_steps, SAVE_INTERVAL)
+        s.run_adjoint()
+        grads[n] = s.gradient(4 * n_steps)
+        s.close()
+    solvers, q0 = [], []
+    for n, a in mine:
+        P = configs.monopole_2d(n=n, n_steps=n_steps, save_interval=SAVE_INTERVAL, controller_switch=True)
+        s = Solver(P)
+        s.set_control_forcing(a * grads[n])
+        solvers.append(s)
+        q0.append(np.ascontiguousarray(P.blocks[0].initial_state))
+    batch = Batch(solvers)
+
+    def reset():
+        for s, q in zip(solvers, q0):
+            s.set_field(1, capi.FIELD_CONSERVED, q)
+
+    for _ in range(args.warmup):
+        reset()
+        batch.run_forward(n_steps)
+    batch.kernel_launches(reset=True)
+    clocks = ClockSampler()
+    clocks.start()
+    times = []
+    costs = None
+    for _ in range(args.steps):
+        reset()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        t = time.perf_counter()
+        costs = batch.run_forward(n_steps)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t)
+    clk = clocks.stop()
+    launches = batch.kernel_launches(reset=True) // args.steps
+    # plain single-solve path on the same instances, once
+    reset()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    plain_costs = [s.run_forward(n_steps, SAVE_INTERVAL) for s in solvers]
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t
+    sec = statistics.mean(times)
+    if world > 1:
+        tt = torch.tensor([sec, t_plain], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        sec, t_plain = float(tt[0]), float(tt[1])
+    pts = sum(n * n for n, _ in cases)
+    max_rel = max(abs(a - b) / abs(b) for a, b in zip(costs, plain_costs))
+    all_costs = sweep.gather_costs(mine_idx, costs, len(cases))
+    line = {
+        "metric": "batched FD-sweep solves/s", "value": len(cases) / sec, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "strong", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (quiescent monopole states, gradient-direction control forcing computed in-process)",
+        "config": {"workload": f"{len(cases)} 2D monopole instances, sizes drawn with seed 0 from "
+                               f"{list(sweep.SIZES)} (squared), control amplitude 10^(-2-0.25k), k = i mod 20, "
+                               f"{n_steps} RK4 steps forward each, one batched launch per stage kernel",
+                   "instances": len(cases), "rk4_steps": n_steps, "total_points": pts,
+                   "l2": "working set (all instances) larger than L2",
+                   "parallelism": f"instances sharded round-robin over {world} GPU(s)" if world > 1 else "single GPU"},
+        "mpt_rhs_per_s": pts * 4 * n_steps / sec / 1e6,
+        "plain_single_solve": {"value": len(cases) / t_plain, "unit": "solves/s", "seconds": t_plain,
+                               "path": "mgd_run_forward per instance, one after another"},
+        "speedup_vs_plain": t_plain / sec,
+        "max_rel_diff_vs_plain_J": max_rel,
+        "J_first": float(all_costs[0]), "J_last": float(all_costs[-1]),
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "sweep":
+        run_sweep(args)
     else:
         run_ours(args)
 

@@ -175,9 +175,17 @@ int mgd_rk4_substep(mgd_ctx* ctx, int mode, double* time, double dt, int stage);
  * last stage of the run, nPatchPoints doubles each
  * (src/ThermalActuatorImpl.f90:161-233, src/ActuatorPatchImpl.f90:226). */
 int mgd_set_control_forcing(mgd_ctx* ctx, const double* host, long long n_entries);
+/* (The forcing and gradient buffers of mgd_set_control_forcing and
+ * mgd_get_gradient may be host or device memory.) */
 
 /* Number of actuator-patch points (the length of one forcing/gradient entry). */
 int mgd_actuator_patch_size(mgd_ctx* ctx, long long* n_points);
+
+/* Quadrature weight H*det of each actuator-patch point in patch order, 0 on
+ * holes (computeQuadratureOnPatches, src/PatchFactoryImpl.f90:376-444):
+ * the weights with which ThermalActuator%computeSensitivity sums the
+ * gradient (src/ThermalActuatorImpl.f90:83-159). out: host or device memory. */
+int mgd_actuator_weights(mgd_ctx* ctx, double* out);
 
 /* Solver%runForward (src/SolverImpl.f90:672-912) from the current conserved
  * variables at time t0 for n_steps RK4 steps; keeps a snapshot every

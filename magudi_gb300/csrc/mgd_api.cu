@@ -118,7 +118,9 @@ int mgd_create(const mgd_options* o, mgd_ctx** out) {
     delete h;
     return 1;
   }
-  if (cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c.stream2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c.side2, cudaStreamNonBlocking) != cudaSuccess) {
     g_createError = "cudaStreamCreate failed";
     cudaStreamDestroy(c.stream);
     delete h;
@@ -128,9 +130,13 @@ int mgd_create(const mgd_options* o, mgd_ctx** out) {
     cudaEventCreateWithFlags(&c.evFork[k], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&c.evJoin[k], cudaEventDisableTiming);
   }
+  for (int k = 0; k < 2; ++k) {
+    cudaEventCreateWithFlags(&c.evRecDone[k], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&c.evAdjDone[k], cudaEventDisableTiming);
+  }
   uploadOperatorTables();
-  cudaMalloc((void**)&c.dCounters, 4 * sizeof(int));
-  const int init[4] = {1, 0, 1, 0};
+  cudaMalloc((void**)&c.dCounters, 8 * sizeof(int));
+  const int init[8] = {1, 0, 1, 0, 1, 0, 0, 0};
   cudaMemcpy(c.dCounters, init, sizeof init, cudaMemcpyHostToDevice);
   cudaMalloc((void**)&c.dApiAmp, MGD_MAX_SOURCES * sizeof(double));
   cudaMemset(c.dApiAmp, 0, MGD_MAX_SOURCES * sizeof(double));
@@ -153,8 +159,15 @@ int mgd_destroy(mgd_ctx* h) {
   cudaFree(c.dSnapshots); cudaFree(c.dStageBuf);
   cudaFree(c.dStepDt); cudaFree(c.dDtPartials); cudaFree(c.dTime);
   if (c.gForward) cudaGraphExecDestroy(c.gForward);
-  if (c.gRecompute) cudaGraphExecDestroy(c.gRecompute);
-  if (c.gAdjoint) cudaGraphExecDestroy(c.gAdjoint);
+  for (int k = 0; k < 2; ++k) {
+    if (c.gRecomputeH[k]) cudaGraphExecDestroy(c.gRecomputeH[k]);
+    if (c.gAdjointH[k]) cudaGraphExecDestroy(c.gAdjointH[k]);
+    cudaEventDestroy(c.evRecDone[k]);
+    cudaEventDestroy(c.evAdjDone[k]);
+  }
+  for (void* p : c.shadowAllocations) cudaFree(p);
+  if (c.stream2) cudaStreamDestroy(c.stream2);
+  if (c.side2) cudaStreamDestroy(c.side2);
   for (int k = 0; k < 8; ++k) {
     cudaEventDestroy(c.evFork[k]);
     cudaEventDestroy(c.evJoin[k]);
@@ -755,6 +768,8 @@ int mgd_finalize_setup(mgd_ctx* h) {
     wT[p] = maskT[p] * b.hostNorm[p];
     wA[p] = maskA[p] * b.hostNorm[p];
   }
+  c.actuatorWeights.assign((size_t)actOffset, 0.0);
+  for (long long k = 0; k < actOffset; ++k) c.actuatorWeights[k] = wA[actPts[k]];
   // acoustic source Gaussians exp(-9/(2 R^2) |x - x0|^2) (src/AcousticSourceImpl.f90:34-64)
   std::vector<double> srcG((size_t)N * std::max<size_t>(1, c.sources.size()), 0.0);
   for (size_t s = 0; s < c.sources.size(); ++s) {
@@ -851,7 +866,7 @@ static RunScalars apiScalars(Context& c) {
   r.step = c.dCounters + 2;
   r.segBase = c.dCounters + 3;
   r.amp = c.dApiAmp;
-  r.dt = c.opts.time_step_size;
+  setStepSize(r, c.opts.time_step_size);
   r.adjointForcingSwitch = c.opts.adjoint_forcing_switch;
   r.nPartialBlocks = reductionBlocks(c.blocks[0]);
   return r;
@@ -879,20 +894,21 @@ namespace mgd {
 // The dissipation kernel runs on the side stream beside the flux kernel; both
 // only read q and join before the divergence kernel updates it.
 void forwardStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bool api, bool controller, bool store,
-                  bool functional) {
+                  bool functional, const Lanes* lanes) {
+  const Lanes L = lanes ? *lanes : Lanes{c.stream, c.side, c.evFork[0], c.evJoin[0]};
   const int stage = api ? 1 : rkStage;
   const bool diss = c.phys.dissipation != 0;
   if (diss) {
-    cudaEventRecord(c.evFork[0], c.stream);
-    cudaStreamWaitEvent(c.side, c.evFork[0], 0);
-    launchDissipation(c, b, b.v.q, 1.0, c.side);
-    cudaEventRecord(c.evJoin[0], c.side);
+    cudaEventRecord(L.fork, L.main);
+    cudaStreamWaitEvent(L.side, L.fork, 0);
+    launchDissipation(c, b, b.v.q, 1.0, L.side);
+    cudaEventRecord(L.join, L.side);
   }
-  launchGradFlux(c, b, true, false, &rs, stage, store);
-  if (diss) cudaStreamWaitEvent(c.stream, c.evJoin[0], 0);
-  launchForwardDivergence(c, b, rkStage, rs, api, controller);
-  if (rkStage > 0) launchPrims(c, b, b.v.q, false);
-  if (functional) launchFunctional(c, b, rs, stage);
+  launchGradFlux(c, b, true, false, &rs, stage, store, L.main);
+  if (diss) cudaStreamWaitEvent(L.main, L.join, 0);
+  launchForwardDivergence(c, b, rkStage, rs, api, controller, L.main);
+  if (rkStage > 0) launchPrims(c, b, b.v.q, false, nullptr, 0, L.main);
+  if (functional) launchFunctional(c, b, rs, stage, L.main);
 }
 
 // One adjoint RK stage (rkStage 4..1) or the adjoint RHS alone (rkStage 0).
@@ -900,19 +916,20 @@ void forwardStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bo
 // kernel read lambda on the side stream beside the core and diffusion
 // kernels; all join before the assembly kernel updates lambda.
 void adjointStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage, double apiFactor, bool api,
-                  bool fromSlot, bool record) {
+                  bool fromSlot, bool record, const Lanes* lanes) {
+  const Lanes L = lanes ? *lanes : Lanes{c.stream, c.side, c.evFork[1], c.evJoin[1]};
   const bool side = c.phys.dissipation != 0 || record;
   if (side) {
-    cudaEventRecord(c.evFork[1], c.stream);
-    cudaStreamWaitEvent(c.side, c.evFork[1], 0);
-    launchDissipation(c, b, b.v.lam, -1.0, c.side);
-    if (record) launchGradientSensitivity(c, b, rs, stage, c.side);
-    cudaEventRecord(c.evJoin[1], c.side);
+    cudaEventRecord(L.fork, L.main);
+    cudaStreamWaitEvent(L.side, L.fork, 0);
+    launchDissipation(c, b, b.v.lam, -1.0, L.side);
+    if (record) launchGradientSensitivity(c, b, rs, stage, L.side);
+    cudaEventRecord(L.join, L.side);
   }
-  launchAdjointCore(c, b, rs, stage, fromSlot);
-  launchAdjointDiffusion(c, b);
-  if (side) cudaStreamWaitEvent(c.stream, c.evJoin[1], 0);
-  launchAdjointAssemble(c, b, rkStage, rs, stage, apiFactor, api, fromSlot);
+  launchAdjointCore(c, b, rs, stage, fromSlot, L.main);
+  launchAdjointDiffusion(c, b, L.main);
+  if (side) cudaStreamWaitEvent(L.main, L.join, 0);
+  launchAdjointAssemble(c, b, rkStage, rs, stage, apiFactor, api, fromSlot, L.main);
 }
 
 }  // namespace mgd
@@ -1030,7 +1047,7 @@ int mgd_rk4_substep(mgd_ctx* h, int mode, double* time, double dt, int stage) {
   if (stage < 1 || stage > 4) return fail(c, "stage must be 1..4");
   DevBlock& b = c.blocks[0];
   RunScalars rs = apiScalars(c);
-  rs.dt = dt;
+  setStepSize(rs, dt);
   if (mode == MGD_FORWARD) {
     if (stage == 2 || stage == 4) *time = *time + dt / 2.0;
     if (setApiTime(c, *time)) return 1;
@@ -1060,14 +1077,34 @@ int mgd_actuator_patch_size(mgd_ctx* h, long long* n) {
 int mgd_set_control_forcing(mgd_ctx* h, const double* host, long long n_entries) {
   Context& c = h->c;
   if (requireReady(c)) return 1;
-  cudaFree(c.dForcing);
-  c.dForcing = nullptr;
   c.nForcingEntries = 0;
-  const size_t n = (size_t)std::max(0LL, n_entries) * c.actuatorPoints;
-  if (n == 0) return 0;
-  CUDA_TRY(c, cudaMalloc((void**)&c.dForcing, n * sizeof(double)));
-  CUDA_TRY(c, cudaMemcpy(c.dForcing, host, n * sizeof(double), cudaMemcpyHostToDevice));
+  const long long n = std::max(0LL, n_entries) * c.actuatorPoints;
+  if (n == 0) {
+    cudaFree(c.dForcing);
+    c.dForcing = nullptr;
+    c.forcingCapacity = 0;
+    return 0;
+  }
+  if (c.forcingCapacity < n) {
+    cudaFree(c.dForcing);
+    c.dForcing = nullptr;
+    c.forcingCapacity = 0;
+    CUDA_TRY(c, cudaMalloc((void**)&c.dForcing, (size_t)n * sizeof(double)));
+    c.forcingCapacity = n;
+  }
+  CUDA_TRY(c, cudaMemcpyAsync(c.dForcing, host, (size_t)n * sizeof(double), cudaMemcpyDefault, c.stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   c.nForcingEntries = n_entries;
+  return 0;
+}
+
+int mgd_actuator_weights(mgd_ctx* h, double* out) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  if (c.actuatorWeights.empty()) return 0;
+  CUDA_TRY(c, cudaMemcpyAsync(out, c.actuatorWeights.data(), c.actuatorWeights.size() * sizeof(double),
+                              cudaMemcpyDefault, c.stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   return 0;
 }
 
@@ -1088,8 +1125,8 @@ static RunScalars runScalars(Context& c) {
   r.stageBuf = c.dStageBuf;
   r.slotStride = c.slotStride;
   r.slotFull = c.slotFull;
-  r.dtStep = c.dStepDt;
-  r.dt = c.opts.time_step_size;
+  r.rk = c.dStepDt;
+  setStepSize(r, c.opts.time_step_size);
   r.adjointForcingSwitch = c.opts.adjoint_forcing_switch;
   return r;
 }
@@ -1100,19 +1137,21 @@ static int setCounters(Context& c, int step, int segBase) {
   return 0;
 }
 
-// Captures `body` into an executable graph on the context stream.
-// The kernels recorded during capture are counted per graph launch instead.
+// Captures `body` into an executable graph on stream s (the context stream
+// when 0). The kernels recorded during capture are counted per graph launch
+// instead.
 template <class F>
-static int capture(Context& c, cudaGraphExec_t* exec, long long* nodes, F body) {
+static int capture(Context& c, cudaGraphExec_t* exec, long long* nodes, F body, cudaStream_t s = 0) {
+  if (!s) s = c.stream;
   if (*exec) {
     cudaGraphExecDestroy(*exec);
     *exec = nullptr;
   }
   cudaGraph_t g = nullptr;
   const long long before = c.launches;
-  CUDA_TRY(c, cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+  CUDA_TRY(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   body();
-  CUDA_TRY(c, cudaStreamEndCapture(c.stream, &g));
+  CUDA_TRY(c, cudaStreamEndCapture(s, &g));
   *nodes = c.launches - before;
   c.launches = before;
   CUDA_TRY(c, cudaGraphInstantiate(exec, g, 0));
@@ -1123,11 +1162,11 @@ static int capture(Context& c, cudaGraphExec_t* exec, long long* nodes, F body) 
 // Per-step step sizes of a run, the constant-CFL reduction scratch and the
 // device copy of the run time.
 static int ensureStepBuffers(Context& c, DevBlock& b, int nSteps) {
-  if (c.stepDtCapacity < nSteps) {
+  if (c.stepDtCapacity < 4LL * nSteps) {
     cudaFree(c.dStepDt);
     c.dStepDt = nullptr;
-    CUDA_TRY(c, cudaMalloc((void**)&c.dStepDt, (size_t)nSteps * sizeof(double)));
-    c.stepDtCapacity = nSteps;
+    CUDA_TRY(c, cudaMalloc((void**)&c.dStepDt, (size_t)4 * nSteps * sizeof(double)));
+    c.stepDtCapacity = 4LL * nSteps;
   }
   const int nb = timeStepBlocks(b);
   if (c.dtPartialCapacity < nb) {
@@ -1148,23 +1187,57 @@ static int ensureStageBuffer(Context& c, DevBlock& b, int S) {
   const int nD = c.nD, nU = c.nU;
   const long long qOnly = (long long)nU * N;
   const long long full = (long long)(nU + PrimLayout{nD}.count() + nD * nD + nD) * N;
-  const long long needFull = 4LL * S * full;
-  if (c.stageBufCapacity >= needFull) {
-    c.slotStride = full;
-    c.slotFull = 1;
-    return 0;
-  }
-  cudaFree(c.dStageBuf);
-  c.dStageBuf = nullptr;
-  c.stageBufCapacity = 0;
+  // preference: two halves of full slots (recomputation beside the adjoint),
+  // one half of full slots, one half of q-only slots
+  const long long options[3][3] = {{2, full, 4LL * S * full}, {1, full, 4LL * S * full}, {1, qOnly, 4LL * S * qOnly}};
   size_t freeB = 0, totalB = 0;
   CUDA_TRY(c, cudaMemGetInfo(&freeB, &totalB));
-  const bool useFull = (double)needFull * sizeof(double) <= 0.5 * (double)freeB;
-  const long long need = useFull ? needFull : 4LL * S * qOnly;
-  CUDA_TRY(c, cudaMalloc((void**)&c.dStageBuf, (size_t)need * sizeof(double)));
-  c.stageBufCapacity = need;
-  c.slotStride = useFull ? full : qOnly;
-  c.slotFull = useFull ? 1 : 0;
+  const double budget = 0.5 * ((double)freeB + (double)c.stageBufCapacity * sizeof(double));
+  int pick = 2;
+  for (int k = 0; k < 3; ++k)
+    if ((double)(options[k][0] * options[k][2]) * sizeof(double) <= budget) {
+      pick = k;
+      break;
+    }
+  const long long need = options[pick][0] * options[pick][2];
+  if (c.stageBufCapacity < need) {
+    cudaFree(c.dStageBuf);
+    c.dStageBuf = nullptr;
+    c.stageBufCapacity = 0;
+    CUDA_TRY(c, cudaMalloc((void**)&c.dStageBuf, (size_t)need * sizeof(double)));
+    c.stageBufCapacity = need;
+  }
+  c.stageHalves = (int)options[pick][0];
+  c.stageHalf = options[pick][2];
+  c.slotStride = options[pick][1];
+  c.slotFull = options[pick][1] == full ? 1 : 0;
+  return 0;
+}
+
+// Forward work arrays of the recomputation that runs beside the adjoint: its
+// own state, primitives, fluxes, dissipation, RK buffers and SAT vectors over
+// the block's grid and patch data.
+static int ensureShadow(Context& c, DevBlock& b) {
+  if (c.shadowReady) return 0;
+  const long long N = b.v.N;
+  const int nD = c.nD, nU = c.nU;
+  BlockView v = b.v;
+  auto alloc = [&](double** p, long long n) -> cudaError_t {
+    cudaError_t e = cudaMalloc((void**)p, (size_t)std::max(1LL, n) * sizeof(double));
+    if (e == cudaSuccess) c.shadowAllocations.push_back(*p);
+    return e;
+  };
+  double* ffv = nullptr;
+  cudaError_t e = cudaSuccess;
+  for (auto x : {alloc(&v.q, N * nU), alloc(&v.prim, N * PrimLayout{nD}.count()), alloc(&v.fhat, N * nD * nU),
+                 alloc(&v.dq, N * nD * nU), alloc(&v.b1, N * nU), alloc(&v.b2, N * nU),
+                 alloc(&ffv, (long long)v.ff.n * nU)})
+    if (x != cudaSuccess) e = x;
+  if (e != cudaSuccess) return fail(c, std::string("device allocation failed for the recomputation: ") +
+                                           cudaGetErrorString(e));
+  v.ff.visc = ffv;
+  c.shadow = v;
+  c.shadowReady = true;
   return 0;
 }
 
@@ -1206,7 +1279,14 @@ int prepareForwardRun(Context& c, int n_steps, int save_interval, double t0, boo
         c.stageTimes[(size_t)4 * s + i - 1] = t;
       }
     c.stepDt.assign(n_steps, dt);
-    CUDA_TRY(c, cudaMemcpy(c.dStepDt, c.stepDt.data(), n_steps * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<double> rk((size_t)4 * n_steps);
+    for (int s = 0; s < n_steps; ++s) {
+      rk[4 * s] = dt;
+      rk[4 * s + 1] = dt / 6.0;
+      rk[4 * s + 2] = dt / 3.0;
+      rk[4 * s + 3] = dt / 2.0;
+    }
+    CUDA_TRY(c, cudaMemcpy(c.dStepDt, rk.data(), rk.size() * sizeof(double), cudaMemcpyHostToDevice));
     std::vector<double> amp(nAmp, 0.0);
     const double pi = 4.0 * std::atan(1.0);
     for (long long k = 0; k < 4LL * n_steps; ++k)
@@ -1243,9 +1323,12 @@ int prepareForwardRun(Context& c, int n_steps, int save_interval, double t0, boo
 int finishForwardRun(Context& c, double* cost) {
   const int n_steps = c.runSteps;
   if (c.opts.use_constant_cfl) {
-    c.stepDt.resize(n_steps);
-    CUDA_TRY(c, cudaMemcpyAsync(c.stepDt.data(), c.dStepDt, n_steps * sizeof(double), cudaMemcpyDeviceToHost,
+    std::vector<double> rk((size_t)4 * n_steps);
+    CUDA_TRY(c, cudaMemcpyAsync(rk.data(), c.dStepDt, rk.size() * sizeof(double), cudaMemcpyDeviceToHost,
                                 c.stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+    c.stepDt.resize(n_steps);
+    for (int s = 0; s < n_steps; ++s) c.stepDt[s] = rk[4 * s];
   }
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   double J = 0.0;
@@ -1297,41 +1380,93 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   const int nU = c.nU, T = c.runSteps, S = c.saveInterval;
   const double dtT = c.stepDt[T - 1];  // step size of the final forward step
   if (ensureStageBuffer(c, b, S)) return 1;
+  const bool twoLanes = c.stageHalves == 2;
+  if (twoLanes && ensureShadow(c, b)) return 1;
   const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
-  RunScalars rs = runScalars(c);
   const bool full = c.slotFull != 0;
+  // The recomputation of segment k-1 runs on the second lanes (own work
+  // arrays, own step counters, the other half of the stage buffer) while the
+  // adjoint consumes segment k; with one half they alternate on one stream.
+  DevBlock rb;
+  rb.desc = b.desc;
+  rb.v = twoLanes ? c.shadow : b.v;
+  rb.tGrad = b.tGrad; rb.tDiss = b.tDiss; rb.tRhs = b.tRhs;
+  rb.tAdjA = b.tAdjA; rb.tAdjD = b.tAdjD; rb.tAdjB = b.tAdjB;
+  const Lanes adjLanes{c.stream, c.side, c.evFork[1], c.evJoin[1]};
+  const Lanes recLanes = twoLanes ? Lanes{c.stream2, c.side2, c.evFork[2], c.evJoin[2]}
+                                  : Lanes{c.stream, c.side, c.evFork[0], c.evJoin[0]};
+  int* recCounters = twoLanes ? c.dCounters + 4 : c.dCounters;
   // adjoint initial condition at the final state (its primitives are current)
   launchPrims(c, b, b.v.q, false);
   launchAdjointInitial(c, b, c.opts.adjoint_forcing_switch ? -dtT / 6.0 : 0.0);
-  if (capture(c, &c.gRecompute, &c.nodesRecompute, [&]() {
-        for (int i = 1; i <= 4; ++i) forwardStage(c, b, i, rs, false, controller, true, false);
-        launchStepAdvance(c, 1);
-      }))
-    return 1;
-  if (capture(c, &c.gAdjoint, &c.nodesAdjoint, [&]() {
-        for (int i = 4; i >= 1; --i) {
-          if (!full) {
-            // restore the forward state of this stage from its slot
-            launchPrims(c, b, nullptr, true, &rs, i);
-            if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs, i, false);
+  long long nodesRec = 0, nodesAdj = 0;
+  for (int half = 0; half < c.stageHalves; ++half) {
+    RunScalars ra = runScalars(c);
+    ra.stageBuf = c.dStageBuf + half * c.stageHalf;
+    RunScalars rr = ra;
+    rr.step = recCounters;
+    rr.segBase = recCounters + 1;
+    if (capture(c, &c.gRecomputeH[half], &nodesRec, [&]() {
+          for (int i = 1; i <= 4; ++i) forwardStage(c, rb, i, rr, false, controller, true, false, &recLanes);
+          launchStepAdvanceOn(recCounters, 1, recLanes.main);
+        }, recLanes.main))
+      return 1;
+    if (capture(c, &c.gAdjointH[half], &nodesAdj, [&]() {
+          for (int i = 4; i >= 1; --i) {
+            if (!full) {
+              // restore the forward state of this stage from its slot
+              launchPrims(c, b, nullptr, true, &ra, i, adjLanes.main);
+              if (c.phys.viscous) launchGradFlux(c, b, false, true, &ra, i, false, adjLanes.main);
+            }
+            adjointStage(c, b, i, ra, i, 0.0, false, full, true, &adjLanes);
           }
-          adjointStage(c, b, i, rs, i, 0.0, false, full, true);
-        }
-        launchStepAdvance(c, -1);
-      }))
-    return 1;
+          launchStepAdvanceOn(c.dCounters, -1, adjLanes.main);
+        }, adjLanes.main))
+      return 1;
+  }
+  c.nodesRecompute = nodesRec + 3;
+  c.nodesAdjoint = nodesAdj + 1;
   const int nSeg = (T + S - 1) / S;
+  // UniformCheckpointer: reload the snapshot of segment k and recompute its stages
+  auto recompute = [&](int k) -> int {
+    const int L = k * S, end = std::min(T, L + S);
+    const int half = k % c.stageHalves;
+    CUDA_TRY(c, cudaMemcpyAsync(rb.v.q, c.dSnapshots + (size_t)k * nU * N, (size_t)nU * N * sizeof(double),
+                                cudaMemcpyDeviceToDevice, recLanes.main));
+    launchPrims(c, rb, rb.v.q, false, nullptr, 0, recLanes.main);
+    launchSetCounters(recCounters, L + 1, L, recLanes.main);
+    for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gRecomputeH[half], recLanes.main));
+    c.launches += 2 + (long long)(end - L) * nodesRec;
+    if (twoLanes) CUDA_TRY(c, cudaEventRecord(c.evRecDone[half], recLanes.main));
+    return 0;
+  };
+  if (twoLanes) {
+    // the second lanes start after everything issued so far on the main stream
+    CUDA_TRY(c, cudaEventRecord(c.evFork[3], c.stream));
+    CUDA_TRY(c, cudaStreamWaitEvent(c.stream2, c.evFork[3], 0));
+  }
+  if (recompute(nSeg - 1)) return 1;
   for (int k = nSeg - 1; k >= 0; --k) {
     const int L = k * S, end = std::min(T, L + S);
-    // UniformCheckpointer: reload the snapshot and recompute the segment's stages
-    CUDA_TRY(c, cudaMemcpyAsync(b.v.q, c.dSnapshots + (size_t)k * nU * N, (size_t)nU * N * sizeof(double),
-                                cudaMemcpyDeviceToDevice, c.stream));
-    launchPrims(c, b, b.v.q, false);
-    if (setCounters(c, L + 1, L)) return 1;
-    for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gRecompute, c.stream));
-    if (setCounters(c, end, L)) return 1;
-    for (int s = end; s >= L + 1; --s) CUDA_TRY(c, cudaGraphLaunch(c.gAdjoint, c.stream));
-    c.launches += (long long)(end - L) * (c.nodesRecompute + c.nodesAdjoint);
+    const int half = k % c.stageHalves;
+    if (twoLanes) {
+      CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.evRecDone[half], 0));
+      if (k >= 1) {
+        // segment k-1 reuses the half that the adjoint of segment k+1 read
+        if (k + 1 <= nSeg - 1) CUDA_TRY(c, cudaStreamWaitEvent(c.stream2, c.evAdjDone[(k + 1) % 2], 0));
+        if (recompute(k - 1)) return 1;
+      }
+    }
+    launchSetCounters(c.dCounters, end, L, c.stream);
+    for (int s = end; s >= L + 1; --s) CUDA_TRY(c, cudaGraphLaunch(c.gAdjointH[half], c.stream));
+    c.launches += 1 + (long long)(end - L) * nodesAdj;
+    if (twoLanes) CUDA_TRY(c, cudaEventRecord(c.evAdjDone[half], c.stream));
+    if (!twoLanes && k >= 1 && recompute(k - 1)) return 1;
+  }
+  if (twoLanes) {
+    // join the second lanes back into the main stream
+    CUDA_TRY(c, cudaEventRecord(c.evJoin[3], c.stream2));
+    CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.evJoin[3], 0));
   }
   if (checkLaunch(c)) return 1;
   std::vector<double> vals;
@@ -1377,7 +1512,8 @@ int mgd_get_gradient(mgd_ctx* h, double* host, long long n_entries) {
   const long long avail = 4LL * c.runSteps;
   const long long n = std::min(n_entries, avail) * c.actuatorPoints;
   if (n <= 0) return 0;
-  CUDA_TRY(c, cudaMemcpy(host, c.dGradient, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+  CUDA_TRY(c, cudaMemcpyAsync(host, c.dGradient, (size_t)n * sizeof(double), cudaMemcpyDefault, c.stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   return 0;
 }
 

@@ -405,4 +405,101 @@ __device__ __forceinline__ void secondPartialViscousTransposeProduct(
   y[ND] += jac * (k * t1) * w[ND];
 }
 
+// Cartesian-grid forms of the two products above, for a metric row with a
+// single non-zero entry a at component K (row K of a diagonal metric). Terms
+// that the general forms multiply by a zero metric entry are dropped, which
+// leaves the remaining arithmetic unchanged; K, I and J are compile-time
+// constants once the callers' loops are unrolled. nTv = n g v / T is passed
+// in (it does not depend on the metric).
+template <int ND, bool VISC>
+__device__ __forceinline__ void addFluxJacobianTransposeProductCart(
+    int K, double a, const double* u, double T, double v, double g, double nTv,
+    const double* tau, const double* hf, const double* w, double* y) {
+  constexpr int E = ND + 1;
+  const double U = a * u[K];
+  double u2 = u[0] * u[0];
+  for (int d = 1; d < ND; ++d) u2 += u[d] * u[d];
+  const double phi2 = 0.5 * (g - 1.0) * u2;
+  double ct[3] = {0.0, 0.0, 0.0}, t1 = 0.0, uct = 0.0;
+  if (VISC) {
+    for (int c = 0; c < ND; ++c) ct[c] = a * tau[ND * c + K];
+    const double cq = a * hf[K];
+    uct = u[0] * ct[0];
+    for (int d = 1; d < ND; ++d) uct += u[d] * ct[d];
+    t1 = uct - cq;
+  }
+  {
+    double s = 0.0;
+    for (int d = 0; d < ND; ++d) s += (d == K ? phi2 * a - U * u[d] : -(U * u[d])) * w[1 + d];
+    s += U * ((g - 2.0) / (g - 1.0) * phi2 - T) * w[E];
+    if (VISC) {
+      const double t2 = nTv * (phi2 / (g - 1.0) - T / g);
+      double sb = 0.0;
+      for (int d = 0; d < ND; ++d) sb += t2 * ct[d] * w[1 + d];
+      sb += (t2 * t1 - v * uct) * w[E];
+      s -= sb;
+    }
+    y[0] += s;
+  }
+  for (int c = 0; c < ND; ++c) {
+    double s;
+    if (c == K) {
+      s = a * w[0];
+      for (int d = 0; d < ND; ++d) {
+        const double q = d == c ? U - (g - 2.0) * u[c] * a : u[d] * a;
+        s += q * w[1 + d];
+      }
+      s += ((T + phi2 / (g - 1.0)) * a - (g - 1.0) * U * u[c]) * w[E];
+    } else {
+      s = 0.0;
+      for (int d = 0; d < ND; ++d) {
+        if (d == c) s += U * w[1 + d];
+        else if (d == K) s += -((g - 1.0) * u[c] * a) * w[1 + d];
+      }
+      s += -((g - 1.0) * U * u[c]) * w[E];
+    }
+    if (VISC) {
+      const double t2 = -nTv * u[c];
+      double sb = 0.0;
+      for (int d = 0; d < ND; ++d) sb += t2 * ct[d] * w[1 + d];
+      sb += (t2 * t1 + v * ct[c]) * w[E];
+      s -= sb;
+    }
+    y[1 + c] += s;
+  }
+  {
+    double s = (g - 1.0) * a * w[1 + K];
+    s += g * U * w[E];
+    if (VISC) {
+      double sb = 0.0;
+      for (int d = 0; d < ND; ++d) sb += nTv * ct[d] * w[1 + d];
+      sb += nTv * t1 * w[E];
+      s -= sb;
+    }
+    y[E] += s;
+  }
+}
+
+// B2(a e_I, b e_J)^T w for diagonal metrics (second partial viscous Jacobian).
+template <int ND>
+__device__ __forceinline__ void secondPartialViscousTransposeProductCart(
+    const double* u, double mu, double la, double k, double jac, int I, double a, int J, double b,
+    const double* w, double* y) {
+  const double t2 = mu * (b * u[J]);
+  const double t3 = la * (a * u[I]);
+  if (I != J) {
+    // t1 = 0: only the (c = I, r = J) and (c = J, r = I) entries survive
+    y[I] += jac * ((mu * a * b) * w[J] + (a * t2) * w[ND]);
+    y[J] += jac * ((la * a * b) * w[I] + (b * t3) * w[ND]);
+    return;
+  }
+  const double t1 = a * b;
+  for (int c = 0; c < ND; ++c) {
+    const double bcc = c == I ? mu * t1 + (mu + la) * a * b : mu * t1;
+    const double e = c == I ? mu * t1 * u[c] + a * t2 + b * t3 : mu * t1 * u[c];
+    y[c] += jac * (bcc * w[c] + e * w[ND]);
+  }
+  y[ND] += jac * (k * t1) * w[ND];
+}
+
 }  // namespace mgd

@@ -116,14 +116,25 @@ struct RunScalars {
   double* stageBuf;       // stage inputs of the current segment (4*S slots)
   long long slotStride;   // doubles per stage slot
   int slotFull;           // slots hold q, primitives, stress and heat flux (else q only)
-  double dt;              // step size when dtStep is null
-  const double* dtStep;   // step size of each step (indexed by step - 1), or null
+  double dt, h6, h3, h2;   // step size and dt/6, dt/3, dt/2 when rk is null
+  const double* rk;        // per step (indexed by step - 1): dt, dt/6, dt/3, dt/2; or null
   int adjointForcingSwitch;
 };
 
-// Step size of the current step of a run (or the per-call step size).
-__device__ __forceinline__ double stepDt(const RunScalars& rs) {
-  return rs.dtStep ? rs.dtStep[*rs.step - 1] : rs.dt;
+// RK4 coefficients of the current step of a run (or of the per-call step).
+struct RkCoeffs {
+  double dt, h6, h3, h2;
+};
+__device__ __forceinline__ RkCoeffs rkCoeffs(const RunScalars& rs) {
+  if (!rs.rk) return {rs.dt, rs.h6, rs.h3, rs.h2};
+  const double* k = rs.rk + 4LL * (*rs.step - 1);
+  return {k[0], k[1], k[2], k[3]};
+}
+inline void setStepSize(RunScalars& rs, double dt) {
+  rs.dt = dt;
+  rs.h6 = dt / 6.0;
+  rs.h3 = dt / 3.0;
+  rs.h2 = dt / 2.0;
 }
 
 struct DevBlock {
@@ -142,6 +153,13 @@ struct DevBlock {
   // ffOfPoint etc. are built on the host at finalize
 };
 
+// A main stream, a side stream for the concurrent branch of a stage, and the
+// fork/join events between them.
+struct Lanes {
+  cudaStream_t main, side;
+  cudaEvent_t fork, join;
+};
+
 struct Context {
   mgd_options opts;
   Physics phys;
@@ -149,6 +167,9 @@ struct Context {
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;          // second stream for concurrent graph branches
   cudaEvent_t evFork[8] = {}, evJoin[8] = {};
+  // lanes of the checkpoint recomputation, which runs beside the adjoint
+  cudaStream_t stream2 = nullptr, side2 = nullptr;
+  cudaEvent_t evRecDone[2] = {}, evAdjDone[2] = {};
   int device = 0;
   std::string error;
   std::vector<DevBlock> blocks;
@@ -157,13 +178,16 @@ struct Context {
   bool finalized = false;
   long long launches = 0;
   long long actuatorPoints = 0;
-  // device scalars: [0] step, [1] segBase, [2] api step (always 1), [3] api segBase
+  // device scalars: [0] step, [1] segBase, [2] api step (always 1), [3] api segBase,
+  // [4] step and [5] segBase of the checkpoint recomputation
   int* dCounters = nullptr;
   double* dApiAmp = nullptr;
   double* dAmp = nullptr;           // per-stage source amplitudes of the run
   long long ampCapacity = 0;
   double* dForcing = nullptr;       // control forcing entries
   long long nForcingEntries = 0;
+  long long forcingCapacity = 0;
+  std::vector<double> actuatorWeights;  // quadrature weight of each actuator-patch point
   double* dGradient = nullptr;      // gradient entries
   long long gradientCapacity = 0;
   double* dPartials = nullptr;      // stage partial sums
@@ -176,18 +200,25 @@ struct Context {
   std::vector<double> stageTimes;   // time of every forward stage of the run
   double* dSnapshots = nullptr;     // (nSnap) x nU x N per block (single block supported)
   long long snapshotCapacity = 0;
-  double* dStageBuf = nullptr;
+  double* dStageBuf = nullptr;       // two halves of 4*S slots (ping-pong between segments)
   long long stageBufCapacity = 0;
+  long long stageHalf = 0;          // doubles per half
+  int stageHalves = 1;
+  // forward work arrays of the recomputation (q, prim, fhat, dq, b1, b2, SAT vectors)
+  std::vector<void*> shadowAllocations;
+  BlockView shadow{};
+  bool shadowReady = false;
   long long slotStride = 0;         // doubles per stage slot of dStageBuf
   int slotFull = 0;                 // slots also hold primitives, stress and heat flux
-  // step sizes of the last run, constant-CFL reduction scratch and run time
+  // RK4 coefficients per step of the last run (dt, dt/6, dt/3, dt/2), their
+  // step sizes on the host, constant-CFL reduction scratch and run time
   double* dStepDt = nullptr;
   long long stepDtCapacity = 0;
   std::vector<double> stepDt;
   double* dDtPartials = nullptr;
   long long dtPartialCapacity = 0;
   double* dTime = nullptr;
-  cudaGraphExec_t gForward = nullptr, gRecompute = nullptr, gAdjoint = nullptr;
+  cudaGraphExec_t gForward = nullptr, gRecomputeH[2] = {}, gAdjointH[2] = {};
   long long nodesForward = 0, nodesRecompute = 0, nodesAdjoint = 0;
 };
 
@@ -213,9 +244,9 @@ struct BatchLaunch {
 
 // ----- stage orchestration (mgd_api.cu) -----
 void forwardStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bool api, bool controller, bool store,
-                  bool functional);
+                  bool functional, const Lanes* lanes = nullptr);
 void adjointStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage, double apiFactor, bool api,
-                  bool fromSlot, bool record);
+                  bool fromSlot, bool record, const Lanes* lanes = nullptr);
 
 int prepareForwardRun(Context& c, int n_steps, int save_interval, double t0, bool snapshots);
 int finishForwardRun(Context& c, double* cost);
@@ -258,8 +289,9 @@ void launchSnapshot(Context& c, DevBlock& b, double* snapshots, int saveInterval
 void launchStepAdvance(Context& c, int delta, cudaStream_t s = 0);
 void launchReducePartials(Context& c, const double* partials, int stride, int count, int nSlots, double* out);
 // Constant-CFL step size of the current primitives: with step == null writes
-// the step size to dtOut[0]; otherwise writes dtOut[*step - 1], advances *time
-// over the step's four stages and stores the stages' source amplitudes in amp.
+// the step size to dtOut[0]; otherwise writes dt, dt/6, dt/3, dt/2 to
+// dtOut[4 (*step - 1) + 0..3], advances *time over the step's four stages and
+// stores the stages' source amplitudes in amp.
 void launchTimeStep(Context& c, DevBlock& b, double* partials, double* dtOut, const int* step, double* time,
                     double* amp, cudaStream_t s = 0);
 int timeStepBlocks(const DevBlock& b);
@@ -275,6 +307,7 @@ void launchBatchForwardDivergence(Context& c, const BatchLaunch& L, int rkStage,
 void launchBatchPrims(Context& c, const BatchLaunch& L, cudaStream_t s);
 void launchBatchFunctional(Context& c, const BatchLaunch& L, int stage, cudaStream_t s);
 void launchStepAdvanceOn(int* counters, int delta, cudaStream_t s);
+void launchSetCounters(int* counters, int step, int segBase, cudaStream_t s);
 constexpr int kBatchThreads = 128;
 
 // Blocks of the fixed-layout reductions (functional, sensitivity).

@@ -431,8 +431,8 @@ __device__ __forceinline__ void forwardDivergencePoint(const BlockView& B, const
     B.rhs[kc] = r;
     return;
   }
-  const double dt = stepDt(rs);
-  const double h6 = dt / 6.0, h3 = dt / 3.0, h2 = dt / 2.0;
+  const RkCoeffs k = rkCoeffs(rs);
+  const double h6 = k.h6, h3 = k.h3, h2 = k.h2, dt = k.dt;
   switch (rkStage) {
     case 1:
       B.b1[kc] = q;
@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(kBlock) kGradientSensitivity(BlockView B, RunS
 // penalty (src/RhsHelperImpl.f90:89-250) folded into the same sweep, and
 // the complete far-field adjoint SAT vector (src/FarFieldPatchImpl.f90:237-257).
 // ---------------------------------------------------------------------------
-template <int ND, bool VISC>
+template <int ND, bool CURV, bool VISC>
 __device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physics& P, const RunScalars& rs,
                                                  int stage, int fromSlot, const Tile& T, int blk) {
   long long p;
@@ -522,7 +522,7 @@ __device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physi
 #pragma unroll
     for (int c = 0; c < nU; ++c) w[i][c] = applyOp<OP_D1ADJ>(B.lam + N * c + I.base[i], I.idx[i], B.ax[i]);
   double m[ND * ND];
-  for (int c = 0; c < ND * ND; ++c) m[c] = B.metrics[p + N * c];
+  for (int c = 0; c < ND * ND; ++c) m[c] = (CURV || (c % (ND + 1)) == 0) ? B.metrics[p + N * c] : 0.0;
   double u[ND];
   for (int d = 0; d < ND; ++d) u[d] = fs.prim[p + N * L.u(d)];
   const double v = fs.prim[p + N * L.v()], Tm = fs.prim[p + N * L.T()];
@@ -533,9 +533,16 @@ __device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physi
   }
   double y[nU];
   for (int c = 0; c < nU; ++c) y[c] = 0.0;
+  if (CURV) {
 #pragma unroll
-  for (int i = 0; i < ND; ++i)
-    addFluxJacobianTransposeProduct<ND, VISC>(m + ND * i, u, Tm, v, P.g, P.powerLawExponent, tau, hf, w[i], y);
+    for (int i = 0; i < ND; ++i)
+      addFluxJacobianTransposeProduct<ND, VISC>(m + ND * i, u, Tm, v, P.g, P.powerLawExponent, tau, hf, w[i], y);
+  } else {
+    const double nTv = VISC ? P.powerLawExponent * P.g * v / Tm : 0.0;
+#pragma unroll
+    for (int i = 0; i < ND; ++i)
+      addFluxJacobianTransposeProductCart<ND, VISC>(i, m[ND * i + i], u, Tm, v, P.g, nTv, tau, hf, w[i], y);
+  }
   for (int c = 0; c < nU; ++c) B.rcore[p + N * c] = y[c];
   double lp[nU];
   for (int c = 0; c < nU; ++c) lp[c] = B.lam[p + N * c];
@@ -546,11 +553,17 @@ __device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physi
     la = fs.prim[p + N * L.la()];
     kd = fs.prim[p + N * L.k()];
     double ad[ND][nV];
+#pragma unroll
     for (int j = 0; j < ND; ++j) {
       for (int c = 0; c < nV; ++c) ad[j][c] = 0.0;
 #pragma unroll
-      for (int i = 0; i < ND; ++i)
-        secondPartialViscousTransposeProduct<ND>(u, mu, la, kd, jac, m + ND * i, m + ND * j, &w[i][1], ad[j]);
+      for (int i = 0; i < ND; ++i) {
+        if (CURV)
+          secondPartialViscousTransposeProduct<ND>(u, mu, la, kd, jac, m + ND * i, m + ND * j, &w[i][1], ad[j]);
+        else
+          secondPartialViscousTransposeProductCart<ND>(u, mu, la, kd, jac, i, m[ND * i + i], j, m[ND * j + j],
+                                                       &w[i][1], ad[j]);
+      }
     }
     for (int k = 0; k < 3; ++k) {
       const int e = B.ffOfPoint[3 * p + k];
@@ -588,10 +601,10 @@ __device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physi
   }
 }
 
-template <int ND, bool VISC>
+template <int ND, bool CURV, bool VISC>
 __global__ void __launch_bounds__(kMaxTile) kAdjointCore(BlockView B, Physics P, RunScalars rs, int stage,
                                                          int fromSlot, Tile T) {
-  adjointCorePoint<ND, VISC>(B, P, rs, stage, fromSlot, T, blockIdx.x);
+  adjointCorePoint<ND, CURV, VISC>(B, P, rs, stage, fromSlot, T, blockIdx.x);
 }
 
 // Divergence of the adjoint viscous diffusion, one thread per point and
@@ -692,8 +705,8 @@ __device__ __forceinline__ void adjointAssemblePoint(const BlockView& B, const P
     B.rhs[kc] = r;
     return;
   }
-  const double dt = stepDt(rs);
-  const double h6 = dt / 6.0, h3 = dt / 3.0, h2 = dt / 2.0;
+  const RkCoeffs k = rkCoeffs(rs);
+  const double h6 = k.h6, h3 = k.h3, h2 = k.h2, dt = k.dt;
   switch (rkStage) {
     case 4:
       B.b1[kc] = lam;
@@ -921,7 +934,11 @@ __global__ void __launch_bounds__(256) kTimeStepFinalize(const double* __restric
     return;
   }
   const int s = *step;
-  dtOut[s - 1] = dt;
+  double* k = dtOut + 4LL * (s - 1);
+  k[0] = dt;
+  k[1] = dt / 6.0;
+  k[2] = dt / 3.0;
+  k[3] = dt / 2.0;
   double t = *time;
   for (int i = 1; i <= 4; ++i) {
     if (i == 2 || i == 4) t = t + dt / 2.0;
@@ -1114,14 +1131,17 @@ void launchAdjointCore(Context& c, DevBlock& b, const RunScalars& rs, int stage,
   const Tile T = b.tAdjA;
   const int G = T.blocks(), W = T.threads();
   cudaStream_t st = on(c, s);
+  const bool curv = b.v.curvilinear != 0, visc = c.phys.viscous != 0;
   MGD_LAUNCH(c);
+#define AC(ND, CU, VI) kAdjointCore<ND, CU, VI><<<G, W, 0, st>>>(b.v, c.phys, rs, stage, fromSlot, T)
   if (c.nD == 2) {
-    if (c.phys.viscous) kAdjointCore<2, true><<<G, W, 0, st>>>(b.v, c.phys, rs, stage, fromSlot, T);
-    else kAdjointCore<2, false><<<G, W, 0, st>>>(b.v, c.phys, rs, stage, fromSlot, T);
+    if (curv) { if (visc) AC(2, true, true); else AC(2, true, false); }
+    else { if (visc) AC(2, false, true); else AC(2, false, false); }
   } else {
-    if (c.phys.viscous) kAdjointCore<3, true><<<G, W, 0, st>>>(b.v, c.phys, rs, stage, fromSlot, T);
-    else kAdjointCore<3, false><<<G, W, 0, st>>>(b.v, c.phys, rs, stage, fromSlot, T);
+    if (curv) { if (visc) AC(3, true, true); else AC(3, true, false); }
+    else { if (visc) AC(3, false, true); else AC(3, false, false); }
   }
+#undef AC
 }
 
 void launchAdjointDiffusion(Context& c, DevBlock& b, cudaStream_t s) {
@@ -1223,6 +1243,17 @@ void launchBatchFunctional(Context& c, const BatchLaunch& L, int stage, cudaStre
 }
 
 void launchStepAdvanceOn(int* counters, int delta, cudaStream_t s) { kStepAdvance<<<1, 32, 0, s>>>(counters, delta); }
+
+__global__ void kSetCounters(int* counters, int step, int segBase) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    counters[0] = step;
+    counters[1] = segBase;
+  }
+}
+
+void launchSetCounters(int* counters, int step, int segBase, cudaStream_t s) {
+  kSetCounters<<<1, 32, 0, s>>>(counters, step, segBase);
+}
 
 int timeStepBlocks(const DevBlock& b) { return gridFor(b.v.N); }
 

@@ -119,7 +119,7 @@ int mgd_forward_rhs_noalloc(mgd_ctx* h, const double* q, double time, double* rh
   rs.step = c.dCounters + 2;
   rs.segBase = c.dCounters + 3;
   rs.amp = scratch;
-  rs.dt = c.opts.time_step_size;
+  setStepSize(rs, c.opts.time_step_size);
   rs.adjointForcingSwitch = c.opts.adjoint_forcing_switch;
   rs.nPartialBlocks = reductionBlocks(b);
   const BlockView saved = b.v;

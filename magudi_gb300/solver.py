@@ -57,6 +57,7 @@ def load_library(build_if_missing=True):
     L.mgd_run_adjoint.argtypes = [ctx, C.POINTER(C.c_double)]
     L.mgd_get_gradient.argtypes = [ctx, C.POINTER(C.c_double), C.c_longlong]
     L.mgd_time_step_size.argtypes = [ctx, C.POINTER(C.c_double)]
+    L.mgd_actuator_weights.argtypes = [ctx, C.POINTER(C.c_double)]
     L.mgd_batch_create.argtypes = [C.POINTER(ctx), C.c_int, C.POINTER(C.c_void_p)]
     L.mgd_batch_run_forward.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double)]
     L.mgd_batch_destroy.argtypes = [C.c_void_p]

@@ -1,0 +1,59 @@
+"""The forward run / discrete adjoint as a torch.autograd.Function (-m gpu):
+the backward pass against central finite differences of J and against the
+oracle's adjoint gradient, with the forcing on the GPU and on the host."""
+import numpy as np
+import pytest
+import torch
+
+import oracle_lib
+from helpers import small_monopole
+from magudi_gb300.autograd import ForwardRun, quadrature_weights
+from magudi_gb300.solver import Solver
+
+pytestmark = pytest.mark.gpu
+
+N_STEPS, S = 16, 4
+
+
+def _problem():
+    return small_monopole(n_steps=N_STEPS, save_interval=S, controller_switch=True)
+
+
+@pytest.mark.parametrize("device", ["cuda", "cpu"])
+def test_backward_matches_finite_differences(device):
+    P = _problem()
+    s = Solver(P)
+    n_act = s.actuator_points()
+    rng = np.random.default_rng(3)
+    f0 = torch.tensor(1e-3 * rng.standard_normal((4 * N_STEPS, n_act)), dtype=torch.float64, device=device,
+                      requires_grad=True)
+    J = ForwardRun.apply(f0, s, N_STEPS, S)
+    J.backward()
+    grad = f0.grad.clone()
+    d = grad / grad.norm()
+    eps = 1e-2 * float(f0.detach().abs().max())
+    with torch.no_grad():
+        Jp = ForwardRun.apply(f0 + eps * d, s, N_STEPS, S)
+        Jm = ForwardRun.apply(f0 - eps * d, s, N_STEPS, S)
+    fd = float((Jp - Jm) / (2 * eps))
+    an = float((grad * d).sum())
+    assert abs(fd - an) <= 1e-6 * abs(an)
+
+
+def test_backward_matches_oracle_gradient():
+    P = _problem()
+    s = Solver(P)
+    n_act = s.actuator_points()
+    rng = np.random.default_rng(8)
+    f = 1e-3 * rng.standard_normal((4 * N_STEPS, n_act))
+    ft = torch.tensor(f, dtype=torch.float64, device="cuda", requires_grad=True)
+    J = ForwardRun.apply(ft, s, N_STEPS, S)
+    J.backward()
+    o = oracle_lib.Oracle(P)
+    o.set_control_forcing(f)
+    Jo = o.run_forward(N_STEPS, S)
+    o.run_adjoint()
+    go = o.gradient(4 * N_STEPS) * quadrature_weights(s, N_STEPS)
+    assert abs(float(J) - Jo) <= 1e-10 * abs(Jo)
+    g = ft.grad.cpu().numpy()
+    assert np.linalg.norm(g - go) <= 1e-10 * np.linalg.norm(go)

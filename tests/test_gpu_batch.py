@@ -42,9 +42,10 @@ def test_batch_matches_single_solves_and_oracle():
     for i, ((n, ny), a) in enumerate(cases):
         P, single = _controlled(n, ny, a * grads[(n, ny)])
         J = single.run_forward(N_STEPS, N_STEPS)
-        # same kernels per point and the same fixed reduction layout: identical results
-        assert costs[i] == J
-        assert np.array_equal(solvers[i].get_field(1, capi.FIELD_CONSERVED), single.get_field(1, capi.FIELD_CONSERVED))
+        # same per-point arithmetic and reduction layout; the batched and single
+        # kernels are compiled separately, so allow FMA-contraction differences
+        assert abs(costs[i] - J) <= 1e-12 * abs(J)
+        assert rel_err(solvers[i].get_field(1, capi.FIELD_CONSERVED), single.get_field(1, capi.FIELD_CONSERVED)) < 1e-13
         o = oracle_lib.Oracle(P)
         o.set_control_forcing(a * grads[(n, ny)])
         Jo = o.run_forward(N_STEPS, keep_stages=False)
@@ -59,7 +60,7 @@ def test_batch_rerun_and_reuse():
     for s in solvers:
         s.set_field(1, capi.FIELD_CONSERVED, s.problem.blocks[0].initial_state)
     c2 = batch.run_forward(N_STEPS)
-    assert np.array_equal(c1, c2)
+    assert np.array_equal(c1, c2)  # deterministic: fixed reduction order, no atomics
 
 
 def test_batch_rejects_mismatched_options():
