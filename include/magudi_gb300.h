@@ -38,7 +38,10 @@ enum {
   MGD_PATCH_SAT_FAR_FIELD = 1,
   MGD_PATCH_SPONGE = 2,
   MGD_PATCH_ACTUATOR = 3,
-  MGD_PATCH_COST_TARGET = 4
+  MGD_PATCH_COST_TARGET = 4,
+  MGD_PATCH_SLIP_WALL = 5,         /* SAT_SLIP_WALL: t_ImpenetrableWall */
+  MGD_PATCH_ISOTHERMAL_WALL = 6,   /* SAT_ISOTHERMAL_WALL */
+  MGD_PATCH_ADIABATIC_WALL = 7     /* SAT_ADIABATIC_WALL */
 };
 
 /* Fields that mgd_set_field / mgd_get_field move between host and device. */
@@ -79,7 +82,19 @@ typedef struct {
   double dissipation_amount;
   double time_step_size;
   double cfl;
+  int functional_type;               /* MGD_FUNCTIONAL_*: which cost functional J is */
 } mgd_options;
+
+/* Cost functionals. SOUND is the reference's acoustic-noise functional
+ * (functional_type = "SOUND", src/AcousticNoiseImpl.f90), integrated in time
+ * over the cost-target patches. TERMINAL_KINETIC_ENERGY (no reference
+ * counterpart) is the kinetic energy sum H det rho |u|^2 / 2 over the whole
+ * grid at the final step; its adjoint starts from lambda(T) = H^-1 dJ/dq(T)
+ * and has no forcing during the run. */
+enum {
+  MGD_FUNCTIONAL_SOUND = 0,
+  MGD_FUNCTIONAL_TERMINAL_KINETIC_ENERGY = 1
+};
 
 /* One block of the region: its size and periodicity (grid00N/dirM/...). */
 typedef struct {
@@ -97,9 +112,13 @@ typedef struct {
   int normal_direction;              /* +-1..3, 0 */
   int extent[6];                     /* iMin iMax jMin jMax kMin kMax as in bc.dat */
   double inviscid_penalty_amount;    /* patches/<name>/inviscid_penalty_amount */
-  double viscous_penalty_amount;     /* patches/<name>/viscous_penalty_amount */
+  double viscous_penalty_amount;     /* patches/<name>/viscous_penalty_amount
+                                        (viscous_penalty_amount1 for isothermal walls) */
   double sponge_amount;              /* patches/<name>/sponge_amount */
   int sponge_exponent;               /* patches/<name>/sponge_exponent */
+  double wall_temperature;           /* isothermal walls: patches/<name>/temperature, or
+                                        <= 0 for the target state's temperature
+                                        (use_target_state, src/PatchFactoryImpl.f90:512-538) */
 } mgd_patch_desc;
 
 /* acoustic_sourceNN/... (src/AcousticSourceImpl.f90:3-32). */

@@ -13,6 +13,9 @@ MGD_NAME_LEN = 64
 FORWARD = 1
 ADJOINT = -1
 
+FUNCTIONAL_SOUND = 0
+FUNCTIONAL_TERMINAL_KINETIC_ENERGY = 1
+
 PERIODIC_NONE = 0
 PERIODIC_PLANE = 1
 PERIODIC_OVERLAP = 2
@@ -21,12 +24,18 @@ PATCH_SAT_FAR_FIELD = 1
 PATCH_SPONGE = 2
 PATCH_ACTUATOR = 3
 PATCH_COST_TARGET = 4
+PATCH_SLIP_WALL = 5
+PATCH_ISOTHERMAL_WALL = 6
+PATCH_ADIABATIC_WALL = 7
 
 PATCH_TYPES = {
     "SAT_FAR_FIELD": PATCH_SAT_FAR_FIELD,
     "SPONGE": PATCH_SPONGE,
     "ACTUATOR": PATCH_ACTUATOR,
     "COST_TARGET": PATCH_COST_TARGET,
+    "SAT_SLIP_WALL": PATCH_SLIP_WALL,
+    "SAT_ISOTHERMAL_WALL": PATCH_ISOTHERMAL_WALL,
+    "SAT_ADIABATIC_WALL": PATCH_ADIABATIC_WALL,
 }
 
 FIELD_CONSERVED = 0
@@ -64,6 +73,7 @@ class Options(C.Structure):
         ("dissipation_amount", C.c_double),
         ("time_step_size", C.c_double),
         ("cfl", C.c_double),
+        ("functional_type", C.c_int),
     ]
 
 
@@ -86,6 +96,7 @@ class PatchDesc(C.Structure):
         ("viscous_penalty_amount", C.c_double),
         ("sponge_amount", C.c_double),
         ("sponge_exponent", C.c_int),
+        ("wall_temperature", C.c_double),
     ]
 
 

@@ -88,6 +88,41 @@ def monopole_2d(n=201, ny=None, dt=0.05, n_steps=960, sponge_points=20, sponge_a
                    n_steps=n_steps, save_interval=save_interval)
 
 
+def wall_channel_2d(n=41, ny=33, wall="SAT_ISOTHERMAL_WALL", wall_temperature=0.0, dt=0.02, n_steps=20,
+                    viscous=True, reynolds=200.0, mach=0.3, sponge_points=6, half_width=6.0):
+    """Channel between two walls: walls of the given bc.dat type on the south
+    (normal +2) and north (normal -2) faces, far-field SATs and sponges on the
+    west and east faces, a uniform stream of Mach `mach` along x as target and
+    initial state. wall_temperature <= 0 takes the target state's temperature
+    (use_target_state)."""
+    gamma = 1.4
+    opts = Options(
+        n_dimensions=2, viscous=viscous, dissipation=True, composite_dissipation=True,
+        curvilinear=False, use_constant_cfl=False, enable_controller=False, enable_functional=False,
+        ratio_of_specific_heats=gamma, reynolds_number=reynolds, prandtl_number=0.72,
+        viscosity_power_law_exponent=0.666, bulk_viscosity_ratio=0.6, dissipation_amount=0.01,
+        time_step_size=dt)
+    coords, x, y = uniform_grid_2d(n, ny, -half_width, half_width)
+    N = n * ny
+    target = quiescent_state(N, 2, gamma)
+    target[1] = mach * target[0]
+    target[3] = target[3] + 0.5 * mach ** 2
+    block = Block(grid_size=(n, ny, 1), coordinates=np.ascontiguousarray(coords),
+                  initial_state=target.copy(), target_state=target.copy(),
+                  control_mollifier=np.ones(N), target_mollifier=np.ones(N),
+                  mean_pressure=np.full(N, 1.0 / gamma))
+    s = sponge_points
+    patches = [
+        Patch("farField.W", "SAT_FAR_FIELD", 1, 1, (1, 1, 1, -1, 1, -1)),
+        Patch("farField.E", "SAT_FAR_FIELD", 1, -1, (-1, -1, 1, -1, 1, -1)),
+        Patch("wall.S", wall, 1, 2, (1, -1, 1, 1, 1, -1), wall_temperature=wall_temperature),
+        Patch("wall.N", wall, 1, -2, (1, -1, -1, -1, 1, -1), wall_temperature=wall_temperature),
+        Patch("sponge.W", "SPONGE", 1, 1, (1, s, 1, -1, 1, -1), sponge_amount=0.2),
+        Patch("sponge.E", "SPONGE", 1, -1, (-s, -1, 1, -1, 1, -1), sponge_amount=0.2),
+    ]
+    return Problem(options=opts, blocks=[block], patches=patches, sources=[], n_steps=n_steps, save_interval=5)
+
+
 def random_state(n_points, n_dimensions, gamma, rng):
     """full_rhs.f90:289-301: rho in U[0.01,10], u in U[-10,10], p in U[0.01,10]/gamma."""
     nU = n_dimensions + 2
@@ -119,10 +154,13 @@ def smooth_perturbed_state(block, n_dimensions, gamma, rng, amplitude=1e-2):
 
 
 def taylor_green_3d(n=256, mach=0.1, reynolds=1600.0, cfl=0.5, n_steps=2000,
-                    dissipation_amount=0.01, power_law=0.666, bulk_viscosity_ratio=0.6):
+                    dissipation_amount=0.01, power_law=0.666, bulk_viscosity_ratio=0.6, dt=None,
+                    save_interval=None):
     """Taylor-Green vortex, PLANE periodicity on [0, 2 pi)^3:
     rho = 1, u = sin x cos y cos z, v = -cos x sin y cos z, w = 0,
-    p = 1/(gamma M^2) + (cos 2x + cos 2y)(cos 2z + 2)/16."""
+    p = 1/(gamma M^2) + (cos 2x + cos 2y)(cos 2z + 2)/16.
+    The cost functional is the kinetic energy at the final step. Constant CFL
+    unless dt is given; the checkpoint interval defaults to about sqrt(n_steps)."""
     gamma = 1.4
     L = 2.0 * np.pi
     x = np.arange(n) * (L / n)
@@ -140,11 +178,13 @@ def taylor_green_3d(n=256, mach=0.1, reynolds=1600.0, cfl=0.5, n_steps=2000,
     q[4] = p / (gamma - 1.0) + 0.5 * (u ** 2 + v ** 2 + w ** 2)
     opts = Options(
         n_dimensions=3, viscous=True, dissipation=True, composite_dissipation=True,
-        curvilinear=False, use_constant_cfl=True, cfl=cfl, enable_controller=False,
-        enable_functional=False, ratio_of_specific_heats=gamma, reynolds_number=reynolds,
+        curvilinear=False, use_constant_cfl=dt is None, cfl=cfl, enable_controller=False,
+        enable_functional=True, ratio_of_specific_heats=gamma, reynolds_number=reynolds,
         prandtl_number=0.72, viscosity_power_law_exponent=power_law,
-        bulk_viscosity_ratio=bulk_viscosity_ratio, dissipation_amount=dissipation_amount)
+        bulk_viscosity_ratio=bulk_viscosity_ratio, dissipation_amount=dissipation_amount,
+        time_step_size=dt or 0.0, functional_type=1)
     block = Block(grid_size=(n, n, n), coordinates=np.ascontiguousarray(coords),
                   periodicity_type=(1, 1, 1), periodic_length=(L, L, L),
                   initial_state=q, target_state=q.copy(), mean_pressure=np.full(N, 1.0 / gamma))
-    return Problem(options=opts, blocks=[block], patches=[], sources=[], n_steps=n_steps)
+    S = save_interval or max(1, int(round(n_steps ** 0.5)))
+    return Problem(options=opts, blocks=[block], patches=[], sources=[], n_steps=n_steps, save_interval=S)

@@ -157,7 +157,7 @@ int mgd_destroy(mgd_ctx* h) {
   cudaFree(c.dCounters); cudaFree(c.dApiAmp); cudaFree(c.dAmp); cudaFree(c.dForcing);
   cudaFree(c.dGradient); cudaFree(c.dPartials); cudaFree(c.dStageValues);
   cudaFree(c.dSnapshots); cudaFree(c.dStageBuf);
-  cudaFree(c.dStepDt); cudaFree(c.dDtPartials); cudaFree(c.dTime);
+  cudaFree(c.dStepDt); cudaFree(c.dDtPartials); cudaFree(c.dTime); cudaFree(c.dNorm);
   if (c.gForward) cudaGraphExecDestroy(c.gForward);
   for (int k = 0; k < 2; ++k) {
     if (c.gRecomputeH[k]) cudaGraphExecDestroy(c.gRecomputeH[k]);
@@ -417,7 +417,7 @@ int mgd_add_block(mgd_ctx* h, const mgd_block_desc* desc, const double* coordina
 int mgd_add_patch(mgd_ctx* h, const mgd_patch_desc* p) {
   Context& c = h->c;
   if (c.finalized) return fail(c, "mgd_add_patch after mgd_finalize_setup");
-  if (p->type < MGD_PATCH_SAT_FAR_FIELD || p->type > MGD_PATCH_COST_TARGET)
+  if (p->type < MGD_PATCH_SAT_FAR_FIELD || p->type > MGD_PATCH_ADIABATIC_WALL)
     return fail(c, std::string("unsupported patch type for patch '") + p->name + "'");
   if (p->grid_index < 1) return fail(c, "patch grid index must be >= 1");
   c.patches.push_back(*p);
@@ -642,10 +642,12 @@ int mgd_finalize_setup(mgd_ctx* h) {
     for (int i = 0; i < nD; ++i)
       if (e[2 * i] < 1 || e[2 * i + 1] > gs[i] || e[2 * i] > e[2 * i + 1])
         return fail(c, std::string("patch '") + p.name + "' has an invalid extent");
-    if (p.type == MGD_PATCH_SAT_FAR_FIELD || p.type == MGD_PATCH_SPONGE) {
+    const bool satType = p.type == MGD_PATCH_SAT_FAR_FIELD || p.type == MGD_PATCH_SLIP_WALL ||
+                         p.type == MGD_PATCH_ISOTHERMAL_WALL || p.type == MGD_PATCH_ADIABATIC_WALL;
+    if (satType || p.type == MGD_PATCH_SPONGE) {
       const int d = std::abs(p.normal_direction);
       if (d < 1 || d > nD) return fail(c, std::string("patch '") + p.name + "' has an invalid normal direction");
-      if (p.type == MGD_PATCH_SAT_FAR_FIELD && e[2 * (d - 1)] != e[2 * (d - 1) + 1])
+      if (satType && e[2 * (d - 1)] != e[2 * (d - 1) + 1])
         return fail(c, std::string("patch '") + p.name + "' extends more than 1 grid point along its normal direction");
     }
     exts.insert(exts.end(), e, e + 6);
@@ -691,8 +693,9 @@ int mgd_finalize_setup(mgd_ctx* h) {
   // masks, actuator indices, cost-target counts, far-field entries
   std::vector<double> maskT(N, 0.0), maskA(N, 0.0), tgt(N, 0.0);
   std::vector<int> actIdx(N, -1), ffOf(3 * N, -1);
-  std::vector<int> ffPoint, ffDir, ffSigned;
-  std::vector<double> ffSigInv, ffSigV, ffSigVRaw;
+  std::vector<int> ffPoint, ffDir, ffSigned, ffKind;
+  std::vector<double> ffSigInv, ffSigV, ffSigVRaw, ffWallInv, ffWallVisc, ffWallT;
+  std::vector<double> qtH;  // target state on the host (isothermal wall temperatures)
   const HostOp d1 = makeFirstDerivative48();
   long long actOffset = 0;
   for (size_t pi = 0; pi < c.patches.size(); ++pi) {
@@ -735,8 +738,59 @@ int mgd_finalize_setup(mgd_ctx* h) {
           ffSigInv.push_back(sInv);
           ffSigVRaw.push_back(sVis);
           ffSigV.push_back(sVis);  // times 1/det below
+          ffKind.push_back(SAT_FAR_FIELD);
+          ffWallInv.push_back(0.0);
+          ffWallVisc.push_back(0.0);
+          ffWallT.push_back(0.0);
         });
-        if (full) return fail(c, "more than three far-field patches meet at one point");
+        if (full) return fail(c, "more than three SAT patches meet at one point");
+        break;
+      }
+      case MGD_PATCH_SLIP_WALL:
+      case MGD_PATCH_ISOTHERMAL_WALL:
+      case MGD_PATCH_ADIABATIC_WALL: {
+        // src/ImpenetrableWallImpl.f90:3-40, src/IsothermalWallImpl.f90:3-80
+        const int dir = std::abs(p.normal_direction);
+        const double nb = d1.norm[0];
+        const double sInv = std::copysign(p.inviscid_penalty_amount, (double)p.normal_direction) / nb;
+        const bool iso = p.type == MGD_PATCH_ISOTHERMAL_WALL;
+        const double sVis = (iso && c.opts.viscous) ? p.viscous_penalty_amount / nb * c.phys.reInv : 0.0;
+        if (iso && p.wall_temperature <= 0.0 && qtH.empty()) {
+          qtH.resize((size_t)N * nU);
+          CUDA_TRY(c, cudaMemcpy(qtH.data(), b.v.qt, qtH.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        }
+        bool full = false;
+        forExtent(e, gs, [&](long long gi, long long) {
+          if (b.hostIblank[gi] == 0) return;
+          int slot = 0;
+          while (slot < 3 && ffOf[3 * gi + slot] >= 0) ++slot;
+          if (slot == 3) { full = true; return; }
+          ffOf[3 * gi + slot] = (int)ffPoint.size();
+          ffPoint.push_back((int)gi);
+          ffDir.push_back(dir);
+          ffSigned.push_back(p.normal_direction);
+          ffSigInv.push_back(0.0);
+          ffSigVRaw.push_back(0.0);
+          ffSigV.push_back(0.0);
+          ffKind.push_back(iso ? SAT_ISOTHERMAL_WALL : SAT_WALL);
+          ffWallInv.push_back(sInv);   // times 1/det below
+          ffWallVisc.push_back(sVis);  // times 1/det below
+          double Tw = p.wall_temperature;
+          if (iso && Tw <= 0.0) {
+            // temperature of the target state (src/PatchFactoryImpl.f90:512-538)
+            const double g = c.phys.g;
+            const double v = 1.0 / qtH[gi];
+            double u2 = 0.0;
+            for (int d = 0; d < nD; ++d) {
+              const double u = v * qtH[(size_t)N * (d + 1) + gi];
+              u2 += u * u;
+            }
+            const double pr = (g - 1.0) * (qtH[(size_t)N * (nD + 1) + gi] - 0.5 * qtH[gi] * u2);
+            Tw = g * pr / (g - 1.0) * v;
+          }
+          ffWallT.push_back(Tw);
+        });
+        if (full) return fail(c, "more than three SAT patches meet at one point");
         break;
       }
       default:
@@ -828,6 +882,10 @@ int mgd_finalize_setup(mgd_ctx* h) {
     chk(devAlloc(b, &ff.sigVRaw, nFF));
     chk(devAlloc(b, &ff.visc, (size_t)nFF * nU));
     chk(devAlloc(b, &ff.viscT, (size_t)nFF * nU));
+    chk(devAlloc(b, &ff.kind, nFF));
+    chk(devAlloc(b, &ff.wallInv, nFF));
+    chk(devAlloc(b, &ff.wallVisc, nFF));
+    chk(devAlloc(b, &ff.wallT, nFF));
     double* dSig = nullptr;
     int* dSigned = nullptr;
     chk(devAlloc(b, &dSig, nFF));
@@ -835,7 +893,15 @@ int mgd_finalize_setup(mgd_ctx* h) {
     if (e != cudaSuccess) return fail(c, "device allocation failed for far-field entries");
     std::vector<double> jacH(N);
     CUDA_TRY(c, cudaMemcpy(jacH.data(), v.jac, N * sizeof(double), cudaMemcpyDeviceToHost));
-    for (int k = 0; k < nFF; ++k) ffSigV[k] = ffSigV[k] * jacH[ffPoint[k]];
+    for (int k = 0; k < nFF; ++k) {
+      ffSigV[k] = ffSigV[k] * jacH[ffPoint[k]];
+      ffWallInv[k] = ffWallInv[k] * jacH[ffPoint[k]];
+      ffWallVisc[k] = ffWallVisc[k] * jacH[ffPoint[k]];
+    }
+    CUDA_TRY(c, cudaMemcpy(ff.kind, ffKind.data(), nFF * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(ff.wallInv, ffWallInv.data(), nFF * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(ff.wallVisc, ffWallVisc.data(), nFF * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(ff.wallT, ffWallT.data(), nFF * sizeof(double), cudaMemcpyHostToDevice));
     CUDA_TRY(c, cudaMemcpy(ff.point, ffPoint.data(), nFF * sizeof(int), cudaMemcpyHostToDevice));
     CUDA_TRY(c, cudaMemcpy(ff.normalDir, ffDir.data(), nFF * sizeof(int), cudaMemcpyHostToDevice));
     CUDA_TRY(c, cudaMemcpy(ff.sigV, ffSigV.data(), nFF * sizeof(double), cudaMemcpyHostToDevice));
@@ -1332,7 +1398,17 @@ int finishForwardRun(Context& c, double* cost) {
   }
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   double J = 0.0;
-  if (c.opts.enable_functional) {
+  if (c.opts.enable_functional && c.opts.functional_type == MGD_FUNCTIONAL_TERMINAL_KINETIC_ENERGY) {
+    DevBlock& b = c.blocks[0];
+    if (!c.dNorm) {
+      CUDA_TRY(c, cudaMalloc((void**)&c.dNorm, (size_t)b.v.N * sizeof(double)));
+      CUDA_TRY(c, cudaMemcpy(c.dNorm, b.hostNorm.data(), (size_t)b.v.N * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    launchKineticEnergy(c, b, c.dNorm, c.dDtPartials, c.dTime);
+    if (checkLaunch(c)) return 1;
+    CUDA_TRY(c, cudaMemcpyAsync(&J, c.dTime, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  } else if (c.opts.enable_functional) {
     std::vector<double> vals;
     if (reduceToHost(c, 4 * n_steps, vals)) return 1;
     for (int s = 0; s < n_steps; ++s)
@@ -1355,7 +1431,7 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
   if (prepareForwardRun(c, n_steps, save_interval, t0, true)) return 1;
   const bool cflMode = c.opts.use_constant_cfl != 0;
   const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
-  const bool functional = c.opts.enable_functional != 0;
+  const bool functional = c.opts.enable_functional != 0 && c.opts.functional_type == MGD_FUNCTIONAL_SOUND;
   RunScalars rs = runScalars(c);
   if (setCounters(c, 1, 0)) return 1;
   if (capture(c, &c.gForward, &c.nodesForward, [&]() {
@@ -1397,11 +1473,14 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
                                   : Lanes{c.stream, c.side, c.evFork[0], c.evJoin[0]};
   int* recCounters = twoLanes ? c.dCounters + 4 : c.dCounters;
   // adjoint initial condition at the final state (its primitives are current)
+  const bool terminal = c.opts.functional_type == MGD_FUNCTIONAL_TERMINAL_KINETIC_ENERGY;
   launchPrims(c, b, b.v.q, false);
-  launchAdjointInitial(c, b, c.opts.adjoint_forcing_switch ? -dtT / 6.0 : 0.0);
+  if (terminal) launchKineticEnergyAdjointInitial(c, b);
+  else launchAdjointInitial(c, b, c.opts.adjoint_forcing_switch ? -dtT / 6.0 : 0.0);
   long long nodesRec = 0, nodesAdj = 0;
   for (int half = 0; half < c.stageHalves; ++half) {
     RunScalars ra = runScalars(c);
+    if (terminal) ra.adjointForcingSwitch = 0;  // no forcing during the run
     ra.stageBuf = c.dStageBuf + half * c.stageHalf;
     RunScalars rr = ra;
     rr.step = recCounters;

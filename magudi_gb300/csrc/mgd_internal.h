@@ -26,11 +26,16 @@ struct PrimLayout {
   __host__ __device__ int count() const { return 6 + nD; }
 };
 
-// Far-field SAT entry: one (patch, point) pair.
+// Boundary SAT entry: one (far-field or wall patch, point) pair.
+enum { SAT_FAR_FIELD = 0, SAT_WALL = 1, SAT_ISOTHERMAL_WALL = 2 };
 struct FarFieldEntries {
   int n = 0;
   int* point = nullptr;      // grid point
   int* normalDir = nullptr;  // 1-based normal direction (unsigned)
+  int* kind = nullptr;       // SAT_FAR_FIELD, SAT_WALL (slip or adiabatic), SAT_ISOTHERMAL_WALL
+  double* wallInv = nullptr;   // walls: signed inviscid penalty / H0 * jacobian
+  double* wallVisc = nullptr;  // isothermal walls: viscous penalty / H0 / Re * jacobian (0 if inviscid)
+  double* wallT = nullptr;     // isothermal walls: wall temperature
   double* M = nullptr;       // nU*nU: inviscidPenaltyAmount * jacobian * A+(target), column-major
   double* sigV = nullptr;    // viscousPenaltyAmount * jacobian
   double* sigVRaw = nullptr; // viscousPenaltyAmount
@@ -218,6 +223,7 @@ struct Context {
   double* dDtPartials = nullptr;
   long long dtPartialCapacity = 0;
   double* dTime = nullptr;
+  double* dNorm = nullptr;          // H det per point (terminal functional)
   cudaGraphExec_t gForward = nullptr, gRecomputeH[2] = {}, gAdjointH[2] = {};
   long long nodesForward = 0, nodesRecompute = 0, nodesAdjoint = 0;
 };
@@ -295,6 +301,9 @@ void launchReducePartials(Context& c, const double* partials, int stride, int co
 void launchTimeStep(Context& c, DevBlock& b, double* partials, double* dtOut, const int* step, double* time,
                     double* amp, cudaStream_t s = 0);
 int timeStepBlocks(const DevBlock& b);
+// Terminal kinetic energy of the current state into out[0] (norm = H det per point).
+void launchKineticEnergy(Context& c, DevBlock& b, const double* norm, double* partials, double* out);
+void launchKineticEnergyAdjointInitial(Context& c, DevBlock& b);
 void launchCoordinateDerivative(Context& c, DevBlock& b, int dir, double* out);
 void launchApplyD1(Context& c, DevBlock& b, int dir, const double* in, double* out, int ncomp);
 void launchFarFieldMatricesWith(Context& c, DevBlock& b, const double* sigInv, const int* signedNormal);

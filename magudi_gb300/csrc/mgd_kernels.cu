@@ -195,6 +195,67 @@ __device__ __forceinline__ FwdState forwardState(const BlockView& B, const RunSc
 }
 
 // ---------------------------------------------------------------------------
+// Wall SAT vectors of one entry (addImpenetrableWallPenalty,
+// src/ImpenetrableWallImpl.f90:58-213, and the viscous penalty of
+// addIsothermalWallPenalty, src/IsothermalWallImpl.f90:92-260; the adiabatic
+// wall adds the impenetrable penalty only, src/AdiabaticWallImpl.f90:80-160).
+// Forward: sat = -s_inv J [m.rho u, (m.rho u) u, (m.rho u) v (E + p)]
+//                - s_visc J [0, rho u, E - rho T_w / gamma].
+// Adjoint: sat = s_inv J (A(m) - m (dp/dq))^T lambda
+//                + s_visc J [-lambda_E T_w / gamma, lambda_1 .. lambda_E].
+// ---------------------------------------------------------------------------
+template <int ND, bool VISC>
+__device__ __forceinline__ void wallSatForward(const BlockView& B, const Physics& P, int e, long long p,
+                                               const double* q, const double* u, double* sat) {
+  constexpr int nU = ND + 2, E = ND + 1;
+  const long long N = B.N;
+  const PrimLayout L{ND};
+  double mn[ND];
+  for (int d = 0; d < ND; ++d) mn[d] = B.metrics[p + N * (ND * (B.ff.normalDir[e] - 1) + d)];
+  double nm = q[1] * mn[0];
+  for (int d = 1; d < ND; ++d) nm += q[1 + d] * mn[d];
+  const double s = B.ff.wallInv[e];
+  sat[0] = -(s * nm);
+  for (int d = 0; d < ND; ++d) sat[1 + d] = -(s * (nm * u[d]));
+  sat[E] = -(s * (nm * B.prim[p + N * L.v()] * (q[E] + B.prim[p + N * L.p()])));
+  if (VISC && B.ff.kind[e] == SAT_ISOTHERMAL_WALL) {
+    const double sv = B.ff.wallVisc[e];
+    for (int c = 1; c < E; ++c) sat[c] -= sv * q[c];
+    sat[E] -= sv * (q[E] - q[0] * B.ff.wallT[e] / P.g);
+  }
+  (void)nU;
+}
+
+template <int ND, bool VISC>
+__device__ __forceinline__ void wallSatAdjoint(const BlockView& B, const Physics& P, int e, long long p,
+                                               const double* u, double T, double v, const double* lam,
+                                               double* sat) {
+  constexpr int nU = ND + 2, E = ND + 1;
+  const long long N = B.N;
+  double mn[ND];
+  for (int d = 0; d < ND; ++d) mn[d] = B.metrics[p + N * (ND * (B.ff.normalDir[e] - 1) + d)];
+  double y[nU];
+  for (int c = 0; c < nU; ++c) y[c] = 0.0;
+  addFluxJacobianTransposeProduct<ND, false>(mn, u, T, v, P.g, 0.0, nullptr, nullptr, lam, y);
+  // minus sum_l m_l (dp/dq) lambda_{1+l}, dp/dq = (gamma - 1) (|u|^2 / 2, -u, 1)
+  double ml = mn[0] * lam[1];
+  for (int l = 1; l < ND; ++l) ml += mn[l] * lam[1 + l];
+  double u2 = u[0] * u[0];
+  for (int d = 1; d < ND; ++d) u2 += u[d] * u[d];
+  const double gm1 = P.g - 1.0;
+  y[0] -= (0.5 * u2 * gm1) * ml;
+  for (int d = 0; d < ND; ++d) y[1 + d] -= (-u[d] * gm1) * ml;
+  y[E] -= gm1 * ml;
+  const double s = B.ff.wallInv[e];
+  for (int c = 0; c < nU; ++c) sat[c] = s * y[c];
+  if (VISC && B.ff.kind[e] == SAT_ISOTHERMAL_WALL) {
+    const double sv = B.ff.wallVisc[e];
+    sat[0] += sv * (-lam[E] * B.ff.wallT[e] / P.g);
+    for (int c = 1; c < nU; ++c) sat[c] += sv * lam[c];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Velocity and temperature gradients, stress and heat flux (State%update,
 // src/StateImpl.f90:494-533 with Grid%computeGradient, src/GridImpl.f90:1172-1421),
 // Cartesian inviscid and viscous fluxes transformed to contravariant form
@@ -301,6 +362,10 @@ __device__ __forceinline__ void gradFluxPoint(const BlockView& B, const Physics&
     for (int s = 0; s < 3; ++s) {
       const int e = B.ffOfPoint[3 * p + s];
       if (e < 0) continue;
+      if (B.ff.kind[e] != SAT_FAR_FIELD) {
+        wallSatForward<ND, VISC>(B, P, e, p, q, u, B.ff.visc + (long long)e * nU);
+        continue;
+      }
       // sat = -sigma_inv J A+ (q - q_target) + sigma_visc J (F_v - F_v,target) . m
       const double* M = B.ff.M + (long long)e * nU * nU;
       double dqv[nU];
@@ -567,7 +632,7 @@ __device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physi
     }
     for (int k = 0; k < 3; ++k) {
       const int e = B.ffOfPoint[3 * p + k];
-      if (e < 0) continue;
+      if (e < 0 || B.ff.kind[e] != SAT_FAR_FIELD) continue;
       double mn[ND];  // metric row of the normal direction, read from memory (no dynamic register index)
       for (int d = 0; d < ND; ++d) mn[d] = B.metrics[p + N * (ND * (B.ff.normalDir[e] - 1) + d)];
       const double sv = B.ff.sigVRaw[e];
@@ -584,6 +649,10 @@ __device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physi
   for (int k = 0; k < 3; ++k) {
     const int e = B.ffOfPoint[3 * p + k];
     if (e < 0) continue;
+    if (B.ff.kind[e] != SAT_FAR_FIELD) {
+      wallSatAdjoint<ND, VISC>(B, P, e, p, u, Tm, v, lp, B.ff.visc + (long long)e * nU);
+      continue;
+    }
     const double* M = B.ff.M + (long long)e * nU * nU;
     double z[nU];
     for (int c = 0; c < nU; ++c) z[c] = 0.0;
@@ -784,6 +853,46 @@ __global__ void __launch_bounds__(kBlock) kStoreAdjointForcing(BlockView B, Phys
     }
   }
   for (int c = 0; c < nU; ++c) B.adjF[p + N * c] = r[c];
+}
+
+// Terminal kinetic energy: block partial sums of H det rho |u|^2 / 2 over the
+// non-hole points (norm = H det), for a fixed-order final reduction.
+template <int ND>
+__global__ void __launch_bounds__(kBlock) kKineticEnergyPartials(BlockView B, const double* __restrict__ norm,
+                                                                 double* __restrict__ partial) {
+  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
+  double v = 0.0;
+  if (p < B.N && B.iblank[p] != 0) {
+    double m2 = 0.0;
+    for (int d = 0; d < ND; ++d) {
+      const double m = B.q[p + B.N * (d + 1)];
+      m2 += m * m;
+    }
+    v = norm[p] * (0.5 * m2 / B.q[p]);
+  }
+  const double s = blockSum(v);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// lambda(T) = H^-1 dJ/dq(T) of the terminal kinetic energy: (-|u|^2/2, u, 0).
+template <int ND>
+__global__ void __launch_bounds__(kBlock) kKineticEnergyAdjointInitial(BlockView B) {
+  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
+  if (p >= B.N) return;
+  constexpr int nU = ND + 2;
+  const long long N = B.N;
+  double l[nU];
+  for (int c = 0; c < nU; ++c) l[c] = 0.0;
+  if (B.iblank[p] != 0) {
+    double u2 = 0.0;
+    for (int d = 0; d < ND; ++d) {
+      const double u = B.q[p + N * (d + 1)] / B.q[p];
+      l[1 + d] = u;
+      u2 += u * u;
+    }
+    l[0] = -0.5 * u2;
+  }
+  for (int c = 0; c < nU; ++c) B.lam[p + N * c] = l[c];
 }
 
 // Snapshot of the conserved variables after a completed forward step.
@@ -1257,6 +1366,20 @@ void launchSetCounters(int* counters, int step, int segBase, cudaStream_t s) {
 
 int timeStepBlocks(const DevBlock& b) { return gridFor(b.v.N); }
 
+void launchKineticEnergy(Context& c, DevBlock& b, const double* norm, double* partials, double* out) {
+  const int nb = gridFor(b.v.N);
+  MGD_LAUNCH(c);
+  if (c.nD == 2) kKineticEnergyPartials<2><<<nb, kBlock, 0, c.stream>>>(b.v, norm, partials);
+  else kKineticEnergyPartials<3><<<nb, kBlock, 0, c.stream>>>(b.v, norm, partials);
+  launchReducePartials(c, partials, nb, nb, 1, out);
+}
+
+void launchKineticEnergyAdjointInitial(Context& c, DevBlock& b) {
+  MGD_LAUNCH(c);
+  if (c.nD == 2) kKineticEnergyAdjointInitial<2><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v);
+  else kKineticEnergyAdjointInitial<3><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v);
+}
+
 void launchTimeStep(Context& c, DevBlock& b, double* partials, double* dtOut, const int* step, double* time,
                     double* amp, cudaStream_t s) {
   const int nb = timeStepBlocks(b);
@@ -1297,6 +1420,7 @@ void launchFarFieldTargetVisc(Context& c, DevBlock& b) {
 }
 
 // Far-field matrices from per-entry inviscid penalty and signed normal direction.
+// (Wall entries get matrices too; their SAT kernels do not read them.)
 void launchFarFieldMatricesWith(Context& c, DevBlock& b, const double* sigInv, const int* signedNormal) {
   if (b.v.ff.n == 0) return;
   MGD_LAUNCH(c);

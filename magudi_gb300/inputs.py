@@ -159,6 +159,14 @@ def patches_from_bc(d, rows):
                                                d.get_float("defaults/viscous_penalty_amount", 1.0))
         p.sponge_amount = d.get_float(key + "sponge_amount", d.get_float("defaults/sponge_amount", 1.0))
         p.sponge_exponent = d.get_int(key + "sponge_exponent", d.get_int("defaults/sponge_exponent", 2))
+        if ptype == "SAT_ISOTHERMAL_WALL":
+            # src/IsothermalWallImpl.f90:3-80: viscous_penalty_amount1, and the wall
+            # temperature from the target state unless use_target_state is off
+            p.viscous_penalty_amount = d.get_float(key + "viscous_penalty_amount1",
+                                                   d.get_float("defaults/viscous_penalty_amount", 1.0))
+            if not d.get_bool("use_target_state", True):
+                gamma = d.get_float("ratio_of_specific_heats", 1.4)
+                p.wall_temperature = d.get_float(key + "temperature", 1.0 / (gamma - 1.0))
         patches.append(p)
     return patches
 

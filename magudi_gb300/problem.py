@@ -40,6 +40,7 @@ class Options:
     dissipation_amount: float = 0.0
     time_step_size: float = 0.0
     cfl: float = 0.5
+    functional_type: int = 0  # capi.FUNCTIONAL_SOUND or FUNCTIONAL_TERMINAL_KINETIC_ENERGY
 
     def to_c(self) -> capi.Options:
         o = capi.Options()
@@ -62,6 +63,7 @@ class Patch:
     viscous_penalty_amount: float = 1.0
     sponge_amount: float = 1.0
     sponge_exponent: int = 2
+    wall_temperature: float = 0.0  # isothermal walls: <= 0 takes the target state's temperature
 
     def to_c(self) -> capi.PatchDesc:
         p = capi.PatchDesc()
@@ -75,6 +77,7 @@ class Patch:
         p.viscous_penalty_amount = self.viscous_penalty_amount
         p.sponge_amount = self.sponge_amount
         p.sponge_exponent = int(self.sponge_exponent)
+        p.wall_temperature = float(self.wall_temperature)
         return p
 
     def resolved_extent(self, grid_size):

@@ -573,7 +573,12 @@ struct Patch {
   std::vector<double> targetViscousFluxes;  // (nPatchPoints, nU, nD)
   std::vector<double> adjointForcing;       // (nPatchPoints, nU)
   std::vector<double> controlForcing;       // (nPatchPoints, nU)
+  std::vector<double> wallTemperature;      // (nPatchPoints), isothermal walls
 };
+
+static bool isWall(int type) {
+  return type == MGD_PATCH_SLIP_WALL || type == MGD_PATCH_ISOTHERMAL_WALL || type == MGD_PATCH_ADIABATIC_WALL;
+}
 
 struct Block {
   mgd_block_desc d;
@@ -930,6 +935,32 @@ static int setupPatches(Region& R) {
         p.targetViscousFluxes.assign(p.nPatchPoints * R.nU * R.nD, 0.0);
       }
     }
+    if (isWall(p.d.type)) {
+      // setupImpenetrableWall, src/ImpenetrableWallImpl.f90:3-40
+      const double nb = b.firstDerivative[dir - 1].normBoundary[0];
+      p.inviscidPenaltyAmount = std::copysign(p.d.inviscid_penalty_amount, (double)p.d.normal_direction) / nb;
+      p.viscousPenaltyAmount = 0.0;
+      if (p.d.type == MGD_PATCH_ISOTHERMAL_WALL && R.o.viscous) {
+        // setupIsothermalWall, src/IsothermalWallImpl.f90:3-80: viscousPenaltyAmounts(1)
+        // = amount / H0 * Re^-1 without the sign of the normal direction
+        p.viscousPenaltyAmount = p.d.viscous_penalty_amount / nb * R.reInv;
+        p.wallTemperature.assign(p.nPatchPoints, p.d.wall_temperature);
+        if (p.d.wall_temperature <= 0.0) {
+          // temperature of the target state (src/PatchFactoryImpl.f90:512-538)
+          const double g = R.o.ratio_of_specific_heats;
+          forPatchPoints(p, b, [&](long long gi, long long pi) {
+            const double v = 1.0 / b.targetState[gi];
+            double u2 = 0.0;
+            for (int d = 0; d < R.nD; ++d) {
+              const double u = v * b.targetState[b.N * (d + 1) + gi];
+              u2 += u * u;
+            }
+            const double pr = (g - 1.0) * (b.targetState[b.N * (R.nD + 1) + gi] - 0.5 * b.targetState[gi] * u2);
+            p.wallTemperature[pi] = g * pr / (g - 1.0) * v;
+          });
+        }
+      }
+    }
     if (p.d.type == MGD_PATCH_COST_TARGET) p.adjointForcing.assign(p.nPatchPoints * R.nU, 0.0);
     if (p.d.type == MGD_PATCH_ACTUATOR) p.controlForcing.assign(p.nPatchPoints * R.nU, 0.0);
     if (p.d.type == MGD_PATCH_SPONGE) p.spongeStrength.assign(p.nPatchPoints, 0.0);
@@ -1279,6 +1310,67 @@ static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjoi
       });
       break;
     }
+    case MGD_PATCH_SLIP_WALL:
+    case MGD_PATCH_ISOTHERMAL_WALL:
+    case MGD_PATCH_ADIABATIC_WALL: {
+      // addImpenetrableWallPenalty, src/ImpenetrableWallImpl.f90:58-213, then for
+      // isothermal walls the viscous penalty of addIsothermalWallPenalty,
+      // src/IsothermalWallImpl.f90:92-260 (the adiabatic wall's viscous
+      // penalties are identically zero, src/AdiabaticWallImpl.f90:80-160).
+      const int dir = std::abs(p.d.normal_direction);
+      forPatchPoints(p, b, [&](long long gi, long long pi) {
+        if (b.iblank[gi] == 0) return;
+        double cv[5], m[3], u[3], pen[5], A[25];
+        for (int c = 0; c < nU; ++c) cv[c] = b.conservedVariables[N * c + gi];
+        for (int d = 0; d < nD; ++d) m[d] = b.metrics[N * (nD * (dir - 1) + d) + gi];
+        for (int d = 0; d < nD; ++d) u[d] = b.velocity[N * d + gi];
+        const double jac = b.jacobian[gi];
+        double normalMomentum = 0.0;
+        for (int d = 0; d < nD; ++d) normalMomentum += cv[1 + d] * m[d];
+        if (mode == MGD_FORWARD) {
+          pen[0] = normalMomentum;
+          for (int d = 0; d < nD; ++d) pen[1 + d] = normalMomentum * u[d];
+          pen[nD + 1] = normalMomentum * b.specificVolume[gi] * (cv[nD + 1] + b.pressure[gi]);
+          for (int r = 0; r < nU; ++r)
+            b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] - p.inviscidPenaltyAmount * jac * pen[r];
+        } else {
+          double dp[5];
+          double u2 = 0.0;
+          for (int d = 0; d < nD; ++d) u2 += u[d] * u[d];
+          dp[0] = 0.5 * u2;
+          for (int d = 0; d < nD; ++d) dp[1 + d] = -u[d];
+          dp[nD + 1] = 1.0;
+          for (int c = 0; c < nU; ++c) dp[c] = dp[c] * (g - 1.0);
+          inviscidJacobian(nD, cv, m, g, A, b.specificVolume[gi], u, b.temperature[gi]);
+          for (int l = 0; l < nD; ++l)
+            for (int c = 0; c < nU; ++c) A[(l + 1) + nU * c] = A[(l + 1) + nU * c] - m[l] * dp[c];
+          for (int r = 0; r < nU; ++r) {
+            double s = A[0 + nU * r] * b.adjointVariables[gi];
+            for (int c = 1; c < nU; ++c) s += A[c + nU * r] * b.adjointVariables[N * c + gi];
+            b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] + p.inviscidPenaltyAmount * jac * s;
+          }
+        }
+        if (p.d.type != MGD_PATCH_ISOTHERMAL_WALL || !R.o.viscous) return;
+        const double Tw = p.wallTemperature[pi];
+        if (mode == MGD_FORWARD) {
+          pen[0] = 0.0;
+          for (int c = 1; c < nU; ++c) pen[c] = cv[c];
+          pen[nD + 1] = pen[nD + 1] - cv[0] * Tw / g;
+          for (int r = 0; r < nU; ++r) pen[r] = jac * pen[r];
+          for (int r = 0; r < nU; ++r)
+            b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] - p.viscousPenaltyAmount * pen[r];
+        } else {
+          double lam[5];
+          for (int c = 0; c < nU; ++c) lam[c] = b.adjointVariables[N * c + gi];
+          pen[0] = -lam[nD + 1] * Tw / g;
+          for (int c = 1; c < nU; ++c) pen[c] = lam[c];
+          for (int r = 0; r < nU; ++r) pen[r] = jac * pen[r];
+          for (int r = 0; r < nU; ++r)
+            b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] + p.viscousPenaltyAmount * pen[r];
+        }
+      });
+      break;
+    }
     case MGD_PATCH_SPONGE:
       for (int l = 0; l < nU; ++l)
         forPatchPoints(p, b, [&](long long gi, long long pi) {
@@ -1487,6 +1579,40 @@ static void substep(Region& R, int mode, double& time, double dt, int stage, boo
 
 static const double kRkNorm[4] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0};
 
+// Terminal kinetic energy sum_p H det rho |u|^2 / 2 over the non-hole points
+// (a cost functional with no reference counterpart, evaluated at the final step).
+static double terminalKineticEnergy(Region& R) {
+  double J = 0.0;
+  for (Block& b : R.blocks) {
+    const long long N = b.N;
+    for (long long p = 0; p < N; ++p) {
+      if (b.iblank[p] == 0) continue;
+      double m2 = 0.0;
+      for (int d = 0; d < R.nD; ++d) m2 += b.conservedVariables[N * (d + 1) + p] * b.conservedVariables[N * (d + 1) + p];
+      J += b.norm[p] * (0.5 * m2 / b.conservedVariables[p]);
+    }
+  }
+  return J;
+}
+
+// lambda(T) = H^-1 dJ/dq(T) of the terminal kinetic energy: (-|u|^2/2, u, 0).
+static void terminalKineticEnergyAdjoint(Region& R) {
+  for (Block& b : R.blocks) {
+    const long long N = b.N;
+    for (long long p = 0; p < N; ++p) {
+      for (int c = 0; c < R.nU; ++c) b.adjointVariables[N * c + p] = 0.0;
+      if (b.iblank[p] == 0) continue;
+      double u2 = 0.0;
+      for (int d = 0; d < R.nD; ++d) {
+        const double u = b.conservedVariables[N * (d + 1) + p] / b.conservedVariables[p];
+        b.adjointVariables[N * (d + 1) + p] = u;
+        u2 += u * u;
+      }
+      b.adjointVariables[p] = -0.5 * u2;
+    }
+  }
+}
+
 // computeTimeStepSize, src/CNSHelperImpl.f90:913-982, through
 // State%computeTimeStepSize (src/StateImpl.f90:605-670) and the minimum over
 // blocks of Region%getTimeStepSize (src/RegionImpl.f90:1842-1875). Uses the
@@ -1560,10 +1686,13 @@ static double runForward(Region& R, int nSteps, double t0, bool keepStages) {
       }
       if (R.o.enable_controller && R.o.controller_switch) loadForcing(R, step, i);
       substep(R, MGD_FORWARD, time, dt, i, true);
-      if (R.o.enable_functional) J = J + kRkNorm[i - 1] * dt * computeFunctional(R);
+      if (R.o.enable_functional && R.o.functional_type == MGD_FUNCTIONAL_SOUND)
+        J = J + kRkNorm[i - 1] * dt * computeFunctional(R);
     }
   }
   R.finalTime = time;
+  if (R.o.enable_functional && R.o.functional_type == MGD_FUNCTIONAL_TERMINAL_KINETIC_ENERGY)
+    J = terminalKineticEnergy(R);
   return J;
 }
 
@@ -1587,13 +1716,19 @@ static double runAdjoint(Region& R) {
   double dt = dtT;
   // final forward state is the current state
   updateAll(R);
-  for (Block& b : R.blocks) std::fill(b.adjointVariables.begin(), b.adjointVariables.end(), 0.0);
-  updateAdjointForcing(R, !R.o.adjoint_forcing_switch);
-  for (Block& b : R.blocks) std::fill(b.rightHandSide.begin(), b.rightHandSide.end(), 0.0);
-  for (Patch& p : R.patches)
-    if (p.d.type == MGD_PATCH_COST_TARGET) patchUpdateRhs(R, p, R.blocks[p.d.grid_index - 1], MGD_ADJOINT, -dtT / 6.0);
-  for (Block& b : R.blocks)
-    for (size_t k = 0; k < b.adjointVariables.size(); ++k) b.adjointVariables[k] = b.adjointVariables[k] + b.rightHandSide[k];
+  const bool terminal = R.o.functional_type == MGD_FUNCTIONAL_TERMINAL_KINETIC_ENERGY;
+  const bool forcing = R.o.adjoint_forcing_switch && !terminal;
+  if (terminal) {
+    terminalKineticEnergyAdjoint(R);
+  } else {
+    for (Block& b : R.blocks) std::fill(b.adjointVariables.begin(), b.adjointVariables.end(), 0.0);
+    updateAdjointForcing(R, !R.o.adjoint_forcing_switch);
+    for (Block& b : R.blocks) std::fill(b.rightHandSide.begin(), b.rightHandSide.end(), 0.0);
+    for (Patch& p : R.patches)
+      if (p.d.type == MGD_PATCH_COST_TARGET) patchUpdateRhs(R, p, R.blocks[p.d.grid_index - 1], MGD_ADJOINT, -dtT / 6.0);
+    for (Block& b : R.blocks)
+      for (size_t k = 0; k < b.adjointVariables.size(); ++k) b.adjointVariables[k] = b.adjointVariables[k] + b.rightHandSide[k];
+  }
   R.gradientEntries.clear();
   double time = R.finalTime - 0.5 * dt, s = 0.0;
   for (int step = R.nSteps; step >= 1; --step) {
@@ -1603,7 +1738,7 @@ static double runAdjoint(Region& R) {
       appendGradient(R);
       s = s + kRkNorm[i - 1] * dt * computeSensitivity(R);
       const bool finalStage = (step == 1 && i == 1);
-      updateAdjointForcing(R, !R.o.adjoint_forcing_switch || finalStage);
+      updateAdjointForcing(R, !forcing || finalStage);
       substep(R, MGD_ADJOINT, time, dt, i, false);
     }
   }

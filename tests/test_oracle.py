@@ -205,3 +205,62 @@ def test_oracle_time_step_size_restated_in_numpy():
     wv = jac ** 2 * np.sum(m ** 2, axis=0) * np.maximum(2.0 * mu, k)
     dt = min(dt, np.min(opt.cfl / wv))
     assert abs(o.time_step_size() - dt) <= 1e-13 * dt
+
+
+@pytest.mark.parametrize("wall", ["SAT_SLIP_WALL", "SAT_ISOTHERMAL_WALL", "SAT_ADIABATIC_WALL"])
+def test_full_rhs_dual_consistency_walls(wall):
+    """Dual consistency of the full RHS with wall SATs on two faces
+    (test/adjoint_relation/SAT_isothermal.f90 and full_rhs.f90)."""
+    P = configs.wall_channel_2d(n=31, ny=29, wall=wall)
+    assert _dual_consistency(P) >= 0.9
+
+
+def test_isothermal_wall_sat_vanishes_on_wall_state():
+    """The forward wall SAT is zero on a state that satisfies the wall
+    conditions: no velocity and the wall temperature (isothermal_wall_SAT.f90:150-200)."""
+    Tw = 2.7
+    P = configs.wall_channel_2d(n=31, ny=29, wall="SAT_ISOTHERMAL_WALL", wall_temperature=Tw)
+    Pref = configs.wall_channel_2d(n=31, ny=29, wall="SAT_SLIP_WALL")
+    rng = np.random.default_rng(4)
+    q, _ = random_full_rhs_state(P, 4)
+    g = P.options.ratio_of_specific_heats
+    n, ny = 31, 29
+    for j in (0, ny - 1):
+        k = np.arange(n) + n * j
+        q[1, k] = 0.0
+        q[2, k] = 0.0
+        q[3, k] = q[0, k] * Tw / g  # rho T / gamma with u = 0
+    rhs = []
+    for prob in (P, Pref):
+        o = oracle_lib.Oracle(prob)
+        o.set_field(1, capi.FIELD_CONSERVED, q)
+        o.update_state()
+        o.compute_rhs(capi.FORWARD, 0.0)
+        rhs.append(o.get_field(1, capi.FIELD_RHS))
+    # the isothermal wall adds nothing beyond the (also vanishing) slip-wall penalty
+    assert np.max(np.abs(rhs[0] - rhs[1])) <= 1e-12 * np.max(np.abs(rhs[1]))
+    del rng
+
+
+def test_terminal_kinetic_energy_gradient_finite_differences():
+    """Terminal kinetic-energy functional on the 3D Taylor-Green vortex: the
+    adjoint state at t = 0 is the H-weighted gradient of J(T) with respect to
+    the initial state, checked against central differences."""
+    P = configs.taylor_green_3d(n=12, dt=0.02, n_steps=6, save_interval=3)
+    q0 = P.blocks[0].initial_state.copy()
+    rng = np.random.default_rng(5)
+    dq = rng.standard_normal(q0.shape) * 1e-2
+    o = oracle_lib.Oracle(P)
+    norm = o.get_field(1, capi.FIELD_NORM)
+
+    def J(q):
+        o.set_field(1, capi.FIELD_CONSERVED, q)
+        return o.run_forward(P.n_steps, P.save_interval)
+
+    J(q0)
+    o.run_adjoint()
+    lam0 = o.get_field(1, capi.FIELD_ADJOINT)
+    an = np.sum(norm * lam0 * dq)
+    eps = 1e-4
+    fd = (J(q0 + eps * dq) - J(q0 - eps * dq)) / (2 * eps)
+    assert abs(fd - an) <= 1e-7 * abs(an)
