@@ -49,9 +49,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rk-steps", type=int, default=N_STEPS,
                     help="RK4 steps per gradient evaluation (profiling runs use a few)")
-    ap.add_argument("--workload", default="gradient", choices=["gradient", "sweep"],
+    ap.add_argument("--workload", default="gradient", choices=["gradient", "sweep", "tgv"],
                     help="gradient: the forward + adjoint gradient evaluation (default); sweep: the batched "
-                         "gradient-check sweep of 64 monopole instances of mixed grid sizes")
+                         "gradient-check sweep of 64 monopole instances of mixed grid sizes; tgv: the 3D "
+                         "Taylor-Green vortex forward + adjoint (terminal kinetic energy, constant CFL)")
+    ap.add_argument("--tgv-n", type=int, default=256)
     ap.add_argument("--sweep-instances", type=int, default=64)
     ap.add_argument("--profile-only", action="store_true",
                     help="run the gradient evaluations and exit (for ncu captures; prints no bench line)")
@@ -444,12 +446,75 @@ def run_sweep(args):
         torch.distributed.destroy_process_group()
 
 
+def run_tgv(args):
+    """3D Taylor-Green vortex on n^3 points, PLANE-periodic, Re 1600, Mach 0.1,
+    constant CFL 0.5: forward run plus the discrete adjoint of the terminal
+    kinetic energy, with checkpoints held on the device. The configured run
+    has 2000 steps; one bench step is a bounded sample of --rk-steps steps
+    (forward + adjoint) of it, and the metric counts grid points x RHS
+    evaluations per second like the default workload."""
+    import torch
+    from magudi_gb300 import configs
+    from magudi_gb300.solver import Solver
+
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    n_steps = args.rk_steps
+    P = configs.taylor_green_3d(n=args.tgv_n, n_steps=n_steps)
+    S = P.save_interval
+    s = Solver(P)
+    q0 = P.blocks[0].initial_state
+    from magudi_gb300 import capi
+
+    def step():
+        s.set_field(1, capi.FIELD_CONSERVED, q0)
+        J = s.run_forward(n_steps, S)
+        s.run_adjoint()
+        return J
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    s.kernel_launches(reset=True)
+    clocks = ClockSampler()
+    clocks.start()
+    times = []
+    J = None
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        J = step()
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t)
+    clk = clocks.stop()
+    sec = statistics.mean(times)
+    pts = args.tgv_n ** 3
+    dts = s.step_sizes(n_steps)
+    line = {
+        "metric": "FP64 Mpt-RHS/s", "value": pts * 8 * n_steps / sec / 1e6, "unit": "Mpt-RHS/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (Taylor-Green initial field)",
+        "config": {"workload": f"3D Taylor-Green vortex {args.tgv_n}^3 PLANE-periodic, Re 1600, M 0.1, SBP 4-8 + "
+                               f"dissipation, constant CFL 0.5, forward + discrete adjoint of the terminal "
+                               f"kinetic energy; sample of {n_steps} of the 2000 steps, checkpoint every {S}",
+                   "grid": f"{args.tgv_n}^3", "rk4_steps": n_steps, "save_interval": S,
+                   "l2": "working set larger than L2", "parallelism": "single GPU"},
+        "J": J, "dt_first": float(dts[0]), "dt_last": float(dts[-1]),
+        "projected_2000_step_gradient_s": sec / n_steps * 2000,
+        "gpu_launches": s.kernel_launches(reset=True) // max(1, args.steps), "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "sweep":
         run_sweep(args)
+    elif args.workload == "tgv":
+        run_tgv(args)
     else:
         run_ours(args)
 
