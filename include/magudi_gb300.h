@@ -41,7 +41,8 @@ enum {
   MGD_PATCH_COST_TARGET = 4,
   MGD_PATCH_SLIP_WALL = 5,         /* SAT_SLIP_WALL: t_ImpenetrableWall */
   MGD_PATCH_ISOTHERMAL_WALL = 6,   /* SAT_ISOTHERMAL_WALL */
-  MGD_PATCH_ADIABATIC_WALL = 7     /* SAT_ADIABATIC_WALL */
+  MGD_PATCH_ADIABATIC_WALL = 7,    /* SAT_ADIABATIC_WALL */
+  MGD_PATCH_BLOCK_INTERFACE = 8    /* SAT_BLOCK_INTERFACE */
 };
 
 /* Fields that mgd_set_field / mgd_get_field move between host and device. */
@@ -119,6 +120,9 @@ typedef struct {
   double wall_temperature;           /* isothermal walls: patches/<name>/temperature, or
                                         <= 0 for the target state's temperature
                                         (use_target_state, src/PatchFactoryImpl.f90:512-538) */
+  char conforms_with[MGD_NAME_LEN];  /* block interfaces: patches/<name>/conforms_with */
+  int interface_index[3];            /* patches/<name>/interface_index1..3 (0 = default 1,2,3)
+                                        (src/InterfaceHelperImpl.f90:3-113) */
 } mgd_patch_desc;
 
 /* acoustic_sourceNN/... (src/AcousticSourceImpl.f90:3-32). */

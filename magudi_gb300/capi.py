@@ -27,6 +27,7 @@ PATCH_COST_TARGET = 4
 PATCH_SLIP_WALL = 5
 PATCH_ISOTHERMAL_WALL = 6
 PATCH_ADIABATIC_WALL = 7
+PATCH_BLOCK_INTERFACE = 8
 
 PATCH_TYPES = {
     "SAT_FAR_FIELD": PATCH_SAT_FAR_FIELD,
@@ -36,6 +37,7 @@ PATCH_TYPES = {
     "SAT_SLIP_WALL": PATCH_SLIP_WALL,
     "SAT_ISOTHERMAL_WALL": PATCH_ISOTHERMAL_WALL,
     "SAT_ADIABATIC_WALL": PATCH_ADIABATIC_WALL,
+    "SAT_BLOCK_INTERFACE": PATCH_BLOCK_INTERFACE,
 }
 
 FIELD_CONSERVED = 0
@@ -97,6 +99,8 @@ class PatchDesc(C.Structure):
         ("sponge_amount", C.c_double),
         ("sponge_exponent", C.c_int),
         ("wall_temperature", C.c_double),
+        ("conforms_with", C.c_char * MGD_NAME_LEN),
+        ("interface_index", C.c_int * 3),
     ]
 
 

@@ -123,6 +123,79 @@ def wall_channel_2d(n=41, ny=33, wall="SAT_ISOTHERMAL_WALL", wall_temperature=0.
     return Problem(options=opts, blocks=[block], patches=patches, sources=[], n_steps=n_steps, save_interval=5)
 
 
+def two_block_2d(nx1=25, nx2=29, ny=31, half_width=6.0, viscous=True, rotate_second=False, curvilinear=None,
+                 interfaces=True, dt=0.02, n_steps=10, sponge_points=5):
+    """Two blocks meeting at x = 0 through SAT_BLOCK_INTERFACE patches: block 1
+    covers [-w, 0] x [-w, w], block 2 covers [0, w] x [-w, w]; far-field SATs
+    and sponges on the outer faces; quiescent target and initial state.
+    rotate_second stores block 2 with its first index along +y and its second
+    along -x (a rotation, so the Jacobian stays positive), which makes the
+    interface a transposing one (interface_index 2, 1, 3). Without
+    `interfaces`, the x = 0 faces carry no patch."""
+    gamma = 1.4
+    curv = rotate_second if curvilinear is None else curvilinear
+    opts = Options(
+        n_dimensions=2, viscous=viscous, dissipation=True, composite_dissipation=True,
+        curvilinear=curv, use_constant_cfl=False, enable_controller=False, enable_functional=False,
+        ratio_of_specific_heats=gamma, reynolds_number=200.0, prandtl_number=0.72,
+        viscosity_power_law_exponent=0.666, bulk_viscosity_ratio=0.6, dissipation_amount=0.01,
+        time_step_size=dt)
+    w = half_width
+    x1 = np.linspace(-w, 0.0, nx1)
+    x2 = np.linspace(0.0, w, nx2)
+    y = np.linspace(-w, w, ny)
+    X1, Y1 = np.meshgrid(x1, y, indexing="xy")
+    c1 = np.stack([X1.ravel(), Y1.ravel()])
+    if rotate_second:
+        # point (i, j): x = x2[nx2 - j], y = y[i - 1]; i fastest
+        Yr, Xr = np.meshgrid(y, x2[::-1], indexing="xy")
+        c2 = np.stack([Xr.ravel(), Yr.ravel()])
+        gs2 = (ny, nx2, 1)
+    else:
+        X2, Y2 = np.meshgrid(x2, y, indexing="xy")
+        c2 = np.stack([X2.ravel(), Y2.ravel()])
+        gs2 = (nx2, ny, 1)
+    blocks = []
+    for c, gs in ((c1, (nx1, ny, 1)), (c2, gs2)):
+        N = c.shape[1]
+        t = quiescent_state(N, 2, gamma)
+        blocks.append(Block(grid_size=gs, coordinates=np.ascontiguousarray(c), initial_state=t.copy(),
+                            target_state=t.copy(), control_mollifier=np.ones(N), target_mollifier=np.ones(N),
+                            mean_pressure=np.full(N, 1.0 / gamma)))
+    s = sponge_points
+    patches = [
+        Patch("farField.W", "SAT_FAR_FIELD", 1, 1, (1, 1, 1, -1, 1, -1)),
+        Patch("farField.S1", "SAT_FAR_FIELD", 1, 2, (1, -1, 1, 1, 1, -1)),
+        Patch("farField.N1", "SAT_FAR_FIELD", 1, -2, (1, -1, -1, -1, 1, -1)),
+        Patch("sponge.W", "SPONGE", 1, 1, (1, s, 1, -1, 1, -1), sponge_amount=0.2),
+    ]
+    if rotate_second:
+        patches += [
+            Patch("farField.E", "SAT_FAR_FIELD", 2, 2, (1, -1, 1, 1, 1, -1)),
+            Patch("farField.S2", "SAT_FAR_FIELD", 2, 1, (1, 1, 1, -1, 1, -1)),
+            Patch("farField.N2", "SAT_FAR_FIELD", 2, -1, (-1, -1, 1, -1, 1, -1)),
+            Patch("sponge.E", "SPONGE", 2, 2, (1, -1, 1, s, 1, -1), sponge_amount=0.2),
+        ]
+        iface2 = Patch("interface.2W", "SAT_BLOCK_INTERFACE", 2, -2, (1, -1, -1, -1, 1, -1),
+                       viscous_penalty_amount=0.5)
+        iface1 = Patch("interface.1E", "SAT_BLOCK_INTERFACE", 1, -1, (-1, -1, 1, -1, 1, -1),
+                       viscous_penalty_amount=0.5, conforms_with="interface.2W", interface_index=(2, 1, 3))
+    else:
+        patches += [
+            Patch("farField.E", "SAT_FAR_FIELD", 2, -1, (-1, -1, 1, -1, 1, -1)),
+            Patch("farField.S2", "SAT_FAR_FIELD", 2, 2, (1, -1, 1, 1, 1, -1)),
+            Patch("farField.N2", "SAT_FAR_FIELD", 2, -2, (1, -1, -1, -1, 1, -1)),
+            Patch("sponge.E", "SPONGE", 2, -1, (-s, -1, 1, -1, 1, -1), sponge_amount=0.2),
+        ]
+        iface2 = Patch("interface.2W", "SAT_BLOCK_INTERFACE", 2, 1, (1, 1, 1, -1, 1, -1),
+                       viscous_penalty_amount=0.5)
+        iface1 = Patch("interface.1E", "SAT_BLOCK_INTERFACE", 1, -1, (-1, -1, 1, -1, 1, -1),
+                       viscous_penalty_amount=0.5, conforms_with="interface.2W")
+    if interfaces:
+        patches += [iface1, iface2]
+    return Problem(options=opts, blocks=blocks, patches=patches, sources=[], n_steps=n_steps, save_interval=5)
+
+
 def random_state(n_points, n_dimensions, gamma, rng):
     """full_rhs.f90:289-301: rho in U[0.01,10], u in U[-10,10], p in U[0.01,10]/gamma."""
     nU = n_dimensions + 2

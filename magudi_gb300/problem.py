@@ -64,6 +64,8 @@ class Patch:
     sponge_amount: float = 1.0
     sponge_exponent: int = 2
     wall_temperature: float = 0.0  # isothermal walls: <= 0 takes the target state's temperature
+    conforms_with: str = ""        # block interfaces: name of the conforming patch
+    interface_index: tuple = (0, 0, 0)  # block interfaces: index reordering (0 = 1, 2, 3)
 
     def to_c(self) -> capi.PatchDesc:
         p = capi.PatchDesc()
@@ -78,6 +80,9 @@ class Patch:
         p.sponge_amount = self.sponge_amount
         p.sponge_exponent = int(self.sponge_exponent)
         p.wall_temperature = float(self.wall_temperature)
+        p.conforms_with = self.conforms_with.encode()[: capi.MGD_NAME_LEN - 1]
+        for i in range(3):
+            p.interface_index[i] = int(self.interface_index[i])
         return p
 
     def resolved_extent(self, grid_size):

@@ -411,31 +411,70 @@ void inviscidJacobian(int nD, const double* cv, const double* m, double g, doubl
 
 // computeIncomingJacobianOfInviscidFlux{2D,3D}, src/CNSHelperImpl.f90:1669-2343
 // (without the variations). The state is passed as conserved variables only.
-void incomingJacobian(int nD, const double* cv, const double* metrics, double g,
-                      int incomingDirection, double* out) {
+// Forward-mode dual number with up to 5 directional derivatives: the exact
+// derivative of the incoming Jacobian of a Roe-averaged state with respect to
+// the left state (the variation the block-interface adjoint needs,
+// src/CNSHelperImpl.f90:1669-2343 with deltaRoeAverage) is obtained by
+// evaluating the same function on dual numbers.
+struct Dual {
+  double v = 0.0;
+  double d[5] = {0, 0, 0, 0, 0};
+  Dual() = default;
+  Dual(double x) : v(x) {}
+};
+static inline double value(double x) { return x; }
+static inline double value(const Dual& x) { return x.v; }
+static inline Dual operator+(const Dual& a, const Dual& b) { Dual r(a.v + b.v); for (int k = 0; k < 5; ++k) r.d[k] = a.d[k] + b.d[k]; return r; }
+static inline Dual operator-(const Dual& a, const Dual& b) { Dual r(a.v - b.v); for (int k = 0; k < 5; ++k) r.d[k] = a.d[k] - b.d[k]; return r; }
+static inline Dual operator-(const Dual& a) { Dual r(-a.v); for (int k = 0; k < 5; ++k) r.d[k] = -a.d[k]; return r; }
+static inline Dual operator*(const Dual& a, const Dual& b) { Dual r(a.v * b.v); for (int k = 0; k < 5; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k]; return r; }
+static inline Dual operator/(const Dual& a, const Dual& b) {
+  Dual r(a.v / b.v);
+  for (int k = 0; k < 5; ++k) r.d[k] = (a.d[k] * b.v - a.v * b.d[k]) / (b.v * b.v);
+  return r;
+}
+static inline Dual operator+(const Dual& a, double b) { return a + Dual(b); }
+static inline Dual operator+(double a, const Dual& b) { return Dual(a) + b; }
+static inline Dual operator-(const Dual& a, double b) { return a - Dual(b); }
+static inline Dual operator-(double a, const Dual& b) { return Dual(a) - b; }
+static inline Dual operator*(const Dual& a, double b) { Dual r(a.v * b); for (int k = 0; k < 5; ++k) r.d[k] = a.d[k] * b; return r; }
+static inline Dual operator*(double a, const Dual& b) { return b * a; }
+static inline Dual operator/(const Dual& a, double b) { return a / Dual(b); }
+static inline Dual operator/(double a, const Dual& b) { return Dual(a) / b; }
+static inline Dual& operator+=(Dual& a, const Dual& b) { a = a + b; return a; }
+static inline Dual sqrt(const Dual& a) {
+  Dual r(std::sqrt(a.v));
+  for (int k = 0; k < 5; ++k) r.d[k] = a.d[k] / (2.0 * r.v);
+  return r;
+}
+using std::sqrt;
+
+template <class S>
+void incomingJacobianT(int nD, const S* cv, const double* metrics, double g,
+                       int incomingDirection, S* out) {
   const int nU = nD + 2;
   double arc = 0.0;
   for (int d = 0; d < nD; ++d) arc += metrics[d] * metrics[d];
   arc = std::sqrt(arc);
   double nm[3];
   for (int d = 0; d < nD; ++d) nm[d] = metrics[d] / arc;
-  const double v = 1.0 / cv[0];
-  double u[3], u2 = 0.0;
+  const S v = 1.0 / cv[0];
+  S u[3], u2 = 0.0;
   for (int d = 0; d < nD; ++d) u[d] = v * cv[d + 1];
   for (int d = 0; d < nD; ++d) u2 += u[d] * u[d];
-  const double T = g * (v * cv[nD + 1] - 0.5 * u2);
-  double U = 0.0;
+  const S T = g * (v * cv[nD + 1] - 0.5 * u2);
+  S U = 0.0;
   for (int d = 0; d < nD; ++d) U += nm[d] * u[d];
-  const double c = std::sqrt((g - 1.0) * T);
-  const double phi2 = 0.5 * (g - 1.0) * u2;
-  double R[25], Lt[25], lam[5];
-  auto r = [&](int i, int j) -> double& { return R[(i - 1) + nU * (j - 1)]; };
-  auto l = [&](int i, int j) -> double& { return Lt[(i - 1) + nU * (j - 1)]; };
-  const double rho = cv[0];
+  const S c = sqrt((g - 1.0) * T);
+  const S phi2 = 0.5 * (g - 1.0) * u2;
+  S R[25], Lt[25], lam[5];
+  auto r = [&](int i, int j) -> S& { return R[(i - 1) + nU * (j - 1)]; };
+  auto l = [&](int i, int j) -> S& { return Lt[(i - 1) + nU * (j - 1)]; };
+  const S rho = cv[0];
   if (nD == 2) {
     lam[0] = U; lam[1] = U; lam[2] = U + c; lam[3] = U - c;
     for (int i = 0; i < 4; ++i) lam[i] = arc * lam[i];
-    for (int i = 0; i < 4; ++i) if (incomingDirection * lam[i] < 0.0) lam[i] = 0.0;
+    for (int i = 0; i < 4; ++i) if (incomingDirection * value(lam[i]) < 0.0) lam[i] = 0.0;
     r(1, 1) = 1.0; r(2, 1) = u[0]; r(3, 1) = u[1]; r(4, 1) = phi2 / (g - 1.0);
     r(1, 2) = 0.0; r(2, 2) = nm[1] * rho; r(3, 2) = -nm[0] * rho;
     r(4, 2) = rho * (nm[1] * u[0] - nm[0] * u[1]);
@@ -455,8 +494,8 @@ void incomingJacobian(int nD, const double* cv, const double* metrics, double g,
   } else {
     lam[0] = U; lam[1] = U; lam[2] = U; lam[3] = U + c; lam[4] = U - c;
     for (int i = 0; i < 5; ++i) lam[i] = arc * lam[i];
-    for (int i = 0; i < 5; ++i) if (incomingDirection * lam[i] < 0.0) lam[i] = 0.0;
-    const double h0 = phi2 / (g - 1.0);
+    for (int i = 0; i < 5; ++i) if (incomingDirection * value(lam[i]) < 0.0) lam[i] = 0.0;
+    const S h0 = phi2 / (g - 1.0);
     r(1, 1) = nm[0]; r(2, 1) = nm[0] * u[0]; r(3, 1) = nm[0] * u[1] + rho * nm[2];
     r(4, 1) = nm[0] * u[2] - rho * nm[1];
     r(5, 1) = rho * (nm[2] * u[1] - nm[1] * u[2]) + h0 * nm[0];
@@ -470,7 +509,7 @@ void incomingJacobian(int nD, const double* cv, const double* metrics, double g,
     r(4, 4) = u[2] + nm[2] * c; r(5, 4) = T + h0 + c * U;
     r(1, 5) = 1.0; r(2, 5) = u[0] - nm[0] * c; r(3, 5) = u[1] - nm[1] * c;
     r(4, 5) = u[2] - nm[2] * c; r(5, 5) = T + h0 - c * U;
-    const double q = 1.0 - phi2 / (c * c);
+    const S q = 1.0 - phi2 / (c * c);
     l(1, 1) = nm[0] * q - v * (nm[2] * u[1] - nm[1] * u[2]);
     l(2, 1) = nm[1] * q - v * (nm[0] * u[2] - nm[2] * u[0]);
     l(3, 1) = nm[2] * q - v * (nm[1] * u[0] - nm[0] * u[1]);
@@ -490,10 +529,35 @@ void incomingJacobian(int nD, const double* cv, const double* metrics, double g,
   }
   for (int j = 1; j <= nU; ++j)
     for (int i = 1; i <= nU; ++i) {
-      double s = r(i, 1) * lam[0] * l(1, j);
+      S s = r(i, 1) * lam[0] * l(1, j);
       for (int k = 2; k <= nU; ++k) s += r(i, k) * lam[k - 1] * l(k, j);
       out[(i - 1) + nU * (j - 1)] = s;
     }
+}
+
+void incomingJacobian(int nD, const double* cv, const double* metrics, double g, int incomingDirection,
+                      double* out) {
+  incomingJacobianT<double>(nD, cv, metrics, g, incomingDirection, out);
+}
+
+// computeRoeAverage, src/CNSHelperImpl.f90:179-351 (without the variations).
+template <class S>
+void roeAverage(int nD, const S* qL, const S* qR, double g, S* roe) {
+  const S sL = sqrt(qL[0]), sR = sqrt(qR[0]);
+  const S vL = 1.0 / qL[0], vR = 1.0 / qR[0];
+  S mL2 = qL[1] * qL[1], mR2 = qR[1] * qR[1];
+  for (int d = 1; d < nD; ++d) {
+    mL2 = mL2 + qL[1 + d] * qL[1 + d];
+    mR2 = mR2 + qR[1 + d] * qR[1 + d];
+  }
+  const S hL = g * qL[nD + 1] - 0.5 * (g - 1.0) * vL * mL2;
+  const S hR = g * qR[nD + 1] - 0.5 * (g - 1.0) * vR * mR2;
+  roe[0] = sL * sR;
+  for (int d = 0; d < nD; ++d) roe[1 + d] = (sR * qL[1 + d] + sL * qR[1 + d]) / (sL + sR);
+  roe[nD + 1] = (sR * hL + sL * hR) / (sL + sR);
+  S m2 = roe[1] * roe[1];
+  for (int d = 1; d < nD; ++d) m2 = m2 + roe[1 + d] * roe[1 + d];
+  roe[nD + 1] = (roe[nD + 1] + 0.5 * (g - 1.0) / roe[0] * m2) / g;
 }
 
 // computeFirstPartialViscousJacobian{2D,3D}, src/CNSHelperImpl.f90:2412-2601.
@@ -574,6 +638,12 @@ struct Patch {
   std::vector<double> adjointForcing;       // (nPatchPoints, nU)
   std::vector<double> controlForcing;       // (nPatchPoints, nU)
   std::vector<double> wallTemperature;      // (nPatchPoints), isothermal walls
+  // block interfaces (src/BlockInterfacePatchImpl.f90, src/InterfaceHelperImpl.f90)
+  int partner = -1;                         // index of the conforming patch
+  int reorder[3] = {1, 2, 3};               // interfaceIndexReorderings of this patch
+  std::vector<long long> partnerPoint;      // partner patch index of each patch point
+  std::vector<double> metricsL, metricsR;   // (nPatchPoints, nD) normal metrics of both sides
+  std::vector<double> ifViscousFlux;        // (nPatchPoints, nU): sum_j Fv(:, j) m_L,j, component 0 zero
 };
 
 static bool isWall(int type) {
@@ -908,6 +978,101 @@ static void cartesianFluxes(Region& R, Block& b, const double* q, double* fInv, 
   }
 }
 
+// Block interfaces: partners and index reorderings (readPatchInterfaceInformation,
+// src/InterfaceHelperImpl.f90:3-113), the point correspondence that
+// reshapeReceivedData applies (src/BlockInterfacePatchImpl.f90:785-931), the
+// penalty amounts (setupBlockInterfacePatch, :3-88) and the normal metrics of
+// both sides (the METRICS exchange of collectInterfaceData, :598-720).
+static int setupInterfaces(Region& R) {
+  const int nP = (int)R.patches.size();
+  for (int i = 0; i < nP; ++i) {
+    Patch& p = R.patches[i];
+    if (p.d.type != MGD_PATCH_BLOCK_INTERFACE || p.d.conforms_with[0] == 0) continue;
+    int j = -1;
+    for (int k = 0; k < nP; ++k)
+      if (std::strncmp(R.patches[k].d.name, p.d.conforms_with, MGD_NAME_LEN) == 0) j = k;
+    if (j < 0 || R.patches[j].d.type != MGD_PATCH_BLOCK_INTERFACE) {
+      R.error = std::string("invalid interface specification for patch '") + p.d.name + "'";
+      return 1;
+    }
+    p.partner = j;
+    for (int c = 0; c < 3; ++c) p.reorder[c] = p.d.interface_index[c] != 0 ? p.d.interface_index[c] : c + 1;
+  }
+  for (int i = 0; i < nP; ++i) {
+    Patch& p = R.patches[i];
+    if (p.d.type != MGD_PATCH_BLOCK_INTERFACE) continue;
+    if (p.partner < 0) continue;
+    Patch& q = R.patches[p.partner];
+    if (q.partner < 0) {
+      q.partner = i;
+      for (int l = 1; l <= 3; ++l)
+        for (int k = 1; k <= 3; ++k)
+          if (std::abs(p.reorder[k - 1]) == l) {
+            q.reorder[l - 1] = p.reorder[k - 1] < 0 ? -k : k;
+            break;
+          }
+    } else if (q.partner != i) {
+      R.error = std::string("interface specification of patch '") + q.d.name + "' violates commutativity";
+      return 1;
+    }
+  }
+  for (int i = 0; i < nP; ++i) {
+    Patch& p = R.patches[i];
+    if (p.d.type != MGD_PATCH_BLOCK_INTERFACE) continue;
+    if (p.partner < 0) {
+      R.error = std::string("block interface patch '") + p.d.name + "' has no conforming patch";
+      return 1;
+    }
+    Patch& q = R.patches[p.partner];
+    Block& b = R.blocks[p.d.grid_index - 1];
+    const int nD = R.nD, dir = std::abs(p.d.normal_direction);
+    const double nb = b.firstDerivative[dir - 1].normBoundary[0];
+    p.inviscidPenaltyAmount = std::copysign(p.d.inviscid_penalty_amount, (double)p.d.normal_direction) / nb;
+    p.viscousPenaltyAmount = R.o.viscous ? std::copysign(p.d.viscous_penalty_amount, (double)p.d.normal_direction) / nb : 0.0;
+    // reshapeReceivedData: transpose when the first two indices swap, then reflect
+    int o[3] = {p.reorder[0], p.reorder[1], p.reorder[2]};
+    const bool transpose = std::abs(o[0]) == 2 && std::abs(o[1]) == 1;
+    if (transpose) std::swap(o[0], o[1]);
+    const long long g0 = p.localSize[0], g1 = p.localSize[1];
+    p.partnerPoint.assign(p.nPatchPoints, 0);
+    for (long long k = 1; k <= p.localSize[2]; ++k)
+      for (long long jj = 1; jj <= g1; ++jj)
+        for (long long ii = 1; ii <= g0; ++ii) {
+          const long long fi = o[0] == -1 ? g0 + 1 - ii : ii;
+          const long long fj = o[1] == -2 ? g1 + 1 - jj : jj;
+          const long long a = transpose ? fj : fi, c = transpose ? fi : fj;
+          const long long qi = (a - 1) + q.localSize[0] * ((c - 1) + q.localSize[1] * (k - 1));
+          if (a < 1 || a > q.localSize[0] || c < 1 || c > q.localSize[1] || qi >= q.nPatchPoints) {
+            R.error = std::string("block interface patches '") + p.d.name + "' and '" + q.d.name +
+                      "' do not conform";
+            return 1;
+          }
+          p.partnerPoint[(ii - 1) + g0 * ((jj - 1) + g1 * (k - 1))] = qi;
+        }
+    p.metricsL.assign(p.nPatchPoints * nD, 0.0);
+    forPatchPoints(p, b, [&](long long gi, long long pi) {
+      for (int d = 0; d < nD; ++d) p.metricsL[p.nPatchPoints * d + pi] = b.metrics[b.N * (nD * (dir - 1) + d) + gi];
+    });
+    p.ifViscousFlux.assign(p.nPatchPoints * R.nU, 0.0);
+  }
+  for (int i = 0; i < nP; ++i) {
+    Patch& p = R.patches[i];
+    if (p.d.type != MGD_PATCH_BLOCK_INTERFACE) continue;
+    const Patch& q = R.patches[p.partner];
+    p.metricsR.assign(p.nPatchPoints * R.nD, 0.0);
+    for (long long pi = 0; pi < p.nPatchPoints; ++pi)
+      for (int d = 0; d < R.nD; ++d) p.metricsR[p.nPatchPoints * d + pi] = q.metricsL[q.nPatchPoints * d + p.partnerPoint[pi]];
+  }
+  return 0;
+}
+
+// Grid index of patch point pi of patch p in its block.
+static long long patchPointGridIndex(const Patch& p, const Block& b, long long pi) {
+  const long long i = pi % p.localSize[0], j = (pi / p.localSize[0]) % p.localSize[1],
+                  k = pi / (p.localSize[0] * p.localSize[1]);
+  return (p.offset[0] + i) + b.gs[0] * ((p.offset[1] + j) + (long long)b.gs[1] * (p.offset[2] + k));
+}
+
 // Far-field patch setup, src/FarFieldPatchImpl.f90:3-74; sponge strengths,
 // src/PatchFactoryImpl.f90:161-374; updatePatchFactories (:446-574).
 static int setupPatches(Region& R) {
@@ -965,6 +1130,7 @@ static int setupPatches(Region& R) {
     if (p.d.type == MGD_PATCH_ACTUATOR) p.controlForcing.assign(p.nPatchPoints * R.nU, 0.0);
     if (p.d.type == MGD_PATCH_SPONGE) p.spongeStrength.assign(p.nPatchPoints, 0.0);
   }
+  if (setupInterfaces(R)) return 1;
   // computeSpongeStrengths
   for (size_t bi = 0; bi < R.blocks.size(); ++bi) {
     Block& b = R.blocks[bi];
@@ -1092,9 +1258,20 @@ static void computeRhsForward(Region& R, Block& b, int bi) {
     for (long long k = 0; k < N * nU * nD; ++k) f1[k] = f1[k] - f2[k];
   if (R.o.viscous)
     for (Patch& p : R.patches) {
-      if (p.d.grid_index != bi + 1 || p.nPatchPoints <= 0 || p.d.type != MGD_PATCH_SAT_FAR_FIELD) continue;
-      for (int c = 0; c < nU * nD; ++c)
-        forPatchPoints(p, b, [&](long long gi, long long pi) { p.viscousFluxes[p.nPatchPoints * c + pi] = f2[N * c + gi]; });
+      if (p.d.grid_index != bi + 1 || p.nPatchPoints <= 0) continue;
+      if (p.d.type == MGD_PATCH_SAT_FAR_FIELD)
+        for (int c = 0; c < nU * nD; ++c)
+          forPatchPoints(p, b, [&](long long gi, long long pi) { p.viscousFluxes[p.nPatchPoints * c + pi] = f2[N * c + gi]; });
+      if (p.d.type == MGD_PATCH_BLOCK_INTERFACE)
+        // viscousFluxesL = sum_j cartesianViscousFluxesL(:,:,j) m_L,j (src/BlockInterfacePatchImpl.f90:645-653)
+        forPatchPoints(p, b, [&](long long gi, long long pi) {
+          p.ifViscousFlux[pi] = 0.0;
+          for (int c = 1; c < nU; ++c) {
+            double s = 0.0;
+            for (int d = 0; d < nD; ++d) s = s + f2[N * (c + nU * d) + gi] * p.metricsL[p.nPatchPoints * d + pi];
+            p.ifViscousFlux[p.nPatchPoints * c + pi] = s;
+          }
+        });
     }
   // transformFluxes, src/CNSHelperImpl.f90:772-840
   auto M = [&](int c, long long p) { return b.metrics[N * (c - 1) + p]; };
@@ -1148,6 +1325,71 @@ static void addFarFieldAdjointPenalty(Region& R, Block& b, int bi) {
           double s = B[0 + (nU - 1) * r] * b.adjointVariables[N * 1 + gi];
           for (int k = 1; k < nU - 1; ++k) s += B[k + (nU - 1) * r] * b.adjointVariables[N * (k + 1) + gi];
           temp1[N * (r + (nU - 1) * l) + gi] = temp1[N * (r + (nU - 1) * l) + gi] - p.viscousPenaltyAmount * s;
+        }
+      }
+    });
+  }
+  for (int i = 0; i < nD; ++i) apply(b.adjointFirstDerivative[i], &temp1[N * (nU - 1) * i], nU - 1, b.gs, i);
+  for (int c = 0; c < nU - 1; ++c)
+    for (long long q = 0; q < N; ++q) {
+      double s = temp1[N * c + q];
+      for (int i = 1; i < nD; ++i) s += temp1[N * (c + (nU - 1) * i) + q];
+      temp2[N * c + q] = s;
+    }
+  const double g = R.o.ratio_of_specific_heats;
+  for (long long q = 0; q < N; ++q) {
+    const double v = b.specificVolume[q];
+    temp2[N * nD + q] = g * v * temp2[N * nD + q];
+    for (int i = 0; i < nD; ++i) temp2[N * i + q] = v * temp2[N * i + q] - b.velocity[N * i + q] * temp2[N * nD + q];
+    for (int c = 1; c < nU; ++c) b.rightHandSide[N * c + q] = b.rightHandSide[N * c + q] + temp2[N * (c - 1) + q];
+    double su = b.velocity[q] * temp2[q];
+    for (int i = 1; i < nD; ++i) su += b.velocity[N * i + q] * temp2[N * i + q];
+    b.rightHandSide[q] = b.rightHandSide[q] - v * b.conservedVariables[N * (nD + 1) + q] * temp2[N * nD + q] - su;
+  }
+}
+
+// addInterfaceAdjointPenalty, src/RhsHelperImpl.f90:831-1026: the viscous
+// second-partial terms of both sides of every block interface at its points,
+// swept with the adjoint derivative over the whole block and mapped to the
+// conservative variables.
+static void addInterfaceAdjointPenalty(Region& R, Block& b, int bi) {
+  const int nD = R.nD, nU = R.nU;
+  const long long N = b.N;
+  bool any = false;
+  for (Patch& p : R.patches) any = any || (p.d.type == MGD_PATCH_BLOCK_INTERFACE && p.d.grid_index == bi + 1);
+  if (!any) return;
+  std::vector<double> temp1(N * (nU - 1) * nD, 0.0), temp2(N * (nU - 1));
+  double B[16];
+  for (Patch& p : R.patches) {
+    if (p.d.type != MGD_PATCH_BLOCK_INTERFACE || p.d.grid_index != bi + 1 || p.nPatchPoints <= 0) continue;
+    const Patch& q = R.patches[p.partner];
+    const Block& bq = R.blocks[q.d.grid_index - 1];
+    forPatchPoints(p, b, [&](long long gi, long long pi) {
+      if (b.iblank[gi] == 0) return;
+      const long long qgi = patchPointGridIndex(q, bq, p.partnerPoint[pi]);
+      double u[3], mL[3], mR[3], m2[3];
+      for (int d = 0; d < nD; ++d) {
+        u[d] = b.velocity[N * d + gi];
+        mL[d] = p.metricsL[p.nPatchPoints * d + pi];
+        mR[d] = p.metricsR[p.nPatchPoints * d + pi];
+      }
+      for (int l = 0; l < nD; ++l) {
+        for (int d = 0; d < nD; ++d) m2[d] = b.metrics[N * (nD * l + d) + gi];
+        for (int side = 0; side < 2; ++side) {
+          secondPartialViscousJacobian(nD, u, b.dynamicViscosity[gi], b.secondCoefficientOfViscosity[gi],
+                                       b.thermalDiffusivity[gi], b.jacobian[gi], side == 0 ? mL : mR, m2, B);
+          for (int r = 0; r < nU - 1; ++r) {
+            double s;
+            if (side == 0) {
+              s = B[0 + (nU - 1) * r] * b.adjointVariables[N * 1 + gi];
+              for (int k = 1; k < nU - 1; ++k) s += B[k + (nU - 1) * r] * b.adjointVariables[N * (k + 1) + gi];
+            } else {
+              s = B[0 + (nU - 1) * r] * bq.adjointVariables[bq.N * 1 + qgi];
+              for (int k = 1; k < nU - 1; ++k) s += B[k + (nU - 1) * r] * bq.adjointVariables[bq.N * (k + 1) + qgi];
+            }
+            double& t = temp1[N * (r + (nU - 1) * l) + gi];
+            t = side == 0 ? t - p.viscousPenaltyAmount * s : t + q.viscousPenaltyAmount * s;
+          }
         }
       }
     });
@@ -1310,6 +1552,101 @@ static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjoi
       });
       break;
     }
+    case MGD_PATCH_BLOCK_INTERFACE: {
+      // addBlockInterfacePenalty, src/BlockInterfacePatchImpl.f90:127-538 (discrete adjoint)
+      const Patch& q = R.patches[p.partner];
+      const Block& bq = R.blocks[q.d.grid_index - 1];
+      const int dirL = p.d.normal_direction, dirR = q.d.normal_direction;
+      const double sInvL = p.inviscidPenaltyAmount, sInvR = q.inviscidPenaltyAmount;
+      const double sVisL = p.viscousPenaltyAmount, sVisR = q.viscousPenaltyAmount;
+      forPatchPoints(p, b, [&](long long gi, long long pi) {
+        if (b.iblank[gi] == 0) return;
+        const long long qpi = p.partnerPoint[pi];
+        const long long qgi = patchPointGridIndex(q, bq, qpi);
+        double qL[5], qR[5], mL[3], mR[3], dq[5];
+        for (int c = 0; c < nU; ++c) {
+          qL[c] = b.conservedVariables[N * c + gi];
+          qR[c] = bq.conservedVariables[bq.N * c + qgi];
+          dq[c] = qL[c] - qR[c];
+        }
+        for (int d = 0; d < nD; ++d) {
+          mL[d] = p.metricsL[p.nPatchPoints * d + pi];
+          mR[d] = p.metricsR[p.nPatchPoints * d + pi];
+        }
+        const double jac = b.jacobian[gi];
+        if (mode == MGD_FORWARD) {
+          double roe[5], A[25];
+          roeAverage<double>(nD, qL, qR, g, roe);
+          incomingJacobianT<double>(nD, roe, mL, g, dirL, A);
+          for (int r = 0; r < nU; ++r) {
+            double s = A[r] * dq[0];
+            for (int c = 1; c < nU; ++c) s += A[r + nU * c] * dq[c];
+            b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] - sInvL * jac * s;
+          }
+          if (R.o.viscous) {
+            const double vL = std::copysign(std::abs(p.viscousPenaltyAmount), (double)dirL);
+            const double vR = std::copysign(std::abs(p.viscousPenaltyAmount), (double)dirR);
+            for (int r = 1; r < nU; ++r)
+              b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] +
+                  jac * (vL * p.ifViscousFlux[p.nPatchPoints * r + pi] + vR * q.ifViscousFlux[q.nPatchPoints * r + qpi]);
+          }
+          return;
+        }
+        double lamL[5], lamR[5];
+        for (int c = 0; c < nU; ++c) {
+          lamL[c] = b.adjointVariables[N * c + gi];
+          lamR[c] = bq.adjointVariables[bq.N * c + qgi];
+        }
+        // A+(Roe(qL, qR)) and its derivative with respect to qL, on dual numbers
+        Dual dL[5], dR[5], droe[5], AL[25], AR[25];
+        for (int c = 0; c < nU; ++c) {
+          dL[c] = Dual(qL[c]);
+          dL[c].d[c] = 1.0;
+          dR[c] = Dual(qR[c]);
+        }
+        roeAverage<Dual>(nD, dL, dR, g, droe);
+        incomingJacobianT<Dual>(nD, droe, mL, g, dirL, AL);
+        incomingJacobianT<Dual>(nD, droe, mR, g, dirR, AR);
+        double cv[5], u[3], tau[9], hf[3], B1[25];
+        if (R.o.viscous) {
+          for (int c = 0; c < nU; ++c) cv[c] = qL[c];
+          for (int d = 0; d < nD; ++d) u[d] = b.velocity[N * d + gi];
+          for (int c = 0; c < nD * nD; ++c) tau[c] = b.stressTensor[N * c + gi];
+          for (int d = 0; d < nD; ++d) hf[d] = b.heatFlux[N * d + gi];
+          (void)cv;
+        }
+        for (int side = 0; side < 2; ++side) {
+          const Dual* A = side == 0 ? AL : AR;
+          const double* lam = side == 0 ? lamL : lamR;
+          const double sInv = side == 0 ? sInvL : -sInvR;
+          for (int r = 0; r < nU; ++r) {
+            double s = A[0 + nU * r].v * lam[0];
+            for (int c = 1; c < nU; ++c) s += A[c + nU * r].v * lam[c];
+            b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] + sInv * jac * s;
+          }
+          for (int l = 0; l < nU; ++l) {
+            double s = 0.0;
+            for (int i2 = 0; i2 < nU; ++i2) {
+              double t = 0.0;
+              for (int j2 = 0; j2 < nU; ++j2) t += A[i2 + nU * j2].d[l] * dq[j2];
+              s += t * lam[i2];
+            }
+            b.rightHandSide[N * l + gi] = b.rightHandSide[N * l + gi] + sInv * jac * s;
+          }
+          if (R.o.viscous) {
+            firstPartialViscousJacobian(nD, side == 0 ? mL : mR, tau, hf, R.powerLawExponent, g,
+                                        b.specificVolume[gi], u, b.temperature[gi], B1);
+            const double sVis = side == 0 ? -sVisL : sVisR;
+            for (int r = 0; r < nU; ++r) {
+              double s = B1[0 + nU * r] * lam[0];
+              for (int c = 1; c < nU; ++c) s += B1[c + nU * r] * lam[c];
+              b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] + sVis * jac * s;
+            }
+          }
+        }
+      });
+      break;
+    }
     case MGD_PATCH_SLIP_WALL:
     case MGD_PATCH_ISOTHERMAL_WALL:
     case MGD_PATCH_ADIABATIC_WALL: {
@@ -1408,6 +1745,10 @@ static void computeRhs(Region& R, int mode, double time, double adjointForcingFa
     if (mode == MGD_FORWARD) computeRhsForward(R, R.blocks[bi], (int)bi);
     else computeRhsAdjoint(R, R.blocks[bi], (int)bi);
   }
+  // the interface data exchange is implicit: the interface penalties read the
+  // partner block's arrays directly (src/RegionImpl.f90:1923-1960)
+  if (mode == MGD_ADJOINT && R.o.viscous)
+    for (size_t bi = 0; bi < R.blocks.size(); ++bi) addInterfaceAdjointPenalty(R, R.blocks[bi], (int)bi);
   for (Block& b : R.blocks)
     for (int j = 0; j < R.nU; ++j)
       for (long long p = 0; p < b.N; ++p) b.rightHandSide[b.N * j + p] = b.rightHandSide[b.N * j + p] * b.jacobian[p];
