@@ -324,7 +324,7 @@ static int computeMetrics(Context& c, DevBlock& b) {
 int mgd_add_block(mgd_ctx* h, const mgd_block_desc* desc, const double* coordinates, const int* iblank) {
   Context& c = h->c;
   if (c.finalized) return fail(c, "mgd_add_block after mgd_finalize_setup");
-  if (!c.blocks.empty()) return fail(c, "only one block per context is supported");
+  if ((int)c.blocks.size() >= MGD_MAX_BLOCKS) return fail(c, "too many blocks");
   DevBlock b;
   b.desc = *desc;
   BlockView& v = b.v;
@@ -417,7 +417,7 @@ int mgd_add_block(mgd_ctx* h, const mgd_block_desc* desc, const double* coordina
 int mgd_add_patch(mgd_ctx* h, const mgd_patch_desc* p) {
   Context& c = h->c;
   if (c.finalized) return fail(c, "mgd_add_patch after mgd_finalize_setup");
-  if (p->type < MGD_PATCH_SAT_FAR_FIELD || p->type > MGD_PATCH_ADIABATIC_WALL)
+  if (p->type < MGD_PATCH_SAT_FAR_FIELD || p->type > MGD_PATCH_BLOCK_INTERFACE)
     return fail(c, std::string("unsupported patch type for patch '") + p->name + "'");
   if (p->grid_index < 1) return fail(c, "patch grid index must be >= 1");
   c.patches.push_back(*p);
@@ -626,24 +626,30 @@ int autotuneTile(Context& c, DevBlock& b, int kernel, const int (*cands)[3], int
 
 }  // namespace mgd
 
-int mgd_finalize_setup(mgd_ctx* h) {
-  Context& c = h->c;
-  if (c.finalized) return 0;
-  if (c.blocks.empty()) return fail(c, "no block");
-  DevBlock& b = c.blocks[0];
+// Patch setup of block bi (updatePatchFactories and the patch setup routines,
+// src/PatchFactoryImpl.f90:161-574): patches on other blocks are skipped.
+// mollifierTotals holds the control and target mollifier quadratures over all
+// blocks (normalizeControlMollifier / normalizeTargetMollifier,
+// src/RegionImpl.f90:459-603, sum over every block).
+static int finalizeBlock(Context& c, int bi, const double* mollifierTotals) {
+  DevBlock& b = c.blocks[bi];
   const int nD = c.nD, nU = c.nU;
   const long long N = b.v.N;
   const int* gs = b.v.gs;
   std::vector<int> exts;
   for (const mgd_patch_desc& p : c.patches) {
-    if (p.grid_index != 1) return fail(c, std::string("patch '") + p.name + "' refers to a missing block");
     int e[6];
+    if (p.grid_index != bi + 1) {
+      exts.insert(exts.end(), 6, 0);  // keeps exts aligned with c.patches
+      continue;
+    }
     resolveExtent(p, gs, nD, e);
     for (int i = 0; i < nD; ++i)
       if (e[2 * i] < 1 || e[2 * i + 1] > gs[i] || e[2 * i] > e[2 * i + 1])
         return fail(c, std::string("patch '") + p.name + "' has an invalid extent");
     const bool satType = p.type == MGD_PATCH_SAT_FAR_FIELD || p.type == MGD_PATCH_SLIP_WALL ||
-                         p.type == MGD_PATCH_ISOTHERMAL_WALL || p.type == MGD_PATCH_ADIABATIC_WALL;
+                         p.type == MGD_PATCH_ISOTHERMAL_WALL || p.type == MGD_PATCH_ADIABATIC_WALL ||
+                         p.type == MGD_PATCH_BLOCK_INTERFACE;
     if (satType || p.type == MGD_PATCH_SPONGE) {
       const int d = std::abs(p.normal_direction);
       if (d < 1 || d > nD) return fail(c, std::string("patch '") + p.name + "' has an invalid normal direction");
@@ -656,7 +662,7 @@ int mgd_finalize_setup(mgd_ctx* h) {
   std::vector<double> sponge(N, 0.0);
   for (size_t pi = 0; pi < c.patches.size(); ++pi) {
     const mgd_patch_desc& p = c.patches[pi];
-    if (p.type != MGD_PATCH_SPONGE) continue;
+    if (p.type != MGD_PATCH_SPONGE || p.grid_index != bi + 1) continue;
     const int* e = &exts[6 * pi];
     const int dir = std::abs(p.normal_direction) - 1;
     const long long st = b.v.ax[dir].stride;
@@ -700,7 +706,10 @@ int mgd_finalize_setup(mgd_ctx* h) {
   long long actOffset = 0;
   for (size_t pi = 0; pi < c.patches.size(); ++pi) {
     const mgd_patch_desc& p = c.patches[pi];
+    if (p.grid_index != bi + 1) continue;
     const int* e = &exts[6 * pi];
+    if (p.type == MGD_PATCH_ACTUATOR && bi > 0)
+      return fail(c, std::string("actuator patch '") + p.name + "' must lie in block 1");
     switch (p.type) {
       case MGD_PATCH_COST_TARGET:
         forExtent(e, gs, [&](long long gi, long long) {
@@ -793,11 +802,42 @@ int mgd_finalize_setup(mgd_ctx* h) {
         if (full) return fail(c, "more than three SAT patches meet at one point");
         break;
       }
+      case MGD_PATCH_BLOCK_INTERFACE: {
+        // setupBlockInterfacePatch, src/BlockInterfacePatchImpl.f90:3-88; the
+        // partner side is filled in by resolveInterfaces
+        const int dir = std::abs(p.normal_direction);
+        const double nb = d1.norm[0];
+        const double sInv = std::copysign(p.inviscid_penalty_amount, (double)p.normal_direction) / nb;
+        const double sVis = c.opts.viscous ? std::copysign(p.viscous_penalty_amount, (double)p.normal_direction) / nb : 0.0;
+        std::vector<int>& table = c.ifacePointEntry[pi];
+        table.assign((size_t)(e[1] - e[0] + 1) * (e[3] - e[2] + 1) * (e[5] - e[4] + 1), -1);
+        bool full = false;
+        forExtent(e, gs, [&](long long gi, long long k) {
+          if (b.hostIblank[gi] == 0) return;
+          int slot = 0;
+          while (slot < 3 && ffOf[3 * gi + slot] >= 0) ++slot;
+          if (slot == 3) { full = true; return; }
+          table[k] = (int)ffPoint.size();
+          ffOf[3 * gi + slot] = (int)ffPoint.size();
+          ffPoint.push_back((int)gi);
+          ffDir.push_back(dir);
+          ffSigned.push_back(p.normal_direction);
+          ffSigInv.push_back(0.0);
+          ffSigVRaw.push_back(0.0);
+          ffSigV.push_back(0.0);
+          ffKind.push_back(SAT_INTERFACE);
+          ffWallInv.push_back(sInv);   // the own inviscid penalty, kept unscaled
+          ffWallVisc.push_back(sVis);  // the own viscous penalty, kept unscaled
+          ffWallT.push_back(0.0);
+        });
+        if (full) return fail(c, "more than three SAT patches meet at one point");
+        break;
+      }
       default:
         break;
     }
   }
-  c.actuatorPoints = actOffset;
+  if (bi == 0) c.actuatorPoints = actOffset;
   std::vector<int> actPts((size_t)std::max(1LL, actOffset), 0);
   for (long long p = 0; p < N; ++p)
     if (actIdx[p] >= 0) actPts[actIdx[p]] = (int)p;
@@ -807,23 +847,19 @@ int mgd_finalize_setup(mgd_ctx* h) {
   std::vector<double> mcH(N), mtH(N);
   CUDA_TRY(c, cudaMemcpy(mcH.data(), b.v.mc, N * sizeof(double), cudaMemcpyDeviceToHost));
   CUDA_TRY(c, cudaMemcpy(mtH.data(), b.v.mt, N * sizeof(double), cudaMemcpyDeviceToHost));
-  if (c.opts.enable_controller) {
-    double s = 0.0;
-    for (long long p = 0; p < N; ++p) s += maskA[p] * b.hostNorm[p] * mcH[p];
-    for (long long p = 0; p < N; ++p) mcH[p] = mcH[p] / s;
-  }
-  if (c.opts.enable_functional) {
-    double s = 0.0;
-    for (long long p = 0; p < N; ++p) s += maskT[p] * b.hostNorm[p] * mtH[p];
-    for (long long p = 0; p < N; ++p) mtH[p] = mtH[p] / s;
-  }
+  if (c.opts.enable_controller && mollifierTotals[0] != 0.0)
+    for (long long p = 0; p < N; ++p) mcH[p] = mcH[p] / mollifierTotals[0];
+  if (c.opts.enable_functional && mollifierTotals[1] != 0.0)
+    for (long long p = 0; p < N; ++p) mtH[p] = mtH[p] / mollifierTotals[1];
   std::vector<double> wT(N), wA(N);
   for (long long p = 0; p < N; ++p) {
     wT[p] = maskT[p] * b.hostNorm[p];
     wA[p] = maskA[p] * b.hostNorm[p];
   }
-  c.actuatorWeights.assign((size_t)actOffset, 0.0);
-  for (long long k = 0; k < actOffset; ++k) c.actuatorWeights[k] = wA[actPts[k]];
+  if (bi == 0) {
+    c.actuatorWeights.assign((size_t)actOffset, 0.0);
+    for (long long k = 0; k < actOffset; ++k) c.actuatorWeights[k] = wA[actPts[k]];
+  }
   // acoustic source Gaussians exp(-9/(2 R^2) |x - x0|^2) (src/AcousticSourceImpl.f90:34-64)
   std::vector<double> srcG((size_t)N * std::max<size_t>(1, c.sources.size()), 0.0);
   for (size_t s = 0; s < c.sources.size(); ++s) {
@@ -886,6 +922,16 @@ int mgd_finalize_setup(mgd_ctx* h) {
     chk(devAlloc(b, &ff.wallInv, nFF));
     chk(devAlloc(b, &ff.wallVisc, nFF));
     chk(devAlloc(b, &ff.wallT, nFF));
+    chk(devAlloc(b, &ff.partnerBlock, nFF));
+    chk(devAlloc(b, &ff.partnerPoint, nFF));
+    chk(devAlloc(b, &ff.partnerEntry, nFF));
+    chk(devAlloc(b, &ff.dirL, nFF));
+    chk(devAlloc(b, &ff.dirR, nFF));
+    chk(devAlloc(b, &ff.metricsR, (size_t)nFF * nD));
+    chk(devAlloc(b, &ff.ifInv, (size_t)nFF * 2));
+    chk(devAlloc(b, &ff.ifVis, (size_t)nFF * 2));
+    chk(devAlloc(b, &ff.ifVisc, (size_t)nFF * nU));
+    chk(devAlloc(b, &ff.ifAd, (size_t)nFF * nD * (nU - 1)));
     double* dSig = nullptr;
     int* dSigned = nullptr;
     chk(devAlloc(b, &dSig, nFF));
@@ -893,11 +939,23 @@ int mgd_finalize_setup(mgd_ctx* h) {
     if (e != cudaSuccess) return fail(c, "device allocation failed for far-field entries");
     std::vector<double> jacH(N);
     CUDA_TRY(c, cudaMemcpy(jacH.data(), v.jac, N * sizeof(double), cudaMemcpyDeviceToHost));
+    b.nInterfaceEntries = 0;
+    b.hostIfaceInv.assign((size_t)nFF, 0.0);
+    b.hostIfaceVis.assign((size_t)nFF, 0.0);
     for (int k = 0; k < nFF; ++k) {
+      if (ffKind[k] == SAT_INTERFACE) {
+        ++b.nInterfaceEntries;
+        b.hostIfaceInv[k] = ffWallInv[k];
+        b.hostIfaceVis[k] = ffWallVisc[k];
+        ffWallInv[k] = ffWallVisc[k] = 0.0;
+        continue;
+      }
       ffSigV[k] = ffSigV[k] * jacH[ffPoint[k]];
       ffWallInv[k] = ffWallInv[k] * jacH[ffPoint[k]];
       ffWallVisc[k] = ffWallVisc[k] * jacH[ffPoint[k]];
     }
+    b.hostFfPoint = ffPoint;
+    b.hostFfSigned = ffSigned;
     CUDA_TRY(c, cudaMemcpy(ff.kind, ffKind.data(), nFF * sizeof(int), cudaMemcpyHostToDevice));
     CUDA_TRY(c, cudaMemcpy(ff.wallInv, ffWallInv.data(), nFF * sizeof(double), cudaMemcpyHostToDevice));
     CUDA_TRY(c, cudaMemcpy(ff.wallVisc, ffWallVisc.data(), nFF * sizeof(double), cudaMemcpyHostToDevice));
@@ -921,8 +979,177 @@ int mgd_finalize_setup(mgd_ctx* h) {
     if (checkLaunch(c)) return 1;
     CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   }
+  return 0;
+}
+
+// Point correspondence of an interface patch and its conforming patch
+// (readPatchInterfaceInformation, src/InterfaceHelperImpl.f90:3-113, and the
+// reordering of reshapeReceivedData, src/BlockInterfacePatchImpl.f90:785-931):
+// the partner patch-local index of each patch point, or an error.
+static int interfaceMap(Context& c, const int* ext, const int* extQ, const int reorder[3],
+                        std::vector<long long>& out) {
+  const long long g0 = ext[1] - ext[0] + 1, g1 = ext[3] - ext[2] + 1, g2 = ext[5] - ext[4] + 1;
+  const long long q0 = extQ[1] - extQ[0] + 1, q1 = extQ[3] - extQ[2] + 1, q2 = extQ[5] - extQ[4] + 1;
+  int o[3] = {reorder[0], reorder[1], reorder[2]};
+  if (o[2] != 3) return fail(c, "interface index reordering of the third index is not supported");
+  const bool transpose = std::abs(o[0]) == 2 && std::abs(o[1]) == 1;
+  if (transpose) std::swap(o[0], o[1]);
+  out.assign((size_t)(g0 * g1 * g2), 0);
+  for (long long k = 1; k <= g2; ++k)
+    for (long long j = 1; j <= g1; ++j)
+      for (long long i = 1; i <= g0; ++i) {
+        const long long fi = o[0] == -1 ? g0 + 1 - i : i;
+        const long long fj = o[1] == -2 ? g1 + 1 - j : j;
+        const long long a = transpose ? fj : fi, b = transpose ? fi : fj;
+        if (a < 1 || a > q0 || b < 1 || b > q1 || k > q2) return fail(c, "block interface patches do not conform");
+        out[(size_t)((i - 1) + g0 * ((j - 1) + g1 * (k - 1)))] = (a - 1) + q0 * ((b - 1) + q1 * (k - 1));
+      }
+  return 0;
+}
+
+// Partners of the block-interface entries of every block: conforming point,
+// its entry, the partner's normal metric row, penalties and normal direction
+// (the METRICS exchange of collectInterfaceData, src/BlockInterfacePatchImpl.f90:598-720).
+static int resolveInterfaces(Context& c) {
+  const int nP = (int)c.patches.size(), nD = c.nD;
+  std::vector<int> partner(nP, -1);
+  std::vector<std::array<int, 3>> reorder(nP, std::array<int, 3>{1, 2, 3});
+  for (int i = 0; i < nP; ++i) {
+    const mgd_patch_desc& p = c.patches[i];
+    if (p.type != MGD_PATCH_BLOCK_INTERFACE || p.conforms_with[0] == 0) continue;
+    for (int k = 0; k < nP; ++k)
+      if (std::strncmp(c.patches[k].name, p.conforms_with, MGD_NAME_LEN) == 0) partner[i] = k;
+    if (partner[i] < 0 || c.patches[partner[i]].type != MGD_PATCH_BLOCK_INTERFACE)
+      return fail(c, std::string("invalid interface specification for patch '") + p.name + "'");
+    for (int d = 0; d < 3; ++d) reorder[i][d] = p.interface_index[d] != 0 ? p.interface_index[d] : d + 1;
+  }
+  for (int i = 0; i < nP; ++i) {
+    if (partner[i] < 0) continue;
+    const int j = partner[i];
+    if (partner[j] < 0) {
+      partner[j] = i;
+      for (int l = 1; l <= 3; ++l)
+        for (int k = 1; k <= 3; ++k)
+          if (std::abs(reorder[i][k - 1]) == l) {
+            reorder[j][l - 1] = reorder[i][k - 1] < 0 ? -k : k;
+            break;
+          }
+    } else if (partner[j] != i) {
+      return fail(c, std::string("interface specification of patch '") + c.patches[j].name + "' violates commutativity");
+    }
+  }
+  // host metrics of every block
+  std::vector<std::vector<double>> metrics(c.blocks.size());
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+    const long long N = c.blocks[bi].v.N;
+    metrics[bi].resize((size_t)N * nD * nD);
+    CUDA_TRY(c, cudaMemcpy(metrics[bi].data(), c.blocks[bi].v.metrics, metrics[bi].size() * sizeof(double),
+                           cudaMemcpyDeviceToHost));
+  }
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+    DevBlock& b = c.blocks[bi];
+    const int nFF = b.v.ff.n;
+    if (b.nInterfaceEntries == 0) continue;
+    std::vector<int> pBlock(nFF, 0), pPoint(nFF, 0), pEntry(nFF, 0), dirL(nFF, 0), dirR(nFF, 0);
+    std::vector<double> mR((size_t)nFF * nD, 0.0), inv((size_t)nFF * 2, 0.0), vis((size_t)nFF * 2, 0.0);
+    for (int i = 0; i < nP; ++i) {
+      const mgd_patch_desc& p = c.patches[i];
+      if (p.type != MGD_PATCH_BLOCK_INTERFACE || p.grid_index != (int)bi + 1) continue;
+      if (partner[i] < 0) return fail(c, std::string("block interface patch '") + p.name + "' has no conforming patch");
+      const mgd_patch_desc& q = c.patches[partner[i]];
+      const int qb = q.grid_index - 1;
+      DevBlock& bq = c.blocks[qb];
+      int ext[6], extQ[6];
+      resolveExtent(p, b.v.gs, nD, ext);
+      resolveExtent(q, bq.v.gs, nD, extQ);
+      std::vector<long long> map;
+      if (interfaceMap(c, ext, extQ, reorder[i].data(), map)) return 1;
+      const std::vector<int>& mine = c.ifacePointEntry[i];
+      const std::vector<int>& theirs = c.ifacePointEntry[partner[i]];
+      const long long q0 = extQ[1] - extQ[0] + 1, q1 = extQ[3] - extQ[2] + 1;
+      const int qdir = std::abs(q.normal_direction);
+      for (size_t k = 0; k < mine.size(); ++k) {
+        const int e = mine[k];
+        if (e < 0) continue;
+        const long long qk = map[k];
+        const int qe = theirs[(size_t)qk];
+        if (qe < 0) return fail(c, std::string("block interface '") + p.name + "' meets a hole of its partner");
+        const long long qi = qk % q0, qj = (qk / q0) % q1, qkk = qk / (q0 * q1);
+        const long long qgi = (extQ[0] - 1 + qi) + (long long)bq.v.gs[0] * ((extQ[2] - 1 + qj) +
+                              (long long)bq.v.gs[1] * (extQ[4] - 1 + qkk));
+        pBlock[e] = qb;
+        pPoint[e] = (int)qgi;
+        pEntry[e] = qe;
+        dirL[e] = p.normal_direction;
+        dirR[e] = q.normal_direction;
+        for (int d = 0; d < nD; ++d)
+          mR[(size_t)e * nD + d] = metrics[qb][(size_t)bq.v.N * (nD * (qdir - 1) + d) + qgi];
+        inv[2 * e] = b.hostIfaceInv[e];
+        inv[2 * e + 1] = bq.hostIfaceInv[qe];
+        vis[2 * e] = b.hostIfaceVis[e];
+        vis[2 * e + 1] = bq.hostIfaceVis[qe];
+      }
+    }
+    FarFieldEntries& ff = b.v.ff;
+    CUDA_TRY(c, cudaMemcpy(ff.partnerBlock, pBlock.data(), nFF * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(ff.partnerPoint, pPoint.data(), nFF * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(ff.partnerEntry, pEntry.data(), nFF * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(ff.dirL, dirL.data(), nFF * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(ff.dirR, dirR.data(), nFF * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(ff.metricsR, mR.data(), mR.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(ff.ifInv, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(ff.ifVis, vis.data(), vis.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  c.hasInterfaces = false;
+  for (const DevBlock& b : c.blocks) c.hasInterfaces = c.hasInterfaces || b.nInterfaceEntries > 0;
+  return 0;
+}
+
+// Control and target mollifier quadratures over every block (the sums that
+// normalizeControlMollifier / normalizeTargetMollifier reduce,
+// src/RegionImpl.f90:459-603).
+static int mollifierTotals(Context& c, double* totals) {
+  totals[0] = totals[1] = 0.0;
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+    DevBlock& b = c.blocks[bi];
+    const long long N = b.v.N;
+    std::vector<double> maskA(N, 0.0), maskT(N, 0.0), mc(N), mt(N);
+    for (const mgd_patch_desc& p : c.patches) {
+      if (p.grid_index != (int)bi + 1) continue;
+      if (p.type != MGD_PATCH_ACTUATOR && p.type != MGD_PATCH_COST_TARGET) continue;
+      int e[6];
+      resolveExtent(p, b.v.gs, c.nD, e);
+      forExtent(e, b.v.gs, [&](long long gi, long long) {
+        (p.type == MGD_PATCH_ACTUATOR ? maskA : maskT)[gi] = 1.0;
+      });
+    }
+    CUDA_TRY(c, cudaMemcpy(mc.data(), b.v.mc, N * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(c, cudaMemcpy(mt.data(), b.v.mt, N * sizeof(double), cudaMemcpyDeviceToHost));
+    for (long long p = 0; p < N; ++p) {
+      if (b.hostIblank[p] == 0) continue;
+      totals[0] += maskA[p] * b.hostNorm[p] * mc[p];
+      totals[1] += maskT[p] * b.hostNorm[p] * mt[p];
+    }
+  }
+  return 0;
+}
+
+int mgd_finalize_setup(mgd_ctx* h) {
+  Context& c = h->c;
+  if (c.finalized) return 0;
+  if (c.blocks.empty()) return fail(c, "no block");
+  for (const mgd_patch_desc& p : c.patches)
+    if (p.grid_index < 1 || p.grid_index > (int)c.blocks.size())
+      return fail(c, std::string("patch '") + p.name + "' refers to a missing block");
+  c.ifacePointEntry.assign(c.patches.size(), std::vector<int>());
+  double totals[2];
+  if (mollifierTotals(c, totals)) return 1;
+  for (int bi = 0; bi < (int)c.blocks.size(); ++bi)
+    if (finalizeBlock(c, bi, totals)) return 1;
+  if (resolveInterfaces(c)) return 1;
   c.finalized = true;
-  if (autotune(c, b)) return 1;
+  for (DevBlock& b : c.blocks)
+    if (autotune(c, b)) return 1;
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   return 0;
 }
@@ -998,14 +1225,59 @@ void adjointStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, in
   launchAdjointAssemble(c, b, rkStage, rs, stage, apiFactor, api, fromSlot, L.main);
 }
 
+// Arrays of every block for the interface kernels.
+static BlockRefs blockRefs(Context& c) {
+  BlockRefs r{};
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+    r.q[bi] = c.blocks[bi].v.q;
+    r.lam[bi] = c.blocks[bi].v.lam;
+    r.ifVisc[bi] = c.blocks[bi].v.ff.ifVisc;
+    r.N[bi] = c.blocks[bi].v.N;
+  }
+  return r;
+}
+
+// The forward RHS (rkStage 0) or one forward RK stage of every block of a
+// multi-block region: all blocks' fluxes first, then the block-interface SATs
+// (which read the partner blocks), then the divergence and update of each block.
+void regionForwardStage(Context& c, int rkStage, const RunScalars& rs) {
+  const BlockRefs refs = blockRefs(c);
+  for (DevBlock& b : c.blocks) {
+    launchDissipation(c, b, b.v.q, 1.0);
+    launchGradFlux(c, b, true, false, &rs, 1, false);
+  }
+  for (DevBlock& b : c.blocks) launchInterfaceSat(c, b, refs);
+  for (DevBlock& b : c.blocks) {
+    launchForwardDivergence(c, b, rkStage, rs, true, false);
+    if (rkStage > 0) launchPrims(c, b, b.v.q, false);
+  }
+}
+
+// The adjoint RHS or one adjoint RK stage of every block (primitives and
+// stress of the forward state are current): interface SATs of every block
+// first, which also read the partner blocks' lambda before any update.
+void regionAdjointStage(Context& c, int rkStage, const RunScalars& rs, double apiFactor) {
+  const BlockRefs refs = blockRefs(c);
+  for (DevBlock& b : c.blocks) launchInterfaceSatAdjoint(c, b, refs);
+  for (DevBlock& b : c.blocks) {
+    launchDissipation(c, b, b.v.lam, -1.0);
+    launchAdjointCore(c, b, rs, 1, false);
+    launchAdjointDiffusion(c, b);
+  }
+  for (DevBlock& b : c.blocks) launchAdjointAssemble(c, b, rkStage, rs, 1, apiFactor, true, false);
+}
+
 }  // namespace mgd
+
+static bool singleBlock(const Context& c) { return c.blocks.size() == 1 && !c.hasInterfaces; }
 
 int mgd_update_state(mgd_ctx* h) {
   Context& c = h->c;
   if (requireReady(c)) return 1;
-  DevBlock& b = c.blocks[0];
-  launchPrims(c, b, b.v.q, false);
-  if (c.phys.viscous) launchGradFlux(c, b, false, true, nullptr, 0, false);
+  for (DevBlock& b : c.blocks) {
+    launchPrims(c, b, b.v.q, false);
+    if (c.phys.viscous) launchGradFlux(c, b, false, true, nullptr, 0, false);
+  }
   if (checkLaunch(c)) return 1;
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   return 0;
@@ -1018,12 +1290,16 @@ int mgd_compute_rhs(mgd_ctx* h, int mode, double time, double adjoint_forcing_fa
   RunScalars rs = apiScalars(c);
   if (mode == MGD_FORWARD) {
     if (setApiTime(c, time)) return 1;
-    launchPrims(c, b, b.v.q, false);
-    forwardStage(c, b, 0, rs, true, false, false, false);
+    for (DevBlock& x : c.blocks) launchPrims(c, x, x.v.q, false);
+    if (singleBlock(c)) forwardStage(c, b, 0, rs, true, false, false, false);
+    else regionForwardStage(c, 0, rs);
   } else if (mode == MGD_ADJOINT) {
-    launchPrims(c, b, b.v.q, false);
-    if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs, 1, false);
-    adjointStage(c, b, 0, rs, 1, adjoint_forcing_factor, true, false, false);
+    for (DevBlock& x : c.blocks) {
+      launchPrims(c, x, x.v.q, false);
+      if (c.phys.viscous) launchGradFlux(c, x, false, true, &rs, 1, false);
+    }
+    if (singleBlock(c)) adjointStage(c, b, 0, rs, 1, adjoint_forcing_factor, true, false, false);
+    else regionAdjointStage(c, 0, rs, adjoint_forcing_factor);
   } else {
     return fail(c, "mode must be MGD_FORWARD or MGD_ADJOINT");
   }
@@ -1037,9 +1313,10 @@ int mgd_update_adjoint_forcing(mgd_ctx* h, int no_adjoint_forcing) {
   // the per-call RHS (inside runs it is evaluated in the adjoint kernel).
   Context& c = h->c;
   if (requireReady(c)) return 1;
-  DevBlock& b = c.blocks[0];
-  launchPrims(c, b, b.v.q, false);
-  launchStoreAdjointForcing(c, b, no_adjoint_forcing != 0);
+  for (DevBlock& b : c.blocks) {
+    launchPrims(c, b, b.v.q, false);
+    launchStoreAdjointForcing(c, b, no_adjoint_forcing != 0);
+  }
   if (checkLaunch(c)) return 1;
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   return 0;
@@ -1073,17 +1350,19 @@ static int ensurePartials(Context& c, long long nSlots) {
 int mgd_compute_functional(mgd_ctx* h, double* value) {
   Context& c = h->c;
   if (requireReady(c)) return 1;
-  DevBlock& b = c.blocks[0];
-  const long long N = b.v.N;
-  std::vector<double> w(N), mt(N), mp(N), pr(N);
-  CUDA_TRY(c, cudaMemcpy(w.data(), b.v.wT, N * sizeof(double), cudaMemcpyDeviceToHost));
-  CUDA_TRY(c, cudaMemcpy(mt.data(), b.v.mt, N * sizeof(double), cudaMemcpyDeviceToHost));
-  CUDA_TRY(c, cudaMemcpy(mp.data(), b.v.meanP, N * sizeof(double), cudaMemcpyDeviceToHost));
-  CUDA_TRY(c, cudaMemcpy(pr.data(), b.v.prim + N * PrimLayout{c.nD}.p(), N * sizeof(double), cudaMemcpyDeviceToHost));
   double s = 0.0;
-  for (long long p = 0; p < N; ++p) {
-    const double F = pr[p] - mp[p];
-    s += w[p] * (F * F * mt[p]);
+  for (DevBlock& b : c.blocks) {
+    const long long N = b.v.N;
+    std::vector<double> w(N), mt(N), mp(N), pr(N);
+    CUDA_TRY(c, cudaMemcpy(w.data(), b.v.wT, N * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(c, cudaMemcpy(mt.data(), b.v.mt, N * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(c, cudaMemcpy(mp.data(), b.v.meanP, N * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(c, cudaMemcpy(pr.data(), b.v.prim + N * PrimLayout{c.nD}.p(), N * sizeof(double),
+                           cudaMemcpyDeviceToHost));
+    for (long long p = 0; p < N; ++p) {
+      const double F = pr[p] - mp[p];
+      s += w[p] * (F * F * mt[p]);
+    }
   }
   *value = s;
   return 0;
@@ -1117,13 +1396,17 @@ int mgd_rk4_substep(mgd_ctx* h, int mode, double* time, double dt, int stage) {
   if (mode == MGD_FORWARD) {
     if (stage == 2 || stage == 4) *time = *time + dt / 2.0;
     if (setApiTime(c, *time)) return 1;
-    launchPrims(c, b, b.v.q, false);
-    forwardStage(c, b, stage, rs, true, false, false, false);
+    for (DevBlock& x : c.blocks) launchPrims(c, x, x.v.q, false);
+    if (singleBlock(c)) forwardStage(c, b, stage, rs, true, false, false, false);
+    else regionForwardStage(c, stage, rs);
   } else if (mode == MGD_ADJOINT) {
     const double factor = stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0);
-    launchPrims(c, b, b.v.q, false);
-    if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs, 1, false);
-    adjointStage(c, b, stage, rs, 1, factor, true, false, false);
+    for (DevBlock& x : c.blocks) {
+      launchPrims(c, x, x.v.q, false);
+      if (c.phys.viscous) launchGradFlux(c, x, false, true, &rs, 1, false);
+    }
+    if (singleBlock(c)) adjointStage(c, b, stage, rs, 1, factor, true, false, false);
+    else regionAdjointStage(c, stage, rs, factor);
     if (stage == 3 || stage == 1) *time = *time - dt / 2.0;
   } else {
     return fail(c, "mode must be MGD_FORWARD or MGD_ADJOINT");
@@ -1425,6 +1708,7 @@ RunScalars runScalarsOf(Context& c) { return runScalars(c); }
 int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, double* cost) {
   Context& c = h->c;
   if (requireReady(c)) return 1;
+  if (!singleBlock(c)) return fail(c, "checkpointed runs support one block without block interfaces");
   if (n_steps < 1) return fail(c, "n_steps must be >= 1");
   if (save_interval < 1) save_interval = n_steps;
   DevBlock& b = c.blocks[0];
@@ -1450,6 +1734,7 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
 int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   Context& c = h->c;
   if (requireReady(c)) return 1;
+  if (!singleBlock(c)) return fail(c, "checkpointed runs support one block without block interfaces");
   if (c.runSteps < 1) return fail(c, "mgd_run_adjoint needs a preceding mgd_run_forward");
   DevBlock& b = c.blocks[0];
   const long long N = b.v.N;

@@ -175,26 +175,113 @@ __device__ __forceinline__ double fastPowPositive(double x, double n, const PowT
 // Incoming Jacobian A+ of the inviscid flux along `metrics` for a state of
 // conserved variables cv (computeIncomingJacobianOfInviscidFlux{2D,3D},
 // src/CNSHelperImpl.f90:1669-2343). out(i,j) at out[i + nU*j].
-template <int ND>
-__host__ __device__ inline void incomingJacobian(const double* cv, const double* metrics, double g,
-                                                 int incomingDirection, double* out) {
+// Forward-mode dual number with K directional derivatives. Evaluating the
+// incoming Jacobian of a Roe-averaged state on duals seeded with the left
+// state gives its exact variation with respect to that state, which the
+// block-interface adjoint needs (src/CNSHelperImpl.f90:1669-2343 with
+// deltaRoeAverage, src/BlockInterfacePatchImpl.f90:337-420).
+template <int K>
+struct DualN {
+  double v;
+  double d[K];
+  __host__ __device__ DualN() : v(0.0) {
+    for (int k = 0; k < K; ++k) d[k] = 0.0;
+  }
+  __host__ __device__ DualN(double x) : v(x) {
+    for (int k = 0; k < K; ++k) d[k] = 0.0;
+  }
+};
+__host__ __device__ inline double valueOf(double x) { return x; }
+template <int K> __host__ __device__ inline double valueOf(const DualN<K>& x) { return x.v; }
+template <int K> __host__ __device__ inline DualN<K> operator+(const DualN<K>& a, const DualN<K>& b) {
+  DualN<K> r(a.v + b.v);
+  for (int k = 0; k < K; ++k) r.d[k] = a.d[k] + b.d[k];
+  return r;
+}
+template <int K> __host__ __device__ inline DualN<K> operator-(const DualN<K>& a, const DualN<K>& b) {
+  DualN<K> r(a.v - b.v);
+  for (int k = 0; k < K; ++k) r.d[k] = a.d[k] - b.d[k];
+  return r;
+}
+template <int K> __host__ __device__ inline DualN<K> operator-(const DualN<K>& a) {
+  DualN<K> r(-a.v);
+  for (int k = 0; k < K; ++k) r.d[k] = -a.d[k];
+  return r;
+}
+template <int K> __host__ __device__ inline DualN<K> operator*(const DualN<K>& a, const DualN<K>& b) {
+  DualN<K> r(a.v * b.v);
+  for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+  return r;
+}
+template <int K> __host__ __device__ inline DualN<K> operator/(const DualN<K>& a, const DualN<K>& b) {
+  DualN<K> r(a.v / b.v);
+  for (int k = 0; k < K; ++k) r.d[k] = (a.d[k] * b.v - a.v * b.d[k]) / (b.v * b.v);
+  return r;
+}
+template <int K> __host__ __device__ inline DualN<K> operator+(const DualN<K>& a, double b) { return a + DualN<K>(b); }
+template <int K> __host__ __device__ inline DualN<K> operator+(double a, const DualN<K>& b) { return DualN<K>(a) + b; }
+template <int K> __host__ __device__ inline DualN<K> operator-(const DualN<K>& a, double b) { return a - DualN<K>(b); }
+template <int K> __host__ __device__ inline DualN<K> operator-(double a, const DualN<K>& b) { return DualN<K>(a) - b; }
+template <int K> __host__ __device__ inline DualN<K> operator*(const DualN<K>& a, double b) {
+  DualN<K> r(a.v * b);
+  for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * b;
+  return r;
+}
+template <int K> __host__ __device__ inline DualN<K> operator*(double a, const DualN<K>& b) { return b * a; }
+template <int K> __host__ __device__ inline DualN<K> operator/(const DualN<K>& a, double b) { return a / DualN<K>(b); }
+template <int K> __host__ __device__ inline DualN<K> operator/(double a, const DualN<K>& b) { return DualN<K>(a) / b; }
+template <int K> __host__ __device__ inline DualN<K>& operator+=(DualN<K>& a, const DualN<K>& b) {
+  a = a + b;
+  return a;
+}
+__host__ __device__ inline double sqrtOf(double x) { return sqrt(x); }
+template <int K> __host__ __device__ inline DualN<K> sqrtOf(const DualN<K>& a) {
+  DualN<K> r(::sqrt(a.v));
+  for (int k = 0; k < K; ++k) r.d[k] = a.d[k] / (2.0 * r.v);
+  return r;
+}
+
+// Roe average of two conserved states (computeRoeAverage,
+// src/CNSHelperImpl.f90:179-351, without the variations).
+template <int ND, class S>
+__host__ __device__ inline void roeAverage(const S* qL, const S* qR, double g, S* roe) {
+  const S sL = sqrtOf(qL[0]), sR = sqrtOf(qR[0]);
+  const S vL = 1.0 / qL[0], vR = 1.0 / qR[0];
+  S mL2 = qL[1] * qL[1], mR2 = qR[1] * qR[1];
+  for (int d = 1; d < ND; ++d) {
+    mL2 = mL2 + qL[1 + d] * qL[1 + d];
+    mR2 = mR2 + qR[1 + d] * qR[1 + d];
+  }
+  const S hL = g * qL[ND + 1] - 0.5 * (g - 1.0) * vL * mL2;
+  const S hR = g * qR[ND + 1] - 0.5 * (g - 1.0) * vR * mR2;
+  roe[0] = sL * sR;
+  for (int d = 0; d < ND; ++d) roe[1 + d] = (sR * qL[1 + d] + sL * qR[1 + d]) / (sL + sR);
+  roe[ND + 1] = (sR * hL + sL * hR) / (sL + sR);
+  S m2 = roe[1] * roe[1];
+  for (int d = 1; d < ND; ++d) m2 = m2 + roe[1 + d] * roe[1 + d];
+  roe[ND + 1] = (roe[ND + 1] + 0.5 * (g - 1.0) / roe[0] * m2) / g;
+}
+
+template <int ND, class S = double>
+__host__ __device__ inline void incomingJacobian(const S* cv, const double* metrics, double g,
+                                                 int incomingDirection, S* out) {
   constexpr int nU = ND + 2;
   double arc = 0.0;
   for (int d = 0; d < ND; ++d) arc += metrics[d] * metrics[d];
   arc = sqrt(arc);
   double nm[3];
   for (int d = 0; d < ND; ++d) nm[d] = metrics[d] / arc;
-  const double v = 1.0 / cv[0];
-  double u[3], u2 = 0.0;
+  const S v = 1.0 / cv[0];
+  S u[3], u2 = 0.0;
   for (int d = 0; d < ND; ++d) u[d] = v * cv[d + 1];
   for (int d = 0; d < ND; ++d) u2 += u[d] * u[d];
-  const double T = g * (v * cv[ND + 1] - 0.5 * u2);
-  double U = 0.0;
+  const S T = g * (v * cv[ND + 1] - 0.5 * u2);
+  S U = 0.0;
   for (int d = 0; d < ND; ++d) U += nm[d] * u[d];
-  const double c = sqrt((g - 1.0) * T);
-  const double phi2 = 0.5 * (g - 1.0) * u2;
-  const double rho = cv[0];
-  double R[nU][nU], L[nU][nU], lam[nU];
+  const S c = sqrtOf((g - 1.0) * T);
+  const S phi2 = 0.5 * (g - 1.0) * u2;
+  const S rho = cv[0];
+  S R[nU][nU], L[nU][nU], lam[nU];
   if constexpr (ND == 2) {
     lam[0] = U; lam[1] = U; lam[2] = U + c; lam[3] = U - c;
     R[0][0] = 1.0; R[1][0] = u[0]; R[2][0] = u[1]; R[3][0] = phi2 / (g - 1.0);
@@ -215,9 +302,9 @@ __host__ __device__ inline void incomingJacobian(const double* cv, const double*
     L[0][3] = -1.0 / T; L[1][3] = 0.0; L[2][3] = 0.5 / T; L[3][3] = 0.5 / T;
   } else {
     lam[0] = U; lam[1] = U; lam[2] = U; lam[3] = U + c; lam[4] = U - c;
-    const double h0 = phi2 / (g - 1.0);
-    const double q = 1.0 - phi2 / (c * c);
-    double (*r)[nU] = R;
+    const S h0 = phi2 / (g - 1.0);
+    const S q = 1.0 - phi2 / (c * c);
+    S (*r)[nU] = R;
     r[0][0] = nm[0]; r[1][0] = nm[0] * u[0]; r[2][0] = nm[0] * u[1] + rho * nm[2];
     r[3][0] = nm[0] * u[2] - rho * nm[1];
     r[4][0] = rho * (nm[2] * u[1] - nm[1] * u[2]) + h0 * nm[0];
@@ -231,7 +318,7 @@ __host__ __device__ inline void incomingJacobian(const double* cv, const double*
     r[3][3] = u[2] + nm[2] * c; r[4][3] = T + h0 + c * U;
     r[0][4] = 1.0; r[1][4] = u[0] - nm[0] * c; r[2][4] = u[1] - nm[1] * c;
     r[3][4] = u[2] - nm[2] * c; r[4][4] = T + h0 - c * U;
-    double (*l)[nU] = L;
+    S (*l)[nU] = L;
     l[0][0] = nm[0] * q - v * (nm[2] * u[1] - nm[1] * u[2]);
     l[1][0] = nm[1] * q - v * (nm[0] * u[2] - nm[2] * u[0]);
     l[2][0] = nm[2] * q - v * (nm[1] * u[0] - nm[0] * u[1]);
@@ -251,11 +338,11 @@ __host__ __device__ inline void incomingJacobian(const double* cv, const double*
   }
   for (int k = 0; k < nU; ++k) {
     lam[k] = arc * lam[k];
-    if (incomingDirection * lam[k] < 0.0) lam[k] = 0.0;
+    if (incomingDirection * valueOf(lam[k]) < 0.0) lam[k] = 0.0;
   }
   for (int j = 0; j < nU; ++j)
     for (int i = 0; i < nU; ++i) {
-      double s = R[i][0] * lam[0] * L[0][j];
+      S s = R[i][0] * lam[0] * L[0][j];
       for (int k = 1; k < nU; ++k) s += R[i][k] * lam[k] * L[k][j];
       out[i + nU * j] = s;
     }

@@ -27,7 +27,7 @@ struct PrimLayout {
 };
 
 // Boundary SAT entry: one (far-field or wall patch, point) pair.
-enum { SAT_FAR_FIELD = 0, SAT_WALL = 1, SAT_ISOTHERMAL_WALL = 2 };
+enum { SAT_FAR_FIELD = 0, SAT_WALL = 1, SAT_ISOTHERMAL_WALL = 2, SAT_INTERFACE = 3 };
 struct FarFieldEntries {
   int n = 0;
   int* point = nullptr;      // grid point
@@ -36,6 +36,17 @@ struct FarFieldEntries {
   double* wallInv = nullptr;   // walls: signed inviscid penalty / H0 * jacobian
   double* wallVisc = nullptr;  // isothermal walls: viscous penalty / H0 / Re * jacobian (0 if inviscid)
   double* wallT = nullptr;     // isothermal walls: wall temperature
+  // block interfaces (kind SAT_INTERFACE)
+  int* partnerBlock = nullptr;   // 0-based block of the conforming point
+  int* partnerPoint = nullptr;   // its grid point
+  int* partnerEntry = nullptr;   // its SAT entry
+  int* dirL = nullptr;           // signed normal direction of this side
+  int* dirR = nullptr;           // and of the partner
+  double* metricsR = nullptr;    // nD: the partner's normal metric row
+  double* ifInv = nullptr;       // 2: inviscid penalty of this side and of the partner (signed, / H0)
+  double* ifVis = nullptr;       // 2: viscous penalty of this side and of the partner (signed, / H0)
+  double* ifVisc = nullptr;      // nU: sum_j F_v(:, j) m_L,j of this side (component 0 zero)
+  double* ifAd = nullptr;        // nD x (nU-1): interface terms of the adjoint viscous diffusion
   double* M = nullptr;       // nU*nU: inviscidPenaltyAmount * jacobian * A+(target), column-major
   double* sigV = nullptr;    // viscousPenaltyAmount * jacobian
   double* sigVRaw = nullptr; // viscousPenaltyAmount
@@ -88,6 +99,15 @@ struct BlockView {
   const int* actPts;      // grid point of each actuator-patch point, patch order
   int nAct;
   FarFieldEntries ff;
+};
+
+// Arrays of every block of a context that the block-interface kernels read
+// across blocks.
+struct BlockRefs {
+  const double* q[MGD_MAX_BLOCKS];
+  const double* lam[MGD_MAX_BLOCKS];
+  const double* ifVisc[MGD_MAX_BLOCKS];
+  long long N[MGD_MAX_BLOCKS];
 };
 
 // Thread-block tiling of a block's points: blocks of t[0] x t[1] x t[2]
@@ -149,6 +169,9 @@ struct DevBlock {
   Tile tGrad{}, tDiss{}, tRhs{}, tAdjA{}, tAdjD{}, tAdjB{};
   std::vector<void*> allocations;
   int nStagePartialBlocks = 0;
+  int nInterfaceEntries = 0;
+  std::vector<double> hostIfaceInv, hostIfaceVis;  // own interface penalties per SAT entry
+  std::vector<int> hostFfPoint, hostFfSigned;
   // host copies kept for setup
   std::vector<double> hostCoords;
   std::vector<int> hostIblank;
@@ -181,6 +204,8 @@ struct Context {
   std::vector<mgd_patch_desc> patches;
   std::vector<mgd_acoustic_source> sources;
   bool finalized = false;
+  bool hasInterfaces = false;
+  std::vector<std::vector<int>> ifacePointEntry;  // per patch: SAT entry of each interface patch point
   long long launches = 0;
   long long actuatorPoints = 0;
   // device scalars: [0] step, [1] segBase, [2] api step (always 1), [3] api segBase,
@@ -301,6 +326,10 @@ void launchReducePartials(Context& c, const double* partials, int stride, int co
 void launchTimeStep(Context& c, DevBlock& b, double* partials, double* dtOut, const int* step, double* time,
                     double* amp, cudaStream_t s = 0);
 int timeStepBlocks(const DevBlock& b);
+// Block-interface SAT vectors of block b's interface entries (forward; adjoint
+// with the interface terms of the adjoint viscous diffusion).
+void launchInterfaceSat(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_t s = 0);
+void launchInterfaceSatAdjoint(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_t s = 0);
 // Terminal kinetic energy of the current state into out[0] (norm = H det per point).
 void launchKineticEnergy(Context& c, DevBlock& b, const double* norm, double* partials, double* out);
 void launchKineticEnergyAdjointInitial(Context& c, DevBlock& b);

@@ -362,6 +362,22 @@ __device__ __forceinline__ void gradFluxPoint(const BlockView& B, const Physics&
     for (int s = 0; s < 3; ++s) {
       const int e = B.ffOfPoint[3 * p + s];
       if (e < 0) continue;
+      if (B.ff.kind[e] == SAT_INTERFACE) {
+        // viscousFluxesL = sum_j F_v(:, j) m_L,j (src/BlockInterfacePatchImpl.f90:645-653);
+        // the SAT vector itself needs the partner block (kInterfaceSat)
+        if (VISC) {
+          double mn[ND];
+          for (int d = 0; d < ND; ++d) mn[d] = B.metrics[p + N * (ND * (B.ff.normalDir[e] - 1) + d)];
+          double* out = B.ff.ifVisc + (long long)e * nU;
+          out[0] = 0.0;
+          for (int r = 1; r < nU; ++r) {
+            double f = Fv[r][0] * mn[0];
+            for (int d = 1; d < ND; ++d) f += Fv[r][d] * mn[d];
+            out[r] = f;
+          }
+        }
+        continue;
+      }
       if (B.ff.kind[e] != SAT_FAR_FIELD) {
         wallSatForward<ND, VISC>(B, P, e, p, q, u, B.ff.visc + (long long)e * nU);
         continue;
@@ -643,12 +659,20 @@ __device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physi
         for (int c = 0; c < nV; ++c) ad[l][c] += sv * t[c];
       }
     }
+    for (int k = 0; k < 3; ++k) {
+      const int e = B.ffOfPoint[3 * p + k];
+      if (e < 0 || B.ff.kind[e] != SAT_INTERFACE) continue;
+      const double* a = B.ff.ifAd + (long long)e * ND * nV;
+      for (int l = 0; l < ND; ++l)
+        for (int c = 0; c < nV; ++c) ad[l][c] += a[l * nV + c];
+    }
     for (int j = 0; j < ND; ++j)
       for (int c = 0; c < nV; ++c) B.ad[p + N * (j * nV + c)] = ad[j][c];
   }
   for (int k = 0; k < 3; ++k) {
     const int e = B.ffOfPoint[3 * p + k];
     if (e < 0) continue;
+    if (B.ff.kind[e] == SAT_INTERFACE) continue;  // kInterfaceSatAdjoint
     if (B.ff.kind[e] != SAT_FAR_FIELD) {
       wallSatAdjoint<ND, VISC>(B, P, e, p, u, Tm, v, lp, B.ff.visc + (long long)e * nU);
       continue;
@@ -918,6 +942,136 @@ __global__ void kReducePartials(const double* __restrict__ partials, int stride,
   for (int b = threadIdx.x; b < count; b += blockDim.x) v += partials[(long long)s * stride + b];
   const double t = blockSum(v);
   if (threadIdx.x == 0) out[s] = t;
+}
+
+// ---------------------------------------------------------------------------
+// Block-interface SATs (addBlockInterfacePenalty, src/BlockInterfacePatchImpl.f90:
+// 127-538, discrete adjoint), one thread per interface entry. Forward:
+//   sat = -s_inv,L J A+(Roe(qL, qR), m_L, dirL) (qL - qR)
+//         + J (s_v,L F_vL + s_v,R F_vR) on momentum and energy,
+// with s_v,L/R = |s_v| signed by the normal direction of each side. Adjoint:
+//   sat = s_inv,L J [A_L^T lamL + (dA_L/dqL (qL - qR))^T lamL] - s_v,L J B1(m_L)^T lamL
+//       - s_inv,R J [A_R^T lamR + (dA_R/dqL (qL - qR))^T lamR] + s_v,R J B1(m_R)^T lamR,
+// where A_R uses the partner's normal metric and direction and dA/dqL comes
+// from evaluating A+(Roe(qL, qR)) on dual numbers seeded with qL. The adjoint
+// kernel also stores the interface terms of the adjoint viscous diffusion
+// (addInterfaceAdjointPenalty, src/RhsHelperImpl.f90:831-1026) for kAdjointCore.
+// ---------------------------------------------------------------------------
+template <int ND, bool VISC>
+__global__ void __launch_bounds__(kBlock) kInterfaceSat(BlockView B, Physics P, BlockRefs R) {
+  const int e = blockIdx.x * kBlock + threadIdx.x;
+  if (e >= B.ff.n || B.ff.kind[e] != SAT_INTERFACE) return;
+  constexpr int nU = ND + 2;
+  const long long N = B.N, p = B.ff.point[e];
+  const int pb = B.ff.partnerBlock[e];
+  const long long pp = B.ff.partnerPoint[e], NR = R.N[pb];
+  double qL[nU], qR[nU], dq[nU], mL[ND], roe[nU], A[nU * nU];
+  for (int c = 0; c < nU; ++c) {
+    qL[c] = B.q[p + N * c];
+    qR[c] = R.q[pb][pp + NR * c];
+    dq[c] = qL[c] - qR[c];
+  }
+  for (int d = 0; d < ND; ++d) mL[d] = B.metrics[p + N * (ND * (B.ff.normalDir[e] - 1) + d)];
+  roeAverage<ND, double>(qL, qR, P.g, roe);
+  incomingJacobian<ND, double>(roe, mL, P.g, B.ff.dirL[e], A);
+  const double jac = B.jac[p];
+  const double s = B.ff.ifInv[2 * e];
+  double* sat = B.ff.visc + (long long)e * nU;
+  double vL = 0.0, vR = 0.0;
+  if (VISC) {
+    const double a = fabs(B.ff.ifVis[2 * e]);
+    vL = B.ff.dirL[e] < 0 ? -a : a;
+    vR = B.ff.dirR[e] < 0 ? -a : a;
+  }
+  const double* fL = B.ff.ifVisc + (long long)e * nU;
+  const double* fR = R.ifVisc[pb] + (long long)B.ff.partnerEntry[e] * nU;
+  for (int r = 0; r < nU; ++r) {
+    double t = A[r] * dq[0];
+    for (int c = 1; c < nU; ++c) t += A[r + nU * c] * dq[c];
+    double v = -(s * jac * t);
+    if (VISC && r > 0) v += jac * (vL * fL[r] + vR * fR[r]);
+    sat[r] = v;
+  }
+}
+
+template <int ND, bool VISC>
+__global__ void __launch_bounds__(kBlock) kInterfaceSatAdjoint(BlockView B, Physics P, BlockRefs R) {
+  const int e = blockIdx.x * kBlock + threadIdx.x;
+  if (e >= B.ff.n || B.ff.kind[e] != SAT_INTERFACE) return;
+  constexpr int nU = ND + 2, nV = ND + 1;
+  using D = DualN<nU>;
+  const long long N = B.N, p = B.ff.point[e];
+  const int pb = B.ff.partnerBlock[e];
+  const long long pp = B.ff.partnerPoint[e], NR = R.N[pb];
+  const PrimLayout L{ND};
+  double qL[nU], dq[nU], lamL[nU], lamR[nU], mL[ND], mR[ND];
+  D dL[nU], dR[nU], roe[nU];
+  for (int c = 0; c < nU; ++c) {
+    qL[c] = B.q[p + N * c];
+    const double qr = R.q[pb][pp + NR * c];
+    dq[c] = qL[c] - qr;
+    dL[c] = D(qL[c]);
+    dL[c].d[c] = 1.0;
+    dR[c] = D(qr);
+    lamL[c] = B.lam[p + N * c];
+    lamR[c] = R.lam[pb][pp + NR * c];
+  }
+  for (int d = 0; d < ND; ++d) {
+    mL[d] = B.metrics[p + N * (ND * (B.ff.normalDir[e] - 1) + d)];
+    mR[d] = B.ff.metricsR[(long long)e * ND + d];
+  }
+  roeAverage<ND, D>(dL, dR, P.g, roe);
+  const double jac = B.jac[p];
+  double sat[nU];
+  for (int c = 0; c < nU; ++c) sat[c] = 0.0;
+  double u[ND], tau[ND * ND], hf[ND];
+  for (int d = 0; d < ND; ++d) u[d] = B.prim[p + N * L.u(d)];
+  const double v = B.prim[p + N * L.v()], T = B.prim[p + N * L.T()];
+  if (VISC) {
+    for (int c = 0; c < ND * ND; ++c) tau[c] = B.tau[p + N * c];
+    for (int d = 0; d < ND; ++d) hf[d] = B.hf[p + N * d];
+  }
+  for (int side = 0; side < 2; ++side) {
+    D A[nU * nU];
+    incomingJacobian<ND, D>(roe, side == 0 ? mL : mR, P.g, side == 0 ? B.ff.dirL[e] : B.ff.dirR[e], A);
+    const double* lam = side == 0 ? lamL : lamR;
+    const double sInv = side == 0 ? B.ff.ifInv[2 * e] : -B.ff.ifInv[2 * e + 1];
+    for (int r = 0; r < nU; ++r) {
+      double t = A[nU * r].v * lam[0];
+      for (int c = 1; c < nU; ++c) t += A[c + nU * r].v * lam[c];
+      sat[r] += sInv * jac * t;
+    }
+    for (int l = 0; l < nU; ++l) {
+      double t = 0.0;
+      for (int i = 0; i < nU; ++i) {
+        double w = 0.0;
+        for (int j = 0; j < nU; ++j) w += A[i + nU * j].d[l] * dq[j];
+        t += w * lam[i];
+      }
+      sat[l] += sInv * jac * t;
+    }
+    if (VISC) {
+      double y[nU];
+      for (int c = 0; c < nU; ++c) y[c] = 0.0;
+      firstPartialViscousTransposeProduct<ND>(side == 0 ? mL : mR, u, T, v, P.g, P.powerLawExponent, tau, hf, lam, y);
+      const double sVis = side == 0 ? -B.ff.ifVis[2 * e] : B.ff.ifVis[2 * e + 1];
+      for (int c = 0; c < nU; ++c) sat[c] += sVis * jac * y[c];
+    }
+  }
+  for (int c = 0; c < nU; ++c) B.ff.visc[(long long)e * nU + c] = sat[c];
+  if (VISC) {
+    const double mu = B.prim[p + N * L.mu()], la = B.prim[p + N * L.la()], kd = B.prim[p + N * L.k()];
+    double* a = B.ff.ifAd + (long long)e * ND * nV;
+    for (int l = 0; l < ND; ++l) {
+      double ml[ND];
+      for (int d = 0; d < ND; ++d) ml[d] = B.metrics[p + N * (ND * l + d)];
+      double tL[nV], tR[nV];
+      for (int c = 0; c < nV; ++c) tL[c] = tR[c] = 0.0;
+      secondPartialViscousTransposeProduct<ND>(u, mu, la, kd, jac, mL, ml, &lamL[1], tL);
+      secondPartialViscousTransposeProduct<ND>(u, mu, la, kd, jac, mR, ml, &lamR[1], tR);
+      for (int c = 0; c < nV; ++c) a[l * nV + c] = B.ff.ifVis[2 * e] * tL[c] - B.ff.ifVis[2 * e + 1] * tR[c];
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1365,6 +1519,32 @@ void launchSetCounters(int* counters, int step, int segBase, cudaStream_t s) {
 }
 
 int timeStepBlocks(const DevBlock& b) { return gridFor(b.v.N); }
+
+void launchInterfaceSat(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_t s) {
+  if (b.nInterfaceEntries == 0) return;
+  const int G = gridFor(b.v.ff.n);
+  MGD_LAUNCH(c);
+  if (c.nD == 2) {
+    if (c.phys.viscous) kInterfaceSat<2, true><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
+    else kInterfaceSat<2, false><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
+  } else {
+    if (c.phys.viscous) kInterfaceSat<3, true><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
+    else kInterfaceSat<3, false><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
+  }
+}
+
+void launchInterfaceSatAdjoint(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_t s) {
+  if (b.nInterfaceEntries == 0) return;
+  const int G = gridFor(b.v.ff.n);
+  MGD_LAUNCH(c);
+  if (c.nD == 2) {
+    if (c.phys.viscous) kInterfaceSatAdjoint<2, true><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
+    else kInterfaceSatAdjoint<2, false><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
+  } else {
+    if (c.phys.viscous) kInterfaceSatAdjoint<3, true><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
+    else kInterfaceSatAdjoint<3, false><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
+  }
+}
 
 void launchKineticEnergy(Context& c, DevBlock& b, const double* norm, double* partials, double* out) {
   const int nb = gridFor(b.v.N);

@@ -63,6 +63,10 @@ int mgd_forward_rhs_noalloc(mgd_ctx* h, const double* q, double time, double* rh
     c.error = "mgd_forward_rhs_noalloc: q and rhs must be device pointers";
     return 1;
   }
+  if (c.blocks.size() != 1) {
+    c.error = "mgd_forward_rhs_noalloc: one block per context";
+    return 1;
+  }
   DevBlock& b = c.blocks[0];
   const long long N = b.v.N;
   const int nD = c.nD, nU = c.nU;

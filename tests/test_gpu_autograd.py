@@ -54,6 +54,6 @@ def test_backward_matches_oracle_gradient():
     Jo = o.run_forward(N_STEPS, S)
     o.run_adjoint()
     go = o.gradient(4 * N_STEPS) * quadrature_weights(s, N_STEPS)
-    assert abs(float(J) - Jo) <= 1e-10 * abs(Jo)
+    assert abs(J.item() - Jo) <= 1e-10 * abs(Jo)
     g = ft.grad.cpu().numpy()
     assert np.linalg.norm(g - go) <= 1e-10 * np.linalg.norm(go)
