@@ -159,6 +159,13 @@ def patches_from_bc(d, rows):
                                                d.get_float("defaults/viscous_penalty_amount", 1.0))
         p.sponge_amount = d.get_float(key + "sponge_amount", d.get_float("defaults/sponge_amount", 1.0))
         p.sponge_exponent = d.get_int(key + "sponge_exponent", d.get_int("defaults/sponge_exponent", 2))
+        if ptype == "SAT_BLOCK_INTERFACE":
+            # src/BlockInterfacePatchImpl.f90:72-86 (viscous default 0.5) and
+            # src/InterfaceHelperImpl.f90:3-113 (conforms_with, interface_index1..3)
+            p.viscous_penalty_amount = d.get_float(key + "viscous_penalty_amount",
+                                                   d.get_float("defaults/viscous_penalty_amount", 0.5))
+            p.conforms_with = d.get_str(key + "conforms_with", "")
+            p.interface_index = tuple(d.get_int(key + f"interface_index{i}", i) for i in (1, 2, 3))
         if ptype == "SAT_ISOTHERMAL_WALL":
             # src/IsothermalWallImpl.f90:3-80: viscous_penalty_amount1, and the wall
             # temperature from the target state unless use_target_state is off

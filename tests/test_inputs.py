@@ -69,3 +69,34 @@ def test_round_trip(tmp_path):
     inputs.write_bc_dat(tmp_path / "bc.dat", P.patches)
     rows = inputs.read_bc_dat(tmp_path / "bc.dat")
     assert [r[4] for r in rows] == [tuple(p.extent) for p in P.patches]
+
+
+def test_wall_and_interface_keys(tmp_path):
+    """Wall and block-interface options keep the reference's key names and
+    defaults (src/IsothermalWallImpl.f90:3-80, src/BlockInterfacePatchImpl.f90:72-86,
+    src/InterfaceHelperImpl.f90:3-113)."""
+    inp = """include_viscous_terms = true
+Reynolds_number = 100.
+use_constant_CFL_mode = false
+time_step_size = 0.01
+use_target_state = false
+patches/wall.S/viscous_penalty_amount1 = 2.0
+patches/wall.S/temperature = 3.5
+patches/interface.1E/conforms_with = "interface.2W"
+patches/interface.1E/interface_index1 = 2
+patches/interface.1E/interface_index2 = -1
+"""
+    bc = """  wall.S          SAT_ISOTHERMAL_WALL   1   2   1 -1  1  1  1 -1
+  interface.1E    SAT_BLOCK_INTERFACE   1  -1  -1 -1  1 -1  1 -1
+  interface.2W    SAT_BLOCK_INTERFACE   2   1   1  1  1 -1  1 -1
+  slip.N          SAT_SLIP_WALL         1  -2   1 -1 -1 -1  1 -1
+"""
+    (tmp_path / "magudi.inp").write_text(inp)
+    (tmp_path / "bc.dat").write_text(bc)
+    d = inputs.parse_input_file(tmp_path / "magudi.inp")
+    ps = inputs.patches_from_bc(d, inputs.read_bc_dat(tmp_path / "bc.dat"))
+    assert ps[0].viscous_penalty_amount == 2.0 and ps[0].wall_temperature == 3.5
+    assert ps[1].conforms_with == "interface.2W" and ps[1].interface_index == (2, -1, 3)
+    assert ps[1].viscous_penalty_amount == 0.5  # interface default
+    assert ps[2].conforms_with == "" and ps[2].interface_index == (1, 2, 3)
+    assert ps[3].type == "SAT_SLIP_WALL"
