@@ -1763,6 +1763,8 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   if (terminal) launchKineticEnergyAdjointInitial(c, b);
   else launchAdjointInitial(c, b, c.opts.adjoint_forcing_switch ? -dtT / 6.0 : 0.0);
   long long nodesRec = 0, nodesAdj = 0;
+  setProgrammaticLaunch(!twoLanes);
+  struct Restore { ~Restore() { setProgrammaticLaunch(true); } } restore;
   for (int half = 0; half < c.stageHalves; ++half) {
     RunScalars ra = runScalars(c);
     if (terminal) ra.adjointForcingSwitch = 0;  // no forcing during the run

@@ -285,6 +285,8 @@ RunScalars runScalarsOf(Context& c);
 int autotuneTile(Context& c, DevBlock& b, int kernel, const int (*cands)[3], int nCands, Tile* best);
 
 // ----- launchers (mgd_kernels.cu) -----
+// Programmatic dependent launch for the launches that follow on this thread.
+void setProgrammaticLaunch(bool on);
 // Every launcher takes the stream it launches on; the context stream when 0.
 void uploadOperatorTables();
 // Primitive variables of qSrc (or, when stage > 0, of the stage-buffer slot

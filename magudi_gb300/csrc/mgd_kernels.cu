@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <utility>
 
 #include "mgd_internal.h"
 #include "sbp_tables.h"
@@ -42,6 +43,39 @@ static void uploadPowTables() {
 
 constexpr int kBlock = 128;      // pointwise kernels
 constexpr int kMaxTile = 256;    // largest stage-kernel tile
+
+// Programmatic dependent launch: every kernel lets the next kernel in its
+// stream start launching as soon as all of its own blocks are running, and
+// waits for its predecessor to complete (and its memory to be visible) before
+// touching memory. Kernels launched without the attribute pass straight through.
+__device__ __forceinline__ void pdlEnter() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+// Early launch pays off on a single stream (the forward run, batched runs);
+// beside a concurrent stream the waiting blocks would hold SM slots that the
+// other stream's kernels could use, so the checkpoint recomputation and the
+// adjoint launch without it.
+static thread_local bool t_programmaticLaunch = true;
+
+void setProgrammaticLaunch(bool on) { t_programmaticLaunch = on; }
+
+template <typename... KArgs, typename... Args>
+static void pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = t_programmaticLaunch ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 
 static inline int gridFor(long long n) { return (int)((n + kBlock - 1) / kBlock); }
 
@@ -170,6 +204,7 @@ __device__ __forceinline__ void primsPoint(const BlockView& B, const Physics& P,
 template <int ND>
 __global__ void __launch_bounds__(kBlock) kPrims(BlockView B, Physics P, const double* __restrict__ qSrc,
                                                  int copyToQ, RunScalars rs, int stage) {
+  pdlEnter();
   primsPoint<ND>(B, P, qSrc, copyToQ, rs, stage, blockIdx.x);
 }
 
@@ -420,6 +455,7 @@ __device__ __forceinline__ void gradFluxPoint(const BlockView& B, const Physics&
 template <int ND, bool CURV, bool VISC>
 __global__ void __launch_bounds__(kMaxTile) kGradFlux(BlockView B, Physics P, RunScalars rs, int flags,
                                                       int stage, Tile T) {
+  pdlEnter();
   gradFluxPoint<ND, CURV, VISC>(B, P, rs, flags, stage, T, blockIdx.x);
 }
 
@@ -451,6 +487,7 @@ __device__ __forceinline__ void dissipationPoint(const BlockView& B, const Physi
 template <int ND>
 __global__ void __launch_bounds__(kMaxTile) kDissipation(BlockView B, Physics P, const double* __restrict__ src,
                                                          double sign, Tile T) {
+  pdlEnter();
   dissipationPoint<ND>(B, P, src, sign, T, blockIdx.x);
 }
 
@@ -537,6 +574,7 @@ __device__ __forceinline__ void forwardDivergencePoint(const BlockView& B, const
 template <int ND>
 __global__ void __launch_bounds__(kMaxTile) kForwardDivergence(BlockView B, Physics P, RunScalars rs, int rkStage,
                                                                int stage, int controller, Tile T) {
+  pdlEnter();
   forwardDivergencePoint<ND>(B, P, rs, rkStage, stage, controller, T, blockIdx.x);
 }
 
@@ -560,6 +598,7 @@ __device__ __forceinline__ void functionalBlock(const BlockView& B, const RunSca
 }
 
 __global__ void __launch_bounds__(kBlock) kFunctional(BlockView B, RunScalars rs, int stage, int pressureComp) {
+  pdlEnter();
   functionalBlock(B, rs, stage, pressureComp, blockIdx.x);
 }
 
@@ -567,6 +606,7 @@ __global__ void __launch_bounds__(kBlock) kFunctional(BlockView B, RunScalars rs
 // (ThermalActuator%updateGradient / computeSensitivity,
 // src/ThermalActuatorImpl.f90:83-159, 383-443), over the actuator points.
 __global__ void __launch_bounds__(kBlock) kGradientSensitivity(BlockView B, RunScalars rs, int stage, int energyComp) {
+  pdlEnter();
   const int i = blockIdx.x * kBlock + threadIdx.x;
   const long long entry = (long long)(rs.nSteps - *rs.step) * 4 + (4 - stage);
   double v = 0.0;
@@ -697,6 +737,7 @@ __device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physi
 template <int ND, bool CURV, bool VISC>
 __global__ void __launch_bounds__(kMaxTile) kAdjointCore(BlockView B, Physics P, RunScalars rs, int stage,
                                                          int fromSlot, Tile T) {
+  pdlEnter();
   adjointCorePoint<ND, CURV, VISC>(B, P, rs, stage, fromSlot, T, blockIdx.x);
 }
 
@@ -717,6 +758,7 @@ __device__ __forceinline__ void adjointDiffusionPoint(const BlockView& B, const 
 
 template <int ND>
 __global__ void __launch_bounds__(kMaxTile) kAdjointDiffusion(BlockView B, Tile T) {
+  pdlEnter();
   adjointDiffusionPoint<ND>(B, T, blockIdx.x);
 }
 
@@ -824,6 +866,7 @@ template <int ND, bool VISC>
 __global__ void __launch_bounds__(kMaxTile) kAdjointAssemble(BlockView B, Physics P, RunScalars rs, int rkStage,
                                                              int stage, double apiFactor, int api, int fromSlot,
                                                              Tile T) {
+  pdlEnter();
   adjointAssemblePoint<ND, VISC>(B, P, rs, rkStage, stage, apiFactor, api, fromSlot, T, blockIdx.x);
 }
 
@@ -831,6 +874,7 @@ __global__ void __launch_bounds__(kMaxTile) kAdjointAssemble(BlockView B, Physic
 // factor = -dt/6 (loadInitialCondition ADJOINT, src/SolverImpl.f90:368-427).
 template <int ND>
 __global__ void __launch_bounds__(kBlock) kAdjointInitial(BlockView B, Physics P, double factor) {
+  pdlEnter();
   const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
   if (p >= B.N) return;
   constexpr int nU = ND + 2, E = ND + 1;
@@ -856,6 +900,7 @@ __global__ void __launch_bounds__(kBlock) kAdjointInitial(BlockView B, Physics P
 
 template <int ND>
 __global__ void __launch_bounds__(kBlock) kStoreAdjointForcing(BlockView B, Physics P, int zero) {
+  pdlEnter();
   const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
   if (p >= B.N) return;
   constexpr int nU = ND + 2, E = ND + 1;
@@ -884,6 +929,7 @@ __global__ void __launch_bounds__(kBlock) kStoreAdjointForcing(BlockView B, Phys
 template <int ND>
 __global__ void __launch_bounds__(kBlock) kKineticEnergyPartials(BlockView B, const double* __restrict__ norm,
                                                                  double* __restrict__ partial) {
+  pdlEnter();
   const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
   double v = 0.0;
   if (p < B.N && B.iblank[p] != 0) {
@@ -901,6 +947,7 @@ __global__ void __launch_bounds__(kBlock) kKineticEnergyPartials(BlockView B, co
 // lambda(T) = H^-1 dJ/dq(T) of the terminal kinetic energy: (-|u|^2/2, u, 0).
 template <int ND>
 __global__ void __launch_bounds__(kBlock) kKineticEnergyAdjointInitial(BlockView B) {
+  pdlEnter();
   const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
   if (p >= B.N) return;
   constexpr int nU = ND + 2;
@@ -922,6 +969,7 @@ __global__ void __launch_bounds__(kBlock) kKineticEnergyAdjointInitial(BlockView
 // Snapshot of the conserved variables after a completed forward step.
 __global__ void kSnapshot(double* __restrict__ snap, const double* __restrict__ q, long long n,
                           const int* __restrict__ step, int saveInterval, int initial) {
+  pdlEnter();
   const long long i = (long long)blockIdx.x * kBlock + threadIdx.x;
   const int s = initial ? 0 : *step;
   if (s % saveInterval != 0 || i >= n) return;
@@ -929,6 +977,7 @@ __global__ void kSnapshot(double* __restrict__ snap, const double* __restrict__ 
 }
 
 __global__ void kStepAdvance(int* counters, int delta) {
+  pdlEnter();
   if (threadIdx.x == 0 && blockIdx.x == 0) counters[0] += delta;
 }
 
@@ -936,6 +985,7 @@ __global__ void kStepAdvance(int* counters, int delta) {
 // `stride`), in a fixed order.
 __global__ void kReducePartials(const double* __restrict__ partials, int stride, int count, int nSlots,
                                 double* __restrict__ out) {
+  pdlEnter();
   const int s = blockIdx.x;
   if (s >= nSlots) return;
   double v = 0.0;
@@ -959,6 +1009,7 @@ __global__ void kReducePartials(const double* __restrict__ partials, int stride,
 // ---------------------------------------------------------------------------
 template <int ND, bool VISC>
 __global__ void __launch_bounds__(kBlock) kInterfaceSat(BlockView B, Physics P, BlockRefs R) {
+  pdlEnter();
   const int e = blockIdx.x * kBlock + threadIdx.x;
   if (e >= B.ff.n || B.ff.kind[e] != SAT_INTERFACE) return;
   constexpr int nU = ND + 2;
@@ -996,6 +1047,7 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSat(BlockView B, Physics P, 
 
 template <int ND, bool VISC>
 __global__ void __launch_bounds__(kBlock) kInterfaceSatAdjoint(BlockView B, Physics P, BlockRefs R) {
+  pdlEnter();
   const int e = blockIdx.x * kBlock + threadIdx.x;
   if (e >= B.ff.n || B.ff.kind[e] != SAT_INTERFACE) return;
   constexpr int nU = ND + 2, nV = ND + 1;
@@ -1081,6 +1133,7 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSatAdjoint(BlockView B, Phys
 template <int ND, bool CURV, bool VISC>
 __global__ void __launch_bounds__(kBatchThreads) kGradFluxBatch(const BatchEntry* __restrict__ E,
                                                                 const int2* __restrict__ map, Physics P, int stage) {
+  pdlEnter();
   const int2 m = map[blockIdx.x];
   const BatchEntry& e = E[m.x];
   gradFluxPoint<ND, CURV, VISC>(e.v, P, e.rs, GF_FLUX, stage, e.tGrad, m.y);
@@ -1089,6 +1142,7 @@ __global__ void __launch_bounds__(kBatchThreads) kGradFluxBatch(const BatchEntry
 template <int ND>
 __global__ void __launch_bounds__(kBatchThreads) kDissipationBatch(const BatchEntry* __restrict__ E,
                                                                    const int2* __restrict__ map, Physics P) {
+  pdlEnter();
   const int2 m = map[blockIdx.x];
   const BatchEntry& e = E[m.x];
   dissipationPoint<ND>(e.v, P, e.v.q, 1.0, e.tDiss, m.y);
@@ -1098,6 +1152,7 @@ template <int ND>
 __global__ void __launch_bounds__(kBatchThreads) kForwardDivergenceBatch(const BatchEntry* __restrict__ E,
                                                                          const int2* __restrict__ map, Physics P,
                                                                          int rkStage) {
+  pdlEnter();
   const int2 m = map[blockIdx.x];
   const BatchEntry& e = E[m.x];
   forwardDivergencePoint<ND>(e.v, P, e.rs, rkStage, rkStage, e.controller, e.tRhs, m.y);
@@ -1106,6 +1161,7 @@ __global__ void __launch_bounds__(kBatchThreads) kForwardDivergenceBatch(const B
 template <int ND>
 __global__ void __launch_bounds__(kBlock) kPrimsBatch(const BatchEntry* __restrict__ E, const int2* __restrict__ map,
                                                       Physics P) {
+  pdlEnter();
   const int2 m = map[blockIdx.x];
   const BatchEntry& e = E[m.x];
   primsPoint<ND>(e.v, P, e.v.q, 0, e.rs, 0, m.y);
@@ -1113,6 +1169,7 @@ __global__ void __launch_bounds__(kBlock) kPrimsBatch(const BatchEntry* __restri
 
 __global__ void __launch_bounds__(kBlock) kFunctionalBatch(const BatchEntry* __restrict__ E,
                                                            const int2* __restrict__ map, int stage, int pressureComp) {
+  pdlEnter();
   const int2 m = map[blockIdx.x];
   const BatchEntry& e = E[m.x];
   functionalBlock(e.v, e.rs, stage, pressureComp, m.y);
@@ -1143,6 +1200,7 @@ constexpr double kHugeStep = 1.7976931348623157e308;
 template <int ND>
 __global__ void __launch_bounds__(kBlock) kTimeStepPartials(BlockView B, Physics P, double cfl,
                                                             double* __restrict__ partial) {
+  pdlEnter();
   const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
   double v = kHugeStep;
   if (p < B.N && B.iblank[p] != 0) {
@@ -1188,6 +1246,7 @@ __global__ void __launch_bounds__(256) kTimeStepFinalize(const double* __restric
                                                          double* __restrict__ dtOut, const int* __restrict__ step,
                                                          double* __restrict__ time, double* __restrict__ amp,
                                                          SourceTable src) {
+  pdlEnter();
   double v = kHugeStep;
   for (int i = threadIdx.x; i < n; i += blockDim.x) v = fmin(v, partial[i]);
   const double dt = blockMin(v);
@@ -1222,6 +1281,7 @@ __global__ void __launch_bounds__(256) kTimeStepFinalize(const double* __restric
 template <int ND>
 __global__ void kCoordinateDerivative(BlockView B, const double* __restrict__ coords, int dir,
                                       double periodicLength, double* __restrict__ out) {
+  pdlEnter();
   const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
   if (p >= B.N) return;
   const PointIndex I = pointIndex(B, p);
@@ -1250,6 +1310,7 @@ __global__ void kCoordinateDerivative(BlockView B, const double* __restrict__ co
 }
 
 __global__ void kApplyD1(BlockView B, int dir, const double* __restrict__ in, double* __restrict__ out, int ncomp) {
+  pdlEnter();
   const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
   if (p >= B.N) return;
   const PointIndex I = pointIndex(B, p);
@@ -1260,6 +1321,7 @@ __global__ void kApplyD1(BlockView B, int dir, const double* __restrict__ in, do
 template <int ND>
 __global__ void kFarFieldMatrices(BlockView B, double g, const double* __restrict__ sigInv,
                                   const int* __restrict__ signedNormal) {
+  pdlEnter();
   const int e = blockIdx.x * kBlock + threadIdx.x;
   if (e >= B.ff.n) return;
   constexpr int nU = ND + 2;
@@ -1278,6 +1340,7 @@ __global__ void kFarFieldMatrices(BlockView B, double g, const double* __restric
 // and hf hold the target state's values when this runs.
 template <int ND>
 __global__ void kFarFieldTargetVisc(BlockView B) {
+  pdlEnter();
   const int e = blockIdx.x * kBlock + threadIdx.x;
   if (e >= B.ff.n) return;
   constexpr int nU = ND + 2, E = ND + 1;
@@ -1306,6 +1369,7 @@ __global__ void kFarFieldTargetVisc(BlockView B) {
 
 __global__ void kPowSelfTest(const double* __restrict__ x, int n, double e, double* __restrict__ fast,
                              double* __restrict__ ref) {
+  pdlEnter();
   const int i = blockIdx.x * kBlock + threadIdx.x;
   if (i >= n) return;
   fast[i] = fastPowPositive(x[i], e, &g_powTables);
@@ -1335,8 +1399,8 @@ void launchPrims(Context& c, DevBlock& b, const double* qSrc, bool copyToQ, cons
   RunScalars r{};
   if (rs) r = *rs;
   MGD_LAUNCH(c);
-  if (c.nD == 2) kPrims<2><<<gridFor(b.v.N), kBlock, 0, on(c, s)>>>(b.v, c.phys, qSrc, copyToQ, r, stage);
-  else kPrims<3><<<gridFor(b.v.N), kBlock, 0, on(c, s)>>>(b.v, c.phys, qSrc, copyToQ, r, stage);
+  if (c.nD == 2) pdl(kPrims<2>, gridFor(b.v.N), kBlock, on(c, s), b.v, c.phys, qSrc, copyToQ, r, stage);
+  else pdl(kPrims<3>, gridFor(b.v.N), kBlock, on(c, s), b.v, c.phys, qSrc, copyToQ, r, stage);
 }
 
 void launchGradFlux(Context& c, DevBlock& b, bool writeFlux, bool writeStress, const RunScalars* rs, int stage,
@@ -1348,7 +1412,7 @@ void launchGradFlux(Context& c, DevBlock& b, bool writeFlux, bool writeStress, c
   const bool curv = b.v.curvilinear != 0, visc = c.phys.viscous != 0;
   MGD_LAUNCH(c);
 #define GF(ND, CU, VI) \
-  kGradFlux<ND, CU, VI><<<T.blocks(), T.threads(), 0, on(c, s)>>>(b.v, c.phys, r, flags, stage, T)
+  pdl(kGradFlux<ND, CU, VI>, T.blocks(), T.threads(), on(c, s), b.v, c.phys, r, flags, stage, T)
   if (c.nD == 2) {
     if (curv) { if (visc) GF(2, true, true); else GF(2, true, false); }
     else { if (visc) GF(2, false, true); else GF(2, false, false); }
@@ -1364,8 +1428,8 @@ void launchDissipation(Context& c, DevBlock& b, const double* src, double sign, 
   const Tile T = b.tDiss;
   const dim3 grid(T.blocks(), c.nU);
   MGD_LAUNCH(c);
-  if (c.nD == 2) kDissipation<2><<<grid, T.threads(), 0, on(c, s)>>>(b.v, c.phys, src, sign, T);
-  else kDissipation<3><<<grid, T.threads(), 0, on(c, s)>>>(b.v, c.phys, src, sign, T);
+  if (c.nD == 2) pdl(kDissipation<2>, grid, T.threads(), on(c, s), b.v, c.phys, src, sign, T);
+  else pdl(kDissipation<3>, grid, T.threads(), on(c, s), b.v, c.phys, src, sign, T);
 }
 
 void launchForwardDivergence(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bool api, bool controller,
@@ -1375,19 +1439,19 @@ void launchForwardDivergence(Context& c, DevBlock& b, int rkStage, const RunScal
   const dim3 grid(T.blocks(), c.nU);
   MGD_LAUNCH(c);
   if (c.nD == 2)
-    kForwardDivergence<2><<<grid, T.threads(), 0, on(c, s)>>>(b.v, c.phys, rs, rkStage, stage, controller, T);
+    pdl(kForwardDivergence<2>, grid, T.threads(), on(c, s), b.v, c.phys, rs, rkStage, stage, controller, T);
   else
-    kForwardDivergence<3><<<grid, T.threads(), 0, on(c, s)>>>(b.v, c.phys, rs, rkStage, stage, controller, T);
+    pdl(kForwardDivergence<3>, grid, T.threads(), on(c, s), b.v, c.phys, rs, rkStage, stage, controller, T);
 }
 
 void launchFunctional(Context& c, DevBlock& b, const RunScalars& rs, int stage, cudaStream_t s) {
   MGD_LAUNCH(c);
-  kFunctional<<<reductionBlocks(b), kBlock, 0, on(c, s)>>>(b.v, rs, stage, PrimLayout{c.nD}.p());
+  pdl(kFunctional, reductionBlocks(b), kBlock, on(c, s), b.v, rs, stage, PrimLayout{c.nD}.p());
 }
 
 void launchGradientSensitivity(Context& c, DevBlock& b, const RunScalars& rs, int stage, cudaStream_t s) {
   MGD_LAUNCH(c);
-  kGradientSensitivity<<<reductionBlocks(b), kBlock, 0, on(c, s)>>>(b.v, rs, stage, c.nD + 1);
+  pdl(kGradientSensitivity, reductionBlocks(b), kBlock, on(c, s), b.v, rs, stage, c.nD + 1);
 }
 
 void launchAdjointCore(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool fromSlot, cudaStream_t s) {
@@ -1396,7 +1460,7 @@ void launchAdjointCore(Context& c, DevBlock& b, const RunScalars& rs, int stage,
   cudaStream_t st = on(c, s);
   const bool curv = b.v.curvilinear != 0, visc = c.phys.viscous != 0;
   MGD_LAUNCH(c);
-#define AC(ND, CU, VI) kAdjointCore<ND, CU, VI><<<G, W, 0, st>>>(b.v, c.phys, rs, stage, fromSlot, T)
+#define AC(ND, CU, VI) pdl(kAdjointCore<ND, CU, VI>, G, W, st, b.v, c.phys, rs, stage, fromSlot, T)
   if (c.nD == 2) {
     if (curv) { if (visc) AC(2, true, true); else AC(2, true, false); }
     else { if (visc) AC(2, false, true); else AC(2, false, false); }
@@ -1412,8 +1476,8 @@ void launchAdjointDiffusion(Context& c, DevBlock& b, cudaStream_t s) {
   const Tile T = b.tAdjD;
   const dim3 grid(T.blocks(), c.nU - 1);
   MGD_LAUNCH(c);
-  if (c.nD == 2) kAdjointDiffusion<2><<<grid, T.threads(), 0, on(c, s)>>>(b.v, T);
-  else kAdjointDiffusion<3><<<grid, T.threads(), 0, on(c, s)>>>(b.v, T);
+  if (c.nD == 2) pdl(kAdjointDiffusion<2>, grid, T.threads(), on(c, s), b.v, T);
+  else pdl(kAdjointDiffusion<3>, grid, T.threads(), on(c, s), b.v, T);
 }
 
 void launchAdjointAssemble(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage, double apiFactor,
@@ -1424,7 +1488,7 @@ void launchAdjointAssemble(Context& c, DevBlock& b, int rkStage, const RunScalar
   cudaStream_t st = on(c, s);
   MGD_LAUNCH(c);
 #define AA(ND, VI) \
-  kAdjointAssemble<ND, VI><<<grid, W, 0, st>>>(b.v, c.phys, rs, rkStage, stage, apiFactor, api, fromSlot, T)
+  pdl(kAdjointAssemble<ND, VI>, grid, W, st, b.v, c.phys, rs, rkStage, stage, apiFactor, api, fromSlot, T)
   if (c.nD == 2) {
     if (c.phys.viscous) AA(2, true); else AA(2, false);
   } else {
@@ -1435,38 +1499,38 @@ void launchAdjointAssemble(Context& c, DevBlock& b, int rkStage, const RunScalar
 
 void launchAdjointInitial(Context& c, DevBlock& b, double factor) {
   MGD_LAUNCH(c);
-  if (c.nD == 2) kAdjointInitial<2><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, factor);
-  else kAdjointInitial<3><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, factor);
+  if (c.nD == 2) pdl(kAdjointInitial<2>, gridFor(b.v.N), kBlock, c.stream, b.v, c.phys, factor);
+  else pdl(kAdjointInitial<3>, gridFor(b.v.N), kBlock, c.stream, b.v, c.phys, factor);
 }
 
 void launchStoreAdjointForcing(Context& c, DevBlock& b, bool zero) {
   MGD_LAUNCH(c);
-  if (c.nD == 2) kStoreAdjointForcing<2><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, zero);
-  else kStoreAdjointForcing<3><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, c.phys, zero);
+  if (c.nD == 2) pdl(kStoreAdjointForcing<2>, gridFor(b.v.N), kBlock, c.stream, b.v, c.phys, zero);
+  else pdl(kStoreAdjointForcing<3>, gridFor(b.v.N), kBlock, c.stream, b.v, c.phys, zero);
 }
 
 void launchSnapshot(Context& c, DevBlock& b, double* snapshots, int saveInterval, bool initial, cudaStream_t s) {
   const long long n = b.v.N * b.v.nU;
   MGD_LAUNCH(c);
-  kSnapshot<<<gridFor(n), kBlock, 0, on(c, s)>>>(snapshots, b.v.q, n, c.dCounters, saveInterval, initial);
+  pdl(kSnapshot, gridFor(n), kBlock, on(c, s), snapshots, b.v.q, n, c.dCounters, saveInterval, initial);
 }
 
 void launchStepAdvance(Context& c, int delta, cudaStream_t s) {
   MGD_LAUNCH(c);
-  kStepAdvance<<<1, 32, 0, on(c, s)>>>(c.dCounters, delta);
+  pdl(kStepAdvance, 1, 32, on(c, s), c.dCounters, delta);
 }
 
 void launchReducePartials(Context& c, const double* partials, int stride, int count, int nSlots, double* out) {
   if (nSlots <= 0) return;
   MGD_LAUNCH(c);
-  kReducePartials<<<nSlots, kBlock, 0, c.stream>>>(partials, stride, count, nSlots, out);
+  pdl(kReducePartials, nSlots, kBlock, c.stream, partials, stride, count, nSlots, out);
 }
 
 void launchBatchGradFlux(Context& c, const BatchLaunch& L, int stage, cudaStream_t s) {
   const int G = L.blocks[BK_GRAD], W = L.threads[BK_GRAD];
   const bool curv = c.opts.curvilinear != 0, visc = c.phys.viscous != 0;
   MGD_LAUNCH(c);
-#define GFB(ND, CU, VI) kGradFluxBatch<ND, CU, VI><<<G, W, 0, s>>>(L.entries, L.map[BK_GRAD], c.phys, stage)
+#define GFB(ND, CU, VI) pdl(kGradFluxBatch<ND, CU, VI>, G, W, s, L.entries, L.map[BK_GRAD], c.phys, stage)
   if (c.nD == 2) {
     if (curv) { if (visc) GFB(2, true, true); else GFB(2, true, false); }
     else { if (visc) GFB(2, false, true); else GFB(2, false, false); }
@@ -1481,33 +1545,34 @@ void launchBatchDissipation(Context& c, const BatchLaunch& L, cudaStream_t s) {
   if (!c.phys.dissipation) return;
   const dim3 grid(L.blocks[BK_DISS], c.nU);
   MGD_LAUNCH(c);
-  if (c.nD == 2) kDissipationBatch<2><<<grid, L.threads[BK_DISS], 0, s>>>(L.entries, L.map[BK_DISS], c.phys);
-  else kDissipationBatch<3><<<grid, L.threads[BK_DISS], 0, s>>>(L.entries, L.map[BK_DISS], c.phys);
+  if (c.nD == 2) pdl(kDissipationBatch<2>, grid, L.threads[BK_DISS], s, L.entries, L.map[BK_DISS], c.phys);
+  else pdl(kDissipationBatch<3>, grid, L.threads[BK_DISS], s, L.entries, L.map[BK_DISS], c.phys);
 }
 
 void launchBatchForwardDivergence(Context& c, const BatchLaunch& L, int rkStage, cudaStream_t s) {
   const dim3 grid(L.blocks[BK_RHS], c.nU);
   MGD_LAUNCH(c);
   if (c.nD == 2)
-    kForwardDivergenceBatch<2><<<grid, L.threads[BK_RHS], 0, s>>>(L.entries, L.map[BK_RHS], c.phys, rkStage);
+    pdl(kForwardDivergenceBatch<2>, grid, L.threads[BK_RHS], s, L.entries, L.map[BK_RHS], c.phys, rkStage);
   else
-    kForwardDivergenceBatch<3><<<grid, L.threads[BK_RHS], 0, s>>>(L.entries, L.map[BK_RHS], c.phys, rkStage);
+    pdl(kForwardDivergenceBatch<3>, grid, L.threads[BK_RHS], s, L.entries, L.map[BK_RHS], c.phys, rkStage);
 }
 
 void launchBatchPrims(Context& c, const BatchLaunch& L, cudaStream_t s) {
   MGD_LAUNCH(c);
-  if (c.nD == 2) kPrimsBatch<2><<<L.blocks[BK_PRIMS], kBlock, 0, s>>>(L.entries, L.map[BK_PRIMS], c.phys);
-  else kPrimsBatch<3><<<L.blocks[BK_PRIMS], kBlock, 0, s>>>(L.entries, L.map[BK_PRIMS], c.phys);
+  if (c.nD == 2) pdl(kPrimsBatch<2>, L.blocks[BK_PRIMS], kBlock, s, L.entries, L.map[BK_PRIMS], c.phys);
+  else pdl(kPrimsBatch<3>, L.blocks[BK_PRIMS], kBlock, s, L.entries, L.map[BK_PRIMS], c.phys);
 }
 
 void launchBatchFunctional(Context& c, const BatchLaunch& L, int stage, cudaStream_t s) {
   MGD_LAUNCH(c);
-  kFunctionalBatch<<<L.blocks[BK_FUNC], kBlock, 0, s>>>(L.entries, L.map[BK_FUNC], stage, PrimLayout{c.nD}.p());
+  pdl(kFunctionalBatch, L.blocks[BK_FUNC], kBlock, s, L.entries, L.map[BK_FUNC], stage, PrimLayout{c.nD}.p());
 }
 
-void launchStepAdvanceOn(int* counters, int delta, cudaStream_t s) { kStepAdvance<<<1, 32, 0, s>>>(counters, delta); }
+void launchStepAdvanceOn(int* counters, int delta, cudaStream_t s) { pdl(kStepAdvance, 1, 32, s, counters, delta); }
 
 __global__ void kSetCounters(int* counters, int step, int segBase) {
+  pdlEnter();
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     counters[0] = step;
     counters[1] = segBase;
@@ -1515,7 +1580,7 @@ __global__ void kSetCounters(int* counters, int step, int segBase) {
 }
 
 void launchSetCounters(int* counters, int step, int segBase, cudaStream_t s) {
-  kSetCounters<<<1, 32, 0, s>>>(counters, step, segBase);
+  pdl(kSetCounters, 1, 32, s, counters, step, segBase);
 }
 
 int timeStepBlocks(const DevBlock& b) { return gridFor(b.v.N); }
@@ -1525,11 +1590,11 @@ void launchInterfaceSat(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_
   const int G = gridFor(b.v.ff.n);
   MGD_LAUNCH(c);
   if (c.nD == 2) {
-    if (c.phys.viscous) kInterfaceSat<2, true><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
-    else kInterfaceSat<2, false><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
+    if (c.phys.viscous) pdl(kInterfaceSat<2, true>, G, kBlock, on(c, s), b.v, c.phys, r);
+    else pdl(kInterfaceSat<2, false>, G, kBlock, on(c, s), b.v, c.phys, r);
   } else {
-    if (c.phys.viscous) kInterfaceSat<3, true><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
-    else kInterfaceSat<3, false><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
+    if (c.phys.viscous) pdl(kInterfaceSat<3, true>, G, kBlock, on(c, s), b.v, c.phys, r);
+    else pdl(kInterfaceSat<3, false>, G, kBlock, on(c, s), b.v, c.phys, r);
   }
 }
 
@@ -1538,34 +1603,34 @@ void launchInterfaceSatAdjoint(Context& c, DevBlock& b, const BlockRefs& r, cuda
   const int G = gridFor(b.v.ff.n);
   MGD_LAUNCH(c);
   if (c.nD == 2) {
-    if (c.phys.viscous) kInterfaceSatAdjoint<2, true><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
-    else kInterfaceSatAdjoint<2, false><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
+    if (c.phys.viscous) pdl(kInterfaceSatAdjoint<2, true>, G, kBlock, on(c, s), b.v, c.phys, r);
+    else pdl(kInterfaceSatAdjoint<2, false>, G, kBlock, on(c, s), b.v, c.phys, r);
   } else {
-    if (c.phys.viscous) kInterfaceSatAdjoint<3, true><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
-    else kInterfaceSatAdjoint<3, false><<<G, kBlock, 0, on(c, s)>>>(b.v, c.phys, r);
+    if (c.phys.viscous) pdl(kInterfaceSatAdjoint<3, true>, G, kBlock, on(c, s), b.v, c.phys, r);
+    else pdl(kInterfaceSatAdjoint<3, false>, G, kBlock, on(c, s), b.v, c.phys, r);
   }
 }
 
 void launchKineticEnergy(Context& c, DevBlock& b, const double* norm, double* partials, double* out) {
   const int nb = gridFor(b.v.N);
   MGD_LAUNCH(c);
-  if (c.nD == 2) kKineticEnergyPartials<2><<<nb, kBlock, 0, c.stream>>>(b.v, norm, partials);
-  else kKineticEnergyPartials<3><<<nb, kBlock, 0, c.stream>>>(b.v, norm, partials);
+  if (c.nD == 2) pdl(kKineticEnergyPartials<2>, nb, kBlock, c.stream, b.v, norm, partials);
+  else pdl(kKineticEnergyPartials<3>, nb, kBlock, c.stream, b.v, norm, partials);
   launchReducePartials(c, partials, nb, nb, 1, out);
 }
 
 void launchKineticEnergyAdjointInitial(Context& c, DevBlock& b) {
   MGD_LAUNCH(c);
-  if (c.nD == 2) kKineticEnergyAdjointInitial<2><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v);
-  else kKineticEnergyAdjointInitial<3><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v);
+  if (c.nD == 2) pdl(kKineticEnergyAdjointInitial<2>, gridFor(b.v.N), kBlock, c.stream, b.v);
+  else pdl(kKineticEnergyAdjointInitial<3>, gridFor(b.v.N), kBlock, c.stream, b.v);
 }
 
 void launchTimeStep(Context& c, DevBlock& b, double* partials, double* dtOut, const int* step, double* time,
                     double* amp, cudaStream_t s) {
   const int nb = timeStepBlocks(b);
   MGD_LAUNCH(c);
-  if (c.nD == 2) kTimeStepPartials<2><<<nb, kBlock, 0, on(c, s)>>>(b.v, c.phys, c.opts.cfl, partials);
-  else kTimeStepPartials<3><<<nb, kBlock, 0, on(c, s)>>>(b.v, c.phys, c.opts.cfl, partials);
+  if (c.nD == 2) pdl(kTimeStepPartials<2>, nb, kBlock, on(c, s), b.v, c.phys, c.opts.cfl, partials);
+  else pdl(kTimeStepPartials<3>, nb, kBlock, on(c, s), b.v, c.phys, c.opts.cfl, partials);
   SourceTable src{};
   src.n = (int)c.sources.size();
   src.twoPi = 2.0 * (4.0 * std::atan(1.0));
@@ -1575,28 +1640,28 @@ void launchTimeStep(Context& c, DevBlock& b, double* partials, double* dtOut, co
     src.phase[k] = c.sources[k].phase;
   }
   MGD_LAUNCH(c);
-  kTimeStepFinalize<<<1, 256, 0, on(c, s)>>>(partials, nb, dtOut, step, time, amp, src);
+  pdl(kTimeStepFinalize, 1, 256, on(c, s), partials, nb, dtOut, step, time, amp, src);
 }
 
 void launchCoordinateDerivative(Context& c, DevBlock& b, int dir, double* out) {
   const double* coords = b.v.q;  // caller stages the coordinates in q
   MGD_LAUNCH(c);
   if (c.nD == 2)
-    kCoordinateDerivative<2><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, coords, dir, b.desc.periodic_length[dir], out);
+    pdl(kCoordinateDerivative<2>, gridFor(b.v.N), kBlock, c.stream, b.v, coords, dir, b.desc.periodic_length[dir], out);
   else
-    kCoordinateDerivative<3><<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, coords, dir, b.desc.periodic_length[dir], out);
+    pdl(kCoordinateDerivative<3>, gridFor(b.v.N), kBlock, c.stream, b.v, coords, dir, b.desc.periodic_length[dir], out);
 }
 
 void launchApplyD1(Context& c, DevBlock& b, int dir, const double* in, double* out, int ncomp) {
   MGD_LAUNCH(c);
-  kApplyD1<<<gridFor(b.v.N), kBlock, 0, c.stream>>>(b.v, dir, in, out, ncomp);
+  pdl(kApplyD1, gridFor(b.v.N), kBlock, c.stream, b.v, dir, in, out, ncomp);
 }
 
 void launchFarFieldTargetVisc(Context& c, DevBlock& b) {
   if (b.v.ff.n == 0) return;
   MGD_LAUNCH(c);
-  if (c.nD == 2) kFarFieldTargetVisc<2><<<gridFor(b.v.ff.n), kBlock, 0, c.stream>>>(b.v);
-  else kFarFieldTargetVisc<3><<<gridFor(b.v.ff.n), kBlock, 0, c.stream>>>(b.v);
+  if (c.nD == 2) pdl(kFarFieldTargetVisc<2>, gridFor(b.v.ff.n), kBlock, c.stream, b.v);
+  else pdl(kFarFieldTargetVisc<3>, gridFor(b.v.ff.n), kBlock, c.stream, b.v);
 }
 
 // Far-field matrices from per-entry inviscid penalty and signed normal direction.
@@ -1605,9 +1670,9 @@ void launchFarFieldMatricesWith(Context& c, DevBlock& b, const double* sigInv, c
   if (b.v.ff.n == 0) return;
   MGD_LAUNCH(c);
   if (c.nD == 2)
-    kFarFieldMatrices<2><<<gridFor(b.v.ff.n), kBlock, 0, c.stream>>>(b.v, c.phys.g, sigInv, signedNormal);
+    pdl(kFarFieldMatrices<2>, gridFor(b.v.ff.n), kBlock, c.stream, b.v, c.phys.g, sigInv, signedNormal);
   else
-    kFarFieldMatrices<3><<<gridFor(b.v.ff.n), kBlock, 0, c.stream>>>(b.v, c.phys.g, sigInv, signedNormal);
+    pdl(kFarFieldMatrices<3>, gridFor(b.v.ff.n), kBlock, c.stream, b.v, c.phys.g, sigInv, signedNormal);
 }
 
 }  // namespace mgd
