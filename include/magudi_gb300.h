@@ -257,6 +257,53 @@ int mgd_batch_destroy(mgd_batch* batch);
 const char* mgd_batch_last_error(const mgd_batch* batch);
 long long mgd_batch_kernel_launches(mgd_batch* batch, int reset);
 
+/* ---- files around the hot path (host code; no GPU needed) ---- */
+
+/* PLOT3D whole-format multi-block files as magudi writes them
+ * (write_skeleton, src/PLOT3DFormat.c:208-292; plot3dWriteSingleGrid /
+ * plot3dWriteSingleSolution, src/PLOT3DHelperImpl.f90:554-784): 4-byte
+ * record markers, native byte order. Grid: x, y, z and iblank of each block
+ * (z = 0 in 2D). Solution: a 4-double auxiliary header per block
+ * (timestep, 0, 0, time) and 5 component slots, components 1..n-1 in slots
+ * 1..n-1 and the last (energy) in slot 5. grid_sizes: 3 per grid; arrays are
+ * component-major (N per component) per grid. */
+int mgd_plot3d_write_grid(const char* filename, int n_grids, const int* grid_sizes, int n_dimensions,
+                          const double* const* coordinates, const int* const* iblank);
+int mgd_plot3d_write_solution(const char* filename, int n_grids, const int* grid_sizes, int n_components,
+                              const double* const* q, const double* aux);
+int mgd_plot3d_read_solution(const char* filename, int n_grids, const int* grid_sizes, int n_components,
+                             double* const* q, double* aux);
+
+/* Actuator-patch control forcing / gradient streams (the .dat files of
+ * src/ActuatorPatchImpl.f90:226-458): raw native doubles, one patch's points
+ * per entry, entries in file order. The entries are read from / written to
+ * entries[e * stride + offset + 0 .. points_per_entry - 1]. */
+int mgd_write_patch_stream(const char* filename, const double* entries, long long n_entries,
+                           long long points_per_entry, long long stride, long long offset);
+int mgd_read_patch_stream(const char* filename, double* entries, long long n_entries, long long points_per_entry,
+                          long long stride, long long offset);
+
+/* State%saveData for one field (MGD_FIELD_CONSERVED or MGD_FIELD_ADJOINT) of
+ * every block as a PLOT3D solution file (src/StateImpl.f90:340-380): the
+ * device-to-host copy is ordered on the context stream and the file is
+ * written by a host thread while later work runs; mgd_wait_io joins it. */
+int mgd_save_solution(mgd_ctx* ctx, const char* filename, int field, int timestep, double time);
+int mgd_wait_io(mgd_ctx* ctx);
+/* Region%loadData of one field from a PLOT3D solution file; *time receives
+ * the file's time. */
+int mgd_load_solution(mgd_ctx* ctx, const char* filename, int field, double* time);
+/* The grid of every block as a PLOT3D grid file. */
+int mgd_save_grid(mgd_ctx* ctx, const char* filename);
+/* <prefix>.gradient_<patch>.dat for every actuator patch, from the gradient
+ * of the last adjoint run; <prefix>.control_forcing_<patch>.dat read into
+ * the control forcing (src/ActuatorPatchImpl.f90:226-458). */
+int mgd_save_gradient(mgd_ctx* ctx, const char* prefix, long long n_entries);
+int mgd_load_control_forcing(mgd_ctx* ctx, const char* prefix, long long n_entries);
+/* ZAXPY on the device (bin/ZAXPY.f90, ControlSpaceAdvancer): control
+ * forcing = a * gradient (+ the current forcing when accumulate != 0), over
+ * the 4 * n_steps entries of the last run, with no host round trip. */
+int mgd_control_zaxpy(mgd_ctx* ctx, double a, int accumulate);
+
 /* Measurement hook (no reference counterpart): times each kernel of one RK
  * stage separately with CUDA events on the context stream; forward gives 2
  * durations [gradient/flux, divergence+RK], adjoint 4 [primitives, stress,

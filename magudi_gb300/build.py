@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math"]
-SOURCES = ["mgd_api.cu", "mgd_kernels.cu", "mgd_noalloc.cu", "mgd_batch.cu"]
+SOURCES = ["mgd_api.cu", "mgd_kernels.cu", "mgd_noalloc.cu", "mgd_batch.cu", "mgd_io.cpp"]
 
 
 def nvcc():
@@ -42,7 +42,7 @@ def build(force=False, verbose=False):
     jobs = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        o = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append([nvcc(), *ARCH_FLAGS, *COMMON_FLAGS, "-c", s, "-o", o])

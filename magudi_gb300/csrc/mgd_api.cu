@@ -152,6 +152,10 @@ int mgd_create(const mgd_options* o, mgd_ctx** out) {
 int mgd_destroy(mgd_ctx* h) {
   if (!h) return 0;
   Context& c = h->c;
+  if (c.ioThread.joinable()) c.ioThread.join();
+  if (c.ioStaging) cudaFreeHost(c.ioStaging);
+  if (c.ioStream) cudaStreamDestroy(c.ioStream);
+  if (c.ioCopied) cudaEventDestroy(c.ioCopied);
   cudaStreamSynchronize(c.stream);
   for (DevBlock& b : c.blocks) freeBlock(b);
   cudaFree(c.dCounters); cudaFree(c.dApiAmp); cudaFree(c.dAmp); cudaFree(c.dForcing);
@@ -1883,6 +1887,181 @@ int mgd_get_gradient(mgd_ctx* h, double* host, long long n_entries) {
   return 0;
 }
 
+
+// ---------------------------------------------------------------------------
+// files: PLOT3D solutions and grids, actuator-patch streams, device ZAXPY
+// ---------------------------------------------------------------------------
+static int joinIo(Context& c) {
+  if (c.ioThread.joinable()) c.ioThread.join();
+  const int s = c.ioStatus;
+  c.ioStatus = 0;
+  if (s) return fail(c, "writing a solution file failed");
+  return 0;
+}
+
+int mgd_wait_io(mgd_ctx* h) { return joinIo(h->c); }
+
+static double* fieldArray(Context& c, DevBlock& b, int field) {
+  return field == MGD_FIELD_ADJOINT ? b.v.lam : (field == MGD_FIELD_CONSERVED ? b.v.q : nullptr);
+}
+
+int mgd_save_solution(mgd_ctx* h, const char* filename, int field, int timestep, double time) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  if (joinIo(c)) return 1;
+  size_t bytes = 0;
+  for (DevBlock& b : c.blocks) {
+    if (!fieldArray(c, b, field)) return fail(c, "mgd_save_solution: field must be CONSERVED or ADJOINT");
+    bytes += (size_t)b.v.N * c.nU * sizeof(double);
+  }
+  if (!c.ioStream) {
+    CUDA_TRY(c, cudaStreamCreateWithFlags(&c.ioStream, cudaStreamNonBlocking));
+    CUDA_TRY(c, cudaEventCreateWithFlags(&c.ioCopied, cudaEventDisableTiming));
+  }
+  if (c.ioStagingBytes < bytes) {
+    if (c.ioStaging) cudaFreeHost(c.ioStaging);
+    c.ioStaging = nullptr;
+    c.ioStagingBytes = 0;
+    CUDA_TRY(c, cudaMallocHost((void**)&c.ioStaging, bytes));
+    c.ioStagingBytes = bytes;
+  }
+  // copy after the work issued so far; later work on the context stream waits for the copy
+  CUDA_TRY(c, cudaEventRecord(c.evFork[4], c.stream));
+  CUDA_TRY(c, cudaStreamWaitEvent(c.ioStream, c.evFork[4], 0));
+  size_t off = 0;
+  std::vector<const double*> arrays;
+  std::vector<int> sizes;
+  for (DevBlock& b : c.blocks) {
+    const size_t n = (size_t)b.v.N * c.nU;
+    CUDA_TRY(c, cudaMemcpyAsync(c.ioStaging + off, fieldArray(c, b, field), n * sizeof(double),
+                                cudaMemcpyDeviceToHost, c.ioStream));
+    arrays.push_back(c.ioStaging + off);
+    for (int d = 0; d < 3; ++d) sizes.push_back(b.v.gs[d]);
+    off += n;
+  }
+  CUDA_TRY(c, cudaEventRecord(c.ioCopied, c.ioStream));
+  CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.ioCopied, 0));
+  const std::string name(filename);
+  const int nU = c.nU;
+  const cudaEvent_t copied = c.ioCopied;
+  const int device = c.device;
+  int* status = &c.ioStatus;
+  c.ioThread = std::thread([=]() {
+    cudaSetDevice(device);
+    if (cudaEventSynchronize(copied) != cudaSuccess) {
+      *status = 1;
+      return;
+    }
+    // plot3dAuxiliaryData: (timestep, 0, 0, time) (src/RegionImpl.f90:1736-1746, src/StateImpl.f90:372)
+    const double aux[4] = {(double)timestep, 0.0, 0.0, time};
+    *status = mgd_plot3d_write_solution(name.c_str(), (int)sizes.size() / 3, sizes.data(), nU, arrays.data(), aux);
+  });
+  return 0;
+}
+
+int mgd_load_solution(mgd_ctx* h, const char* filename, int field, double* time) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  if (joinIo(c)) return 1;
+  std::vector<std::vector<double>> host;
+  std::vector<double*> arrays;
+  std::vector<int> sizes;
+  for (DevBlock& b : c.blocks) {
+    if (!fieldArray(c, b, field)) return fail(c, "mgd_load_solution: field must be CONSERVED or ADJOINT");
+    host.emplace_back((size_t)b.v.N * c.nU);
+    for (int d = 0; d < 3; ++d) sizes.push_back(b.v.gs[d]);
+  }
+  for (auto& v : host) arrays.push_back(v.data());
+  double aux[4] = {0, 0, 0, 0};
+  if (mgd_plot3d_read_solution(filename, (int)c.blocks.size(), sizes.data(), c.nU, arrays.data(), aux))
+    return fail(c, std::string("cannot read PLOT3D solution file '") + filename + "' for this region");
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi)
+    CUDA_TRY(c, cudaMemcpy(fieldArray(c, c.blocks[bi], field), host[bi].data(), host[bi].size() * sizeof(double),
+                           cudaMemcpyHostToDevice));
+  if (time) *time = aux[3];
+  return 0;
+}
+
+int mgd_save_grid(mgd_ctx* h, const char* filename) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  std::vector<const double*> coords;
+  std::vector<const int*> ib;
+  std::vector<int> sizes;
+  for (DevBlock& b : c.blocks) {
+    coords.push_back(b.hostCoords.data());
+    ib.push_back(b.hostIblank.data());
+    for (int d = 0; d < 3; ++d) sizes.push_back(b.v.gs[d]);
+  }
+  if (mgd_plot3d_write_grid(filename, (int)c.blocks.size(), sizes.data(), c.nD, coords.data(), ib.data()))
+    return fail(c, std::string("cannot write PLOT3D grid file '") + filename + "'");
+  return 0;
+}
+
+// Actuator patches in bc.dat order with their point counts and offsets in an entry.
+static std::vector<std::pair<const mgd_patch_desc*, long long>> actuatorPatches(Context& c) {
+  std::vector<std::pair<const mgd_patch_desc*, long long>> out;
+  for (const mgd_patch_desc& p : c.patches) {
+    if (p.type != MGD_PATCH_ACTUATOR || p.grid_index != 1) continue;
+    int e[6];
+    resolveExtent(p, c.blocks[0].v.gs, c.nD, e);
+    out.emplace_back(&p, (long long)(e[1] - e[0] + 1) * (e[3] - e[2] + 1) * (e[5] - e[4] + 1));
+  }
+  return out;
+}
+
+int mgd_save_gradient(mgd_ctx* h, const char* prefix, long long n_entries) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  const long long P = c.actuatorPoints, n = std::min(n_entries, 4LL * c.runSteps);
+  if (n <= 0 || P <= 0) return fail(c, "mgd_save_gradient needs an adjoint run and an actuator patch");
+  std::vector<double> g((size_t)(n * P));
+  CUDA_TRY(c, cudaMemcpy(g.data(), c.dGradient, g.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  long long off = 0;
+  for (auto& pp : actuatorPatches(c)) {
+    const std::string name = std::string(prefix) + ".gradient_" + pp.first->name + ".dat";
+    if (mgd_write_patch_stream(name.c_str(), g.data(), n, pp.second, P, off))
+      return fail(c, "cannot write '" + name + "'");
+    off += pp.second;
+  }
+  return 0;
+}
+
+int mgd_load_control_forcing(mgd_ctx* h, const char* prefix, long long n_entries) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  const long long P = c.actuatorPoints;
+  if (n_entries <= 0 || P <= 0) return fail(c, "mgd_load_control_forcing needs entries and an actuator patch");
+  std::vector<double> f((size_t)(n_entries * P));
+  long long off = 0;
+  for (auto& pp : actuatorPatches(c)) {
+    const std::string name = std::string(prefix) + ".control_forcing_" + pp.first->name + ".dat";
+    if (mgd_read_patch_stream(name.c_str(), f.data(), n_entries, pp.second, P, off))
+      return fail(c, "cannot read '" + name + "'");
+    off += pp.second;
+  }
+  return mgd_set_control_forcing(h, f.data(), n_entries);
+}
+
+int mgd_control_zaxpy(mgd_ctx* h, double a, int accumulate) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  const long long P = c.actuatorPoints, n = 4LL * c.runSteps;
+  if (n <= 0 || P <= 0 || !c.dGradient) return fail(c, "mgd_control_zaxpy needs an adjoint run and an actuator patch");
+  if (accumulate && c.nForcingEntries != n) return fail(c, "mgd_control_zaxpy: the current forcing has another length");
+  if (c.forcingCapacity < n * P) {
+    if (accumulate) return fail(c, "mgd_control_zaxpy: no forcing to accumulate into");
+    cudaFree(c.dForcing);
+    c.dForcing = nullptr;
+    CUDA_TRY(c, cudaMalloc((void**)&c.dForcing, (size_t)(n * P) * sizeof(double)));
+    c.forcingCapacity = n * P;
+  }
+  launchAxpy(c, c.dForcing, c.dGradient, a, n * P, accumulate != 0);
+  if (checkLaunch(c)) return 1;
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  c.nForcingEntries = n;
+  return 0;
+}
 
 // Times each kernel of one RK stage separately with CUDA events on the
 // context stream, avg_ms receiving the mean duration per launch over `reps`

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/magudi_gb300.h"
@@ -250,6 +251,13 @@ struct Context {
   double* dTime = nullptr;
   double* dNorm = nullptr;          // H det per point (terminal functional)
   cudaGraphExec_t gForward = nullptr, gRecomputeH[2] = {}, gAdjointH[2] = {};
+  // asynchronous solution files: pinned staging, copy stream, writer thread
+  cudaStream_t ioStream = nullptr;
+  cudaEvent_t ioCopied = nullptr;
+  double* ioStaging = nullptr;
+  size_t ioStagingBytes = 0;
+  std::thread ioThread;
+  int ioStatus = 0;
   long long nodesForward = 0, nodesRecompute = 0, nodesAdjoint = 0;
 };
 
@@ -328,6 +336,7 @@ void launchReducePartials(Context& c, const double* partials, int stride, int co
 void launchTimeStep(Context& c, DevBlock& b, double* partials, double* dtOut, const int* step, double* time,
                     double* amp, cudaStream_t s = 0);
 int timeStepBlocks(const DevBlock& b);
+void launchAxpy(Context& c, double* z, const double* x, double a, long long n, bool accumulate);
 // Block-interface SAT vectors of block b's interface entries (forward; adjoint
 // with the interface terms of the adjoint viscous diffusion).
 void launchInterfaceSat(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_t s = 0);

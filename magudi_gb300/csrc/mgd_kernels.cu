@@ -1585,6 +1585,20 @@ void launchSetCounters(int* counters, int step, int segBase, cudaStream_t s) {
 
 int timeStepBlocks(const DevBlock& b) { return gridFor(b.v.N); }
 
+// z = a x + (accumulate ? z : 0) (ZAXPY, bin/ZAXPY.f90).
+__global__ void kAxpy(double* __restrict__ z, const double* __restrict__ x, double a, long long n, int accumulate) {
+  pdlEnter();
+  const long long i = (long long)blockIdx.x * kBlock + threadIdx.x;
+  if (i >= n) return;
+  z[i] = accumulate ? a * x[i] + z[i] : a * x[i];
+}
+
+void launchAxpy(Context& c, double* z, const double* x, double a, long long n, bool accumulate) {
+  if (n <= 0) return;
+  MGD_LAUNCH(c);
+  pdl(kAxpy, (unsigned)((n + kBlock - 1) / kBlock), kBlock, c.stream, z, x, a, n, accumulate ? 1 : 0);
+}
+
 void launchInterfaceSat(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_t s) {
   if (b.nInterfaceEntries == 0) return;
   const int G = gridFor(b.v.ff.n);

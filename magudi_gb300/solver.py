@@ -58,6 +58,13 @@ def load_library(build_if_missing=True):
     L.mgd_get_gradient.argtypes = [ctx, C.POINTER(C.c_double), C.c_longlong]
     L.mgd_time_step_size.argtypes = [ctx, C.POINTER(C.c_double)]
     L.mgd_actuator_weights.argtypes = [ctx, C.POINTER(C.c_double)]
+    L.mgd_save_solution.argtypes = [ctx, C.c_char_p, C.c_int, C.c_int, C.c_double]
+    L.mgd_wait_io.argtypes = [ctx]
+    L.mgd_load_solution.argtypes = [ctx, C.c_char_p, C.c_int, C.POINTER(C.c_double)]
+    L.mgd_save_grid.argtypes = [ctx, C.c_char_p]
+    L.mgd_save_gradient.argtypes = [ctx, C.c_char_p, C.c_longlong]
+    L.mgd_load_control_forcing.argtypes = [ctx, C.c_char_p, C.c_longlong]
+    L.mgd_control_zaxpy.argtypes = [ctx, C.c_double, C.c_int]
     L.mgd_batch_create.argtypes = [C.POINTER(ctx), C.c_int, C.POINTER(C.c_void_p)]
     L.mgd_batch_run_forward.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double)]
     L.mgd_batch_destroy.argtypes = [C.c_void_p]
@@ -202,6 +209,32 @@ class Solver:
         out = np.zeros(max(1, n_steps))
         self._check(self.L.mgd_get_step_sizes(self.h, capi.dptr(out), n_steps))
         return out[:n_steps]
+
+    # files (PLOT3D solutions and grids, actuator-patch streams)
+    def save_solution(self, filename, field=capi.FIELD_CONSERVED, timestep=0, time=0.0):
+        """Asynchronous: the file is written by a host thread; wait_io() joins it."""
+        self._check(self.L.mgd_save_solution(self.h, str(filename).encode(), field, timestep, time))
+
+    def wait_io(self):
+        self._check(self.L.mgd_wait_io(self.h))
+
+    def load_solution(self, filename, field=capi.FIELD_CONSERVED):
+        t = C.c_double()
+        self._check(self.L.mgd_load_solution(self.h, str(filename).encode(), field, C.byref(t)))
+        return t.value
+
+    def save_grid(self, filename):
+        self._check(self.L.mgd_save_grid(self.h, str(filename).encode()))
+
+    def save_gradient(self, prefix, n_entries):
+        self._check(self.L.mgd_save_gradient(self.h, str(prefix).encode(), n_entries))
+
+    def load_control_forcing(self, prefix, n_entries):
+        self._check(self.L.mgd_load_control_forcing(self.h, str(prefix).encode(), n_entries))
+
+    def control_zaxpy(self, a, accumulate=False):
+        """Control forcing = a * gradient (+ forcing) on the device."""
+        self._check(self.L.mgd_control_zaxpy(self.h, a, int(accumulate)))
 
     def profile_stage_kernels(self, mode, reps=20):
         """Mean per-launch milliseconds of each kernel of one RK stage."""
