@@ -124,19 +124,22 @@ def wall_channel_2d(n=41, ny=33, wall="SAT_ISOTHERMAL_WALL", wall_temperature=0.
 
 
 def two_block_2d(nx1=25, nx2=29, ny=31, half_width=6.0, viscous=True, rotate_second=False, curvilinear=None,
-                 interfaces=True, dt=0.02, n_steps=10, sponge_points=5):
+                 interfaces=True, dt=0.02, n_steps=10, sponge_points=5, functional=False, controller_switch=False):
     """Two blocks meeting at x = 0 through SAT_BLOCK_INTERFACE patches: block 1
     covers [-w, 0] x [-w, w], block 2 covers [0, w] x [-w, w]; far-field SATs
     and sponges on the outer faces; quiescent target and initial state.
     rotate_second stores block 2 with its first index along +y and its second
     along -x (a rotation, so the Jacobian stays positive), which makes the
     interface a transposing one (interface_index 2, 1, 3). Without
-    `interfaces`, the x = 0 faces carry no patch."""
+    `interfaces`, the x = 0 faces carry no patch. With `functional`, an
+    acoustic source and an actuator sit in block 1 at (-1.5, 0) and the cost
+    target in block 2 at (1.5, 0), so that sound crosses the interface."""
     gamma = 1.4
     curv = rotate_second if curvilinear is None else curvilinear
     opts = Options(
         n_dimensions=2, viscous=viscous, dissipation=True, composite_dissipation=True,
-        curvilinear=curv, use_constant_cfl=False, enable_controller=False, enable_functional=False,
+        curvilinear=curv, use_constant_cfl=False, enable_controller=functional, enable_functional=functional,
+        controller_switch=controller_switch,
         ratio_of_specific_heats=gamma, reynolds_number=200.0, prandtl_number=0.72,
         viscosity_power_law_exponent=0.666, bulk_viscosity_ratio=0.6, dissipation_amount=0.01,
         time_step_size=dt)
@@ -159,8 +162,10 @@ def two_block_2d(nx1=25, nx2=29, ny=31, half_width=6.0, viscous=True, rotate_sec
     for c, gs in ((c1, (nx1, ny, 1)), (c2, gs2)):
         N = c.shape[1]
         t = quiescent_state(N, 2, gamma)
+        cm = np.exp(-((c[0] + 1.5) ** 2 + c[1] ** 2) / 2.0)
+        tm = np.exp(-((c[0] - 1.5) ** 2 + c[1] ** 2) / 2.0)
         blocks.append(Block(grid_size=gs, coordinates=np.ascontiguousarray(c), initial_state=t.copy(),
-                            target_state=t.copy(), control_mollifier=np.ones(N), target_mollifier=np.ones(N),
+                            target_state=t.copy(), control_mollifier=cm, target_mollifier=tm,
                             mean_pressure=np.full(N, 1.0 / gamma)))
     s = sponge_points
     patches = [
@@ -193,7 +198,19 @@ def two_block_2d(nx1=25, nx2=29, ny=31, half_width=6.0, viscous=True, rotate_sec
                        viscous_penalty_amount=0.5, conforms_with="interface.2W")
     if interfaces:
         patches += [iface1, iface2]
-    return Problem(options=opts, blocks=blocks, patches=patches, sources=[], n_steps=n_steps, save_interval=5)
+    sources = []
+    if functional:
+        ci = _extents(x1, -3.5, -0.5)
+        cj = _extents(y, -2.0, 2.0)
+        patches.append(Patch("controlRegion", "ACTUATOR", 1, 0, (ci[0], ci[1], cj[0], cj[1], 1, -1)))
+        ti = _extents(x2, 0.5, 3.5)
+        if rotate_second:  # block 2 index 1 runs along y, index 2 along -x
+            lo, hi = nx2 + 1 - ti[1], nx2 + 1 - ti[0]
+            patches.append(Patch("targetRegion", "COST_TARGET", 2, 0, (cj[0], cj[1], lo, hi, 1, -1)))
+        else:
+            patches.append(Patch("targetRegion", "COST_TARGET", 2, 0, (ti[0], ti[1], cj[0], cj[1], 1, -1)))
+        sources = [AcousticSource((-1.5, 0.0), 0.01, 0.2, 1.5, -math.pi / 2)]
+    return Problem(options=opts, blocks=blocks, patches=patches, sources=sources, n_steps=n_steps, save_interval=5)
 
 
 def random_state(n_points, n_dimensions, gamma, rng):

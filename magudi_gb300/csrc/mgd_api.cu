@@ -157,7 +157,12 @@ int mgd_destroy(mgd_ctx* h) {
   if (c.ioStream) cudaStreamDestroy(c.ioStream);
   if (c.ioCopied) cudaEventDestroy(c.ioCopied);
   cudaStreamSynchronize(c.stream);
-  for (DevBlock& b : c.blocks) freeBlock(b);
+  for (DevBlock& b : c.blocks) {
+    freeBlock(b);
+    cudaFree(b.runSnap);
+    cudaFree(b.runStage);
+    cudaFree(b.runPartials);
+  }
   cudaFree(c.dCounters); cudaFree(c.dApiAmp); cudaFree(c.dAmp); cudaFree(c.dForcing);
   cudaFree(c.dGradient); cudaFree(c.dPartials); cudaFree(c.dStageValues);
   cudaFree(c.dSnapshots); cudaFree(c.dStageBuf);
@@ -1709,12 +1714,214 @@ RunScalars runScalarsOf(Context& c) { return runScalars(c); }
 
 }  // namespace mgd
 
+// ---------------------------------------------------------------------------
+// Checkpointed runs of multi-block regions (block interfaces): one stream, the
+// stage kernels of every block per stage, interface SATs between the flux and
+// divergence kernels, per-block snapshots, stage slots and partial sums.
+// ---------------------------------------------------------------------------
+static int growDevice(Context& c, double** p, long long* cap, long long need) {
+  if (*cap >= need) return 0;
+  cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  CUDA_TRY(c, cudaMalloc((void**)p, (size_t)std::max(1LL, need) * sizeof(double)));
+  *cap = need;
+  return 0;
+}
+
+static RunScalars blockRunScalars(Context& c, DevBlock& b, bool first) {
+  RunScalars r = runScalars(c);
+  r.partials = b.runPartials;
+  r.nPartialBlocks = reductionBlocks(b);
+  r.stageBuf = b.runStage;
+  if (!first) {
+    // actuator patches lie in block 1
+    r.forcing = nullptr;
+    r.nForcingEntries = 0;
+    r.P = 0;
+  }
+  return r;
+}
+
+static BlockRefs runRefs(Context& c) {
+  BlockRefs r = blockRefs(c);
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+    r.stage[bi] = c.blocks[bi].runStage;
+    r.slotStride[bi] = c.slotStride;
+  }
+  return r;
+}
+
+// Per-stage values of every block summed over the blocks (block partial
+// sums reduced in a fixed order, then the blocks in order).
+static int reduceRegion(Context& c, int nSlots, std::vector<double>& out) {
+  out.assign(nSlots, 0.0);
+  if (c.stageValueCapacity < nSlots) {
+    cudaFree(c.dStageValues);
+    CUDA_TRY(c, cudaMalloc((void**)&c.dStageValues, (size_t)std::max(1, nSlots) * sizeof(double)));
+    c.stageValueCapacity = nSlots;
+  }
+  std::vector<double> v(nSlots);
+  for (DevBlock& b : c.blocks) {
+    const int nb = reductionBlocks(b);
+    launchReducePartials(c, b.runPartials, nb, nb, nSlots, c.dStageValues);
+    CUDA_TRY(c, cudaMemcpyAsync(v.data(), c.dStageValues, (size_t)nSlots * sizeof(double), cudaMemcpyDeviceToHost,
+                                c.stream));
+    CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+    for (int k = 0; k < nSlots; ++k) out[k] += v[k];
+  }
+  return checkLaunch(c);
+}
+
+// One forward RK stage of every block; store writes the stage slots.
+static void regionRunStage(Context& c, std::vector<RunScalars>& rs, int i, bool controller, bool store,
+                           bool functional) {
+  const BlockRefs refs = blockRefs(c);
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+    DevBlock& b = c.blocks[bi];
+    launchDissipation(c, b, b.v.q, 1.0);
+    launchGradFlux(c, b, true, false, &rs[bi], i, store);
+  }
+  for (DevBlock& b : c.blocks) launchInterfaceSat(c, b, refs);
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+    DevBlock& b = c.blocks[bi];
+    launchForwardDivergence(c, b, i, rs[bi], false, controller && bi == 0);
+    launchPrims(c, b, b.v.q, false);
+    if (functional) launchFunctional(c, b, rs[bi], i);
+  }
+}
+
+static int regionRunForward(Context& c, int n_steps, int save_interval, double t0, double* cost) {
+  if (c.opts.use_constant_cfl) return fail(c, "multi-block runs use a constant time_step_size");
+  if (c.opts.functional_type != MGD_FUNCTIONAL_SOUND) return fail(c, "multi-block runs use the SOUND functional");
+  if (prepareForwardRun(c, n_steps, save_interval, t0, false)) return 1;
+  const long long nSnap = n_steps / save_interval + 2;
+  for (DevBlock& b : c.blocks) {
+    if (growDevice(c, &b.runSnap, &b.runSnapCap, nSnap * c.nU * b.v.N)) return 1;
+    if (growDevice(c, &b.runPartials, &b.runPartialCap, 4LL * n_steps * reductionBlocks(b))) return 1;
+    launchPrims(c, b, b.v.q, false);
+    launchSnapshot(c, b, b.runSnap, save_interval, true);
+  }
+  const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
+  const bool functional = c.opts.enable_functional != 0;
+  std::vector<RunScalars> rs;
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) rs.push_back(blockRunScalars(c, c.blocks[bi], bi == 0));
+  if (setCounters(c, 1, 0)) return 1;
+  if (capture(c, &c.gForward, &c.nodesForward, [&]() {
+        for (int i = 1; i <= 4; ++i) regionRunStage(c, rs, i, controller, false, functional);
+        for (DevBlock& b : c.blocks) launchSnapshot(c, b, b.runSnap, save_interval, false);
+        launchStepAdvance(c, 1);
+      }))
+    return 1;
+  for (int s = 0; s < n_steps; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gForward, c.stream));
+  c.launches += (long long)n_steps * c.nodesForward;
+  if (checkLaunch(c)) return 1;
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  double J = 0.0;
+  if (functional) {
+    std::vector<double> vals;
+    if (reduceRegion(c, 4 * n_steps, vals)) return 1;
+    for (int s = 0; s < n_steps; ++s)
+      for (int i = 0; i < 4; ++i) J = J + kRkNorm[i] * c.stepDt[s] * vals[(size_t)4 * s + i];
+  }
+  *cost = J;
+  return 0;
+}
+
+static int regionRunAdjoint(Context& c, double* sensitivity) {
+  const int nU = c.nU, nD = c.nD, T = c.runSteps, S = c.saveInterval;
+  const double dtT = c.stepDt[T - 1];
+  // stage slots: full (state, primitives, stress, heat flux) when they fit in half the free memory
+  size_t freeB = 0, totalB = 0;
+  CUDA_TRY(c, cudaMemGetInfo(&freeB, &totalB));
+  long long pts = 0, held = 0;
+  for (DevBlock& b : c.blocks) {
+    pts += b.v.N;
+    held += b.runStageCap;
+  }
+  const long long fullPer = nU + PrimLayout{nD}.count() + nD * nD + nD;
+  const bool full = (double)(4LL * S * fullPer * pts) * sizeof(double) <= 0.5 * ((double)freeB + held * 8.0);
+  for (DevBlock& b : c.blocks) {
+    const long long stride = (full ? fullPer : nU) * b.v.N;
+    if (growDevice(c, &b.runStage, &b.runStageCap, 4LL * S * stride)) return 1;
+  }
+  // the slot stride differs per block: the run scalars and the references carry each block's
+  c.slotFull = full ? 1 : 0;
+  const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
+  std::vector<RunScalars> rs;
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+    RunScalars r = blockRunScalars(c, c.blocks[bi], bi == 0);
+    r.slotFull = c.slotFull;
+    r.slotStride = (full ? fullPer : nU) * c.blocks[bi].v.N;
+    rs.push_back(r);
+  }
+  BlockRefs refs = runRefs(c);
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) refs.slotStride[bi] = rs[bi].slotStride;
+  for (DevBlock& b : c.blocks) {
+    launchPrims(c, b, b.v.q, false);
+    launchAdjointInitial(c, b, c.opts.adjoint_forcing_switch ? -dtT / 6.0 : 0.0);
+  }
+  if (capture(c, &c.gRecomputeH[0], &c.nodesRecompute, [&]() {
+        for (int i = 1; i <= 4; ++i) regionRunStage(c, rs, i, controller, true, false);
+        launchStepAdvance(c, 1);
+      }))
+    return 1;
+  if (capture(c, &c.gAdjointH[0], &c.nodesAdjoint, [&]() {
+        for (int i = 4; i >= 1; --i) {
+          if (!full)
+            for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+              DevBlock& b = c.blocks[bi];
+              launchPrims(c, b, nullptr, true, &rs[bi], i);
+              if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs[bi], i, false);
+            }
+          for (size_t bi = 0; bi < c.blocks.size(); ++bi)
+            launchInterfaceSatAdjoint(c, c.blocks[bi], refs, &rs[bi], i, full);
+          for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+            DevBlock& b = c.blocks[bi];
+            launchDissipation(c, b, b.v.lam, -1.0);
+            launchGradientSensitivity(c, b, rs[bi], i);
+            launchAdjointCore(c, b, rs[bi], i, full);
+            launchAdjointDiffusion(c, b);
+          }
+          for (size_t bi = 0; bi < c.blocks.size(); ++bi)
+            launchAdjointAssemble(c, c.blocks[bi], i, rs[bi], i, 0.0, false, full);
+        }
+        launchStepAdvance(c, -1);
+      }))
+    return 1;
+  const int nSeg = (T + S - 1) / S;
+  for (int k = nSeg - 1; k >= 0; --k) {
+    const int L = k * S, end = std::min(T, L + S);
+    for (DevBlock& b : c.blocks) {
+      CUDA_TRY(c, cudaMemcpyAsync(b.v.q, b.runSnap + (size_t)k * nU * b.v.N, (size_t)nU * b.v.N * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, c.stream));
+      launchPrims(c, b, b.v.q, false);
+    }
+    launchSetCounters(c.dCounters, L + 1, L, c.stream);
+    for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gRecomputeH[0], c.stream));
+    launchSetCounters(c.dCounters, end, L, c.stream);
+    for (int s = end; s >= L + 1; --s) CUDA_TRY(c, cudaGraphLaunch(c.gAdjointH[0], c.stream));
+    c.launches += (long long)(end - L) * (c.nodesRecompute + c.nodesAdjoint);
+  }
+  if (checkLaunch(c)) return 1;
+  std::vector<double> vals;
+  if (reduceRegion(c, 4 * T, vals)) return 1;
+  double sum = 0.0;
+  for (int n = T; n >= 1; --n)
+    for (int i = 4; i >= 1; --i) {
+      const long long entry = (long long)(T - n) * 4 + (4 - i);
+      sum = sum + kRkNorm[i - 1] * c.stepDt[n - 1] * vals[entry];
+    }
+  *sensitivity = sum;
+  return 0;
+}
+
 int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, double* cost) {
   Context& c = h->c;
   if (requireReady(c)) return 1;
-  if (!singleBlock(c)) return fail(c, "checkpointed runs support one block without block interfaces");
   if (n_steps < 1) return fail(c, "n_steps must be >= 1");
   if (save_interval < 1) save_interval = n_steps;
+  if (!singleBlock(c)) return regionRunForward(c, n_steps, save_interval, t0, cost);
   DevBlock& b = c.blocks[0];
   if (prepareForwardRun(c, n_steps, save_interval, t0, true)) return 1;
   const bool cflMode = c.opts.use_constant_cfl != 0;
@@ -1738,8 +1945,8 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
 int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   Context& c = h->c;
   if (requireReady(c)) return 1;
-  if (!singleBlock(c)) return fail(c, "checkpointed runs support one block without block interfaces");
   if (c.runSteps < 1) return fail(c, "mgd_run_adjoint needs a preceding mgd_run_forward");
+  if (!singleBlock(c)) return regionRunAdjoint(c, sensitivity);
   DevBlock& b = c.blocks[0];
   const long long N = b.v.N;
   const int nU = c.nU, T = c.runSteps, S = c.saveInterval;

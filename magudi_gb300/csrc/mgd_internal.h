@@ -109,6 +109,8 @@ struct BlockRefs {
   const double* lam[MGD_MAX_BLOCKS];
   const double* ifVisc[MGD_MAX_BLOCKS];
   long long N[MGD_MAX_BLOCKS];
+  const double* stage[MGD_MAX_BLOCKS];  // stage buffers of a run (slots of all blocks share counters)
+  long long slotStride[MGD_MAX_BLOCKS];
 };
 
 // Thread-block tiling of a block's points: blocks of t[0] x t[1] x t[2]
@@ -171,6 +173,13 @@ struct DevBlock {
   std::vector<void*> allocations;
   int nStagePartialBlocks = 0;
   int nInterfaceEntries = 0;
+  // buffers of multi-block checkpointed runs
+  double* runSnap = nullptr;
+  long long runSnapCap = 0;
+  double* runStage = nullptr;
+  long long runStageCap = 0;
+  double* runPartials = nullptr;
+  long long runPartialCap = 0;
   std::vector<double> hostIfaceInv, hostIfaceVis;  // own interface penalties per SAT entry
   std::vector<int> hostFfPoint, hostFfSigned;
   // host copies kept for setup
@@ -340,7 +349,8 @@ void launchAxpy(Context& c, double* z, const double* x, double a, long long n, b
 // Block-interface SAT vectors of block b's interface entries (forward; adjoint
 // with the interface terms of the adjoint viscous diffusion).
 void launchInterfaceSat(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_t s = 0);
-void launchInterfaceSatAdjoint(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_t s = 0);
+void launchInterfaceSatAdjoint(Context& c, DevBlock& b, const BlockRefs& r, const RunScalars* rs = nullptr,
+                               int stage = 1, bool fromSlot = false, cudaStream_t s = 0);
 // Terminal kinetic energy of the current state into out[0] (norm = H det per point).
 void launchKineticEnergy(Context& c, DevBlock& b, const double* norm, double* partials, double* out);
 void launchKineticEnergyAdjointInitial(Context& c, DevBlock& b);

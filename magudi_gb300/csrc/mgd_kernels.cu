@@ -1046,7 +1046,8 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSat(BlockView B, Physics P, 
 }
 
 template <int ND, bool VISC>
-__global__ void __launch_bounds__(kBlock) kInterfaceSatAdjoint(BlockView B, Physics P, BlockRefs R) {
+__global__ void __launch_bounds__(kBlock) kInterfaceSatAdjoint(BlockView B, Physics P, BlockRefs R, RunScalars rs,
+                                                                int stage, int fromSlot) {
   pdlEnter();
   const int e = blockIdx.x * kBlock + threadIdx.x;
   if (e >= B.ff.n || B.ff.kind[e] != SAT_INTERFACE) return;
@@ -1056,11 +1057,18 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSatAdjoint(BlockView B, Phys
   const int pb = B.ff.partnerBlock[e];
   const long long pp = B.ff.partnerPoint[e], NR = R.N[pb];
   const PrimLayout L{ND};
+  // forward state of both sides: the blocks' arrays, or their stage slots in a run
+  const FwdState fs = forwardState<ND>(B, rs, stage, fromSlot != 0);
+  const double* qRb = R.q[pb];
+  if (fromSlot) {
+    const int slot = ((*rs.step) - (*rs.segBase) - 1) * 4 + stage - 1;
+    qRb = R.stage[pb] + (long long)slot * R.slotStride[pb];
+  }
   double qL[nU], dq[nU], lamL[nU], lamR[nU], mL[ND], mR[ND];
   D dL[nU], dR[nU], roe[nU];
   for (int c = 0; c < nU; ++c) {
-    qL[c] = B.q[p + N * c];
-    const double qr = R.q[pb][pp + NR * c];
+    qL[c] = fs.q[p + N * c];
+    const double qr = qRb[pp + NR * c];
     dq[c] = qL[c] - qr;
     dL[c] = D(qL[c]);
     dL[c].d[c] = 1.0;
@@ -1077,11 +1085,11 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSatAdjoint(BlockView B, Phys
   double sat[nU];
   for (int c = 0; c < nU; ++c) sat[c] = 0.0;
   double u[ND], tau[ND * ND], hf[ND];
-  for (int d = 0; d < ND; ++d) u[d] = B.prim[p + N * L.u(d)];
-  const double v = B.prim[p + N * L.v()], T = B.prim[p + N * L.T()];
+  for (int d = 0; d < ND; ++d) u[d] = fs.prim[p + N * L.u(d)];
+  const double v = fs.prim[p + N * L.v()], T = fs.prim[p + N * L.T()];
   if (VISC) {
-    for (int c = 0; c < ND * ND; ++c) tau[c] = B.tau[p + N * c];
-    for (int d = 0; d < ND; ++d) hf[d] = B.hf[p + N * d];
+    for (int c = 0; c < ND * ND; ++c) tau[c] = fs.tau[p + N * c];
+    for (int d = 0; d < ND; ++d) hf[d] = fs.hf[p + N * d];
   }
   for (int side = 0; side < 2; ++side) {
     D A[nU * nU];
@@ -1112,7 +1120,7 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSatAdjoint(BlockView B, Phys
   }
   for (int c = 0; c < nU; ++c) B.ff.visc[(long long)e * nU + c] = sat[c];
   if (VISC) {
-    const double mu = B.prim[p + N * L.mu()], la = B.prim[p + N * L.la()], kd = B.prim[p + N * L.k()];
+    const double mu = fs.prim[p + N * L.mu()], la = fs.prim[p + N * L.la()], kd = fs.prim[p + N * L.k()];
     double* a = B.ff.ifAd + (long long)e * ND * nV;
     for (int l = 0; l < ND; ++l) {
       double ml[ND];
@@ -1612,16 +1620,20 @@ void launchInterfaceSat(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_
   }
 }
 
-void launchInterfaceSatAdjoint(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_t s) {
+void launchInterfaceSatAdjoint(Context& c, DevBlock& b, const BlockRefs& r, const RunScalars* rs, int stage,
+                               bool fromSlot, cudaStream_t s) {
   if (b.nInterfaceEntries == 0) return;
   const int G = gridFor(b.v.ff.n);
+  RunScalars x{};
+  if (rs) x = *rs;
+  const int fs = fromSlot ? 1 : 0;
   MGD_LAUNCH(c);
   if (c.nD == 2) {
-    if (c.phys.viscous) pdl(kInterfaceSatAdjoint<2, true>, G, kBlock, on(c, s), b.v, c.phys, r);
-    else pdl(kInterfaceSatAdjoint<2, false>, G, kBlock, on(c, s), b.v, c.phys, r);
+    if (c.phys.viscous) pdl(kInterfaceSatAdjoint<2, true>, G, kBlock, on(c, s), b.v, c.phys, r, x, stage, fs);
+    else pdl(kInterfaceSatAdjoint<2, false>, G, kBlock, on(c, s), b.v, c.phys, r, x, stage, fs);
   } else {
-    if (c.phys.viscous) pdl(kInterfaceSatAdjoint<3, true>, G, kBlock, on(c, s), b.v, c.phys, r);
-    else pdl(kInterfaceSatAdjoint<3, false>, G, kBlock, on(c, s), b.v, c.phys, r);
+    if (c.phys.viscous) pdl(kInterfaceSatAdjoint<3, true>, G, kBlock, on(c, s), b.v, c.phys, r, x, stage, fs);
+    else pdl(kInterfaceSatAdjoint<3, false>, G, kBlock, on(c, s), b.v, c.phys, r, x, stage, fs);
   }
 }
 

@@ -64,8 +64,24 @@ def test_two_block_rk4_substeps_match_oracle():
             assert rel_err(pair[0].get_field(bi, f), pair[1].get_field(bi, f)) < 1e-12
 
 
-def test_checkpointed_runs_refuse_multiblock():
+def test_multiblock_runs_refuse_cfl_mode():
     P = configs.two_block_2d()
+    P.options.use_constant_cfl = True
     s = Solver(P)
     with pytest.raises(MagudiError):
         s.run_forward(4, 2)
+
+
+@pytest.mark.parametrize("rotate", [False, True])
+def test_two_block_runs_match_oracle(rotate):
+    """Checkpointed forward and adjoint runs across a block interface."""
+    P = configs.two_block_2d(functional=True, rotate_second=rotate, n_steps=40, dt=0.05)
+    g, o = Solver(P), oracle_lib.Oracle(P)
+    Jg, Jo = g.run_forward(P.n_steps, 7), o.run_forward(P.n_steps, 7)
+    assert abs(Jg - Jo) <= 1e-10 * abs(Jo)
+    for bi in (1, 2):
+        assert rel_err(g.get_field(bi, capi.FIELD_CONSERVED), o.get_field(bi, capi.FIELD_CONSERVED)) < 1e-11
+    Gg, Go = g.run_adjoint(), o.run_adjoint()
+    assert abs(Gg - Go) <= 1e-10 * abs(Go)
+    n = 4 * P.n_steps
+    assert rel_err(g.gradient(n), o.gradient(n)) < 1e-10
