@@ -42,7 +42,8 @@ enum {
   MGD_PATCH_SLIP_WALL = 5,         /* SAT_SLIP_WALL: t_ImpenetrableWall */
   MGD_PATCH_ISOTHERMAL_WALL = 6,   /* SAT_ISOTHERMAL_WALL */
   MGD_PATCH_ADIABATIC_WALL = 7,    /* SAT_ADIABATIC_WALL */
-  MGD_PATCH_BLOCK_INTERFACE = 8    /* SAT_BLOCK_INTERFACE */
+  MGD_PATCH_BLOCK_INTERFACE = 8,   /* SAT_BLOCK_INTERFACE */
+  MGD_PATCH_SOLENOIDAL_EXCITATION = 9 /* SOLENOIDAL_EXCITATION */
 };
 
 /* Fields that mgd_set_field / mgd_get_field move between host and device. */
@@ -123,6 +124,19 @@ typedef struct {
   char conforms_with[MGD_NAME_LEN];  /* block interfaces: patches/<name>/conforms_with */
   int interface_index[3];            /* patches/<name>/interface_index1..3 (0 = default 1,2,3)
                                         (src/InterfaceHelperImpl.f90:3-113) */
+  /* Solenoidal excitation (src/SolenoidalExcitationPatchImpl.f90:3-120):
+     patches/<name>/number_of_modes, origin_x/y, velocity_x/y, amplitude and
+     radius, and the modes the reference draws at setup: angular_frequencies
+     (n_modes) and phases (n_modes x 3, mode index fastest), already scaled
+     as its setup scales them (2 pi frequency (l + r_l - 1/2) / (n_modes / 2)
+     and 2 pi r). The arrays are copied by mgd_add_patch. */
+  int n_modes;
+  double origin[2];
+  double velocity[2];
+  double amplitude;
+  double radius;
+  const double* angular_frequencies;
+  const double* phases;
 } mgd_patch_desc;
 
 /* acoustic_sourceNN/... (src/AcousticSourceImpl.f90:3-32). */

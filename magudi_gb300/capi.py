@@ -28,6 +28,7 @@ PATCH_SLIP_WALL = 5
 PATCH_ISOTHERMAL_WALL = 6
 PATCH_ADIABATIC_WALL = 7
 PATCH_BLOCK_INTERFACE = 8
+PATCH_SOLENOIDAL_EXCITATION = 9
 
 PATCH_TYPES = {
     "SAT_FAR_FIELD": PATCH_SAT_FAR_FIELD,
@@ -38,6 +39,7 @@ PATCH_TYPES = {
     "SAT_ISOTHERMAL_WALL": PATCH_ISOTHERMAL_WALL,
     "SAT_ADIABATIC_WALL": PATCH_ADIABATIC_WALL,
     "SAT_BLOCK_INTERFACE": PATCH_BLOCK_INTERFACE,
+    "SOLENOIDAL_EXCITATION": PATCH_SOLENOIDAL_EXCITATION,
 }
 
 FIELD_CONSERVED = 0
@@ -101,6 +103,13 @@ class PatchDesc(C.Structure):
         ("wall_temperature", C.c_double),
         ("conforms_with", C.c_char * MGD_NAME_LEN),
         ("interface_index", C.c_int * 3),
+        ("n_modes", C.c_int),
+        ("origin", C.c_double * 2),
+        ("velocity", C.c_double * 2),
+        ("amplitude", C.c_double),
+        ("radius", C.c_double),
+        ("angular_frequencies", C.POINTER(C.c_double)),
+        ("phases", C.POINTER(C.c_double)),
     ]
 
 

@@ -213,6 +213,139 @@ def two_block_2d(nx1=25, nx2=29, ny=31, half_width=6.0, viscous=True, rotate_sec
     return Problem(options=opts, blocks=blocks, patches=patches, sources=sources, n_steps=n_steps, save_interval=5)
 
 
+def _tanh_cluster(n, beta, left=True):
+    """n points on [0, 1] clustered toward 0 (left) or 1 by a tanh mapping."""
+    s = np.linspace(0.0, 1.0, n)
+    if left:
+        return 1.0 - np.tanh(beta * (1.0 - s)) / np.tanh(beta)
+    return np.tanh(beta * s) / np.tanh(beta)
+
+
+def jet_3block_3d(nx=384, ny_core=192, ny_side=171, nz=192, mach=1.3, reynolds=2500.0, theta=0.04, cfl=0.5,
+                  dt=None, n_steps=1000, save_interval=None, length=20.0, core_half_width=2.0, side_extent=8.0,
+                  flare=0.5, sponge_points=None, excitation_modes=8, excitation_amplitude=1e-3, seed=2022,
+                  dissipation_amount=0.01, target=(2.5, 1.6, 0.3, 1.0), side_beta=1.0):
+    """Three-block curvilinear jet (the 3D multi-block jet workload).
+
+    Axial direction x (index i, `nx` points, tanh-clustered toward the inflow
+    over [0, length]); cross-stream y (index j) and z (index k). Block 1 is
+    the core, |y|, |z| <= core_half_width (ny_core x nz, uniform); blocks 2
+    and 3 are shear-layer blocks below and above it in y out to side_extent
+    (ny_side points, tanh-clustered toward the core), sharing the core's z
+    points. All three blocks carry the flare mapping y, z -> (y, z)(1 + flare
+    x / length), so every grid is curvilinear (non-orthogonal), and the
+    blocks meet at two SAT_BLOCK_INTERFACE pairs. With the defaults the point
+    count is 384 x 192 x 192 + 2 x 384 x 171 x 192 = 39.4 M, the point count
+    of a 192^2 x 384 core with two 128 x 256 x 384 shear-layer blocks.
+
+    Flow: a Mach `mach` round jet of diameter 1 along x (top hat with a tanh
+    shear layer of momentum thickness theta), rho = 1 and p = 1/gamma
+    everywhere, Re = `reynolds`. A SOLENOIDAL_EXCITATION patch (8 modes,
+    amplitude 1e-3, seeded) forces the core near the inflow, convected at
+    0.65 of the jet speed. The cost functional is the squared pressure on a
+    cylindrical shell target in all blocks, target = (axial centre, radius,
+    radial width, axial width) of its Gaussian mollifier; the
+    control is a thermal actuator on an annulus at the nozzle lip in the
+    core. Far-field SATs on every outer face, sponges on the outflow and
+    lateral faces. dt defaults to `cfl` over the largest inviscid spectral
+    radius of the initial state.
+
+    The composite dissipation enters the RHS as amount * D_diss q * (1/det)
+    (addDissipation before the 1/det scaling, src/RhsHelperImpl.f90:10-87,
+    src/RegionImpl.f90:1968-1976), so its explicit stability limit tightens
+    with the cell volume: with D_diss's interior spectral radius 1 per
+    direction, RK4 needs roughly 3 dt amount / det < 2.8. The amount is
+    therefore capped at 0.5 det_min / dt (det estimated from the grid-line
+    spacings); on the full 39.4 M-point grid that cap, not 0.01, applies."""
+    gamma = 1.4
+    U = mach  # ambient sound speed 1
+    L, Yc, Ys = length, core_half_width, side_extent
+    x = L * _tanh_cluster(nx, 1.2)
+    yc = np.linspace(-Yc, Yc, ny_core)
+    z = np.linspace(-Yc, Yc, nz)
+    y_up = Yc + (Ys - Yc) * _tanh_cluster(ny_side, side_beta)
+    ys = (yc, -y_up[::-1], y_up)
+    opts = Options(
+        n_dimensions=3, viscous=True, dissipation=True, composite_dissipation=True, curvilinear=True,
+        use_constant_cfl=False, time_step_size=0.0, enable_controller=True, enable_functional=True,
+        ratio_of_specific_heats=gamma, reynolds_number=reynolds, prandtl_number=0.72,
+        viscosity_power_law_exponent=0.666, bulk_viscosity_ratio=0.6, dissipation_amount=dissipation_amount)
+    blocks = []
+    smax, vmin = 0.0, np.inf
+    for yy in ys:
+        Z, Y, X = np.meshgrid(z, yy, x, indexing="ij")  # (nz, ny, nx): point = i + nx (j + ny k)
+        f = 1.0 + flare * X / L
+        coords = np.stack([X.ravel(), (Y * f).ravel(), (Z * f).ravel()])
+        N = coords.shape[1]
+        r = np.sqrt(coords[1] ** 2 + coords[2] ** 2)
+        u = 0.5 * U * (1.0 - np.tanh((r - 0.5) / (2.0 * theta)))
+        q = quiescent_state(N, 3, gamma)
+        q[1] = u
+        q[4] = q[4] + 0.5 * u * u
+        shape = (len(z), len(yy), len(x))
+        # inviscid spectral radius sum_d (|u_d| + c) / h_d with h_d the grid-line spacing
+        rad = np.zeros(shape)
+        vol = np.ones(shape)
+        for axis in (2, 1, 0):
+            d = np.sqrt(sum(np.diff(c.reshape(shape), axis=axis) ** 2 for c in coords))
+            h = np.concatenate([d, np.take(d, [-1], axis=axis)], axis=axis)
+            speed = (np.abs(u.reshape(shape)) if axis == 2 else 0.0) + 1.0
+            rad += speed / h
+            vol *= h
+        smax = max(smax, float(rad.max()))
+        vmin = min(vmin, float(vol.min()))
+        tm = np.exp(-((r - target[1]) / target[2]) ** 2 - ((coords[0] - target[0]) / target[3]) ** 2)
+        mc = np.exp(-((r - 0.5) / 0.15) ** 2 - ((coords[0] - 0.4) / 0.25) ** 2)
+        blocks.append(Block(grid_size=(nx, len(yy), nz), coordinates=np.ascontiguousarray(coords),
+                            initial_state=q.copy(), target_state=q.copy(), control_mollifier=mc,
+                            target_mollifier=tm, mean_pressure=np.full(N, 1.0 / gamma)))
+    if dt is None:
+        dt = cfl / smax
+    opts.time_step_size = float(dt)
+    opts.dissipation_amount = float(min(dissipation_amount, 0.5 * vmin / dt))
+    s = sponge_points or max(4, nx // 24)
+    sl = max(4, min(ny_side, nz) // 12)
+    patches = []
+    for b in (1, 2, 3):
+        patches += [
+            Patch(f"inflow{b}", "SAT_FAR_FIELD", b, 1, (1, 1, 1, -1, 1, -1)),
+            Patch(f"outflow{b}", "SAT_FAR_FIELD", b, -1, (-1, -1, 1, -1, 1, -1)),
+            Patch(f"farField.B{b}", "SAT_FAR_FIELD", b, 3, (1, -1, 1, -1, 1, 1)),
+            Patch(f"farField.F{b}", "SAT_FAR_FIELD", b, -3, (1, -1, 1, -1, -1, -1)),
+            Patch(f"sponge.out{b}", "SPONGE", b, -1, (-s, -1, 1, -1, 1, -1), sponge_amount=0.2),
+            Patch(f"sponge.B{b}", "SPONGE", b, 3, (1, -1, 1, -1, 1, sl), sponge_amount=0.2),
+            Patch(f"sponge.F{b}", "SPONGE", b, -3, (1, -1, 1, -1, -sl, -1), sponge_amount=0.2),
+            Patch(f"target{b}", "COST_TARGET", b, 0, (1, -1, 1, -1, 1, -1)),
+        ]
+    # cross-stream (j) indices of the actuator box |y|, |z| <= 0.85 in the core
+    jlo = int(np.searchsorted(yc, -0.85)) + 1
+    jhi = int(np.searchsorted(yc, 0.85))
+    klo = int(np.searchsorted(z, -0.85)) + 1
+    khi = int(np.searchsorted(z, 0.85))
+    ihi = max(2, int(np.searchsorted(x, 1.2)))
+    iexc = max(2, int(np.searchsorted(x, 2.0)))
+    patches += [
+        Patch("farField.S", "SAT_FAR_FIELD", 2, 2, (1, -1, 1, 1, 1, -1)),
+        Patch("farField.N", "SAT_FAR_FIELD", 3, -2, (1, -1, -1, -1, 1, -1)),
+        Patch("sponge.S", "SPONGE", 2, 2, (1, -1, 1, sl, 1, -1), sponge_amount=0.2),
+        Patch("sponge.N", "SPONGE", 3, -2, (1, -1, -sl, -1, 1, -1), sponge_amount=0.2),
+        Patch("interface.1S", "SAT_BLOCK_INTERFACE", 1, 2, (1, -1, 1, 1, 1, -1), viscous_penalty_amount=0.5,
+              conforms_with="interface.2N"),
+        Patch("interface.2N", "SAT_BLOCK_INTERFACE", 2, -2, (1, -1, -1, -1, 1, -1), viscous_penalty_amount=0.5,
+              conforms_with="interface.1S"),
+        Patch("interface.1N", "SAT_BLOCK_INTERFACE", 1, -2, (1, -1, -1, -1, 1, -1), viscous_penalty_amount=0.5,
+              conforms_with="interface.3S"),
+        Patch("interface.3S", "SAT_BLOCK_INTERFACE", 3, 2, (1, -1, 1, 1, 1, -1), viscous_penalty_amount=0.5,
+              conforms_with="interface.1N"),
+        Patch("controlRegion", "ACTUATOR", 1, 0, (1, ihi, jlo, jhi, klo, khi)),
+        Patch("excitationSupport", "SOLENOIDAL_EXCITATION", 1, 0, (1, iexc, 1, -1, 1, -1),
+              n_modes=excitation_modes, origin=(0.75, 0.0), velocity=(0.65 * U, 0.0),
+              amplitude=excitation_amplitude, frequency=0.4 * U, radius=1.0, random_seed=seed),
+    ]
+    S = save_interval or max(1, int(round((n_steps / 4.0) ** 0.5)))
+    return Problem(options=opts, blocks=blocks, patches=patches, sources=[], n_steps=n_steps, save_interval=S)
+
+
 def random_state(n_points, n_dimensions, gamma, rng):
     """full_rhs.f90:289-301: rho in U[0.01,10], u in U[-10,10], p in U[0.01,10]/gamma."""
     nU = n_dimensions + 2

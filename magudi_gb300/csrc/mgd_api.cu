@@ -140,6 +140,8 @@ int mgd_create(const mgd_options* o, mgd_ctx** out) {
   cudaMemcpy(c.dCounters, init, sizeof init, cudaMemcpyHostToDevice);
   cudaMalloc((void**)&c.dApiAmp, MGD_MAX_SOURCES * sizeof(double));
   cudaMemset(c.dApiAmp, 0, MGD_MAX_SOURCES * sizeof(double));
+  cudaMalloc((void**)&c.dApiTime, sizeof(double));
+  cudaMemset(c.dApiTime, 0, sizeof(double));
   if (cudaGetLastError() != cudaSuccess) {
     g_createError = "device allocation failed";
     delete h;
@@ -164,6 +166,7 @@ int mgd_destroy(mgd_ctx* h) {
     cudaFree(b.runPartials);
   }
   cudaFree(c.dCounters); cudaFree(c.dApiAmp); cudaFree(c.dAmp); cudaFree(c.dForcing);
+  cudaFree(c.dApiTime); cudaFree(c.dStageTime);
   cudaFree(c.dGradient); cudaFree(c.dPartials); cudaFree(c.dStageValues);
   cudaFree(c.dSnapshots); cudaFree(c.dStageBuf);
   cudaFree(c.dStepDt); cudaFree(c.dDtPartials); cudaFree(c.dTime); cudaFree(c.dNorm);
@@ -426,10 +429,30 @@ int mgd_add_block(mgd_ctx* h, const mgd_block_desc* desc, const double* coordina
 int mgd_add_patch(mgd_ctx* h, const mgd_patch_desc* p) {
   Context& c = h->c;
   if (c.finalized) return fail(c, "mgd_add_patch after mgd_finalize_setup");
-  if (p->type < MGD_PATCH_SAT_FAR_FIELD || p->type > MGD_PATCH_BLOCK_INTERFACE)
+  if (p->type < MGD_PATCH_SAT_FAR_FIELD || p->type > MGD_PATCH_SOLENOIDAL_EXCITATION)
     return fail(c, std::string("unsupported patch type for patch '") + p->name + "'");
   if (p->grid_index < 1) return fail(c, "patch grid index must be >= 1");
+  std::vector<double> omega, phases;
+  if (p->type == MGD_PATCH_SOLENOIDAL_EXCITATION) {
+    // src/SolenoidalExcitationPatchImpl.f90:40-50 (number_of_modes clipped at 0)
+    const int nM = std::max(0, p->n_modes);
+    if (nM > kMaxExcitationModes)
+      return fail(c, std::string("patch '") + p->name + "': more than " + std::to_string(kMaxExcitationModes) +
+                         " excitation modes");
+    if (nM > 0 && (!p->angular_frequencies || !p->phases))
+      return fail(c, std::string("patch '") + p->name + "': the excitation modes are missing");
+    if (!(p->radius > 0.0)) return fail(c, std::string("patch '") + p->name + "': radius must be positive");
+    if (nM > 0) {
+      omega.assign(p->angular_frequencies, p->angular_frequencies + nM);
+      phases.assign(p->phases, p->phases + 3 * nM);
+    }
+  }
   c.patches.push_back(*p);
+  c.patches.back().n_modes = std::max(0, p->n_modes);
+  c.patches.back().angular_frequencies = nullptr;  // copied below; the caller's arrays may go
+  c.patches.back().phases = nullptr;
+  c.patchOmega.push_back(std::move(omega));
+  c.patchPhases.push_back(std::move(phases));
   return 0;
 }
 
@@ -640,6 +663,103 @@ int autotuneTile(Context& c, DevBlock& b, int kernel, const int (*cands)[3], int
 // mollifierTotals holds the control and target mollifier quadratures over all
 // blocks (normalizeControlMollifier / normalizeTargetMollifier,
 // src/RegionImpl.f90:459-603, sum over every block).
+// Solenoidal-excitation entries of block bi (setupSolenoidalExcitationPatch,
+// src/SolenoidalExcitationPatchImpl.f90:93-130): the non-hole points of each
+// patch with its strength amplitude exp(-g |x - x0|^2), g = 9 / (2 radius^2),
+// the offsets from the origin and the spatial functions of every mode, and a
+// dense map from grid point to entry.
+static int setupExcitation(Context& c, int bi, const std::vector<int>& exts) {
+  DevBlock& b = c.blocks[bi];
+  const long long N = b.v.N;
+  const int* gs = b.v.gs;
+  std::vector<int> idx;
+  struct HostPatch {
+    ExcPatch x;
+    size_t pi;
+    std::vector<double> S, dx, dy, cache;
+    std::vector<int> pts;
+  };
+  std::vector<HostPatch> hs;
+  int total = 0;
+  for (size_t pi = 0; pi < c.patches.size(); ++pi) {
+    const mgd_patch_desc& p = c.patches[pi];
+    if (p.type != MGD_PATCH_SOLENOIDAL_EXCITATION || p.grid_index != bi + 1 || p.n_modes <= 0) continue;
+    if (idx.empty()) idx.assign(N, -1);
+    HostPatch h;
+    h.pi = pi;
+    const int nM = p.n_modes;
+    const double g = 9.0 / (2.0 * p.radius * p.radius);
+    const std::vector<double>& w = c.patchOmega[pi];
+    const std::vector<double>& ph = c.patchPhases[pi];
+    bool overlap = false;
+    forExtent(&exts[6 * pi], gs, [&](long long gi, long long) {
+      if (b.hostIblank[gi] == 0) return;
+      if (idx[gi] >= 0) {
+        overlap = true;
+        return;
+      }
+      idx[gi] = total + (int)h.pts.size();
+      h.pts.push_back((int)gi);
+      const double dx = b.hostCoords[gi] - p.origin[0], dy = b.hostCoords[N + gi] - p.origin[1];
+      h.dx.push_back(dx);
+      h.dy.push_back(dy);
+      h.S.push_back(p.amplitude * std::exp(-g * (dx * dx + dy * dy)));
+    });
+    if (overlap) return fail(c, "overlapping solenoidal-excitation patches are not supported");
+    const long long nE = (long long)h.pts.size();
+    h.cache.assign((size_t)4 * nM * nE, 0.0);
+    for (long long e = 0; e < nE; ++e)
+      for (int l = 0; l < nM; ++l) {
+        const double a = w[l] * h.dx[e] + ph[l], d = w[l] * h.dy[e] + ph[nM + l];
+        h.cache[e + nE * l] = std::sin(a);
+        h.cache[e + nE * (nM + l)] = std::cos(a);
+        h.cache[e + nE * (2 * nM + l)] = std::sin(d);
+        h.cache[e + nE * (3 * nM + l)] = std::cos(d);
+      }
+    h.x.nE = (int)nE;
+    h.x.off = total;
+    h.x.nModes = nM;
+    h.x.g = g;
+    h.x.speed[0] = p.velocity[0];
+    h.x.speed[1] = p.velocity[1];
+    total += (int)nE;
+    hs.push_back(std::move(h));
+  }
+  b.exc.clear();
+  if (hs.empty()) return 0;
+  int* dIdx = nullptr;
+  double* dF = nullptr;
+  cudaError_t e = cudaSuccess;
+  auto chk = [&](cudaError_t x) { if (x != cudaSuccess) e = x; };
+  chk(devAlloc(b, &dIdx, N));
+  chk(devAlloc(b, &dF, 3LL * total));
+  for (HostPatch& h : hs) {
+    double *w, *S, *dx, *dy, *cache;
+    int* pts;
+    const long long nE = h.x.nE;
+    chk(devAlloc(b, &w, h.x.nModes));
+    chk(devAlloc(b, &S, nE));
+    chk(devAlloc(b, &dx, nE));
+    chk(devAlloc(b, &dy, nE));
+    chk(devAlloc(b, &cache, 4LL * h.x.nModes * nE));
+    chk(devAlloc(b, &pts, nE));
+    if (e != cudaSuccess) break;
+    chk(cudaMemcpy(w, c.patchOmega[h.pi].data(), h.x.nModes * sizeof(double), cudaMemcpyHostToDevice));
+    chk(cudaMemcpy(S, h.S.data(), nE * sizeof(double), cudaMemcpyHostToDevice));
+    chk(cudaMemcpy(dx, h.dx.data(), nE * sizeof(double), cudaMemcpyHostToDevice));
+    chk(cudaMemcpy(dy, h.dy.data(), nE * sizeof(double), cudaMemcpyHostToDevice));
+    chk(cudaMemcpy(cache, h.cache.data(), h.cache.size() * sizeof(double), cudaMemcpyHostToDevice));
+    chk(cudaMemcpy(pts, h.pts.data(), nE * sizeof(int), cudaMemcpyHostToDevice));
+    h.x.omega = w; h.x.S = S; h.x.dx = dx; h.x.dy = dy; h.x.cache = cache; h.x.point = pts;
+    b.exc.push_back(h.x);
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(dIdx, idx.data(), N * sizeof(int), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return fail(c, std::string("solenoidal-excitation setup failed: ") + cudaGetErrorString(e));
+  b.v.excIdx = dIdx;
+  b.v.excF = dF;
+  return 0;
+}
+
 static int finalizeBlock(Context& c, int bi, const double* mollifierTotals) {
   DevBlock& b = c.blocks[bi];
   const int nD = c.nD, nU = c.nU;
@@ -667,6 +787,7 @@ static int finalizeBlock(Context& c, int bi, const double* mollifierTotals) {
     }
     exts.insert(exts.end(), e, e + 6);
   }
+  if (setupExcitation(c, bi, exts)) return 1;
   // sponge strengths (computeSpongeStrengths, src/PatchFactoryImpl.f90:161-374)
   std::vector<double> sponge(N, 0.0);
   for (size_t pi = 0; pi < c.patches.size(); ++pi) {
@@ -1168,6 +1289,7 @@ static RunScalars apiScalars(Context& c) {
   r.step = c.dCounters + 2;
   r.segBase = c.dCounters + 3;
   r.amp = c.dApiAmp;
+  r.stageTime = c.dApiTime;
   setStepSize(r, c.opts.time_step_size);
   r.adjointForcingSwitch = c.opts.adjoint_forcing_switch;
   r.nPartialBlocks = reductionBlocks(c.blocks[0]);
@@ -1182,6 +1304,8 @@ static int setApiTime(Context& c, double time) {
     amp[s] = src.amplitude * std::cos(2.0 * pi * src.frequency * time + src.phase);
   }
   CUDA_TRY(c, cudaMemcpyAsync(c.dApiAmp, amp, sizeof amp, cudaMemcpyHostToDevice, c.stream));
+  // pageable source: the copy completes before the call returns
+  CUDA_TRY(c, cudaMemcpyAsync(c.dApiTime, &time, sizeof time, cudaMemcpyHostToDevice, c.stream));
   return 0;
 }
 
@@ -1199,15 +1323,16 @@ void forwardStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bo
                   bool functional, const Lanes* lanes) {
   const Lanes L = lanes ? *lanes : Lanes{c.stream, c.side, c.evFork[0], c.evJoin[0]};
   const int stage = api ? 1 : rkStage;
-  const bool diss = c.phys.dissipation != 0;
-  if (diss) {
+  const bool diss = c.phys.dissipation != 0, exc = !b.exc.empty();
+  if (diss || exc) {
     cudaEventRecord(L.fork, L.main);
     cudaStreamWaitEvent(L.side, L.fork, 0);
-    launchDissipation(c, b, b.v.q, 1.0, L.side);
+    if (diss) launchDissipation(c, b, b.v.q, 1.0, L.side);
+    if (exc) launchExcitation(c, b, rs, stage, false, false, L.side);
     cudaEventRecord(L.join, L.side);
   }
   launchGradFlux(c, b, true, false, &rs, stage, store, L.main);
-  if (diss) cudaStreamWaitEvent(L.main, L.join, 0);
+  if (diss || exc) cudaStreamWaitEvent(L.main, L.join, 0);
   launchForwardDivergence(c, b, rkStage, rs, api, controller, L.main);
   if (rkStage > 0) launchPrims(c, b, b.v.q, false, nullptr, 0, L.main);
   if (functional) launchFunctional(c, b, rs, stage, L.main);
@@ -1220,12 +1345,14 @@ void forwardStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bo
 void adjointStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage, double apiFactor, bool api,
                   bool fromSlot, bool record, const Lanes* lanes) {
   const Lanes L = lanes ? *lanes : Lanes{c.stream, c.side, c.evFork[1], c.evJoin[1]};
-  const bool side = c.phys.dissipation != 0 || record;
+  const bool exc = !b.exc.empty();
+  const bool side = c.phys.dissipation != 0 || record || exc;
   if (side) {
     cudaEventRecord(L.fork, L.main);
     cudaStreamWaitEvent(L.side, L.fork, 0);
-    launchDissipation(c, b, b.v.lam, -1.0, L.side);
+    if (c.phys.dissipation) launchDissipation(c, b, b.v.lam, -1.0, L.side);
     if (record) launchGradientSensitivity(c, b, rs, stage, L.side);
+    if (exc) launchExcitation(c, b, rs, stage, true, fromSlot, L.side);
     cudaEventRecord(L.join, L.side);
   }
   launchAdjointCore(c, b, rs, stage, fromSlot, L.main);
@@ -1254,6 +1381,7 @@ void regionForwardStage(Context& c, int rkStage, const RunScalars& rs) {
   for (DevBlock& b : c.blocks) {
     launchDissipation(c, b, b.v.q, 1.0);
     launchGradFlux(c, b, true, false, &rs, 1, false);
+    launchExcitation(c, b, rs, 1, false, false);
   }
   for (DevBlock& b : c.blocks) launchInterfaceSat(c, b, refs);
   for (DevBlock& b : c.blocks) {
@@ -1270,6 +1398,7 @@ void regionAdjointStage(Context& c, int rkStage, const RunScalars& rs, double ap
   for (DevBlock& b : c.blocks) launchInterfaceSatAdjoint(c, b, refs);
   for (DevBlock& b : c.blocks) {
     launchDissipation(c, b, b.v.lam, -1.0);
+    launchExcitation(c, b, rs, 1, true, false);
     launchAdjointCore(c, b, rs, 1, false);
     launchAdjointDiffusion(c, b);
   }
@@ -1303,6 +1432,7 @@ int mgd_compute_rhs(mgd_ctx* h, int mode, double time, double adjoint_forcing_fa
     if (singleBlock(c)) forwardStage(c, b, 0, rs, true, false, false, false);
     else regionForwardStage(c, 0, rs);
   } else if (mode == MGD_ADJOINT) {
+    if (setApiTime(c, time)) return 1;
     for (DevBlock& x : c.blocks) {
       launchPrims(c, x, x.v.q, false);
       if (c.phys.viscous) launchGradFlux(c, x, false, true, &rs, 1, false);
@@ -1410,6 +1540,9 @@ int mgd_rk4_substep(mgd_ctx* h, int mode, double* time, double dt, int stage) {
     else regionForwardStage(c, stage, rs);
   } else if (mode == MGD_ADJOINT) {
     const double factor = stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0);
+    // time of the matching forward stage: stages 4 and 2 run at the current
+    // time, stages 3 and 1 half a step earlier
+    if (setApiTime(c, (stage == 3 || stage == 1) ? *time - dt / 2.0 : *time)) return 1;
     for (DevBlock& x : c.blocks) {
       launchPrims(c, x, x.v.q, false);
       if (c.phys.viscous) launchGradFlux(c, x, false, true, &rs, 1, false);
@@ -1484,6 +1617,7 @@ static RunScalars runScalars(Context& c) {
   r.slotStride = c.slotStride;
   r.slotFull = c.slotFull;
   r.rk = c.dStepDt;
+  r.stageTime = c.dStageTime;
   setStepSize(r, c.opts.time_step_size);
   r.adjointForcingSwitch = c.opts.adjoint_forcing_switch;
   return r;
@@ -1587,9 +1721,11 @@ static int ensureShadow(Context& c, DevBlock& b) {
   };
   double* ffv = nullptr;
   cudaError_t e = cudaSuccess;
+  long long nExc = 0;
+  for (const ExcPatch& X : b.exc) nExc += X.nE;
   for (auto x : {alloc(&v.q, N * nU), alloc(&v.prim, N * PrimLayout{nD}.count()), alloc(&v.fhat, N * nD * nU),
                  alloc(&v.dq, N * nD * nU), alloc(&v.b1, N * nU), alloc(&v.b2, N * nU),
-                 alloc(&ffv, (long long)v.ff.n * nU)})
+                 alloc(&ffv, (long long)v.ff.n * nU), alloc(&v.excF, 3 * nExc)})
     if (x != cudaSuccess) e = x;
   if (e != cudaSuccess) return fail(c, std::string("device allocation failed for the recomputation: ") +
                                            cudaGetErrorString(e));
@@ -1624,6 +1760,13 @@ int prepareForwardRun(Context& c, int n_steps, int save_interval, double t0, boo
     CUDA_TRY(c, cudaMalloc((void**)&c.dAmp, nAmp * sizeof(double)));
     c.ampCapacity = nAmp;
   }
+  if (c.stageTimeCapacity < 4LL * n_steps) {
+    cudaFree(c.dStageTime);
+    c.dStageTime = nullptr;
+    c.stageTimeCapacity = 0;
+    CUDA_TRY(c, cudaMalloc((void**)&c.dStageTime, (size_t)4 * n_steps * sizeof(double)));
+    c.stageTimeCapacity = 4LL * n_steps;
+  }
   if (cflMode) {
     // step sizes, stage times and source amplitudes are produced on the device
     CUDA_TRY(c, cudaMemcpyAsync(c.dTime, &t0, sizeof(double), cudaMemcpyHostToDevice, c.stream));
@@ -1653,6 +1796,8 @@ int prepareForwardRun(Context& c, int n_steps, int save_interval, double t0, boo
         amp[k * nSrc + s] = src.amplitude * std::cos(2.0 * pi * src.frequency * c.stageTimes[k] + src.phase);
       }
     CUDA_TRY(c, cudaMemcpy(c.dAmp, amp.data(), nAmp * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(c, cudaMemcpy(c.dStageTime, c.stageTimes.data(), c.stageTimes.size() * sizeof(double),
+                           cudaMemcpyHostToDevice));
   }
   if (snapshots) {
     const long long nSnap = n_steps / save_interval + 2;
@@ -1781,6 +1926,7 @@ static void regionRunStage(Context& c, std::vector<RunScalars>& rs, int i, bool 
     DevBlock& b = c.blocks[bi];
     launchDissipation(c, b, b.v.q, 1.0);
     launchGradFlux(c, b, true, false, &rs[bi], i, store);
+    launchExcitation(c, b, rs[bi], i, false, false);
   }
   for (DevBlock& b : c.blocks) launchInterfaceSat(c, b, refs);
   for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
@@ -1879,6 +2025,7 @@ static int regionRunAdjoint(Context& c, double* sensitivity) {
           for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
             DevBlock& b = c.blocks[bi];
             launchDissipation(c, b, b.v.lam, -1.0);
+            launchExcitation(c, b, rs[bi], i, true, full);
             launchGradientSensitivity(c, b, rs[bi], i);
             launchAdjointCore(c, b, rs[bi], i, full);
             launchAdjointDiffusion(c, b);
@@ -1930,7 +2077,7 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
   RunScalars rs = runScalars(c);
   if (setCounters(c, 1, 0)) return 1;
   if (capture(c, &c.gForward, &c.nodesForward, [&]() {
-        if (cflMode) launchTimeStep(c, b, c.dDtPartials, c.dStepDt, c.dCounters, c.dTime, c.dAmp);
+        if (cflMode) launchTimeStep(c, b, c.dDtPartials, c.dStepDt, c.dCounters, c.dTime, c.dStageTime, c.dAmp);
         for (int i = 1; i <= 4; ++i) forwardStage(c, b, i, rs, false, controller, false, functional);
         launchSnapshot(c, b, c.dSnapshots, save_interval, false);
         launchStepAdvance(c, 1);
@@ -1962,6 +2109,7 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   DevBlock rb;
   rb.desc = b.desc;
   rb.v = twoLanes ? c.shadow : b.v;
+  rb.exc = b.exc;
   rb.tGrad = b.tGrad; rb.tDiss = b.tDiss; rb.tRhs = b.tRhs;
   rb.tAdjA = b.tAdjA; rb.tAdjD = b.tAdjD; rb.tAdjB = b.tAdjB;
   const Lanes adjLanes{c.stream, c.side, c.evFork[1], c.evJoin[1]};
@@ -2068,7 +2216,7 @@ int mgd_time_step_size(mgd_ctx* h, double* dt) {
   DevBlock& b = c.blocks[0];
   if (ensureStepBuffers(c, b, std::max(1, c.runSteps))) return 1;
   launchPrims(c, b, b.v.q, false);
-  launchTimeStep(c, b, c.dDtPartials, c.dTime, nullptr, nullptr, nullptr);
+  launchTimeStep(c, b, c.dDtPartials, c.dTime, nullptr, nullptr, nullptr, nullptr);
   if (checkLaunch(c)) return 1;
   CUDA_TRY(c, cudaMemcpyAsync(dt, c.dTime, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));

@@ -97,6 +97,10 @@ int mgd_batch_create(mgd_ctx* const* instances, int n_instances, mgd_batch** out
       g_batchCreateError = "batched runs use a constant time_step_size";
       return 1;
     }
+    if (!c.blocks[0].exc.empty()) {
+      g_batchCreateError = "batched runs do not take solenoidal-excitation patches";
+      return 1;
+    }
   }
   mgd_batch* b = new mgd_batch();
   b->inst.assign(instances, instances + n_instances);

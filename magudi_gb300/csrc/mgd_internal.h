@@ -100,6 +100,11 @@ struct BlockView {
   const int* actPts;      // grid point of each actuator-patch point, patch order
   int nAct;
   FarFieldEntries ff;
+  // solenoidal excitation: entry of each point (null when the block has none)
+  // and 3 values per entry for the current stage, written by kExcitation:
+  // forward (f_x, f_y, u . f), adjoint (its terms for components 0, 1, 2)
+  const int* excIdx;
+  double* excF;
 };
 
 // Arrays of every block of a context that the block-interface kernels read
@@ -147,6 +152,7 @@ struct RunScalars {
   double dt, h6, h3, h2;   // step size and dt/6, dt/3, dt/2 when rk is null
   const double* rk;        // per step (indexed by step - 1): dt, dt/6, dt/3, dt/2; or null
   int adjointForcingSwitch;
+  const double* stageTime; // time of each forward stage, (step-1)*4 + stage-1
 };
 
 // RK4 coefficients of the current step of a run (or of the per-call step).
@@ -165,9 +171,27 @@ inline void setStepSize(RunScalars& rs, double dt) {
   rs.h2 = dt / 2.0;
 }
 
+// One solenoidal-excitation patch of a block: its entries (non-hole patch
+// points, entry index off..off+nE-1 of the block) with the time-invariant
+// part of the forcing (setupSolenoidalExcitationPatch,
+// src/SolenoidalExcitationPatchImpl.f90:93-130): strength, offsets from the
+// origin and the spatial functions sin/cos(w (x - x0) + phi_1),
+// sin/cos(w (y - y0) + phi_2) of every mode (entry fastest).
+struct ExcPatch {
+  int nE = 0, off = 0, nModes = 0;
+  double g = 0, speed[2] = {0, 0};
+  const double* omega = nullptr;  // nModes
+  const double* S = nullptr;      // nE
+  const double* dx = nullptr;     // nE
+  const double* dy = nullptr;     // nE
+  const double* cache = nullptr;  // 4 * nModes * nE
+  const int* point = nullptr;     // grid point of each entry
+};
+
 struct DevBlock {
   mgd_block_desc desc;
   BlockView v;
+  std::vector<ExcPatch> exc;
   // tile shapes of the stage kernels, chosen by the autotuner
   Tile tGrad{}, tDiss{}, tRhs{}, tAdjA{}, tAdjD{}, tAdjB{};
   std::vector<void*> allocations;
@@ -212,6 +236,7 @@ struct Context {
   std::string error;
   std::vector<DevBlock> blocks;
   std::vector<mgd_patch_desc> patches;
+  std::vector<std::vector<double>> patchOmega, patchPhases;  // solenoidal-excitation modes per patch
   std::vector<mgd_acoustic_source> sources;
   bool finalized = false;
   bool hasInterfaces = false;
@@ -222,6 +247,9 @@ struct Context {
   // [4] step and [5] segBase of the checkpoint recomputation
   int* dCounters = nullptr;
   double* dApiAmp = nullptr;
+  double* dApiTime = nullptr;       // stage time of the per-call path
+  double* dStageTime = nullptr;     // time of every forward stage of the run
+  long long stageTimeCapacity = 0;
   double* dAmp = nullptr;           // per-stage source amplitudes of the run
   long long ampCapacity = 0;
   double* dForcing = nullptr;       // control forcing entries
@@ -324,6 +352,11 @@ void launchForwardDivergence(Context& c, DevBlock& b, int rkStage, const RunScal
 void launchFunctional(Context& c, DevBlock& b, const RunScalars& rs, int stage, cudaStream_t s = 0);
 // Adjoint: inviscid/viscous Jacobian-transpose products and viscous diffusion.
 void launchAdjointCore(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool fromSlot, cudaStream_t s = 0);
+// Solenoidal-excitation values of the stage into b.v.excF (forward: the
+// forcing and u . f of the current state; adjoint: the transpose terms of the
+// forward state of the stage, with lambda before the stage update).
+void launchExcitation(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool adjoint, bool fromSlot,
+                      cudaStream_t s = 0);
 // Adjoint: divergence of the viscous diffusion (per component).
 void launchAdjointDiffusion(Context& c, DevBlock& b, cudaStream_t s = 0);
 // Adjoint: final assembly, SATs, cost-target forcing and the RK4 adjoint update.
@@ -343,7 +376,7 @@ void launchReducePartials(Context& c, const double* partials, int stride, int co
 // dtOut[4 (*step - 1) + 0..3], advances *time over the step's four stages and
 // stores the stages' source amplitudes in amp.
 void launchTimeStep(Context& c, DevBlock& b, double* partials, double* dtOut, const int* step, double* time,
-                    double* amp, cudaStream_t s = 0);
+                    double* stageTime, double* amp, cudaStream_t s = 0);
 int timeStepBlocks(const DevBlock& b);
 void launchAxpy(Context& c, double* z, const double* x, double a, long long n, bool accumulate);
 // Block-interface SAT vectors of block b's interface entries (forward; adjoint
@@ -368,6 +401,7 @@ void launchBatchFunctional(Context& c, const BatchLaunch& L, int stage, cudaStre
 void launchStepAdvanceOn(int* counters, int delta, cudaStream_t s);
 void launchSetCounters(int* counters, int step, int segBase, cudaStream_t s);
 constexpr int kBatchThreads = 128;
+constexpr int kMaxExcitationModes = 256;  // modes of one solenoidal-excitation patch
 
 // Blocks of the fixed-layout reductions (functional, sensitivity).
 int reductionBlocks(const DevBlock& b);

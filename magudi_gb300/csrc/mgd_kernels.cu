@@ -530,6 +530,10 @@ __device__ __forceinline__ void forwardDivergencePoint(const BlockView& B, const
   const double q = B.q[kc];
   const double S = B.sponge[p];
   if (S != 0.0) r -= S * (q - B.qt[kc]);
+  if (B.excIdx && (c == 1 || c == 2 || c == E)) {
+    const int e = B.excIdx[p];
+    if (e >= 0) r += B.excF[3LL * e + (c == E ? 2 : c - 1)];
+  }
   if (c == E) {
     const int step = *rs.step;
     if (controller) {
@@ -810,6 +814,10 @@ __device__ __forceinline__ void adjointAssemblePoint(const BlockView& B, const P
   const double lam = B.lam[kc];
   const double S = B.sponge[p];
   if (S != 0.0) r += S * lam;
+  if (B.excIdx && c <= 2) {
+    const int e = B.excIdx[p];
+    if (e >= 0) r += B.excF[3LL * e + c];
+  }
   const double cnt = B.tgtCount[p];
   if (api) {
     if (cnt != 0.0 && apiFactor != 0.0) r += apiFactor * B.adjF[kc];
@@ -860,6 +868,71 @@ __device__ __forceinline__ void adjointAssemblePoint(const BlockView& B, const P
       B.lam[kc] = B.b2[kc] - h6 * r;
       break;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Solenoidal excitation of one patch (addSolenoidalExcitation,
+// src/SolenoidalExcitationPatchImpl.f90:159-278) at the stage's forward time.
+// Per entry: f = S sum_l [t1 (w t4 - 2 g dy t3), t3 (w t2 - 2 g dx t1)] with
+// t1..t4 = sin/cos(w (x - x0) + phi_1 - w c_x t), sin/cos(w (y - y0) + phi_2 - w c_y t)
+// formed from the cached spatial functions and the temporal functions, which
+// each thread block evaluates once into shared memory.
+// Forward: (f_x, f_y, u . f) for the x/y momentum and energy equations.
+// Adjoint: -(dR/dq)^T lambda of the energy term u . f,
+// (v (u . f) lambda_E, -v f_x lambda_E, -v f_y lambda_E) for components 0..2,
+// with the forward state of the stage and lambda before the stage update.
+// ---------------------------------------------------------------------------
+template <int ND>
+__global__ void __launch_bounds__(kBlock) kExcitation(BlockView B, ExcPatch X, RunScalars rs, int stage, int adjoint,
+                                                      int fromSlot) {
+  pdlEnter();
+  __shared__ double tf[4 * kMaxExcitationModes];
+  const int nM = X.nModes;
+  const double t = rs.stageTime[(long long)(*rs.step - 1) * 4 + (stage - 1)];
+  for (int l = threadIdx.x; l < nM; l += blockDim.x) {
+    double sn, cs;
+    sincos(X.omega[l] * X.speed[0] * t, &sn, &cs);
+    tf[l] = sn;
+    tf[nM + l] = cs;
+    sincos(X.omega[l] * X.speed[1] * t, &sn, &cs);
+    tf[2 * nM + l] = sn;
+    tf[3 * nM + l] = cs;
+  }
+  __syncthreads();
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= X.nE) return;
+  const long long nE = X.nE;
+  const double dx = X.dx[e], dy = X.dy[e], g2 = 2.0 * X.g;
+  double f1 = 0.0, f2 = 0.0;
+  for (int l = 0; l < nM; ++l) {
+    const double s1 = X.cache[e + nE * l], s2 = X.cache[e + nE * (nM + l)];
+    const double s3 = X.cache[e + nE * (2 * nM + l)], s4 = X.cache[e + nE * (3 * nM + l)];
+    const double t1 = s1 * tf[nM + l] - s2 * tf[l];
+    const double t2 = s2 * tf[nM + l] + s1 * tf[l];
+    const double t3 = s3 * tf[3 * nM + l] - s4 * tf[2 * nM + l];
+    const double t4 = s4 * tf[3 * nM + l] + s3 * tf[2 * nM + l];
+    const double w = X.omega[l];
+    f1 += t1 * (w * t4 - g2 * dy * t3);
+    f2 += t3 * (w * t2 - g2 * dx * t1);
+  }
+  const double S = X.S[e];
+  f1 = S * f1;
+  f2 = S * f2;
+  const long long N = B.N, p = X.point[e];
+  const PrimLayout L{ND};
+  double* out = B.excF + 3LL * (X.off + e);
+  if (!adjoint) {
+    out[0] = f1;
+    out[1] = f2;
+    out[2] = B.prim[p + N * L.u(0)] * f1 + B.prim[p + N * L.u(1)] * f2;
+    return;
+  }
+  const FwdState fs = forwardState<ND>(B, rs, stage, fromSlot != 0);
+  const double vl = fs.prim[p + N * L.v()] * B.lam[p + N * (ND + 1)];
+  const double uf = fs.prim[p + N * L.u(0)] * f1 + fs.prim[p + N * L.u(1)] * f2;
+  out[0] = vl * uf;
+  out[1] = -vl * f1;
+  out[2] = -vl * f2;
 }
 
 template <int ND, bool VISC>
@@ -1252,8 +1325,8 @@ struct SourceTable {
 
 __global__ void __launch_bounds__(256) kTimeStepFinalize(const double* __restrict__ partial, int n,
                                                          double* __restrict__ dtOut, const int* __restrict__ step,
-                                                         double* __restrict__ time, double* __restrict__ amp,
-                                                         SourceTable src) {
+                                                         double* __restrict__ time, double* __restrict__ stageTime,
+                                                         double* __restrict__ amp, SourceTable src) {
   pdlEnter();
   double v = kHugeStep;
   for (int i = threadIdx.x; i < n; i += blockDim.x) v = fmin(v, partial[i]);
@@ -1272,6 +1345,7 @@ __global__ void __launch_bounds__(256) kTimeStepFinalize(const double* __restric
   double t = *time;
   for (int i = 1; i <= 4; ++i) {
     if (i == 2 || i == 4) t = t + dt / 2.0;
+    if (stageTime) stageTime[(long long)(s - 1) * 4 + (i - 1)] = t;
     for (int k = 0; k < src.n; ++k) {
       const double arg = __dadd_rn(__dmul_rn(__dmul_rn(src.twoPi, src.frequency[k]), t), src.phase[k]);
       amp[((long long)(s - 1) * 4 + (i - 1)) * src.n + k] = src.amplitude[k] * cos(arg);
@@ -1455,6 +1529,17 @@ void launchForwardDivergence(Context& c, DevBlock& b, int rkStage, const RunScal
 void launchFunctional(Context& c, DevBlock& b, const RunScalars& rs, int stage, cudaStream_t s) {
   MGD_LAUNCH(c);
   pdl(kFunctional, reductionBlocks(b), kBlock, on(c, s), b.v, rs, stage, PrimLayout{c.nD}.p());
+}
+
+void launchExcitation(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool adjoint, bool fromSlot,
+                      cudaStream_t s) {
+  for (const ExcPatch& X : b.exc) {
+    if (X.nE == 0) continue;
+    const int grid = (X.nE + kBlock - 1) / kBlock;
+    MGD_LAUNCH(c);
+    if (c.nD == 2) pdl(kExcitation<2>, grid, kBlock, on(c, s), b.v, X, rs, stage, (int)adjoint, (int)fromSlot);
+    else pdl(kExcitation<3>, grid, kBlock, on(c, s), b.v, X, rs, stage, (int)adjoint, (int)fromSlot);
+  }
 }
 
 void launchGradientSensitivity(Context& c, DevBlock& b, const RunScalars& rs, int stage, cudaStream_t s) {
@@ -1652,7 +1737,7 @@ void launchKineticEnergyAdjointInitial(Context& c, DevBlock& b) {
 }
 
 void launchTimeStep(Context& c, DevBlock& b, double* partials, double* dtOut, const int* step, double* time,
-                    double* amp, cudaStream_t s) {
+                    double* stageTime, double* amp, cudaStream_t s) {
   const int nb = timeStepBlocks(b);
   MGD_LAUNCH(c);
   if (c.nD == 2) pdl(kTimeStepPartials<2>, nb, kBlock, on(c, s), b.v, c.phys, c.opts.cfl, partials);
@@ -1666,7 +1751,7 @@ void launchTimeStep(Context& c, DevBlock& b, double* partials, double* dtOut, co
     src.phase[k] = c.sources[k].phase;
   }
   MGD_LAUNCH(c);
-  pdl(kTimeStepFinalize, 1, 256, on(c, s), partials, nb, dtOut, step, time, amp, src);
+  pdl(kTimeStepFinalize, 1, 256, on(c, s), partials, nb, dtOut, step, time, stageTime, amp, src);
 }
 
 void launchCoordinateDerivative(Context& c, DevBlock& b, int dir, double* out) {

@@ -103,7 +103,11 @@ int mgd_forward_rhs_noalloc(mgd_ctx* h, const double* q, double time, double* rh
     const mgd_acoustic_source& src = c.sources[s];
     amp[s] = src.amplitude * std::cos(2.0 * pi * src.frequency * time + src.phase);
   }
-  e = cudaMemcpyAsync(scratch, amp, sizeof amp, cudaMemcpyHostToDevice, c.stream);
+  // the stage time follows the amplitudes (solenoidal excitation)
+  double head[MGD_MAX_SOURCES + 1];
+  std::memcpy(head, amp, sizeof amp);
+  head[MGD_MAX_SOURCES] = time;
+  e = cudaMemcpyAsync(scratch, head, sizeof head, cudaMemcpyHostToDevice, c.stream);
   if (e != cudaSuccess) {
     c.error = std::string("mgd_forward_rhs_noalloc: ") + cudaGetErrorString(e);
     return 1;
@@ -123,6 +127,7 @@ int mgd_forward_rhs_noalloc(mgd_ctx* h, const double* q, double time, double* rh
   rs.step = c.dCounters + 2;
   rs.segBase = c.dCounters + 3;
   rs.amp = scratch;
+  rs.stageTime = scratch + MGD_MAX_SOURCES;
   setStepSize(rs, c.opts.time_step_size);
   rs.adjointForcingSwitch = c.opts.adjoint_forcing_switch;
   rs.nPartialBlocks = reductionBlocks(b);

@@ -166,6 +166,20 @@ def patches_from_bc(d, rows):
                                                    d.get_float("defaults/viscous_penalty_amount", 0.5))
             p.conforms_with = d.get_str(key + "conforms_with", "")
             p.interface_index = tuple(d.get_int(key + f"interface_index{i}", i) for i in (1, 2, 3))
+        if ptype == "SOLENOIDAL_EXCITATION":
+            # src/SolenoidalExcitationPatchImpl.f90:40-62: number_of_modes, amplitude,
+            # frequency and radius are required; the modes are drawn from random_seed
+            for req in ("number_of_modes", "amplitude", "frequency", "radius"):
+                if d.get(key + req) is None:
+                    raise InputError(f"Required option '{key + req}' not found!")
+            p.n_modes = max(0, d.get_int(key + "number_of_modes", 0))
+            p.origin = (d.get_float(key + "origin_x", 0.0), d.get_float(key + "origin_y", 0.0))
+            p.velocity = (d.get_float(key + "velocity_x", 0.0), d.get_float(key + "velocity_y", 0.0))
+            p.amplitude = d.get_float(key + "amplitude", 0.0)
+            p.frequency = d.get_float(key + "frequency", 0.0)
+            p.radius = d.get_float(key + "radius", 1.0)
+            p.random_seed = d.get_int(key + "random_seed", -1)
+            p.randomize_frequency = d.get_bool(key + "randomize_frequency", True)
         if ptype == "SAT_ISOTHERMAL_WALL":
             # src/IsothermalWallImpl.f90:3-80: viscous_penalty_amount1, and the wall
             # temperature from the target state unless use_target_state is off

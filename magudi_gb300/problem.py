@@ -66,6 +66,27 @@ class Patch:
     wall_temperature: float = 0.0  # isothermal walls: <= 0 takes the target state's temperature
     conforms_with: str = ""        # block interfaces: name of the conforming patch
     interface_index: tuple = (0, 0, 0)  # block interfaces: index reordering (0 = 1, 2, 3)
+    # solenoidal excitation (patches/<name>/number_of_modes, origin_x/y, velocity_x/y,
+    # amplitude, frequency, radius, random_seed, randomize_frequency)
+    n_modes: int = 0
+    origin: tuple = (0.0, 0.0)
+    velocity: tuple = (0.0, 0.0)
+    amplitude: float = 0.0
+    frequency: float = 0.0
+    radius: float = 1.0
+    random_seed: int = -1
+    randomize_frequency: bool = True
+    # explicit modes (angular frequencies (n_modes), phases (n_modes, 3)) override the seeded draw
+    angular_frequencies: object = None
+    phases: object = None
+
+    def excitation_modes(self):
+        """Angular frequencies (n_modes) and phases (n_modes, 3) of a solenoidal
+        excitation patch: the explicit arrays when given, else `solenoidal_modes`."""
+        if self.angular_frequencies is not None:
+            return (np.ascontiguousarray(self.angular_frequencies, dtype=np.float64),
+                    np.asarray(self.phases, dtype=np.float64).reshape(self.n_modes, 3))
+        return solenoidal_modes(self.n_modes, self.frequency, self.random_seed, self.randomize_frequency)
 
     def to_c(self) -> capi.PatchDesc:
         p = capi.PatchDesc()
@@ -83,6 +104,17 @@ class Patch:
         p.conforms_with = self.conforms_with.encode()[: capi.MGD_NAME_LEN - 1]
         for i in range(3):
             p.interface_index[i] = int(self.interface_index[i])
+        if self.type == "SOLENOIDAL_EXCITATION" and self.n_modes > 0:
+            w, ph = self.excitation_modes()
+            # the C struct points into these arrays: keep them alive with the patch
+            self._modes = (np.ascontiguousarray(w), np.ascontiguousarray(ph.T).ravel())
+            p.n_modes = int(self.n_modes)
+            p.angular_frequencies = capi.dptr(self._modes[0])
+            p.phases = capi.dptr(self._modes[1])
+        p.origin[0], p.origin[1] = (float(x) for x in self.origin)
+        p.velocity[0], p.velocity[1] = (float(x) for x in self.velocity)
+        p.amplitude = float(self.amplitude)
+        p.radius = float(self.radius)
         return p
 
     def resolved_extent(self, grid_size):
@@ -178,3 +210,24 @@ def quiescent_state(n_points: int, n_dimensions: int, gamma: float) -> np.ndarra
     q[0] = 1.0
     q[n_dimensions + 1] = 1.0 / gamma / (gamma - 1.0)
     return q
+
+
+def solenoidal_modes(n_modes: int, frequency: float, seed: int, randomize_frequency: bool = True):
+    """Modes of a solenoidal excitation patch, drawn as the reference's setup
+    draws them (src/SolenoidalExcitationPatchImpl.f90:64-90): three columns of
+    uniform phases r in [0, 1) (phases(:, 1..3)), then one uniform r_l per mode
+    for the frequency jitter (0.5 when not randomized); phases = 2 pi r and
+    angular frequency l = 2 pi frequency (l + r_l - 1/2) / (n_modes / 2).
+    The reference draws from gfortran's random_number after random_seed(put =
+    seed); that stream is compiler-specific, so this front end draws from
+    numpy's PCG64 generator seeded with `seed` (numpy.random.default_rng).
+    A Fortran caller passes its own arrays through the C ABI instead.
+    Returns (angular_frequencies (n_modes), phases (n_modes, 3))."""
+    if n_modes <= 0:
+        return np.zeros(0), np.zeros((0, 3))
+    rng = np.random.default_rng(seed)
+    r = rng.random((3, n_modes))
+    jitter = rng.random(n_modes) if randomize_frequency else np.full(n_modes, 0.5)
+    l = np.arange(1, n_modes + 1, dtype=np.float64)
+    w = 2.0 * np.pi * frequency * (l + (jitter - 0.5)) / (0.5 * n_modes)
+    return w, np.ascontiguousarray((2.0 * np.pi * r).T)

@@ -644,6 +644,11 @@ struct Patch {
   std::vector<long long> partnerPoint;      // partner patch index of each patch point
   std::vector<double> metricsL, metricsR;   // (nPatchPoints, nD) normal metrics of both sides
   std::vector<double> ifViscousFlux;        // (nPatchPoints, nU): sum_j Fv(:, j) m_L,j, component 0 zero
+  // solenoidal excitation (src/SolenoidalExcitationPatchImpl.f90:3-120)
+  std::vector<double> excOmega, excPhases;  // (nModes), (nModes, 3)
+  double excGaussianFactor = 0;
+  std::vector<double> excStrength;          // (nPatchPoints)
+  std::vector<double> excCache;             // (nPatchPoints, nModes, 4): spatialFunctionsCache
 };
 
 static bool isWall(int type) {
@@ -1126,6 +1131,27 @@ static int setupPatches(Region& R) {
         }
       }
     }
+    if (p.d.type == MGD_PATCH_SOLENOIDAL_EXCITATION) {
+      // setupSolenoidalExcitationPatch, src/SolenoidalExcitationPatchImpl.f90:93-130
+      const int nM = p.d.n_modes;
+      const long long P = p.nPatchPoints;
+      p.excGaussianFactor = 9.0 / (2.0 * p.d.radius * p.d.radius);
+      p.excStrength.assign(P, 0.0);
+      p.excCache.assign((size_t)P * std::max(0, nM) * 4, 0.0);
+      forPatchPoints(p, b, [&](long long gi, long long pi) {
+        if (b.iblank[gi] == 0) return;
+        const double dx = b.coordinates[gi] - p.d.origin[0], dy = b.coordinates[b.N + gi] - p.d.origin[1];
+        p.excStrength[pi] = p.d.amplitude * std::exp(-p.excGaussianFactor * (dx * dx + dy * dy));
+        for (int l = 0; l < nM; ++l) {
+          const double w = p.excOmega[l];
+          const double a = w * dx + p.excPhases[l], c = w * dy + p.excPhases[nM + l];
+          p.excCache[pi + P * (l + (long long)nM * 0)] = std::sin(a);
+          p.excCache[pi + P * (l + (long long)nM * 1)] = std::cos(a);
+          p.excCache[pi + P * (l + (long long)nM * 2)] = std::sin(c);
+          p.excCache[pi + P * (l + (long long)nM * 3)] = std::cos(c);
+        }
+      });
+    }
     if (p.d.type == MGD_PATCH_COST_TARGET) p.adjointForcing.assign(p.nPatchPoints * R.nU, 0.0);
     if (p.d.type == MGD_PATCH_ACTUATOR) p.controlForcing.assign(p.nPatchPoints * R.nU, 0.0);
     if (p.d.type == MGD_PATCH_SPONGE) p.spongeStrength.assign(p.nPatchPoints, 0.0);
@@ -1495,7 +1521,7 @@ static void computeRhsAdjoint(Region& R, Block& b, int bi) {
 // Patch%updateRhs for the implemented patch types (src/FarFieldPatchImpl.f90:93-286,
 // src/SpongePatchImpl.f90:65-165, src/ActuatorPatchImpl.f90:108-181,
 // src/CostTargetPatchImpl.f90:72-136).
-static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjointForcingFactor) {
+static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjointForcingFactor, double time = 0.0) {
   const int nD = R.nD, nU = R.nU;
   const long long N = b.N;
   const double g = R.o.ratio_of_specific_heats;
@@ -1728,6 +1754,54 @@ static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjoi
           b.rightHandSide[N * l + gi] = b.rightHandSide[N * l + gi] + t;
         });
       break;
+    case MGD_PATCH_SOLENOIDAL_EXCITATION: {
+      // addSolenoidalExcitation, src/SolenoidalExcitationPatchImpl.f90:159-278. time is
+      // the forward time of the stage in both modes. The adjoint terms are the
+      // exact transpose of the forward term's state dependence (u . f in the
+      // energy equation), -(dR/dq)^T lambda as for every other patch; the
+      // reference's adjoint branch (:262-270) has the opposite sign and is
+      // evaluated at state%timeProgressive.
+      const int nM = p.d.n_modes;
+      if (nM <= 0) break;
+      const long long P = p.nPatchPoints;
+      std::vector<double> tf((size_t)nM * 4);
+      for (int l = 0; l < nM; ++l) {
+        tf[l] = std::sin(p.excOmega[l] * p.d.velocity[0] * time);
+        tf[nM + l] = std::cos(p.excOmega[l] * p.d.velocity[0] * time);
+        tf[2 * nM + l] = std::sin(p.excOmega[l] * p.d.velocity[1] * time);
+        tf[3 * nM + l] = std::cos(p.excOmega[l] * p.d.velocity[1] * time);
+      }
+      forPatchPoints(p, b, [&](long long gi, long long pi) {
+        if (b.iblank[gi] == 0) return;
+        const double dx = b.coordinates[gi] - p.d.origin[0], dy = b.coordinates[N + gi] - p.d.origin[1];
+        double f1 = 0.0, f2 = 0.0;
+        for (int l = 0; l < nM; ++l) {
+          const double* sc = &p.excCache[0];
+          const double s1 = sc[pi + P * l], s2 = sc[pi + P * (nM + l)], s3 = sc[pi + P * (2 * nM + l)],
+                       s4 = sc[pi + P * (3 * nM + l)];
+          const double t1 = s1 * tf[nM + l] - s2 * tf[l];
+          const double t2 = s2 * tf[nM + l] + s1 * tf[l];
+          const double t3 = s3 * tf[3 * nM + l] - s4 * tf[2 * nM + l];
+          const double t4 = s4 * tf[3 * nM + l] + s3 * tf[2 * nM + l];
+          f1 += t1 * (p.excOmega[l] * t4 - 2.0 * p.excGaussianFactor * dy * t3);
+          f2 += t3 * (p.excOmega[l] * t2 - 2.0 * p.excGaussianFactor * dx * t1);
+        }
+        f1 = p.excStrength[pi] * f1;
+        f2 = p.excStrength[pi] * f2;
+        const double uf = b.velocity[gi] * f1 + b.velocity[N + gi] * f2;
+        if (mode == MGD_FORWARD) {
+          b.rightHandSide[N * 1 + gi] = b.rightHandSide[N * 1 + gi] + f1;
+          b.rightHandSide[N * 2 + gi] = b.rightHandSide[N * 2 + gi] + f2;
+          b.rightHandSide[N * (nD + 1) + gi] = b.rightHandSide[N * (nD + 1) + gi] + uf;
+        } else {
+          const double vl = b.specificVolume[gi] * b.adjointVariables[N * (nD + 1) + gi];
+          b.rightHandSide[gi] = b.rightHandSide[gi] + vl * uf;
+          b.rightHandSide[N * 1 + gi] = b.rightHandSide[N * 1 + gi] - vl * f1;
+          b.rightHandSide[N * 2 + gi] = b.rightHandSide[N * 2 + gi] - vl * f2;
+        }
+      });
+      break;
+    }
     case MGD_PATCH_COST_TARGET:
       if (mode == MGD_FORWARD) break;
       for (int l = 0; l < nU; ++l)
@@ -1752,7 +1826,7 @@ static void computeRhs(Region& R, int mode, double time, double adjointForcingFa
   for (Block& b : R.blocks)
     for (int j = 0; j < R.nU; ++j)
       for (long long p = 0; p < b.N; ++p) b.rightHandSide[b.N * j + p] = b.rightHandSide[b.N * j + p] * b.jacobian[p];
-  for (Patch& p : R.patches) patchUpdateRhs(R, p, R.blocks[p.d.grid_index - 1], mode, adjointForcingFactor);
+  for (Patch& p : R.patches) patchUpdateRhs(R, p, R.blocks[p.d.grid_index - 1], mode, adjointForcingFactor, time);
   // State%addSources -> AcousticSource%add, src/StateImpl.f90:672-705, src/AcousticSourceImpl.f90:34-64
   if (mode == MGD_FORWARD)
     for (const mgd_acoustic_source& s : R.sources) {
@@ -1874,7 +1948,8 @@ static void loadForcing(Region& R, int step, int stage) {
 }
 
 // substepForwardRK4 / substepAdjointRK4, src/RK4IntegratorImpl.f90:65-270.
-static void substep(Region& R, int mode, double& time, double dt, int stage, bool updateAfter) {
+static void substep(Region& R, int mode, double& time, double dt, int stage, bool updateAfter,
+                    const double* forwardStageTime = nullptr) {
   if (mode == MGD_FORWARD) {
     if (stage == 1) for (Block& b : R.blocks) b.buffer1 = b.conservedVariables;
     if (stage == 2 || stage == 4) time = time + dt / 2.0;
@@ -1898,7 +1973,10 @@ static void substep(Region& R, int mode, double& time, double dt, int stage, boo
   } else {
     if (stage == 4) for (Block& b : R.blocks) b.buffer1 = b.adjointVariables;
     const double factor = stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0);
-    computeRhs(R, MGD_ADJOINT, time, factor);
+    // time of the matching forward stage: stages 4 and 2 run at the current
+    // time, stages 3 and 1 half a step earlier
+    const double ts = forwardStageTime ? *forwardStageTime : ((stage == 3 || stage == 1) ? time - dt / 2.0 : time);
+    computeRhs(R, MGD_ADJOINT, ts, factor);
     for (Block& b : R.blocks) {
       const long long n = b.N * R.nU;
       for (long long k = 0; k < n; ++k) {
@@ -2023,7 +2101,8 @@ static double runForward(Region& R, int nSteps, double t0, bool keepStages) {
         std::vector<double> all;
         for (Block& b : R.blocks) all.insert(all.end(), b.conservedVariables.begin(), b.conservedVariables.end());
         R.stageStates.push_back(std::move(all));
-        R.stageTimes.push_back(time);
+        // the stage's own time (substepForward advances it at stages 2 and 4)
+        R.stageTimes.push_back((i == 2 || i == 4) ? time + dt / 2.0 : time);
       }
       if (R.o.enable_controller && R.o.controller_switch) loadForcing(R, step, i);
       substep(R, MGD_FORWARD, time, dt, i, true);
@@ -2080,7 +2159,7 @@ static double runAdjoint(Region& R) {
       s = s + kRkNorm[i - 1] * dt * computeSensitivity(R);
       const bool finalStage = (step == 1 && i == 1);
       updateAdjointForcing(R, !forcing || finalStage);
-      substep(R, MGD_ADJOINT, time, dt, i, false);
+      substep(R, MGD_ADJOINT, time, dt, i, false, &R.stageTimes[(size_t)(step - 1) * 4 + (i - 1)]);
     }
   }
   return s;
@@ -2185,6 +2264,13 @@ int orc_add_patch(void* h, const mgd_patch_desc* p) {
   Region& R = *(Region*)h;
   orc::Patch q;
   q.d = *p;
+  q.d.angular_frequencies = nullptr;
+  q.d.phases = nullptr;
+  if (p->type == MGD_PATCH_SOLENOIDAL_EXCITATION) {
+    if (p->n_modes < 0 || (p->n_modes > 0 && (!p->angular_frequencies || !p->phases))) return 1;
+    q.excOmega.assign(p->angular_frequencies, p->angular_frequencies + p->n_modes);
+    q.excPhases.assign(p->phases, p->phases + 3 * p->n_modes);
+  }
   R.patches.push_back(q);
   return 0;
 }

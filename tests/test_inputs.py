@@ -1,7 +1,8 @@
 """magudi.inp / bc.dat front end (CPU)."""
+import numpy as np
 import pytest
 
-from magudi_gb300 import inputs
+from magudi_gb300 import capi, inputs
 from magudi_gb300.capi import PERIODIC_PLANE
 
 INP = """# comment line
@@ -100,3 +101,35 @@ patches/interface.1E/interface_index2 = -1
     assert ps[1].viscous_penalty_amount == 0.5  # interface default
     assert ps[2].conforms_with == "" and ps[2].interface_index == (1, 2, 3)
     assert ps[3].type == "SAT_SLIP_WALL"
+
+
+def test_solenoidal_excitation_keys(tmp_path):
+    inp = """patches/excitationSupport/number_of_modes = 8
+patches/excitationSupport/origin_x = 1.5
+patches/excitationSupport/velocity_x = 0.65
+patches/excitationSupport/amplitude = 1.0d-3
+patches/excitationSupport/frequency = 0.3
+patches/excitationSupport/radius = 2.0
+patches/excitationSupport/random_seed = 12
+"""
+    bc = "  excitationSupport    SOLENOIDAL_EXCITATION    1       0   69  186  248  393    1   -1\n"
+    (tmp_path / "magudi.inp").write_text(inp)
+    (tmp_path / "bc.dat").write_text(bc)
+    d = inputs.parse_input_file(tmp_path / "magudi.inp")
+    (p,) = inputs.patches_from_bc(d, inputs.read_bc_dat(tmp_path / "bc.dat"))
+    assert p.n_modes == 8 and p.origin == (1.5, 0.0) and p.velocity == (0.65, 0.0)
+    assert p.amplitude == 1e-3 and p.frequency == 0.3 and p.radius == 2.0 and p.random_seed == 12
+    w, ph = p.excitation_modes()
+    # angular frequency l = 2 pi f (l + r_l - 1/2) / (n / 2), r_l in [0, 1)
+    l = np.arange(1, 9)
+    lo = 2 * np.pi * 0.3 * (l - 0.5) / 4.0
+    hi = 2 * np.pi * 0.3 * (l + 0.5) / 4.0
+    assert np.all((w >= lo) & (w < hi))
+    assert ph.shape == (8, 3) and np.all((ph >= 0) & (ph < 2 * np.pi))
+    c = p.to_c()
+    assert c.type == capi.PATCH_SOLENOIDAL_EXCITATION and c.n_modes == 8
+    assert c.angular_frequencies[3] == w[3] and c.phases[8 + 2] == ph[2, 1]
+    (tmp_path / "magudi.inp").write_text(inp.replace("patches/excitationSupport/radius = 2.0\n", ""))
+    d = inputs.parse_input_file(tmp_path / "magudi.inp")
+    with pytest.raises(inputs.InputError):
+        inputs.patches_from_bc(d, inputs.read_bc_dat(tmp_path / "bc.dat"))
