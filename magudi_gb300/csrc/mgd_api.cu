@@ -1922,13 +1922,19 @@ static int reduceRegion(Context& c, int nSlots, std::vector<double>& out) {
 static void regionRunStage(Context& c, std::vector<RunScalars>& rs, int i, bool controller, bool store,
                            bool functional) {
   const BlockRefs refs = blockRefs(c);
+  // dissipation and excitation of every block on the side stream beside the
+  // flux and interface kernels; both only read the state of the stage
+  cudaEventRecord(c.evFork[0], c.stream);
+  cudaStreamWaitEvent(c.side, c.evFork[0], 0);
   for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
     DevBlock& b = c.blocks[bi];
-    launchDissipation(c, b, b.v.q, 1.0);
-    launchGradFlux(c, b, true, false, &rs[bi], i, store);
-    launchExcitation(c, b, rs[bi], i, false, false);
+    if (c.phys.dissipation) launchDissipation(c, b, b.v.q, 1.0, c.side);
+    launchExcitation(c, b, rs[bi], i, false, false, c.side);
   }
+  cudaEventRecord(c.evJoin[0], c.side);
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) launchGradFlux(c, c.blocks[bi], true, false, &rs[bi], i, store);
   for (DevBlock& b : c.blocks) launchInterfaceSat(c, b, refs);
+  cudaStreamWaitEvent(c.stream, c.evJoin[0], 0);
   for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
     DevBlock& b = c.blocks[bi];
     launchForwardDivergence(c, b, i, rs[bi], false, controller && bi == 0);
@@ -2020,16 +2026,26 @@ static int regionRunAdjoint(Context& c, double* sensitivity) {
               launchPrims(c, b, nullptr, true, &rs[bi], i);
               if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs[bi], i, false);
             }
+          // dissipation, excitation and gradient/sensitivity of every block on
+          // the side stream (they read lambda and the forward state of the
+          // stage); interface SATs, cores and diffusion on the main stream
+          cudaEventRecord(c.evFork[1], c.stream);
+          cudaStreamWaitEvent(c.side, c.evFork[1], 0);
+          for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+            DevBlock& b = c.blocks[bi];
+            if (c.phys.dissipation) launchDissipation(c, b, b.v.lam, -1.0, c.side);
+            launchExcitation(c, b, rs[bi], i, true, full, c.side);
+            launchGradientSensitivity(c, b, rs[bi], i, c.side);
+          }
+          cudaEventRecord(c.evJoin[1], c.side);
           for (size_t bi = 0; bi < c.blocks.size(); ++bi)
             launchInterfaceSatAdjoint(c, c.blocks[bi], refs, &rs[bi], i, full);
           for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
             DevBlock& b = c.blocks[bi];
-            launchDissipation(c, b, b.v.lam, -1.0);
-            launchExcitation(c, b, rs[bi], i, true, full);
-            launchGradientSensitivity(c, b, rs[bi], i);
             launchAdjointCore(c, b, rs[bi], i, full);
             launchAdjointDiffusion(c, b);
           }
+          cudaStreamWaitEvent(c.stream, c.evJoin[1], 0);
           for (size_t bi = 0; bi < c.blocks.size(); ++bi)
             launchAdjointAssemble(c, c.blocks[bi], i, rs[bi], i, 0.0, false, full);
         }

@@ -1125,7 +1125,7 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSatAdjoint(BlockView B, Phys
   const int e = blockIdx.x * kBlock + threadIdx.x;
   if (e >= B.ff.n || B.ff.kind[e] != SAT_INTERFACE) return;
   constexpr int nU = ND + 2, nV = ND + 1;
-  using D = DualN<nU>;
+  using D = DualN<1>;
   const long long N = B.N, p = B.ff.point[e];
   const int pb = B.ff.partnerBlock[e];
   const long long pp = B.ff.partnerPoint[e], NR = R.N[pb];
@@ -1137,15 +1137,11 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSatAdjoint(BlockView B, Phys
     const int slot = ((*rs.step) - (*rs.segBase) - 1) * 4 + stage - 1;
     qRb = R.stage[pb] + (long long)slot * R.slotStride[pb];
   }
-  double qL[nU], dq[nU], lamL[nU], lamR[nU], mL[ND], mR[ND];
-  D dL[nU], dR[nU], roe[nU];
+  double qL[nU], qR[nU], dq[nU], lamL[nU], lamR[nU], mL[ND], mR[ND];
   for (int c = 0; c < nU; ++c) {
     qL[c] = fs.q[p + N * c];
-    const double qr = qRb[pp + NR * c];
-    dq[c] = qL[c] - qr;
-    dL[c] = D(qL[c]);
-    dL[c].d[c] = 1.0;
-    dR[c] = D(qr);
+    qR[c] = qRb[pp + NR * c];
+    dq[c] = qL[c] - qR[c];
     lamL[c] = B.lam[p + N * c];
     lamR[c] = R.lam[pb][pp + NR * c];
   }
@@ -1153,40 +1149,56 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSatAdjoint(BlockView B, Phys
     mL[d] = B.metrics[p + N * (ND * (B.ff.normalDir[e] - 1) + d)];
     mR[d] = B.ff.metricsR[(long long)e * ND + d];
   }
-  roeAverage<ND, D>(dL, dR, P.g, roe);
   const double jac = B.jac[p];
+  const double sL = B.ff.ifInv[2 * e] * jac, sR = -B.ff.ifInv[2 * e + 1] * jac;
   double sat[nU];
   for (int c = 0; c < nU; ++c) sat[c] = 0.0;
-  double u[ND], tau[ND * ND], hf[ND];
-  for (int d = 0; d < ND; ++d) u[d] = fs.prim[p + N * L.u(d)];
-  const double v = fs.prim[p + N * L.v()], T = fs.prim[p + N * L.T()];
-  if (VISC) {
-    for (int c = 0; c < ND * ND; ++c) tau[c] = fs.tau[p + N * c];
-    for (int d = 0; d < ND; ++d) hf[d] = fs.hf[p + N * d];
-  }
-  for (int side = 0; side < 2; ++side) {
-    D A[nU * nU];
-    incomingJacobian<ND, D>(roe, side == 0 ? mL : mR, P.g, side == 0 ? B.ff.dirL[e] : B.ff.dirR[e], A);
-    const double* lam = side == 0 ? lamL : lamR;
-    const double sInv = side == 0 ? B.ff.ifInv[2 * e] : -B.ff.ifInv[2 * e + 1];
-    for (int r = 0; r < nU; ++r) {
-      double t = A[nU * r].v * lam[0];
-      for (int c = 1; c < nU; ++c) t += A[c + nU * r].v * lam[c];
-      sat[r] += sInv * jac * t;
+  // One forward-mode pass per left-state component l: the Roe average and both
+  // sides' incoming Jacobians on single-derivative dual numbers seeded with
+  // d/dq_L[l] give sum_ij lambda_i (dA_ij/dq_l) dq_j; the first pass also
+  // gives A^T lambda. (One derivative per pass keeps the duals in registers.)
+#pragma unroll 1
+  for (int l = 0; l < nU; ++l) {
+    D dL[nU], dR[nU], roe[nU];
+    for (int c = 0; c < nU; ++c) {
+      dL[c] = D(qL[c]);
+      dL[c].d[0] = c == l ? 1.0 : 0.0;
+      dR[c] = D(qR[c]);
     }
-    for (int l = 0; l < nU; ++l) {
+    roeAverage<ND, D>(dL, dR, P.g, roe);
+#pragma unroll 1
+    for (int side = 0; side < 2; ++side) {
+      D A[nU * nU];
+      incomingJacobian<ND, D>(roe, side == 0 ? mL : mR, P.g, side == 0 ? B.ff.dirL[e] : B.ff.dirR[e], A);
+      const double* lam = side == 0 ? lamL : lamR;
+      const double sInv = side == 0 ? sL : sR;
+      if (l == 0)
+        for (int r = 0; r < nU; ++r) {
+          double t = A[nU * r].v * lam[0];
+          for (int c = 1; c < nU; ++c) t += A[c + nU * r].v * lam[c];
+          sat[r] += sInv * t;
+        }
       double t = 0.0;
       for (int i = 0; i < nU; ++i) {
         double w = 0.0;
-        for (int j = 0; j < nU; ++j) w += A[i + nU * j].d[l] * dq[j];
+        for (int j = 0; j < nU; ++j) w += A[i + nU * j].d[0] * dq[j];
         t += w * lam[i];
       }
-      sat[l] += sInv * jac * t;
+      sat[l] += sInv * t;
     }
-    if (VISC) {
+  }
+  double u[ND];
+  for (int d = 0; d < ND; ++d) u[d] = fs.prim[p + N * L.u(d)];
+  if (VISC) {
+    double tau[ND * ND], hf[ND];
+    const double v = fs.prim[p + N * L.v()], T = fs.prim[p + N * L.T()];
+    for (int c = 0; c < ND * ND; ++c) tau[c] = fs.tau[p + N * c];
+    for (int d = 0; d < ND; ++d) hf[d] = fs.hf[p + N * d];
+    for (int side = 0; side < 2; ++side) {
       double y[nU];
       for (int c = 0; c < nU; ++c) y[c] = 0.0;
-      firstPartialViscousTransposeProduct<ND>(side == 0 ? mL : mR, u, T, v, P.g, P.powerLawExponent, tau, hf, lam, y);
+      firstPartialViscousTransposeProduct<ND>(side == 0 ? mL : mR, u, T, v, P.g, P.powerLawExponent, tau, hf,
+                                              side == 0 ? lamL : lamR, y);
       const double sVis = side == 0 ? -B.ff.ifVis[2 * e] : B.ff.ifVis[2 * e + 1];
       for (int c = 0; c < nU; ++c) sat[c] += sVis * jac * y[c];
     }
