@@ -248,6 +248,15 @@ int mgd_get_step_sizes(mgd_ctx* ctx, double* host, int n_steps);
  * *sensitivity = the time-integrated cost sensitivity (Grad0). */
 int mgd_run_adjoint(mgd_ctx* ctx, double* sensitivity);
 
+/* adjoint_nonzero_initial_condition (src/SolverImpl.f90:1027-1102, set per
+ * segment by bin/msadjoint.f90:141-400): when enabled, mgd_run_adjoint starts
+ * from the adjoint field the context holds (loaded with mgd_set_field(...,
+ * MGD_FIELD_ADJOINT, ...)) instead of zero, and adds the final step's
+ * cost-target forcing (or the terminal functional's gradient) to it, as
+ * loadInitialCondition(ADJOINT) does with a restart file
+ * (src/SolverImpl.f90:368-427). Stays as set until changed; off at creation. */
+int mgd_set_adjoint_nonzero_initial_condition(mgd_ctx* ctx, int enable);
+
 /* The gradient vector of the last mgd_run_adjoint, in the order the reference
  * writes <prefix>.gradient_<patch>.dat (ThermalActuator%updateGradient,
  * src/ThermalActuatorImpl.f90:383-443): 4*n_steps entries of nPatchPoints. */

@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <array>
 #include <map>
+#include <mutex>
 #include <tuple>
 #include <cmath>
 #include <cstdio>
@@ -553,14 +554,19 @@ struct TuneKey {
 };
 
 static int autotune(Context& c, DevBlock& b) {
+  // shared by all contexts of the process; contexts may be set up from several threads
   static std::map<TuneKey, std::array<Tile, 6>> cache;
+  static std::mutex cacheMutex;
   TuneKey key{c.nD, {b.v.gs[0], b.v.gs[1], b.v.gs[2]}, b.v.curvilinear, c.phys.viscous, c.phys.dissipation,
               c.phys.composite};
   Tile* slots[6] = {&b.tGrad, &b.tDiss, &b.tRhs, &b.tAdjA, &b.tAdjD, &b.tAdjB};
-  auto it = cache.find(key);
-  if (it != cache.end()) {
-    for (int k = 0; k < 6; ++k) *slots[k] = it->second[k];
-    return 0;
+  {
+    std::lock_guard<std::mutex> lock(cacheMutex);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      for (int k = 0; k < 6; ++k) *slots[k] = it->second[k];
+      return 0;
+    }
   }
   std::vector<std::array<int, 3>> cands;
   if (c.nD == 2)
@@ -612,7 +618,10 @@ static int autotune(Context& c, DevBlock& b) {
   if (checkLaunch(c)) return 1;
   std::array<Tile, 6> entry;
   for (int k = 0; k < 6; ++k) entry[k] = *slots[k];
-  cache[key] = entry;
+  {
+    std::lock_guard<std::mutex> lock(cacheMutex);
+    cache[key] = entry;
+  }
   return 0;
 }
 
@@ -2219,6 +2228,11 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
       sum = sum + kRkNorm[i - 1] * c.stepDt[n - 1] * vals[entry];
     }
   *sensitivity = sum;
+  return 0;
+}
+
+int mgd_set_adjoint_nonzero_initial_condition(mgd_ctx* h, int enable) {
+  h->c.adjointNonzeroIC = enable != 0;
   return 0;
 }
 

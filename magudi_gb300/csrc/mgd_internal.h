@@ -240,6 +240,7 @@ struct Context {
   std::vector<mgd_acoustic_source> sources;
   bool finalized = false;
   bool hasInterfaces = false;
+  bool adjointNonzeroIC = false;   // adjoint_nonzero_initial_condition
   std::vector<std::vector<int>> ifacePointEntry;  // per patch: SAT entry of each interface patch point
   long long launches = 0;
   long long actuatorPoints = 0;

@@ -946,7 +946,7 @@ __global__ void __launch_bounds__(kMaxTile) kAdjointAssemble(BlockView B, Physic
 // Adjoint initial condition lambda(T) = factor * adjointForcing(q(T)),
 // factor = -dt/6 (loadInitialCondition ADJOINT, src/SolverImpl.f90:368-427).
 template <int ND>
-__global__ void __launch_bounds__(kBlock) kAdjointInitial(BlockView B, Physics P, double factor) {
+__global__ void __launch_bounds__(kBlock) kAdjointInitial(BlockView B, Physics P, double factor, int accumulate) {
   pdlEnter();
   const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
   if (p >= B.N) return;
@@ -968,7 +968,7 @@ __global__ void __launch_bounds__(kBlock) kAdjointInitial(BlockView B, Physics P
       r[0] += factor * (0.5 * u2 * F);
     }
   }
-  for (int c = 0; c < nU; ++c) B.lam[p + N * c] = r[c];
+  for (int c = 0; c < nU; ++c) B.lam[p + N * c] = accumulate ? B.lam[p + N * c] + r[c] : r[c];
 }
 
 template <int ND>
@@ -1019,7 +1019,7 @@ __global__ void __launch_bounds__(kBlock) kKineticEnergyPartials(BlockView B, co
 
 // lambda(T) = H^-1 dJ/dq(T) of the terminal kinetic energy: (-|u|^2/2, u, 0).
 template <int ND>
-__global__ void __launch_bounds__(kBlock) kKineticEnergyAdjointInitial(BlockView B) {
+__global__ void __launch_bounds__(kBlock) kKineticEnergyAdjointInitial(BlockView B, int accumulate) {
   pdlEnter();
   const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
   if (p >= B.N) return;
@@ -1036,7 +1036,7 @@ __global__ void __launch_bounds__(kBlock) kKineticEnergyAdjointInitial(BlockView
     }
     l[0] = -0.5 * u2;
   }
-  for (int c = 0; c < nU; ++c) B.lam[p + N * c] = l[c];
+  for (int c = 0; c < nU; ++c) B.lam[p + N * c] = accumulate ? B.lam[p + N * c] + l[c] : l[c];
 }
 
 // Snapshot of the conserved variables after a completed forward step.
@@ -1604,8 +1604,9 @@ void launchAdjointAssemble(Context& c, DevBlock& b, int rkStage, const RunScalar
 
 void launchAdjointInitial(Context& c, DevBlock& b, double factor) {
   MGD_LAUNCH(c);
-  if (c.nD == 2) pdl(kAdjointInitial<2>, gridFor(b.v.N), kBlock, c.stream, b.v, c.phys, factor);
-  else pdl(kAdjointInitial<3>, gridFor(b.v.N), kBlock, c.stream, b.v, c.phys, factor);
+  const int acc = c.adjointNonzeroIC ? 1 : 0;
+  if (c.nD == 2) pdl(kAdjointInitial<2>, gridFor(b.v.N), kBlock, c.stream, b.v, c.phys, factor, acc);
+  else pdl(kAdjointInitial<3>, gridFor(b.v.N), kBlock, c.stream, b.v, c.phys, factor, acc);
 }
 
 void launchStoreAdjointForcing(Context& c, DevBlock& b, bool zero) {
@@ -1744,8 +1745,9 @@ void launchKineticEnergy(Context& c, DevBlock& b, const double* norm, double* pa
 
 void launchKineticEnergyAdjointInitial(Context& c, DevBlock& b) {
   MGD_LAUNCH(c);
-  if (c.nD == 2) pdl(kKineticEnergyAdjointInitial<2>, gridFor(b.v.N), kBlock, c.stream, b.v);
-  else pdl(kKineticEnergyAdjointInitial<3>, gridFor(b.v.N), kBlock, c.stream, b.v);
+  const int acc = c.adjointNonzeroIC ? 1 : 0;
+  if (c.nD == 2) pdl(kKineticEnergyAdjointInitial<2>, gridFor(b.v.N), kBlock, c.stream, b.v, acc);
+  else pdl(kKineticEnergyAdjointInitial<3>, gridFor(b.v.N), kBlock, c.stream, b.v, acc);
 }
 
 void launchTimeStep(Context& c, DevBlock& b, double* partials, double* dtOut, const int* step, double* time,

@@ -679,6 +679,7 @@ struct Region {
   std::vector<Patch> patches;
   std::vector<mgd_acoustic_source> sources;
   std::string error;
+  bool adjointNonzeroIC = false;
   // run state
   std::vector<double> forcingEntries;  // control forcing, file order
   long long nForcingEntries = 0;
@@ -2015,19 +2016,23 @@ static double terminalKineticEnergy(Region& R) {
 }
 
 // lambda(T) = H^-1 dJ/dq(T) of the terminal kinetic energy: (-|u|^2/2, u, 0).
-static void terminalKineticEnergyAdjoint(Region& R) {
+// With a nonzero initial condition the gradient is added to the adjoint field held.
+static void terminalKineticEnergyAdjoint(Region& R, bool accumulate) {
   for (Block& b : R.blocks) {
     const long long N = b.N;
     for (long long p = 0; p < N; ++p) {
-      for (int c = 0; c < R.nU; ++c) b.adjointVariables[N * c + p] = 0.0;
-      if (b.iblank[p] == 0) continue;
-      double u2 = 0.0;
-      for (int d = 0; d < R.nD; ++d) {
-        const double u = b.conservedVariables[N * (d + 1) + p] / b.conservedVariables[p];
-        b.adjointVariables[N * (d + 1) + p] = u;
-        u2 += u * u;
+      double l[5] = {0, 0, 0, 0, 0};
+      if (b.iblank[p] != 0) {
+        double u2 = 0.0;
+        for (int d = 0; d < R.nD; ++d) {
+          const double u = b.conservedVariables[N * (d + 1) + p] / b.conservedVariables[p];
+          l[1 + d] = u;
+          u2 += u * u;
+        }
+        l[0] = -0.5 * u2;
       }
-      b.adjointVariables[p] = -0.5 * u2;
+      for (int c = 0; c < R.nU; ++c)
+        b.adjointVariables[N * c + p] = accumulate ? b.adjointVariables[N * c + p] + l[c] : l[c];
     }
   }
 }
@@ -2139,9 +2144,11 @@ static double runAdjoint(Region& R) {
   const bool terminal = R.o.functional_type == MGD_FUNCTIONAL_TERMINAL_KINETIC_ENERGY;
   const bool forcing = R.o.adjoint_forcing_switch && !terminal;
   if (terminal) {
-    terminalKineticEnergyAdjoint(R);
+    terminalKineticEnergyAdjoint(R, R.adjointNonzeroIC);
   } else {
-    for (Block& b : R.blocks) std::fill(b.adjointVariables.begin(), b.adjointVariables.end(), 0.0);
+    // adjoint_nonzero_initial_condition keeps the adjoint field held (src/SolverImpl.f90:1097-1102)
+    if (!R.adjointNonzeroIC)
+      for (Block& b : R.blocks) std::fill(b.adjointVariables.begin(), b.adjointVariables.end(), 0.0);
     updateAdjointForcing(R, !R.o.adjoint_forcing_switch);
     for (Block& b : R.blocks) std::fill(b.rightHandSide.begin(), b.rightHandSide.end(), 0.0);
     for (Patch& p : R.patches)
@@ -2272,6 +2279,11 @@ int orc_add_patch(void* h, const mgd_patch_desc* p) {
     q.excPhases.assign(p->phases, p->phases + 3 * p->n_modes);
   }
   R.patches.push_back(q);
+  return 0;
+}
+
+int orc_set_adjoint_nonzero_initial_condition(void* h, int enable) {
+  ((Region*)h)->adjointNonzeroIC = enable != 0;
   return 0;
 }
 

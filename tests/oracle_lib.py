@@ -49,6 +49,7 @@ def lib():
         L.orc_run_forward.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_double)]
         L.orc_run_forward_nostore.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double)]
         L.orc_run_adjoint.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.orc_set_adjoint_nonzero_initial_condition.argtypes = [C.c_void_p, C.c_int]
         L.orc_time_step_size.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.orc_step_sizes.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.orc_get_gradient.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_longlong]
@@ -194,6 +195,9 @@ class Oracle:
         v = C.c_double()
         self.L.orc_run_adjoint(self.h, C.byref(v))
         return v.value
+
+    def set_adjoint_nonzero_initial_condition(self, enable):
+        self.L.orc_set_adjoint_nonzero_initial_condition(self.h, int(bool(enable)))
 
     def time_step_size(self):
         v = C.c_double()
