@@ -28,7 +28,7 @@ extern "C" {
 #define MGD_NAME_LEN 64
 
 /* include/Region.f90:9-11 (FORWARD = +1, ADJOINT = -1, LINEARIZED = 0). */
-enum { MGD_FORWARD = 1, MGD_ADJOINT = -1 };
+enum { MGD_FORWARD = 1, MGD_ADJOINT = -1, MGD_LINEARIZED = 0 };
 
 /* src/GridImpl.f90:202-210 periodicity types. */
 enum { MGD_PERIODIC_NONE = 0, MGD_PERIODIC_PLANE = 1, MGD_PERIODIC_OVERLAP = 2 };
@@ -185,9 +185,13 @@ int mgd_finalize_setup(mgd_ctx* ctx);
 /* State%update on every block (src/StateImpl.f90:466-537). */
 int mgd_update_state(mgd_ctx* ctx);
 
-/* Region%computeRhs (src/RegionImpl.f90:1877-2027). mode = MGD_FORWARD or
- * MGD_ADJOINT; time is state%time; adjoint_forcing_factor is
- * state%adjointForcingFactor. The result stays on the device
+/* Region%computeRhs (src/RegionImpl.f90:1877-2027). mode = MGD_FORWARD,
+ * MGD_ADJOINT or MGD_LINEARIZED; time is state%time; adjoint_forcing_factor is
+ * state%adjointForcingFactor. MGD_LINEARIZED (computeRhsLinearized,
+ * src/RhsHelperImpl.f90:598-829) is the tangent RHS of the perturbation held
+ * in MGD_FIELD_ADJOINT (the reference keeps it in adjointVariables) about the
+ * current conserved state; it covers far-field, sponge, actuator and
+ * cost-target patches and refuses the others. The result stays on the device
  * (read it with mgd_get_field(..., MGD_FIELD_RHS, ...)). */
 int mgd_compute_rhs(mgd_ctx* ctx, int mode, double time, double adjoint_forcing_factor);
 
@@ -200,8 +204,8 @@ int mgd_compute_functional(mgd_ctx* ctx, double* value);
 /* ThermalActuator%computeSensitivity (src/ThermalActuatorImpl.f90:83-159). */
 int mgd_compute_sensitivity(mgd_ctx* ctx, double* value);
 
-/* RK4Integrator%substepForward / substepAdjoint
- * (src/RK4IntegratorImpl.f90:65-270), followed for the forward mode by
+/* RK4Integrator%substepForward / substepAdjoint / substepLinearized
+ * (src/RK4IntegratorImpl.f90:65-380), followed for the forward mode by
  * State%update as Solver%runForward does (src/SolverImpl.f90:827-834).
  * *time is advanced (forward) or retreated (adjoint) as the reference does. */
 int mgd_rk4_substep(mgd_ctx* ctx, int mode, double* time, double dt, int stage);

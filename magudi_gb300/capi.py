@@ -12,6 +12,7 @@ MGD_NAME_LEN = 64
 
 FORWARD = 1
 ADJOINT = -1
+LINEARIZED = 0
 
 FUNCTIONAL_SOUND = 0
 FUNCTIONAL_TERMINAL_KINETIC_ENERGY = 1

@@ -1430,6 +1430,27 @@ int mgd_update_state(mgd_ctx* h) {
   return 0;
 }
 
+// The linearized RHS covers the far-field, sponge, actuator and cost-target
+// patches; contexts with other patch types are refused for that mode.
+static int refuseLinearized(Context& c) {
+  for (const mgd_patch_desc& p : c.patches)
+    if (p.type == MGD_PATCH_SLIP_WALL || p.type == MGD_PATCH_ISOTHERMAL_WALL || p.type == MGD_PATCH_ADIABATIC_WALL ||
+        p.type == MGD_PATCH_BLOCK_INTERFACE || p.type == MGD_PATCH_SOLENOIDAL_EXCITATION)
+      return fail(c, "the linearized RHS takes far-field, sponge, actuator and cost-target patches only");
+  return 0;
+}
+
+// The linearized RHS (rkStage 0) or one linearized RK stage of every block:
+// the perturbation in lambda about the current conserved state.
+static void linearizedStages(Context& c, int rkStage, const RunScalars& rs, double factor) {
+  for (DevBlock& x : c.blocks) {
+    launchPrims(c, x, x.v.q, false);
+    if (c.phys.viscous) launchGradFlux(c, x, false, true, &rs, 1, false);
+    if (c.phys.dissipation) launchDissipation(c, x, x.v.lam, 1.0);
+    launchLinearized(c, x, rkStage, rs, factor);
+  }
+}
+
 int mgd_compute_rhs(mgd_ctx* h, int mode, double time, double adjoint_forcing_factor) {
   Context& c = h->c;
   if (requireReady(c)) return 1;
@@ -1448,8 +1469,11 @@ int mgd_compute_rhs(mgd_ctx* h, int mode, double time, double adjoint_forcing_fa
     }
     if (singleBlock(c)) adjointStage(c, b, 0, rs, 1, adjoint_forcing_factor, true, false, false);
     else regionAdjointStage(c, 0, rs, adjoint_forcing_factor);
+  } else if (mode == MGD_LINEARIZED) {
+    if (refuseLinearized(c)) return 1;
+    linearizedStages(c, 0, rs, adjoint_forcing_factor);
   } else {
-    return fail(c, "mode must be MGD_FORWARD or MGD_ADJOINT");
+    return fail(c, "mode must be MGD_FORWARD, MGD_ADJOINT or MGD_LINEARIZED");
   }
   if (checkLaunch(c)) return 1;
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));
@@ -1559,8 +1583,14 @@ int mgd_rk4_substep(mgd_ctx* h, int mode, double* time, double dt, int stage) {
     if (singleBlock(c)) adjointStage(c, b, stage, rs, 1, factor, true, false, false);
     else regionAdjointStage(c, stage, rs, factor);
     if (stage == 3 || stage == 1) *time = *time - dt / 2.0;
+  } else if (mode == MGD_LINEARIZED) {
+    // substepLinearizedRK4 (src/RK4IntegratorImpl.f90:272-380): the perturbation
+    // in lambda advances about the conserved state held, which stays fixed
+    if (refuseLinearized(c)) return 1;
+    if (stage == 2 || stage == 4) *time = *time + dt / 2.0;
+    linearizedStages(c, stage, rs, 1.0);
   } else {
-    return fail(c, "mode must be MGD_FORWARD or MGD_ADJOINT");
+    return fail(c, "mode must be MGD_FORWARD, MGD_ADJOINT or MGD_LINEARIZED");
   }
   if (checkLaunch(c)) return 1;
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));

@@ -492,6 +492,72 @@ __device__ __forceinline__ void secondPartialViscousTransposeProduct(
   y[ND] += jac * (k * t1) * w[ND];
 }
 
+// Linearized (tangent) flux products, the non-transposed counterparts of the
+// two products above (computeRhsLinearized, src/RhsHelperImpl.f90:655-775).
+// Ax = A(m) x with the rows of computeJacobianOfInviscidFlux{2D,3D}
+// (src/CNSHelperImpl.f90:1098-1445) contracted with x; with VISC also
+// Bx = B1(m) x with the rows of computeFirstPartialViscousJacobian{2D,3D}
+// (:2412-2601). Both are contravariant along the metric row m.
+template <int ND, bool VISC>
+__device__ __forceinline__ void fluxJacobianProduct(const double* m, const double* u, double T, double v, double g,
+                                                    double n, const double* tau, const double* hf, const double* x,
+                                                    double* Ax, double* Bx) {
+  constexpr int E = ND + 1;
+  double U = m[0] * u[0], u2 = u[0] * u[0], mx = m[0] * x[1], ux = u[0] * x[1];
+  for (int d = 1; d < ND; ++d) {
+    U += m[d] * u[d];
+    u2 += u[d] * u[d];
+    mx += m[d] * x[1 + d];
+    ux += u[d] * x[1 + d];
+  }
+  const double phi2 = 0.5 * (g - 1.0) * u2;
+  Ax[0] = mx;
+  for (int d = 0; d < ND; ++d)
+    Ax[1 + d] = (phi2 * m[d] - U * u[d]) * x[0] + U * x[1 + d] + u[d] * mx - (g - 1.0) * m[d] * ux +
+                (g - 1.0) * m[d] * x[E];
+  Ax[E] = U * ((g - 2.0) / (g - 1.0) * phi2 - T) * x[0] + (T + phi2 / (g - 1.0)) * mx - (g - 1.0) * U * ux +
+          g * U * x[E];
+  if (VISC) {
+    double ct[3];
+    for (int a = 0; a < ND; ++a) {
+      double s = m[0] * tau[ND * a];
+      for (int d = 1; d < ND; ++d) s += m[d] * tau[ND * a + d];
+      ct[a] = s;
+    }
+    double cq = m[0] * hf[0], uct = u[0] * ct[0], ctx = ct[0] * x[1];
+    for (int d = 1; d < ND; ++d) {
+      cq += m[d] * hf[d];
+      uct += u[d] * ct[d];
+      ctx += ct[d] * x[1 + d];
+    }
+    const double t1 = uct - cq, nTv = n * g * v / T;
+    const double sg = nTv * ((phi2 / (g - 1.0) - T / g) * x[0] - ux + x[E]);
+    Bx[0] = 0.0;
+    for (int d = 0; d < ND; ++d) Bx[1 + d] = ct[d] * sg;
+    Bx[E] = t1 * sg + v * (ctx - uct * x[0]);
+  }
+}
+
+// y += B2(m1, m2) x (computeSecondPartialViscousJacobian{2D,3D},
+// src/CNSHelperImpl.f90:2636-2757, applied to x); x and y have nD+1 entries.
+template <int ND>
+__device__ __forceinline__ void secondPartialViscousProduct(const double* u, double mu, double la, double k,
+                                                            double jac, const double* m1, const double* m2,
+                                                            const double* x, double* y) {
+  double t1 = m1[0] * m2[0], mx1 = m1[0] * x[0], mx2 = m2[0] * x[0], ux = u[0] * x[0];
+  double m1u = m1[0] * u[0], m2u = m2[0] * u[0];
+  for (int d = 1; d < ND; ++d) {
+    t1 += m1[d] * m2[d];
+    mx1 += m1[d] * x[d];
+    mx2 += m2[d] * x[d];
+    ux += u[d] * x[d];
+    m1u += m1[d] * u[d];
+    m2u += m2[d] * u[d];
+  }
+  for (int r = 0; r < ND; ++r) y[r] += jac * (mu * t1 * x[r] + mu * m2[r] * mx1 + la * m1[r] * mx2);
+  y[ND] += jac * (mu * t1 * ux + mu * m2u * mx1 + la * m1u * mx2 + k * t1 * x[ND]);
+}
+
 // Cartesian-grid forms of the two products above, for a metric row with a
 // single non-zero entry a at component K (row K of a diagonal metric). Terms
 // that the general forms multiply by a zero metric entry are dropped, which

@@ -510,7 +510,7 @@ __device__ __forceinline__ double dissipationTerm(const BlockView& B, const Phys
 template <int ND>
 __device__ __forceinline__ void forwardDivergencePoint(const BlockView& B, const Physics& P, const RunScalars& rs,
                                                        int rkStage, int stage, int controller, const Tile& T,
-                                                       int blk) {
+                                                       int blk, int lin = 0, double linFactor = 0.0) {
   long long p;
   PointIndex I;
   if (!locate(B, T, blk, p, I)) return;
@@ -529,12 +529,20 @@ __device__ __forceinline__ void forwardDivergencePoint(const BlockView& B, const
   const long long kc = p + N * c;
   const double q = B.q[kc];
   const double S = B.sponge[p];
-  if (S != 0.0) r -= S * (q - B.qt[kc]);
-  if (B.excIdx && (c == 1 || c == 2 || c == E)) {
+  if (lin) {
+    // linearized: the sponge acts on the perturbation (q here), the cost
+    // target adds its stored adjoint forcing (src/SpongePatchImpl.f90:142-158,
+    // src/CostTargetPatchImpl.f90:104-133); no sources, no control
+    if (S != 0.0) r -= S * q;
+    if (linFactor != 0.0 && B.tgtCount[p] != 0.0) r += linFactor * B.adjF[kc];
+  } else if (S != 0.0) {
+    r -= S * (q - B.qt[kc]);
+  }
+  if (!lin && B.excIdx && (c == 1 || c == 2 || c == E)) {
     const int e = B.excIdx[p];
     if (e >= 0) r += B.excF[3LL * e + (c == E ? 2 : c - 1)];
   }
-  if (c == E) {
+  if (c == E && !lin) {
     const int step = *rs.step;
     if (controller) {
       const int ai = B.actIdx[p];
@@ -577,9 +585,10 @@ __device__ __forceinline__ void forwardDivergencePoint(const BlockView& B, const
 
 template <int ND>
 __global__ void __launch_bounds__(kMaxTile) kForwardDivergence(BlockView B, Physics P, RunScalars rs, int rkStage,
-                                                               int stage, int controller, Tile T) {
+                                                               int stage, int controller, Tile T, int lin,
+                                                               double linFactor) {
   pdlEnter();
-  forwardDivergencePoint<ND>(B, P, rs, rkStage, stage, controller, T, blockIdx.x);
+  forwardDivergencePoint<ND>(B, P, rs, rkStage, stage, controller, T, blockIdx.x, lin, linFactor);
 }
 
 // Functional (AcousticNoise%compute, src/AcousticNoiseImpl.f90:123-206) of the
@@ -867,6 +876,91 @@ __device__ __forceinline__ void adjointAssemblePoint(const BlockView& B, const P
     default:
       B.lam[kc] = B.b2[kc] - h6 * r;
       break;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Linearized RHS (computeRhsLinearized, src/RhsHelperImpl.f90:598-829) of the
+// perturbation held in lambda about the current state, whose primitives,
+// stress and heat flux are current.
+// kLinearizedTemp: temp = (delta u, gamma v (delta E - v E delta rho
+// - u . (delta(rho u) - u delta rho))) into t2 (:694-710).
+// ---------------------------------------------------------------------------
+template <int ND>
+__global__ void __launch_bounds__(kBlock) kLinearizedTemp(BlockView B, Physics P) {
+  pdlEnter();
+  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
+  if (p >= B.N) return;
+  constexpr int E = ND + 1;
+  const long long N = B.N;
+  const PrimLayout L{ND};
+  const double v = B.prim[p + N * L.v()], x0 = B.lam[p];
+  double t[ND + 1];
+  double su = 0.0;
+  for (int d = 0; d < ND; ++d) {
+    t[d] = -B.prim[p + N * L.u(d)] * x0 + B.lam[p + N * (1 + d)];
+    su = d == 0 ? B.prim[p + N * L.u(d)] * t[d] : su + B.prim[p + N * L.u(d)] * t[d];
+  }
+  double te = -v * B.q[p + N * E] * x0;
+  te = te - su + B.lam[p + N * E];
+  t[ND] = te * P.g;
+  for (int c = 0; c <= ND; ++c) B.t2[p + N * c] = t[c] * v;
+}
+
+// kLinearizedFlux: per point and direction i the contravariant linearized flux
+// A_i dq - (B1_i dq + (0, sum_j B2(m_i, m_j) D_j temp)) into fhat, and the
+// linearized far-field SAT of each entry at the point,
+// -sigma_inv J A+(q_target) dq + sigma_visc J (linearized viscous flux along
+// the normal) (src/FarFieldPatchImpl.f90:258-266).
+template <int ND, bool VISC>
+__global__ void __launch_bounds__(kMaxTile) kLinearizedFlux(BlockView B, Physics P, Tile T) {
+  pdlEnter();
+  long long p;
+  PointIndex I;
+  if (!locate(B, T, blockIdx.x, p, I)) return;
+  constexpr int nU = ND + 2, nV = ND + 1;
+  const long long N = B.N;
+  const PrimLayout L{ND};
+  double x[nU];
+  for (int c = 0; c < nU; ++c) x[c] = B.lam[p + N * c];
+  double m[ND * ND];
+  for (int c = 0; c < ND * ND; ++c) m[c] = B.metrics[p + N * c];
+  double u[ND];
+  for (int d = 0; d < ND; ++d) u[d] = B.prim[p + N * L.u(d)];
+  const double v = B.prim[p + N * L.v()], Tm = B.prim[p + N * L.T()];
+  double tau[ND * ND], hf[ND], dt[ND][nV];
+  double mu = 0.0, la = 0.0, kd = 0.0, jac = 0.0;
+  if (VISC) {
+    for (int c = 0; c < ND * ND; ++c) tau[c] = B.tau[p + N * c];
+    for (int d = 0; d < ND; ++d) hf[d] = B.hf[p + N * d];
+    mu = B.prim[p + N * L.mu()];
+    la = B.prim[p + N * L.la()];
+    kd = B.prim[p + N * L.k()];
+    jac = B.jac[p];
+#pragma unroll
+    for (int j = 0; j < ND; ++j)
+#pragma unroll
+      for (int c = 0; c < nV; ++c) dt[j][c] = applyOp<OP_D1>(B.t2 + N * c + I.base[j], I.idx[j], B.ax[j]);
+  }
+#pragma unroll
+  for (int i = 0; i < ND; ++i) {
+    double Ax[nU], Bx[nU];
+    fluxJacobianProduct<ND, VISC>(m + ND * i, u, Tm, v, P.g, P.powerLawExponent, tau, hf, x, Ax, Bx);
+    if (VISC) {
+#pragma unroll
+      for (int j = 0; j < ND; ++j) secondPartialViscousProduct<ND>(u, mu, la, kd, jac, m + ND * i, m + ND * j, dt[j], Bx + 1);
+    }
+    for (int c = 0; c < nU; ++c) B.fhat[p + N * (i * nU + c)] = VISC ? Ax[c] - Bx[c] : Ax[c];
+    for (int s = 0; s < 3; ++s) {
+      const int e = B.ffOfPoint[3 * p + s];
+      if (e < 0 || B.ff.kind[e] != SAT_FAR_FIELD || B.ff.normalDir[e] - 1 != i) continue;
+      const double* M = B.ff.M + (long long)e * nU * nU;
+      for (int r = 0; r < nU; ++r) {
+        double t = M[r] * x[0];
+        for (int c = 1; c < nU; ++c) t += M[r + nU * c] * x[c];
+        B.ff.visc[(long long)e * nU + r] = VISC ? -t + B.ff.sigV[e] * Bx[r] : -t;
+      }
+    }
   }
 }
 
@@ -1248,7 +1342,7 @@ __global__ void __launch_bounds__(kBatchThreads) kForwardDivergenceBatch(const B
   pdlEnter();
   const int2 m = map[blockIdx.x];
   const BatchEntry& e = E[m.x];
-  forwardDivergencePoint<ND>(e.v, P, e.rs, rkStage, rkStage, e.controller, e.tRhs, m.y);
+  forwardDivergencePoint<ND>(e.v, P, e.rs, rkStage, rkStage, e.controller, e.tRhs, m.y, 0, 0.0);
 }
 
 template <int ND>
@@ -1533,9 +1627,34 @@ void launchForwardDivergence(Context& c, DevBlock& b, int rkStage, const RunScal
   const dim3 grid(T.blocks(), c.nU);
   MGD_LAUNCH(c);
   if (c.nD == 2)
-    pdl(kForwardDivergence<2>, grid, T.threads(), on(c, s), b.v, c.phys, rs, rkStage, stage, controller, T);
+    pdl(kForwardDivergence<2>, grid, T.threads(), on(c, s), b.v, c.phys, rs, rkStage, stage, controller, T, 0, 0.0);
   else
-    pdl(kForwardDivergence<3>, grid, T.threads(), on(c, s), b.v, c.phys, rs, rkStage, stage, controller, T);
+    pdl(kForwardDivergence<3>, grid, T.threads(), on(c, s), b.v, c.phys, rs, rkStage, stage, controller, T, 0, 0.0);
+}
+
+void launchLinearized(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, double factor, cudaStream_t s) {
+  const cudaStream_t st = on(c, s);
+  if (c.phys.viscous) {
+    MGD_LAUNCH(c);
+    if (c.nD == 2) pdl(kLinearizedTemp<2>, gridFor(b.v.N), kBlock, st, b.v, c.phys);
+    else pdl(kLinearizedTemp<3>, gridFor(b.v.N), kBlock, st, b.v, c.phys);
+  }
+  {
+    const Tile T = b.tGrad;
+    MGD_LAUNCH(c);
+#define LF(ND, VISC) pdl(kLinearizedFlux<ND, VISC>, T.blocks(), T.threads(), st, b.v, c.phys, T)
+    if (c.nD == 2) { if (c.phys.viscous) LF(2, true); else LF(2, false); }
+    else { if (c.phys.viscous) LF(3, true); else LF(3, false); }
+#undef LF
+  }
+  // the divergence and RK update act on the perturbation: a view with q = lambda
+  BlockView v = b.v;
+  v.q = b.v.lam;
+  const Tile T = b.tRhs;
+  const dim3 grid(T.blocks(), c.nU);
+  MGD_LAUNCH(c);
+  if (c.nD == 2) pdl(kForwardDivergence<2>, grid, T.threads(), st, v, c.phys, rs, rkStage, 1, 0, T, 1, factor);
+  else pdl(kForwardDivergence<3>, grid, T.threads(), st, v, c.phys, rs, rkStage, 1, 0, T, 1, factor);
 }
 
 void launchFunctional(Context& c, DevBlock& b, const RunScalars& rs, int stage, cudaStream_t s) {

@@ -1258,9 +1258,10 @@ static void normalizeMollifiers(Region& R) {
 static void addDissipation(Region& R, Block& b, int mode) {
   const int nD = R.nD, nU = R.nU;
   const long long N = b.N;
-  const double amount = mode == MGD_FORWARD ? R.o.dissipation_amount : -R.o.dissipation_amount;
+  const double amount = mode == MGD_ADJOINT ? -R.o.dissipation_amount : R.o.dissipation_amount;
   std::vector<double> d(N * nU);
   for (int i = 0; i < nD; ++i) {
+    // LINEARIZED dissipates the perturbation held in adjointVariables
     const std::vector<double>& src = mode == MGD_FORWARD ? b.conservedVariables : b.adjointVariables;
     std::copy(src.begin(), src.end(), d.begin());
     apply(b.dissipation[i], d.data(), nU, b.gs, i);
@@ -1519,6 +1520,98 @@ static void computeRhsAdjoint(Region& R, Block& b, int bi) {
   if (R.o.viscous) addFarFieldAdjointPenalty(R, b, bi);
 }
 
+// computeRhsLinearized, src/RhsHelperImpl.f90:598-829: the linearized
+// (tangent) RHS of the perturbation held in adjointVariables about the
+// current conserved state (its dependent variables current). The flux
+// Jacobians carry the metrics, so fluxes1 - fluxes2 are contravariant.
+static void computeRhsLinearized(Region& R, Block& b, int bi) {
+  const int nD = R.nD, nU = R.nU;
+  const long long N = b.N;
+  const double g = R.o.ratio_of_specific_heats;
+  std::vector<double> f1(N * nU * nD, 0.0), f2(N * nU * nD, 0.0);
+  std::fill(b.rightHandSide.begin(), b.rightHandSide.end(), 0.0);
+  const std::vector<double>& dq = b.adjointVariables;
+#pragma omp parallel for schedule(static)
+  for (long long j = 0; j < N; ++j) {
+    double cv[5], u[3], m[3], A[25];
+    for (int c = 0; c < nU; ++c) cv[c] = b.conservedVariables[N * c + j];
+    for (int d = 0; d < nD; ++d) u[d] = b.velocity[N * d + j];
+    for (int i = 0; i < nD; ++i) {
+      for (int d = 0; d < nD; ++d) m[d] = b.metrics[N * (nD * i + d) + j];
+      inviscidJacobian(nD, cv, m, g, A, b.specificVolume[j], u, b.temperature[j]);
+      for (int r = 0; r < nU; ++r) {
+        double s = A[r] * dq[j];
+        for (int c = 1; c < nU; ++c) s += A[r + nU * c] * dq[N * c + j];
+        f1[N * (r + nU * i) + j] = f1[N * (r + nU * i) + j] + s;
+      }
+    }
+  }
+  if (R.o.viscous) {
+    // temp = (delta u, gamma v (delta E - v E delta rho - u . (delta(rho u) - u delta rho))),
+    // then its derivative along each direction (src/RhsHelperImpl.f90:694-718)
+    const int nV = nU - 1;
+    std::vector<double> temp(N * nV * nD);
+    for (long long k = 0; k < N; ++k) {
+      double t[4];
+      for (int i = 0; i < nD; ++i) t[i] = -b.velocity[N * i + k] * dq[k] + dq[N * (i + 1) + k];
+      t[nD] = -b.specificVolume[k] * b.conservedVariables[N * (nU - 1) + k] * dq[k];
+      double su = b.velocity[k] * t[0];
+      for (int i = 1; i < nD; ++i) su += b.velocity[N * i + k] * t[i];
+      t[nD] = t[nD] - su + dq[N * (nU - 1) + k];
+      t[nD] = t[nD] * g;
+      for (int c = 0; c < nV; ++c) t[c] = t[c] * b.specificVolume[k];
+      for (int i = 0; i < nD; ++i)
+        for (int c = 0; c < nV; ++c) temp[N * (c + nV * i) + k] = t[c];
+    }
+    for (int i = 0; i < nD; ++i) apply(b.firstDerivative[i], &temp[N * nV * i], nV, b.gs, i);
+#pragma omp parallel for schedule(static)
+    for (long long k = 0; k < N; ++k) {
+      double cv[5], u[3], m1[3], m2[3], tau[9], hf[3], B1[25], B2[16], lin[4 * 3];
+      for (int c = 0; c < nU; ++c) cv[c] = b.conservedVariables[N * c + k];
+      for (int d = 0; d < nD; ++d) u[d] = b.velocity[N * d + k];
+      for (int c = 0; c < nD * nD; ++c) tau[c] = b.stressTensor[N * c + k];
+      for (int d = 0; d < nD; ++d) hf[d] = b.heatFlux[N * d + k];
+      for (int t = 0; t < nV * nD; ++t) lin[t] = 0.0;
+      for (int i = 0; i < nD; ++i) {
+        for (int d = 0; d < nD; ++d) m1[d] = b.metrics[N * (nD * i + d) + k];
+        firstPartialViscousJacobian(nD, m1, tau, hf, R.powerLawExponent, g, b.specificVolume[k], u,
+                                    b.temperature[k], B1);
+        for (int r = 0; r < nU; ++r) {
+          double s = B1[r] * dq[k];
+          for (int c = 1; c < nU; ++c) s += B1[r + nU * c] * dq[N * c + k];
+          f2[N * (r + nU * i) + k] = f2[N * (r + nU * i) + k] + s;
+        }
+        for (int jj = 0; jj < nD; ++jj) {
+          for (int d = 0; d < nD; ++d) m2[d] = b.metrics[N * (nD * jj + d) + k];
+          secondPartialViscousJacobian(nD, u, b.dynamicViscosity[k], b.secondCoefficientOfViscosity[k],
+                                       b.thermalDiffusivity[k], b.jacobian[k], m1, m2, B2);
+          for (int r = 0; r < nV; ++r) {
+            double s = B2[r] * temp[N * (0 + nV * jj) + k];
+            for (int c = 1; c < nV; ++c) s += B2[r + nV * c] * temp[N * (c + nV * jj) + k];
+            lin[r + nV * i] = lin[r + nV * i] + s;
+          }
+        }
+        for (int r = 0; r < nV; ++r) f2[N * (r + 1 + nU * i) + k] = f2[N * (r + 1 + nU * i) + k] + lin[r + nV * i];
+      }
+    }
+    // far-field patches keep the linearized viscous fluxes (src/RhsHelperImpl.f90:788-800)
+    for (Patch& p : R.patches) {
+      if (p.d.grid_index != bi + 1 || p.nPatchPoints <= 0 || p.d.type != MGD_PATCH_SAT_FAR_FIELD) continue;
+      for (int c = 0; c < nU * nD; ++c)
+        forPatchPoints(p, b, [&](long long gi, long long pi) { p.viscousFluxes[p.nPatchPoints * c + pi] = f2[N * c + gi]; });
+    }
+    for (long long k = 0; k < N * nU * nD; ++k) f1[k] = f1[k] - f2[k];
+  }
+  for (int i = 0; i < nD; ++i) apply(b.firstDerivative[i], &f1[N * nU * i], nU, b.gs, i);
+  for (int c = 0; c < nU; ++c)
+    for (long long p = 0; p < N; ++p) {
+      double s = f1[N * c + p];
+      for (int i = 1; i < nD; ++i) s += f1[N * (c + nU * i) + p];
+      b.rightHandSide[N * c + p] = b.rightHandSide[N * c + p] - s;
+    }
+  if (R.o.dissipation) addDissipation(R, b, MGD_LINEARIZED);
+}
+
 // Patch%updateRhs for the implemented patch types (src/FarFieldPatchImpl.f90:93-286,
 // src/SpongePatchImpl.f90:65-165, src/ActuatorPatchImpl.f90:108-181,
 // src/CostTargetPatchImpl.f90:72-136).
@@ -1554,6 +1647,18 @@ static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjoi
               }
               b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] + p.viscousPenaltyAmount * jac * s;
             }
+        } else if (mode == MGD_LINEARIZED) {
+          // src/FarFieldPatchImpl.f90:258-266: the collected fluxes are the
+          // contravariant linearized viscous fluxes
+          for (int r = 0; r < nU; ++r) {
+            double s = Ain[r] * b.adjointVariables[gi];
+            for (int c = 1; c < nU; ++c) s += Ain[r + nU * c] * b.adjointVariables[N * c + gi];
+            b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] - p.inviscidPenaltyAmount * jac * s;
+          }
+          if (R.o.viscous)
+            for (int r = 0; r < nU; ++r)
+              b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] +
+                  p.viscousPenaltyAmount * jac * p.viscousFluxes[p.nPatchPoints * (r + nU * (dir - 1)) + pi];
         } else {
           for (int r = 0; r < nU; ++r) {
             double s = Ain[0 + nU * r] * b.adjointVariables[gi];
@@ -1742,6 +1847,8 @@ static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjoi
           double& r = b.rightHandSide[N * l + gi];
           if (mode == MGD_FORWARD)
             r = r - p.spongeStrength[pi] * (b.conservedVariables[N * l + gi] - b.targetState[N * l + gi]);
+          else if (mode == MGD_LINEARIZED)
+            r = r - p.spongeStrength[pi] * b.adjointVariables[N * l + gi];
           else
             r = r + p.spongeStrength[pi] * b.adjointVariables[N * l + gi];
         });
@@ -1816,8 +1923,15 @@ static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjoi
 
 // Region%computeRhs, src/RegionImpl.f90:1877-2027 (single block sets, no interfaces).
 static void computeRhs(Region& R, int mode, double time, double adjointForcingFactor) {
+  if (mode == MGD_LINEARIZED)
+    for (Patch& p : R.patches)
+      if (isWall(p.d.type) || p.d.type == MGD_PATCH_BLOCK_INTERFACE || p.d.type == MGD_PATCH_SOLENOIDAL_EXCITATION) {
+        R.error = "the linearized RHS takes far-field, sponge, actuator and cost-target patches only";
+        return;
+      }
   for (size_t bi = 0; bi < R.blocks.size(); ++bi) {
     if (mode == MGD_FORWARD) computeRhsForward(R, R.blocks[bi], (int)bi);
+    else if (mode == MGD_LINEARIZED) computeRhsLinearized(R, R.blocks[bi], (int)bi);
     else computeRhsAdjoint(R, R.blocks[bi], (int)bi);
   }
   // the interface data exchange is implicit: the interface penalties read the
@@ -1971,6 +2085,27 @@ static void substep(Region& R, int mode, double& time, double dt, int stage, boo
       }
     }
     if (updateAfter) updateAll(R);
+  } else if (mode == MGD_LINEARIZED) {
+    // substepLinearizedRK4, src/RK4IntegratorImpl.f90:272-380: RK4 on the
+    // perturbation in adjointVariables, about the current conserved state
+    if (stage == 1) for (Block& b : R.blocks) b.buffer1 = b.adjointVariables;
+    if (stage == 2 || stage == 4) time = time + dt / 2.0;
+    computeRhs(R, MGD_LINEARIZED, time, 1.0);
+    for (Block& b : R.blocks) {
+      const long long n = b.N * R.nU;
+      for (long long k = 0; k < n; ++k) {
+        const double r = b.rightHandSide[k];
+        switch (stage) {
+          case 1: b.buffer2[k] = b.adjointVariables[k] + dt * r / 6.0;
+                  b.adjointVariables[k] = b.buffer1[k] + dt * r / 2.0; break;
+          case 2: b.buffer2[k] = b.buffer2[k] + dt * r / 3.0;
+                  b.adjointVariables[k] = b.buffer1[k] + dt * r / 2.0; break;
+          case 3: b.buffer2[k] = b.buffer2[k] + dt * r / 3.0;
+                  b.adjointVariables[k] = b.buffer1[k] + dt * r; break;
+          case 4: b.adjointVariables[k] = b.buffer2[k] + dt * r / 6.0; break;
+        }
+      }
+    }
   } else {
     if (stage == 4) for (Block& b : R.blocks) b.buffer1 = b.adjointVariables;
     const double factor = stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0);
@@ -2343,8 +2478,10 @@ int orc_update_state(void* h) {
 }
 
 int orc_compute_rhs(void* h, int mode, double time, double factor) {
-  orc::computeRhs(*(Region*)h, mode, time, factor);
-  return 0;
+  Region& R = *(Region*)h;
+  R.error.clear();
+  orc::computeRhs(R, mode, time, factor);
+  return R.error.empty() ? 0 : 1;
 }
 
 int orc_update_adjoint_forcing(void* h, int noForcing) {

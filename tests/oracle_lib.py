@@ -153,7 +153,8 @@ class Oracle:
         self.L.orc_update_state(self.h)
 
     def compute_rhs(self, mode, time=0.0, adjoint_forcing_factor=1.0):
-        self.L.orc_compute_rhs(self.h, mode, time, adjoint_forcing_factor)
+        if self.L.orc_compute_rhs(self.h, mode, time, adjoint_forcing_factor) != 0:
+            raise RuntimeError(self.L.orc_last_error(self.h).decode())
 
     def update_adjoint_forcing(self, no_forcing=False):
         self.L.orc_update_adjoint_forcing(self.h, int(no_forcing))

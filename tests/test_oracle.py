@@ -460,3 +460,64 @@ def test_jet_3block_gradient_finite_difference_sweep():
         J1 = o2.run_forward(P.n_steps, keep_stages=False)
         best = min(best, abs((J1 - J0) / eps - G0) / G0)
     assert best < 1e-5
+
+
+def _linearized_case(P, seed):
+    from magudi_gb300.configs import smooth_perturbed_state
+    rng = np.random.default_rng(seed)
+    q0 = smooth_perturbed_state(P.blocks[0], P.options.n_dimensions, P.options.ratio_of_specific_heats, rng,
+                                amplitude=0.05)
+    dq = rng.uniform(-1.0, 1.0, q0.shape) * np.abs(q0).mean(axis=1, keepdims=True)
+    lam = rng.uniform(-1.0, 1.0, q0.shape)
+    return q0, dq, lam
+
+
+@pytest.mark.parametrize("viscous", [True, False])
+def test_linearized_rhs_matches_central_difference(viscous):
+    """computeRhsLinearized (src/RhsHelperImpl.f90:598-829) with the far-field
+    and sponge linearizations is the derivative of the forward RHS."""
+    P = small_monopole(n=31, ny=29, sponge_points=5)
+    P.options.viscous = viscous
+    q0, dq, _ = _linearized_case(P, 7)
+    o = oracle_lib.Oracle(P)
+    o.set_field(1, capi.FIELD_CONSERVED, q0)
+    o.update_state()
+    o.set_field(1, capi.FIELD_ADJOINT, dq)
+    o.compute_rhs(capi.LINEARIZED, 0.3, 0.0)
+    L = o.get_field(1, capi.FIELD_RHS)
+    errs = []
+    for e in (1e-3, 1e-4, 1e-5):
+        r = []
+        for sgn in (1.0, -1.0):
+            o.set_field(1, capi.FIELD_CONSERVED, q0 + sgn * e * dq)
+            o.update_state()
+            o.compute_rhs(capi.FORWARD, 0.3)
+            r.append(o.get_field(1, capi.FIELD_RHS))
+        errs.append(np.linalg.norm((r[0] - r[1]) / (2 * e) - L) / np.linalg.norm(L))
+    assert min(errs) < 1e-7 and errs[1] < 0.05 * errs[0]
+
+
+def test_linearized_rhs_is_the_transpose_of_the_adjoint_rhs():
+    """<lambda, L dq>_H = -<R^dagger lambda, dq>_H to rounding: the linearized
+    and the adjoint RHS are exact transposes of each other."""
+    P = small_monopole(n=31, ny=29, sponge_points=5)
+    q0, dq, lam = _linearized_case(P, 9)
+    o = oracle_lib.Oracle(P)
+    o.set_field(1, capi.FIELD_CONSERVED, q0)
+    o.update_state()
+    H = o.get_field(1, capi.FIELD_NORM)
+    o.set_field(1, capi.FIELD_ADJOINT, dq)
+    o.compute_rhs(capi.LINEARIZED, 0.3, 0.0)
+    a = np.sum(lam * H * o.get_field(1, capi.FIELD_RHS))
+    o.set_field(1, capi.FIELD_ADJOINT, lam)
+    o.compute_rhs(capi.ADJOINT, 0.3, 0.0)
+    b = np.sum(o.get_field(1, capi.FIELD_RHS) * H * dq)
+    assert abs(a + b) <= 1e-11 * abs(a)
+
+
+def test_linearized_rhs_refuses_wall_patches():
+    P = configs.wall_channel_2d()
+    o = oracle_lib.Oracle(P)
+    o.update_state()
+    with pytest.raises(RuntimeError):
+        o.compute_rhs(capi.LINEARIZED, 0.0, 0.0)
