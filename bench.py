@@ -49,12 +49,13 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rk-steps", type=int, default=N_STEPS,
                     help="RK4 steps per gradient evaluation (profiling runs use a few)")
-    ap.add_argument("--workload", default="gradient", choices=["gradient", "sweep", "tgv", "jet", "msgrad"],
+    ap.add_argument("--workload", default="gradient", choices=["gradient", "sweep", "tgv", "jet", "msgrad", "tangent"],
                     help="gradient: the forward + adjoint gradient evaluation (default); sweep: the batched "
                          "gradient-check sweep of 64 monopole instances of mixed grid sizes; tgv: the 3D "
                          "Taylor-Green vortex forward + adjoint (terminal kinetic energy, constant CFL); jet: "
                          "the three-block curvilinear 3D jet forward + adjoint; msgrad: the monopole gradient with "
-                         "the 960 steps split into --ms-segments time segments run concurrently")
+                         "the 960 steps split into --ms-segments time segments run concurrently; tangent: the "
+                         "monopole forward run followed by the linearized (tangent) run along it")
     ap.add_argument("--ms-segments", type=int, default=8)
     ap.add_argument("--tgv-n", type=int, default=256)
     ap.add_argument("--jet-steps", type=int, default=8, help="RK4 steps of the jet sample (of the 1000-step run)")
@@ -671,6 +672,70 @@ def run_msgrad(args):
         print(json.dumps(line), flush=True)
 
 
+def run_tangent(args):
+    """Tangent (linearized) run of the 2D monopole (201^2, 960 steps):
+    Solver%runLinearized along the checkpointed forward trajectory
+    (checkpoints every 10 steps, each segment's stage states recomputed
+    before its linearized steps). One bench step is the forward run plus the
+    tangent run; the metric counts forward and linearized RHS evaluations
+    per second, and the tangent run alone is reported beside it."""
+    import numpy as np
+    import torch
+    from magudi_gb300 import capi
+    from magudi_gb300.solver import Solver
+
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    T = args.rk_steps
+    P = problem(T)
+    s = Solver(P)
+    q0 = P.blocks[0].initial_state
+    rng = np.random.default_rng(0)
+    dq0 = 1e-3 * rng.standard_normal(q0.shape) * np.abs(q0).mean(axis=1, keepdims=True)
+
+    def step():
+        # each library call returns after its work completed on the device
+        s.set_field(1, capi.FIELD_CONSERVED, q0)
+        t0 = time.perf_counter()
+        s.run_forward(T, SAVE_INTERVAL)
+        t1 = time.perf_counter()
+        s.set_field(1, capi.FIELD_ADJOINT, dq0)
+        s.run_linearized()
+        t2 = time.perf_counter()
+        return t2 - t0, t2 - t1
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    s.kernel_launches(reset=True)
+    clocks = ClockSampler()
+    clocks.start()
+    times, tan = [], []
+    for _ in range(args.steps):
+        a, b = step()
+        times.append(a)
+        tan.append(b)
+    clk = clocks.stop()
+    sec = statistics.mean(times)
+    sec_tan = statistics.mean(tan)
+    pts = GRID * GRID
+    dT = s.get_field(1, capi.FIELD_ADJOINT)
+    line = {
+        "metric": "FP64 Mpt-RHS/s", "value": pts * 8 * T / sec / 1e6, "unit": "Mpt-RHS/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (monopole)",
+        "config": {"workload": f"2D acoustic monopole {GRID}x{GRID}, {T} RK4 steps forward, then the linearized "
+                               f"(tangent) run along the checkpointed trajectory (checkpoint every {SAVE_INTERVAL})",
+                   "l2": "working set fits in L2 (no flush)", "parallelism": "single GPU"},
+        "tangent_run": {"value": pts * 4 * T / sec_tan / 1e6, "unit": "Mpt-RHS/s (linearized RHS)",
+                        "seconds": sec_tan},
+        "final_perturbation_norm": float(np.linalg.norm(dT)),
+        "gpu_launches": s.kernel_launches(reset=True) // max(1, args.steps), "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -683,6 +748,8 @@ def main():
         run_jet(args)
     elif args.workload == "msgrad":
         run_msgrad(args)
+    elif args.workload == "tangent":
+        run_tangent(args)
     else:
         run_ours(args)
 

@@ -252,6 +252,14 @@ int mgd_get_step_sizes(mgd_ctx* ctx, double* host, int n_steps);
  * *sensitivity = the time-integrated cost sensitivity (Grad0). */
 int mgd_run_adjoint(mgd_ctx* ctx, double* sensitivity);
 
+/* Solver%runLinearized (src/SolverImpl.f90:1300-1450) over the steps of the
+ * last mgd_run_forward: the perturbation held in MGD_FIELD_ADJOINT (the
+ * linearized initial condition) advances with substepLinearizedRK4 along the
+ * checkpointed forward trajectory, with the forward run's step sizes; the
+ * final perturbation is left in MGD_FIELD_ADJOINT and the conserved state of
+ * the final step is kept. One block; the patch types of MGD_LINEARIZED. */
+int mgd_run_linearized(mgd_ctx* ctx);
+
 /* adjoint_nonzero_initial_condition (src/SolverImpl.f90:1027-1102, set per
  * segment by bin/msadjoint.f90:141-400): when enabled, mgd_run_adjoint starts
  * from the adjoint field the context holds (loaded with mgd_set_field(...,

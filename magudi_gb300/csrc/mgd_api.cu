@@ -2261,6 +2261,77 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   return 0;
 }
 
+// Solver%runLinearized (src/SolverImpl.f90:1300-1450) over the steps of the
+// last forward run: the perturbation in lambda advances with
+// substepLinearizedRK4 along the forward trajectory, whose stage states the
+// checkpointer provides (reverseMigrator%migrateTo, :1378-1386). Here each
+// segment's stage states are recomputed from its snapshot into the stage
+// slots, then the segment's linearized steps read them. The conserved state
+// of the final step is restored at the end.
+int mgd_run_linearized(mgd_ctx* h) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  if (c.runSteps < 1) return fail(c, "mgd_run_linearized needs a preceding mgd_run_forward");
+  if (!singleBlock(c)) return fail(c, "mgd_run_linearized takes one block");
+  if (refuseLinearized(c)) return 1;
+  DevBlock& b = c.blocks[0];
+  const long long N = b.v.N;
+  const int nU = c.nU, T = c.runSteps, S = c.saveInterval;
+  if (ensureStageBuffer(c, b, S)) return 1;
+  const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
+  double* qFinal = nullptr;
+  CUDA_TRY(c, cudaMalloc((void**)&qFinal, (size_t)nU * N * sizeof(double)));
+  struct Free { double* p; ~Free() { cudaFree(p); } } freeFinal{qFinal};
+  CUDA_TRY(c, cudaMemcpyAsync(qFinal, b.v.q, (size_t)nU * N * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+  setProgrammaticLaunch(true);
+  RunScalars rs = runScalars(c);
+  rs.stageBuf = c.dStageBuf;
+  cudaGraphExec_t gRec = nullptr, gLin = nullptr;
+  struct Graphs {
+    cudaGraphExec_t* a;
+    cudaGraphExec_t* b;
+    ~Graphs() {
+      if (*a) cudaGraphExecDestroy(*a);
+      if (*b) cudaGraphExecDestroy(*b);
+    }
+  } graphs{&gRec, &gLin};
+  long long nodesRec = 0, nodesLin = 0;
+  const Lanes lanes{c.stream, c.side, c.evFork[0], c.evJoin[0]};
+  if (capture(c, &gRec, &nodesRec, [&]() {
+        for (int i = 1; i <= 4; ++i) forwardStage(c, b, i, rs, false, controller, true, false, &lanes);
+        launchStepAdvance(c, 1);
+      }))
+    return 1;
+  if (capture(c, &gLin, &nodesLin, [&]() {
+        for (int i = 1; i <= 4; ++i) {
+          // forward state of stage i from its slot, with its stress and heat flux
+          launchPrims(c, b, nullptr, true, &rs, i);
+          if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs, i, false);
+          if (c.phys.dissipation) launchDissipation(c, b, b.v.lam, 1.0);
+          launchLinearized(c, b, i, rs, 0.0);
+        }
+        launchStepAdvance(c, 1);
+      }))
+    return 1;
+  const int nSeg = (T + S - 1) / S;
+  for (int k = 0; k < nSeg; ++k) {
+    const int L = k * S, end = std::min(T, L + S);
+    CUDA_TRY(c, cudaMemcpyAsync(b.v.q, c.dSnapshots + (size_t)k * nU * N, (size_t)nU * N * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c.stream));
+    launchPrims(c, b, b.v.q, false);
+    launchSetCounters(c.dCounters, L + 1, L, c.stream);
+    for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(gRec, c.stream));
+    launchSetCounters(c.dCounters, L + 1, L, c.stream);
+    for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(gLin, c.stream));
+    c.launches += 3 + (long long)(end - L) * (nodesRec + nodesLin);
+  }
+  CUDA_TRY(c, cudaMemcpyAsync(b.v.q, qFinal, (size_t)nU * N * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+  launchPrims(c, b, b.v.q, false);
+  if (checkLaunch(c)) return 1;
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  return 0;
+}
+
 int mgd_set_adjoint_nonzero_initial_condition(mgd_ctx* h, int enable) {
   h->c.adjointNonzeroIC = enable != 0;
   return 0;

@@ -56,6 +56,7 @@ def load_library(build_if_missing=True):
     L.mgd_run_forward.argtypes = [ctx, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_double)]
     L.mgd_run_adjoint.argtypes = [ctx, C.POINTER(C.c_double)]
     L.mgd_set_adjoint_nonzero_initial_condition.argtypes = [ctx, C.c_int]
+    L.mgd_run_linearized.argtypes = [ctx]
     L.mgd_get_gradient.argtypes = [ctx, C.POINTER(C.c_double), C.c_longlong]
     L.mgd_time_step_size.argtypes = [ctx, C.POINTER(C.c_double)]
     L.mgd_actuator_weights.argtypes = [ctx, C.POINTER(C.c_double)]
@@ -192,6 +193,11 @@ class Solver:
         v = C.c_double()
         self._check(self.L.mgd_run_adjoint(self.h, C.byref(v)))
         return v.value
+
+    def run_linearized(self):
+        """Tangent run over the steps of the last run_forward: the perturbation
+        in FIELD_ADJOINT advances along the checkpointed trajectory."""
+        self._check(self.L.mgd_run_linearized(self.h))
 
     def set_adjoint_nonzero_initial_condition(self, enable):
         """adjoint_nonzero_initial_condition: run_adjoint starts from the adjoint

@@ -2307,6 +2307,24 @@ static double runAdjoint(Region& R) {
   return s;
 }
 
+// Solver%runLinearized, src/SolverImpl.f90:1300-1450, over the steps of the
+// last runForward: the perturbation in adjointVariables advances along the
+// kept stage states with the forward run's step sizes; the final forward
+// state is restored afterwards.
+static void runLinearized(Region& R) {
+  std::vector<double> finalState;
+  for (Block& b : R.blocks) finalState.insert(finalState.end(), b.conservedVariables.begin(), b.conservedVariables.end());
+  double time = R.t0;
+  for (int step = 1; step <= R.nSteps; ++step) {
+    const double dt = R.stepDt[step - 1];
+    for (int i = 1; i <= 4; ++i) {
+      setForwardState(R, R.stageStates[(size_t)(step - 1) * 4 + (i - 1)]);
+      substep(R, MGD_LINEARIZED, time, dt, i, false);
+    }
+  }
+  setForwardState(R, finalState);
+}
+
 }  // namespace orc
 
 // ---------------------------------------------------------------------------
@@ -2415,6 +2433,17 @@ int orc_add_patch(void* h, const mgd_patch_desc* p) {
   }
   R.patches.push_back(q);
   return 0;
+}
+
+int orc_run_linearized(void* h) {
+  Region& R = *(Region*)h;
+  R.error.clear();
+  if (R.stageStates.empty()) {
+    R.error = "run_linearized needs a preceding run_forward that kept its stages";
+    return 1;
+  }
+  orc::runLinearized(R);
+  return R.error.empty() ? 0 : 1;
 }
 
 int orc_set_adjoint_nonzero_initial_condition(void* h, int enable) {

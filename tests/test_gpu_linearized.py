@@ -88,3 +88,36 @@ def test_linearized_rhs_refuses_wall_patches():
     s = Solver(configs.wall_channel_2d())
     with pytest.raises(MagudiError):
         s.compute_rhs(capi.LINEARIZED, 0.0, 0.0)
+
+
+@pytest.mark.parametrize("save_interval", [4, 12])
+def test_linearized_run_matches_oracle(save_interval):
+    P = small_monopole(n=29, ny=29, n_steps=12, save_interval=save_interval)
+    q0, dq, _ = _case(P, 4)
+    out = []
+    for s in (Solver(P), oracle_lib.Oracle(P)):
+        s.set_field(1, capi.FIELD_CONSERVED, q0)
+        s.run_forward(P.n_steps, save_interval)
+        s.set_field(1, capi.FIELD_ADJOINT, dq)
+        s.run_linearized()
+        out.append((s.get_field(1, capi.FIELD_ADJOINT), s.get_field(1, capi.FIELD_CONSERVED)))
+    assert rel_err(out[0][0], out[1][0]) < 1e-11
+    assert rel_err(out[0][1], out[1][1]) < 1e-11
+
+
+def test_linearized_and_adjoint_runs_are_dual_on_the_gpu():
+    P = small_monopole(n=29, ny=29, n_steps=12, save_interval=4)
+    P.options.adjoint_forcing_switch = False
+    q0, dq, lamT = _case(P, 6)
+    s = Solver(P)
+    s.set_field(1, capi.FIELD_CONSERVED, q0)
+    s.run_forward(P.n_steps, 4)
+    H = s.get_field(1, capi.FIELD_NORM)
+    s.set_field(1, capi.FIELD_ADJOINT, dq)
+    s.run_linearized()
+    b = np.sum(lamT * H * s.get_field(1, capi.FIELD_ADJOINT))
+    s.set_field(1, capi.FIELD_ADJOINT, lamT)
+    s.set_adjoint_nonzero_initial_condition(True)
+    s.run_adjoint()
+    a = np.sum(s.get_field(1, capi.FIELD_ADJOINT) * H * dq)
+    assert abs(a - b) <= 1e-11 * abs(b)

@@ -521,3 +521,47 @@ def test_linearized_rhs_refuses_wall_patches():
     o.update_state()
     with pytest.raises(RuntimeError):
         o.compute_rhs(capi.LINEARIZED, 0.0, 0.0)
+
+
+def test_linearized_run_matches_central_difference_of_forward_runs():
+    """runLinearized's final perturbation is the derivative of the final state
+    of the forward run along the initial perturbation."""
+    P = small_monopole(n=29, ny=29, n_steps=12, save_interval=4)
+    q0, dq, _ = _linearized_case(P, 4)
+    o = oracle_lib.Oracle(P)
+    o.set_field(1, capi.FIELD_CONSERVED, q0)
+    o.run_forward(P.n_steps, 4)
+    o.set_field(1, capi.FIELD_ADJOINT, dq)
+    o.run_linearized()
+    dT = o.get_field(1, capi.FIELD_ADJOINT)
+    errs = []
+    for e in (1e-3, 1e-4, 1e-5):
+        qs = []
+        for sgn in (1.0, -1.0):
+            o2 = oracle_lib.Oracle(P)
+            o2.set_field(1, capi.FIELD_CONSERVED, q0 + sgn * e * dq)
+            o2.run_forward(P.n_steps, 4, keep_stages=False)
+            qs.append(o2.get_field(1, capi.FIELD_CONSERVED))
+        errs.append(np.linalg.norm((qs[0] - qs[1]) / (2 * e) - dT) / np.linalg.norm(dT))
+    assert min(errs) < 1e-7
+
+
+def test_linearized_and_adjoint_runs_are_dual():
+    """<lambda(0), dq(0)>_H = <lambda(T), dq(T)>_H: the adjoint run from a given
+    terminal condition (adjoint_nonzero_initial_condition, no functional
+    forcing) transposes the tangent run exactly."""
+    P = small_monopole(n=29, ny=29, n_steps=12, save_interval=4)
+    P.options.adjoint_forcing_switch = False
+    q0, dq, lamT = _linearized_case(P, 6)
+    o = oracle_lib.Oracle(P)
+    o.set_field(1, capi.FIELD_CONSERVED, q0)
+    o.run_forward(P.n_steps, 4)
+    H = o.get_field(1, capi.FIELD_NORM)
+    o.set_field(1, capi.FIELD_ADJOINT, dq)
+    o.run_linearized()
+    b = np.sum(lamT * H * o.get_field(1, capi.FIELD_ADJOINT))
+    o.set_field(1, capi.FIELD_ADJOINT, lamT)
+    o.set_adjoint_nonzero_initial_condition(True)
+    o.run_adjoint()
+    a = np.sum(o.get_field(1, capi.FIELD_ADJOINT) * H * dq)
+    assert abs(a - b) <= 1e-11 * abs(b)
