@@ -248,15 +248,20 @@ def jet_3block_3d(nx=384, ny_core=192, ny_side=171, nz=192, mach=1.3, reynolds=2
     control is a thermal actuator on an annulus at the nozzle lip in the
     core. Far-field SATs on every outer face, sponges on the outflow and
     lateral faces. dt defaults to `cfl` over the largest inviscid spectral
-    radius of the initial state.
+    radius sum_d (|u_d| + c) / h_d of the initial state, h_d the grid-line
+    spacing.
 
     The composite dissipation enters the RHS as amount * D_diss q * (1/det)
     (addDissipation before the 1/det scaling, src/RhsHelperImpl.f90:10-87,
     src/RegionImpl.f90:1968-1976), so its explicit stability limit tightens
-    with the cell volume: with D_diss's interior spectral radius 1 per
-    direction, RK4 needs roughly 3 dt amount / det < 2.8. The amount is
-    therefore capped at 0.5 det_min / dt (det estimated from the grid-line
-    spacings); on the full 39.4 M-point grid that cap, not 0.01, applies."""
+    with the cell volume. The 1D SBP 4-8 composite operator has spectral
+    radius 2.42 with its boundary closures (1 in the interior), so at a corner
+    where three closures meet RK4 needs about 7.3 dt amount / det < 2.8. The
+    amount is capped at 0.2 det_min / dt (det estimated from the grid-line
+    spacings); on the full 39.4 M-point grid that cap, not 0.01, applies.
+    A cap of 0.5 det_min / dt let the closure corners at the inflow, the
+    interface and a z face grow without bound.
+    """
     gamma = 1.4
     U = mach  # ambient sound speed 1
     L, Yc, Ys = length, core_half_width, side_extent
@@ -302,7 +307,7 @@ def jet_3block_3d(nx=384, ny_core=192, ny_side=171, nz=192, mach=1.3, reynolds=2
     if dt is None:
         dt = cfl / smax
     opts.time_step_size = float(dt)
-    opts.dissipation_amount = float(min(dissipation_amount, 0.5 * vmin / dt))
+    opts.dissipation_amount = float(min(dissipation_amount, 0.2 * vmin / dt))
     s = sponge_points or max(4, nx // 24)
     sl = max(4, min(ny_side, nz) // 12)
     patches = []

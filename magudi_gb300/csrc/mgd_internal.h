@@ -123,8 +123,9 @@ struct BlockRefs {
 struct Tile {
   int t[3];
   int n[3];
-  int threads() const { return t[0] * t[1] * t[2]; }
-  int blocks() const { return n[0] * n[1] * n[2]; }
+  int split;  // adjoint core only: nD threads per point (kAdjointCoreSplit)
+  __host__ __device__ int threads() const { return t[0] * t[1] * t[2]; }
+  __host__ __device__ int blocks() const { return n[0] * n[1] * n[2]; }
 };
 
 // Constants of the physics and of the run.
