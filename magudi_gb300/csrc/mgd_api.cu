@@ -594,10 +594,6 @@ static int autotune(Context& c, DevBlock& b) {
     return ms;
   };
   const long long saved = c.launches;
-  // MGD_ADJOINT_CORE_SPLIT=0 or 1 overrides the timed choice between the
-  // per-point and the two-threads-per-point adjoint core (2D)
-  const char* env = std::getenv("MGD_ADJOINT_CORE_SPLIT");
-  const int splitChoice = env ? std::atoi(env) : -1;
   for (int k = 0; k < 6; ++k) {
     if ((k == 1 && !c.phys.dissipation) || (k == 4 && !c.phys.viscous)) continue;
     float best = 1e30f;
@@ -614,13 +610,6 @@ static int autotune(Context& c, DevBlock& b) {
         default: ms = timeIt([&] { launchAdjointAssemble(c, b, 0, rs, 1, 0.0, true, false); }); break;
       }
       if (ms < best) { best = ms; bestTile = *slots[k]; }
-      if (k == 3 && c.nD == 2 && splitChoice != 0) {
-        // the adjoint core also with two threads per point
-        slots[k]->split = 1;
-        ms = timeIt([&] { launchAdjointCore(c, b, rs, 1, false); });
-        if (ms < best || splitChoice == 1) { best = ms; bestTile = *slots[k]; }
-        slots[k]->split = 0;
-      }
     }
     *slots[k] = bestTile;
   }

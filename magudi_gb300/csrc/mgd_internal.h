@@ -123,7 +123,6 @@ struct BlockRefs {
 struct Tile {
   int t[3];
   int n[3];
-  int split;  // adjoint core only: nD threads per point (kAdjointCoreSplit)
   __host__ __device__ int threads() const { return t[0] * t[1] * t[2]; }
   __host__ __device__ int blocks() const { return n[0] * n[1] * n[2]; }
 };
