@@ -190,8 +190,8 @@ int mgd_update_state(mgd_ctx* ctx);
  * state%adjointForcingFactor. MGD_LINEARIZED (computeRhsLinearized,
  * src/RhsHelperImpl.f90:598-829) is the tangent RHS of the perturbation held
  * in MGD_FIELD_ADJOINT (the reference keeps it in adjointVariables) about the
- * current conserved state; it covers far-field, sponge, actuator and
- * cost-target patches and refuses the others. The result stays on the device
+ * current conserved state; it covers far-field, wall, sponge, actuator and
+ * cost-target patches and refuses block interfaces and excitations. The result stays on the device
  * (read it with mgd_get_field(..., MGD_FIELD_RHS, ...)). */
 int mgd_compute_rhs(mgd_ctx* ctx, int mode, double time, double adjoint_forcing_factor);
 

@@ -1431,13 +1431,12 @@ int mgd_update_state(mgd_ctx* h) {
   return 0;
 }
 
-// The linearized RHS covers the far-field, sponge, actuator and cost-target
-// patches; contexts with other patch types are refused for that mode.
+// The linearized RHS covers the far-field, wall, sponge, actuator and
+// cost-target patches; contexts with other patch types are refused for that mode.
 static int refuseLinearized(Context& c) {
   for (const mgd_patch_desc& p : c.patches)
-    if (p.type == MGD_PATCH_SLIP_WALL || p.type == MGD_PATCH_ISOTHERMAL_WALL || p.type == MGD_PATCH_ADIABATIC_WALL ||
-        p.type == MGD_PATCH_BLOCK_INTERFACE || p.type == MGD_PATCH_SOLENOIDAL_EXCITATION)
-      return fail(c, "the linearized RHS takes far-field, sponge, actuator and cost-target patches only");
+    if (p.type == MGD_PATCH_BLOCK_INTERFACE || p.type == MGD_PATCH_SOLENOIDAL_EXCITATION)
+      return fail(c, "the linearized RHS takes far-field, wall, sponge, actuator and cost-target patches only");
   return 0;
 }
 
@@ -2303,13 +2302,17 @@ int mgd_run_linearized(mgd_ctx* h) {
         launchStepAdvance(c, 1);
       }))
     return 1;
+  const bool full = c.slotFull != 0;
   if (capture(c, &gLin, &nodesLin, [&]() {
         for (int i = 1; i <= 4; ++i) {
-          // forward state of stage i from its slot, with its stress and heat flux
-          launchPrims(c, b, nullptr, true, &rs, i);
-          if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs, i, false);
+          // forward state of stage i: read from its full slot, or restored
+          // from a q-only slot with its primitives, stress and heat flux
+          if (!full) {
+            launchPrims(c, b, nullptr, true, &rs, i);
+            if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs, i, false);
+          }
           if (c.phys.dissipation) launchDissipation(c, b, b.v.lam, 1.0);
-          launchLinearized(c, b, i, rs, 0.0);
+          launchLinearized(c, b, i, rs, 0.0, i, full);
         }
         launchStepAdvance(c, 1);
       }))

@@ -350,11 +350,13 @@ void launchDissipation(Context& c, DevBlock& b, const double* src, double sign, 
 void launchForwardDivergence(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bool api, bool controller,
                              cudaStream_t s = 0);
 // Linearized RHS (rkStage 0, into b.v.rhs) or one linearized RK stage of the
-// perturbation in b.v.lam about the current state (primitives, stress and
-// heat flux current; the dissipation of lambda already in b.v.dq); factor
-// scales the stored cost-target adjoint forcing as the reference's
-// LINEARIZED mode adds it.
-void launchLinearized(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, double factor, cudaStream_t s = 0);
+// perturbation in b.v.lam about a forward state: the block's current state
+// (primitives, stress and heat flux current), or with fromSlot the full stage
+// slot of (step, stage) of a run; the dissipation of lambda already in
+// b.v.dq. factor scales the stored cost-target adjoint forcing as the
+// reference's LINEARIZED mode adds it.
+void launchLinearized(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, double factor, int stage = 1,
+                      bool fromSlot = false, cudaStream_t s = 0);
 // Functional partial sums of the state just produced (stage slot of step/stage).
 void launchFunctional(Context& c, DevBlock& b, const RunScalars& rs, int stage, cudaStream_t s = 0);
 // Adjoint: inviscid/viscous Jacobian-transpose products and viscous diffusion.

@@ -908,21 +908,23 @@ __device__ __forceinline__ void adjointAssemblePoint(const BlockView& B, const P
 // - u . (delta(rho u) - u delta rho))) into t2 (:694-710).
 // ---------------------------------------------------------------------------
 template <int ND>
-__global__ void __launch_bounds__(kBlock) kLinearizedTemp(BlockView B, Physics P) {
+__global__ void __launch_bounds__(kBlock) kLinearizedTemp(BlockView B, Physics P, RunScalars rs, int stage,
+                                                          int fromSlot) {
   pdlEnter();
   const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
   if (p >= B.N) return;
   constexpr int E = ND + 1;
   const long long N = B.N;
   const PrimLayout L{ND};
-  const double v = B.prim[p + N * L.v()], x0 = B.lam[p];
+  const FwdState fs = forwardState<ND>(B, rs, stage, fromSlot != 0);
+  const double v = fs.prim[p + N * L.v()], x0 = B.lam[p];
   double t[ND + 1];
   double su = 0.0;
   for (int d = 0; d < ND; ++d) {
-    t[d] = -B.prim[p + N * L.u(d)] * x0 + B.lam[p + N * (1 + d)];
-    su = d == 0 ? B.prim[p + N * L.u(d)] * t[d] : su + B.prim[p + N * L.u(d)] * t[d];
+    t[d] = -fs.prim[p + N * L.u(d)] * x0 + B.lam[p + N * (1 + d)];
+    su = d == 0 ? fs.prim[p + N * L.u(d)] * t[d] : su + fs.prim[p + N * L.u(d)] * t[d];
   }
-  double te = -v * B.q[p + N * E] * x0;
+  double te = -v * fs.q[p + N * E] * x0;
   te = te - su + B.lam[p + N * E];
   t[ND] = te * P.g;
   for (int c = 0; c <= ND; ++c) B.t2[p + N * c] = t[c] * v;
@@ -934,7 +936,8 @@ __global__ void __launch_bounds__(kBlock) kLinearizedTemp(BlockView B, Physics P
 // -sigma_inv J A+(q_target) dq + sigma_visc J (linearized viscous flux along
 // the normal) (src/FarFieldPatchImpl.f90:258-266).
 template <int ND, bool VISC>
-__global__ void __launch_bounds__(kMaxTile) kLinearizedFlux(BlockView B, Physics P, Tile T) {
+__global__ void __launch_bounds__(kMaxTile) kLinearizedFlux(BlockView B, Physics P, RunScalars rs, int stage,
+                                                            int fromSlot, Tile T) {
   pdlEnter();
   long long p;
   PointIndex I;
@@ -942,21 +945,22 @@ __global__ void __launch_bounds__(kMaxTile) kLinearizedFlux(BlockView B, Physics
   constexpr int nU = ND + 2, nV = ND + 1;
   const long long N = B.N;
   const PrimLayout L{ND};
+  const FwdState fs = forwardState<ND>(B, rs, stage, fromSlot != 0);
   double x[nU];
   for (int c = 0; c < nU; ++c) x[c] = B.lam[p + N * c];
   double m[ND * ND];
   for (int c = 0; c < ND * ND; ++c) m[c] = B.metrics[p + N * c];
   double u[ND];
-  for (int d = 0; d < ND; ++d) u[d] = B.prim[p + N * L.u(d)];
-  const double v = B.prim[p + N * L.v()], Tm = B.prim[p + N * L.T()];
+  for (int d = 0; d < ND; ++d) u[d] = fs.prim[p + N * L.u(d)];
+  const double v = fs.prim[p + N * L.v()], Tm = fs.prim[p + N * L.T()];
   double tau[ND * ND], hf[ND], dt[ND][nV];
   double mu = 0.0, la = 0.0, kd = 0.0, jac = 0.0;
   if (VISC) {
-    for (int c = 0; c < ND * ND; ++c) tau[c] = B.tau[p + N * c];
-    for (int d = 0; d < ND; ++d) hf[d] = B.hf[p + N * d];
-    mu = B.prim[p + N * L.mu()];
-    la = B.prim[p + N * L.la()];
-    kd = B.prim[p + N * L.k()];
+    for (int c = 0; c < ND * ND; ++c) tau[c] = fs.tau[p + N * c];
+    for (int d = 0; d < ND; ++d) hf[d] = fs.hf[p + N * d];
+    mu = fs.prim[p + N * L.mu()];
+    la = fs.prim[p + N * L.la()];
+    kd = fs.prim[p + N * L.k()];
     jac = B.jac[p];
 #pragma unroll
     for (int j = 0; j < ND; ++j)
@@ -974,7 +978,30 @@ __global__ void __launch_bounds__(kMaxTile) kLinearizedFlux(BlockView B, Physics
     for (int c = 0; c < nU; ++c) B.fhat[p + N * (i * nU + c)] = VISC ? Ax[c] - Bx[c] : Ax[c];
     for (int s = 0; s < 3; ++s) {
       const int e = B.ffOfPoint[3 * p + s];
-      if (e < 0 || B.ff.kind[e] != SAT_FAR_FIELD || B.ff.normalDir[e] - 1 != i) continue;
+      if (e < 0 || B.ff.normalDir[e] - 1 != i) continue;
+      if (B.ff.kind[e] == SAT_WALL || B.ff.kind[e] == SAT_ISOTHERMAL_WALL) {
+        // linearized wall penalties (src/ImpenetrableWallImpl.f90:187-191,
+        // src/IsothermalWallImpl.f90:309-322): -s_inv J (A(m) - m (dp/dq)) dq,
+        // and for isothermal walls -s_visc J (0, d(rho u), dE - d rho T_w / gamma)
+        double Aw[nU];
+        fluxJacobianProduct<ND, false>(m + ND * i, u, Tm, v, P.g, 0.0, nullptr, nullptr, x, Aw, nullptr);
+        double u2 = u[0] * u[0], ux = u[0] * x[1];
+        for (int d = 1; d < ND; ++d) {
+          u2 += u[d] * u[d];
+          ux += u[d] * x[1 + d];
+        }
+        const double dpx = (P.g - 1.0) * (0.5 * u2 * x[0] - ux + x[nU - 1]);
+        for (int l = 0; l < ND; ++l) Aw[1 + l] -= m[ND * i + l] * dpx;
+        double* sat = B.ff.visc + (long long)e * nU;
+        for (int r = 0; r < nU; ++r) sat[r] = -B.ff.wallInv[e] * Aw[r];
+        if (VISC && B.ff.kind[e] == SAT_ISOTHERMAL_WALL) {
+          const double sv = B.ff.wallVisc[e];
+          for (int r = 1; r < nU - 1; ++r) sat[r] -= sv * x[r];
+          sat[nU - 1] -= sv * (x[nU - 1] - x[0] * B.ff.wallT[e] / P.g);
+        }
+        continue;
+      }
+      if (B.ff.kind[e] != SAT_FAR_FIELD) continue;
       const double* M = B.ff.M + (long long)e * nU * nU;
       for (int r = 0; r < nU; ++r) {
         double t = M[r] * x[0];
@@ -1653,17 +1680,19 @@ void launchForwardDivergence(Context& c, DevBlock& b, int rkStage, const RunScal
     pdl(kForwardDivergence<3>, grid, T.threads(), on(c, s), b.v, c.phys, rs, rkStage, stage, controller, T, 0, 0.0);
 }
 
-void launchLinearized(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, double factor, cudaStream_t s) {
+void launchLinearized(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, double factor, int stage,
+                      bool fromSlot, cudaStream_t s) {
   const cudaStream_t st = on(c, s);
+  const int fsl = fromSlot ? 1 : 0;
   if (c.phys.viscous) {
     MGD_LAUNCH(c);
-    if (c.nD == 2) pdl(kLinearizedTemp<2>, gridFor(b.v.N), kBlock, st, b.v, c.phys);
-    else pdl(kLinearizedTemp<3>, gridFor(b.v.N), kBlock, st, b.v, c.phys);
+    if (c.nD == 2) pdl(kLinearizedTemp<2>, gridFor(b.v.N), kBlock, st, b.v, c.phys, rs, stage, fsl);
+    else pdl(kLinearizedTemp<3>, gridFor(b.v.N), kBlock, st, b.v, c.phys, rs, stage, fsl);
   }
   {
     const Tile T = b.tGrad;
     MGD_LAUNCH(c);
-#define LF(ND, VISC) pdl(kLinearizedFlux<ND, VISC>, T.blocks(), T.threads(), st, b.v, c.phys, T)
+#define LF(ND, VISC) pdl(kLinearizedFlux<ND, VISC>, T.blocks(), T.threads(), st, b.v, c.phys, rs, stage, fsl, T)
     if (c.nD == 2) { if (c.phys.viscous) LF(2, true); else LF(2, false); }
     else { if (c.phys.viscous) LF(3, true); else LF(3, false); }
 #undef LF

@@ -1803,6 +1803,8 @@ static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjoi
           for (int r = 0; r < nU; ++r)
             b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] - p.inviscidPenaltyAmount * jac * pen[r];
         } else {
+          // ADJOINT and LINEARIZED: the penalty's Jacobian (A(m) - m (dp/dq)),
+          // transposed for the adjoint (src/ImpenetrableWallImpl.f90:174-193)
           double dp[5];
           double u2 = 0.0;
           for (int d = 0; d < nD; ++d) u2 += u[d] * u[d];
@@ -1813,11 +1815,18 @@ static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjoi
           inviscidJacobian(nD, cv, m, g, A, b.specificVolume[gi], u, b.temperature[gi]);
           for (int l = 0; l < nD; ++l)
             for (int c = 0; c < nU; ++c) A[(l + 1) + nU * c] = A[(l + 1) + nU * c] - m[l] * dp[c];
-          for (int r = 0; r < nU; ++r) {
-            double s = A[0 + nU * r] * b.adjointVariables[gi];
-            for (int c = 1; c < nU; ++c) s += A[c + nU * r] * b.adjointVariables[N * c + gi];
-            b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] + p.inviscidPenaltyAmount * jac * s;
-          }
+          if (mode == MGD_LINEARIZED)
+            for (int r = 0; r < nU; ++r) {
+              double s = A[r] * b.adjointVariables[gi];
+              for (int c = 1; c < nU; ++c) s += A[r + nU * c] * b.adjointVariables[N * c + gi];
+              b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] - p.inviscidPenaltyAmount * jac * s;
+            }
+          else
+            for (int r = 0; r < nU; ++r) {
+              double s = A[0 + nU * r] * b.adjointVariables[gi];
+              for (int c = 1; c < nU; ++c) s += A[c + nU * r] * b.adjointVariables[N * c + gi];
+              b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] + p.inviscidPenaltyAmount * jac * s;
+            }
         }
         if (p.d.type != MGD_PATCH_ISOTHERMAL_WALL || !R.o.viscous) return;
         const double Tw = p.wallTemperature[pi];
@@ -1825,6 +1834,14 @@ static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjoi
           pen[0] = 0.0;
           for (int c = 1; c < nU; ++c) pen[c] = cv[c];
           pen[nD + 1] = pen[nD + 1] - cv[0] * Tw / g;
+          for (int r = 0; r < nU; ++r) pen[r] = jac * pen[r];
+          for (int r = 0; r < nU; ++r)
+            b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] - p.viscousPenaltyAmount * pen[r];
+        } else if (mode == MGD_LINEARIZED) {
+          // src/IsothermalWallImpl.f90:309-322
+          pen[0] = 0.0;
+          for (int c = 1; c < nU; ++c) pen[c] = b.adjointVariables[N * c + gi];
+          pen[nD + 1] = pen[nD + 1] - b.adjointVariables[gi] * Tw / g;
           for (int r = 0; r < nU; ++r) pen[r] = jac * pen[r];
           for (int r = 0; r < nU; ++r)
             b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] - p.viscousPenaltyAmount * pen[r];
@@ -1925,8 +1942,8 @@ static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjoi
 static void computeRhs(Region& R, int mode, double time, double adjointForcingFactor) {
   if (mode == MGD_LINEARIZED)
     for (Patch& p : R.patches)
-      if (isWall(p.d.type) || p.d.type == MGD_PATCH_BLOCK_INTERFACE || p.d.type == MGD_PATCH_SOLENOIDAL_EXCITATION) {
-        R.error = "the linearized RHS takes far-field, sponge, actuator and cost-target patches only";
+      if (p.d.type == MGD_PATCH_BLOCK_INTERFACE || p.d.type == MGD_PATCH_SOLENOIDAL_EXCITATION) {
+        R.error = "the linearized RHS takes far-field, wall, sponge, actuator and cost-target patches only";
         return;
       }
   for (size_t bi = 0; bi < R.blocks.size(); ++bi) {

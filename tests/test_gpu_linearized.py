@@ -83,9 +83,22 @@ def test_linearized_rhs_is_the_transpose_of_the_adjoint_rhs_on_the_gpu():
     assert abs(a + b) <= 1e-11 * abs(a)
 
 
-def test_linearized_rhs_refuses_wall_patches():
+@pytest.mark.parametrize("wall", ["SAT_SLIP_WALL", "SAT_ISOTHERMAL_WALL", "SAT_ADIABATIC_WALL"])
+def test_linearized_rhs_with_walls_matches_oracle(wall):
+    P = configs.wall_channel_2d(wall=wall)
+    q0, dq, _ = _case(P, 12)
+    pair = Solver(P), oracle_lib.Oracle(P)
+    for s in pair:
+        s.set_field(1, capi.FIELD_CONSERVED, q0)
+        s.set_field(1, capi.FIELD_ADJOINT, dq)
+        s.update_state()
+        s.compute_rhs(capi.LINEARIZED, 0.2, 0.0)
+    assert rel_err(*(s.get_field(1, capi.FIELD_RHS) for s in pair)) < RHS_TOL
+
+
+def test_linearized_rhs_refuses_block_interfaces():
     from magudi_gb300.solver import MagudiError
-    s = Solver(configs.wall_channel_2d())
+    s = Solver(configs.two_block_2d())
     with pytest.raises(MagudiError):
         s.compute_rhs(capi.LINEARIZED, 0.0, 0.0)
 

@@ -515,8 +515,40 @@ def test_linearized_rhs_is_the_transpose_of_the_adjoint_rhs():
     assert abs(a + b) <= 1e-11 * abs(a)
 
 
-def test_linearized_rhs_refuses_wall_patches():
-    P = configs.wall_channel_2d()
+@pytest.mark.parametrize("wall", ["SAT_SLIP_WALL", "SAT_ISOTHERMAL_WALL", "SAT_ADIABATIC_WALL"])
+def test_linearized_rhs_with_walls_is_derivative_and_transpose(wall):
+    """Linearized wall penalties (src/ImpenetrableWallImpl.f90:187-191,
+    src/IsothermalWallImpl.f90:309-322): central differences of the forward
+    RHS, and exact transposition against the adjoint RHS."""
+    P = configs.wall_channel_2d(wall=wall)
+    q0, dq, lam = _linearized_case(P, 12)
+    o = oracle_lib.Oracle(P)
+    o.set_field(1, capi.FIELD_CONSERVED, q0)
+    o.update_state()
+    H = o.get_field(1, capi.FIELD_NORM)
+    o.set_field(1, capi.FIELD_ADJOINT, dq)
+    o.compute_rhs(capi.LINEARIZED, 0.3, 0.0)
+    L = o.get_field(1, capi.FIELD_RHS)
+    errs = []
+    for e in (1e-4, 1e-5):
+        r = []
+        for sgn in (1.0, -1.0):
+            o2 = oracle_lib.Oracle(P)
+            o2.set_field(1, capi.FIELD_CONSERVED, q0 + sgn * e * dq)
+            o2.update_state()
+            o2.compute_rhs(capi.FORWARD, 0.3)
+            r.append(o2.get_field(1, capi.FIELD_RHS))
+        errs.append(np.linalg.norm((r[0] - r[1]) / (2 * e) - L) / np.linalg.norm(L))
+    assert min(errs) < 1e-7
+    a = np.sum(lam * H * L)
+    o.set_field(1, capi.FIELD_ADJOINT, lam)
+    o.compute_rhs(capi.ADJOINT, 0.3, 0.0)
+    b = np.sum(o.get_field(1, capi.FIELD_RHS) * H * dq)
+    assert abs(a + b) <= 1e-11 * abs(a)
+
+
+def test_linearized_rhs_refuses_block_interfaces():
+    P = configs.two_block_2d()
     o = oracle_lib.Oracle(P)
     o.update_state()
     with pytest.raises(RuntimeError):
