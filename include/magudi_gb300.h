@@ -257,8 +257,15 @@ int mgd_run_adjoint(mgd_ctx* ctx, double* sensitivity);
  * linearized initial condition) advances with substepLinearizedRK4 along the
  * checkpointed forward trajectory, with the forward run's step sizes; the
  * final perturbation is left in MGD_FIELD_ADJOINT and the conserved state of
- * the final step is kept. One block; the patch types of MGD_LINEARIZED. */
-int mgd_run_linearized(mgd_ctx* ctx);
+ * the final step is kept. delta_forcing (host or device, may be NULL) is a
+ * control perturbation of n_entries entries in the control-forcing layout,
+ * added by the actuators as the reference's deltaControlForcing
+ * (src/ActuatorPatchImpl.f90:162-170). *delta_cost (may be NULL) receives the
+ * tangent of the time-integrated SOUND functional: with a zero initial
+ * perturbation, the directional derivative of J along delta_forcing, the
+ * forward-mode counterpart of mgd_run_adjoint's gradient. One block; the
+ * patch types of MGD_LINEARIZED. */
+int mgd_run_linearized(mgd_ctx* ctx, const double* delta_forcing, long long n_entries, double* delta_cost);
 
 /* adjoint_nonzero_initial_condition (src/SolverImpl.f90:1027-1102, set per
  * segment by bin/msadjoint.f90:141-400): when enabled, mgd_run_adjoint starts

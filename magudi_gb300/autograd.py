@@ -61,6 +61,21 @@ class ForwardRun(torch.autograd.Function):
         return grad_J * w * g, None, None, None
 
 
+    @staticmethod
+    def jvp(ctx, forcing_t, solver_t, n_t, s_t):
+        """Forward mode: the tangent run (Solver%runLinearized) along the
+        control perturbation forcing_t from a zero initial perturbation, on the
+        checkpoints of this forward run; returns dJ = <dJ/df, forcing_t>."""
+        s, n = ctx.solver, ctx.n_steps
+        if forcing_t is None:
+            return torch.zeros((), dtype=torch.float64, device=ctx.device)
+        s.set_field(1, capi.FIELD_ADJOINT, np.zeros((s.nU, s.problem.blocks[0].n_points)))
+        ft = forcing_t.detach().to(torch.float64).contiguous()
+        v = C.c_double()
+        s._check(s.L.mgd_run_linearized(s.h, _ptr(ft), 4 * n, C.byref(v)))
+        return torch.tensor(v.value, dtype=torch.float64, device=ctx.device)
+
+
 def quadrature_weights(solver, n_steps):
     """w_s(e) dt_n(e) W_i for every forcing entry e (rows) and actuator point i."""
     P = solver.actuator_points()

@@ -168,7 +168,7 @@ int mgd_destroy(mgd_ctx* h) {
     cudaFree(b.runPartials);
   }
   cudaFree(c.dCounters); cudaFree(c.dApiAmp); cudaFree(c.dAmp); cudaFree(c.dForcing);
-  cudaFree(c.dApiTime); cudaFree(c.dStageTime);
+  cudaFree(c.dApiTime); cudaFree(c.dStageTime); cudaFree(c.dDeltaForcing);
   cudaFree(c.dGradient); cudaFree(c.dPartials); cudaFree(c.dStageValues);
   cudaFree(c.dSnapshots); cudaFree(c.dStageBuf);
   cudaFree(c.dStepDt); cudaFree(c.dDtPartials); cudaFree(c.dTime); cudaFree(c.dNorm);
@@ -2266,9 +2266,12 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
 // substepLinearizedRK4 along the forward trajectory, whose stage states the
 // checkpointer provides (reverseMigrator%migrateTo, :1378-1386). Here each
 // segment's stage states are recomputed from its snapshot into the stage
-// slots, then the segment's linearized steps read them. The conserved state
-// of the final step is restored at the end.
-int mgd_run_linearized(mgd_ctx* h) {
+// slots, then the segment's linearized steps read them. With a control
+// perturbation the actuators add it (src/ActuatorPatchImpl.f90:162-170), and
+// the tangent of the functional, sum over stages of w_i dt times the
+// functional's tangent after each stage, is reduced like J. The conserved
+// state of the final step is restored at the end.
+int mgd_run_linearized(mgd_ctx* h, const double* delta_forcing, long long n_entries, double* delta_cost) {
   Context& c = h->c;
   if (requireReady(c)) return 1;
   if (c.runSteps < 1) return fail(c, "mgd_run_linearized needs a preceding mgd_run_forward");
@@ -2279,6 +2282,22 @@ int mgd_run_linearized(mgd_ctx* h) {
   const int nU = c.nU, T = c.runSteps, S = c.saveInterval;
   if (ensureStageBuffer(c, b, S)) return 1;
   const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
+  const bool deltaControl = c.opts.enable_controller && c.opts.controller_switch && delta_forcing && n_entries > 0 &&
+                            c.actuatorPoints > 0;
+  if (deltaControl) {
+    const long long n = n_entries * c.actuatorPoints;
+    if (c.deltaForcingCapacity < n) {
+      cudaFree(c.dDeltaForcing);
+      c.dDeltaForcing = nullptr;
+      c.deltaForcingCapacity = 0;
+      CUDA_TRY(c, cudaMalloc((void**)&c.dDeltaForcing, (size_t)n * sizeof(double)));
+      c.deltaForcingCapacity = n;
+    }
+    CUDA_TRY(c, cudaMemcpyAsync(c.dDeltaForcing, delta_forcing, (size_t)n * sizeof(double), cudaMemcpyDefault,
+                                c.stream));
+  }
+  const bool functional = c.opts.enable_functional && c.opts.functional_type == MGD_FUNCTIONAL_SOUND;
+  if (functional && ensurePartials(c, 4LL * T)) return 1;
   double* qFinal = nullptr;
   CUDA_TRY(c, cudaMalloc((void**)&qFinal, (size_t)nU * N * sizeof(double)));
   struct Free { double* p; ~Free() { cudaFree(p); } } freeFinal{qFinal};
@@ -2286,6 +2305,10 @@ int mgd_run_linearized(mgd_ctx* h) {
   setProgrammaticLaunch(true);
   RunScalars rs = runScalars(c);
   rs.stageBuf = c.dStageBuf;
+  // the linearized stages read the perturbation's entries as their forcing
+  RunScalars rl = rs;
+  rl.forcing = deltaControl ? c.dDeltaForcing : nullptr;
+  rl.nForcingEntries = deltaControl ? n_entries : 0;
   cudaGraphExec_t gRec = nullptr, gLin = nullptr;
   struct Graphs {
     cudaGraphExec_t* a;
@@ -2311,8 +2334,10 @@ int mgd_run_linearized(mgd_ctx* h) {
             launchPrims(c, b, nullptr, true, &rs, i);
             if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs, i, false);
           }
+          // the functional's tangent after the stage before (state and perturbation at this stage's start)
+          if (functional) launchFunctionalTangent(c, b, rl, i, full);
           if (c.phys.dissipation) launchDissipation(c, b, b.v.lam, 1.0);
-          launchLinearized(c, b, i, rs, 0.0, i, full);
+          launchLinearized(c, b, i, rl, 0.0, i, full, deltaControl);
         }
         launchStepAdvance(c, 1);
       }))
@@ -2331,8 +2356,19 @@ int mgd_run_linearized(mgd_ctx* h) {
   }
   CUDA_TRY(c, cudaMemcpyAsync(b.v.q, qFinal, (size_t)nU * N * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
   launchPrims(c, b, b.v.q, false);
+  double dJ = 0.0;
+  if (functional) {
+    // the last stage's term, at the final state: the counters stand at step T + 1
+    launchFunctionalTangent(c, b, rl, 1, false);
+    if (checkLaunch(c)) return 1;
+    std::vector<double> vals;
+    if (reduceToHost(c, 4 * T, vals)) return 1;
+    for (int st = 0; st < T; ++st)
+      for (int i = 0; i < 4; ++i) dJ = dJ + kRkNorm[i] * c.stepDt[st] * vals[(size_t)4 * st + i];
+  }
   if (checkLaunch(c)) return 1;
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  if (delta_cost) *delta_cost = dJ;
   return 0;
 }
 

@@ -254,6 +254,8 @@ struct Context {
   double* dAmp = nullptr;           // per-stage source amplitudes of the run
   long long ampCapacity = 0;
   double* dForcing = nullptr;       // control forcing entries
+  double* dDeltaForcing = nullptr;  // control perturbation of a tangent run
+  long long deltaForcingCapacity = 0;
   long long nForcingEntries = 0;
   long long forcingCapacity = 0;
   std::vector<double> actuatorWeights;  // quadrature weight of each actuator-patch point
@@ -356,7 +358,11 @@ void launchForwardDivergence(Context& c, DevBlock& b, int rkStage, const RunScal
 // b.v.dq. factor scales the stored cost-target adjoint forcing as the
 // reference's LINEARIZED mode adds it.
 void launchLinearized(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, double factor, int stage = 1,
-                      bool fromSlot = false, cudaStream_t s = 0);
+                      bool fromSlot = false, bool controller = false, cudaStream_t s = 0);
+// Tangent of the functional at the forward state of (step, stage) along lambda,
+// into the partial sums of the stage before.
+void launchFunctionalTangent(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool fromSlot,
+                             cudaStream_t s = 0);
 // Functional partial sums of the state just produced (stage slot of step/stage).
 void launchFunctional(Context& c, DevBlock& b, const RunScalars& rs, int stage, cudaStream_t s = 0);
 // Adjoint: inviscid/viscous Jacobian-transpose products and viscous diffusion.

@@ -547,8 +547,10 @@ __device__ __forceinline__ void forwardDivergencePoint(const BlockView& B, const
     const int e = B.excIdx[p];
     if (e >= 0) r += B.excF[3LL * e + (c == E ? 2 : c - 1)];
   }
-  if (c == E && !lin) {
+  if (c == E) {
     const int step = *rs.step;
+    // the actuators add the control forcing, or in a tangent run its
+    // perturbation (rs.forcing then holds the perturbation's entries)
     if (controller) {
       const int ai = B.actIdx[p];
       if (ai >= 0) {
@@ -556,7 +558,7 @@ __device__ __forceinline__ void forwardDivergencePoint(const BlockView& B, const
         if (e >= 0 && e < rs.nForcingEntries) r += B.mc[p] * rs.forcing[e * rs.P + ai];
       }
     }
-    if (B.nSources > 0) {
+    if (!lin && B.nSources > 0) {
       const double* amp = rs.amp + ((long long)(step - 1) * 4 + (stage - 1)) * B.nSources;
       for (int k = 0; k < B.nSources; ++k) r += amp[k] * B.srcG[p + N * k];
     }
@@ -618,6 +620,37 @@ __device__ __forceinline__ void functionalBlock(const BlockView& B, const RunSca
 __global__ void __launch_bounds__(kBlock) kFunctional(BlockView B, RunScalars rs, int stage, int pressureComp) {
   pdlEnter();
   functionalBlock(B, rs, stage, pressureComp, blockIdx.x);
+}
+
+// Tangent of the functional at the forward state of (step, stage) along the
+// perturbation in lambda: per cost-target point wT m_t 2 (p - p_mean) delta p,
+// delta p = (gamma - 1)(|u|^2/2 delta rho - u . delta(rho u) + delta E). The
+// state at the start of (step, stage) is the state after the stage before,
+// so the block partial sum goes to that stage's slot, (step-1)*4 + stage - 2.
+template <int ND>
+__global__ void __launch_bounds__(kBlock) kFunctionalTangent(BlockView B, Physics P, RunScalars rs, int stage,
+                                                             int fromSlot) {
+  pdlEnter();
+  const int slot = ((*rs.step) - 1) * 4 + (stage - 2);
+  const FwdState fs = forwardState<ND>(B, rs, stage, fromSlot != 0);
+  const PrimLayout L{ND};
+  const long long N = B.N;
+  const int i = blockIdx.x * kBlock + threadIdx.x;
+  double val = 0.0;
+  if (i < B.nTgt) {
+    const long long p = B.tgtPts[i];
+    double u2 = 0.0, ux = 0.0;
+    for (int d = 0; d < ND; ++d) {
+      const double u = fs.prim[p + N * L.u(d)];
+      u2 += u * u;
+      ux += u * B.lam[p + N * (d + 1)];
+    }
+    const double dp = P.gm1 * (0.5 * u2 * B.lam[p] - ux + B.lam[p + N * (ND + 1)]);
+    const double F = fs.prim[p + N * L.p()] - B.meanP[p];
+    val = B.wT[p] * (2.0 * F * dp * B.mt[p]);
+  }
+  const double sum = blockSum(val);
+  if (threadIdx.x == 0 && slot >= 0) rs.partials[(long long)slot * rs.nPartialBlocks + blockIdx.x] = sum;
 }
 
 // Gradient entry and sensitivity partial sums of lambda at an adjoint stage
@@ -1681,7 +1714,7 @@ void launchForwardDivergence(Context& c, DevBlock& b, int rkStage, const RunScal
 }
 
 void launchLinearized(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, double factor, int stage,
-                      bool fromSlot, cudaStream_t s) {
+                      bool fromSlot, bool controller, cudaStream_t s) {
   const cudaStream_t st = on(c, s);
   const int fsl = fromSlot ? 1 : 0;
   if (c.phys.viscous) {
@@ -1703,8 +1736,9 @@ void launchLinearized(Context& c, DevBlock& b, int rkStage, const RunScalars& rs
   const Tile T = b.tRhs;
   const dim3 grid(T.blocks(), c.nU);
   MGD_LAUNCH(c);
-  if (c.nD == 2) pdl(kForwardDivergence<2>, grid, T.threads(), st, v, c.phys, rs, rkStage, 1, 0, T, 1, factor);
-  else pdl(kForwardDivergence<3>, grid, T.threads(), st, v, c.phys, rs, rkStage, 1, 0, T, 1, factor);
+  const int ctl = controller ? 1 : 0;
+  if (c.nD == 2) pdl(kForwardDivergence<2>, grid, T.threads(), st, v, c.phys, rs, rkStage, stage, ctl, T, 1, factor);
+  else pdl(kForwardDivergence<3>, grid, T.threads(), st, v, c.phys, rs, rkStage, stage, ctl, T, 1, factor);
 }
 
 void launchFunctional(Context& c, DevBlock& b, const RunScalars& rs, int stage, cudaStream_t s) {
@@ -1721,6 +1755,13 @@ void launchExcitation(Context& c, DevBlock& b, const RunScalars& rs, int stage, 
     if (c.nD == 2) pdl(kExcitation<2>, grid, kBlock, on(c, s), b.v, X, rs, stage, (int)adjoint, (int)fromSlot);
     else pdl(kExcitation<3>, grid, kBlock, on(c, s), b.v, X, rs, stage, (int)adjoint, (int)fromSlot);
   }
+}
+
+void launchFunctionalTangent(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool fromSlot, cudaStream_t s) {
+  MGD_LAUNCH(c);
+  const int fsl = fromSlot ? 1 : 0;
+  if (c.nD == 2) pdl(kFunctionalTangent<2>, reductionBlocks(b), kBlock, on(c, s), b.v, c.phys, rs, stage, fsl);
+  else pdl(kFunctionalTangent<3>, reductionBlocks(b), kBlock, on(c, s), b.v, c.phys, rs, stage, fsl);
 }
 
 void launchGradientSensitivity(Context& c, DevBlock& b, const RunScalars& rs, int stage, cudaStream_t s) {

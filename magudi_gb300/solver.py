@@ -56,7 +56,7 @@ def load_library(build_if_missing=True):
     L.mgd_run_forward.argtypes = [ctx, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_double)]
     L.mgd_run_adjoint.argtypes = [ctx, C.POINTER(C.c_double)]
     L.mgd_set_adjoint_nonzero_initial_condition.argtypes = [ctx, C.c_int]
-    L.mgd_run_linearized.argtypes = [ctx]
+    L.mgd_run_linearized.argtypes = [ctx, C.POINTER(C.c_double), C.c_longlong, C.POINTER(C.c_double)]
     L.mgd_get_gradient.argtypes = [ctx, C.POINTER(C.c_double), C.c_longlong]
     L.mgd_time_step_size.argtypes = [ctx, C.POINTER(C.c_double)]
     L.mgd_actuator_weights.argtypes = [ctx, C.POINTER(C.c_double)]
@@ -194,10 +194,19 @@ class Solver:
         self._check(self.L.mgd_run_adjoint(self.h, C.byref(v)))
         return v.value
 
-    def run_linearized(self):
+    def run_linearized(self, delta_forcing=None):
         """Tangent run over the steps of the last run_forward: the perturbation
-        in FIELD_ADJOINT advances along the checkpointed trajectory."""
-        self._check(self.L.mgd_run_linearized(self.h))
+        in FIELD_ADJOINT advances along the checkpointed trajectory, the
+        actuators adding the control perturbation delta_forcing (entries x
+        actuator points, or None). Returns the tangent of the functional."""
+        v = C.c_double()
+        if delta_forcing is None:
+            self._check(self.L.mgd_run_linearized(self.h, None, 0, C.byref(v)))
+        else:
+            a = np.ascontiguousarray(delta_forcing, dtype=np.float64)
+            n = a.size // max(1, self.actuator_points())
+            self._check(self.L.mgd_run_linearized(self.h, capi.dptr(a), n, C.byref(v)))
+        return v.value
 
     def set_adjoint_nonzero_initial_condition(self, enable):
         """adjoint_nonzero_initial_condition: run_adjoint starts from the adjoint

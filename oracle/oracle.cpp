@@ -680,6 +680,9 @@ struct Region {
   std::vector<mgd_acoustic_source> sources;
   std::string error;
   bool adjointNonzeroIC = false;
+  bool linearizedControl = false;           // runLinearized: actuators add the control perturbation
+  std::vector<double> deltaForcingEntries;  // control perturbation of a tangent run, file order
+  long long nDeltaForcingEntries = 0;
   // run state
   std::vector<double> forcingEntries;  // control forcing, file order
   long long nForcingEntries = 0;
@@ -1871,7 +1874,9 @@ static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjoi
         });
       break;
     case MGD_PATCH_ACTUATOR:
-      if (mode != MGD_FORWARD || !R.o.controller_switch) break;
+      // FORWARD adds the control forcing, LINEARIZED (in a tangent run) its
+      // perturbation (src/ActuatorPatchImpl.f90:162-170)
+      if (!R.o.controller_switch || !(mode == MGD_FORWARD || (mode == MGD_LINEARIZED && R.linearizedControl))) break;
       for (int l = 0; l < nU; ++l)
         forPatchPoints(p, b, [&](long long gi, long long pi) {
           if (b.iblank[gi] == 0) return;
@@ -2324,22 +2329,78 @@ static double runAdjoint(Region& R) {
   return s;
 }
 
+// Tangent of the acoustic-noise functional at the current forward state
+// along the perturbation in adjointVariables: the patch quadrature of
+// m_t 2 (p - p_mean) delta p, delta p = (gamma - 1)(|u|^2/2 delta rho
+// - u . delta(rho u) + delta E).
+static double functionalTangent(Region& R) {
+  const double g = R.o.ratio_of_specific_heats;
+  double dJ = 0.0;
+  for (size_t bi = 0; bi < R.blocks.size(); ++bi) {
+    Block& b = R.blocks[bi];
+    const long long N = b.N;
+    std::vector<double> f(N);
+    for (long long p = 0; p < N; ++p) {
+      const std::vector<double>& x = b.adjointVariables;
+      double u2 = 0.0, ux = 0.0;
+      for (int d = 0; d < R.nD; ++d) {
+        const double u = b.velocity[N * d + p];
+        u2 += u * u;
+        ux += u * x[N * (d + 1) + p];
+      }
+      const double dp = (g - 1.0) * (0.5 * u2 * x[p] - ux + x[N * (R.nD + 1) + p]);
+      const double F = b.pressure[p] - b.meanPressure[p];
+      f[p] = 2.0 * F * dp * b.targetMollifier[p];
+    }
+    dJ += quadratureOnPatches(R, b, (int)bi, MGD_PATCH_COST_TARGET, f.data());
+  }
+  return dJ;
+}
+
 // Solver%runLinearized, src/SolverImpl.f90:1300-1450, over the steps of the
 // last runForward: the perturbation in adjointVariables advances along the
-// kept stage states with the forward run's step sizes; the final forward
-// state is restored afterwards.
-static void runLinearized(Region& R) {
+// kept stage states with the forward run's step sizes, the actuators adding
+// the control perturbation when one is set. Returns the tangent of the
+// time-integrated functional, sum over stages of w_i dt times the
+// functional's tangent after each stage (the forward run's quadrature). The
+// final forward state is restored afterwards.
+static double runLinearized(Region& R) {
   std::vector<double> finalState;
   for (Block& b : R.blocks) finalState.insert(finalState.end(), b.conservedVariables.begin(), b.conservedVariables.end());
-  double time = R.t0;
+  const bool control = R.o.enable_controller && R.o.controller_switch && R.nDeltaForcingEntries > 0;
+  const bool functional = R.o.enable_functional && R.o.functional_type == MGD_FUNCTIONAL_SOUND;
+  const std::vector<double> savedEntries = R.forcingEntries;
+  const long long savedN = R.nForcingEntries;
+  if (control) {
+    R.forcingEntries = R.deltaForcingEntries;
+    R.nForcingEntries = R.nDeltaForcingEntries;
+  }
+  R.linearizedControl = control;
+  double time = R.t0, dJ = 0.0;
   for (int step = 1; step <= R.nSteps; ++step) {
     const double dt = R.stepDt[step - 1];
     for (int i = 1; i <= 4; ++i) {
       setForwardState(R, R.stageStates[(size_t)(step - 1) * 4 + (i - 1)]);
+      if (control) loadForcing(R, step, i);
       substep(R, MGD_LINEARIZED, time, dt, i, false);
+      if (functional) {
+        // forward state after stage i
+        if (i < 4) setForwardState(R, R.stageStates[(size_t)(step - 1) * 4 + i]);
+        else if (step < R.nSteps) setForwardState(R, R.stageStates[(size_t)step * 4]);
+        else setForwardState(R, finalState);
+        dJ = dJ + kRkNorm[i - 1] * dt * functionalTangent(R);
+      }
     }
   }
+  R.linearizedControl = false;
+  if (control) {
+    R.forcingEntries = savedEntries;
+    R.nForcingEntries = savedN;
+    for (Patch& p : R.patches)
+      if (p.d.type == MGD_PATCH_ACTUATOR) std::fill(p.controlForcing.begin(), p.controlForcing.end(), 0.0);
+  }
   setForwardState(R, finalState);
+  return dJ;
 }
 
 }  // namespace orc
@@ -2452,14 +2513,18 @@ int orc_add_patch(void* h, const mgd_patch_desc* p) {
   return 0;
 }
 
-int orc_run_linearized(void* h) {
+int orc_run_linearized(void* h, const double* deltaForcing, long long nEntries, double* deltaCost) {
   Region& R = *(Region*)h;
   R.error.clear();
   if (R.stageStates.empty()) {
     R.error = "run_linearized needs a preceding run_forward that kept its stages";
     return 1;
   }
-  orc::runLinearized(R);
+  const long long P = orc::actuatorPoints(R);
+  R.nDeltaForcingEntries = deltaForcing ? nEntries : 0;
+  R.deltaForcingEntries.assign(deltaForcing ? deltaForcing : nullptr, deltaForcing ? deltaForcing + P * nEntries : nullptr);
+  const double dJ = orc::runLinearized(R);
+  if (deltaCost) *deltaCost = dJ;
   return R.error.empty() ? 0 : 1;
 }
 

@@ -50,7 +50,7 @@ def lib():
         L.orc_run_forward_nostore.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double)]
         L.orc_run_adjoint.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.orc_set_adjoint_nonzero_initial_condition.argtypes = [C.c_void_p, C.c_int]
-        L.orc_run_linearized.argtypes = [C.c_void_p]
+        L.orc_run_linearized.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_longlong, C.POINTER(C.c_double)]
         L.orc_time_step_size.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.orc_step_sizes.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.orc_get_gradient.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_longlong]
@@ -201,9 +201,17 @@ class Oracle:
     def set_adjoint_nonzero_initial_condition(self, enable):
         self.L.orc_set_adjoint_nonzero_initial_condition(self.h, int(bool(enable)))
 
-    def run_linearized(self):
-        if self.L.orc_run_linearized(self.h) != 0:
+    def run_linearized(self, delta_forcing=None):
+        """Tangent run; returns the tangent of the functional."""
+        v = C.c_double()
+        if delta_forcing is None:
+            rc = self.L.orc_run_linearized(self.h, None, 0, C.byref(v))
+        else:
+            a = np.ascontiguousarray(delta_forcing, dtype=np.float64)
+            rc = self.L.orc_run_linearized(self.h, capi.dptr(a), a.size // max(1, self.actuator_points()), C.byref(v))
+        if rc != 0:
             raise RuntimeError(self.L.orc_last_error(self.h).decode())
+        return v.value
 
     def time_step_size(self):
         v = C.c_double()

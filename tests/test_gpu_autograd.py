@@ -57,3 +57,30 @@ def test_backward_matches_oracle_gradient():
     assert abs(J.item() - Jo) <= 1e-10 * abs(Jo)
     g = ft.grad.cpu().numpy()
     assert np.linalg.norm(g - go) <= 1e-10 * np.linalg.norm(go)
+
+
+@pytest.mark.parametrize("device", ["cuda", "cpu"])
+def test_forward_mode_jvp_matches_the_adjoint_gradient(device):
+    """torch forward-mode AD through the tangent run: <dJ/df, t> from the jvp
+    equals the same inner product from the backward (adjoint) gradient, and
+    the oracle's tangent run gives the same value."""
+    import torch.autograd.forward_ad as fwAD
+    P = _problem()
+    s = Solver(P)
+    n_act = s.actuator_points()
+    rng = np.random.default_rng(5)
+    f0 = torch.tensor(1e-3 * rng.standard_normal((4 * N_STEPS, n_act)), dtype=torch.float64, device=device)
+    t = torch.tensor(rng.standard_normal((4 * N_STEPS, n_act)), dtype=torch.float64, device=device)
+    with fwAD.dual_level():
+        J = ForwardRun.apply(fwAD.make_dual(f0, t), s, N_STEPS, S)
+        jvp = float(fwAD.unpack_dual(J).tangent)
+    f1 = f0.clone().requires_grad_(True)
+    ForwardRun.apply(f1, s, N_STEPS, S).backward()
+    vjp = float((f1.grad * t).sum())
+    assert abs(jvp - vjp) <= 1e-10 * abs(vjp)
+    o = oracle_lib.Oracle(P)
+    o.set_control_forcing(f0.cpu().numpy())
+    o.run_forward(N_STEPS, S)
+    o.set_field(1, 1, np.zeros((4, P.blocks[0].n_points)))
+    dJ = o.run_linearized(t.cpu().numpy())
+    assert abs(jvp - dJ) <= 1e-10 * abs(dJ)

@@ -597,3 +597,35 @@ def test_linearized_and_adjoint_runs_are_dual():
     o.run_adjoint()
     a = np.sum(o.get_field(1, capi.FIELD_ADJOINT) * H * dq)
     assert abs(a - b) <= 1e-11 * abs(b)
+
+
+def test_tangent_run_of_the_functional_matches_the_adjoint_and_central_differences():
+    """Forward mode through the tangent run: along the adjoint gradient
+    direction the tangent of J equals the adjoint's sensitivity to rounding
+    (jvp = vjp), and along a random control perturbation it matches central
+    differences of J."""
+    P = small_monopole(n=29, ny=29, n_steps=12, save_interval=4)
+    P.options.controller_switch = True
+    o = oracle_lib.Oracle(P)
+    N = P.blocks[0].n_points
+    zeros = np.zeros((4, N))
+    J0 = o.run_forward(P.n_steps, 4)
+    G0 = o.run_adjoint()
+    g = o.gradient(4 * P.n_steps)
+    o.run_forward(P.n_steps, 4)
+    o.set_field(1, capi.FIELD_ADJOINT, zeros)
+    dJ = o.run_linearized(g)
+    assert abs(dJ - G0) <= 1e-11 * abs(G0)
+    rng = np.random.default_rng(2)
+    df = rng.standard_normal(g.shape)
+    o.set_field(1, capi.FIELD_ADJOINT, zeros)
+    dJr = o.run_linearized(df)
+    best = 1.0
+    for e in (1e-1, 1e-2, 1e-3):
+        Js = []
+        for sgn in (1.0, -1.0):
+            o2 = oracle_lib.Oracle(P)
+            o2.set_control_forcing(sgn * e * df)
+            Js.append(o2.run_forward(P.n_steps, keep_stages=False))
+        best = min(best, abs((Js[0] - Js[1]) / (2 * e) - dJr) / abs(dJr))
+    assert best < 1e-5
