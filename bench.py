@@ -347,6 +347,19 @@ def run_ours(args):
                      "fp64": {"achieved_tflops": achieved_tf, "peak_tflops": fp64_peak,
                               "frac": achieved_tf / fp64_peak, "peak_source": "measured: cuBLAS DGEMM 4096^3"}},
     }
+    if rank == 0 and world == 1:
+        # the same gradient through the per-call entry points (the reference's own
+        # control flow over the computeRhs seam), timed once beside the graph path
+        from magudi_gb300.drivers import per_call_gradient
+        t_start = time.perf_counter()
+        Jp, Gp = per_call_gradient(s, P, n_steps, SAVE_INTERVAL)
+        tp = time.perf_counter() - t_start
+        line["plain_per_call"] = {
+            "value": pts * 8 * n_steps / tp / 1e6, "unit": "Mpt-RHS/s", "seconds": tp,
+            "speedup_of_graph_path": tp / (ms / 1e3),
+            "J_rel_diff": abs(Jp - J) / abs(J), "grad0_rel_diff": abs(Gp - G) / abs(G),
+            "path": "mgd_rk4_substep + functional/sensitivity calls per stage, checkpoints and segment "
+                    "stage states in host memory (Solver%runForward / runAdjoint with UniformCheckpointer)"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, dt, cores = cpu_sample(args.cpu_sample_steps)
         line["cpu_baseline"] = {"value": v, "unit": "Mpt-RHS/s", "cores": cores, "kind": "port",

@@ -214,3 +214,16 @@ def test_controlled_forward_matches_oracle():
     J1g = g2.run_forward(P.n_steps, P.save_interval)
     J1o = o2.run_forward(P.n_steps, P.save_interval)
     assert abs(J1g - J1o) <= RUN_TOL * abs(J1o)
+
+
+def test_per_call_control_flow_reproduces_the_runs_on_the_gpu():
+    """The reference's solver loop over the per-call C entry points gives the
+    J and gradient norm of mgd_run_forward / mgd_run_adjoint."""
+    from magudi_gb300.drivers import per_call_gradient
+    P = small_monopole(n_steps=13, save_interval=5)
+    s = Solver(P)
+    J = s.run_forward(P.n_steps, 5)
+    G = s.run_adjoint()
+    Jp, Gp = per_call_gradient(Solver(P), P, P.n_steps, 5)
+    assert abs(Jp - J) <= 1e-12 * abs(J)
+    assert abs(Gp - G) <= 1e-11 * abs(G)

@@ -629,3 +629,17 @@ def test_tangent_run_of_the_functional_matches_the_adjoint_and_central_differenc
             Js.append(o2.run_forward(P.n_steps, keep_stages=False))
         best = min(best, abs((Js[0] - Js[1]) / (2 * e) - dJr) / abs(dJr))
     assert best < 1e-5
+
+
+def test_per_call_control_flow_reproduces_the_runs():
+    """The reference's solver loop over the per-call entry points
+    (magudi_gb300.drivers) gives the J and gradient norm of the run entry
+    points, on the oracle."""
+    from magudi_gb300.drivers import per_call_gradient
+    P = small_monopole(n=29, ny=29, n_steps=11, save_interval=4)
+    o = oracle_lib.Oracle(P)
+    J = o.run_forward(P.n_steps, 4)
+    G = o.run_adjoint()
+    Jp, Gp = per_call_gradient(oracle_lib.Oracle(P), P, P.n_steps, 4)
+    assert abs(Jp - J) <= 1e-12 * abs(J)
+    assert abs(Gp - G) <= 1e-12 * abs(G)
