@@ -26,6 +26,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -102,7 +103,8 @@ class ClockSampler:
 
     def __init__(self):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks.csv") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/mgd_clocks.csv"
+        # raw samples; the JSON line carries their summary (MGD_CLOCKS_CSV keeps a copy elsewhere)
+        self.path = os.environ.get("MGD_CLOCKS_CSV", os.path.join(tempfile.gettempdir(), "mgd_clocks.csv"))
 
     def start(self):
         try:
