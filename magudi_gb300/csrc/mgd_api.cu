@@ -1431,24 +1431,31 @@ int mgd_update_state(mgd_ctx* h) {
   return 0;
 }
 
-// The linearized RHS covers the far-field, wall, sponge, actuator and
-// cost-target patches; contexts with other patch types are refused for that mode.
+// The linearized RHS covers every patch type but the solenoidal excitation,
+// which the reference does not linearize either.
 static int refuseLinearized(Context& c) {
   for (const mgd_patch_desc& p : c.patches)
-    if (p.type == MGD_PATCH_BLOCK_INTERFACE || p.type == MGD_PATCH_SOLENOIDAL_EXCITATION)
-      return fail(c, "the linearized RHS takes far-field, wall, sponge, actuator and cost-target patches only");
+    if (p.type == MGD_PATCH_SOLENOIDAL_EXCITATION)
+      // addSolenoidalExcitation has no LINEARIZED branch (src/SolenoidalExcitationPatchImpl.f90:192)
+      return fail(c, "the linearized RHS does not take solenoidal-excitation patches");
   return 0;
 }
 
 // The linearized RHS (rkStage 0) or one linearized RK stage of every block:
-// the perturbation in lambda about the current conserved state.
+// the perturbation in lambda about the current conserved state. The fluxes of
+// every block come first, then the interface SATs (which read the partner
+// blocks' perturbations and linearized viscous fluxes), then the divergence
+// and update of each block.
 static void linearizedStages(Context& c, int rkStage, const RunScalars& rs, double factor) {
   for (DevBlock& x : c.blocks) {
     launchPrims(c, x, x.v.q, false);
     if (c.phys.viscous) launchGradFlux(c, x, false, true, &rs, 1, false);
     if (c.phys.dissipation) launchDissipation(c, x, x.v.lam, 1.0);
-    launchLinearized(c, x, rkStage, rs, factor);
+    launchLinearizedFlux(c, x, rs, 1, false);
   }
+  const BlockRefs refs = blockRefs(c);
+  for (DevBlock& x : c.blocks) launchInterfaceSatLinearized(c, x, refs);
+  for (DevBlock& x : c.blocks) launchLinearizedDivergence(c, x, rkStage, rs, factor, 1, false);
 }
 
 int mgd_compute_rhs(mgd_ctx* h, int mode, double time, double adjoint_forcing_factor) {

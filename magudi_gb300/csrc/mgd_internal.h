@@ -359,6 +359,12 @@ void launchForwardDivergence(Context& c, DevBlock& b, int rkStage, const RunScal
 // reference's LINEARIZED mode adds it.
 void launchLinearized(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, double factor, int stage = 1,
                       bool fromSlot = false, bool controller = false, cudaStream_t s = 0);
+// The two halves of launchLinearized for multi-block regions, whose interface
+// SATs (launchInterfaceSatLinearized) go between them.
+void launchLinearizedFlux(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool fromSlot, cudaStream_t s = 0);
+void launchLinearizedDivergence(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, double factor, int stage,
+                                bool controller, cudaStream_t s = 0);
+void launchInterfaceSatLinearized(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_t s = 0);
 // Tangent of the functional at the forward state of (step, stage) along lambda,
 // into the partial sums of the stage before.
 void launchFunctionalTangent(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool fromSlot,

@@ -1012,6 +1012,16 @@ __global__ void __launch_bounds__(kMaxTile) kLinearizedFlux(BlockView B, Physics
     for (int s = 0; s < 3; ++s) {
       const int e = B.ffOfPoint[3 * p + s];
       if (e < 0 || B.ff.normalDir[e] - 1 != i) continue;
+      if (B.ff.kind[e] == SAT_INTERFACE) {
+        // the interface keeps its side's linearized viscous flux along its
+        // normal for kInterfaceSatLinearized (src/RhsHelperImpl.f90:788-800)
+        if (VISC) {
+          double* out = B.ff.ifVisc + (long long)e * nU;
+          out[0] = 0.0;
+          for (int r = 1; r < nU; ++r) out[r] = Bx[r];
+        }
+        continue;
+      }
       if (B.ff.kind[e] == SAT_WALL || B.ff.kind[e] == SAT_ISOTHERMAL_WALL) {
         // linearized wall penalties (src/ImpenetrableWallImpl.f90:187-191,
         // src/IsothermalWallImpl.f90:309-322): -s_inv J (A(m) - m (dp/dq)) dq,
@@ -1288,6 +1298,59 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSat(BlockView B, Physics P, 
     double t = A[r] * dq[0];
     for (int c = 1; c < nU; ++c) t += A[r + nU * c] * dq[c];
     double v = -(s * jac * t);
+    if (VISC && r > 0) v += jac * (vL * fL[r] + vR * fR[r]);
+    sat[r] = v;
+  }
+}
+
+// Linearized block-interface SAT of one entry (src/BlockInterfacePatchImpl.f90:468-515):
+// -s_inv J (A+ (dq_L - dq_R) + (dA+ along (dq_L, dq_R)) (q_L - q_R)), the
+// derivative of the Roe-averaged A+ taken on one-derivative dual numbers, plus
+// J (s_vL F_L + s_vR F_R) with the two sides' linearized viscous fluxes.
+template <int ND, bool VISC>
+__global__ void __launch_bounds__(kBlock) kInterfaceSatLinearized(BlockView B, Physics P, BlockRefs R) {
+  pdlEnter();
+  const int e = blockIdx.x * kBlock + threadIdx.x;
+  if (e >= B.ff.n || B.ff.kind[e] != SAT_INTERFACE) return;
+  constexpr int nU = ND + 2;
+  using D = DualN<1>;
+  const long long N = B.N, p = B.ff.point[e];
+  const int pb = B.ff.partnerBlock[e];
+  const long long pp = B.ff.partnerPoint[e], NR = R.N[pb];
+  double dq[nU], dx[nU], mL[ND];
+  D dL[nU], dR[nU], roe[nU];
+  for (int c = 0; c < nU; ++c) {
+    const double qL = B.q[p + N * c], qR = R.q[pb][pp + NR * c];
+    const double xL = B.lam[p + N * c], xR = R.lam[pb][pp + NR * c];
+    dq[c] = qL - qR;
+    dx[c] = xL - xR;
+    dL[c] = D(qL);
+    dL[c].d[0] = xL;
+    dR[c] = D(qR);
+    dR[c].d[0] = xR;
+  }
+  for (int d = 0; d < ND; ++d) mL[d] = B.metrics[p + N * (ND * (B.ff.normalDir[e] - 1) + d)];
+  roeAverage<ND, D>(dL, dR, P.g, roe);
+  D A[nU * nU];
+  incomingJacobian<ND, D>(roe, mL, P.g, B.ff.dirL[e], A);
+  const double jac = B.jac[p];
+  const double s = B.ff.ifInv[2 * e];
+  double vL = 0.0, vR = 0.0;
+  if (VISC) {
+    const double a = fabs(B.ff.ifVis[2 * e]);
+    vL = B.ff.dirL[e] < 0 ? -a : a;
+    vR = B.ff.dirR[e] < 0 ? -a : a;
+  }
+  const double* fL = B.ff.ifVisc + (long long)e * nU;
+  const double* fR = R.ifVisc[pb] + (long long)B.ff.partnerEntry[e] * nU;
+  double* sat = B.ff.visc + (long long)e * nU;
+  for (int r = 0; r < nU; ++r) {
+    double t1 = A[r].v * dx[0], t2 = A[r].d[0] * dq[0];
+    for (int c = 1; c < nU; ++c) {
+      t1 += A[r + nU * c].v * dx[c];
+      t2 += A[r + nU * c].d[0] * dq[c];
+    }
+    double v = -(s * jac * t1) - s * jac * t2;
     if (VISC && r > 0) v += jac * (vL * fL[r] + vR * fR[r]);
     sat[r] = v;
   }
@@ -1713,8 +1776,7 @@ void launchForwardDivergence(Context& c, DevBlock& b, int rkStage, const RunScal
     pdl(kForwardDivergence<3>, grid, T.threads(), on(c, s), b.v, c.phys, rs, rkStage, stage, controller, T, 0, 0.0);
 }
 
-void launchLinearized(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, double factor, int stage,
-                      bool fromSlot, bool controller, cudaStream_t s) {
+void launchLinearizedFlux(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool fromSlot, cudaStream_t s) {
   const cudaStream_t st = on(c, s);
   const int fsl = fromSlot ? 1 : 0;
   if (c.phys.viscous) {
@@ -1722,23 +1784,44 @@ void launchLinearized(Context& c, DevBlock& b, int rkStage, const RunScalars& rs
     if (c.nD == 2) pdl(kLinearizedTemp<2>, gridFor(b.v.N), kBlock, st, b.v, c.phys, rs, stage, fsl);
     else pdl(kLinearizedTemp<3>, gridFor(b.v.N), kBlock, st, b.v, c.phys, rs, stage, fsl);
   }
-  {
-    const Tile T = b.tGrad;
-    MGD_LAUNCH(c);
+  const Tile T = b.tGrad;
+  MGD_LAUNCH(c);
 #define LF(ND, VISC) pdl(kLinearizedFlux<ND, VISC>, T.blocks(), T.threads(), st, b.v, c.phys, rs, stage, fsl, T)
-    if (c.nD == 2) { if (c.phys.viscous) LF(2, true); else LF(2, false); }
-    else { if (c.phys.viscous) LF(3, true); else LF(3, false); }
+  if (c.nD == 2) { if (c.phys.viscous) LF(2, true); else LF(2, false); }
+  else { if (c.phys.viscous) LF(3, true); else LF(3, false); }
 #undef LF
+}
+
+void launchInterfaceSatLinearized(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_t s) {
+  if (b.nInterfaceEntries == 0) return;
+  const int G = gridFor(b.v.ff.n);
+  MGD_LAUNCH(c);
+  if (c.nD == 2) {
+    if (c.phys.viscous) pdl(kInterfaceSatLinearized<2, true>, G, kBlock, on(c, s), b.v, c.phys, r);
+    else pdl(kInterfaceSatLinearized<2, false>, G, kBlock, on(c, s), b.v, c.phys, r);
+  } else {
+    if (c.phys.viscous) pdl(kInterfaceSatLinearized<3, true>, G, kBlock, on(c, s), b.v, c.phys, r);
+    else pdl(kInterfaceSatLinearized<3, false>, G, kBlock, on(c, s), b.v, c.phys, r);
   }
+}
+
+void launchLinearizedDivergence(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, double factor, int stage,
+                                bool controller, cudaStream_t s) {
   // the divergence and RK update act on the perturbation: a view with q = lambda
   BlockView v = b.v;
   v.q = b.v.lam;
   const Tile T = b.tRhs;
   const dim3 grid(T.blocks(), c.nU);
-  MGD_LAUNCH(c);
   const int ctl = controller ? 1 : 0;
-  if (c.nD == 2) pdl(kForwardDivergence<2>, grid, T.threads(), st, v, c.phys, rs, rkStage, stage, ctl, T, 1, factor);
-  else pdl(kForwardDivergence<3>, grid, T.threads(), st, v, c.phys, rs, rkStage, stage, ctl, T, 1, factor);
+  MGD_LAUNCH(c);
+  if (c.nD == 2) pdl(kForwardDivergence<2>, grid, T.threads(), on(c, s), v, c.phys, rs, rkStage, stage, ctl, T, 1, factor);
+  else pdl(kForwardDivergence<3>, grid, T.threads(), on(c, s), v, c.phys, rs, rkStage, stage, ctl, T, 1, factor);
+}
+
+void launchLinearized(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, double factor, int stage,
+                      bool fromSlot, bool controller, cudaStream_t s) {
+  launchLinearizedFlux(c, b, rs, stage, fromSlot, s);
+  launchLinearizedDivergence(c, b, rkStage, rs, factor, stage, controller, s);
 }
 
 void launchFunctional(Context& c, DevBlock& b, const RunScalars& rs, int stage, cudaStream_t s) {

@@ -1597,11 +1597,21 @@ static void computeRhsLinearized(Region& R, Block& b, int bi) {
         for (int r = 0; r < nV; ++r) f2[N * (r + 1 + nU * i) + k] = f2[N * (r + 1 + nU * i) + k] + lin[r + nV * i];
       }
     }
-    // far-field patches keep the linearized viscous fluxes (src/RhsHelperImpl.f90:788-800)
+    // far-field and block-interface patches keep the linearized viscous fluxes
+    // (src/RhsHelperImpl.f90:788-800); an interface keeps the contravariant
+    // flux along its normal direction
     for (Patch& p : R.patches) {
-      if (p.d.grid_index != bi + 1 || p.nPatchPoints <= 0 || p.d.type != MGD_PATCH_SAT_FAR_FIELD) continue;
-      for (int c = 0; c < nU * nD; ++c)
-        forPatchPoints(p, b, [&](long long gi, long long pi) { p.viscousFluxes[p.nPatchPoints * c + pi] = f2[N * c + gi]; });
+      if (p.d.grid_index != bi + 1 || p.nPatchPoints <= 0) continue;
+      if (p.d.type == MGD_PATCH_SAT_FAR_FIELD)
+        for (int c = 0; c < nU * nD; ++c)
+          forPatchPoints(p, b, [&](long long gi, long long pi) { p.viscousFluxes[p.nPatchPoints * c + pi] = f2[N * c + gi]; });
+      if (p.d.type == MGD_PATCH_BLOCK_INTERFACE) {
+        const int dir = std::abs(p.d.normal_direction) - 1;
+        forPatchPoints(p, b, [&](long long gi, long long pi) {
+          p.ifViscousFlux[pi] = 0.0;
+          for (int c = 1; c < nU; ++c) p.ifViscousFlux[p.nPatchPoints * c + pi] = f2[N * (c + nU * dir) + gi];
+        });
+      }
     }
     for (long long k = 0; k < N * nU * nD; ++k) f1[k] = f1[k] - f2[k];
   }
@@ -1717,6 +1727,41 @@ static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjoi
             double s = A[r] * dq[0];
             for (int c = 1; c < nU; ++c) s += A[r + nU * c] * dq[c];
             b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] - sInvL * jac * s;
+          }
+          if (R.o.viscous) {
+            const double vL = std::copysign(std::abs(p.viscousPenaltyAmount), (double)dirL);
+            const double vR = std::copysign(std::abs(p.viscousPenaltyAmount), (double)dirR);
+            for (int r = 1; r < nU; ++r)
+              b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] +
+                  jac * (vL * p.ifViscousFlux[p.nPatchPoints * r + pi] + vR * q.ifViscousFlux[q.nPatchPoints * r + qpi]);
+          }
+          return;
+        }
+        if (mode == MGD_LINEARIZED) {
+          // src/BlockInterfacePatchImpl.f90:468-515: A+ of the Roe average applied to
+          // (delta q_L - delta q_R) plus its derivative along (delta q_L, delta q_R)
+          // applied to (q_L - q_R), the derivative on dual numbers; the viscous
+          // part with the collected linearized viscous fluxes of both sides
+          double xL[5], xR[5];
+          Dual dL[5], dR[5], droe[5], AL[25];
+          for (int c = 0; c < nU; ++c) {
+            xL[c] = b.adjointVariables[N * c + gi];
+            xR[c] = bq.adjointVariables[bq.N * c + qgi];
+            dL[c] = Dual(qL[c]);
+            dL[c].d[0] = xL[c];
+            dR[c] = Dual(qR[c]);
+            dR[c].d[0] = xR[c];
+          }
+          roeAverage<Dual>(nD, dL, dR, g, droe);
+          incomingJacobianT<Dual>(nD, droe, mL, g, dirL, AL);
+          for (int r = 0; r < nU; ++r) {
+            double s1 = AL[r].v * (xL[0] - xR[0]), s2 = AL[r].d[0] * dq[0];
+            for (int c = 1; c < nU; ++c) {
+              s1 += AL[r + nU * c].v * (xL[c] - xR[c]);
+              s2 += AL[r + nU * c].d[0] * dq[c];
+            }
+            b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] - sInvL * jac * s1;
+            b.rightHandSide[N * r + gi] = b.rightHandSide[N * r + gi] - sInvL * jac * s2;
           }
           if (R.o.viscous) {
             const double vL = std::copysign(std::abs(p.viscousPenaltyAmount), (double)dirL);
@@ -1947,8 +1992,10 @@ static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjoi
 static void computeRhs(Region& R, int mode, double time, double adjointForcingFactor) {
   if (mode == MGD_LINEARIZED)
     for (Patch& p : R.patches)
-      if (p.d.type == MGD_PATCH_BLOCK_INTERFACE || p.d.type == MGD_PATCH_SOLENOIDAL_EXCITATION) {
-        R.error = "the linearized RHS takes far-field, wall, sponge, actuator and cost-target patches only";
+      if (p.d.type == MGD_PATCH_SOLENOIDAL_EXCITATION) {
+        // addSolenoidalExcitation has no LINEARIZED branch (assert_key(mode, (FORWARD, ADJOINT)),
+        // src/SolenoidalExcitationPatchImpl.f90:192)
+        R.error = "the linearized RHS does not take solenoidal-excitation patches";
         return;
       }
   for (size_t bi = 0; bi < R.blocks.size(); ++bi) {

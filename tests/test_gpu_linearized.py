@@ -96,9 +96,41 @@ def test_linearized_rhs_with_walls_matches_oracle(wall):
     assert rel_err(*(s.get_field(1, capi.FIELD_RHS) for s in pair)) < RHS_TOL
 
 
-def test_linearized_rhs_refuses_block_interfaces():
+def _small_jet_without_excitation():
+    P = configs.jet_3block_3d(nx=28, ny_core=25, ny_side=26, nz=25, length=4.0, n_steps=4, save_interval=2)
+    P.patches = [p for p in P.patches if p.type != "SOLENOIDAL_EXCITATION"]
+    return P
+
+
+@pytest.mark.parametrize("name", ["two_block", "two_block_rotated", "jet3d"])
+def test_linearized_rhs_with_block_interfaces_matches_oracle(name):
+    if name == "jet3d":
+        P = _small_jet_without_excitation()
+    else:
+        P = configs.two_block_2d(rotate_second=name.endswith("rotated"))
+    rng = np.random.default_rng(8)
+    states = []
+    for b in P.blocks:
+        q = configs.smooth_perturbed_state(b, P.options.n_dimensions, 1.4, rng, amplitude=0.05)
+        dq = rng.uniform(-1.0, 1.0, q.shape) * np.abs(q).mean(axis=1, keepdims=True)
+        states.append((q, dq))
+    pair = Solver(P), oracle_lib.Oracle(P)
+    for s in pair:
+        for bi, (q, dq) in enumerate(states, start=1):
+            s.set_field(bi, capi.FIELD_CONSERVED, q)
+            s.set_field(bi, capi.FIELD_ADJOINT, dq)
+        s.update_state()
+        s.compute_rhs(capi.LINEARIZED, 0.2, 0.0)
+    for bi in range(1, len(P.blocks) + 1):
+        assert rel_err(*(s.get_field(bi, capi.FIELD_RHS) for s in pair)) < RHS_TOL
+
+
+def test_linearized_rhs_refuses_solenoidal_excitation():
+    from helpers import add_solenoidal_excitation
     from magudi_gb300.solver import MagudiError
-    s = Solver(configs.two_block_2d())
+    P = small_monopole(n=31, ny=29, sponge_points=5)
+    add_solenoidal_excitation(P, extent=(4, 26, 3, 25, 1, -1))
+    s = Solver(P)
     with pytest.raises(MagudiError):
         s.compute_rhs(capi.LINEARIZED, 0.0, 0.0)
 

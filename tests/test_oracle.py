@@ -547,8 +547,49 @@ def test_linearized_rhs_with_walls_is_derivative_and_transpose(wall):
     assert abs(a + b) <= 1e-11 * abs(a)
 
 
-def test_linearized_rhs_refuses_block_interfaces():
-    P = configs.two_block_2d()
+@pytest.mark.parametrize("rotate", [False, True])
+def test_linearized_rhs_with_block_interfaces_is_derivative_and_transpose(rotate):
+    """Linearized block-interface penalty (src/BlockInterfacePatchImpl.f90:468-515)
+    across two blocks: central differences of the forward RHS of both blocks
+    and exact transposition against the adjoint RHS."""
+    P = configs.two_block_2d(rotate_second=rotate)
+    rng = np.random.default_rng(21)
+    q0, dq, lam = [], [], []
+    for b in P.blocks:
+        q = configs.smooth_perturbed_state(b, 2, 1.4, rng, amplitude=0.05)
+        q0.append(q)
+        dq.append(rng.uniform(-1.0, 1.0, q.shape) * np.abs(q).mean(axis=1, keepdims=True))
+        lam.append(rng.uniform(-1.0, 1.0, q.shape))
+    def rhs(o, mode, states, field):
+        for bi in (1, 2):
+            o.set_field(bi, field, states[bi - 1])
+        if mode == capi.FORWARD:
+            o.update_state()
+        o.compute_rhs(mode, 0.3, 0.0)
+        return [o.get_field(bi, capi.FIELD_RHS) for bi in (1, 2)]
+    o = oracle_lib.Oracle(P)
+    for bi in (1, 2):
+        o.set_field(bi, capi.FIELD_CONSERVED, q0[bi - 1])
+    o.update_state()
+    H = [o.get_field(bi, capi.FIELD_NORM) for bi in (1, 2)]
+    L = rhs(o, capi.LINEARIZED, dq, capi.FIELD_ADJOINT)
+    nrm = np.sqrt(sum(np.sum(x ** 2) for x in L))
+    errs = []
+    for e in (1e-4, 1e-5):
+        rp = rhs(oracle_lib.Oracle(P), capi.FORWARD, [q + e * d for q, d in zip(q0, dq)], capi.FIELD_CONSERVED)
+        rm = rhs(oracle_lib.Oracle(P), capi.FORWARD, [q - e * d for q, d in zip(q0, dq)], capi.FIELD_CONSERVED)
+        errs.append(np.sqrt(sum(np.sum(((a - b) / (2 * e) - l) ** 2) for a, b, l in zip(rp, rm, L))) / nrm)
+    assert min(errs) < 1e-7
+    a = sum(np.sum(l_ * h * x) for l_, h, x in zip(lam, H, L))
+    Ra = rhs(o, capi.ADJOINT, lam, capi.FIELD_ADJOINT)
+    b = sum(np.sum(r * h * d) for r, h, d in zip(Ra, H, dq))
+    assert abs(a + b) <= 1e-11 * abs(a)
+
+
+def test_linearized_rhs_refuses_solenoidal_excitation():
+    from helpers import add_solenoidal_excitation
+    P = small_monopole(n=31, ny=29, sponge_points=5)
+    add_solenoidal_excitation(P, extent=(4, 26, 3, 25, 1, -1))
     o = oracle_lib.Oracle(P)
     o.update_state()
     with pytest.raises(RuntimeError):
