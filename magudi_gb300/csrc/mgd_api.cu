@@ -1706,7 +1706,10 @@ static int ensureStepBuffers(Context& c, DevBlock& b, int nSteps) {
     CUDA_TRY(c, cudaMalloc((void**)&c.dStepDt, (size_t)4 * nSteps * sizeof(double)));
     c.stepDtCapacity = 4LL * nSteps;
   }
-  const int nb = timeStepBlocks(b);
+  // partial minima of every block (a region's step size is the minimum over its blocks)
+  int nb = 0;
+  for (DevBlock& x : c.blocks) nb += timeStepBlocks(x);
+  (void)b;
   if (c.dtPartialCapacity < nb) {
     cudaFree(c.dDtPartials);
     c.dDtPartials = nullptr;
@@ -1990,8 +1993,8 @@ static void regionRunStage(Context& c, std::vector<RunScalars>& rs, int i, bool 
 }
 
 static int regionRunForward(Context& c, int n_steps, int save_interval, double t0, double* cost) {
-  if (c.opts.use_constant_cfl) return fail(c, "multi-block runs use a constant time_step_size");
   if (c.opts.functional_type != MGD_FUNCTIONAL_SOUND) return fail(c, "multi-block runs use the SOUND functional");
+  const bool cflMode = c.opts.use_constant_cfl != 0;
   if (prepareForwardRun(c, n_steps, save_interval, t0, false)) return 1;
   const long long nSnap = n_steps / save_interval + 2;
   for (DevBlock& b : c.blocks) {
@@ -2006,6 +2009,8 @@ static int regionRunForward(Context& c, int n_steps, int save_interval, double t
   for (size_t bi = 0; bi < c.blocks.size(); ++bi) rs.push_back(blockRunScalars(c, c.blocks[bi], bi == 0));
   if (setCounters(c, 1, 0)) return 1;
   if (capture(c, &c.gForward, &c.nodesForward, [&]() {
+        // constant CFL: the step size from every block's state at the start of the step
+        if (cflMode) launchTimeStepRegion(c, c.dDtPartials, c.dStepDt, c.dCounters, c.dTime, c.dStageTime, c.dAmp);
         for (int i = 1; i <= 4; ++i) regionRunStage(c, rs, i, controller, false, functional);
         for (DevBlock& b : c.blocks) launchSnapshot(c, b, b.runSnap, save_interval, false);
         launchStepAdvance(c, 1);
@@ -2015,6 +2020,13 @@ static int regionRunForward(Context& c, int n_steps, int save_interval, double t
   c.launches += (long long)n_steps * c.nodesForward;
   if (checkLaunch(c)) return 1;
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  if (cflMode) {
+    // recorded step sizes for J and the adjoint
+    std::vector<double> rk((size_t)4 * n_steps);
+    CUDA_TRY(c, cudaMemcpy(rk.data(), c.dStepDt, rk.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    c.stepDt.resize(n_steps);
+    for (int s = 0; s < n_steps; ++s) c.stepDt[s] = rk[4 * s];
+  }
   double J = 0.0;
   if (functional) {
     std::vector<double> vals;

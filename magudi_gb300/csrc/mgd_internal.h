@@ -399,6 +399,8 @@ void launchReducePartials(Context& c, const double* partials, int stride, int co
 void launchTimeStep(Context& c, DevBlock& b, double* partials, double* dtOut, const int* step, double* time,
                     double* stageTime, double* amp, cudaStream_t s = 0);
 int timeStepBlocks(const DevBlock& b);
+void launchTimeStepRegion(Context& c, double* partials, double* dtOut, const int* step, double* time,
+                          double* stageTime, double* amp, cudaStream_t s = 0);
 void launchAxpy(Context& c, double* z, const double* x, double a, long long n, bool accumulate);
 // Block-interface SAT vectors of block b's interface entries (forward; adjoint
 // with the interface terms of the adjoint viscous diffusion).

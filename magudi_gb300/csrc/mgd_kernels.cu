@@ -2061,6 +2061,31 @@ void launchTimeStep(Context& c, DevBlock& b, double* partials, double* dtOut, co
   pdl(kTimeStepFinalize, 1, 256, on(c, s), partials, nb, dtOut, step, time, stageTime, amp, src);
 }
 
+// The same over every block of a region: each block's partial minima at its
+// offset in partials, one finalize over all of them (the minimum over blocks
+// of Region%getTimeStepSize, src/RegionImpl.f90:1842-1875).
+void launchTimeStepRegion(Context& c, double* partials, double* dtOut, const int* step, double* time,
+                          double* stageTime, double* amp, cudaStream_t s) {
+  int off = 0;
+  for (DevBlock& b : c.blocks) {
+    const int nb = timeStepBlocks(b);
+    MGD_LAUNCH(c);
+    if (c.nD == 2) pdl(kTimeStepPartials<2>, nb, kBlock, on(c, s), b.v, c.phys, c.opts.cfl, partials + off);
+    else pdl(kTimeStepPartials<3>, nb, kBlock, on(c, s), b.v, c.phys, c.opts.cfl, partials + off);
+    off += nb;
+  }
+  SourceTable src{};
+  src.n = (int)c.sources.size();
+  src.twoPi = 2.0 * (4.0 * std::atan(1.0));
+  for (int k = 0; k < src.n; ++k) {
+    src.amplitude[k] = c.sources[k].amplitude;
+    src.frequency[k] = c.sources[k].frequency;
+    src.phase[k] = c.sources[k].phase;
+  }
+  MGD_LAUNCH(c);
+  pdl(kTimeStepFinalize, 1, 256, on(c, s), partials, off, dtOut, step, time, stageTime, amp, src);
+}
+
 void launchCoordinateDerivative(Context& c, DevBlock& b, int dir, double* out) {
   const double* coords = b.v.q;  // caller stages the coordinates in q
   MGD_LAUNCH(c);

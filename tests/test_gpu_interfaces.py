@@ -64,12 +64,22 @@ def test_two_block_rk4_substeps_match_oracle():
             assert rel_err(pair[0].get_field(bi, f), pair[1].get_field(bi, f)) < 1e-12
 
 
-def test_multiblock_runs_refuse_cfl_mode():
-    P = configs.two_block_2d()
+@pytest.mark.parametrize("rotate", [False, True])
+def test_two_block_constant_cfl_runs_match_oracle(rotate):
+    """Constant-CFL checkpointed runs across a block interface: the step size of
+    each step is the minimum over both blocks (Region%getTimeStepSize,
+    src/RegionImpl.f90:1842-1875), recorded for the adjoint."""
+    P = configs.two_block_2d(functional=True, rotate_second=rotate, n_steps=30, dt=0.05)
     P.options.use_constant_cfl = True
-    s = Solver(P)
-    with pytest.raises(MagudiError):
-        s.run_forward(4, 2)
+    P.options.cfl = 0.6
+    g, o = Solver(P), oracle_lib.Oracle(P)
+    Jg, Jo = g.run_forward(P.n_steps, 7), o.run_forward(P.n_steps, 7)
+    assert abs(Jg - Jo) <= 1e-10 * abs(Jo)
+    assert rel_err(g.step_sizes(P.n_steps), o.step_sizes(P.n_steps)) < 1e-13
+    Gg, Go = g.run_adjoint(), o.run_adjoint()
+    assert abs(Gg - Go) <= 1e-10 * abs(Go)
+    n = 4 * P.n_steps
+    assert rel_err(g.gradient(n), o.gradient(n)) < 1e-10
 
 
 @pytest.mark.parametrize("rotate", [False, True])
