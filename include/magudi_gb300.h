@@ -263,8 +263,8 @@ int mgd_run_adjoint(mgd_ctx* ctx, double* sensitivity);
  * (src/ActuatorPatchImpl.f90:162-170). *delta_cost (may be NULL) receives the
  * tangent of the time-integrated SOUND functional: with a zero initial
  * perturbation, the directional derivative of J along delta_forcing, the
- * forward-mode counterpart of mgd_run_adjoint's gradient. One block; the
- * patch types of MGD_LINEARIZED. */
+ * forward-mode counterpart of mgd_run_adjoint's gradient. Multi-block
+ * regions carry the block-interface SATs; the patch types of MGD_LINEARIZED. */
 int mgd_run_linearized(mgd_ctx* ctx, const double* delta_forcing, long long n_entries, double* delta_cost);
 
 /* adjoint_nonzero_initial_condition (src/SolverImpl.f90:1027-1102, set per

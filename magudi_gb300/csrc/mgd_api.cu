@@ -2290,11 +2290,13 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
 // the tangent of the functional, sum over stages of w_i dt times the
 // functional's tangent after each stage, is reduced like J. The conserved
 // state of the final step is restored at the end.
+static int regionRunLinearized(Context& c, const double* delta_forcing, long long n_entries, double* delta_cost);
+
 int mgd_run_linearized(mgd_ctx* h, const double* delta_forcing, long long n_entries, double* delta_cost) {
   Context& c = h->c;
   if (requireReady(c)) return 1;
   if (c.runSteps < 1) return fail(c, "mgd_run_linearized needs a preceding mgd_run_forward");
-  if (!singleBlock(c)) return fail(c, "mgd_run_linearized takes one block");
+  if (!singleBlock(c)) return regionRunLinearized(c, delta_forcing, n_entries, delta_cost);
   if (refuseLinearized(c)) return 1;
   DevBlock& b = c.blocks[0];
   const long long N = b.v.N;
@@ -2672,4 +2674,136 @@ int mgd_selftest_pow(const double* x, int n, double e, double* fast, double* ref
   const cudaError_t err = cudaGetLastError();
   cudaFree(dx); cudaFree(df); cudaFree(dr);
   return err == cudaSuccess ? 0 : 1;
+}
+
+// The tangent run of a multi-block region over the checkpoints of its last
+// forward run (regionRunForward): per segment, every block's stage states
+// are recomputed into its own slots, then the segment's linearized steps run
+// with the block-interface SATs between the blocks' fluxes and divergences.
+static int regionRunLinearized(Context& c, const double* delta_forcing, long long n_entries, double* delta_cost) {
+  if (refuseLinearized(c)) return 1;
+  const int nU = c.nU, nD = c.nD, T = c.runSteps, S = c.saveInterval;
+  const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
+  const bool deltaControl = c.opts.enable_controller && c.opts.controller_switch && delta_forcing && n_entries > 0 &&
+                            c.actuatorPoints > 0;
+  if (deltaControl) {
+    const long long n = n_entries * c.actuatorPoints;
+    if (c.deltaForcingCapacity < n) {
+      cudaFree(c.dDeltaForcing);
+      c.dDeltaForcing = nullptr;
+      c.deltaForcingCapacity = 0;
+      CUDA_TRY(c, cudaMalloc((void**)&c.dDeltaForcing, (size_t)n * sizeof(double)));
+      c.deltaForcingCapacity = n;
+    }
+    CUDA_TRY(c, cudaMemcpyAsync(c.dDeltaForcing, delta_forcing, (size_t)n * sizeof(double), cudaMemcpyDefault,
+                                c.stream));
+  }
+  const bool functional = c.opts.enable_functional && c.opts.functional_type == MGD_FUNCTIONAL_SOUND;
+  // stage slots as the region's adjoint run sizes them
+  size_t freeB = 0, totalB = 0;
+  CUDA_TRY(c, cudaMemGetInfo(&freeB, &totalB));
+  long long pts = 0, held = 0;
+  for (DevBlock& b : c.blocks) {
+    pts += b.v.N;
+    held += b.runStageCap;
+  }
+  const long long fullPer = nU + PrimLayout{nD}.count() + nD * nD + nD;
+  const bool full = (double)(4LL * S * fullPer * pts) * sizeof(double) <= 0.5 * ((double)freeB + held * 8.0);
+  for (DevBlock& b : c.blocks) {
+    const long long stride = (full ? fullPer : nU) * b.v.N;
+    if (growDevice(c, &b.runStage, &b.runStageCap, 4LL * S * stride)) return 1;
+  }
+  c.slotFull = full ? 1 : 0;
+  std::vector<RunScalars> rs, rl;
+  std::vector<double*> qFinal(c.blocks.size(), nullptr);
+  struct FreeAll {
+    std::vector<double*>* v;
+    ~FreeAll() {
+      for (double* p : *v) cudaFree(p);
+    }
+  } freeAll{&qFinal};
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+    DevBlock& b = c.blocks[bi];
+    RunScalars r = blockRunScalars(c, b, bi == 0);
+    r.slotFull = c.slotFull;
+    r.slotStride = (full ? fullPer : nU) * b.v.N;
+    rs.push_back(r);
+    RunScalars l = r;
+    l.forcing = (deltaControl && bi == 0) ? c.dDeltaForcing : nullptr;
+    l.nForcingEntries = (deltaControl && bi == 0) ? n_entries : 0;
+    rl.push_back(l);
+    CUDA_TRY(c, cudaMalloc((void**)&qFinal[bi], (size_t)nU * b.v.N * sizeof(double)));
+    CUDA_TRY(c, cudaMemcpyAsync(qFinal[bi], b.v.q, (size_t)nU * b.v.N * sizeof(double), cudaMemcpyDeviceToDevice,
+                                c.stream));
+  }
+  BlockRefs refs = runRefs(c);
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) refs.slotStride[bi] = rs[bi].slotStride;
+  cudaGraphExec_t gRec = nullptr, gLin = nullptr;
+  struct Graphs {
+    cudaGraphExec_t* a;
+    cudaGraphExec_t* b;
+    ~Graphs() {
+      if (*a) cudaGraphExecDestroy(*a);
+      if (*b) cudaGraphExecDestroy(*b);
+    }
+  } graphs{&gRec, &gLin};
+  long long nodesRec = 0, nodesLin = 0;
+  if (capture(c, &gRec, &nodesRec, [&]() {
+        for (int i = 1; i <= 4; ++i) regionRunStage(c, rs, i, controller, true, false);
+        launchStepAdvance(c, 1);
+      }))
+    return 1;
+  if (capture(c, &gLin, &nodesLin, [&]() {
+        for (int i = 1; i <= 4; ++i) {
+          for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+            DevBlock& b = c.blocks[bi];
+            if (!full) {
+              launchPrims(c, b, nullptr, true, &rs[bi], i);
+              if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs[bi], i, false);
+            }
+            if (functional) launchFunctionalTangent(c, b, rl[bi], i, full);
+            if (c.phys.dissipation) launchDissipation(c, b, b.v.lam, 1.0);
+            launchLinearizedFlux(c, b, rl[bi], i, full);
+          }
+          for (size_t bi = 0; bi < c.blocks.size(); ++bi)
+            launchInterfaceSatLinearized(c, c.blocks[bi], refs, &rl[bi], i, full);
+          for (size_t bi = 0; bi < c.blocks.size(); ++bi)
+            launchLinearizedDivergence(c, c.blocks[bi], i, rl[bi], 0.0, i, deltaControl && bi == 0);
+        }
+        launchStepAdvance(c, 1);
+      }))
+    return 1;
+  const int nSeg = (T + S - 1) / S;
+  for (int k = 0; k < nSeg; ++k) {
+    const int L = k * S, end = std::min(T, L + S);
+    for (DevBlock& b : c.blocks) {
+      CUDA_TRY(c, cudaMemcpyAsync(b.v.q, b.runSnap + (size_t)k * nU * b.v.N, (size_t)nU * b.v.N * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, c.stream));
+      launchPrims(c, b, b.v.q, false);
+    }
+    launchSetCounters(c.dCounters, L + 1, L, c.stream);
+    for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(gRec, c.stream));
+    launchSetCounters(c.dCounters, L + 1, L, c.stream);
+    for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(gLin, c.stream));
+    c.launches += 2 + (long long)(end - L) * (nodesRec + nodesLin);
+  }
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+    DevBlock& b = c.blocks[bi];
+    CUDA_TRY(c, cudaMemcpyAsync(b.v.q, qFinal[bi], (size_t)nU * b.v.N * sizeof(double), cudaMemcpyDeviceToDevice,
+                                c.stream));
+    launchPrims(c, b, b.v.q, false);
+    // the last stage's term, at the final state: the counters stand at step T + 1
+    if (functional) launchFunctionalTangent(c, b, rl[bi], 1, false);
+  }
+  if (checkLaunch(c)) return 1;
+  double dJ = 0.0;
+  if (functional) {
+    std::vector<double> vals;
+    if (reduceRegion(c, 4 * T, vals)) return 1;
+    for (int st = 0; st < T; ++st)
+      for (int i = 0; i < 4; ++i) dJ = dJ + kRkNorm[i] * c.stepDt[st] * vals[(size_t)4 * st + i];
+  }
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  if (delta_cost) *delta_cost = dJ;
+  return 0;
 }

@@ -364,7 +364,8 @@ void launchLinearized(Context& c, DevBlock& b, int rkStage, const RunScalars& rs
 void launchLinearizedFlux(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool fromSlot, cudaStream_t s = 0);
 void launchLinearizedDivergence(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, double factor, int stage,
                                 bool controller, cudaStream_t s = 0);
-void launchInterfaceSatLinearized(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_t s = 0);
+void launchInterfaceSatLinearized(Context& c, DevBlock& b, const BlockRefs& r, const RunScalars* rs = nullptr,
+                                  int stage = 1, bool fromSlot = false, cudaStream_t s = 0);
 // Tangent of the functional at the forward state of (step, stage) along lambda,
 // into the partial sums of the stage before.
 void launchFunctionalTangent(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool fromSlot,

@@ -1308,7 +1308,8 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSat(BlockView B, Physics P, 
 // derivative of the Roe-averaged A+ taken on one-derivative dual numbers, plus
 // J (s_vL F_L + s_vR F_R) with the two sides' linearized viscous fluxes.
 template <int ND, bool VISC>
-__global__ void __launch_bounds__(kBlock) kInterfaceSatLinearized(BlockView B, Physics P, BlockRefs R) {
+__global__ void __launch_bounds__(kBlock) kInterfaceSatLinearized(BlockView B, Physics P, BlockRefs R, RunScalars rs,
+                                                                   int stage, int fromSlot) {
   pdlEnter();
   const int e = blockIdx.x * kBlock + threadIdx.x;
   if (e >= B.ff.n || B.ff.kind[e] != SAT_INTERFACE) return;
@@ -1317,10 +1318,18 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSatLinearized(BlockView B, P
   const long long N = B.N, p = B.ff.point[e];
   const int pb = B.ff.partnerBlock[e];
   const long long pp = B.ff.partnerPoint[e], NR = R.N[pb];
+  // forward state of both sides: the blocks' arrays, or their stage slots in a tangent run
+  const double* qLb = B.q;
+  const double* qRb = R.q[pb];
+  if (fromSlot) {
+    const int slot = ((*rs.step) - (*rs.segBase) - 1) * 4 + stage - 1;
+    qLb = rs.stageBuf + (long long)slot * rs.slotStride;
+    qRb = R.stage[pb] + (long long)slot * R.slotStride[pb];
+  }
   double dq[nU], dx[nU], mL[ND];
   D dL[nU], dR[nU], roe[nU];
   for (int c = 0; c < nU; ++c) {
-    const double qL = B.q[p + N * c], qR = R.q[pb][pp + NR * c];
+    const double qL = qLb[p + N * c], qR = qRb[pp + NR * c];
     const double xL = B.lam[p + N * c], xR = R.lam[pb][pp + NR * c];
     dq[c] = qL - qR;
     dx[c] = xL - xR;
@@ -1792,16 +1801,19 @@ void launchLinearizedFlux(Context& c, DevBlock& b, const RunScalars& rs, int sta
 #undef LF
 }
 
-void launchInterfaceSatLinearized(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_t s) {
+void launchInterfaceSatLinearized(Context& c, DevBlock& b, const BlockRefs& r, const RunScalars* rs, int stage,
+                                  bool fromSlot, cudaStream_t s) {
   if (b.nInterfaceEntries == 0) return;
   const int G = gridFor(b.v.ff.n);
+  const RunScalars x = rs ? *rs : RunScalars{};
+  const int fsl = fromSlot ? 1 : 0;
   MGD_LAUNCH(c);
   if (c.nD == 2) {
-    if (c.phys.viscous) pdl(kInterfaceSatLinearized<2, true>, G, kBlock, on(c, s), b.v, c.phys, r);
-    else pdl(kInterfaceSatLinearized<2, false>, G, kBlock, on(c, s), b.v, c.phys, r);
+    if (c.phys.viscous) pdl(kInterfaceSatLinearized<2, true>, G, kBlock, on(c, s), b.v, c.phys, r, x, stage, fsl);
+    else pdl(kInterfaceSatLinearized<2, false>, G, kBlock, on(c, s), b.v, c.phys, r, x, stage, fsl);
   } else {
-    if (c.phys.viscous) pdl(kInterfaceSatLinearized<3, true>, G, kBlock, on(c, s), b.v, c.phys, r);
-    else pdl(kInterfaceSatLinearized<3, false>, G, kBlock, on(c, s), b.v, c.phys, r);
+    if (c.phys.viscous) pdl(kInterfaceSatLinearized<3, true>, G, kBlock, on(c, s), b.v, c.phys, r, x, stage, fsl);
+    else pdl(kInterfaceSatLinearized<3, false>, G, kBlock, on(c, s), b.v, c.phys, r, x, stage, fsl);
   }
 }
 

@@ -684,3 +684,28 @@ def test_per_call_control_flow_reproduces_the_runs():
     Jp, Gp = per_call_gradient(oracle_lib.Oracle(P), P, P.n_steps, 4)
     assert abs(Jp - J) <= 1e-12 * abs(J)
     assert abs(Gp - G) <= 1e-12 * abs(G)
+
+
+@pytest.mark.parametrize("rotate", [False, True])
+def test_two_block_linearized_and_adjoint_runs_are_dual(rotate):
+    """Across a block interface, the tangent run and the adjoint run from a
+    given terminal condition transpose each other exactly:
+    <lambda(0), dq(0)>_H = <lambda(T), dq(T)>_H summed over the blocks."""
+    P = configs.two_block_2d(functional=True, rotate_second=rotate, n_steps=10, dt=0.05)
+    P.options.adjoint_forcing_switch = False
+    rng = np.random.default_rng(31)
+    o = oracle_lib.Oracle(P)
+    o.run_forward(P.n_steps, 4)
+    H = [o.get_field(bi, capi.FIELD_NORM) for bi in (1, 2)]
+    dq0 = [1e-3 * rng.standard_normal((4, b.n_points)) for b in P.blocks]
+    lamT = [rng.standard_normal((4, b.n_points)) for b in P.blocks]
+    for bi in (1, 2):
+        o.set_field(bi, capi.FIELD_ADJOINT, dq0[bi - 1])
+    o.run_linearized()
+    b = sum(np.sum(lamT[bi - 1] * H[bi - 1] * o.get_field(bi, capi.FIELD_ADJOINT)) for bi in (1, 2))
+    for bi in (1, 2):
+        o.set_field(bi, capi.FIELD_ADJOINT, lamT[bi - 1])
+    o.set_adjoint_nonzero_initial_condition(True)
+    o.run_adjoint()
+    a = sum(np.sum(o.get_field(bi, capi.FIELD_ADJOINT) * H[bi - 1] * dq0[bi - 1]) for bi in (1, 2))
+    assert abs(a - b) <= 1e-11 * abs(b)
