@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--jet-save-interval", type=int, default=4)
     ap.add_argument("--jet-scale", type=float, default=1.0, help="grid scale of the jet (1 = 39.4 M points)")
     ap.add_argument("--sweep-instances", type=int, default=64)
+    ap.add_argument("--sweep-per-call-sample", type=int, default=4,
+                    help="instances timed through the per-call entry points beside the batch")
     ap.add_argument("--profile-only", action="store_true",
                     help="run the gradient evaluations and exit (for ncu captures; prints no bench line)")
     return ap.parse_args()
@@ -400,11 +402,12 @@ def run_sweep(args):
         s.run_adjoint()
         grads[n] = s.gradient(4 * n_steps)
         s.close()
-    solvers, q0 = [], []
+    solvers, q0, forcings = [], [], []
     for n, a in mine:
         P = configs.monopole_2d(n=n, n_steps=n_steps, save_interval=SAVE_INTERVAL, controller_switch=True)
         s = Solver(P)
-        s.set_control_forcing(a * grads[n])
+        forcings.append(a * grads[n])
+        s.set_control_forcing(forcings[-1])
         solvers.append(s)
         q0.append(np.ascontiguousarray(P.blocks[0].initial_state))
     batch = Batch(solvers)
@@ -439,6 +442,15 @@ def run_sweep(args):
     plain_costs = [s.run_forward(n_steps, SAVE_INTERVAL) for s in solvers]
     torch.cuda.synchronize()
     t_plain = time.perf_counter() - t
+    # the reference's control flow over the per-call entry points (one
+    # mgd_rk4_substep per stage, the stage's forcing handed to the actuators),
+    # timed on a sample of the instances
+    from magudi_gb300.drivers import per_call_forward
+    K = min(len(solvers), args.sweep_per_call_sample)
+    t = time.perf_counter()
+    pc_costs = [per_call_forward(solvers[i], solvers[i].problem, n_steps, forcings[i]) for i in range(K)]
+    t_pc = time.perf_counter() - t
+    pc_rel = max(abs(a - b) / abs(b) for a, b in zip(pc_costs, costs[:K])) if K else 0.0
     sec = statistics.mean(times)
     if world > 1:
         tt = torch.tensor([sec, t_plain], device="cuda")
@@ -463,6 +475,11 @@ def run_sweep(args):
                                "path": "mgd_run_forward per instance, one after another"},
         "speedup_vs_plain": t_plain / sec,
         "max_rel_diff_vs_plain_J": max_rel,
+        "per_call_sample": {"instances": K, "seconds": t_pc, "value": K / t_pc if K else None, "unit": "solves/s",
+                            "batch_speedup": (len(cases) / sec) / (K / t_pc) if K else None,
+                            "max_rel_diff_vs_batch_J": pc_rel,
+                            "path": "mgd_rk4_substep + functional per stage with the stage's forcing handed to the "
+                                    "actuators (Solver%runForward over the computeRhs seam), the first instances"},
         "J_first": float(all_costs[0]), "J_last": float(all_costs[-1]),
         "gpu_launches": launches,
         "clocks": clk,

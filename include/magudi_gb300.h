@@ -267,6 +267,16 @@ int mgd_run_adjoint(mgd_ctx* ctx, double* sensitivity);
  * regions carry the block-interface SATs; the patch types of MGD_LINEARIZED. */
 int mgd_run_linearized(mgd_ctx* ctx, const double* delta_forcing, long long n_entries, double* delta_cost);
 
+/* The actuator patches' controlForcing for the per-call forward RHS
+ * (mgd_compute_rhs, mgd_rk4_substep, MGD_FORWARD): nPatchPoints values per
+ * actuator patch, concatenated in patch order (mgd_actuator_patch_size), as
+ * the controller's updateForcing fills them for the coming stage
+ * (src/ThermalActuatorImpl.f90:161-233); the RHS adds control mollifier x
+ * forcing to the energy equation (src/ActuatorPatchImpl.f90:108-181) while
+ * controller_switch is on. Host or device pointer; NULL clears it. The
+ * checkpointed runs take their forcing from mgd_set_control_forcing instead. */
+int mgd_set_patch_control_forcing(mgd_ctx* ctx, const double* forcing);
+
 /* adjoint_nonzero_initial_condition (src/SolverImpl.f90:1027-1102, set per
  * segment by bin/msadjoint.f90:141-400): when enabled, mgd_run_adjoint starts
  * from the adjoint field the context holds (loaded with mgd_set_field(...,

@@ -168,7 +168,7 @@ int mgd_destroy(mgd_ctx* h) {
     cudaFree(b.runPartials);
   }
   cudaFree(c.dCounters); cudaFree(c.dApiAmp); cudaFree(c.dAmp); cudaFree(c.dForcing);
-  cudaFree(c.dApiTime); cudaFree(c.dStageTime); cudaFree(c.dDeltaForcing);
+  cudaFree(c.dApiTime); cudaFree(c.dStageTime); cudaFree(c.dDeltaForcing); cudaFree(c.dApiForcing);
   cudaFree(c.dGradient); cudaFree(c.dPartials); cudaFree(c.dStageValues);
   cudaFree(c.dSnapshots); cudaFree(c.dStageBuf);
   cudaFree(c.dStepDt); cudaFree(c.dDtPartials); cudaFree(c.dTime); cudaFree(c.dNorm);
@@ -1300,6 +1300,7 @@ static RunScalars apiScalars(Context& c) {
   r.segBase = c.dCounters + 3;
   r.amp = c.dApiAmp;
   r.stageTime = c.dApiTime;
+  r.apiForcing = c.apiForcingSet ? c.dApiForcing : nullptr;
   setStepSize(r, c.opts.time_step_size);
   r.adjointForcingSwitch = c.opts.adjoint_forcing_switch;
   r.nPartialBlocks = reductionBlocks(c.blocks[0]);
@@ -1317,6 +1318,12 @@ static int setApiTime(Context& c, double time) {
   // pageable source: the copy completes before the call returns
   CUDA_TRY(c, cudaMemcpyAsync(c.dApiTime, &time, sizeof time, cudaMemcpyHostToDevice, c.stream));
   return 0;
+}
+
+// The per-call forward RHS adds the actuators' forcing when the caller set one
+// (ActuatorPatch%updateRhs, src/ActuatorPatchImpl.f90:108-181).
+static bool apiController(const Context& c) {
+  return c.apiForcingSet && c.opts.enable_controller && c.opts.controller_switch;
 }
 
 static int requireReady(Context& c) {
@@ -1395,7 +1402,8 @@ void regionForwardStage(Context& c, int rkStage, const RunScalars& rs) {
   }
   for (DevBlock& b : c.blocks) launchInterfaceSat(c, b, refs);
   for (DevBlock& b : c.blocks) {
-    launchForwardDivergence(c, b, rkStage, rs, true, false);
+    // actuator patches lie in block 1
+    launchForwardDivergence(c, b, rkStage, rs, true, apiController(c) && &b == &c.blocks[0]);
     if (rkStage > 0) launchPrims(c, b, b.v.q, false);
   }
 }
@@ -1466,7 +1474,7 @@ int mgd_compute_rhs(mgd_ctx* h, int mode, double time, double adjoint_forcing_fa
   if (mode == MGD_FORWARD) {
     if (setApiTime(c, time)) return 1;
     for (DevBlock& x : c.blocks) launchPrims(c, x, x.v.q, false);
-    if (singleBlock(c)) forwardStage(c, b, 0, rs, true, false, false, false);
+    if (singleBlock(c)) forwardStage(c, b, 0, rs, true, apiController(c), false, false);
     else regionForwardStage(c, 0, rs);
   } else if (mode == MGD_ADJOINT) {
     if (setApiTime(c, time)) return 1;
@@ -1576,7 +1584,7 @@ int mgd_rk4_substep(mgd_ctx* h, int mode, double* time, double dt, int stage) {
     if (stage == 2 || stage == 4) *time = *time + dt / 2.0;
     if (setApiTime(c, *time)) return 1;
     for (DevBlock& x : c.blocks) launchPrims(c, x, x.v.q, false);
-    if (singleBlock(c)) forwardStage(c, b, stage, rs, true, false, false, false);
+    if (singleBlock(c)) forwardStage(c, b, stage, rs, true, apiController(c), false, false);
     else regionForwardStage(c, stage, rs);
   } else if (mode == MGD_ADJOINT) {
     const double factor = stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0);
@@ -2390,6 +2398,22 @@ int mgd_run_linearized(mgd_ctx* h, const double* delta_forcing, long long n_entr
   if (checkLaunch(c)) return 1;
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   if (delta_cost) *delta_cost = dJ;
+  return 0;
+}
+
+int mgd_set_patch_control_forcing(mgd_ctx* h, const double* forcing) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  if (!forcing) {
+    c.apiForcingSet = false;
+    return 0;
+  }
+  if (c.actuatorPoints == 0) return fail(c, "the region has no actuator patch");
+  if (!c.dApiForcing) CUDA_TRY(c, cudaMalloc((void**)&c.dApiForcing, (size_t)c.actuatorPoints * sizeof(double)));
+  CUDA_TRY(c, cudaMemcpyAsync(c.dApiForcing, forcing, (size_t)c.actuatorPoints * sizeof(double), cudaMemcpyDefault,
+                              c.stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  c.apiForcingSet = true;
   return 0;
 }
 

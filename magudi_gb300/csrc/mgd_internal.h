@@ -140,6 +140,7 @@ struct RunScalars {
   const int* segBase;     // first step of the checkpoint segment minus 1
   const double* amp;      // source amplitudes per (step-1)*4 + stage-1, nSources each
   const double* forcing;  // control forcing entries, P each (file order)
+  const double* apiForcing;  // per-call path: the actuator patches' current forcing (P values), or null
   long long nForcingEntries;
   int nSteps;
   long long P;            // actuator-patch points
@@ -255,6 +256,8 @@ struct Context {
   long long ampCapacity = 0;
   double* dForcing = nullptr;       // control forcing entries
   double* dDeltaForcing = nullptr;  // control perturbation of a tangent run
+  double* dApiForcing = nullptr;    // actuator forcing of the per-call RHS (P values), set or not
+  bool apiForcingSet = false;
   long long deltaForcingCapacity = 0;
   long long nForcingEntries = 0;
   long long forcingCapacity = 0;

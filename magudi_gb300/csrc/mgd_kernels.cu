@@ -554,8 +554,12 @@ __device__ __forceinline__ void forwardDivergencePoint(const BlockView& B, const
     if (controller) {
       const int ai = B.actIdx[p];
       if (ai >= 0) {
-        const long long e = (long long)(rs.nSteps - step) * 4 + (4 - stage);
-        if (e >= 0 && e < rs.nForcingEntries) r += B.mc[p] * rs.forcing[e * rs.P + ai];
+        if (rs.apiForcing) {
+          r += B.mc[p] * rs.apiForcing[ai];
+        } else {
+          const long long e = (long long)(rs.nSteps - step) * 4 + (4 - stage);
+          if (e >= 0 && e < rs.nForcingEntries) r += B.mc[p] * rs.forcing[e * rs.P + ai];
+        }
       }
     }
     if (!lin && B.nSources > 0) {

@@ -17,9 +17,12 @@ from . import capi
 RK_NORM = (1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0)
 
 
-def per_call_gradient(s, problem, n_steps, save_interval):
+def per_call_gradient(s, problem, n_steps, save_interval, forcing=None):
     """J and the gradient norm (sensitivity) of n_steps constant-dt steps from
-    the problem's initial state, checkpoints every save_interval steps."""
+    the problem's initial state, checkpoints every save_interval steps. With
+    forcing (4 n_steps entries x actuator points, file order), the stage's
+    entry is handed to the actuators before each forward substep, as the
+    controller's updateForcing does (src/ThermalActuatorImpl.f90:161-233)."""
     dt = problem.options.time_step_size
     N, nU = problem.blocks[0].n_points, problem.n_unknowns
     s.set_field(1, capi.FIELD_CONSERVED, problem.blocks[0].initial_state)
@@ -30,6 +33,8 @@ def per_call_gradient(s, problem, n_steps, save_interval):
         if (step - 1) % save_interval == 0:
             snaps[step - 1] = (s.get_field(1, capi.FIELD_CONSERVED), t)
         for i in range(1, 5):
+            if forcing is not None:
+                s.set_patch_control_forcing(forcing[(n_steps - step) * 4 + (4 - i)])
             t = s.rk4_substep(capi.FORWARD, t, dt, i)
             J += RK_NORM[i - 1] * dt * s.functional()
     # loadInitialCondition(ADJOINT): lambda(T) = (-dt/6) x the cost-target forcing at T
@@ -47,6 +52,8 @@ def per_call_gradient(s, problem, n_steps, save_interval):
         for step in range(L + 1, end + 1):
             for i in range(1, 5):
                 stages[(step, i)] = s.get_field(1, capi.FIELD_CONSERVED)
+                if forcing is not None:
+                    s.set_patch_control_forcing(forcing[(n_steps - step) * 4 + (4 - i)])
                 tl = s.rk4_substep(capi.FORWARD, tl, dt, i)
         for step in range(end, L, -1):
             for i in range(4, 0, -1):
@@ -55,4 +62,25 @@ def per_call_gradient(s, problem, n_steps, save_interval):
                 G += RK_NORM[i - 1] * dt * s.sensitivity()
                 s.update_adjoint_forcing(step == 1 and i == 1)
                 t = s.rk4_substep(capi.ADJOINT, t, dt, i)
+    if forcing is not None:
+        s.set_patch_control_forcing(None)
     return J, G
+
+
+def per_call_forward(s, problem, n_steps, forcing=None):
+    """J of n_steps constant-dt forward steps through mgd_rk4_substep and the
+    functional, one call per stage (Solver%runForward, src/SolverImpl.f90:672-912),
+    handing each stage's forcing entry to the actuators when forcing is given."""
+    dt = problem.options.time_step_size
+    s.set_field(1, capi.FIELD_CONSERVED, problem.blocks[0].initial_state)
+    s.update_state()
+    t, J = 0.0, 0.0
+    for step in range(1, n_steps + 1):
+        for i in range(1, 5):
+            if forcing is not None:
+                s.set_patch_control_forcing(forcing[(n_steps - step) * 4 + (4 - i)])
+            t = s.rk4_substep(capi.FORWARD, t, dt, i)
+            J += RK_NORM[i - 1] * dt * s.functional()
+    if forcing is not None:
+        s.set_patch_control_forcing(None)
+    return J

@@ -56,6 +56,7 @@ def load_library(build_if_missing=True):
     L.mgd_run_forward.argtypes = [ctx, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_double)]
     L.mgd_run_adjoint.argtypes = [ctx, C.POINTER(C.c_double)]
     L.mgd_set_adjoint_nonzero_initial_condition.argtypes = [ctx, C.c_int]
+    L.mgd_set_patch_control_forcing.argtypes = [ctx, C.POINTER(C.c_double)]
     L.mgd_run_linearized.argtypes = [ctx, C.POINTER(C.c_double), C.c_longlong, C.POINTER(C.c_double)]
     L.mgd_get_gradient.argtypes = [ctx, C.POINTER(C.c_double), C.c_longlong]
     L.mgd_time_step_size.argtypes = [ctx, C.POINTER(C.c_double)]
@@ -207,6 +208,14 @@ class Solver:
             n = a.size // max(1, self.actuator_points())
             self._check(self.L.mgd_run_linearized(self.h, capi.dptr(a), n, C.byref(v)))
         return v.value
+
+    def set_patch_control_forcing(self, forcing):
+        """The actuator patches' forcing for the per-call forward RHS (P values), or None."""
+        if forcing is None:
+            self._check(self.L.mgd_set_patch_control_forcing(self.h, None))
+        else:
+            a = np.ascontiguousarray(forcing, dtype=np.float64)
+            self._check(self.L.mgd_set_patch_control_forcing(self.h, capi.dptr(a)))
 
     def set_adjoint_nonzero_initial_condition(self, enable):
         """adjoint_nonzero_initial_condition: run_adjoint starts from the adjoint

@@ -2320,6 +2320,9 @@ static double runForward(Region& R, int nSteps, double t0, bool keepStages) {
     }
   }
   R.finalTime = time;
+  // the per-call RHS adds only the forcing its caller sets (orc_set_patch_control_forcing)
+  for (Patch& p : R.patches)
+    if (p.d.type == MGD_PATCH_ACTUATOR) std::fill(p.controlForcing.begin(), p.controlForcing.end(), 0.0);
   if (R.o.enable_functional && R.o.functional_type == MGD_FUNCTIONAL_TERMINAL_KINETIC_ENERGY)
     J = terminalKineticEnergy(R);
   return J;
@@ -2573,6 +2576,22 @@ int orc_run_linearized(void* h, const double* deltaForcing, long long nEntries, 
   const double dJ = orc::runLinearized(R);
   if (deltaCost) *deltaCost = dJ;
   return R.error.empty() ? 0 : 1;
+}
+
+// ActuatorPatch%controlForcing of the energy component for the per-call RHS:
+// nPatchPoints values per actuator patch in patch order; NULL clears them.
+int orc_set_patch_control_forcing(void* h, const double* forcing) {
+  Region& R = *(Region*)h;
+  long long off = 0;
+  for (orc::Patch& p : R.patches) {
+    if (p.d.type != MGD_PATCH_ACTUATOR || p.nPatchPoints <= 0) continue;
+    std::fill(p.controlForcing.begin(), p.controlForcing.end(), 0.0);
+    if (forcing)
+      for (long long i = 0; i < p.nPatchPoints; ++i)
+        p.controlForcing[p.nPatchPoints * (R.nD + 1) + i] = forcing[off + i];
+    off += p.nPatchPoints;
+  }
+  return 0;
 }
 
 int orc_set_adjoint_nonzero_initial_condition(void* h, int enable) {

@@ -50,6 +50,7 @@ def lib():
         L.orc_run_forward_nostore.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double)]
         L.orc_run_adjoint.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.orc_set_adjoint_nonzero_initial_condition.argtypes = [C.c_void_p, C.c_int]
+        L.orc_set_patch_control_forcing.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.orc_run_linearized.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.c_longlong, C.POINTER(C.c_double)]
         L.orc_time_step_size.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.orc_step_sizes.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
@@ -197,6 +198,13 @@ class Oracle:
         v = C.c_double()
         self.L.orc_run_adjoint(self.h, C.byref(v))
         return v.value
+
+    def set_patch_control_forcing(self, forcing):
+        if forcing is None:
+            self.L.orc_set_patch_control_forcing(self.h, None)
+        else:
+            a = np.ascontiguousarray(forcing, dtype=np.float64)
+            self.L.orc_set_patch_control_forcing(self.h, capi.dptr(a))
 
     def set_adjoint_nonzero_initial_condition(self, enable):
         self.L.orc_set_adjoint_nonzero_initial_condition(self.h, int(bool(enable)))
