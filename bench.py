@@ -264,12 +264,28 @@ def run_ours(args):
         G = s.run_adjoint()
         return J, G
 
+    # run-level tile tuning on short gradient runs (setup, outside the timed region)
+    set_q(q0_dev.data_ptr())
+    t_tune = time.perf_counter()
+    tuned_ms = s.tune_run(4 * SAVE_INTERVAL, SAVE_INTERVAL)
+    tuning = {"seconds": time.perf_counter() - t_tune, "run_steps": 4 * SAVE_INTERVAL, "tuned_run_ms": tuned_ms,
+              "tiles": [list(s.stage_tile(k)) for k in range(6)], "gradient_flux_threads_per_point": s.gradient_lanes()}
     for _ in range(args.warmup):
         gradient_step(q0_dev.data_ptr())
     torch.cuda.synchronize()
     if args.profile_only:
         for _ in range(args.steps):
             J, G = gradient_step(q0_dev.data_ptr())
+        # one forward and one adjoint RHS of the final state through the
+        # per-call entry points, in an NVTX range for filtered ncu captures
+        # (ncu --nvtx --nvtx-include "stage_rhs/")
+        s.compute_rhs(capi.FORWARD, 0.0)
+        s.compute_rhs(capi.ADJOINT, 0.0, 1.0)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("stage_rhs")
+        s.compute_rhs(capi.FORWARD, 0.0)
+        s.compute_rhs(capi.ADJOINT, 0.0, 1.0)
+        torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
         print(json.dumps({"profile_only": True, "rk_steps": n_steps, "J": J, "grad0": G}), flush=True)
         return
@@ -336,7 +352,8 @@ def run_ours(args):
         "data": "synthetic (quiescent monopole initial state generated in-process)",
         "config": {"workload": WORKLOAD, "grid": "201x201", "rk4_steps": N_STEPS, "save_interval": SAVE_INTERVAL,
                    "l2": "512 MB buffer written between timed steps (working set fits in L2)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "tile_tuning": tuning},
         "adjoint_gradient_s": ms / 1e3,
         "J": J, "grad0": G,
         "e2e": {"value": e2e, "unit": "Mpt-RHS/s", "ms_per_step": e2e_ms,

@@ -389,6 +389,37 @@ void* mgd_stream(mgd_ctx* ctx);
 /* Counts kernel launches made by the context since the last reset. */
 long long mgd_kernel_launches(mgd_ctx* ctx, int reset);
 
+/* Measurement and test hook (no reference counterpart): the form of the
+ * gradient/flux kernel of 2D blocks that the setup's autotuner chose, one
+ * thread per point (1) or two adjacent threads per point, one per axis (2).
+ * lanes = 1 or 2 sets that form for every block of the context from the next
+ * launch on; lanes = 0 only reports it. Returns the form in effect (3D blocks
+ * always use 1), or -1 for other values of lanes. */
+int mgd_gradient_lanes(mgd_ctx* ctx, int lanes);
+
+/* Run-level autotuner (no reference counterpart): chooses the thread-block
+ * tiles of the six stage kernels (and the 2D gradient/flux form) by timing
+ * whole checkpointed runs, mgd_run_forward(n_steps, save_interval) followed
+ * by mgd_run_adjoint when with_adjoint != 0, from the context's current state:
+ * coordinate descent over the kernels, two passes, fastest of two runs per
+ * candidate. Inside a run the stage kernels share the SMs with the side-stream
+ * dissipation and the concurrent checkpoint recomputation, so the tiles that
+ * finish a run first differ from those of the setup's per-kernel timings.
+ * Every block gets the same tiles. The state and adjoint fields are restored
+ * afterwards, the chosen tiles also go to later contexts of the process with
+ * the same grid and physics, and *best_ms (may be NULL) receives the tuned
+ * run's wall time. Call it before the runs: it discards the last run's
+ * trajectory (a following mgd_run_adjoint needs a new mgd_run_forward). */
+int mgd_tune_run(mgd_ctx* ctx, int n_steps, int save_interval, int with_adjoint, double* best_ms);
+
+/* Measurement and test hook (no reference counterpart): the thread-block
+ * tile (points per CTA along each axis) of one stage kernel, 0 gradient/flux,
+ * 1 dissipation, 2 divergence + RK update, 3 adjoint core, 4 adjoint
+ * diffusion, 5 adjoint assembly + RK update. set != 0 gives every block of
+ * the context that tile from the next launch on (tile[0..2] >= 1 with a
+ * product of at most 256); set = 0 writes the current tile to tile[0..2]. */
+int mgd_stage_tile(mgd_ctx* ctx, int kernel, int* tile, int set);
+
 #ifdef __cplusplus
 }
 #endif

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <array>
 #include <cstdlib>
 #include <map>
@@ -198,6 +199,36 @@ long long mgd_kernel_launches(mgd_ctx* h, int reset) {
   const long long n = h->c.launches;
   if (reset) h->c.launches = 0;
   return n;
+}
+
+int mgd_stage_tile(mgd_ctx* h, int kernel, int* tile, int set) {
+  Context& c = h->c;
+  if (kernel < 0 || kernel > 5 || !tile) return fail(c, "mgd_stage_tile: kernel must be 0..5 and tile non-null");
+  if (c.blocks.empty()) return fail(c, "mgd_stage_tile: no blocks");
+  auto slot = [&](DevBlock& b) -> Tile& {
+    Tile* s[6] = {&b.tGrad, &b.tDiss, &b.tRhs, &b.tAdjA, &b.tAdjD, &b.tAdjB};
+    return *s[kernel];
+  };
+  if (!set) {
+    const Tile& t = slot(c.blocks[0]);
+    for (int d = 0; d < 3; ++d) tile[d] = t.t[d];
+    return 0;
+  }
+  if (tile[0] < 1 || tile[1] < 1 || tile[2] < 1 || (long long)tile[0] * tile[1] * tile[2] > 256)
+    return fail(c, "mgd_stage_tile: tile extents must be >= 1 with at most 256 threads");
+  for (auto& b : c.blocks) slot(b) = makeTile(b, tile[0], tile[1], tile[2]);
+  return 0;
+}
+
+int mgd_gradient_lanes(mgd_ctx* h, int lanes) {
+  Context& c = h->c;
+  if (lanes < 0 || lanes > 2) {
+    fail(c, "mgd_gradient_lanes: lanes must be 0, 1 or 2");
+    return -1;
+  }
+  if (lanes > 0 && c.nD == 2)
+    for (auto& b : c.blocks) b.gradLanes = lanes;
+  return c.nD == 2 && !c.blocks.empty() ? c.blocks[0].gradLanes : 1;
 }
 
 // Grid%update (src/GridImpl.f90:746-1066) from device coordinate derivatives.
@@ -554,28 +585,53 @@ struct TuneKey {
   }
 };
 
+// Tiles of the six stage kernels of a block, shared by all contexts of the
+// process (contexts may be set up from several threads): filled by the
+// per-kernel autotuner at setup and replaced by mgd_tune_run.
+struct Tuned {
+  std::array<Tile, 6> tiles;
+  int gradLanes;
+};
+static std::map<TuneKey, Tuned> g_tuneCache;
+static std::mutex g_tuneCacheMutex;
+
+static TuneKey tuneKey(const Context& c, const DevBlock& b) {
+  return TuneKey{c.nD, {b.v.gs[0], b.v.gs[1], b.v.gs[2]}, b.v.curvilinear, c.phys.viscous, c.phys.dissipation,
+                 c.phys.composite};
+}
+
+static void storeTuned(const Context& c, const DevBlock& b) {
+  const Tile* slots[6] = {&b.tGrad, &b.tDiss, &b.tRhs, &b.tAdjA, &b.tAdjD, &b.tAdjB};
+  Tuned entry;
+  for (int k = 0; k < 6; ++k) entry.tiles[k] = *slots[k];
+  entry.gradLanes = b.gradLanes;
+  std::lock_guard<std::mutex> lock(g_tuneCacheMutex);
+  g_tuneCache[tuneKey(c, b)] = entry;
+}
+
 static int autotune(Context& c, DevBlock& b) {
-  // shared by all contexts of the process; contexts may be set up from several threads
-  static std::map<TuneKey, std::array<Tile, 6>> cache;
-  static std::mutex cacheMutex;
-  TuneKey key{c.nD, {b.v.gs[0], b.v.gs[1], b.v.gs[2]}, b.v.curvilinear, c.phys.viscous, c.phys.dissipation,
-              c.phys.composite};
+  const TuneKey key = tuneKey(c, b);
   Tile* slots[6] = {&b.tGrad, &b.tDiss, &b.tRhs, &b.tAdjA, &b.tAdjD, &b.tAdjB};
   {
-    std::lock_guard<std::mutex> lock(cacheMutex);
-    auto it = cache.find(key);
-    if (it != cache.end()) {
-      for (int k = 0; k < 6; ++k) *slots[k] = it->second[k];
+    std::lock_guard<std::mutex> lock(g_tuneCacheMutex);
+    auto it = g_tuneCache.find(key);
+    if (it != g_tuneCache.end()) {
+      for (int k = 0; k < 6; ++k) *slots[k] = it->second.tiles[k];
+      b.gradLanes = it->second.gradLanes;
       return 0;
     }
   }
+  // CTAs of 128 or 256 threads: the stage kernels of one RK stage share the
+  // SMs with the side-stream dissipation and, in adjoint runs, with the
+  // concurrent checkpoint recomputation, and smaller CTAs that are fastest
+  // alone fill the SMs' CTA slots (at most 32 per SM) and slow those down
   std::vector<std::array<int, 3>> cands;
   if (c.nD == 2)
-    cands = {{32, 1, 1}, {64, 1, 1}, {128, 1, 1}, {32, 2, 1}, {32, 4, 1}, {16, 4, 1}, {16, 8, 1},
-             {32, 8, 1}, {64, 2, 1}, {8, 8, 1}, {16, 2, 1}};
+    cands = {{128, 1, 1}, {64, 2, 1}, {32, 4, 1}, {16, 8, 1}, {8, 16, 1},
+             {256, 1, 1}, {128, 2, 1}, {64, 4, 1}, {32, 8, 1}, {16, 16, 1}};
   else
-    cands = {{32, 2, 2}, {32, 4, 1}, {16, 4, 2}, {16, 8, 1}, {8, 8, 2}, {32, 1, 4}, {64, 2, 1},
-             {32, 2, 1}, {16, 2, 2}, {8, 4, 4}, {32, 4, 2}};
+    cands = {{32, 2, 2}, {32, 4, 1}, {16, 4, 2}, {16, 8, 1}, {8, 8, 2}, {32, 1, 4}, {64, 2, 1}, {8, 4, 4},
+             {32, 4, 2}, {16, 4, 4}, {64, 2, 2}};
   RunScalars rs = apiScalars(c);
   if (setApiTime(c, 0.0)) return 1;
   launchPrims(c, b, b.v.q, false);
@@ -583,10 +639,14 @@ static int autotune(Context& c, DevBlock& b) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
+  // kTuneReps back-to-back launches per timing, the fastest of kTunePasses
+  // passes over the candidates: single timings of kernels of tens of
+  // microseconds right after setup vary with the clock ramp
+  constexpr int kTuneReps = 10, kTunePasses = 2;
   auto timeIt = [&](auto fn) {
     fn();
     cudaEventRecord(e0, c.stream);
-    for (int r = 0; r < 3; ++r) fn();
+    for (int r = 0; r < kTuneReps; ++r) fn();
     cudaEventRecord(e1, c.stream);
     cudaEventSynchronize(e1);
     float ms = 0.f;
@@ -596,33 +656,37 @@ static int autotune(Context& c, DevBlock& b) {
   const long long saved = c.launches;
   for (int k = 0; k < 6; ++k) {
     if ((k == 1 && !c.phys.dissipation) || (k == 4 && !c.phys.viscous)) continue;
-    float best = 1e30f;
-    Tile bestTile = *slots[k];
-    for (const auto& cd : cands) {
-      *slots[k] = makeTile(b, cd[0], cd[1], cd[2]);
-      float ms;
+    auto launch = [&]() {
       switch (k) {
-        case 0: ms = timeIt([&] { launchGradFlux(c, b, true, false, &rs, 1, false); }); break;
-        case 1: ms = timeIt([&] { launchDissipation(c, b, b.v.q, 1.0); }); break;
-        case 2: ms = timeIt([&] { launchForwardDivergence(c, b, 0, rs, true, false); }); break;
-        case 3: ms = timeIt([&] { launchAdjointCore(c, b, rs, 1, false); }); break;
-        case 4: ms = timeIt([&] { launchAdjointDiffusion(c, b); }); break;
-        default: ms = timeIt([&] { launchAdjointAssemble(c, b, 0, rs, 1, 0.0, true, false); }); break;
+        case 0: launchGradFlux(c, b, true, false, &rs, 1, false); break;
+        case 1: launchDissipation(c, b, b.v.q, 1.0); break;
+        case 2: launchForwardDivergence(c, b, 0, rs, true, false); break;
+        case 3: launchAdjointCore(c, b, rs, 1, false); break;
+        case 4: launchAdjointDiffusion(c, b); break;
+        default: launchAdjointAssemble(c, b, 0, rs, 1, 0.0, true, false); break;
       }
-      if (ms < best) { best = ms; bestTile = *slots[k]; }
-    }
-    *slots[k] = bestTile;
+    };
+    // the gradient/flux kernel of 2D blocks also has a two-lanes-per-point form
+    const int nLaneForms = (k == 0 && c.nD == 2) ? 2 : 1;
+    const int nc = (int)cands.size();
+    std::vector<float> ms((size_t)nLaneForms * nc, 1e30f);
+    for (int r = 0; r < 20; ++r) launch();  // clocks up before the first timing
+    for (int pass = 0; pass < kTunePasses; ++pass)
+      for (int lf = 0; lf < nLaneForms; ++lf)
+        for (int i = 0; i < nc; ++i) {
+          *slots[k] = makeTile(b, cands[i][0], cands[i][1], cands[i][2]);
+          if (k == 0) b.gradLanes = lf + 1;
+          ms[(size_t)lf * nc + i] = std::min(ms[(size_t)lf * nc + i], timeIt(launch));
+        }
+    const int best = (int)(std::min_element(ms.begin(), ms.end()) - ms.begin());
+    *slots[k] = makeTile(b, cands[best % nc][0], cands[best % nc][1], cands[best % nc][2]);
+    if (k == 0) b.gradLanes = best / nc + 1;
   }
   c.launches = saved;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (checkLaunch(c)) return 1;
-  std::array<Tile, 6> entry;
-  for (int k = 0; k < 6; ++k) entry[k] = *slots[k];
-  {
-    std::lock_guard<std::mutex> lock(cacheMutex);
-    cache[key] = entry;
-  }
+  storeTuned(c, b);
   return 0;
 }
 
@@ -637,6 +701,9 @@ int autotuneTile(Context& c, DevBlock& b, int kernel, const int (*cands)[3], int
   launchPrims(c, b, b.v.q, false);
   Tile* slot = kernel == BK_GRAD ? &b.tGrad : (kernel == BK_DISS ? &b.tDiss : &b.tRhs);
   const Tile saved = *slot;
+  // the batched kernels have one lane per point
+  const int savedLanes = b.gradLanes;
+  b.gradLanes = 1;
   const long long savedLaunches = c.launches;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -652,7 +719,7 @@ int autotuneTile(Context& c, DevBlock& b, int kernel, const int (*cands)[3], int
     };
     run();
     cudaEventRecord(e0, c.stream);
-    for (int r = 0; r < 3; ++r) run();
+    for (int r = 0; r < 10; ++r) run();
     cudaEventRecord(e1, c.stream);
     cudaEventSynchronize(e1);
     float ms = 0.f;
@@ -660,6 +727,7 @@ int autotuneTile(Context& c, DevBlock& b, int kernel, const int (*cands)[3], int
     if (ms < bestMs) { bestMs = ms; *best = *slot; }
   }
   *slot = saved;
+  b.gradLanes = savedLanes;
   c.launches = savedLaunches;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -2192,7 +2260,7 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   rb.desc = b.desc;
   rb.v = twoLanes ? c.shadow : b.v;
   rb.exc = b.exc;
-  rb.tGrad = b.tGrad; rb.tDiss = b.tDiss; rb.tRhs = b.tRhs;
+  rb.tGrad = b.tGrad; rb.tDiss = b.tDiss; rb.tRhs = b.tRhs; rb.gradLanes = b.gradLanes;
   rb.tAdjA = b.tAdjA; rb.tAdjD = b.tAdjD; rb.tAdjB = b.tAdjB;
   const Lanes adjLanes{c.stream, c.side, c.evFork[1], c.evJoin[1]};
   const Lanes recLanes = twoLanes ? Lanes{c.stream2, c.side2, c.evFork[2], c.evJoin[2]}
@@ -2829,5 +2897,104 @@ static int regionRunLinearized(Context& c, const double* delta_forcing, long lon
   }
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));
   if (delta_cost) *delta_cost = dJ;
+  return 0;
+}
+
+int mgd_tune_run(mgd_ctx* h, int n_steps, int save_interval, int with_adjoint, double* best_ms) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  if (n_steps < 1) return fail(c, "mgd_tune_run: n_steps must be >= 1");
+  if (save_interval < 1) save_interval = n_steps;
+  // the state and adjoint of every block, restored before every timed run and at the end
+  std::vector<double*> saved;
+  auto release = [&]() {
+    for (double* p : saved) cudaFree(p);
+  };
+  for (auto& b : c.blocks) {
+    double* p = nullptr;
+    if (cudaMalloc((void**)&p, (size_t)2 * c.nU * b.v.N * sizeof(double)) != cudaSuccess) {
+      release();
+      return fail(c, "mgd_tune_run: out of device memory for the saved state");
+    }
+    saved.push_back(p);
+    cudaMemcpyAsync(p, b.v.q, (size_t)c.nU * b.v.N * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
+    cudaMemcpyAsync(p + (size_t)c.nU * b.v.N, b.v.lam, (size_t)c.nU * b.v.N * sizeof(double),
+                    cudaMemcpyDeviceToDevice, c.stream);
+  }
+  auto restore = [&]() {
+    for (size_t i = 0; i < c.blocks.size(); ++i) {
+      DevBlock& b = c.blocks[i];
+      cudaMemcpyAsync(b.v.q, saved[i], (size_t)c.nU * b.v.N * sizeof(double), cudaMemcpyDeviceToDevice, c.stream);
+      cudaMemcpyAsync(b.v.lam, saved[i] + (size_t)c.nU * b.v.N, (size_t)c.nU * b.v.N * sizeof(double),
+                      cudaMemcpyDeviceToDevice, c.stream);
+    }
+    return cudaStreamSynchronize(c.stream) == cudaSuccess ? 0 : fail(c, "mgd_tune_run: state restore failed");
+  };
+  const long long launches = c.launches;
+  // wall time of one forward (+ adjoint) run from the saved state
+  auto runOnce = [&](double* ms) -> int {
+    if (restore()) return 1;
+    const auto t = std::chrono::steady_clock::now();
+    double J = 0.0, G = 0.0;
+    if (mgd_run_forward(h, n_steps, save_interval, 0.0, &J)) return 1;
+    if (with_adjoint && mgd_run_adjoint(h, &G)) return 1;
+    if (cudaStreamSynchronize(c.stream) != cudaSuccess) return fail(c, "mgd_tune_run: run failed");
+    *ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
+    return 0;
+  };
+  auto timed = [&](double* ms) -> int {  // fastest of two runs
+    double a = 0.0, b = 0.0;
+    if (runOnce(&a) || runOnce(&b)) return 1;
+    *ms = std::min(a, b);
+    return 0;
+  };
+  std::vector<std::array<int, 3>> cands;
+  if (c.nD == 2)
+    cands = {{8, 8, 1}, {16, 4, 1}, {32, 2, 1}, {64, 1, 1}, {8, 16, 1}, {16, 8, 1},
+             {32, 4, 1}, {64, 2, 1}, {128, 1, 1}, {16, 16, 1}, {32, 8, 1}};
+  else
+    cands = {{8, 4, 2}, {16, 2, 2}, {32, 2, 1}, {8, 8, 2}, {16, 4, 2}, {32, 2, 2}, {32, 4, 1},
+             {16, 8, 1}, {8, 4, 4}, {64, 2, 1}, {16, 4, 4}};
+  auto slotOf = [](DevBlock& b, int k) -> Tile& {
+    Tile* s[6] = {&b.tGrad, &b.tDiss, &b.tRhs, &b.tAdjA, &b.tAdjD, &b.tAdjB};
+    return *s[k];
+  };
+  auto setAll = [&](int k, const std::array<int, 3>& t, int lanes) {
+    for (auto& b : c.blocks) {
+      slotOf(b, k) = makeTile(b, t[0], t[1], t[2]);
+      if (k == 0 && c.nD == 2) b.gradLanes = lanes;
+    }
+  };
+  int rc = 0;
+  double best = 0.0;
+  for (int w = 0; w < 2 && !rc; ++w) rc = runOnce(&best);  // warm-up: clocks, graph buffers
+  if (!rc) rc = timed(&best);
+  for (int pass = 0; pass < 2 && !rc; ++pass)
+    for (int k = 0; k < 6 && !rc; ++k) {
+      if ((k == 1 && !c.phys.dissipation) || (k == 4 && !c.phys.viscous) || (k >= 3 && !with_adjoint)) continue;
+      const Tile& cur = slotOf(c.blocks[0], k);
+      std::array<int, 3> bestT = {cur.t[0], cur.t[1], cur.t[2]};
+      int bestLanes = c.blocks[0].gradLanes;
+      const int forms = (k == 0 && c.nD == 2) ? 2 : 1;
+      for (int lf = 0; lf < forms && !rc; ++lf)
+        for (const auto& t : cands) {
+          setAll(k, t, lf + 1);
+          double ms = 0.0;
+          if ((rc = timed(&ms))) break;
+          if (ms < best) {
+            best = ms;
+            bestT = t;
+            bestLanes = lf + 1;
+          }
+        }
+      setAll(k, bestT, bestLanes);
+    }
+  const int rr = restore();
+  release();
+  c.launches = launches;
+  c.runSteps = 0;  // the tuning runs leave no trajectory for mgd_run_adjoint
+  if (rc || rr) return 1;
+  for (auto& b : c.blocks) storeTuned(c, b);
+  if (best_ms) *best_ms = best;
   return 0;
 }

@@ -120,9 +120,16 @@ struct BlockRefs {
 
 // Thread-block tiling of a block's points: blocks of t[0] x t[1] x t[2]
 // threads cover n[0] x n[1] x n[2] tiles of the grid.
+// Thread-block tiling of a block's grid: t[] points per CTA along each axis,
+// n[] CTAs along each axis. div[] holds the divisors t[0], t[0] t[1], n[0],
+// n[0] n[1] of the kernels' index decomposition with their reciprocals
+// rcp[] = floor(2^64 / d) + 1 (0 for d = 1), so that a kernel divides by
+// multiply-high instead of an integer division sequence.
 struct Tile {
   int t[3];
   int n[3];
+  unsigned div[4];
+  unsigned long long rcp[4];
   __host__ __device__ int threads() const { return t[0] * t[1] * t[2]; }
   __host__ __device__ int blocks() const { return n[0] * n[1] * n[2]; }
 };
@@ -195,6 +202,7 @@ struct DevBlock {
   std::vector<ExcPatch> exc;
   // tile shapes of the stage kernels, chosen by the autotuner
   Tile tGrad{}, tDiss{}, tRhs{}, tAdjA{}, tAdjD{}, tAdjB{};
+  int gradLanes = 1;  // 2D: kGradFlux with one lane per point (1) or two, one per direction (2)
   std::vector<void*> allocations;
   int nStagePartialBlocks = 0;
   int nInterfaceEntries = 0;

@@ -80,10 +80,27 @@ static void pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s,
 
 static inline int gridFor(long long n) { return (int)((n + kBlock - 1) / kBlock); }
 
+// rcp = floor(2^64 / d) + 1 for d >= 2 (0 for d = 1). For 32-bit x the
+// quotient floor(x / d) is the high word of x * rcp: rcp d = 2^64 + e with
+// 1 <= e <= d, so x rcp / 2^64 = x / d + x e / (d 2^64), and x e < 2^64 keeps
+// the added term below 1/d, short of the next integer (division by invariant
+// integers using multiplication, Granlund and Montgomery, 1994).
+static unsigned long long reciprocal64(unsigned d) {
+  if (d <= 1) return 0;
+  // ~0ULL / d = floor((2^64 - 1) / d): one less than floor(2^64 / d) when d divides 2^64
+  const unsigned long long f = ~0ULL / d + (((d & (d - 1)) == 0) ? 1 : 0);
+  return f + 1;
+}
+
 Tile makeTile(const DevBlock& b, int tx, int ty, int tz) {
   Tile t;
   t.t[0] = tx; t.t[1] = b.v.nD >= 2 ? ty : 1; t.t[2] = b.v.nD >= 3 ? tz : 1;
   for (int d = 0; d < 3; ++d) t.n[d] = (b.v.gs[d] + t.t[d] - 1) / t.t[d];
+  t.div[0] = (unsigned)t.t[0];
+  t.div[1] = (unsigned)(t.t[0] * t.t[1]);
+  t.div[2] = (unsigned)t.n[0];
+  t.div[3] = (unsigned)(t.n[0] * t.n[1]);
+  for (int k = 0; k < 4; ++k) t.rcp[k] = reciprocal64(t.div[k]);
   return t;
 }
 
@@ -134,8 +151,13 @@ __device__ __forceinline__ PointIndex pointIndex(const BlockView& B, long long p
 // tile overhangs the grid.
 __device__ __forceinline__ bool locateAt(const BlockView& B, const Tile& T, int b, int t, long long& p,
                                          PointIndex& r) {
-  const int lx = t % T.t[0], ly = (t / T.t[0]) % T.t[1], lz = t / (T.t[0] * T.t[1]);
-  const int bx = b % T.n[0], by = (b / T.n[0]) % T.n[1], bz = b / (T.n[0] * T.n[1]);
+  // x / d by multiply-high with the tile's reciprocals (x >= 0, 32-bit)
+  auto q = [&](int x, int k) -> int {
+    return T.div[k] == 1 ? x : (int)__umul64hi((unsigned long long)(unsigned)x, T.rcp[k]);
+  };
+  const int t0 = q(t, 0), b0 = q(b, 2);
+  const int lx = t - t0 * T.t[0], lz = q(t, 1), ly = t0 - lz * T.t[1];
+  const int bx = b - b0 * T.n[0], bz = q(b, 3), by = b0 - bz * T.n[1];
   r.idx[0] = bx * T.t[0] + lx;
   r.idx[1] = by * T.t[1] + ly;
   r.idx[2] = bz * T.t[2] + lz;
@@ -304,12 +326,20 @@ __device__ __forceinline__ void wallSatAdjoint(const BlockView& B, const Physics
 // ---------------------------------------------------------------------------
 enum { GF_FLUX = 1, GF_STRESS = 4, GF_STORE = 8 };
 
-template <int ND, bool CURV, bool VISC>
+// LANES = 2 (2D only): two adjacent lanes per point. Lane d applies the
+// derivative stencils along axis d and the pair swaps its three results by
+// shuffle, which halves the dependent stencil loads of each thread; both
+// lanes then form stress and fluxes, lane d writes the contravariant flux of
+// direction d, and the stores of the stage slot and the SAT vectors are split
+// between the lanes.
+template <int ND, bool CURV, bool VISC, int LANES = 1>
 __device__ __forceinline__ void gradFluxPoint(const BlockView& B, const Physics& P, const RunScalars& rs, int flags,
                                               int stage, const Tile& T, int blk) {
+  static_assert(LANES == 1 || (LANES == 2 && ND == 2), "two lanes per point only in 2D");
+  const int lane = LANES == 2 ? (int)(threadIdx.x & 1) : 0;
   long long p;
   PointIndex I;
-  if (!locate(B, T, blk, p, I)) return;
+  if (!locateAt(B, T, blk, LANES == 2 ? (int)(threadIdx.x >> 1) : (int)threadIdx.x, p, I)) return;
   constexpr int nU = ND + 2, E = ND + 1;
   const long long N = B.N;
   const PrimLayout L{ND};
@@ -319,8 +349,9 @@ __device__ __forceinline__ void gradFluxPoint(const BlockView& B, const Physics&
   if (flags & GF_STORE) {
     const int s = ((*rs.step) - (*rs.segBase) - 1) * 4 + stage - 1;
     slot = rs.stageBuf + (long long)s * rs.slotStride;
-    for (int c = 0; c < nU; ++c) slot[p + N * c] = q[c];
-    if (rs.slotFull)
+    if (lane == 0)
+      for (int c = 0; c < nU; ++c) slot[p + N * c] = q[c];
+    if (rs.slotFull && lane == LANES - 1)
       for (int c = 0; c < 6 + ND; ++c) slot[p + N * (nU + c)] = B.prim[p + N * c];
   }
   double m[ND * ND];
@@ -331,11 +362,28 @@ __device__ __forceinline__ void gradFluxPoint(const BlockView& B, const Physics&
   if (VISC && (flags & (GF_FLUX | GF_STRESS))) {
     const double jac = B.jac[p];
     double du[ND][ND], dT[ND];
+    if constexpr (LANES == 2) {
+      const int d = lane;
+      const long long bd = d ? I.base[1] : I.base[0];
+      const int id = d ? I.idx[1] : I.idx[0];
+      const Axis ax = d ? B.ax[1] : B.ax[0];
+      const double a0 = applyOp<OP_D1>(B.prim + N * L.u(0) + bd, id, ax);
+      const double a1 = applyOp<OP_D1>(B.prim + N * L.u(1) + bd, id, ax);
+      const double aT = applyOp<OP_D1>(B.prim + N * L.T() + bd, id, ax);
+      const unsigned pair = 3u << (threadIdx.x & 30);
+      const double b0 = __shfl_xor_sync(pair, a0, 1);
+      const double b1 = __shfl_xor_sync(pair, a1, 1);
+      const double bT = __shfl_xor_sync(pair, aT, 1);
+      du[0][0] = d ? b0 : a0; du[0][1] = d ? a0 : b0;
+      du[1][0] = d ? b1 : a1; du[1][1] = d ? a1 : b1;
+      dT[0] = d ? bT : aT; dT[1] = d ? aT : bT;
+    } else {
 #pragma unroll
-    for (int d = 0; d < ND; ++d) {
+      for (int d = 0; d < ND; ++d) {
 #pragma unroll
-      for (int c = 0; c < ND; ++c) du[c][d] = applyOp<OP_D1>(B.prim + N * L.u(c) + I.base[d], I.idx[d], B.ax[d]);
-      dT[d] = applyOp<OP_D1>(B.prim + N * L.T() + I.base[d], I.idx[d], B.ax[d]);
+        for (int c = 0; c < ND; ++c) du[c][d] = applyOp<OP_D1>(B.prim + N * L.u(c) + I.base[d], I.idx[d], B.ax[d]);
+        dT[d] = applyOp<OP_D1>(B.prim + N * L.T() + I.base[d], I.idx[d], B.ax[d]);
+      }
     }
     double gu[ND][ND], gT[ND];
     for (int x = 0; x < ND; ++x) {
@@ -368,13 +416,17 @@ __device__ __forceinline__ void gradFluxPoint(const BlockView& B, const Physics&
     }
     for (int x = 0; x < ND; ++x) hf[x] = -kd * gT[x];
     if (flags & GF_STRESS) {
-      for (int c = 0; c < ND * ND; ++c) B.tau[p + N * c] = tau[c];
-      for (int x = 0; x < ND; ++x) B.hf[p + N * x] = hf[x];
+      if (lane == 0)
+        for (int c = 0; c < ND * ND; ++c) B.tau[p + N * c] = tau[c];
+      if (lane == LANES - 1)
+        for (int x = 0; x < ND; ++x) B.hf[p + N * x] = hf[x];
     }
     if (slot && rs.slotFull) {
       double* st = slot + N * (nU + 6 + ND);
-      for (int c = 0; c < ND * ND; ++c) st[p + N * c] = tau[c];
-      for (int x = 0; x < ND; ++x) st[p + N * (ND * ND + x)] = hf[x];
+      if (lane == 0)
+        for (int c = 0; c < ND * ND; ++c) st[p + N * c] = tau[c];
+      if (lane == LANES - 1)
+        for (int x = 0; x < ND; ++x) st[p + N * (ND * ND + x)] = hf[x];
     }
   }
   if (flags & GF_FLUX) {
@@ -399,7 +451,7 @@ __device__ __forceinline__ void gradFluxPoint(const BlockView& B, const Physics&
         Fv[E][d] = e - hf[d];
       }
     }
-    for (int s = 0; s < 3; ++s) {
+    for (int s = 0; s < 3 && lane == 0; ++s) {
       const int e = B.ffOfPoint[3 * p + s];
       if (e < 0) continue;
       if (B.ff.kind[e] == SAT_INTERFACE) {
@@ -443,17 +495,26 @@ __device__ __forceinline__ void gradFluxPoint(const BlockView& B, const Physics&
     if (VISC)
       for (int r = 1; r < nU; ++r)
         for (int d = 0; d < ND; ++d) F[r][d] = F[r][d] - Fv[r][d];
-    for (int i = 0; i < ND; ++i)
+    if constexpr (LANES == 2) {
+      const int i = lane;
       for (int c = 0; c < nU; ++c) {
-        double s;
-        if (CURV) {
-          s = m[ND * i] * F[c][0];
-          for (int d = 1; d < ND; ++d) s += m[ND * i + d] * F[c][d];
-        } else {
-          s = m[ND * i + i] * F[c][i];
-        }
+        const double s = CURV ? (i ? m[2] : m[0]) * F[c][0] + (i ? m[3] : m[1]) * F[c][1]
+                              : (i ? m[3] : m[0]) * (i ? F[c][1] : F[c][0]);
         B.fhat[p + N * (i * nU + c)] = s;
       }
+    } else {
+      for (int i = 0; i < ND; ++i)
+        for (int c = 0; c < nU; ++c) {
+          double s;
+          if (CURV) {
+            s = m[ND * i] * F[c][0];
+            for (int d = 1; d < ND; ++d) s += m[ND * i + d] * F[c][d];
+          } else {
+            s = m[ND * i + i] * F[c][i];
+          }
+          B.fhat[p + N * (i * nU + c)] = s;
+        }
+    }
   }
 }
 
@@ -462,6 +523,13 @@ __global__ void __launch_bounds__(kMaxTile) kGradFlux(BlockView B, Physics P, Ru
                                                       int stage, Tile T) {
   pdlEnter();
   gradFluxPoint<ND, CURV, VISC>(B, P, rs, flags, stage, T, blockIdx.x);
+}
+
+template <bool CURV, bool VISC>
+__global__ void __launch_bounds__(2 * kMaxTile) kGradFluxPair(BlockView B, Physics P, RunScalars rs, int flags,
+                                                              int stage, Tile T) {
+  pdlEnter();
+  gradFluxPoint<2, CURV, VISC, 2>(B, P, rs, flags, stage, T, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -1758,7 +1826,12 @@ void launchGradFlux(Context& c, DevBlock& b, bool writeFlux, bool writeStress, c
   MGD_LAUNCH(c);
 #define GF(ND, CU, VI) \
   pdl(kGradFlux<ND, CU, VI>, T.blocks(), T.threads(), on(c, s), b.v, c.phys, r, flags, stage, T)
-  if (c.nD == 2) {
+#define GP(CU, VI) \
+  pdl(kGradFluxPair<CU, VI>, T.blocks(), 2 * T.threads(), on(c, s), b.v, c.phys, r, flags, stage, T)
+  if (c.nD == 2 && b.gradLanes == 2) {
+    if (curv) { if (visc) GP(true, true); else GP(true, false); }
+    else { if (visc) GP(false, true); else GP(false, false); }
+  } else if (c.nD == 2) {
     if (curv) { if (visc) GF(2, true, true); else GF(2, true, false); }
     else { if (visc) GF(2, false, true); else GF(2, false, false); }
   } else {
@@ -1766,6 +1839,7 @@ void launchGradFlux(Context& c, DevBlock& b, bool writeFlux, bool writeStress, c
     else { if (visc) GF(3, false, true); else GF(3, false, false); }
   }
 #undef GF
+#undef GP
 }
 
 void launchDissipation(Context& c, DevBlock& b, const double* src, double sign, cudaStream_t s) {

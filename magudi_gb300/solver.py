@@ -81,6 +81,12 @@ def load_library(build_if_missing=True):
     L.mgd_stream.argtypes = [ctx]
     L.mgd_kernel_launches.restype = C.c_longlong
     L.mgd_kernel_launches.argtypes = [ctx, C.c_int]
+    L.mgd_gradient_lanes.restype = C.c_int
+    L.mgd_gradient_lanes.argtypes = [ctx, C.c_int]
+    L.mgd_tune_run.restype = C.c_int
+    L.mgd_tune_run.argtypes = [ctx, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    L.mgd_stage_tile.restype = C.c_int
+    L.mgd_stage_tile.argtypes = [ctx, C.c_int, C.POINTER(C.c_int), C.c_int]
     _lib = L
     return L
 
@@ -278,6 +284,32 @@ class Solver:
 
     def kernel_launches(self, reset=False):
         return self.L.mgd_kernel_launches(self.h, int(reset))
+
+    def tune_run(self, n_steps, save_interval, with_adjoint=True):
+        """Run-level autotuning of the stage-kernel tiles on short checkpointed
+        runs from the current state (which is restored). Returns the tuned
+        run's wall time in ms."""
+        v = C.c_double()
+        self._check(self.L.mgd_tune_run(self.h, int(n_steps), int(save_interval), int(bool(with_adjoint)),
+                                        C.byref(v)))
+        return v.value
+
+    def stage_tile(self, kernel, tile=None):
+        """Tile (points per CTA along x, y, z) of stage kernel `kernel` (0..5):
+        returns the current one, or sets `tile` first."""
+        t = (C.c_int * 3)(*(tile or (0, 0, 0)))
+        self._check(self.L.mgd_stage_tile(self.h, int(kernel), t, 1 if tile else 0))
+        if tile:
+            self._check(self.L.mgd_stage_tile(self.h, int(kernel), t, 0))
+        return tuple(t)
+
+    def gradient_lanes(self, lanes=0):
+        """Form of the 2D gradient/flux kernel: 1 or 2 threads per point
+        (lanes = 0 reports the autotuned form, 1 or 2 sets it)."""
+        r = self.L.mgd_gradient_lanes(self.h, int(lanes))
+        if r < 0:
+            raise MagudiError(self.L.mgd_last_error(self.h).decode())
+        return r
 
 
 class Batch:
