@@ -65,6 +65,11 @@ def parse():
     ap.add_argument("--sweep-instances", type=int, default=64)
     ap.add_argument("--sweep-per-call-sample", type=int, default=4,
                     help="instances timed through the per-call entry points beside the batch")
+    ap.add_argument("--tiles", default=None,
+                    help="stage-kernel tiles instead of run-level tuning, e.g. 8x16x1,8x8x1,8x16x1,8x8x1,8x8x1,16x4x1 "
+                         "(gradient/flux, dissipation, divergence, adjoint core, diffusion, assembly), as a bench "
+                         "line's config.tile_tuning.tiles reports them")
+    ap.add_argument("--grad-lanes", type=int, default=0, help="with --tiles: 2D gradient/flux threads per point")
     ap.add_argument("--profile-only", action="store_true",
                     help="run the gradient evaluations and exit (for ncu captures; prints no bench line)")
     return ap.parse_args()
@@ -267,15 +272,27 @@ def run_ours(args):
     # run-level tile tuning on short gradient runs (setup, outside the timed region)
     set_q(q0_dev.data_ptr())
     t_tune = time.perf_counter()
-    tuned_ms = s.tune_run(4 * SAVE_INTERVAL, SAVE_INTERVAL)
+    if args.tiles:
+        for k, t in enumerate(args.tiles.split(",")):
+            s.stage_tile(k, tuple(int(x) for x in t.split("x")))
+        if args.grad_lanes:
+            s.gradient_lanes(args.grad_lanes)
+        tuned_ms = None
+    else:
+        tuned_ms = s.tune_run(4 * SAVE_INTERVAL, SAVE_INTERVAL)
     tuning = {"seconds": time.perf_counter() - t_tune, "run_steps": 4 * SAVE_INTERVAL, "tuned_run_ms": tuned_ms,
-              "tiles": [list(s.stage_tile(k)) for k in range(6)], "gradient_flux_threads_per_point": s.gradient_lanes()}
+              "tiles": [list(s.stage_tile(k)) for k in range(6)], "gradient_flux_threads_per_point": s.gradient_lanes(),
+              "source": "--tiles" if args.tiles else "mgd_tune_run"}
     for _ in range(args.warmup):
         gradient_step(q0_dev.data_ptr())
     torch.cuda.synchronize()
     if args.profile_only:
+        # the timed-equivalent evaluations in an NVTX range (ncu --nvtx --nvtx-include "gradient/")
+        torch.cuda.nvtx.range_push("gradient")
         for _ in range(args.steps):
             J, G = gradient_step(q0_dev.data_ptr())
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         # one forward and one adjoint RHS of the final state through the
         # per-call entry points, in an NVTX range for filtered ncu captures
         # (ncu --nvtx --nvtx-include "stage_rhs/")
