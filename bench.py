@@ -172,26 +172,29 @@ def measured_peaks():
 # Algorithmic traffic and FP64 operations per grid point of each stage kernel
 # on the 2D viscous Cartesian workload (each array element that the kernel
 # needs read or written once; stencil neighbours are re-reads, not counted).
-# bytes: doubles x 8 plus int32 index words x 4; flops: adds and multiplies
-# count 1, FMAs 2.
+# bytes: doubles x 8 plus int32 index words x 4. flops: the FP64 operations
+# the kernel executes per point on the 201x201 grid, counted by ncu
+# (2 x DFMA + DADD + DMUL over the launch, divided by the points; the kernels
+# evaluate each term of their operation list once, boundary closure rows
+# included).
 KERNEL_UNITS = {
     # q 4, prim (u 2, p, T, mu, la, k) 7, metric diagonal 2, jac 1; writes fhat 8; ffOfPoint 3 ints
-    "forward_gradient_flux": {"bytes": 8 * (4 + 7 + 2 + 1 + 8) + 4 * 3, "flops": 130},
+    "forward_gradient_flux": {"bytes": 8 * (4 + 7 + 2 + 1 + 8) + 4 * 3, "flops": 122},
     # q 4 read, dq 4 written
-    "forward_dissipation": {"bytes": 8 * (4 + 4), "flops": 80},
+    "forward_dissipation": {"bytes": 8 * (4 + 4), "flops": 122},
     # fhat 8, dq 4, jac 1, q 4, qt 4, sponge 1, srcG 1, b1 4, b2 4 read; b2 4, q 4 written; ffOfPoint 3 + iblank 1 ints
-    "forward_divergence_rk": {"bytes": 8 * (8 + 4 + 1 + 4 + 4 + 1 + 1 + 4 + 4 + 4 + 4) + 4 * 4, "flops": 90},
+    "forward_divergence_rk": {"bytes": 8 * (8 + 4 + 1 + 4 + 4 + 1 + 1 + 4 + 4 + 4 + 4) + 4 * 4, "flops": 118},
     # q 4 read, prim 8 written
-    "forward_primitives": {"bytes": 8 * (4 + 8), "flops": 55},
+    "forward_primitives": {"bytes": 8 * (4 + 8), "flops": 69},
     # lambda 4, metric diagonal 2, prim (u 2, v, T, mu, la, k) 7, tau 4, hf 2, jac 1 read; rcore 4, ad 6 written
-    "adjoint_core": {"bytes": 8 * (4 + 2 + 7 + 4 + 2 + 1 + 4 + 6) + 4 * 3, "flops": 370},
+    "adjoint_core": {"bytes": 8 * (4 + 2 + 7 + 4 + 2 + 1 + 4 + 6) + 4 * 3, "flops": 480},
     # lambda 4 read, dq 4 written
-    "adjoint_dissipation": {"bytes": 8 * (4 + 4), "flops": 80},
+    "adjoint_dissipation": {"bytes": 8 * (4 + 4), "flops": 122},
     # ad 6 read, t2 3 written
-    "adjoint_diffusion": {"bytes": 8 * (6 + 3), "flops": 48},
+    "adjoint_diffusion": {"bytes": 8 * (6 + 3), "flops": 84},
     # rcore 4, prim (v, u 2) 3, q_E 1, t2 3, dq 4, jac 1, lambda 4, sponge 1, tgtCount 1, b1 4, b2 4 read;
     # b2 4, lambda 4 written; ffOfPoint 3 + iblank 1 ints
-    "adjoint_assemble_rk": {"bytes": 8 * (4 + 3 + 1 + 3 + 4 + 1 + 4 + 1 + 1 + 4 + 4 + 4 + 4) + 4 * 4, "flops": 60},
+    "adjoint_assemble_rk": {"bytes": 8 * (4 + 3 + 1 + 3 + 4 + 1 + 4 + 1 + 1 + 4 + 4 + 4 + 4) + 4 * 4, "flops": 47},
 }
 # DRAM bytes (read + write) per launch from an ncu capture of the 201x201
 # gradient workload (dram__bytes_read.sum + dram__bytes_write.sum, three
