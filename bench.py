@@ -70,6 +70,8 @@ def parse():
                          "(gradient/flux, dissipation, divergence, adjoint core, diffusion, assembly), as a bench "
                          "line's config.tile_tuning.tiles reports them")
     ap.add_argument("--grad-lanes", type=int, default=0, help="with --tiles: 2D gradient/flux threads per point")
+    ap.add_argument("--checkpoint-only", action="store_true",
+                    help="recompute checkpoint segments in the adjoint instead of keeping the trajectory on the device")
     ap.add_argument("--profile-only", action="store_true",
                     help="run the gradient evaluations and exit (for ncu captures; prints no bench line)")
     return ap.parse_args()
@@ -253,6 +255,9 @@ def run_ours(args):
     pts = blk.n_points
     nU = P.n_unknowns
     s = Solver(P)
+    # the 960-step trajectory (4 x 960 stage slots, about 22 GB) stays on the
+    # device: the adjoint reads it instead of recomputing checkpoint segments
+    s.set_trajectory_storage(not args.checkpoint_only)
     stream = torch.cuda.ExternalStream(s.stream_handle())
     n_entries = 4 * n_steps
     Pact = s.actuator_points()
@@ -373,7 +378,11 @@ def run_ours(args):
         "config": {"workload": WORKLOAD, "grid": "201x201", "rk4_steps": N_STEPS, "save_interval": SAVE_INTERVAL,
                    "l2": "512 MB buffer written between timed steps (working set fits in L2)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "tile_tuning": tuning},
+                   "tile_tuning": tuning,
+                   "adjoint_forward_states": ("checkpoints every %d steps, segments recomputed beside the adjoint"
+                                              % SAVE_INTERVAL) if args.checkpoint_only else
+                                             "resident trajectory: every stage's state, primitives, stress and "
+                                             "heat flux kept on the device by the forward run"},
         "adjoint_gradient_s": ms / 1e3,
         "J": J, "grad0": G,
         "e2e": {"value": e2e, "unit": "Mpt-RHS/s", "ms_per_step": e2e_ms,

@@ -277,6 +277,19 @@ int mgd_run_linearized(mgd_ctx* ctx, const double* delta_forcing, long long n_en
  * checkpointed runs take their forcing from mgd_set_control_forcing instead. */
 int mgd_set_patch_control_forcing(mgd_ctx* ctx, const double* forcing);
 
+/* Resident trajectory (no reference counterpart; the reference always
+ * recomputes checkpoint segments, src/SolverImpl.f90:1027-1245 with
+ * UniformCheckpointer): with enable != 0, mgd_run_forward of a single-block
+ * context also stores every RK stage's state, primitives, stress and heat
+ * flux on the device when the 4 x n_steps stage slots fit in max_bytes
+ * (<= 0: half of the free device memory), and the following mgd_run_adjoint
+ * reads them instead of recomputing the segments between checkpoints. The
+ * results are identical either way; runs that do not fit, multi-block
+ * contexts, and an adjoint after anything else that reuses the stage buffer
+ * (mgd_run_linearized) recompute as usual. Off by default: a forward-only
+ * user would hold the slots for nothing. */
+int mgd_set_trajectory_storage(mgd_ctx* ctx, int enable, double max_bytes);
+
 /* adjoint_nonzero_initial_condition (src/SolverImpl.f90:1027-1102, set per
  * segment by bin/msadjoint.f90:141-400): when enabled, mgd_run_adjoint starts
  * from the adjoint field the context holds (loaded with mgd_set_field(...,

@@ -201,6 +201,14 @@ long long mgd_kernel_launches(mgd_ctx* h, int reset) {
   return n;
 }
 
+int mgd_set_trajectory_storage(mgd_ctx* h, int enable, double max_bytes) {
+  Context& c = h->c;
+  c.trajectoryStorage = enable != 0;
+  c.trajectoryMaxBytes = max_bytes;
+  if (!enable) c.trajectorySteps = 0;
+  return 0;
+}
+
 int mgd_stage_tile(mgd_ctx* h, int kernel, int* tile, int set) {
   Context& c = h->c;
   if (kernel < 0 || kernel > 5 || !tile) return fail(c, "mgd_stage_tile: kernel must be 0..5 and tile non-null");
@@ -1800,6 +1808,7 @@ static int ensureStepBuffers(Context& c, DevBlock& b, int nSteps) {
 // input state q and, when memory allows, also its primitive variables, stress
 // and heat flux, so the adjoint stages read them instead of recomputing them.
 static int ensureStageBuffer(Context& c, DevBlock& b, int S) {
+  c.trajectorySteps = 0;  // the slots are about to hold recomputed segments
   const long long N = b.v.N;
   const int nD = c.nD, nU = c.nU;
   const long long qOnly = (long long)nU * N;
@@ -1828,6 +1837,38 @@ static int ensureStageBuffer(Context& c, DevBlock& b, int S) {
   c.stageHalf = options[pick][2];
   c.slotStride = options[pick][1];
   c.slotFull = options[pick][1] == full ? 1 : 0;
+  return 0;
+}
+
+// Stage buffer for a resident trajectory of T steps: 4 T full slots when they
+// fit the budget (*resident = true), else nothing changes (*resident = false).
+static int ensureTrajectoryBuffer(Context& c, DevBlock& b, int T, bool* resident) {
+  *resident = false;
+  c.trajectorySteps = 0;
+  const long long N = b.v.N;
+  const long long full = (long long)(c.nU + PrimLayout{c.nD}.count() + c.nD * c.nD + c.nD) * N;
+  const long long need = 4LL * T * full;
+  size_t freeB = 0, totalB = 0;
+  CUDA_TRY(c, cudaMemGetInfo(&freeB, &totalB));
+  const double budget = c.trajectoryMaxBytes > 0.0
+                            ? c.trajectoryMaxBytes
+                            : 0.5 * ((double)freeB + (double)c.stageBufCapacity * sizeof(double));
+  if ((double)need * sizeof(double) > budget) return 0;
+  if (c.stageBufCapacity < need) {
+    cudaFree(c.dStageBuf);
+    c.dStageBuf = nullptr;
+    c.stageBufCapacity = 0;
+    if (cudaMalloc((void**)&c.dStageBuf, (size_t)need * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();  // out of memory: fall back to checkpoints
+      return 0;
+    }
+    c.stageBufCapacity = need;
+  }
+  c.stageHalves = 1;
+  c.stageHalf = need;
+  c.slotStride = full;
+  c.slotFull = 1;
+  *resident = true;
   return 0;
 }
 
@@ -2224,11 +2265,16 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
   const bool cflMode = c.opts.use_constant_cfl != 0;
   const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
   const bool functional = c.opts.enable_functional != 0 && c.opts.functional_type == MGD_FUNCTIONAL_SOUND;
+  // with a resident trajectory the flux kernel also stores every stage's
+  // state, primitives, stress and heat flux, which the adjoint run then reads
+  // instead of recomputing checkpoint segments
+  bool resident = false;
+  if (c.trajectoryStorage && ensureTrajectoryBuffer(c, b, n_steps, &resident)) return 1;
   RunScalars rs = runScalars(c);
   if (setCounters(c, 1, 0)) return 1;
   if (capture(c, &c.gForward, &c.nodesForward, [&]() {
         if (cflMode) launchTimeStep(c, b, c.dDtPartials, c.dStepDt, c.dCounters, c.dTime, c.dStageTime, c.dAmp);
-        for (int i = 1; i <= 4; ++i) forwardStage(c, b, i, rs, false, controller, false, functional);
+        for (int i = 1; i <= 4; ++i) forwardStage(c, b, i, rs, false, controller, resident, functional);
         launchSnapshot(c, b, c.dSnapshots, save_interval, false);
         launchStepAdvance(c, 1);
       }))
@@ -2236,7 +2282,9 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
   for (int s = 0; s < n_steps; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gForward, c.stream));
   c.launches += (long long)n_steps * c.nodesForward;
   if (checkLaunch(c)) return 1;
-  return finishForwardRun(c, cost);
+  if (finishForwardRun(c, cost)) return 1;
+  c.trajectorySteps = resident ? n_steps : 0;
+  return 0;
 }
 
 int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
@@ -2246,9 +2294,12 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   if (!singleBlock(c)) return regionRunAdjoint(c, sensitivity);
   DevBlock& b = c.blocks[0];
   const long long N = b.v.N;
-  const int nU = c.nU, T = c.runSteps, S = c.saveInterval;
+  const int nU = c.nU, T = c.runSteps;
+  // a resident trajectory of this run: one segment over all steps, no recomputation
+  const bool resident = c.trajectorySteps == T;
+  const int S = resident ? T : c.saveInterval;
   const double dtT = c.stepDt[T - 1];  // step size of the final forward step
-  if (ensureStageBuffer(c, b, S)) return 1;
+  if (!resident && ensureStageBuffer(c, b, S)) return 1;
   const bool twoLanes = c.stageHalves == 2;
   if (twoLanes && ensureShadow(c, b)) return 1;
   const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
@@ -2281,7 +2332,7 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
     RunScalars rr = ra;
     rr.step = recCounters;
     rr.segBase = recCounters + 1;
-    if (capture(c, &c.gRecomputeH[half], &nodesRec, [&]() {
+    if (!resident && capture(c, &c.gRecomputeH[half], &nodesRec, [&]() {
           for (int i = 1; i <= 4; ++i) forwardStage(c, rb, i, rr, false, controller, true, false, &recLanes);
           launchStepAdvanceOn(recCounters, 1, recLanes.main);
         }, recLanes.main))
@@ -2320,7 +2371,7 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
     CUDA_TRY(c, cudaEventRecord(c.evFork[3], c.stream));
     CUDA_TRY(c, cudaStreamWaitEvent(c.stream2, c.evFork[3], 0));
   }
-  if (recompute(nSeg - 1)) return 1;
+  if (!resident && recompute(nSeg - 1)) return 1;
   for (int k = nSeg - 1; k >= 0; --k) {
     const int L = k * S, end = std::min(T, L + S);
     const int half = k % c.stageHalves;

@@ -292,6 +292,12 @@ struct Context {
   bool shadowReady = false;
   long long slotStride = 0;         // doubles per stage slot of dStageBuf
   int slotFull = 0;                 // slots also hold primitives, stress and heat flux
+  // Resident trajectory: the forward run stores every stage's slot (4 T full
+  // slots in dStageBuf) when enabled and within the byte budget (<= 0: half
+  // the free device memory); trajectorySteps = T while those slots are intact
+  int trajectoryStorage = 0;
+  double trajectoryMaxBytes = 0.0;
+  int trajectorySteps = 0;
   // RK4 coefficients per step of the last run (dt, dt/6, dt/3, dt/2), their
   // step sizes on the host, constant-CFL reduction scratch and run time
   double* dStepDt = nullptr;

@@ -83,6 +83,8 @@ def load_library(build_if_missing=True):
     L.mgd_kernel_launches.argtypes = [ctx, C.c_int]
     L.mgd_gradient_lanes.restype = C.c_int
     L.mgd_gradient_lanes.argtypes = [ctx, C.c_int]
+    L.mgd_set_trajectory_storage.restype = C.c_int
+    L.mgd_set_trajectory_storage.argtypes = [ctx, C.c_int, C.c_double]
     L.mgd_tune_run.restype = C.c_int
     L.mgd_tune_run.argtypes = [ctx, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.mgd_stage_tile.restype = C.c_int
@@ -284,6 +286,12 @@ class Solver:
 
     def kernel_launches(self, reset=False):
         return self.L.mgd_kernel_launches(self.h, int(reset))
+
+    def set_trajectory_storage(self, enable=True, max_bytes=0.0):
+        """Store every RK stage of the forward run on the device (when it fits
+        in max_bytes, <= 0: half the free device memory) so that run_adjoint
+        reads the trajectory instead of recomputing checkpoint segments."""
+        self._check(self.L.mgd_set_trajectory_storage(self.h, int(bool(enable)), float(max_bytes)))
 
     def tune_run(self, n_steps, save_interval, with_adjoint=True):
         """Run-level autotuning of the stage-kernel tiles on short checkpointed

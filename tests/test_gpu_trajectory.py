@@ -1,0 +1,71 @@
+"""Resident trajectory (-m gpu): the forward run stores every RK stage on the
+device and the adjoint run reads it instead of recomputing checkpoint
+segments. The adjoint consumes the same forward states either way, so J, the
+sensitivity and the gradient are bitwise those of the checkpointed run, and
+both match the oracle."""
+import numpy as np
+import pytest
+
+import oracle_lib
+from helpers import rel_err, small_monopole
+from magudi_gb300 import capi, configs
+from magudi_gb300.solver import Solver
+
+pytestmark = pytest.mark.gpu
+
+
+def _gradient(s, P):
+    J = s.run_forward(P.n_steps, P.save_interval)
+    G = s.run_adjoint()
+    return J, G, s.gradient(4 * P.n_steps), s.get_field(1, capi.FIELD_ADJOINT)
+
+
+@pytest.mark.parametrize("cfl", [False, True])
+def test_resident_trajectory_is_bitwise_the_checkpointed_gradient(cfl):
+    P = small_monopole(n_steps=30, save_interval=7, **({"cfl": 0.8} if cfl else {}))
+    a, b = Solver(P), Solver(P)
+    b.set_trajectory_storage(True)
+    ra, rb = _gradient(a, P), _gradient(b, P)
+    assert ra[0] == rb[0] and ra[1] == rb[1]
+    assert np.array_equal(ra[2], rb[2]) and np.array_equal(ra[3], rb[3])
+    o = oracle_lib.Oracle(P)
+    ro = _gradient(o, P)
+    assert abs(rb[0] - ro[0]) <= 1e-10 * abs(ro[0])
+    assert abs(rb[1] - ro[1]) <= 1e-10 * abs(ro[1])
+    assert rel_err(rb[2], ro[2]) < 1e-10
+
+
+def test_budget_too_small_falls_back_to_checkpoints():
+    P = small_monopole(n_steps=20, save_interval=5)
+    a, b = Solver(P), Solver(P)
+    b.set_trajectory_storage(True, max_bytes=1024.0)
+    ra, rb = _gradient(a, P), _gradient(b, P)
+    assert ra[0] == rb[0] and ra[1] == rb[1] and np.array_equal(ra[2], rb[2])
+
+
+def test_tangent_run_between_forward_and_adjoint_invalidates_the_trajectory():
+    """The tangent run recomputes segments into the stage buffer; the adjoint
+    after it then recomputes too and still gives the checkpointed gradient."""
+    P = small_monopole(n_steps=16, save_interval=4)
+    a, b = Solver(P), Solver(P)
+    b.set_trajectory_storage(True)
+    ra = _gradient(a, P)
+    Jb = b.run_forward(P.n_steps, P.save_interval)
+    b.set_field(1, capi.FIELD_ADJOINT, np.zeros((4, P.blocks[0].n_points)))
+    b.run_linearized()
+    b.set_field(1, capi.FIELD_ADJOINT, np.zeros((4, P.blocks[0].n_points)))
+    Gb = b.run_adjoint()
+    assert Jb == ra[0] and Gb == ra[1]
+    assert np.array_equal(b.gradient(4 * P.n_steps), ra[2])
+
+
+def test_wall_channel_with_resident_trajectory():
+    P = configs.wall_channel_2d(wall="SAT_ISOTHERMAL_WALL", n_steps=12)
+    a, b = Solver(P), Solver(P)
+    b.set_trajectory_storage(True)
+    for s in (a, b):
+        s.run_forward(P.n_steps, 5)
+        s.set_field(1, capi.FIELD_ADJOINT, np.full((4, P.blocks[0].n_points), 1e-3))
+        s.set_adjoint_nonzero_initial_condition(True)
+        s.run_adjoint()
+    assert np.array_equal(a.get_field(1, capi.FIELD_ADJOINT), b.get_field(1, capi.FIELD_ADJOINT))
