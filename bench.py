@@ -70,6 +70,7 @@ def parse():
                          "(gradient/flux, dissipation, divergence, adjoint core, diffusion, assembly), as a bench "
                          "line's config.tile_tuning.tiles reports them")
     ap.add_argument("--grad-lanes", type=int, default=0, help="with --tiles: 2D gradient/flux threads per point")
+    ap.add_argument("--core-lanes", type=int, default=0, help="with --tiles: 2D adjoint core threads per point")
     ap.add_argument("--checkpoint-only", action="store_true",
                     help="recompute checkpoint segments in the adjoint instead of keeping the trajectory on the device")
     ap.add_argument("--profile-only", action="store_true",
@@ -285,11 +286,14 @@ def run_ours(args):
             s.stage_tile(k, tuple(int(x) for x in t.split("x")))
         if args.grad_lanes:
             s.gradient_lanes(args.grad_lanes)
+        if args.core_lanes:
+            s.adjoint_core_lanes(args.core_lanes)
         tuned_ms = None
     else:
         tuned_ms = s.tune_run(4 * SAVE_INTERVAL, SAVE_INTERVAL)
     tuning = {"seconds": time.perf_counter() - t_tune, "run_steps": 4 * SAVE_INTERVAL, "tuned_run_ms": tuned_ms,
               "tiles": [list(s.stage_tile(k)) for k in range(6)], "gradient_flux_threads_per_point": s.gradient_lanes(),
+              "adjoint_core_threads_per_point": s.adjoint_core_lanes(),
               "source": "--tiles" if args.tiles else "mgd_tune_run"}
     for _ in range(args.warmup):
         gradient_step(q0_dev.data_ptr())

@@ -410,6 +410,13 @@ long long mgd_kernel_launches(mgd_ctx* ctx, int reset);
  * always use 1), or -1 for other values of lanes. */
 int mgd_gradient_lanes(mgd_ctx* ctx, int lanes);
 
+/* Measurement and test hook (no reference counterpart): the form of the
+ * adjoint core of 2D blocks, one thread per point (1) or one per point and
+ * axis (2, the axes' shares summed in shared memory). Only mgd_tune_run
+ * chooses the second form. lanes = 1 or 2 sets it for every block of the
+ * context, 0 only reports it; returns the form in effect (3D: 1), or -1. */
+int mgd_adjoint_core_lanes(mgd_ctx* ctx, int lanes);
+
 /* Run-level autotuner (no reference counterpart): chooses the thread-block
  * tiles of the six stage kernels (and the 2D gradient/flux form) by timing
  * whole checkpointed runs, mgd_run_forward(n_steps, save_interval) followed

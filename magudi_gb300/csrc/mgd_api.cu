@@ -228,6 +228,17 @@ int mgd_stage_tile(mgd_ctx* h, int kernel, int* tile, int set) {
   return 0;
 }
 
+int mgd_adjoint_core_lanes(mgd_ctx* h, int lanes) {
+  Context& c = h->c;
+  if (lanes < 0 || lanes > 2) {
+    fail(c, "mgd_adjoint_core_lanes: lanes must be 0, 1 or 2");
+    return -1;
+  }
+  if (lanes > 0 && c.nD == 2)
+    for (auto& b : c.blocks) b.coreLanes = lanes;
+  return c.nD == 2 && !c.blocks.empty() ? c.blocks[0].coreLanes : 1;
+}
+
 int mgd_gradient_lanes(mgd_ctx* h, int lanes) {
   Context& c = h->c;
   if (lanes < 0 || lanes > 2) {
@@ -598,7 +609,7 @@ struct TuneKey {
 // per-kernel autotuner at setup and replaced by mgd_tune_run.
 struct Tuned {
   std::array<Tile, 6> tiles;
-  int gradLanes;
+  int gradLanes, coreLanes;
 };
 static std::map<TuneKey, Tuned> g_tuneCache;
 static std::mutex g_tuneCacheMutex;
@@ -613,6 +624,7 @@ static void storeTuned(const Context& c, const DevBlock& b) {
   Tuned entry;
   for (int k = 0; k < 6; ++k) entry.tiles[k] = *slots[k];
   entry.gradLanes = b.gradLanes;
+  entry.coreLanes = b.coreLanes;
   std::lock_guard<std::mutex> lock(g_tuneCacheMutex);
   g_tuneCache[tuneKey(c, b)] = entry;
 }
@@ -626,6 +638,7 @@ static int autotune(Context& c, DevBlock& b) {
     if (it != g_tuneCache.end()) {
       for (int k = 0; k < 6; ++k) *slots[k] = it->second.tiles[k];
       b.gradLanes = it->second.gradLanes;
+      b.coreLanes = it->second.coreLanes;
       return 0;
     }
   }
@@ -2311,7 +2324,7 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   rb.desc = b.desc;
   rb.v = twoLanes ? c.shadow : b.v;
   rb.exc = b.exc;
-  rb.tGrad = b.tGrad; rb.tDiss = b.tDiss; rb.tRhs = b.tRhs; rb.gradLanes = b.gradLanes;
+  rb.tGrad = b.tGrad; rb.tDiss = b.tDiss; rb.tRhs = b.tRhs; rb.gradLanes = b.gradLanes; rb.coreLanes = b.coreLanes;
   rb.tAdjA = b.tAdjA; rb.tAdjD = b.tAdjD; rb.tAdjB = b.tAdjB;
   const Lanes adjLanes{c.stream, c.side, c.evFork[1], c.evJoin[1]};
   const Lanes recLanes = twoLanes ? Lanes{c.stream2, c.side2, c.evFork[2], c.evJoin[2]}
@@ -3014,6 +3027,7 @@ int mgd_tune_run(mgd_ctx* h, int n_steps, int save_interval, int with_adjoint, d
     for (auto& b : c.blocks) {
       slotOf(b, k) = makeTile(b, t[0], t[1], t[2]);
       if (k == 0 && c.nD == 2) b.gradLanes = lanes;
+      if (k == 3 && c.nD == 2) b.coreLanes = lanes;
     }
   };
   int rc = 0;
@@ -3025,8 +3039,10 @@ int mgd_tune_run(mgd_ctx* h, int n_steps, int save_interval, int with_adjoint, d
       if ((k == 1 && !c.phys.dissipation) || (k == 4 && !c.phys.viscous) || (k >= 3 && !with_adjoint)) continue;
       const Tile& cur = slotOf(c.blocks[0], k);
       std::array<int, 3> bestT = {cur.t[0], cur.t[1], cur.t[2]};
-      int bestLanes = c.blocks[0].gradLanes;
-      const int forms = (k == 0 && c.nD == 2) ? 2 : 1;
+      int bestLanes = k == 3 ? c.blocks[0].coreLanes : c.blocks[0].gradLanes;
+      // 2D: the gradient/flux kernel and the adjoint core also have a form
+      // with one thread per point and direction
+      const int forms = ((k == 0 || k == 3) && c.nD == 2) ? 2 : 1;
       for (int lf = 0; lf < forms && !rc; ++lf)
         for (const auto& t : cands) {
           setAll(k, t, lf + 1);

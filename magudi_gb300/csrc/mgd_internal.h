@@ -203,6 +203,7 @@ struct DevBlock {
   // tile shapes of the stage kernels, chosen by the autotuner
   Tile tGrad{}, tDiss{}, tRhs{}, tAdjA{}, tAdjD{}, tAdjB{};
   int gradLanes = 1;  // 2D: kGradFlux with one lane per point (1) or two, one per direction (2)
+  int coreLanes = 1;  // 2D: kAdjointCore (1) or kAdjointCoreSplit, one thread per point and direction (2)
   std::vector<void*> allocations;
   int nStagePartialBlocks = 0;
   int nInterfaceEntries = 0;

@@ -78,6 +78,22 @@ static void pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s,
 
 
 
+// pdl with dynamic shared memory.
+template <typename... KArgs, typename... Args>
+static void pdlShared(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args&&... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = t_programmaticLaunch ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 static inline int gridFor(long long n) { return (int)((n + kBlock - 1) / kBlock); }
 
 // rcp = floor(2^64 / d) + 1 for d >= 2 (0 for d = 1). For 32-bit x the
@@ -816,6 +832,40 @@ __device__ __forceinline__ void adjointCoreFinish(const BlockView& B, const Phys
   }
 }
 
+// One direction's share of the adjoint core at a point: w = D+_I lambda, the
+// (A_I - B1_I)^T w product into y and the B2(m_I, m_j)^T w products into
+// ad[j]. y and ad start from zero, so summing the directions' shares in
+// direction order reproduces the per-point accumulation exactly.
+template <int ND, bool CURV, bool VISC, int I>
+__device__ __forceinline__ void adjointCoreDirection(const BlockView& B, const Physics& P, const PointIndex& Ix,
+                                                     const double* m, const double* u, double Tm, double v,
+                                                     const double* tau, const double* hf, double mu, double la,
+                                                     double kd, double jac, double* y, double (*ad)[ND + 1]) {
+  constexpr int nU = ND + 2, nV = ND + 1;
+  const long long N = B.N;
+  double w[nU];
+#pragma unroll
+  for (int c = 0; c < nU; ++c) w[c] = applyOp<OP_D1ADJ>(B.lam + N * c + Ix.base[I], Ix.idx[I], B.ax[I]);
+  for (int c = 0; c < nU; ++c) y[c] = 0.0;
+  if (CURV) {
+    addFluxJacobianTransposeProduct<ND, VISC>(m + ND * I, u, Tm, v, P.g, P.powerLawExponent, tau, hf, w, y);
+  } else {
+    const double nTv = VISC ? P.powerLawExponent * P.g * v / Tm : 0.0;
+    addFluxJacobianTransposeProductCart<ND, VISC>(I, m[ND * I + I], u, Tm, v, P.g, nTv, tau, hf, w, y);
+  }
+  if (VISC) {
+#pragma unroll
+    for (int j = 0; j < ND; ++j) {
+      for (int c = 0; c < nV; ++c) ad[j][c] = 0.0;
+      if (CURV)
+        secondPartialViscousTransposeProduct<ND>(u, mu, la, kd, jac, m + ND * I, m + ND * j, &w[1], ad[j]);
+      else
+        secondPartialViscousTransposeProductCart<ND>(u, mu, la, kd, jac, I, m[ND * I + I], j, m[ND * j + j], &w[1],
+                                                     ad[j]);
+    }
+  }
+}
+
 template <int ND, bool CURV, bool VISC>
 __device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physics& P, const RunScalars& rs,
                                                  int stage, int fromSlot, const Tile& T, int blk) {
@@ -870,6 +920,77 @@ __device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physi
       }
     }
   }
+  adjointCoreFinish<ND, VISC>(B, P, p, fs, m, u, Tm, v, tau, hf, y, ad);
+}
+
+// The adjoint core with nD threads per point: thread block = tile threads x
+// nD, thread (point, direction I) forms its direction's share
+// (adjointCoreDirection), the shares meet in shared memory and the
+// direction-0 thread of each point sums them in direction order and finishes
+// the point. Twice (2D) the threads of the per-point kernel, each with a
+// third of its stencil work, for grids too small to fill the GPU per point.
+template <int ND, bool CURV, bool VISC>
+__global__ void __launch_bounds__(2 * kMaxTile) kAdjointCoreSplit(BlockView B, Physics P, RunScalars rs, int stage,
+                                                                 int fromSlot, Tile T) {
+  pdlEnter();
+  constexpr int nU = ND + 2, nV = ND + 1, K = nU + ND * nV;
+  extern __shared__ double share[];
+  const int TT = T.threads();
+  const int pt = threadIdx.x % TT, dir = threadIdx.x / TT;
+  long long p = 0;
+  PointIndex I;
+  const bool ok = locateAt(B, T, blockIdx.x, pt, p, I);
+  const long long N = B.N;
+  const PrimLayout L{ND};
+  FwdState fs{};
+  double m[ND * ND], u[ND], tau[ND * ND], hf[ND];
+  double v = 0.0, Tm = 0.0;
+  if (ok) {
+    fs = forwardState<ND>(B, rs, stage, fromSlot != 0);
+    for (int c = 0; c < ND * ND; ++c) m[c] = (CURV || (c % (ND + 1)) == 0) ? B.metrics[p + N * c] : 0.0;
+    for (int d = 0; d < ND; ++d) u[d] = fs.prim[p + N * L.u(d)];
+    v = fs.prim[p + N * L.v()];
+    Tm = fs.prim[p + N * L.T()];
+    if (VISC) {
+      for (int c = 0; c < ND * ND; ++c) tau[c] = fs.tau[p + N * c];
+      for (int d = 0; d < ND; ++d) hf[d] = fs.hf[p + N * d];
+    }
+    double mu = 0.0, la = 0.0, kd = 0.0, jac = 0.0;
+    if (VISC) {
+      mu = fs.prim[p + N * L.mu()];
+      la = fs.prim[p + N * L.la()];
+      kd = fs.prim[p + N * L.k()];
+      jac = B.jac[p];
+    }
+    double y[nU], ad[ND][nV];
+    if (dir == 0)
+      adjointCoreDirection<ND, CURV, VISC, 0>(B, P, I, m, u, Tm, v, tau, hf, mu, la, kd, jac, y, ad);
+    else if (ND > 1 && dir == 1)
+      adjointCoreDirection<ND, CURV, VISC, (ND > 1 ? 1 : 0)>(B, P, I, m, u, Tm, v, tau, hf, mu, la, kd, jac, y, ad);
+    else
+      adjointCoreDirection<ND, CURV, VISC, (ND > 2 ? 2 : 0)>(B, P, I, m, u, Tm, v, tau, hf, mu, la, kd, jac, y, ad);
+    double* mine = share + (long long)dir * K * TT + pt;
+    for (int c = 0; c < nU; ++c) mine[c * TT] = y[c];
+    if (VISC)
+      for (int j = 0; j < ND; ++j)
+        for (int c = 0; c < nV; ++c) mine[(nU + j * nV + c) * TT] = ad[j][c];
+  }
+  __syncthreads();
+  if (!ok || dir != 0) return;
+  double y[nU], ad[ND][nV];
+  for (int c = 0; c < nU; ++c) {
+    double t = share[c * TT + pt];
+    for (int i = 1; i < ND; ++i) t += share[((long long)i * K + c) * TT + pt];
+    y[c] = t;
+  }
+  if (VISC)
+    for (int j = 0; j < ND; ++j)
+      for (int c = 0; c < nV; ++c) {
+        const int k = nU + j * nV + c;
+        double t = share[k * TT + pt];
+        for (int i = 1; i < ND; ++i) t += share[((long long)i * K + k) * TT + pt];
+        ad[j][c] = t;
+      }
   adjointCoreFinish<ND, VISC>(B, P, p, fs, m, u, Tm, v, tau, hf, y, ad);
 }
 
@@ -1948,6 +2069,15 @@ void launchAdjointCore(Context& c, DevBlock& b, const RunScalars& rs, int stage,
   cudaStream_t st = on(c, s);
   const bool curv = b.v.curvilinear != 0, visc = c.phys.viscous != 0;
   MGD_LAUNCH(c);
+  if (b.coreLanes == 2 && c.nD == 2) {
+    // nD threads per point; their shares meet in shared memory
+    const size_t smem = (size_t)2 * (4 + 2 * 3) * W * sizeof(double);
+#define ACS(CU, VI) pdlShared(kAdjointCoreSplit<2, CU, VI>, G, 2 * W, smem, st, b.v, c.phys, rs, stage, fromSlot, T)
+    if (curv) { if (visc) ACS(true, true); else ACS(true, false); }
+    else { if (visc) ACS(false, true); else ACS(false, false); }
+#undef ACS
+    return;
+  }
 #define AC(ND, CU, VI) pdl(kAdjointCore<ND, CU, VI>, G, W, st, b.v, c.phys, rs, stage, fromSlot, T)
   if (c.nD == 2) {
     if (curv) { if (visc) AC(2, true, true); else AC(2, true, false); }

@@ -83,6 +83,8 @@ def load_library(build_if_missing=True):
     L.mgd_kernel_launches.argtypes = [ctx, C.c_int]
     L.mgd_gradient_lanes.restype = C.c_int
     L.mgd_gradient_lanes.argtypes = [ctx, C.c_int]
+    L.mgd_adjoint_core_lanes.restype = C.c_int
+    L.mgd_adjoint_core_lanes.argtypes = [ctx, C.c_int]
     L.mgd_set_trajectory_storage.restype = C.c_int
     L.mgd_set_trajectory_storage.argtypes = [ctx, C.c_int, C.c_double]
     L.mgd_tune_run.restype = C.c_int
@@ -310,6 +312,14 @@ class Solver:
         if tile:
             self._check(self.L.mgd_stage_tile(self.h, int(kernel), t, 0))
         return tuple(t)
+
+    def adjoint_core_lanes(self, lanes=0):
+        """Form of the 2D adjoint core: 1 or 2 threads per point (lanes = 0
+        reports it, 1 or 2 sets it)."""
+        r = self.L.mgd_adjoint_core_lanes(self.h, int(lanes))
+        if r < 0:
+            raise MagudiError(self.L.mgd_last_error(self.h).decode())
+        return r
 
     def gradient_lanes(self, lanes=0):
         """Form of the 2D gradient/flux kernel: 1 or 2 threads per point

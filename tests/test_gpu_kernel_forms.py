@@ -1,10 +1,11 @@
-"""Both forms of the 2D gradient/flux kernel against the oracle (-m gpu): one
-thread per point, and two adjacent threads per point (one per axis, results
-swapped by shuffle). The setup's autotuner keeps the faster form;
-mgd_gradient_lanes sets either one, so both are checked here on every path
-that launches the kernel: forward and adjoint RHS (curvilinear grid, walls,
-block interfaces), checkpointed forward + adjoint runs with the concurrent
-recomputation, and the tangent run."""
+"""Both forms of the 2D gradient/flux kernel and of the 2D adjoint core
+against the oracle (-m gpu): one thread per point, and one thread per point
+and axis (gradient/flux: results swapped by shuffle; adjoint core: shares
+summed in shared memory). The tuners keep the faster forms;
+mgd_gradient_lanes and mgd_adjoint_core_lanes set them, so every form is
+checked here on every path that launches the kernels: forward and adjoint RHS
+(curvilinear grid, walls, block interfaces), checkpointed forward + adjoint
+runs with the concurrent recomputation, and the tangent run."""
 import numpy as np
 import pytest
 
@@ -15,13 +16,15 @@ from magudi_gb300.solver import MagudiError, Solver
 
 pytestmark = pytest.mark.gpu
 
-LANES = [1, 2]
+# (gradient/flux threads per point, adjoint core threads per point)
+LANES = [(1, 1), (2, 1), (1, 2)]
 
 
 def _gpu(P, lanes):
     s = Solver(P)
-    assert s.gradient_lanes() in (1, 2)
-    assert s.gradient_lanes(lanes) == lanes
+    assert s.gradient_lanes() in (1, 2) and s.adjoint_core_lanes() in (1, 2)
+    assert s.gradient_lanes(lanes[0]) == lanes[0]
+    assert s.adjoint_core_lanes(lanes[1]) == lanes[1]
     return s
 
 
@@ -44,6 +47,8 @@ def test_lanes_argument_is_checked():
     s = Solver(small_monopole())
     with pytest.raises(MagudiError):
         s.gradient_lanes(3)
+    with pytest.raises(MagudiError):
+        s.adjoint_core_lanes(-1)
 
 
 @pytest.mark.parametrize("lanes", LANES)
@@ -130,6 +135,7 @@ def test_run_level_tuning_restores_the_state_and_keeps_parity():
     g2 = Solver(P)
     assert [g2.stage_tile(k) for k in range(6)] == [g.stage_tile(k) for k in range(6)]
     assert g2.gradient_lanes() == g.gradient_lanes()
+    assert g2.adjoint_core_lanes() == g.adjoint_core_lanes()
 
 
 def test_stage_tile_hook_checks_its_arguments():
