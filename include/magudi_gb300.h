@@ -284,9 +284,9 @@ int mgd_set_patch_control_forcing(mgd_ctx* ctx, const double* forcing);
  * flux on the device when the 4 x n_steps stage slots fit in max_bytes
  * (<= 0: half of the free device memory), and the following mgd_run_adjoint
  * reads them instead of recomputing the segments between checkpoints. The
- * results are identical either way; runs that do not fit, multi-block
- * contexts, and an adjoint after anything else that reuses the stage buffer
- * (mgd_run_linearized) recompute as usual. Off by default: a forward-only
+ * results are identical either way. mgd_run_linearized reads the same slots
+ * and leaves them for a later mgd_run_adjoint. Runs that do not fit and
+ * multi-block contexts recompute as usual. Off by default: a forward-only
  * user would hold the slots for nothing. */
 int mgd_set_trajectory_storage(mgd_ctx* ctx, int enable, double max_bytes);
 

@@ -2440,8 +2440,12 @@ int mgd_run_linearized(mgd_ctx* h, const double* delta_forcing, long long n_entr
   if (refuseLinearized(c)) return 1;
   DevBlock& b = c.blocks[0];
   const long long N = b.v.N;
-  const int nU = c.nU, T = c.runSteps, S = c.saveInterval;
-  if (ensureStageBuffer(c, b, S)) return 1;
+  const int nU = c.nU, T = c.runSteps;
+  // a resident trajectory of this run: one segment, no recomputation (and the
+  // slots stay intact for a following adjoint run)
+  const bool resident = c.trajectorySteps == T;
+  const int S = resident ? T : c.saveInterval;
+  if (!resident && ensureStageBuffer(c, b, S)) return 1;
   const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
   const bool deltaControl = c.opts.enable_controller && c.opts.controller_switch && delta_forcing && n_entries > 0 &&
                             c.actuatorPoints > 0;
@@ -2481,7 +2485,7 @@ int mgd_run_linearized(mgd_ctx* h, const double* delta_forcing, long long n_entr
   } graphs{&gRec, &gLin};
   long long nodesRec = 0, nodesLin = 0;
   const Lanes lanes{c.stream, c.side, c.evFork[0], c.evJoin[0]};
-  if (capture(c, &gRec, &nodesRec, [&]() {
+  if (!resident && capture(c, &gRec, &nodesRec, [&]() {
         for (int i = 1; i <= 4; ++i) forwardStage(c, b, i, rs, false, controller, true, false, &lanes);
         launchStepAdvance(c, 1);
       }))
@@ -2506,11 +2510,13 @@ int mgd_run_linearized(mgd_ctx* h, const double* delta_forcing, long long n_entr
   const int nSeg = (T + S - 1) / S;
   for (int k = 0; k < nSeg; ++k) {
     const int L = k * S, end = std::min(T, L + S);
-    CUDA_TRY(c, cudaMemcpyAsync(b.v.q, c.dSnapshots + (size_t)k * nU * N, (size_t)nU * N * sizeof(double),
-                                cudaMemcpyDeviceToDevice, c.stream));
-    launchPrims(c, b, b.v.q, false);
-    launchSetCounters(c.dCounters, L + 1, L, c.stream);
-    for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(gRec, c.stream));
+    if (!resident) {
+      CUDA_TRY(c, cudaMemcpyAsync(b.v.q, c.dSnapshots + (size_t)k * nU * N, (size_t)nU * N * sizeof(double),
+                                  cudaMemcpyDeviceToDevice, c.stream));
+      launchPrims(c, b, b.v.q, false);
+      launchSetCounters(c.dCounters, L + 1, L, c.stream);
+      for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(gRec, c.stream));
+    }
     launchSetCounters(c.dCounters, L + 1, L, c.stream);
     for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(gLin, c.stream));
     c.launches += 3 + (long long)(end - L) * (nodesRec + nodesLin);

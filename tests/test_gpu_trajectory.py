@@ -43,16 +43,25 @@ def test_budget_too_small_falls_back_to_checkpoints():
     assert ra[0] == rb[0] and ra[1] == rb[1] and np.array_equal(ra[2], rb[2])
 
 
-def test_tangent_run_between_forward_and_adjoint_invalidates_the_trajectory():
-    """The tangent run recomputes segments into the stage buffer; the adjoint
-    after it then recomputes too and still gives the checkpointed gradient."""
+def test_tangent_run_reads_the_trajectory_and_keeps_it_for_the_adjoint():
+    """A tangent run between the forward and adjoint runs reads the resident
+    slots too: its result and the gradient after it are those of the
+    checkpointed runs."""
     P = small_monopole(n_steps=16, save_interval=4)
     a, b = Solver(P), Solver(P)
     b.set_trajectory_storage(True)
     ra = _gradient(a, P)
+    rng = np.random.default_rng(4)
+    dq0 = 1e-3 * rng.standard_normal((4, P.blocks[0].n_points))
+    t = Solver(P)  # checkpointed tangent run from the initial state
+    t.run_forward(P.n_steps, P.save_interval)
+    t.set_field(1, capi.FIELD_ADJOINT, dq0)
+    t.run_linearized()
+    dq_a = t.get_field(1, capi.FIELD_ADJOINT)
     Jb = b.run_forward(P.n_steps, P.save_interval)
-    b.set_field(1, capi.FIELD_ADJOINT, np.zeros((4, P.blocks[0].n_points)))
+    b.set_field(1, capi.FIELD_ADJOINT, dq0)
     b.run_linearized()
+    assert np.array_equal(b.get_field(1, capi.FIELD_ADJOINT), dq_a)
     b.set_field(1, capi.FIELD_ADJOINT, np.zeros((4, P.blocks[0].n_points)))
     Gb = b.run_adjoint()
     assert Jb == ra[0] and Gb == ra[1]
