@@ -701,13 +701,18 @@ def run_msgrad(args):
     Pseg = configs.monopole_2d(n=GRID, n_steps=nts, save_interval=SAVE_INTERVAL)
     Pfull = configs.monopole_2d(n=GRID, n_steps=T, save_interval=SAVE_INTERVAL)
     single = Solver(Pfull)
+    resident = not args.checkpoint_only
     q0 = Pfull.blocks[0].initial_state
     ics = [None]
     for k in range(1, K):
         single.set_field(1, capi.FIELD_CONSERVED, q0)
         single.run_forward(k * nts, SAVE_INTERVAL)
         ics.append([single.get_field(1, capi.FIELD_CONSERVED)])
-    ms = MultiSegment(Pseg, K, nts, penalty_weight=1.0, save_interval=SAVE_INTERVAL)
+    # both the segments and the single run keep their trajectories on the device
+    single.set_trajectory_storage(resident)
+    single.set_field(1, capi.FIELD_CONSERVED, q0)
+    single.tune_run(4 * SAVE_INTERVAL, SAVE_INTERVAL)
+    ms = MultiSegment(Pseg, K, nts, penalty_weight=1.0, save_interval=SAVE_INTERVAL, store_trajectory=resident)
 
     def ms_step():
         r = ms.forward(ics)
@@ -747,6 +752,8 @@ def run_msgrad(args):
                                f"(initial conditions on the trajectory, quadratic matching penalty), forward + "
                                f"discrete adjoint of every segment, segments concurrent; checkpoint every "
                                f"{SAVE_INTERVAL} steps",
+                   "trajectory": "recomputed from checkpoints" if args.checkpoint_only else
+                                 "resident in every segment's context and in the single run",
                    "segments": K, "segment_steps": nts, "l2": "working set fits in L2 (no flush)",
                    "parallelism": "single GPU, one context and host thread per segment"},
         "J": J, "gradient_inner_product": G,
@@ -761,11 +768,12 @@ def run_msgrad(args):
 
 def run_tangent(args):
     """Tangent (linearized) run of the 2D monopole (201^2, 960 steps):
-    Solver%runLinearized along the checkpointed forward trajectory
-    (checkpoints every 10 steps, each segment's stage states recomputed
-    before its linearized steps). One bench step is the forward run plus the
-    tangent run; the metric counts forward and linearized RHS evaluations
-    per second, and the tangent run alone is reported beside it."""
+    Solver%runLinearized along the forward trajectory, kept on the device by
+    the forward run (with --checkpoint-only: checkpoints every 10 steps, each
+    segment's stage states recomputed before its linearized steps). One bench
+    step is the forward run plus the tangent run; the metric counts forward
+    and linearized RHS evaluations per second, and the tangent run alone is
+    reported beside it."""
     import numpy as np
     import torch
     from magudi_gb300 import capi

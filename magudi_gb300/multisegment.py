@@ -73,7 +73,7 @@ class MultiSegment:
 
     def __init__(self, problem, n_segments, segment_length, penalty_weight, penalty_type="quadratic",
                  huber_threshold=1e-12, state_mollifier=None, start_time=0.0, save_interval=None,
-                 backend=None, concurrent=True):
+                 backend=None, concurrent=True, store_trajectory=False):
         if penalty_type not in ("quadratic", "huber"):
             raise ValueError(f"Unknown time_splitting/penalty_type '{penalty_type}': expected 'quadratic' or 'huber'.")
         if n_segments < 1 or segment_length < 1:
@@ -91,6 +91,10 @@ class MultiSegment:
         self.save_interval = save_interval or max(1, int(round(segment_length ** 0.5)))
         self.concurrent = concurrent
         self.ctx = [backend(problem) for _ in range(n_segments)]
+        if store_trajectory:
+            # each segment's forward run keeps its stages on the device for its adjoint run
+            for c in self.ctx:
+                c.set_trajectory_storage(True)
         self.n_blocks = len(problem.blocks)
         self.norms = [np.asarray(self.ctx[0].get_field(b, capi.FIELD_NORM)).reshape(-1)
                       for b in range(1, self.n_blocks + 1)]

@@ -36,3 +36,22 @@ def test_multisegment_matches_oracle(kind, mollified):
     assert rel_err(ag.gradient, ao.gradient) < RUN_TOL
     for k in range(1, K):
         assert rel_err(ag.ic_gradients[k][0], ao.ic_gradients[k][0]) < RUN_TOL
+
+
+def test_multisegment_with_resident_trajectories_is_bitwise_the_checkpointed_one():
+    """Every segment context keeps its trajectory (store_trajectory): J, the
+    control gradient and the initial-condition gradients are those of the
+    segments that recompute checkpoints."""
+    P = _problem()
+    ics = _trajectory_ics(P, perturb=2e-4, seed=5)
+    out = []
+    for store in (False, True):
+        ms = MultiSegment(P, K, NTS, penalty_weight=3.0, store_trajectory=store)
+        rng = np.random.default_rng(1)
+        ms.set_control_forcing(1e-3 * rng.standard_normal((4 * K * NTS, ms.P)))
+        out.append((ms.forward(ics), ms.adjoint()))
+    (f0, a0), (f1, a1) = out
+    assert f0.J == f1.J and a0.total == a1.total
+    assert np.array_equal(a0.gradient, a1.gradient)
+    for k in range(1, K):
+        assert np.array_equal(a0.ic_gradients[k][0], a1.ic_gradients[k][0])
