@@ -33,7 +33,10 @@ class ForwardRun(torch.autograd.Function):
     """J = ForwardRun.apply(forcing, solver, n_steps, save_interval).
 
     forcing: float64 tensor (4 * n_steps, P) on the CPU or the solver's GPU.
-    Each call restarts the run from the problem's initial state."""
+    Each call restarts the run from the problem's initial state. With
+    solver.set_trajectory_storage(True) the forward run keeps every stage on
+    the device and backward() reads it instead of recomputing checkpoint
+    segments (same gradient)."""
 
     @staticmethod
     def forward(ctx, forcing, solver, n_steps, save_interval):

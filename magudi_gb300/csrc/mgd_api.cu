@@ -1441,7 +1441,18 @@ void forwardStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bo
   if (diss || exc) cudaStreamWaitEvent(L.main, L.join, 0);
   launchForwardDivergence(c, b, rkStage, rs, api, controller, L.main);
   if (rkStage > 0) launchPrims(c, b, b.v.q, false, nullptr, 0, L.main);
-  if (functional) launchFunctional(c, b, rs, stage, L.main);
+  if (functional) {
+    if ((diss || exc) && rkStage >= 1 && rkStage <= 3) {
+      // beside the next stage's flux kernel: that stage's side work queues
+      // behind it and its join comes before that stage's primitives replace
+      // these and before the step counter advances
+      cudaEventRecord(L.fork, L.main);
+      cudaStreamWaitEvent(L.side, L.fork, 0);
+      launchFunctional(c, b, rs, stage, L.side);
+    } else {
+      launchFunctional(c, b, rs, stage, L.main);
+    }
+  }
 }
 
 // One adjoint RK stage (rkStage 4..1) or the adjoint RHS alone (rkStage 0).
