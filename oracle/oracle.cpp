@@ -4,7 +4,7 @@
 // TEST INFRASTRUCTURE ONLY. This file is the parity oracle for the CUDA path
 // and the timed CPU baseline. It is never linked into, loaded by or called
 // from the product library; only tests/, __graft_entry__.smoke() and the
-// cpu_baseline / --impl reference legs of bench.py use it, as the checker.
+// cpu_baseline / --impl reference legs of bench.py use it, to compare against.
 //
 // Every routine restates the reference routine cited beside it (paths are
 // relative to the magudi source tree). Loop orders, the order of operations

@@ -1,6 +1,6 @@
 """ctypes front end of the CPU oracle (oracle/oracle.cpp) for the tests.
 
-The oracle is the checker: tests compare the CUDA library against it. It is
+Tests compare the CUDA library against the oracle. It is
 built by oracle/build.sh into oracle/_build/liboracle.so.
 """
 import ctypes as C

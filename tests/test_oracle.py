@@ -1,5 +1,5 @@
 """The CPU oracle against the reference's golden vectors and property tests
-(CPU only). These pin the oracle before it is trusted as the checker:
+(CPU only). These pin the oracle before the GPU tests compare against it:
 
 - SBP 4-8 first derivative vs the reference's own Python implementation
   (tests/golden/sbp48_first_derivative.npz, made by make_sbp_golden.py);
