@@ -36,8 +36,7 @@ GRID = 201
 N_STEPS = 960
 SAVE_INTERVAL = 10
 WORKLOAD = ("2D acoustic monopole 201x201, FP64 viscous NS, SBP 4-8 + dissipation 0.01, far-field SAT + "
-            "20-pt sponge, forward 960 RK4 steps (dt 0.05) + discrete adjoint, uniform checkpointing "
-            "every 10 steps on the device")
+            "20-pt sponge, forward 960 RK4 steps (dt 0.05) + discrete adjoint gradient, checkpoints every 10 steps")
 
 
 def parse():
