@@ -58,6 +58,7 @@ def parse():
                          "monopole forward run followed by the linearized (tangent) run along it")
     ap.add_argument("--ms-segments", type=int, default=8)
     ap.add_argument("--tgv-n", type=int, default=256)
+    ap.add_argument("--tgv-steps", type=int, default=10, help="RK4 steps of the Taylor-Green sample (of the 2000-step run)")
     ap.add_argument("--jet-steps", type=int, default=8, help="RK4 steps of the jet sample (of the 1000-step run)")
     ap.add_argument("--jet-save-interval", type=int, default=4)
     ap.add_argument("--jet-scale", type=float, default=1.0, help="grid scale of the jet (1 = 39.4 M points)")
@@ -543,7 +544,7 @@ def run_tgv(args):
     """3D Taylor-Green vortex on n^3 points, PLANE-periodic, Re 1600, Mach 0.1,
     constant CFL 0.5: forward run plus the discrete adjoint of the terminal
     kinetic energy, with checkpoints held on the device. The configured run
-    has 2000 steps; one bench step is a bounded sample of --rk-steps steps
+    has 2000 steps; one bench step is a bounded sample of --tgv-steps steps
     (forward + adjoint) of it, and the metric counts grid points x RHS
     evaluations per second like the default workload."""
     import torch
@@ -552,7 +553,7 @@ def run_tgv(args):
 
     rank, world, local = rank_info()
     torch.cuda.set_device(local)
-    n_steps = args.rk_steps
+    n_steps = args.tgv_steps
     P = configs.taylor_green_3d(n=args.tgv_n, n_steps=n_steps)
     S = P.save_interval
     s = Solver(P)

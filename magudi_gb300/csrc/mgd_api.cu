@@ -642,17 +642,18 @@ static int autotune(Context& c, DevBlock& b) {
       return 0;
     }
   }
-  // CTAs of 128 or 256 threads: the stage kernels of one RK stage share the
-  // SMs with the side-stream dissipation and, in adjoint runs, with the
-  // concurrent checkpoint recomputation, and smaller CTAs that are fastest
-  // alone fill the SMs' CTA slots (at most 32 per SM) and slow those down
+  // 2D: CTAs of 128 or 256 threads. At 2D sizes a stage kernel is a single
+  // wave that shares the SMs with the side-stream dissipation and, in adjoint
+  // runs, the concurrent checkpoint recomputation; smaller CTAs that are
+  // fastest alone fill the SMs' CTA slots (at most 32 per SM) and slow those
+  // down. 3D kernels run many waves and also take 64-thread tiles.
   std::vector<std::array<int, 3>> cands;
   if (c.nD == 2)
     cands = {{128, 1, 1}, {64, 2, 1}, {32, 4, 1}, {16, 8, 1}, {8, 16, 1},
              {256, 1, 1}, {128, 2, 1}, {64, 4, 1}, {32, 8, 1}, {16, 16, 1}};
   else
-    cands = {{32, 2, 2}, {32, 4, 1}, {16, 4, 2}, {16, 8, 1}, {8, 8, 2}, {32, 1, 4}, {64, 2, 1}, {8, 4, 4},
-             {32, 4, 2}, {16, 4, 4}, {64, 2, 2}};
+    cands = {{32, 2, 2}, {32, 4, 1}, {16, 4, 2}, {16, 8, 1}, {8, 8, 2}, {32, 1, 4}, {64, 2, 1},
+             {32, 2, 1}, {16, 2, 2}, {8, 4, 4}, {32, 4, 2}};
   RunScalars rs = apiScalars(c);
   if (setApiTime(c, 0.0)) return 1;
   launchPrims(c, b, b.v.q, false);
