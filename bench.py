@@ -361,9 +361,9 @@ def run_ours(args):
     kern = dict(zip(FORWARD_KERNELS, fwd))
     kern.update(zip(ADJOINT_KERNELS, adj))
     # launches per gradient evaluation: forward stage kernels run in the forward
-    # pass and again in the checkpoint recomputation, the functional only in the
-    # forward pass, adjoint kernels once
-    per_grad = {k: 8 * n_steps for k in FORWARD_KERNELS}
+    # pass (and again in the checkpoint recomputation unless the trajectory is
+    # resident), the functional only in the forward pass, adjoint kernels once
+    per_grad = {k: (8 if args.checkpoint_only else 4) * n_steps for k in FORWARD_KERNELS}
     per_grad["forward_functional"] = 4 * n_steps
     per_grad.update({k: 4 * n_steps for k in ADJOINT_KERNELS})
     share = {k: kern[k] * per_grad[k] for k in kern}

@@ -209,6 +209,10 @@ class Oracle:
     def set_adjoint_nonzero_initial_condition(self, enable):
         self.L.orc_set_adjoint_nonzero_initial_condition(self.h, int(bool(enable)))
 
+    def set_trajectory_storage(self, enable=True, max_bytes=0.0):
+        """The oracle always recomputes checkpoint segments, as the reference
+        does; the setting only mirrors the library's API (same results)."""
+
     def run_linearized(self, delta_forcing=None):
         """Tangent run; returns the tangent of the functional."""
         v = C.c_double()

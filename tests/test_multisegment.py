@@ -74,3 +74,23 @@ def test_multisegment_gradient_finite_difference(kind, mollified):
             Js.append(ms2.forward(ics2).J)
         best = min(best, abs((Js[0] - Js[1]) / (2 * e) - a.total) / a.total)
     assert best < 1e-6
+
+
+def test_store_trajectory_option_reaches_every_segment_context():
+    """store_trajectory asks every segment context to keep its trajectory; on
+    the oracle (which always recomputes) the results are unchanged."""
+    P = _problem()
+    ics = _trajectory_ics(P, perturb=1e-4, seed=2)
+    calls = []
+
+    class Recording(oracle_lib.Oracle):
+        def set_trajectory_storage(self, enable=True, max_bytes=0.0):
+            calls.append(enable)
+
+    out = []
+    for store in (False, True):
+        ms = MultiSegment(P, K, NTS, penalty_weight=2.0, backend=Recording, concurrent=False,
+                          store_trajectory=store)
+        out.append((ms.forward(ics).J, ms.adjoint().total))
+    assert calls == [True] * K
+    assert out[0] == out[1]
