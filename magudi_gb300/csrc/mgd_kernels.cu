@@ -48,6 +48,8 @@ constexpr int kMaxTile = 256;    // largest stage-kernel tile
 // stream start launching as soon as all of its own blocks are running, and
 // waits for its predecessor to complete (and its memory to be visible) before
 // touching memory. Kernels launched without the attribute pass straight through.
+// Waiting before the trigger (early launch one kernel deep) measured about 1%
+// slower in the 201x201 gradient and the batched sweep.
 __device__ __forceinline__ void pdlEnter() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   asm volatile("griddepcontrol.wait;" ::: "memory");
