@@ -3048,6 +3048,19 @@ int mgd_tune_run(mgd_ctx* h, int n_steps, int save_interval, int with_adjoint, d
       if (k == 3 && c.nD == 2) b.coreLanes = lanes;
     }
   };
+  // the tiles and forms on entry, put back if a timed run fails
+  struct Entry {
+    std::array<Tile, 6> tiles;
+    int gradLanes, coreLanes;
+  };
+  std::vector<Entry> entry;
+  for (auto& b : c.blocks) {
+    Entry e;
+    for (int k = 0; k < 6; ++k) e.tiles[k] = slotOf(b, k);
+    e.gradLanes = b.gradLanes;
+    e.coreLanes = b.coreLanes;
+    entry.push_back(e);
+  }
   int rc = 0;
   double best = 0.0;
   for (int w = 0; w < 2 && !rc; ++w) rc = runOnce(&best);  // warm-up: clocks, graph buffers
@@ -3074,10 +3087,21 @@ int mgd_tune_run(mgd_ctx* h, int n_steps, int save_interval, int with_adjoint, d
         }
       setAll(k, bestT, bestLanes);
     }
+  if (rc) {
+    const std::string err = c.error;
+    for (size_t i = 0; i < c.blocks.size(); ++i) {
+      DevBlock& b = c.blocks[i];
+      for (int k = 0; k < 6; ++k) slotOf(b, k) = entry[i].tiles[k];
+      b.gradLanes = entry[i].gradLanes;
+      b.coreLanes = entry[i].coreLanes;
+    }
+    c.error = err;
+  }
   const int rr = restore();
   release();
   c.launches = launches;
   c.runSteps = 0;  // the tuning runs leave no trajectory for mgd_run_adjoint
+  c.trajectorySteps = 0;
   if (rc || rr) return 1;
   for (auto& b : c.blocks) storeTuned(c, b);
   if (best_ms) *best_ms = best;
