@@ -3031,9 +3031,12 @@ int mgd_tune_run(mgd_ctx* h, int n_steps, int save_interval, int with_adjoint, d
     return 0;
   };
   std::vector<std::array<int, 3>> cands;
+  // (2D also whole-warp tiles that are not powers of two: other CTA counts
+  // per grid, which can spread a single wave more evenly over the SMs)
   if (c.nD == 2)
     cands = {{8, 8, 1}, {16, 4, 1}, {32, 2, 1}, {64, 1, 1}, {8, 16, 1}, {16, 8, 1},
-             {32, 4, 1}, {64, 2, 1}, {128, 1, 1}, {16, 16, 1}, {32, 8, 1}};
+             {32, 4, 1}, {64, 2, 1}, {128, 1, 1}, {16, 16, 1}, {32, 8, 1},
+             {8, 12, 1}, {16, 6, 1}, {16, 10, 1}, {8, 20, 1}, {16, 12, 1}, {32, 6, 1}};
   else
     cands = {{8, 4, 2}, {16, 2, 2}, {32, 2, 1}, {8, 8, 2}, {16, 4, 2}, {32, 2, 2}, {32, 4, 1},
              {16, 8, 1}, {8, 4, 4}, {64, 2, 1}, {16, 4, 4}};

@@ -145,3 +145,21 @@ def test_stage_tile_hook_checks_its_arguments():
     with pytest.raises(MagudiError):
         s.stage_tile(0, (32, 16, 1))  # 512 threads
     assert s.stage_tile(2, (16, 8, 1)) == (16, 8, 1)
+
+
+@pytest.mark.parametrize("tile", [(12, 10, 1), (7, 9, 1)])
+def test_tiles_that_are_not_powers_of_two(tile):
+    """Tiles of any shape: the kernels split CTA indices with reciprocals of
+    the tile's extents, exact for any divisor."""
+    P = small_monopole(n_steps=12, save_interval=5)
+    g, o = Solver(P), oracle_lib.Oracle(P)
+    for k in range(6):
+        assert g.stage_tile(k, tile) == tile
+    q, lam = random_full_rhs_state(P, 23)
+    _rhs_pair(g, o, 1, [q], [lam])
+    for s in (g, o):
+        s.set_field(1, capi.FIELD_CONSERVED, P.blocks[0].initial_state)
+    Jg, Jo = g.run_forward(P.n_steps, P.save_interval), o.run_forward(P.n_steps, P.save_interval)
+    assert abs(Jg - Jo) <= 1e-10 * abs(Jo)
+    Gg, Go = g.run_adjoint(), o.run_adjoint()
+    assert abs(Gg - Go) <= 1e-10 * abs(Go)
