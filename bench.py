@@ -399,7 +399,9 @@ def run_ours(args):
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
                      "traffic": MEASURED_TRAFFIC.get(dominant), "peak_source": peak_kind,
                      "fp64": {"achieved_tflops": achieved_tf, "peak_tflops": fp64_peak,
-                              "frac": achieved_tf / fp64_peak, "peak_source": "measured: cuBLAS DGEMM 4096^3"}},
+                              "frac": achieved_tf / fp64_peak, "peak_source": "measured: cuBLAS DGEMM 4096^3"},
+                     "note": "FP64 path with no tensor-core work: the binding roof is the FP64 pipe (fp64.frac); "
+                             "the 201x201 working set stays in L2, so the HBM fraction is not the bound"},
     }
     if rank == 0 and world == 1:
         # the same gradient through the per-call entry points (the reference's own
