@@ -77,3 +77,13 @@ def test_create_without_gpu_fails_loudly(lib):
 def test_extent_resolution_matches_bc_dat_convention():
     p = problem.Patch("s", "SPONGE", 1, -1, (-20, -1, 1, -1, 1, -1))
     assert p.resolved_extent((201, 201, 1)) == (182, 201, 1, 201, 1, 1)
+
+
+@pytest.mark.parametrize("compiler,std", [("gcc", "-std=c99"), ("g++", "-std=c++11")])
+def test_header_is_strict_c_and_cxx(tmp_path, compiler, std):
+    """A host that binds the library compiles the header as plain C99 or C++11,
+    warnings as errors."""
+    ext = "c" if compiler == "gcc" else "cpp"
+    src = tmp_path / f"use.{ext}"
+    src.write_text(f'#include "{HEADER}"\nint main(void) {{ mgd_ctx* c = 0; (void)c; return 0; }}\n')
+    subprocess.check_call([compiler, std, "-pedantic", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", str(src)])
