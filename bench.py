@@ -5,8 +5,11 @@ FP64 viscous Navier-Stokes with SBP 4-8 derivatives and dissipation,
 far-field SATs, 20-point sponges, a Gaussian cost target and control
 mollifier; 960 RK4 steps forward (dt = 0.05) with a snapshot every 10 steps,
 then the discrete adjoint over the same horizon with uniform checkpointing
-(forward recomputed on the device between snapshots) -- one complete
-forward + adjoint gradient evaluation.
+(each 10-step segment's forward states recomputed on the device from its
+snapshot, beside the adjoint) -- one complete forward + adjoint gradient
+evaluation. The same gradient with the whole trajectory kept resident on the
+device (no recomputation) is timed after it and reported as a secondary
+figure (`resident_trajectory`).
 
 Metric: FP64 Mpt-RHS/s = grid points x (forward + adjoint RHS evaluations)
 / seconds / 1e6 (the forward recomputation of checkpointing is not counted).
@@ -15,10 +18,12 @@ initial state already in HBM; `e2e` is the same metric through the C ABI
 with the initial state uploaded from pinned host memory and the gradient
 vector, J and Grad0 read back each step.
 
---impl reference times the CPU restatement of the reference (oracle/) on the
-host cores (the Fortran reference cannot be built: it needs an MPI Fortran
-toolchain and CMake-generated headers) on a bounded sample of the same
-workload (fewer RK steps of the same grid), scaled to the same metric.
+The CPU baseline and --impl reference run the CPU restatement of the
+reference (oracle/; the Fortran reference cannot be built: it needs an MPI
+Fortran toolchain and CMake-generated headers) on the host cores over the
+complete workload: every timed step is the whole 960-step forward + adjoint
+gradient. The bench line's `parity` compares the GPU's J, Grad0 and gradient
+vector with that CPU run.
 """
 import argparse
 import json
@@ -45,7 +50,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-sample-steps", type=int, default=400)
+    ap.add_argument("--cpu-warmup-rk-steps", type=int, default=20,
+                    help="RK4 steps of each warm-up sample of the CPU legs (--impl reference)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--rk-steps", type=int, default=N_STEPS,
                     help="RK4 steps per gradient evaluation (profiling runs use a few)")
@@ -72,10 +78,19 @@ def parse():
     ap.add_argument("--grad-lanes", type=int, default=0, help="with --tiles: 2D gradient/flux threads per point")
     ap.add_argument("--core-lanes", type=int, default=0, help="with --tiles: 2D adjoint core threads per point")
     ap.add_argument("--checkpoint-only", action="store_true",
-                    help="recompute checkpoint segments in the adjoint instead of keeping the trajectory on the device")
+                    help="msgrad and tangent workloads: recompute checkpoint segments instead of keeping the "
+                         "trajectory on the device")
+    ap.add_argument("--resident", action="store_true",
+                    help="gradient workload: time the resident trajectory (no recomputation) as the primary figure; "
+                         "by default the checkpoint recomputation is primary and the resident trajectory secondary")
     ap.add_argument("--profile-only", action="store_true",
                     help="run the gradient evaluations and exit (for ncu captures; prints no bench line)")
     return ap.parse_args()
+
+
+def progress(msg):
+    """One line on stderr per phase, so that a run that stops part way shows where."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
 
 
 def rank_info():
@@ -87,21 +102,52 @@ def problem(n_steps=N_STEPS):
     return configs.monopole_2d(n=GRID, n_steps=n_steps, save_interval=SAVE_INTERVAL)
 
 
-def cpu_sample(sample_steps, threads=None):
-    """Times the oracle on the full grid for `sample_steps` RK steps forward +
-    adjoint; returns (Mpt-RHS/s, seconds, cores)."""
+CPU_LEGS = {
+    "strict": "oracle/oracle.cpp built -O3 -fno-fast-math -ffp-contract=off -fopenmp (the parity checker)",
+    "tuned": "oracle/oracle.cpp built with the reference's release flags -O3 -ffast-math -funroll-loops -fopenmp",
+}
+
+
+def cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
+def cpu_gradient(variant="strict", steps=N_STEPS, threads=None, want_vector=False):
+    """Runs the CPU oracle over `steps` RK4 steps forward + adjoint of the
+    201x201 monopole (the full workload at steps = 960) on all host cores;
+    returns seconds, Mpt-RHS/s, J, Grad0 and (optionally) the gradient vector."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
     cores = threads or os.cpu_count()
-    oracle_lib.set_threads(cores)
-    P = problem()
-    o = oracle_lib.Oracle(P)
+    oracle_lib.set_threads(cores, variant)
+    P = problem(steps)
+    o = oracle_lib.Oracle(P, variant=variant)
     t = time.perf_counter()
-    o.run_forward(sample_steps)
-    o.run_adjoint()
+    J = o.run_forward(steps, SAVE_INTERVAL)
+    G = o.run_adjoint()
     dt = time.perf_counter() - t
-    pts = P.blocks[0].n_points
-    return pts * 8 * sample_steps / dt / 1e6, dt, cores
+    out = {"seconds": dt, "value": P.blocks[0].n_points * 8 * steps / dt / 1e6, "J": J, "grad0": G,
+           "cores": cores, "variant": variant}
+    if want_vector:
+        out["gradient"] = o.gradient(4 * steps)
+    del o
+    return out
+
+
+def parity_of(J, G, grad, ref):
+    """Relative differences of the GPU's J, Grad0 and gradient vector from the
+    strict oracle's complete run of the same workload."""
+    import numpy as np
+    return {"J_rel": abs(J - ref["J"]) / abs(ref["J"]), "grad0_rel": abs(G - ref["grad0"]) / abs(ref["grad0"]),
+            "gradient_vector_rel": float(np.linalg.norm(grad - ref["gradient"]) / np.linalg.norm(ref["gradient"])),
+            "tolerance": 1e-10, "against": "strict CPU oracle, complete 960-step forward + adjoint run"}
 
 
 class ClockSampler:
@@ -148,21 +194,26 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def fp64_peak_tflops(torch):
-    """Measured FP64 rate of this GPU: cuBLAS DGEMM 4096^3, best of 3."""
-    n = 4096
+def fp64_peak(torch, clocks):
+    """FP64 roof of this GPU: a cuBLAS DGEMM 6144^3 (best of 8 after a
+    warm-up), and beside it the nominal rate of the SMs' FP64 pipes (4 flops
+    per clock per SM: 2 DFMA lane-operations) at the sampled maximum clock."""
+    n = 6144
     a = torch.randn(n, n, dtype=torch.float64, device="cuda")
     b = torch.randn(n, n, dtype=torch.float64, device="cuda")
     torch.matmul(a, b)
     best = 1e30
-    for _ in range(3):
+    for _ in range(8):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         torch.matmul(a, b)
         e1.record()
         torch.cuda.synchronize()
         best = min(best, e0.elapsed_time(e1) / 1e3)
-    return 2.0 * n ** 3 / best / 1e12
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = (clocks or {}).get("sm_max_mhz") or 2070.0
+    return {"peak_tflops": 2.0 * n ** 3 / best / 1e12, "source": "measured: cuBLAS DGEMM 6144^3, best of 8",
+            "nominal_tflops": sms * 4 * mhz * 1e6 / 1e12}
 
 
 def measured_peaks():
@@ -211,28 +262,42 @@ ADJOINT_KERNELS = ["adjoint_core", "adjoint_dissipation", "adjoint_diffusion", "
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference on all host
+    cores, every timed step the complete workload (960 RK4 steps forward +
+    adjoint of the 201x201 monopole). The warm-up steps run a short sample of
+    each CPU build (the CPU code has nothing to warm but caches and pages)
+    and pick the faster build for the timed steps."""
     rank, world, _ = rank_info()
     if rank != 0:
         return
-    per_step = []
-    mpts = None
-    for i in range(args.warmup + args.steps):
-        v, dt, cores = cpu_sample(args.cpu_sample_steps)
-        if i >= args.warmup:
-            per_step.append(v)
-            mpts = v
-    value = statistics.mean(per_step)
+    sample = max(1, args.cpu_warmup_rk_steps)
+    warm = {}
+    for v in ("strict", "tuned"):
+        for _ in range(max(1, args.warmup)):
+            warm[v] = cpu_gradient(v, sample)["seconds"]
+    variant = min(warm, key=warm.get)
+    per_step, runs = [], []
+    n_steps = args.rk_steps
+    for _ in range(args.steps):
+        r = cpu_gradient(variant, n_steps)
+        runs.append(r)
+        per_step.append(r["seconds"])
+    sec = statistics.mean(per_step)
     pts = GRID * GRID
-    ms = pts * 8 * N_STEPS / (value * 1e6) * 1e3
+    value = pts * 8 * n_steps / sec / 1e6
+    cores = runs[-1]["cores"]
+    desc = (f"{CPU_LEGS[variant]}, OpenMP on {cores} threads of {cpu_model()}; every timed step the complete "
+            f"{n_steps}-step forward + adjoint gradient; warm-up steps: {sample}-step samples of both builds "
+            f"({', '.join(f'{k} {warm[k]:.2f} s' for k in warm)}), the faster build timed")
     line = {
         "impl": "reference", "metric": "FP64 Mpt-RHS/s", "value": value, "unit": "Mpt-RHS/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "grid": "201x201", "rk4_steps": N_STEPS, "save_interval": SAVE_INTERVAL,
-                   "sample": f"{args.cpu_sample_steps} RK4 steps forward + adjoint per timed step, scaled to 960"},
-        "cpu_baseline": {"value": value, "unit": "Mpt-RHS/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": f"oracle (C++ restatement, OpenMP) on the 201x201 grid, {args.cpu_sample_steps} "
-                                   f"RK4 steps forward + adjoint"},
+        "config": {"workload": WORKLOAD, "grid": "201x201", "rk4_steps": n_steps, "save_interval": SAVE_INTERVAL,
+                   "sample": "the complete workload in every timed step"},
+        "adjoint_gradient_s": sec, "J": runs[-1]["J"], "grad0": runs[-1]["grad0"],
+        "cpu_baseline": {"value": value, "unit": "Mpt-RHS/s", "cores": cores, "kind": "port", "build": variant,
+                         "cpu": cpu_model(), "sample": desc},
         "e2e": {"value": value, "unit": "Mpt-RHS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -256,9 +321,12 @@ def run_ours(args):
     pts = blk.n_points
     nU = P.n_unknowns
     s = Solver(P)
-    # the 960-step trajectory (4 x 960 stage slots, about 22 GB) stays on the
-    # device: the adjoint reads it instead of recomputing checkpoint segments
-    s.set_trajectory_storage(not args.checkpoint_only)
+    # the workload as configured: snapshots every 10 steps, each segment's
+    # forward states recomputed on the device beside the adjoint (--resident
+    # times the resident trajectory instead; the other mode is measured after
+    # the timed steps as a secondary figure)
+    resident = bool(args.resident)
+    s.set_trajectory_storage(resident)
     stream = torch.cuda.ExternalStream(s.stream_handle())
     n_entries = 4 * n_steps
     Pact = s.actuator_points()
@@ -278,7 +346,23 @@ def run_ours(args):
         G = s.run_adjoint()
         return J, G
 
+    def timed_gradients(k):
+        times, J, G = [], None, None
+        for _ in range(k):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            if world > 1:
+                torch.distributed.barrier()
+            e0.record(stream)
+            J, G = gradient_step(q0_dev.data_ptr())
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        return times, J, G
+
     # run-level tile tuning on short gradient runs (setup, outside the timed region)
+    progress("tile tuning")
     set_q(q0_dev.data_ptr())
     t_tune = time.perf_counter()
     if args.tiles:
@@ -319,22 +403,12 @@ def run_ours(args):
         print(json.dumps({"profile_only": True, "rk_steps": n_steps, "J": J, "grad0": G}), flush=True)
         return
     s.kernel_launches(reset=True)
+    progress("timed gradients")
     clocks = ClockSampler()
     clocks.start()
-    times = []
-    J = G = None
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        if world > 1:
-            torch.distributed.barrier()
-        e0.record(stream)
-        J, G = gradient_step(q0_dev.data_ptr())
-        e1.record(stream)
-        torch.cuda.synchronize()
-        times.append(e0.elapsed_time(e1))
+    times, J, G = timed_gradients(args.steps)
     launches = s.kernel_launches(reset=True) // args.steps
+    grad_vec = s.gradient(n_entries)
     # end to end through the C ABI with host buffers
     e2e_times = []
     for _ in range(args.steps):
@@ -346,6 +420,14 @@ def run_ours(args):
         torch.cuda.synchronize()
         e2e_times.append((time.perf_counter() - t) * 1e3)
     clk = clocks.stop()
+    # secondary figure: the same gradient in the other storage mode (same tiles)
+    progress("secondary storage mode")
+    s.set_trajectory_storage(not resident)
+    gradient_step(q0_dev.data_ptr())
+    torch.cuda.synchronize()
+    alt_times, J_alt, G_alt = timed_gradients(args.steps)
+    alt_ms = statistics.mean(alt_times)
+    s.set_trajectory_storage(resident)
     ms = statistics.mean(times)
     if world > 1:
         t = torch.tensor([ms], device="cuda")
@@ -356,6 +438,7 @@ def run_ours(args):
     e2e_ms = statistics.mean(e2e_times)
     e2e = world * pts * rhs_evals / (e2e_ms / 1e3) / 1e6
     # per-kernel timing for the roofline (separate short loops on the same stream)
+    progress("per-kernel timing and FP64 peak")
     fwd = s.profile_stage_kernels(capi.FORWARD, 30)
     adj = s.profile_stage_kernels(capi.ADJOINT, 30)
     kern = dict(zip(FORWARD_KERNELS, fwd))
@@ -363,7 +446,7 @@ def run_ours(args):
     # launches per gradient evaluation: forward stage kernels run in the forward
     # pass (and again in the checkpoint recomputation unless the trajectory is
     # resident), the functional only in the forward pass, adjoint kernels once
-    per_grad = {k: (8 if args.checkpoint_only else 4) * n_steps for k in FORWARD_KERNELS}
+    per_grad = {k: (4 if resident else 8) * n_steps for k in FORWARD_KERNELS}
     per_grad["forward_functional"] = 4 * n_steps
     per_grad.update({k: 4 * n_steps for k in ADJOINT_KERNELS})
     share = {k: kern[k] * per_grad[k] for k in kern}
@@ -373,7 +456,11 @@ def run_ours(args):
     t_launch = kern[dominant] / 1e3
     achieved_gbs = units["bytes"] * pts / t_launch / 1e9
     achieved_tf = units["flops"] * pts / t_launch / 1e12
-    fp64_peak = fp64_peak_tflops(torch)
+    fp64 = fp64_peak(torch, clk)
+    mode_text = {False: "checkpoints every %d steps, each segment's forward states recomputed on the device beside "
+                        "the adjoint (UniformCheckpointer)" % SAVE_INTERVAL,
+                 True: "resident trajectory: every stage's state, primitives, stress and heat flux kept on the device "
+                       "by the forward run, no recomputation"}
     line = {
         "metric": "FP64 Mpt-RHS/s", "value": value, "unit": "Mpt-RHS/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -383,30 +470,34 @@ def run_ours(args):
                    "l2": "512 MB buffer written between timed steps (working set fits in L2)",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "tile_tuning": tuning,
-                   "adjoint_forward_states": ("checkpoints every %d steps, segments recomputed beside the adjoint"
-                                              % SAVE_INTERVAL) if args.checkpoint_only else
-                                             "resident trajectory: every stage's state, primitives, stress and "
-                                             "heat flux kept on the device by the forward run"},
+                   "adjoint_forward_states": mode_text[resident]},
         "adjoint_gradient_s": ms / 1e3,
         "J": J, "grad0": G,
         "e2e": {"value": e2e, "unit": "Mpt-RHS/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": pts * nU * 8, "d2h_bytes_per_step": n_entries * Pact * 8 + 16},
         "gpu_launches": launches,
         "clocks": clk,
+        ("checkpoint_recompute" if resident else "resident_trajectory"): {
+            "value": world * pts * rhs_evals / (alt_ms / 1e3) / 1e6, "unit": "Mpt-RHS/s", "ms_per_step": alt_ms,
+            "steps": args.steps, "adjoint_forward_states": mode_text[not resident],
+            "J_rel_diff": abs(J_alt - J) / abs(J), "grad0_rel_diff": abs(G_alt - G) / abs(G)},
         "kernels_ms_per_launch": kern,
         "kernel_time_share": {k: share[k] / sum(share.values()) for k in share},
-        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved_gbs,
-                     "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
-                     "traffic": MEASURED_TRAFFIC.get(dominant), "peak_source": peak_kind,
-                     "fp64": {"achieved_tflops": achieved_tf, "peak_tflops": fp64_peak,
-                              "frac": achieved_tf / fp64_peak, "peak_source": "measured: cuBLAS DGEMM 4096^3"},
-                     "note": "FP64 path with no tensor-core work: the binding roof is the FP64 pipe (fp64.frac); "
-                             "the 201x201 working set stays in L2, so the HBM fraction is not the bound"},
+        "roofline": {"bound": "fp64", "kernel": dominant, "achieved": achieved_tf, "peak": fp64["peak_tflops"],
+                     "unit": "TFLOP/s", "frac": achieved_tf / fp64["peak_tflops"],
+                     "traffic": MEASURED_TRAFFIC.get(dominant), "peak_source": fp64["source"],
+                     "peak_nominal_tflops": fp64["nominal_tflops"], "flops_per_point": units["flops"],
+                     "hbm": {"achieved_gbs": achieved_gbs, "peak_gbs": peaks["hbm_gbs"],
+                             "frac": achieved_gbs / peaks["hbm_gbs"], "bytes_per_point": units["bytes"],
+                             "peak_source": peak_kind},
+                     "note": "FP64 path with no tensor-core work: the binding roof is the FP64 pipe; the 201x201 "
+                             "working set stays in L2, so the HBM fraction is not the bound"},
     }
     if rank == 0 and world == 1:
         # the same gradient through the per-call entry points (the reference's own
         # control flow over the computeRhs seam), timed once beside the graph path
         from magudi_gb300.drivers import per_call_gradient
+        progress("per-call gradient")
         t_start = time.perf_counter()
         Jp, Gp = per_call_gradient(s, P, n_steps, SAVE_INTERVAL)
         tp = time.perf_counter() - t_start
@@ -417,10 +508,22 @@ def run_ours(args):
             "path": "mgd_rk4_substep + functional/sensitivity calls per stage, checkpoints and segment "
                     "stage states in host memory (Solver%runForward / runAdjoint with UniformCheckpointer)"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, dt, cores = cpu_sample(args.cpu_sample_steps)
-        line["cpu_baseline"] = {"value": v, "unit": "Mpt-RHS/s", "cores": cores, "kind": "port",
-                                "sample": f"oracle (C++ restatement of the reference, OpenMP) on the 201x201 grid, "
-                                          f"{args.cpu_sample_steps} RK4 steps forward + adjoint ({dt:.1f} s)"}
+        # the complete workload on the host cores: the strict build is the
+        # parity reference of this run, the faster build the CPU baseline
+        progress("CPU oracle, strict build")
+        legs = {"strict": cpu_gradient("strict", n_steps, want_vector=True)}
+        progress("CPU oracle, tuned build")
+        legs["tuned"] = cpu_gradient("tuned", n_steps)
+        line["parity"] = parity_of(J, G, grad_vec, legs["strict"])
+        fast = min(legs, key=lambda k: legs[k]["seconds"])
+        line["cpu_baseline"] = {
+            "value": legs[fast]["value"], "unit": "Mpt-RHS/s", "cores": legs[fast]["cores"], "kind": "port",
+            "build": fast, "cpu": cpu_model(),
+            "sample": f"the complete workload ({n_steps} RK4 steps forward + adjoint, 201x201) on the host cores "
+                      f"with {CPU_LEGS[fast]}: {legs[fast]['seconds']:.1f} s",
+            "legs": {k: {"value": v["value"], "seconds": v["seconds"], "flags": CPU_LEGS[k],
+                         "J_rel_vs_strict": abs(v["J"] - legs["strict"]["J"]) / abs(legs["strict"]["J"])}
+                     for k, v in legs.items()}}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -85,7 +85,30 @@ typedef struct {
   double time_step_size;
   double cfl;
   int functional_type;               /* MGD_FUNCTIONAL_*: which cost functional J is */
+  /* Solution limits (enable_solution_limits, minimum_density,
+   * maximum_density, minimum_temperature, maximum_temperature;
+   * src/SimulationFlagsImpl.f90:34, src/SolverOptionsImpl.f90:73-78): with
+   * the flag set, a forward run checks the density and the temperature of
+   * every grid point at the start of every RK stage, as
+   * checkSolutionLimits (src/SolverImpl.f90:189-304) does, and stops at the
+   * first stage whose state lies outside the open ranges (non-finite values
+   * count as outside); see MGD_SOLUTION_LIMITS. */
+  int enable_solution_limits;
+  double minimum_density;
+  double maximum_density;
+  double minimum_temperature;
+  double maximum_temperature;
 } mgd_options;
+
+/* Status of mgd_run_forward / mgd_run_adjoint when the solution left the
+ * limits (not a failure of the call): the run stopped as Solver%runForward
+ * does on a checkSolutionLimits violation (src/SolverImpl.f90:813-818,
+ * 1193-1198) and its cost (or sensitivity) is HUGE (DBL_MAX). The
+ * conserved variables are left at the violating state (the state the
+ * reference saves as "<prefix>-crashed.q"), and mgd_last_error names the
+ * quantity, block, grid point, value, step and stage. An mgd_run_adjoint
+ * after such a run returns the same status with a HUGE sensitivity. */
+#define MGD_SOLUTION_LIMITS 2
 
 /* Cost functionals. SOUND is the reference's acoustic-noise functional
  * (functional_type = "SOUND", src/AcousticNoiseImpl.f90), integrated in time
@@ -252,6 +275,14 @@ int mgd_get_step_sizes(mgd_ctx* ctx, double* host, int n_steps);
  * *sensitivity = the time-integrated cost sensitivity (Grad0). */
 int mgd_run_adjoint(mgd_ctx* ctx, double* sensitivity);
 
+/* checkSolutionLimits (src/SolverImpl.f90:189-304) for hosts that drive the
+ * per-call entry points: *within = 1 when the density and the temperature of
+ * every grid point of every block lie strictly inside the ranges set in
+ * the options struct (the primitive variables must be current: see mgd_update_state),
+ * else 0 with the reference's message in mgd_last_error. Needs
+ * enable_solution_limits. */
+int mgd_check_solution_limits(mgd_ctx* ctx, int* within);
+
 /* Solver%runLinearized (src/SolverImpl.f90:1300-1450) over the steps of the
  * last mgd_run_forward: the perturbation held in MGD_FIELD_ADJOINT (the
  * linearized initial condition) advances with substepLinearizedRK4 along the
@@ -393,7 +424,16 @@ int mgd_selftest_pow(const double* x, int n, double e, double* fast, double* ref
  * rejected with an error. The first call on a device looks up that array's
  * device address, so make it before any stream capture. Calls share the
  * array: calls that overlap on the GPU (from different contexts or host
- * threads) race and must be serialised by the caller. */
+ * threads) race and must be serialised by the caller. Like mgd_compute_rhs
+ * it adds the actuators' forcing set by mgd_set_patch_control_forcing when
+ * the controller is on, and it refuses regions of several blocks and blocks
+ * with block-interface patches. Ordering: the kernels run on the context's
+ * own stream, which does not wait for the caller's streams, so q must be
+ * complete on the device when the call is made (synchronise the stream that
+ * wrote it); rhs is complete when the call returns. The call also uses the
+ * context's launch counters and per-call step counters, so it must not
+ * overlap any other call on the same context; it leaves the context's
+ * state, run checkpoints and gradient untouched. */
 int mgd_forward_rhs_noalloc(mgd_ctx* ctx, const double* q, double time, double* rhs);
 
 /* CUDA stream the context launches on (cudaStream_t as void*). */

@@ -57,6 +57,9 @@ FIELD_PRESSURE = 10
 FIELD_TEMPERATURE = 11
 FIELD_ARC_LENGTHS = 12
 
+# status of a run that stopped at a solution-limit violation (cost = HUGE)
+SOLUTION_LIMITS = 2
+
 
 class Options(C.Structure):
     _fields_ = [
@@ -79,6 +82,11 @@ class Options(C.Structure):
         ("time_step_size", C.c_double),
         ("cfl", C.c_double),
         ("functional_type", C.c_int),
+        ("enable_solution_limits", C.c_int),
+        ("minimum_density", C.c_double),
+        ("maximum_density", C.c_double),
+        ("minimum_temperature", C.c_double),
+        ("maximum_temperature", C.c_double),
     ]
 
 

@@ -13,6 +13,7 @@
 #include <tuple>
 #include <cmath>
 #include <cstdio>
+#include <limits>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -145,6 +146,8 @@ int mgd_create(const mgd_options* o, mgd_ctx** out) {
   cudaMemset(c.dApiAmp, 0, MGD_MAX_SOURCES * sizeof(double));
   cudaMalloc((void**)&c.dApiTime, sizeof(double));
   cudaMemset(c.dApiTime, 0, sizeof(double));
+  cudaMalloc((void**)&c.dLimitKey, sizeof(unsigned long long));
+  cudaMemset(c.dLimitKey, 0xFF, sizeof(unsigned long long));
   if (cudaGetLastError() != cudaSuccess) {
     g_createError = "device allocation failed";
     delete h;
@@ -168,6 +171,7 @@ int mgd_destroy(mgd_ctx* h) {
     cudaFree(b.runStage);
     cudaFree(b.runPartials);
   }
+  cudaFree(c.dLimitKey);
   cudaFree(c.dCounters); cudaFree(c.dApiAmp); cudaFree(c.dAmp); cudaFree(c.dForcing);
   cudaFree(c.dApiTime); cudaFree(c.dStageTime); cudaFree(c.dDeltaForcing); cudaFree(c.dApiForcing);
   cudaFree(c.dGradient); cudaFree(c.dPartials); cudaFree(c.dStageValues);
@@ -1528,6 +1532,12 @@ void regionAdjointStage(Context& c, int rkStage, const RunScalars& rs, double ap
 
 static bool singleBlock(const Context& c) { return c.blocks.size() == 1 && !c.hasInterfaces; }
 
+namespace mgd {
+bool perCallController(const Context& c) { return apiController(c); }
+const double* perCallForcing(const Context& c) { return c.apiForcingSet ? c.dApiForcing : nullptr; }
+bool singleBlockRegion(const Context& c) { return singleBlock(c); }
+}  // namespace mgd
+
 int mgd_update_state(mgd_ctx* h) {
   Context& c = h->c;
   if (requireReady(c)) return 1;
@@ -1537,6 +1547,21 @@ int mgd_update_state(mgd_ctx* h) {
   }
   if (checkLaunch(c)) return 1;
   CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  return 0;
+}
+
+int mgd_check_solution_limits(mgd_ctx* h, int* within) {
+  Context& c = h->c;
+  if (requireReady(c)) return 1;
+  if (!within) return fail(c, "mgd_check_solution_limits: within must not be null");
+  if (!c.opts.enable_solution_limits) return fail(c, "mgd_check_solution_limits: enable_solution_limits is off");
+  CUDA_TRY(c, cudaMemsetAsync(c.dLimitKey, 0xFF, sizeof(unsigned long long), c.stream));
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) launchSolutionLimits(c, c.blocks[bi], (int)bi, nullptr, 1, c.dLimitKey);
+  if (checkLaunch(c)) return 1;
+  double v = 0.0;
+  const int st = limitOutcome(c, &v, true);
+  if (st != 0 && st != MGD_SOLUTION_LIMITS) return st;
+  *within = st == 0;
   return 0;
 }
 
@@ -1943,6 +1968,9 @@ int prepareForwardRun(Context& c, int n_steps, int save_interval, double t0, boo
   c.runSteps = n_steps;
   c.saveInterval = save_interval;
   c.runT0 = t0;
+  c.limitViolated = false;
+  if (c.opts.enable_solution_limits)
+    CUDA_TRY(c, cudaMemsetAsync(c.dLimitKey, 0xFF, sizeof(unsigned long long), c.stream));
   if (ensureStepBuffers(c, b, n_steps)) return 1;
   const int nSrc = (int)c.sources.size();
   const long long nAmp = (long long)4 * n_steps * std::max(1, nSrc);
@@ -2048,6 +2076,41 @@ int finishForwardRun(Context& c, double* cost) {
 
 RunScalars runScalarsOf(Context& c) { return runScalars(c); }
 
+// After a forward run with solution limits (or a per-call check): decodes the
+// first violation, if any, into the reference's message
+// (src/SolverImpl.f90:231-280), sets *value = HUGE and returns
+// MGD_SOLUTION_LIMITS; 0 when the state stayed inside the limits.
+int limitOutcome(Context& c, double* value, bool perCall) {
+  if (!c.opts.enable_solution_limits) return 0;
+  unsigned long long key = kNoLimitViolation;
+  CUDA_TRY(c, cudaMemcpyAsync(&key, c.dLimitKey, sizeof key, cudaMemcpyDeviceToHost, c.stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c.stream));
+  if (key == kNoLimitViolation) return 0;
+  const long long ordinal = (long long)(key >> 36);
+  const int bi = (int)((key >> 33) & 7), quantity = (int)((key >> 32) & 1);
+  const long long p = (long long)(key & 0xffffffffULL);
+  DevBlock& b = c.blocks[bi];
+  const long long N = b.v.N;
+  double v = 0.0;
+  const double* src = quantity == 0 ? b.v.q + p : b.v.prim + p + N * (2 + c.nD);
+  CUDA_TRY(c, cudaMemcpy(&v, src, sizeof v, cudaMemcpyDeviceToHost));
+  const long long i = p % b.v.gs[0] + 1, j = (p / b.v.gs[0]) % b.v.gs[1] + 1, k = p / ((long long)b.v.gs[0] * b.v.gs[1]) + 1;
+  const double lo = quantity == 0 ? c.opts.minimum_density : c.opts.minimum_temperature;
+  const double hi = quantity == 0 ? c.opts.maximum_density : c.opts.maximum_temperature;
+  char msg[320];
+  std::snprintf(msg, sizeof msg, "%s on grid %d at (%lld, %lld, %lld): %.2E out of range (%.2E, %.2E)!",
+                quantity == 0 ? "Density" : "Temperature", bi + 1, i, j, k, v, lo, hi);
+  std::string text = msg;
+  if (!perCall) {
+    std::snprintf(msg, sizeof msg, " (forward step %lld, stage %lld)", ordinal / 4 + 1, ordinal % 4 + 1);
+    text += msg;
+  }
+  c.limitMessage = text;
+  c.error = text;
+  *value = std::numeric_limits<double>::max();
+  return MGD_SOLUTION_LIMITS;
+}
+
 }  // namespace mgd
 
 // ---------------------------------------------------------------------------
@@ -2148,12 +2211,22 @@ static int regionRunForward(Context& c, int n_steps, int save_interval, double t
   const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
   const bool functional = c.opts.enable_functional != 0;
   std::vector<RunScalars> rs;
-  for (size_t bi = 0; bi < c.blocks.size(); ++bi) rs.push_back(blockRunScalars(c, c.blocks[bi], bi == 0));
+  const bool limits = c.opts.enable_solution_limits != 0;
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+    rs.push_back(blockRunScalars(c, c.blocks[bi], bi == 0));
+    if (limits) rs.back().limitKey = c.dLimitKey;
+  }
   if (setCounters(c, 1, 0)) return 1;
   if (capture(c, &c.gForward, &c.nodesForward, [&]() {
         // constant CFL: the step size from every block's state at the start of the step
         if (cflMode) launchTimeStepRegion(c, c.dDtPartials, c.dStepDt, c.dCounters, c.dTime, c.dStageTime, c.dAmp);
-        for (int i = 1; i <= 4; ++i) regionRunStage(c, rs, i, controller, false, functional);
+        for (int i = 1; i <= 4; ++i) {
+          // checkSolutionLimits over every block before every substep
+          if (limits)
+            for (size_t bi = 0; bi < c.blocks.size(); ++bi)
+              launchSolutionLimits(c, c.blocks[bi], (int)bi, c.dCounters, i, c.dLimitKey);
+          regionRunStage(c, rs, i, controller, false, functional);
+        }
         for (DevBlock& b : c.blocks) launchSnapshot(c, b, b.runSnap, save_interval, false);
         launchStepAdvance(c, 1);
       }))
@@ -2177,6 +2250,10 @@ static int regionRunForward(Context& c, int n_steps, int save_interval, double t
       for (int i = 0; i < 4; ++i) J = J + kRkNorm[i] * c.stepDt[s] * vals[(size_t)4 * s + i];
   }
   *cost = J;
+  if (const int st = limitOutcome(c, cost, false)) {
+    c.limitViolated = st == MGD_SOLUTION_LIMITS;
+    return st;
+  }
   return 0;
 }
 
@@ -2296,10 +2373,16 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
   bool resident = false;
   if (c.trajectoryStorage && ensureTrajectoryBuffer(c, b, n_steps, &resident)) return 1;
   RunScalars rs = runScalars(c);
+  const bool limits = c.opts.enable_solution_limits != 0;
+  if (limits) rs.limitKey = c.dLimitKey;
   if (setCounters(c, 1, 0)) return 1;
   if (capture(c, &c.gForward, &c.nodesForward, [&]() {
         if (cflMode) launchTimeStep(c, b, c.dDtPartials, c.dStepDt, c.dCounters, c.dTime, c.dStageTime, c.dAmp);
-        for (int i = 1; i <= 4; ++i) forwardStage(c, b, i, rs, false, controller, resident, functional);
+        for (int i = 1; i <= 4; ++i) {
+          // checkSolutionLimits before every substep (src/SolverImpl.f90:812-818)
+          if (limits) launchSolutionLimits(c, b, 0, c.dCounters, i, c.dLimitKey);
+          forwardStage(c, b, i, rs, false, controller, resident, functional);
+        }
         launchSnapshot(c, b, c.dSnapshots, save_interval, false);
         launchStepAdvance(c, 1);
       }))
@@ -2309,13 +2392,28 @@ int mgd_run_forward(mgd_ctx* h, int n_steps, int save_interval, double t0, doubl
   if (checkLaunch(c)) return 1;
   if (finishForwardRun(c, cost)) return 1;
   c.trajectorySteps = resident ? n_steps : 0;
+  if (const int st = limitOutcome(c, cost, false)) {
+    c.limitViolated = st == MGD_SOLUTION_LIMITS;
+    c.trajectorySteps = 0;
+    return st;
+  }
   return 0;
+}
+
+// The adjoint of a forward run that stopped at a solution-limit violation
+// stops too (src/SolverImpl.f90:1193-1198): HUGE and the same status.
+static int limitStop(Context& c, double* value) {
+  if (!c.limitViolated) return 0;
+  *value = std::numeric_limits<double>::max();
+  c.error = c.limitMessage;
+  return MGD_SOLUTION_LIMITS;
 }
 
 int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   Context& c = h->c;
   if (requireReady(c)) return 1;
   if (c.runSteps < 1) return fail(c, "mgd_run_adjoint needs a preceding mgd_run_forward");
+  if (const int st = limitStop(c, sensitivity)) return st;
   if (!singleBlock(c)) return regionRunAdjoint(c, sensitivity);
   DevBlock& b = c.blocks[0];
   const long long N = b.v.N;
@@ -2448,6 +2546,7 @@ int mgd_run_linearized(mgd_ctx* h, const double* delta_forcing, long long n_entr
   Context& c = h->c;
   if (requireReady(c)) return 1;
   if (c.runSteps < 1) return fail(c, "mgd_run_linearized needs a preceding mgd_run_forward");
+  if (const int st = limitStop(c, delta_cost)) return st;
   if (!singleBlock(c)) return regionRunLinearized(c, delta_forcing, n_entries, delta_cost);
   if (refuseLinearized(c)) return 1;
   DevBlock& b = c.blocks[0];

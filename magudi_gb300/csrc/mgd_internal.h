@@ -161,7 +161,23 @@ struct RunScalars {
   const double* rk;        // per step (indexed by step - 1): dt, dt/6, dt/3, dt/2; or null
   int adjointForcingSwitch;
   const double* stageTime; // time of each forward stage, (step-1)*4 + stage-1
+  // solution limits of a forward run (null when off): the key of the first
+  // violation, all ones while there is none; the RK update kernels leave the
+  // state unchanged once it is set, so the run ends on the violating state
+  const unsigned long long* limitKey;
 };
+
+// Open ranges of checkSolutionLimits (src/SolverImpl.f90:189-304).
+struct SolutionLimits {
+  double rhoMin, rhoMax, TMin, TMax;
+};
+// Key of a solution-limit violation: the earliest forward stage first, then
+// the block, density before temperature, the lowest grid point.
+__host__ __device__ inline unsigned long long limitKeyOf(long long ordinal, int block, int quantity, long long p) {
+  return ((unsigned long long)ordinal << 36) | ((unsigned long long)block << 33) |
+         ((unsigned long long)quantity << 32) | (unsigned long long)p;
+}
+constexpr unsigned long long kNoLimitViolation = ~0ULL;
 
 // RK4 coefficients of the current step of a run (or of the per-call step).
 struct RkCoeffs {
@@ -308,6 +324,11 @@ struct Context {
   long long dtPartialCapacity = 0;
   double* dTime = nullptr;
   double* dNorm = nullptr;          // H det per point (terminal functional)
+  // solution limits: device key of the first violation of the current run,
+  // and whether the last forward run stopped at one
+  unsigned long long* dLimitKey = nullptr;
+  bool limitViolated = false;
+  std::string limitMessage;
   cudaGraphExec_t gForward = nullptr, gRecomputeH[2] = {}, gAdjointH[2] = {};
   // asynchronous solution files: pinned staging, copy stream, writer thread
   cudaStream_t ioStream = nullptr;
@@ -345,6 +366,18 @@ void forwardStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bo
 void adjointStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage, double apiFactor, bool api,
                   bool fromSlot, bool record, const Lanes* lanes = nullptr);
 
+// The per-call forward RHS adds the actuators' forcing (perCallController)
+// from perCallForcing (null until the caller set a forcing); both as
+// mgd_compute_rhs uses them. singleBlockRegion: one block and no
+// block-interface patch.
+bool perCallController(const Context& c);
+const double* perCallForcing(const Context& c);
+bool singleBlockRegion(const Context& c);
+// Reads the solution-limit key of the last check: MGD_SOLUTION_LIMITS with
+// *value = HUGE and the reference's message in c.error after a violation
+// (perCall: no step and stage in the message), 0 otherwise.
+int limitOutcome(Context& c, double* value, bool perCall);
+
 int prepareForwardRun(Context& c, int n_steps, int save_interval, double t0, bool snapshots);
 int finishForwardRun(Context& c, double* cost);
 RunScalars runScalarsOf(Context& c);
@@ -362,6 +395,11 @@ void launchPrims(Context& c, DevBlock& b, const double* qSrc, bool copyToQ, cons
 // Gradients, stress, heat flux and contravariant fluxes (flags GF_*).
 void launchGradFlux(Context& c, DevBlock& b, bool writeFlux, bool writeStress, const RunScalars* rs, int stage,
                     bool storeStage, cudaStream_t s = 0);
+// checkSolutionLimits of block b's current state (q and its primitives) at
+// the start of RK stage `stage` of the step *step (ordinal 0 when step is
+// null): atomically lowers *key to the key of the first violating point.
+void launchSolutionLimits(Context& c, DevBlock& b, int blockIndex, const int* step, int stage,
+                          unsigned long long* key, cudaStream_t s = 0);
 // Artificial dissipation of src (q forward, lambda adjoint) into b.v.dq,
 // scaled by sign (+1 forward, -1 adjoint).
 void launchDissipation(Context& c, DevBlock& b, const double* src, double sign, cudaStream_t s = 0);

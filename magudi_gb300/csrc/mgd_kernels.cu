@@ -602,6 +602,8 @@ template <int ND>
 __device__ __forceinline__ void forwardDivergencePoint(const BlockView& B, const Physics& P, const RunScalars& rs,
                                                        int rkStage, int stage, int controller, const Tile& T,
                                                        int blk, int lin = 0, double linFactor = 0.0) {
+  // after a solution-limit violation in this run the state stays as it is
+  if (rkStage > 0 && rs.limitKey && *rs.limitKey != kNoLimitViolation) return;
   long long p;
   PointIndex I;
   if (!locate(B, T, blk, p, I)) return;
@@ -686,6 +688,24 @@ __global__ void __launch_bounds__(kMaxTile) kForwardDivergence(BlockView B, Phys
                                                                double linFactor) {
   pdlEnter();
   forwardDivergencePoint<ND>(B, P, rs, rkStage, stage, controller, T, blockIdx.x, lin, linFactor);
+}
+
+// checkSolutionLimits (src/SolverImpl.f90:189-304) on one point: density and
+// temperature strictly inside their ranges; a comparison with NaN fails, so
+// non-finite values are violations too. The first violation by key wins.
+template <int ND>
+__global__ void __launch_bounds__(kBlock) kSolutionLimits(BlockView B, SolutionLimits L, const int* step, int stage,
+                                                          int blockIndex, unsigned long long* key) {
+  pdlEnter();
+  const long long p = (long long)blockIdx.x * kBlock + threadIdx.x;
+  if (p >= B.N) return;
+  const double rho = B.q[p];
+  const double T = B.prim[p + B.N * (2 + ND)];
+  const int quantity = !(rho > L.rhoMin && rho < L.rhoMax) ? 0 : !(T > L.TMin && T < L.TMax) ? 1 : 2;
+  if (quantity < 2) {
+    const long long ordinal = step ? (long long)(*step - 1) * 4 + (stage - 1) : 0;
+    atomicMin(key, limitKeyOf(ordinal, blockIndex, quantity, p));
+  }
 }
 
 // Functional (AcousticNoise%compute, src/AcousticNoiseImpl.f90:123-206) of the
@@ -2188,6 +2208,17 @@ void launchBatchPrims(Context& c, const BatchLaunch& L, cudaStream_t s) {
 void launchBatchFunctional(Context& c, const BatchLaunch& L, int stage, cudaStream_t s) {
   MGD_LAUNCH(c);
   pdl(kFunctionalBatch, L.blocks[BK_FUNC], kBlock, s, L.entries, L.map[BK_FUNC], stage, PrimLayout{c.nD}.p());
+}
+
+void launchSolutionLimits(Context& c, DevBlock& b, int blockIndex, const int* step, int stage,
+                          unsigned long long* key, cudaStream_t s) {
+  const SolutionLimits L{c.opts.minimum_density, c.opts.maximum_density, c.opts.minimum_temperature,
+                         c.opts.maximum_temperature};
+  if (c.nD == 2)
+    pdl(kSolutionLimits<2>, gridFor(b.v.N), kBlock, on(c, s), b.v, L, step, stage, blockIndex, key);
+  else
+    pdl(kSolutionLimits<3>, gridFor(b.v.N), kBlock, on(c, s), b.v, L, step, stage, blockIndex, key);
+  MGD_LAUNCH(c);
 }
 
 void launchStepAdvanceOn(int* counters, int delta, cudaStream_t s) { pdl(kStepAdvance, 1, 32, s, counters, delta); }

@@ -7,11 +7,14 @@
 // loops that cannot afford cudaMalloc's implicit device synchronisation.
 // mgd_forward_rhs_noalloc reads the caller's state and writes the caller's
 // RHS buffer; every intermediate it needs (primitive variables,
-// contravariant fluxes, the dissipation term, the far-field viscous traces,
-// the source amplitudes) lives in one fixed array in device memory that is
-// part of the library image.
+// contravariant fluxes, the dissipation term, the SAT vectors of the
+// boundary entries, the solenoidal-excitation values, the source amplitudes
+// and the stage time) lives in one fixed array in device memory that is part
+// of the library image, so the context's own state and run buffers stay as
+// they were.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -63,21 +66,28 @@ int mgd_forward_rhs_noalloc(mgd_ctx* h, const double* q, double time, double* rh
     c.error = "mgd_forward_rhs_noalloc: q and rhs must be device pointers";
     return 1;
   }
-  if (c.blocks.size() != 1) {
-    c.error = "mgd_forward_rhs_noalloc: one block per context";
+  if (!singleBlockRegion(c)) {
+    // regions of several blocks, or one block with block-interface patches
+    // (an O-grid cut), need the interface SATs of mgd_compute_rhs
+    c.error = "mgd_forward_rhs_noalloc: one block without block-interface patches per context; "
+              "use mgd_compute_rhs for multi-block regions and interface patches";
     return 1;
   }
   DevBlock& b = c.blocks[0];
   const long long N = b.v.N;
   const int nD = c.nD, nU = c.nU;
   const PrimLayout L{nD};
-  // scratch layout: [amplitudes | primitives | fluxes | dissipation | far-field traces]
-  const long long nAmp = align32(MGD_MAX_SOURCES);
+  // scratch layout: [amplitudes, time | primitives | fluxes | dissipation |
+  //                  SAT vectors | solenoidal-excitation values]
+  long long nExcEntries = 0;
+  for (const ExcPatch& x : b.exc) nExcEntries = std::max(nExcEntries, (long long)x.off + x.nE);
+  const long long nAmp = align32(MGD_MAX_SOURCES + 1);
   const long long nPrim = align32(N * L.count());
   const long long nFlux = align32(N * nD * nU);
   const long long nDiss = align32(c.phys.composite ? N * nU : N * nD * nU);
   const long long nFF = align32((long long)b.v.ff.n * nU);
-  const long long need = nAmp + nPrim + nFlux + nDiss + nFF;
+  const long long nExc = align32(3 * nExcEntries);
+  const long long need = nAmp + nPrim + nFlux + nDiss + nFF + nExc;
   if (need > kNoAllocScratchDoubles) {
     c.error = "mgd_forward_rhs_noalloc: the block needs " + std::to_string(need) +
               " doubles of scratch but the fixed array holds " + std::to_string(kNoAllocScratchDoubles) +
@@ -123,6 +133,7 @@ int mgd_forward_rhs_noalloc(mgd_ctx* h, const double* q, double time, double* rh
   view.fhat = view.prim + nPrim;
   view.dq = view.fhat + nFlux;
   view.ff.visc = view.dq + nDiss;
+  if (nExcEntries) view.excF = view.ff.visc + nFF;
   RunScalars rs{};
   rs.step = c.dCounters + 2;
   rs.segBase = c.dCounters + 3;
@@ -131,10 +142,16 @@ int mgd_forward_rhs_noalloc(mgd_ctx* h, const double* q, double time, double* rh
   setStepSize(rs, c.opts.time_step_size);
   rs.adjointForcingSwitch = c.opts.adjoint_forcing_switch;
   rs.nPartialBlocks = reductionBlocks(b);
+  // the actuators' forcing of the per-call path, as mgd_compute_rhs adds it
+  // (ActuatorPatch%updateRhs, src/ActuatorPatchImpl.f90:108-181)
+  rs.apiForcing = perCallForcing(c);
+  // The launchers read the block through b.v, so the view stands in for it
+  // during this call. Calls on one context do not overlap (one calling
+  // thread per context), so no other call sees the substitution.
   const BlockView saved = b.v;
   b.v = view;
   launchPrims(c, b, view.q, false);
-  forwardStage(c, b, 0, rs, true, false, false, false);
+  forwardStage(c, b, 0, rs, true, perCallController(c), false, false);
   b.v = saved;
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);

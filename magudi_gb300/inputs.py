@@ -134,6 +134,13 @@ def options_from_inputs(d, n_dimensions):
         if "dissipation_amount" not in d:
             raise InputError("Required parameter 'dissipation_amount' not specified!")
         o.dissipation_amount = d.get_float("dissipation_amount", 0.0)
+    # src/SimulationFlagsImpl.f90:34 and src/SolverOptionsImpl.f90:73-78
+    o.enable_solution_limits = d.get_bool("enable_solution_limits", False)
+    if o.enable_solution_limits:
+        for key in ("minimum_density", "maximum_density", "minimum_temperature", "maximum_temperature"):
+            if key not in d:
+                raise InputError(f"Required parameter '{key}' not specified!")
+            setattr(o, key, d.get_float(key, 0.0))
     if o.use_constant_cfl:
         o.cfl = d.get_float("cfl", 0.5)
     else:

@@ -41,6 +41,12 @@ class Options:
     time_step_size: float = 0.0
     cfl: float = 0.5
     functional_type: int = 0  # capi.FUNCTIONAL_SOUND or FUNCTIONAL_TERMINAL_KINETIC_ENERGY
+    # enable_solution_limits and its required ranges (src/SolverOptionsImpl.f90:73-78)
+    enable_solution_limits: bool = False
+    minimum_density: float = 0.0
+    maximum_density: float = 0.0
+    minimum_temperature: float = 0.0
+    maximum_temperature: float = 0.0
 
     def to_c(self) -> capi.Options:
         o = capi.Options()

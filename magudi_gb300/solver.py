@@ -91,6 +91,7 @@ def load_library(build_if_missing=True):
     L.mgd_tune_run.argtypes = [ctx, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
     L.mgd_stage_tile.restype = C.c_int
     L.mgd_stage_tile.argtypes = [ctx, C.c_int, C.POINTER(C.c_int), C.c_int]
+    L.mgd_check_solution_limits.argtypes = [ctx, C.POINTER(C.c_int)]
     _lib = L
     return L
 
@@ -132,9 +133,22 @@ class Solver:
         if finalize:
             self._check(self.L.mgd_finalize_setup(self.h))
 
+    # the message of the last run that stopped at a solution-limit violation
+    limit_violation = None
+
     def _check(self, rc):
         if rc:
             raise MagudiError(self.L.mgd_last_error(self.h).decode())
+
+    def _run_status(self, rc):
+        """Runs return HUGE (not an exception) when the solution left the
+        limits, as Solver%runForward / runAdjoint do; the message is kept in
+        limit_violation."""
+        if rc == capi.SOLUTION_LIMITS:
+            self.limit_violation = self.L.mgd_last_error(self.h).decode()
+            return
+        self.limit_violation = None
+        self._check(rc)
 
     def close(self):
         if getattr(self, "h", None):
@@ -197,13 +211,21 @@ class Solver:
 
     def run_forward(self, n_steps, save_interval=10, t0=0.0):
         v = C.c_double()
-        self._check(self.L.mgd_run_forward(self.h, n_steps, save_interval, t0, C.byref(v)))
+        self._run_status(self.L.mgd_run_forward(self.h, n_steps, save_interval, t0, C.byref(v)))
         return v.value
 
     def run_adjoint(self):
         v = C.c_double()
-        self._check(self.L.mgd_run_adjoint(self.h, C.byref(v)))
+        self._run_status(self.L.mgd_run_adjoint(self.h, C.byref(v)))
         return v.value
+
+    def check_solution_limits(self):
+        """checkSolutionLimits of the current state: True when inside the
+        limits, else False with the message in limit_violation."""
+        w = C.c_int()
+        self._check(self.L.mgd_check_solution_limits(self.h, C.byref(w)))
+        self.limit_violation = None if w.value else self.L.mgd_last_error(self.h).decode()
+        return bool(w.value)
 
     def run_linearized(self, delta_forcing=None):
         """Tangent run over the steps of the last run_forward: the perturbation

@@ -36,7 +36,7 @@
 
 namespace orc {
 
-enum { SYMMETRIC = 0, SKEW_SYMMETRIC = 1 };
+enum { SYMMETRIC = 0, SKEW_SYMMETRIC = 1, ASYMMETRIC = 2 };
 
 // t_StencilOperator (include/StencilOperator.f90:12-29). rhsBoundary1(k,m):
 // k = column inside the boundary window, m = output row; stored column-major
@@ -44,7 +44,8 @@ enum { SYMMETRIC = 0, SKEW_SYMMETRIC = 1 };
 struct StencilOp {
   int symmetryType = SYMMETRIC;
   int interiorWidth = 0, boundaryWidth = 0, boundaryDepth = 0;
-  std::vector<double> interior;  // rhsInterior(-w/2 : w/2)
+  std::vector<double> interior;  // rhsInterior(lo : lo + interiorWidth - 1)
+  int lo = 0;                    // lower bound of rhsInterior: -w/2, or set by an ASYMMETRIC operator
   std::vector<double> rb1, rb2;  // rhsBoundary1/2(boundaryWidth, boundaryDepth)
   std::vector<double> normBoundary;
   int nGhost[2] = {0, 0};
@@ -53,12 +54,13 @@ struct StencilOp {
 
   void allocate() {  // allocateData, src/StencilOperatorImpl.f90:15-33
     interior.assign(interiorWidth, 0.0);
+    lo = -(interiorWidth / 2);
     rb1.assign(boundaryWidth * boundaryDepth, 0.0);
     rb2.assign(boundaryWidth * boundaryDepth, 0.0);
     normBoundary.assign(boundaryDepth, 1.0);
   }
-  double& in(int j) { return interior[j + interiorWidth / 2]; }
-  double in(int j) const { return interior[j + interiorWidth / 2]; }
+  double& in(int j) { return interior[j - lo]; }
+  double in(int j) const { return interior[j - lo]; }
   double& b1(int k, int m) { return rb1[(k - 1) + boundaryWidth * (m - 1)]; }
   double b1(int k, int m) const { return rb1[(k - 1) + boundaryWidth * (m - 1)]; }
   double& b2(int k, int m) { return rb2[(k - 1) + boundaryWidth * (m - 1)]; }
@@ -313,11 +315,15 @@ void apply(const StencilOp& op, double* x, int ncomp, const int gs[3], int dir) 
   const long long N = (long long)gs[0] * gs[1] * gs[2];
   const int n = (int)L.n, h = op.interiorWidth / 2;
   const int g0 = op.nGhost[0], g1 = op.nGhost[1];
-  for (int c = 0; c < ncomp; ++c) {
-    double* xc = x + N * c;
-#pragma omp parallel for schedule(static)
-    for (long long line = 0; line < L.nLines; ++line) {
-      std::vector<double> xg(n + g0 + g1);
+  // one parallel loop over every (component, line) pair; each thread keeps
+  // its ghosted copy of a line for all the lines it handles
+#pragma omp parallel
+  {
+    std::vector<double> xg(n + g0 + g1);
+#pragma omp for schedule(static)
+    for (long long cl = 0; cl < (long long)ncomp * L.nLines; ++cl) {
+      const long long line = cl % L.nLines;
+      double* xc = x + N * (cl / L.nLines);
       const long long b = L.base(line);
       for (int i = 0; i < n; ++i) xg[g0 + i] = xc[b + i * L.stride];
       // fillGhostPoints for a single process, src/MPIHelperImpl.f90:113-390.
@@ -332,6 +338,10 @@ void apply(const StencilOp& op, double* x, int ncomp, const int gs[3], int dir) 
         if (op.symmetryType == SKEW_SYMMETRIC) {
           s = op.in(1) * (p[1] - p[-1]);
           for (int j = 2; j <= h; ++j) s += op.in(j) * (p[j] - p[-j]);
+        } else if (op.symmetryType == ASYMMETRIC) {
+          // sum(rhsInterior * x(i + lbound : i + ubound)), left to right
+          s = op.in(op.lo) * p[op.lo];
+          for (int j = op.lo + 1; j < op.lo + op.interiorWidth; ++j) s += op.in(j) * p[j];
         } else {
           s = op.in(1) * (p[1] + p[-1]);
           for (int j = 2; j <= h; ++j) s += op.in(j) * (p[j] + p[-j]);
@@ -693,6 +703,7 @@ struct Region {
   std::vector<double> stageTimes;
   std::vector<double> stepDt;  // time step of each forward step
   double finalTime = 0.0;
+  bool limitViolated = false;  // the last forward run stopped at a solution-limit violation
 };
 
 static long long patchGridIndex(const Block& b, long long i, long long j, long long k) {
@@ -1266,14 +1277,17 @@ static void addDissipation(Region& R, Block& b, int mode) {
   for (int i = 0; i < nD; ++i) {
     // LINEARIZED dissipates the perturbation held in adjointVariables
     const std::vector<double>& src = mode == MGD_FORWARD ? b.conservedVariables : b.adjointVariables;
-    std::copy(src.begin(), src.end(), d.begin());
+#pragma omp parallel for schedule(static)
+    for (long long k = 0; k < N * nU; ++k) d[k] = src[k];
     apply(b.dissipation[i], d.data(), nU, b.gs, i);
     if (!R.o.composite_dissipation) {
+#pragma omp parallel for collapse(2) schedule(static)
       for (int j = 0; j < nU; ++j)
         for (long long p = 0; p < N; ++p) d[N * j + p] = -b.arcLengths[N * i + p] * d[N * j + p];
       apply(b.dissipationTranspose[i], d.data(), nU, b.gs, i);
       applyNorm(b.firstDerivative[i], d.data(), nU, b.gs, i, true);
     }
+#pragma omp parallel for schedule(static)
     for (long long k = 0; k < N * nU; ++k) b.rightHandSide[k] = b.rightHandSide[k] + amount * d[k];
   }
 }
@@ -1286,6 +1300,7 @@ static void computeRhsForward(Region& R, Block& b, int bi) {
   std::fill(b.rightHandSide.begin(), b.rightHandSide.end(), 0.0);
   cartesianFluxes(R, b, b.conservedVariables.data(), f1.data(), R.o.viscous ? f2.data() : nullptr);
   if (R.o.viscous)
+#pragma omp parallel for schedule(static)
     for (long long k = 0; k < N * nU * nD; ++k) f1[k] = f1[k] - f2[k];
   if (R.o.viscous)
     for (Patch& p : R.patches) {
@@ -1320,6 +1335,7 @@ static void computeRhsForward(Region& R, Block& b, int bi) {
         f2[N * (c + nU * i) + p] = s;
       }
   for (int i = 0; i < nD; ++i) apply(b.firstDerivative[i], &f2[N * nU * i], nU, b.gs, i);
+#pragma omp parallel for collapse(2) schedule(static)
   for (int c = 0; c < nU; ++c)
     for (long long p = 0; p < N; ++p) {
       double s = f2[N * c + p];
@@ -1361,6 +1377,7 @@ static void addFarFieldAdjointPenalty(Region& R, Block& b, int bi) {
     });
   }
   for (int i = 0; i < nD; ++i) apply(b.adjointFirstDerivative[i], &temp1[N * (nU - 1) * i], nU - 1, b.gs, i);
+#pragma omp parallel for collapse(2) schedule(static)
   for (int c = 0; c < nU - 1; ++c)
     for (long long q = 0; q < N; ++q) {
       double s = temp1[N * c + q];
@@ -1368,6 +1385,7 @@ static void addFarFieldAdjointPenalty(Region& R, Block& b, int bi) {
       temp2[N * c + q] = s;
     }
   const double g = R.o.ratio_of_specific_heats;
+#pragma omp parallel for schedule(static)
   for (long long q = 0; q < N; ++q) {
     const double v = b.specificVolume[q];
     temp2[N * nD + q] = g * v * temp2[N * nD + q];
@@ -1426,6 +1444,7 @@ static void addInterfaceAdjointPenalty(Region& R, Block& b, int bi) {
     });
   }
   for (int i = 0; i < nD; ++i) apply(b.adjointFirstDerivative[i], &temp1[N * (nU - 1) * i], nU - 1, b.gs, i);
+#pragma omp parallel for collapse(2) schedule(static)
   for (int c = 0; c < nU - 1; ++c)
     for (long long q = 0; q < N; ++q) {
       double s = temp1[N * c + q];
@@ -1433,6 +1452,7 @@ static void addInterfaceAdjointPenalty(Region& R, Block& b, int bi) {
       temp2[N * c + q] = s;
     }
   const double g = R.o.ratio_of_specific_heats;
+#pragma omp parallel for schedule(static)
   for (long long q = 0; q < N; ++q) {
     const double v = b.specificVolume[q];
     temp2[N * nD + q] = g * v * temp2[N * nD + q];
@@ -1452,7 +1472,8 @@ static void computeRhsAdjoint(Region& R, Block& b, int bi) {
   std::vector<double> temp1(N * nU * nD);
   std::fill(b.rightHandSide.begin(), b.rightHandSide.end(), 0.0);
   for (int i = 0; i < nD; ++i) {
-    std::copy(b.adjointVariables.begin(), b.adjointVariables.end(), temp1.begin() + N * nU * i);
+#pragma omp parallel for schedule(static)
+    for (long long k = 0; k < N * nU; ++k) temp1[N * nU * i + k] = b.adjointVariables[k];
     apply(b.adjointFirstDerivative[i], &temp1[N * nU * i], nU, b.gs, i);
   }
 #pragma omp parallel for schedule(static)
@@ -1503,12 +1524,14 @@ static void computeRhsAdjoint(Region& R, Block& b, int bi) {
         for (int r = 0; r < nU - 1; ++r) temp1[N * (r + 1 + nU * jj) + k] = ad[r + (nU - 1) * jj];
     }
     for (int jj = 0; jj < nD; ++jj) apply(b.adjointFirstDerivative[jj], &temp1[N * (1 + nU * jj)], nU - 1, b.gs, jj);
+#pragma omp parallel for collapse(2) schedule(static)
     for (int c = 0; c < nU - 1; ++c)
       for (long long k = 0; k < N; ++k) {
         double s = temp1[N * (c + 1) + k];
         for (int jj = 1; jj < nD; ++jj) s += temp1[N * (c + 1 + nU * jj) + k];
         temp2[N * c + k] = s;
       }
+#pragma omp parallel for schedule(static)
     for (long long k = 0; k < N; ++k) {
       const double v = b.specificVolume[k];
       temp2[N * nD + k] = g * v * temp2[N * nD + k];
@@ -2008,6 +2031,7 @@ static void computeRhs(Region& R, int mode, double time, double adjointForcingFa
   if (mode == MGD_ADJOINT && R.o.viscous)
     for (size_t bi = 0; bi < R.blocks.size(); ++bi) addInterfaceAdjointPenalty(R, R.blocks[bi], (int)bi);
   for (Block& b : R.blocks)
+#pragma omp parallel for collapse(2) schedule(static)
     for (int j = 0; j < R.nU; ++j)
       for (long long p = 0; p < b.N; ++p) b.rightHandSide[b.N * j + p] = b.rightHandSide[b.N * j + p] * b.jacobian[p];
   for (Patch& p : R.patches) patchUpdateRhs(R, p, R.blocks[p.d.grid_index - 1], mode, adjointForcingFactor, time);
@@ -2018,6 +2042,7 @@ static void computeRhs(Region& R, int mode, double time, double adjointForcingFa
       const double w = 2.0 * pi * s.frequency, gf = 9.0 / (2.0 * s.radius * s.radius);
       const double a = s.amplitude * std::cos(w * time + s.phase);
       for (Block& b : R.blocks)
+#pragma omp parallel for schedule(static)
         for (long long p = 0; p < b.N; ++p) {
           if (b.iblank[p] == 0) continue;
           double r = 0.0;
@@ -2029,6 +2054,7 @@ static void computeRhs(Region& R, int mode, double time, double adjointForcingFa
         }
     }
   for (Block& b : R.blocks)
+#pragma omp parallel for collapse(2) schedule(static)
     for (int j = 0; j < R.nU; ++j)
       for (long long p = 0; p < b.N; ++p)
         if (b.iblank[p] == 0) b.rightHandSide[b.N * j + p] = 0.0;
@@ -2140,6 +2166,7 @@ static void substep(Region& R, int mode, double& time, double dt, int stage, boo
     computeRhs(R, MGD_FORWARD, time, 1.0);
     for (Block& b : R.blocks) {
       const long long n = b.N * R.nU;
+#pragma omp parallel for schedule(static)
       for (long long k = 0; k < n; ++k) {
         const double r = b.rightHandSide[k];
         switch (stage) {
@@ -2162,6 +2189,7 @@ static void substep(Region& R, int mode, double& time, double dt, int stage, boo
     computeRhs(R, MGD_LINEARIZED, time, 1.0);
     for (Block& b : R.blocks) {
       const long long n = b.N * R.nU;
+#pragma omp parallel for schedule(static)
       for (long long k = 0; k < n; ++k) {
         const double r = b.rightHandSide[k];
         switch (stage) {
@@ -2184,6 +2212,7 @@ static void substep(Region& R, int mode, double& time, double dt, int stage, boo
     computeRhs(R, MGD_ADJOINT, ts, factor);
     for (Block& b : R.blocks) {
       const long long n = b.N * R.nU;
+#pragma omp parallel for schedule(static)
       for (long long k = 0; k < n; ++k) {
         const double r = b.rightHandSide[k];
         switch (stage) {
@@ -2293,9 +2322,26 @@ static double computeTimeStepSize(Region& R) {
 // Solver%runForward, src/SolverImpl.f90:672-912 (functional on, constant dt).
 // Stage inputs are kept in memory for the adjoint run; that matches
 // UniformCheckpointer's recomputation exactly because the forward is deterministic.
+// checkSolutionLimits, src/SolverImpl.f90:189-304 (hard limits), with
+// isVariableWithinRange, src/GridImpl.f90:1579-1622: block by block, the
+// density and then the temperature of every grid point must lie strictly
+// inside (minimum, maximum). A non-finite value also counts as outside (the
+// reference's minimum search skips NaN; here a NaN stops the run).
+static bool solutionWithinLimits(const Region& R) {
+  auto inside = [](double f, double lo, double hi) { return f > lo && f < hi; };
+  for (const Block& b : R.blocks) {
+    for (long long p = 0; p < b.N; ++p)
+      if (!inside(b.conservedVariables[p], R.o.minimum_density, R.o.maximum_density)) return false;
+    for (long long p = 0; p < b.N; ++p)
+      if (!inside(b.temperature[p], R.o.minimum_temperature, R.o.maximum_temperature)) return false;
+  }
+  return true;
+}
+
 static double runForward(Region& R, int nSteps, double t0, bool keepStages) {
   R.nSteps = nSteps;
   R.t0 = t0;
+  R.limitViolated = false;
   double time = t0, J = 0.0;
   updateAll(R);
   R.stageStates.clear();
@@ -2306,6 +2352,12 @@ static double runForward(Region& R, int nSteps, double t0, bool keepStages) {
     const double dt = computeTimeStepSize(R);
     R.stepDt.push_back(dt);
     for (int i = 1; i <= 4; ++i) {
+      // src/SolverImpl.f90:812-818: costFunctional = HUGE and return
+      if (R.o.enable_solution_limits && !solutionWithinLimits(R)) {
+        R.limitViolated = true;
+        R.finalTime = time;
+        return std::numeric_limits<double>::max();
+      }
       if (keepStages) {
         std::vector<double> all;
         for (Block& b : R.blocks) all.insert(all.end(), b.conservedVariables.begin(), b.conservedVariables.end());
@@ -2694,15 +2746,17 @@ int orc_actuator_patch_size(void* h, long long* n) {
   return 0;
 }
 
+// Status 2 (MGD_SOLUTION_LIMITS): the run stopped at a solution-limit
+// violation with *cost = HUGE, the state left at the violating stage input.
 int orc_run_forward(void* h, int nSteps, int saveInterval, double t0, double* cost) {
   (void)saveInterval;
   *cost = orc::runForward(*(Region*)h, nSteps, t0, true);
-  return 0;
+  return ((Region*)h)->limitViolated ? MGD_SOLUTION_LIMITS : 0;
 }
 
 int orc_run_forward_nostore(void* h, int nSteps, double t0, double* cost) {
   *cost = orc::runForward(*(Region*)h, nSteps, t0, false);
-  return 0;
+  return ((Region*)h)->limitViolated ? MGD_SOLUTION_LIMITS : 0;
 }
 
 int orc_time_step_size(void* h, double* dt) {
@@ -2716,7 +2770,13 @@ int orc_step_sizes(void* h, double* out) {
   return (int)R.stepDt.size();
 }
 
+// After a forward run that stopped at a solution-limit violation the adjoint
+// stops at the same state (src/SolverImpl.f90:1193-1198): sensitivity HUGE.
 int orc_run_adjoint(void* h, double* s) {
+  if (((Region*)h)->limitViolated) {
+    *s = std::numeric_limits<double>::max();
+    return MGD_SOLUTION_LIMITS;
+  }
   *s = orc::runAdjoint(*(Region*)h);
   return 0;
 }

@@ -8,7 +8,9 @@ import sys
 
 import numpy as np
 
-root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_plot3d_golden.py <path to the magudi source tree>")
+root = sys.argv[1]
 sys.path.insert(0, os.path.join(root, "utils", "magudi_utils", "src"))
 import magudi_utils.plot3dnasa as p3d  # noqa: E402
 

@@ -50,4 +50,6 @@ def main(magudi_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_sbp_golden.py <path to the magudi source tree>")
+    main(sys.argv[1])

@@ -13,20 +13,25 @@ from magudi_gb300 import capi
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+# The same source built with the reference's release flags (-O3 -ffast-math
+# -funroll-loops): the timed CPU leg of the bench, never the parity checker.
+TUNED_LIB_PATH = os.path.join(ROOT, "oracle", "_build", "liboracle_tuned.so")
 
-_lib = None
+_libs = {}
 
 
 def build():
     subprocess.check_call(["bash", os.path.join(ROOT, "oracle", "build.sh")])
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB_PATH):
+def lib(variant="strict"):
+    """The oracle library: "strict" (IEEE arithmetic, the checker) or
+    "tuned" (fast-math release build, for CPU timing)."""
+    if variant not in _libs:
+        path = LIB_PATH if variant == "strict" else TUNED_LIB_PATH
+        if not os.path.exists(path):
             build()
-        L = C.CDLL(LIB_PATH)
+        L = C.CDLL(path)
         L.orc_create.restype = C.c_void_p
         L.orc_create.argtypes = [C.POINTER(capi.Options)]
         L.orc_destroy.argtypes = [C.c_void_p]
@@ -60,12 +65,12 @@ def lib():
         L.orc_apply_operator.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.c_int,
                                          C.POINTER(C.c_int), C.c_int]
         L.orc_set_threads.argtypes = [C.c_int]
-        _lib = L
-    return _lib
+        _libs[variant] = L
+    return _libs[variant]
 
 
-def set_threads(n):
-    return lib().orc_set_threads(n)
+def set_threads(n, variant="strict"):
+    return lib(variant).orc_set_threads(n)
 
 
 def operator(which):
@@ -94,8 +99,8 @@ def apply_operator(which, x, grid_size, direction, periodicity=0):
 class Oracle:
     """One oracle region built from a magudi_gb300.problem.Problem."""
 
-    def __init__(self, problem, finalize=True):
-        L = lib()
+    def __init__(self, problem, finalize=True, variant="strict"):
+        L = lib(variant)
         self.L = L
         self.problem = problem
         self._opts = problem.options.to_c()
@@ -186,17 +191,21 @@ class Oracle:
         n = a.size // max(1, self.actuator_points())
         self.L.orc_set_control_forcing(self.h, capi.dptr(a), n)
 
+    # status of the last run: capi.SOLUTION_LIMITS when it stopped at a
+    # solution-limit violation (value HUGE), else 0
+    run_status = 0
+
     def run_forward(self, n_steps, save_interval=10, t0=0.0, keep_stages=True):
         v = C.c_double()
         if keep_stages:
-            self.L.orc_run_forward(self.h, n_steps, save_interval, t0, C.byref(v))
+            self.run_status = self.L.orc_run_forward(self.h, n_steps, save_interval, t0, C.byref(v))
         else:
-            self.L.orc_run_forward_nostore(self.h, n_steps, t0, C.byref(v))
+            self.run_status = self.L.orc_run_forward_nostore(self.h, n_steps, t0, C.byref(v))
         return v.value
 
     def run_adjoint(self):
         v = C.c_double()
-        self.L.orc_run_adjoint(self.h, C.byref(v))
+        self.run_status = self.L.orc_run_adjoint(self.h, C.byref(v))
         return v.value
 
     def set_patch_control_forcing(self, forcing):

@@ -21,12 +21,13 @@ def _run(*args, timeout=300):
 
 def test_command_line_takes_the_contract_options():
     out = _run("--help", timeout=120)
-    for opt in ("--gpus", "--steps", "--warmup", "--impl", "--workload", "--checkpoint-only", "--tiles"):
+    for opt in ("--gpus", "--steps", "--warmup", "--impl", "--workload", "--resident", "--tiles"):
         assert opt in out
 
 
 def test_reference_arm_prints_one_contract_line():
-    out = _run("--impl", "reference", "--steps", "1", "--warmup", "0", "--cpu-sample-steps", "2")
+    # a 4-step gradient instead of the 960-step one keeps the CPU suite short
+    out = _run("--impl", "reference", "--steps", "1", "--warmup", "1", "--rk-steps", "4", "--cpu-warmup-rk-steps", "2")
     lines = [l for l in out.splitlines() if l.strip().startswith("{")]
     assert len(lines) == 1
     d = json.loads(lines[0])
@@ -36,4 +37,6 @@ def test_reference_arm_prints_one_contract_line():
     assert d["impl"] == "reference" and d["metric"] == "FP64 Mpt-RHS/s" and d["value"] > 0.0
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["build"] in ("strict", "tuned")
+    assert d["config"]["rk4_steps"] == 4 and abs(d["ms_per_step"] / 1e3 - d["adjoint_gradient_s"]) < 1e-9
     assert "workload" in d["config"]
