@@ -98,6 +98,7 @@ typedef struct {
   double maximum_density;
   double minimum_temperature;
   double maximum_temperature;
+  int discretization_scheme;         /* MGD_SBP_*: defaults/discretization_scheme */
 } mgd_options;
 
 /* Status of mgd_run_forward / mgd_run_adjoint when the solution left the
@@ -109,6 +110,16 @@ typedef struct {
  * quantity, block, grid point, value, step and stage. An mgd_run_adjoint
  * after such a run returns the same status with a HUGE sensitivity. */
 #define MGD_SOLUTION_LIMITS 2
+
+/* defaults/discretization_scheme (src/StencilOperatorImpl.f90:1164-1960):
+ * the SBP first derivative with its composite and non-composite artificial
+ * dissipation. SBP 1-2 has no non-composite dissipation. */
+enum {
+  MGD_SBP_48 = 0, /* "SBP 4-8" */
+  MGD_SBP_12 = 1, /* "SBP 1-2" */
+  MGD_SBP_24 = 2, /* "SBP 2-4" */
+  MGD_SBP_36 = 3  /* "SBP 3-6" */
+};
 
 /* Cost functionals. SOUND is the reference's acoustic-noise functional
  * (functional_type = "SOUND", src/AcousticNoiseImpl.f90), integrated in time

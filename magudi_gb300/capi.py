@@ -57,6 +57,13 @@ FIELD_PRESSURE = 10
 FIELD_TEMPERATURE = 11
 FIELD_ARC_LENGTHS = 12
 
+# defaults/discretization_scheme
+SBP_48 = 0
+SBP_12 = 1
+SBP_24 = 2
+SBP_36 = 3
+SBP_SCHEMES = {"SBP 4-8": SBP_48, "SBP 1-2": SBP_12, "SBP 2-4": SBP_24, "SBP 3-6": SBP_36}
+
 # status of a run that stopped at a solution-limit violation (cost = HUGE)
 SOLUTION_LIMITS = 2
 
@@ -87,6 +94,7 @@ class Options(C.Structure):
         ("maximum_density", C.c_double),
         ("minimum_temperature", C.c_double),
         ("maximum_temperature", C.c_double),
+        ("discretization_scheme", C.c_int),
     ]
 
 

@@ -85,6 +85,14 @@ int mgd_create(const mgd_options* o, mgd_ctx** out) {
     g_createError = "n_dimensions must be 2 or 3";
     return 1;
   }
+  if (o->discretization_scheme < MGD_SBP_48 || o->discretization_scheme > MGD_SBP_36) {
+    g_createError = "discretization_scheme must be one of MGD_SBP_48, MGD_SBP_12, MGD_SBP_24, MGD_SBP_36";
+    return 1;
+  }
+  if (o->discretization_scheme == MGD_SBP_12 && o->dissipation && !o->composite_dissipation) {
+    g_createError = "SBP 1-2 has no non-composite dissipation operator";
+    return 1;
+  }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     g_createError = "no CUDA device available";
@@ -362,7 +370,8 @@ static int computeMetrics(Context& c, DevBlock& b) {
       return fail(c, msg);
     }
   // norm = H (per non-periodic direction) * det, jacobian = 1/det
-  const HostOp d1 = makeFirstDerivative48();
+  const HostOp d1 = schemeOps(c.opts.discretization_scheme).d1;
+  const int nn = (int)d1.norm.size();
   std::vector<double> norm(N, 1.0), jac(N), arcA((size_t)N * nD);
   for (int d = 0; d < nD; ++d) {
     if (b.desc.periodicity_type[d] != MGD_PERIODIC_NONE) continue;
@@ -370,8 +379,8 @@ static int computeMetrics(Context& c, DevBlock& b) {
     const long long st = b.v.ax[d].stride;
     for (long long p = 0; p < N; ++p) {
       const int i = (int)((p / st) % n);
-      if (i < 8) norm[p] = d1.norm[i] * norm[p];
-      else if (i >= n - 8) norm[p] = d1.norm[n - 1 - i] * norm[p];
+      if (i < nn) norm[p] = d1.norm[i] * norm[p];
+      else if (i >= n - nn) norm[p] = d1.norm[n - 1 - i] * norm[p];
     }
   }
   for (long long p = 0; p < N; ++p) {
@@ -402,12 +411,14 @@ int mgd_add_block(mgd_ctx* h, const mgd_block_desc* desc, const double* coordina
   for (int i = 0; i < 3; ++i) v.gs[i] = i < c.nD ? desc->grid_size[i] : 1;
   for (int i = 0; i < c.nD; ++i)
     if (v.gs[i] < 2 * 12 + 1 && desc->periodicity_type[i] == MGD_PERIODIC_NONE)
-      return fail(c, "each non-periodic direction needs at least 25 points for the SBP 4-8 closures");
+      return fail(c, "each non-periodic direction needs at least 25 points (the closure windows of the kernels' "
+                     "operator tables)");
   v.N = (long long)v.gs[0] * v.gs[1] * v.gs[2];
   for (int i = 0; i < 3; ++i) {
     v.ax[i].n = v.gs[i];
     v.ax[i].per = i < c.nD ? desc->periodicity_type[i] : MGD_PERIODIC_NONE;
     v.ax[i].stride = i == 0 ? 1 : (i == 1 ? v.gs[0] : (long long)v.gs[0] * v.gs[1]);
+    v.ax[i].scheme = c.opts.discretization_scheme;
   }
   v.curvilinear = c.opts.curvilinear;
   b.tGrad = b.tDiss = b.tRhs = b.tAdjA = b.tAdjD = b.tAdjB = c.nD == 2 ? makeTile(b, 32, 4, 1) : makeTile(b, 32, 2, 2);
@@ -936,7 +947,7 @@ static int finalizeBlock(Context& c, int bi, const double* mollifierTotals) {
   std::vector<int> ffPoint, ffDir, ffSigned, ffKind;
   std::vector<double> ffSigInv, ffSigV, ffSigVRaw, ffWallInv, ffWallVisc, ffWallT;
   std::vector<double> qtH;  // target state on the host (isothermal wall temperatures)
-  const HostOp d1 = makeFirstDerivative48();
+  const HostOp d1 = schemeOps(c.opts.discretization_scheme).d1;
   long long actOffset = 0;
   for (size_t pi = 0; pi < c.patches.size(); ++pi) {
     const mgd_patch_desc& p = c.patches[pi];

@@ -22,9 +22,15 @@ template <> struct OpShape<OP_DISS> { static constexpr int depth = 2, width = 5,
 template <> struct OpShape<OP_DISST> { static constexpr int depth = 8, width = 10, half = 2; static constexpr bool skew = false; };
 template <> struct OpShape<OP_DCOMP> { static constexpr int depth = 8, width = 12, half = 4; static constexpr bool skew = false; };
 
+// SBP schemes (defaults/discretization_scheme): index = MGD_SBP_* (4-8, 1-2,
+// 2-4, 3-6). Every scheme's operators are stored in the fixed shapes of
+// OpShape (the 4-8 shapes, the largest): lower-order closures are padded
+// with interior rows and their interiors with zero coefficients.
+constexpr int kSchemes = 4;
+
 struct OpTables {
-  double interior[OP_COUNT][9];         // offsets -half..half
-  double left[OP_COUNT][16 * 12];       // depth x width row-major
+  double interior[kSchemes][OP_COUNT][9];  // offsets -half..half
+  int asym[kSchemes][OP_COUNT];            // general interior sum and explicit right block
 };
 
 // One copy per translation unit; only mgd_kernels.cu launches kernels and
@@ -32,13 +38,16 @@ struct OpTables {
 // constant memory; boundary-closure rows differ between lanes and are read
 // from global memory through L1, which serves divergent addresses at once.
 static __constant__ OpTables c_ops;
-static __device__ double g_opLeft[OP_COUNT][16 * 12];
+static __device__ double g_opLeft[kSchemes][OP_COUNT][16 * 12];
+static __device__ double g_opRight[kSchemes][OP_COUNT][16 * 12];  // explicit right blocks (asym only)
 
-// One direction of a block: n points along it, memory stride, periodicity.
+// One direction of a block: n points along it, memory stride, periodicity,
+// and the block's SBP scheme.
 struct Axis {
   int n;
   int per;          // 0 none, 1 plane, 2 overlap
   long long stride;
+  int scheme;       // MGD_SBP_*
 };
 
 // Index of point i + j along a periodic line (fillGhostPoints for one
@@ -57,12 +66,14 @@ __device__ __forceinline__ int wrapIndex(int i, int n, int per) {
 template <int OP>
 __device__ __forceinline__ double applyOp(const double* __restrict__ line, int i, const Axis& ax) {
   using S = OpShape<OP>;
-  const double* __restrict__ cin = c_ops.interior[OP];
+  const double* __restrict__ cin = c_ops.interior[ax.scheme][OP];
+  // only the non-composite dissipation pair of SBP 3-6 is asymmetric
+  const bool asym = !S::skew && (OP == OP_DISS || OP == OP_DISST) && c_ops.asym[ax.scheme][OP];
   const long long st = ax.stride;
   if (ax.per == 0) {
     if (i < S::depth) {
       // boundary closure rows are rare: keep them compact (few registers)
-      const double* __restrict__ row = &g_opLeft[OP][i * S::width];
+      const double* __restrict__ row = &g_opLeft[ax.scheme][OP][i * S::width];
       double s = __ldg(row) * __ldg(line);
 #pragma unroll 1
       for (int k = 1; k < S::width; ++k) s += __ldg(row + k) * __ldg(line + k * st);
@@ -70,8 +81,16 @@ __device__ __forceinline__ double applyOp(const double* __restrict__ line, int i
     }
     if (i >= ax.n - S::depth) {
       const int m = ax.n - 1 - i;
-      const double* __restrict__ row = &g_opLeft[OP][m * S::width];
       const double* __restrict__ end = line + (long long)(ax.n - S::width) * st;
+      if (asym) {
+        // explicit right block, columns left to right
+        const double* __restrict__ row = &g_opRight[ax.scheme][OP][m * S::width];
+        double s = __ldg(row) * __ldg(end);
+#pragma unroll 1
+        for (int k = 1; k < S::width; ++k) s += __ldg(row + k) * __ldg(end + k * st);
+        return s;
+      }
+      const double* __restrict__ row = &g_opLeft[ax.scheme][OP][m * S::width];
       // right block = reflection of the left block, negated for skew operators
       double s = __ldg(row + S::width - 1) * __ldg(end);
 #pragma unroll 1
@@ -84,6 +103,11 @@ __device__ __forceinline__ double applyOp(const double* __restrict__ line, int i
 #pragma unroll
       for (int j = 2; j <= S::half; ++j) s += cin[S::half + j] * (__ldg(c + j * st) - __ldg(c - j * st));
       return s;
+    } else if (asym) {
+      double s = cin[0] * __ldg(c - S::half * st);
+#pragma unroll
+      for (int j = 1 - S::half; j <= S::half; ++j) s += cin[S::half + j] * __ldg(c + j * st);
+      return s;
     } else {
       double s = cin[S::half + 1] * (__ldg(c + st) + __ldg(c - st));
 #pragma unroll
@@ -93,6 +117,12 @@ __device__ __forceinline__ double applyOp(const double* __restrict__ line, int i
   }
   // periodic: interior stencil everywhere with wrapped indices
   auto at = [&](int j) { return __ldg(line + (long long)wrapIndex(i + j, ax.n, ax.per) * st); };
+  if (asym) {
+    double s = cin[0] * at(-S::half);
+#pragma unroll
+    for (int j = 1 - S::half; j <= S::half; ++j) s += cin[S::half + j] * at(j);
+    return s;
+  }
   if (S::skew) {
     double s = cin[S::half + 1] * (at(1) - at(-1));
 #pragma unroll

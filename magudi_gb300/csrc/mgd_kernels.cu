@@ -25,7 +25,6 @@
 namespace mgd {
 
 
-__constant__ double c_norm[8];
 __device__ PowTables g_powTables;
 
 static void uploadPowTables() {
@@ -130,19 +129,33 @@ void uploadOperatorTables() {
   if (dev < 64 && done[dev]) return;
   OpTables t;
   std::memset(&t, 0, sizeof t);
-  const HostOp d1 = makeFirstDerivative48();
-  const HostOp ad = makeAdjoint(d1);
-  const HostOp di = makeDissipation48();
-  const HostOp dt = makeDissipationTransposeNormInverse48(d1);
-  const HostOp dc = makeCompositeDissipation48();
-  const HostOp* ops[OP_COUNT] = {&d1, &ad, &di, &dt, &dc};
-  for (int o = 0; o < OP_COUNT; ++o) {
-    for (size_t j = 0; j < ops[o]->interior.size(); ++j) t.interior[o][j] = ops[o]->interior[j];
-    for (size_t j = 0; j < ops[o]->left.size(); ++j) t.left[o][j] = ops[o]->left[j];
+  static double left[kSchemes][OP_COUNT][16 * 12], right[kSchemes][OP_COUNT][16 * 12];
+  std::memset(left, 0, sizeof left);
+  std::memset(right, 0, sizeof right);
+  for (int sc = 0; sc < kSchemes; ++sc) {
+    const SchemeOps so = schemeOps(sc);
+    // every operator in the kernels' shapes (OpShape); the non-composite
+    // transpose carries the inverse of the first-derivative norm
+    HostOp ops[OP_COUNT];
+    ops[OP_D1] = embed(so.d1, 8, 12, 4);
+    ops[OP_D1ADJ] = embed(makeAdjoint(so.d1), 12, 16, 4);
+    ops[OP_DCOMP] = embed(so.dcomp, 8, 12, 4);
+    if (so.hasDissipation) {
+      ops[OP_DISS] = embed(so.diss, 2, 5, 2);
+      ops[OP_DISST] = embed(so.dissT, 8, 10, 2);
+      foldNormInverse(ops[OP_DISST], so.d1.norm);
+    }
+    for (int o = 0; o < OP_COUNT; ++o) {
+      const HostOp& h = ops[o];
+      for (size_t j = 0; j < h.interior.size(); ++j) t.interior[sc][o][j] = h.interior[j];
+      for (size_t j = 0; j < h.left.size(); ++j) left[sc][o][j] = h.left[j];
+      for (size_t j = 0; j < h.right.size(); ++j) right[sc][o][j] = h.right[j];
+      t.asym[sc][o] = h.asym ? 1 : 0;
+    }
   }
   cudaMemcpyToSymbol(c_ops, &t, sizeof t);
-  cudaMemcpyToSymbol(g_opLeft, t.left, sizeof t.left);
-  cudaMemcpyToSymbol(c_norm, d1.norm.data(), 8 * sizeof(double));
+  cudaMemcpyToSymbol(g_opLeft, left, sizeof left);
+  cudaMemcpyToSymbol(g_opRight, right, sizeof right);
   uploadPowTables();
   if (dev < 64) done[dev] = true;
 }
@@ -1848,7 +1861,7 @@ __global__ void kCoordinateDerivative(BlockView B, const double* __restrict__ co
     if (ax.per != MGD_PERIODIC_PLANE) {
       s = applyOp<OP_D1>(line, I.idx[dir], ax);
     } else {
-      const double* cin = c_ops.interior[OP_D1];
+      const double* cin = c_ops.interior[ax.scheme][OP_D1];
       auto at = [&](int j) {
         const int k = I.idx[dir] + j;
         double x = line[(long long)wrapIndex(k, ax.n, ax.per) * ax.stride];

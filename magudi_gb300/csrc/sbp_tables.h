@@ -17,13 +17,22 @@ namespace mgd {
 struct HostOp {
   int depth = 0, width = 0, half = 0;
   bool skew = false;
+  bool asym = false;             // interior stencil not (skew-)symmetric: general sum, explicit right block
   std::vector<double> interior;  // coefficients of offsets -half..half
   std::vector<double> left;      // depth x width, row-major
+  std::vector<double> right;     // asym only: depth x width, row m = point n-1-m, column k = point n-width+k
   std::vector<double> norm;      // boundary norm weights (first derivative only)
   double& L(int m, int k) { return left[(size_t)m * width + k]; }
   double L(int m, int k) const { return left[(size_t)m * width + k]; }
+  double& R(int m, int k) { return right[(size_t)m * width + k]; }
+  double R(int m, int k) const { return right[(size_t)m * width + k]; }
   double& I(int j) { return interior[j + half]; }
   double I(int j) const { return interior[j + half]; }
+  void allocate(int d, int w, int h) {
+    depth = d; width = w; half = h;
+    interior.assign(2 * h + 1, 0.0);
+    left.assign((size_t)d * w, 0.0);
+  }
 };
 
 inline HostOp makeFirstDerivative48() {
@@ -124,8 +133,12 @@ inline std::vector<double> denseMatrix(const HostOp& op, int n) {
       for (int k = 0; k < op.width; ++k) M[(size_t)r * n + k] = op.L(r, k);
     } else if (r >= n - op.depth) {
       const int m = n - 1 - r;
-      const double sgn = op.skew ? -1.0 : 1.0;
-      for (int k = 0; k < op.width; ++k) M[(size_t)r * n + (n - 1 - k)] = sgn * op.L(m, k);
+      if (op.asym) {
+        for (int k = 0; k < op.width; ++k) M[(size_t)r * n + (n - op.width + k)] = op.R(m, k);
+      } else {
+        const double sgn = op.skew ? -1.0 : 1.0;
+        for (int k = 0; k < op.width; ++k) M[(size_t)r * n + (n - 1 - k)] = sgn * op.L(m, k);
+      }
     } else {
       for (int j = -op.half; j <= op.half; ++j) M[(size_t)r * n + r + j] = op.I(j);
     }
@@ -215,6 +228,243 @@ inline HostOp makeCompositeDissipation48() {
   for (int m = 0; m < 8; ++m)
     for (int t = 0; t < rows[m].count; ++t) d.L(m, rows[m].first + t) = rows[m].num[t] / rows[m].den / 256.0;
   return d;
+}
+
+// ---------------------------------------------------------------------------
+// The lower-order schemes of defaults/discretization_scheme ("SBP 1-2",
+// "SBP 2-4", "SBP 3-6"; setupOperator, src/StencilOperatorImpl.f90:1164-1585):
+// first derivative, composite dissipation, and the non-composite dissipation
+// and its transpose. Boundary rows are written as (row, first column,
+// values), 0-based, like the reference's rhsBoundary1(k0:, m) assignments.
+// ---------------------------------------------------------------------------
+struct OpRow { int m, k0, n; double v[9]; };
+inline void setRows(HostOp& op, const OpRow* rows, int count, double scale = 1.0) {
+  for (int r = 0; r < count; ++r)
+    for (int t = 0; t < rows[r].n; ++t) op.L(rows[r].m, rows[r].k0 + t) = rows[r].v[t] * scale;
+}
+
+inline HostOp makeFirstDerivative12() {  // :1164-1177
+  HostOp d;
+  d.allocate(1, 2, 1);
+  d.skew = true;
+  d.I(1) = 1.0 / 2.0; d.I(-1) = -d.I(1);
+  d.norm = {1.0 / 2.0};
+  d.L(0, 0) = -1.0; d.L(0, 1) = 1.0;
+  return d;
+}
+inline HostOp makeCompositeDissipation12() {  // :1194-1210
+  HostOp d;
+  d.allocate(1, 2, 1);
+  d.I(0) = -2.0 / 2.0; d.I(1) = 1.0 / 2.0; d.I(-1) = d.I(1);
+  d.L(0, 0) = -2.0 / 2.0; d.L(0, 1) = 2.0 / 2.0;
+  return d;
+}
+
+inline HostOp makeFirstDerivative24() {  // :1212-1245
+  HostOp d;
+  d.allocate(4, 6, 2);
+  d.skew = true;
+  d.I(1) = 2.0 / 3.0; d.I(2) = -1.0 / 12.0;
+  for (int j = 1; j <= 2; ++j) d.I(-j) = -d.I(j);
+  d.norm = {17.0 / 48.0, 59.0 / 48.0, 43.0 / 48.0, 49.0 / 48.0};
+  const OpRow rows[4] = {{0, 0, 4, {-24.0 / 17.0, 59.0 / 34.0, -4.0 / 17.0, -3.0 / 34.0}},
+                         {1, 0, 3, {-1.0 / 2.0, 0.0, 1.0 / 2.0}},
+                         {2, 0, 5, {4.0 / 43.0, -59.0 / 86.0, 0.0, 59.0 / 86.0, -4.0 / 43.0}},
+                         {3, 0, 6, {3.0 / 98.0, 0.0, -59.0 / 98.0, 0.0, 32.0 / 49.0, -4.0 / 49.0}}};
+  setRows(d, rows, 4);
+  return d;
+}
+inline HostOp makeCompositeDissipation24() {  // :1282-1317
+  HostOp d;
+  d.allocate(4, 6, 2);
+  const double c[3] = {-6.0, 4.0, -1.0};
+  for (int j = 0; j <= 2; ++j) d.I(j) = d.I(-j) = c[j] / 16.0;
+  const OpRow rows[4] = {{0, 0, 3, {-96.0 / 17.0, 192.0 / 17.0, -96.0 / 17.0}},
+                         {1, 0, 4, {192.0 / 59.0, -432.0 / 59.0, 288.0 / 59.0, -48.0 / 59.0}},
+                         {2, 0, 5, {-96.0 / 43.0, 288.0 / 43.0, -336.0 / 43.0, 192.0 / 43.0, -48.0 / 43.0}},
+                         {3, 1, 5, {-48.0 / 49.0, 192.0 / 49.0, -288.0 / 49.0, 192.0 / 49.0, -48.0 / 49.0}}};
+  setRows(d, rows, 4, 1.0 / 16.0);
+  return d;
+}
+inline HostOp makeDissipation24() {  // :1319-1329
+  HostOp d;
+  d.allocate(1, 3, 1);
+  d.I(-1) = 1.0; d.I(0) = -2.0; d.I(1) = 1.0;
+  for (int k = 0; k < 3; ++k) d.L(0, k) = d.I(k - 1);
+  return d;
+}
+inline HostOp makeDissipationTranspose24() {  // :1331-1345
+  HostOp d;
+  d.allocate(3, 4, 1);
+  d.I(-1) = 1.0; d.I(0) = -2.0; d.I(1) = 1.0;
+  for (int m = 0; m < 3; ++m) d.L(m, 0) = d.L(m, 1) = d.I(m - 1);
+  for (int m = 1; m < 3; ++m) d.L(m, 2) = d.I(m - 2);
+  d.L(2, 3) = d.I(-1);
+  return d;
+}
+
+inline HostOp makeFirstDerivative36() {  // :1362-1421
+  HostOp d;
+  d.allocate(6, 9, 3);
+  d.skew = true;
+  d.I(1) = 3.0 / 4.0; d.I(2) = -3.0 / 20.0; d.I(3) = 1.0 / 60.0;
+  for (int j = 1; j <= 3; ++j) d.I(-j) = -d.I(j);
+  d.norm = {13649.0 / 43200.0, 12013.0 / 8640.0, 2711.0 / 4320.0, 5359.0 / 4320.0, 7877.0 / 8640.0,
+            43801.0 / 43200.0};
+  const OpRow rows[6] = {
+      {0, 0, 6, {-21600.0 / 13649.0, 104009.0 / 54596.0, 30443.0 / 81894.0, -33311.0 / 27298.0, 16863.0 / 27298.0,
+                 -15025.0 / 163788.0}},
+      {1, 0, 6, {-104009.0 / 240260.0, 0.0, -311.0 / 72078.0, 20229.0 / 24026.0, -24337.0 / 48052.0,
+                 36661.0 / 360390.0}},
+      {2, 0, 6, {-30443.0 / 162660.0, 311.0 / 32532.0, 0.0, -11155.0 / 16266.0, 41287.0 / 32532.0,
+                 -21999.0 / 54220.0}},
+      {3, 0, 7, {33311.0 / 107180.0, -20229.0 / 21436.0, 485.0 / 1398.0, 0.0, 4147.0 / 21436.0,
+                 25427.0 / 321540.0, 72.0 / 5359.0}},
+      {4, 0, 8, {-16863.0 / 78770.0, 24337.0 / 31508.0, -41287.0 / 47262.0, -4147.0 / 15754.0, 0.0,
+                 342523.0 / 472620.0, -1296.0 / 7877.0, 144.0 / 7877.0}},
+      {5, 0, 9, {15025.0 / 525612.0, -36661.0 / 262806.0, 21999.0 / 87602.0, -25427.0 / 262806.0,
+                 -342523.0 / 525612.0, 0.0, 32400.0 / 43801.0, -6480.0 / 43801.0, 720.0 / 43801.0}}};
+  setRows(d, rows, 6);
+  return d;
+}
+inline HostOp makeCompositeDissipation36() {  // :1487-1543
+  HostOp d;
+  d.allocate(6, 9, 3);
+  const double c[4] = {-20.0, 15.0, -6.0, 1.0};
+  for (int j = 0; j <= 3; ++j) d.I(j) = d.I(-j) = c[j] / 64.0;
+  const OpRow rows[6] = {
+      {0, 0, 4, {-129600.0 / 13649.0, 388800.0 / 13649.0, -388800.0 / 13649.0, 129600.0 / 13649.0}},
+      {1, 0, 5, {77760.0 / 12013.0, -241920.0 / 12013.0, 259200.0 / 12013.0, -103680.0 / 12013.0,
+                 8640.0 / 12013.0}},
+      {2, 0, 6, {-38880.0 / 2711.0, 129600.0 / 2711.0, -159840.0 / 2711.0, 90720.0 / 2711.0, -25920.0 / 2711.0,
+                 4320.0 / 2711.0}},
+      {3, 0, 7, {12960.0 / 5359.0, -51840.0 / 5359.0, 90720.0 / 5359.0, -95040.0 / 5359.0, 64800.0 / 5359.0,
+                 -25920.0 / 5359.0, 4320.0 / 5359.0}},
+      {4, 1, 7, {8640.0 / 7877.0, -51840.0 / 7877.0, 129600.0 / 7877.0, -172800.0 / 7877.0, 129600.0 / 7877.0,
+                 -51840.0 / 7877.0, 8640.0 / 7877.0}},
+      {5, 2, 7, {43200.0 / 43801.0, -259200.0 / 43801.0, 648000.0 / 43801.0, -864000.0 / 43801.0,
+                 648000.0 / 43801.0, -259200.0 / 43801.0, 43200.0 / 43801.0}}};
+  setRows(d, rows, 6, 1.0 / 64.0);
+  return d;
+}
+// "SBP 3-6 dissipation" (:1545-1561): interior offsets -2..1, both closure
+// rows repeat it, the right block is the negated reflection.
+inline HostOp makeDissipation36() {
+  HostOp d;
+  d.allocate(2, 4, 2);
+  d.asym = true;
+  const double c[4] = {-1.0, 3.0, -3.0, 1.0};
+  for (int j = -2; j <= 1; ++j) d.I(j) = c[j + 2];
+  d.right.assign(2 * 4, 0.0);
+  for (int m = 0; m < 2; ++m)
+    for (int k = 0; k < 4; ++k) d.L(m, k) = c[k];
+  for (int m = 0; m < 2; ++m)
+    for (int k = 0; k < 4; ++k) d.R(m, k) = -d.L(m, 3 - k);
+  return d;
+}
+// "SBP 3-6 dissipation transpose" (:1563-1585): interior offsets -1..2 and
+// the reference's explicit left and right blocks.
+inline HostOp makeDissipationTranspose36() {
+  HostOp d;
+  d.allocate(4, 6, 2);
+  d.asym = true;
+  const double c[4] = {1.0, -3.0, 3.0, -1.0};  // offsets -1..2
+  for (int j = -1; j <= 2; ++j) d.I(j) = c[j + 1];
+  auto in = [&](int j) { return c[j + 1]; };
+  // rhsBoundary1(k, m): L(m - 1, k - 1)
+  for (int k = 1; k <= 3; ++k)
+    for (int m = 1; m <= 4; ++m) d.L(m - 1, k - 1) = in(3 - m);
+  for (int m = 2; m <= 4; ++m) d.L(m - 1, 3) = in(4 - m);
+  for (int m = 3; m <= 4; ++m) d.L(m - 1, 4) = in(5 - m);
+  d.L(3, 5) = in(2);
+  // rhsBoundary2(k, m): R(m - 1, k - 1)
+  d.right.assign(4 * 6, 0.0);
+  for (int m = 1; m <= 4; ++m) d.R(m - 1, 5) = d.R(m - 1, 4) = in(3 - m);
+  for (int m = 2; m <= 4; ++m) d.R(m - 1, 3) = in(m - 3);
+  for (int m = 3; m <= 4; ++m) d.R(m - 1, 2) = in(m - 4);
+  d.R(3, 1) = in(-1);
+  return d;
+}
+
+// The scheme's operators in their own shapes.
+struct SchemeOps {
+  HostOp d1, dcomp, diss, dissT;
+  bool hasDissipation = true;  // SBP 1-2 has no non-composite dissipation
+};
+inline SchemeOps schemeOps(int scheme) {
+  SchemeOps s;
+  switch (scheme) {
+    case 1:
+      s.d1 = makeFirstDerivative12(); s.dcomp = makeCompositeDissipation12(); s.hasDissipation = false;
+      break;
+    case 2:
+      s.d1 = makeFirstDerivative24(); s.dcomp = makeCompositeDissipation24();
+      s.diss = makeDissipation24(); s.dissT = makeDissipationTranspose24();
+      break;
+    case 3:
+      s.d1 = makeFirstDerivative36(); s.dcomp = makeCompositeDissipation36();
+      s.diss = makeDissipation36(); s.dissT = makeDissipationTranspose36();
+      break;
+    default: {
+      s.d1 = makeFirstDerivative48(); s.dcomp = makeCompositeDissipation48();
+      s.diss = makeDissipation48();
+      // "SBP 4-8 dissipation transpose" (:1942-1960) equals the transpose of "SBP 4-8 dissipation"
+      HostOp t;
+      t.allocate(5, 7, 2);
+      for (int j = -2; j <= 2; ++j) t.I(j) = s.diss.I(j);
+      const std::vector<double> D = denseMatrix(s.diss, 40);
+      for (int m = 0; m < 5; ++m)
+        for (int k = 0; k < 7; ++k) t.L(m, k) = D[(size_t)k * 40 + m];
+      s.dissT = t;
+    }
+  }
+  return s;
+}
+
+// An operator in the fixed shape (D rows, W columns, half-width Hf) of the
+// kernels' tables: the closure rows as given, the rows from the operator's
+// depth to D as its interior stencil, the interior zero-padded to Hf; an
+// explicit right block likewise. The value of every output point is
+// unchanged (rows between the operator's depth and D sum the same products
+// in closure order).
+inline HostOp embed(const HostOp& op, int D, int W, int Hf) {
+  HostOp e;
+  e.allocate(D, W, Hf);
+  e.skew = op.skew;
+  e.asym = op.asym;
+  e.norm = op.norm;
+  for (int j = -op.half; j <= op.half; ++j) e.I(j) = op.I(j);
+  for (int m = 0; m < D; ++m) {
+    if (m < op.depth) {
+      for (int k = 0; k < op.width; ++k) e.L(m, k) = op.L(m, k);
+    } else {
+      for (int j = -op.half; j <= op.half; ++j)
+        if (op.I(j) != 0.0) e.L(m, m + j) = op.I(j);
+    }
+  }
+  if (op.asym) {
+    e.right.assign((size_t)D * W, 0.0);
+    for (int m = 0; m < D; ++m) {
+      if (m < op.depth) {
+        for (int k = 0; k < op.width; ++k) e.R(m, W - op.width + k) = op.R(m, k);
+      } else {
+        // point n-1-m: coefficient I(j) on point n-1-m+j = column W-1-m+j
+        for (int j = -op.half; j <= op.half; ++j)
+          if (op.I(j) != 0.0) e.R(m, W - 1 - m + j) = op.I(j);
+      }
+    }
+  }
+  return e;
+}
+
+// Folds the inverse of the first-derivative norm into the boundary rows of
+// an operator in kernel shape (applyNormInverse after the operator).
+inline void foldNormInverse(HostOp& t, const std::vector<double>& norm) {
+  for (size_t m = 0; m < norm.size() && (int)m < t.depth; ++m)
+    for (int k = 0; k < t.width; ++k) {
+      t.L((int)m, k) = t.L((int)m, k) / norm[m];
+      if (t.asym) t.R((int)m, k) = t.R((int)m, k) / norm[m];
+    }
 }
 
 }  // namespace mgd

@@ -14,7 +14,7 @@ options_from_inputs, patches_from_bc, sources_from_inputs, block_periodicity
                    src/FarFieldPatchImpl.f90:42-63, src/SpongePatchImpl.f90:30-45,
                    src/StateImpl.f90:135-150, src/GridImpl.f90:195-214).
 """
-from .capi import PATCH_TYPES, PERIODIC_NONE, PERIODIC_OVERLAP, PERIODIC_PLANE
+from .capi import PATCH_TYPES, PERIODIC_NONE, PERIODIC_OVERLAP, PERIODIC_PLANE, SBP_SCHEMES
 from .problem import AcousticSource, Options, Patch
 
 
@@ -148,8 +148,12 @@ def options_from_inputs(d, n_dimensions):
             raise InputError("Required parameter 'time_step_size' not specified!")
         o.time_step_size = d.get_float("time_step_size", 0.0)
     scheme = d.get_str("defaults/discretization_scheme", "SBP 4-8")
-    if scheme != "SBP 4-8":
-        raise InputError(f"discretization scheme '{scheme}' is not supported (SBP 4-8 only)")
+    if scheme not in SBP_SCHEMES:
+        raise InputError(f"discretization scheme '{scheme}' is not supported "
+                         f"(one of {', '.join(sorted(SBP_SCHEMES))})")
+    o.discretization_scheme = SBP_SCHEMES[scheme]
+    if scheme == "SBP 1-2" and o.dissipation and not o.composite_dissipation:
+        raise InputError("SBP 1-2 has no non-composite dissipation operator")
     return o
 
 
@@ -238,3 +242,30 @@ def write_bc_dat(path, patches):
             e = p.extent
             f.write(f"  {p.name:<20} {p.type:<21} {p.grid_index:>4d} {p.normal_direction:>7d}"
                     + "".join(f" {x:>4d}" for x in e) + "\n")
+
+
+def problem_from_inputs(inp_path, bc_path, blocks):
+    """A Problem from a magudi.inp and a bc.dat, unchanged, and the blocks'
+    arrays (what the reference reads from its grid, initial-condition,
+    mollifier and mean-pressure files): `blocks` is a list of
+    problem.Block with grid_size and coordinates set. Options, patches and
+    acoustic sources come from the two files; each block's periodicity from
+    grid00N/dirM/...; a block without a target state gets the quiescent one
+    (Solver%setup, src/SolverImpl.f90:509-520); number_of_timesteps and
+    save_interval become the run length and the checkpoint interval
+    (src/SolverImpl.f90:483-496, src/UniformCheckpointerImpl.f90:3-40)."""
+    from .problem import Problem, quiescent_state
+    d = parse_input_file(inp_path)
+    n_dimensions = 3 if any(int(b.grid_size[2]) > 1 for b in blocks) else 2
+    options = options_from_inputs(d, n_dimensions)
+    for i, b in enumerate(blocks, start=1):
+        b.periodicity_type, b.periodic_length = block_periodicity(d, i, n_dimensions)
+        if b.target_state is None:
+            b.target_state = quiescent_state(b.n_points, n_dimensions, options.ratio_of_specific_heats)
+    patches = patches_from_bc(d, read_bc_dat(bc_path))
+    n_steps = max(0, d.get_int("number_of_timesteps", 1000))
+    save_interval = d.get_int("save_interval", -1)
+    if save_interval <= 0:
+        save_interval = n_steps
+    return Problem(options=options, blocks=list(blocks), patches=patches,
+                   sources=sources_from_inputs(d, n_dimensions), n_steps=n_steps, save_interval=save_interval)

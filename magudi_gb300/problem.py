@@ -47,6 +47,7 @@ class Options:
     maximum_density: float = 0.0
     minimum_temperature: float = 0.0
     maximum_temperature: float = 0.0
+    discretization_scheme: int = 0  # capi.SBP_*: SBP 4-8, 1-2, 2-4 or 3-6
 
     def to_c(self) -> capi.Options:
         o = capi.Options()

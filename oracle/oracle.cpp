@@ -252,6 +252,247 @@ StencilOp sbp48DissipationTranspose() {
   return op;
 }
 
+// The lower-order schemes of setupOperator (src/StencilOperatorImpl.f90:1164-1585):
+// boundary rows are given as (row m, first column k0, values) like the
+// reference's rhsBoundary1(k0:k0+n-1, m) assignments.
+struct BoundaryRow { int m, k0, n; double v[9]; };
+static void setRows(StencilOp& op, const BoundaryRow* rows, int count, double scale = 1.0) {
+  for (int r = 0; r < count; ++r)
+    for (int t = 0; t < rows[r].n; ++t) op.b1(rows[r].k0 + t, rows[r].m) = rows[r].v[t] * scale;
+}
+
+// "SBP 1-2 first derivative", :1164-1177.
+StencilOp sbp12FirstDerivative() {
+  StencilOp op;
+  op.symmetryType = SKEW_SYMMETRIC;
+  op.interiorWidth = 3; op.boundaryWidth = 2; op.boundaryDepth = 1;
+  op.allocate();
+  op.in(1) = 1.0 / 2.0;
+  op.in(-1) = -op.in(1);
+  op.normBoundary = {1.0 / 2.0};
+  op.b1(1, 1) = -1.0;
+  op.b1(2, 1) = 1.0;
+  op.fillRightBoundary();
+  return op;
+}
+
+// "SBP 1-2 composite dissipation", :1194-1210.
+StencilOp sbp12CompositeDissipation() {
+  StencilOp op;
+  op.symmetryType = SYMMETRIC;
+  op.interiorWidth = 3; op.boundaryWidth = 2; op.boundaryDepth = 1;
+  op.allocate();
+  op.in(0) = -2.0 / 2.0;
+  op.in(1) = 1.0 / 2.0;
+  op.in(-1) = op.in(1);
+  op.normBoundary = {1.0 / 2.0};
+  op.b1(1, 1) = -2.0 / 2.0;
+  op.b1(2, 1) = 2.0 / 2.0;
+  op.fillRightBoundary();
+  return op;
+}
+
+// "SBP 2-4 first derivative", :1212-1245.
+StencilOp sbp24FirstDerivative() {
+  StencilOp op;
+  op.symmetryType = SKEW_SYMMETRIC;
+  op.interiorWidth = 5; op.boundaryWidth = 6; op.boundaryDepth = 4;
+  op.allocate();
+  op.in(1) = 2.0 / 3.0;
+  op.in(2) = -1.0 / 12.0;
+  for (int j = 1; j <= 2; ++j) op.in(-j) = -op.in(j);
+  op.normBoundary = {17.0 / 48.0, 59.0 / 48.0, 43.0 / 48.0, 49.0 / 48.0};
+  const BoundaryRow rows[4] = {
+      {1, 1, 4, {-24.0 / 17.0, 59.0 / 34.0, -4.0 / 17.0, -3.0 / 34.0}},
+      {2, 1, 3, {-1.0 / 2.0, 0.0, 1.0 / 2.0}},
+      {3, 1, 5, {4.0 / 43.0, -59.0 / 86.0, 0.0, 59.0 / 86.0, -4.0 / 43.0}},
+      {4, 1, 6, {3.0 / 98.0, 0.0, -59.0 / 98.0, 0.0, 32.0 / 49.0, -4.0 / 49.0}}};
+  setRows(op, rows, 4);
+  op.fillRightBoundary();
+  return op;
+}
+
+// "SBP 2-4 composite dissipation", :1282-1317 (rows and interior / 16).
+StencilOp sbp24CompositeDissipation() {
+  StencilOp op;
+  op.symmetryType = SYMMETRIC;
+  op.interiorWidth = 5; op.boundaryWidth = 6; op.boundaryDepth = 4;
+  op.allocate();
+  const double in[3] = {-6.0, 4.0, -1.0};
+  for (int j = 0; j <= 2; ++j) op.in(j) = in[j] / 16.0;
+  for (int j = 1; j <= 2; ++j) op.in(-j) = op.in(j);
+  op.normBoundary = {17.0 / 48.0, 59.0 / 48.0, 43.0 / 48.0, 49.0 / 48.0};
+  const BoundaryRow rows[4] = {
+      {1, 1, 3, {-96.0 / 17.0, 192.0 / 17.0, -96.0 / 17.0}},
+      {2, 1, 4, {192.0 / 59.0, -432.0 / 59.0, 288.0 / 59.0, -48.0 / 59.0}},
+      {3, 1, 5, {-96.0 / 43.0, 288.0 / 43.0, -336.0 / 43.0, 192.0 / 43.0, -48.0 / 43.0}},
+      {4, 2, 5, {-48.0 / 49.0, 192.0 / 49.0, -288.0 / 49.0, 192.0 / 49.0, -48.0 / 49.0}}};
+  setRows(op, rows, 4);
+  for (double& v : op.rb1) v = v / 16.0;
+  op.fillRightBoundary();
+  return op;
+}
+
+// "SBP 2-4 dissipation", :1319-1329.
+StencilOp sbp24Dissipation() {
+  StencilOp op;
+  op.symmetryType = SYMMETRIC;
+  op.interiorWidth = 3; op.boundaryWidth = 3; op.boundaryDepth = 1;
+  op.allocate();
+  op.in(-1) = 1.0; op.in(0) = -2.0; op.in(1) = 1.0;
+  for (int k = 1; k <= 3; ++k) op.b1(k, 1) = op.in(k - 2);
+  op.fillRightBoundary();
+  return op;
+}
+
+// "SBP 2-4 dissipation transpose", :1331-1345.
+StencilOp sbp24DissipationTranspose() {
+  StencilOp op;
+  op.symmetryType = SYMMETRIC;
+  op.interiorWidth = 3; op.boundaryWidth = 4; op.boundaryDepth = 3;
+  op.allocate();
+  op.in(-1) = 1.0; op.in(0) = -2.0; op.in(1) = 1.0;
+  for (int m = 1; m <= 3; ++m) op.b1(1, m) = op.in(m - 2);
+  for (int m = 1; m <= 3; ++m) op.b1(2, m) = op.in(m - 2);
+  for (int m = 2; m <= 3; ++m) op.b1(3, m) = op.in(m - 3);
+  op.b1(4, 3) = op.in(-1);
+  op.fillRightBoundary();
+  return op;
+}
+
+// "SBP 3-6 first derivative", :1362-1421.
+StencilOp sbp36FirstDerivative() {
+  StencilOp op;
+  op.symmetryType = SKEW_SYMMETRIC;
+  op.interiorWidth = 7; op.boundaryWidth = 9; op.boundaryDepth = 6;
+  op.allocate();
+  op.in(1) = 3.0 / 4.0;
+  op.in(2) = -3.0 / 20.0;
+  op.in(3) = 1.0 / 60.0;
+  for (int j = 1; j <= 3; ++j) op.in(-j) = -op.in(j);
+  op.normBoundary = {13649.0 / 43200.0, 12013.0 / 8640.0, 2711.0 / 4320.0,
+                     5359.0 / 4320.0,   7877.0 / 8640.0,  43801.0 / 43200.0};
+  const BoundaryRow rows[6] = {
+      {1, 1, 6, {-21600.0 / 13649.0, 104009.0 / 54596.0, 30443.0 / 81894.0, -33311.0 / 27298.0,
+                 16863.0 / 27298.0, -15025.0 / 163788.0}},
+      {2, 1, 6, {-104009.0 / 240260.0, 0.0, -311.0 / 72078.0, 20229.0 / 24026.0, -24337.0 / 48052.0,
+                 36661.0 / 360390.0}},
+      {3, 1, 6, {-30443.0 / 162660.0, 311.0 / 32532.0, 0.0, -11155.0 / 16266.0, 41287.0 / 32532.0,
+                 -21999.0 / 54220.0}},
+      {4, 1, 7, {33311.0 / 107180.0, -20229.0 / 21436.0, 485.0 / 1398.0, 0.0, 4147.0 / 21436.0,
+                 25427.0 / 321540.0, 72.0 / 5359.0}},
+      {5, 1, 8, {-16863.0 / 78770.0, 24337.0 / 31508.0, -41287.0 / 47262.0, -4147.0 / 15754.0, 0.0,
+                 342523.0 / 472620.0, -1296.0 / 7877.0, 144.0 / 7877.0}},
+      {6, 1, 9, {15025.0 / 525612.0, -36661.0 / 262806.0, 21999.0 / 87602.0, -25427.0 / 262806.0,
+                 -342523.0 / 525612.0, 0.0, 32400.0 / 43801.0, -6480.0 / 43801.0, 720.0 / 43801.0}}};
+  setRows(op, rows, 6);
+  op.fillRightBoundary();
+  return op;
+}
+
+// "SBP 3-6 composite dissipation", :1487-1543 (rows and interior / 64).
+StencilOp sbp36CompositeDissipation() {
+  StencilOp op;
+  op.symmetryType = SYMMETRIC;
+  op.interiorWidth = 7; op.boundaryWidth = 9; op.boundaryDepth = 6;
+  op.allocate();
+  const double in[4] = {-20.0, 15.0, -6.0, 1.0};
+  for (int j = 0; j <= 3; ++j) op.in(j) = in[j] / 64.0;
+  for (int j = 1; j <= 3; ++j) op.in(-j) = op.in(j);
+  op.normBoundary = {13649.0 / 43200.0, 12013.0 / 8640.0, 2711.0 / 4320.0,
+                     5359.0 / 4320.0,   7877.0 / 8640.0,  43801.0 / 43200.0};
+  const BoundaryRow rows[6] = {
+      {1, 1, 4, {-129600.0 / 13649.0, 388800.0 / 13649.0, -388800.0 / 13649.0, 129600.0 / 13649.0}},
+      {2, 1, 5, {77760.0 / 12013.0, -241920.0 / 12013.0, 259200.0 / 12013.0, -103680.0 / 12013.0,
+                 8640.0 / 12013.0}},
+      {3, 1, 6, {-38880.0 / 2711.0, 129600.0 / 2711.0, -159840.0 / 2711.0, 90720.0 / 2711.0,
+                 -25920.0 / 2711.0, 4320.0 / 2711.0}},
+      {4, 1, 7, {12960.0 / 5359.0, -51840.0 / 5359.0, 90720.0 / 5359.0, -95040.0 / 5359.0, 64800.0 / 5359.0,
+                 -25920.0 / 5359.0, 4320.0 / 5359.0}},
+      {5, 2, 7, {8640.0 / 7877.0, -51840.0 / 7877.0, 129600.0 / 7877.0, -172800.0 / 7877.0, 129600.0 / 7877.0,
+                 -51840.0 / 7877.0, 8640.0 / 7877.0}},
+      {6, 3, 7, {43200.0 / 43801.0, -259200.0 / 43801.0, 648000.0 / 43801.0, -864000.0 / 43801.0,
+                 648000.0 / 43801.0, -259200.0 / 43801.0, 43200.0 / 43801.0}}};
+  setRows(op, rows, 6);
+  for (double& v : op.rb1) v = v / 64.0;
+  op.fillRightBoundary();
+  return op;
+}
+
+// "SBP 3-6 dissipation", :1545-1561: ASYMMETRIC, rhsInterior(-2:1), with an
+// explicit right boundary.
+StencilOp sbp36Dissipation() {
+  StencilOp op;
+  op.symmetryType = ASYMMETRIC;
+  op.interiorWidth = 4; op.boundaryWidth = 4; op.boundaryDepth = 2;
+  op.allocate();
+  op.lo = -2;
+  const double in[4] = {-1.0, 3.0, -3.0, 1.0};
+  for (int j = -2; j <= 1; ++j) op.in(j) = in[j + 2];
+  for (int m = 1; m <= 2; ++m)
+    for (int k = 1; k <= 4; ++k) op.b1(k, m) = op.in(k - 3);
+  for (int m = 1; m <= 2; ++m)
+    for (int k = 1; k <= 4; ++k) op.b2(k, m) = -op.b1(5 - k, m);
+  return op;
+}
+
+// "SBP 3-6 dissipation transpose", :1563-1585: ASYMMETRIC, rhsInterior(-1:2).
+StencilOp sbp36DissipationTranspose() {
+  StencilOp op;
+  op.symmetryType = ASYMMETRIC;
+  op.interiorWidth = 4; op.boundaryWidth = 6; op.boundaryDepth = 4;
+  op.allocate();
+  op.lo = -1;
+  const double in[4] = {1.0, -3.0, 3.0, -1.0};
+  for (int j = -1; j <= 2; ++j) op.in(j) = in[j + 1];
+  // rhsBoundary1(k, 1:4) = rhsInterior(2:-1:-1) for k = 1..3, then shorter rows
+  for (int k = 1; k <= 3; ++k)
+    for (int m = 1; m <= 4; ++m) op.b1(k, m) = op.in(3 - m);
+  for (int m = 2; m <= 4; ++m) op.b1(4, m) = op.in(4 - m);
+  for (int m = 3; m <= 4; ++m) op.b1(5, m) = op.in(5 - m);
+  op.b1(6, 4) = op.in(2);
+  // rhsBoundary2
+  for (int m = 1; m <= 4; ++m) op.b2(6, m) = op.in(3 - m);
+  for (int m = 1; m <= 4; ++m) op.b2(5, m) = op.in(3 - m);
+  for (int m = 2; m <= 4; ++m) op.b2(4, m) = op.in(m - 3);
+  for (int m = 3; m <= 4; ++m) op.b2(3, m) = op.in(m - 4);
+  op.b2(2, 4) = op.in(-1);
+  for (int m = 1; m <= 4; ++m) op.b2(1, m) = 0.0;
+  return op;
+}
+
+// The operators of one discretization_scheme (MGD_SBP_*).
+StencilOp firstDerivativeOf(int scheme) {
+  switch (scheme) {
+    case MGD_SBP_12: return sbp12FirstDerivative();
+    case MGD_SBP_24: return sbp24FirstDerivative();
+    case MGD_SBP_36: return sbp36FirstDerivative();
+    default: return sbp48FirstDerivative();
+  }
+}
+StencilOp compositeDissipationOf(int scheme) {
+  switch (scheme) {
+    case MGD_SBP_12: return sbp12CompositeDissipation();
+    case MGD_SBP_24: return sbp24CompositeDissipation();
+    case MGD_SBP_36: return sbp36CompositeDissipation();
+    default: return sbp48CompositeDissipation();
+  }
+}
+StencilOp dissipationOf(int scheme) {
+  switch (scheme) {
+    case MGD_SBP_24: return sbp24Dissipation();
+    case MGD_SBP_36: return sbp36Dissipation();
+    default: return sbp48Dissipation();
+  }
+}
+StencilOp dissipationTransposeOf(int scheme) {
+  switch (scheme) {
+    case MGD_SBP_24: return sbp24DissipationTranspose();
+    case MGD_SBP_36: return sbp36DissipationTranspose();
+    default: return sbp48DissipationTranspose();
+  }
+}
+
 // getAdjointOperator, src/StencilOperatorImpl.f90:2285-2372: H^-1 D^T H.
 StencilOp adjointOf(const StencilOp& d) {
   StencilOp a;
@@ -2556,9 +2797,15 @@ int orc_add_block(void* h, const mgd_block_desc* d, const double* coords, const 
   b.isCurvilinear = R.o.curvilinear != 0;
   b.coordinates.assign(coords, coords + b.N * R.nD);
   b.iblank.assign(iblank, iblank + b.N);
-  auto d1 = orc::sbp48FirstDerivative();
-  auto diss = R.o.composite_dissipation ? orc::sbp48CompositeDissipation() : orc::sbp48Dissipation();
-  auto dissT = orc::sbp48DissipationTranspose();
+  // defaults/discretization_scheme (src/SolverOptionsImpl.f90:95, src/GridImpl.f90 setupOperator calls)
+  const int scheme = R.o.discretization_scheme;
+  if (scheme == MGD_SBP_12 && R.o.dissipation && !R.o.composite_dissipation) {
+    R.error = "SBP 1-2 has no non-composite dissipation operator";
+    return 1;
+  }
+  auto d1 = orc::firstDerivativeOf(scheme);
+  auto diss = R.o.composite_dissipation ? orc::compositeDissipationOf(scheme) : orc::dissipationOf(scheme);
+  auto dissT = orc::dissipationTransposeOf(scheme);
   for (int i = 0; i < R.nD; ++i) {
     orc::StencilOp a = d1, ad = orc::adjointOf(d1), di = diss, dt = dissT;
     orc::updateOperator(a, d->periodicity_type[i]);
@@ -2792,12 +3039,18 @@ int orc_get_gradient(void* h, double* dst, long long nEntries) {
 // Operator tables for the coefficient tests: which = 0 first derivative,
 // 1 adjoint first derivative, 2 dissipation, 3 dissipation transpose,
 // 4 composite dissipation.
+// The scheme is which / 8 (MGD_SBP_*), the operator which % 8.
+static orc::StencilOp operatorOf(int which) {
+  const int scheme = which / 8, k = which % 8;
+  orc::StencilOp d1 = orc::firstDerivativeOf(scheme);
+  return k == 0 ? d1 : k == 1 ? orc::adjointOf(d1)
+         : k == 2 ? orc::dissipationOf(scheme)
+         : k == 3 ? orc::dissipationTransposeOf(scheme) : orc::compositeDissipationOf(scheme);
+}
+
 int orc_operator_info(int which, int* dims /* symmetry, iw, bw, bd */, double* interior,
                       double* rb1, double* norm) {
-  orc::StencilOp d1 = orc::sbp48FirstDerivative();
-  orc::StencilOp op = which == 0 ? d1 : which == 1 ? orc::adjointOf(d1)
-                      : which == 2 ? orc::sbp48Dissipation()
-                      : which == 3 ? orc::sbp48DissipationTranspose() : orc::sbp48CompositeDissipation();
+  orc::StencilOp op = operatorOf(which);
   dims[0] = op.symmetryType; dims[1] = op.interiorWidth; dims[2] = op.boundaryWidth; dims[3] = op.boundaryDepth;
   if (interior) std::copy(op.interior.begin(), op.interior.end(), interior);
   if (rb1) std::copy(op.rb1.begin(), op.rb1.end(), rb1);
@@ -2807,10 +3060,7 @@ int orc_operator_info(int which, int* dims /* symmetry, iw, bw, bd */, double* i
 
 // Applies one operator along direction dir of an (n0,n1,n2) array in place.
 int orc_apply_operator(int which, int periodicity, double* x, int ncomp, const int* gs, int dir) {
-  orc::StencilOp d1 = orc::sbp48FirstDerivative();
-  orc::StencilOp op = which == 0 ? d1 : which == 1 ? orc::adjointOf(d1)
-                      : which == 2 ? orc::sbp48Dissipation()
-                      : which == 3 ? orc::sbp48DissipationTranspose() : orc::sbp48CompositeDissipation();
+  orc::StencilOp op = operatorOf(which);
   orc::updateOperator(op, periodicity);
   int g[3] = {gs[0], gs[1], gs[2]};
   orc::apply(op, x, ncomp, g, dir);

@@ -1,4 +1,5 @@
-"""Generates tests/golden/sbp48_first_derivative.npz from the reference's own
+"""Generates tests/golden/sbp48_first_derivative.npz (SBP 4-8) and
+tests/golden/sbp_first_derivative_schemes.npz (SBP 1-2, 2-4, 3-6) from the reference's own
 Python SBP implementation (magudi_utils/SummationByParts.py, function
 `derivative`), run unmodified from the magudi source tree.
 
@@ -46,6 +47,17 @@ def main(magudi_root):
     out["dx_sin"] = np.asarray(derivative(s.view(_TupleIndexed), order=1, axis=0, scheme="SBP 4-8"))
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "sbp48_first_derivative.npz")
     np.savez(path, **out)
+    print("wrote", path)
+    # the other schemes of the same function, one random input per size
+    other = {}
+    for scheme in ("SBP 1-2", "SBP 2-4", "SBP 3-6"):
+        tag = scheme.replace("SBP ", "").replace("-", "")
+        for n in (24, 37):
+            x = rng.standard_normal((n, 3))
+            other[f"s{tag}_x_{n}"] = x
+            other[f"s{tag}_dx_{n}"] = np.asarray(derivative(x.view(_TupleIndexed), order=1, axis=0, scheme=scheme))
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "sbp_first_derivative_schemes.npz")
+    np.savez(path, **other)
     print("wrote", path)
 
 

@@ -73,10 +73,12 @@ def set_threads(n, variant="strict"):
     return lib(variant).orc_set_threads(n)
 
 
-def operator(which):
-    """(symmetry, interior, rhsBoundary1 (width, depth) array, normBoundary)."""
+def operator(which, scheme=capi.SBP_48):
+    """(symmetry, interior, rhsBoundary1 (width, depth) array, normBoundary) of
+    operator `which` of the SBP scheme (capi.SBP_*)."""
     L = lib()
     dims = (C.c_int * 4)()
+    which = which + 8 * scheme
     L.orc_operator_info(which, dims, None, None, None)
     sym, iw, bw, bd = list(dims)
     interior = np.zeros(iw)
@@ -86,13 +88,14 @@ def operator(which):
     return sym, interior, rb1.reshape(bd, bw).T, norm[:nn]
 
 
-def apply_operator(which, x, grid_size, direction, periodicity=0):
-    """Applies operator `which` (0 D, 1 D-adjoint, 2 dissipation, 3 its transpose)
-    along `direction` (0-based) to x of shape (nc, N); returns a new array."""
+def apply_operator(which, x, grid_size, direction, periodicity=0, scheme=capi.SBP_48):
+    """Applies operator `which` (0 D, 1 D-adjoint, 2 dissipation, 3 its
+    transpose, 4 composite dissipation) of the SBP scheme (capi.SBP_*) along
+    `direction` (0-based) to x of shape (nc, N); returns a new array."""
     y = np.ascontiguousarray(x, dtype=np.float64).copy()
     gs = (C.c_int * 3)(*grid_size)
     nc = y.shape[0] if y.ndim == 2 else 1
-    lib().orc_apply_operator(which, periodicity, capi.dptr(y), nc, gs, direction)
+    lib().orc_apply_operator(which + 8 * scheme, periodicity, capi.dptr(y), nc, gs, direction)
     return y
 
 
