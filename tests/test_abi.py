@@ -87,3 +87,50 @@ def test_header_is_strict_c_and_cxx(tmp_path, compiler, std):
     src = tmp_path / f"use.{ext}"
     src.write_text(f'#include "{HEADER}"\nint main(void) {{ mgd_ctx* c = 0; (void)c; return 0; }}\n')
     subprocess.check_call([compiler, std, "-pedantic", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", str(src)])
+
+
+def _fortran_types(path):
+    """Fields of every bind(C) derived type in a Fortran source: name ->
+    [(field, kind, count)]."""
+    import re as _re
+    text = open(path).read()
+    out = {}
+    for m in _re.finditer(r"type, bind\(C\) :: (\w+)(.*?)end type", text, _re.S):
+        fields = []
+        for line in m.group(2).splitlines():
+            line = line.strip()
+            f = _re.match(r"(integer\(c_int\)|real\(c_double\)|character\(kind=c_char\)|type\(c_ptr\)) :: (\w+)"
+                          r"(?:\((\w+)\))?$", line)
+            if f:
+                fields.append((f.group(2), f.group(1), f.group(3)))
+        out[m.group(1)] = fields
+    return out
+
+
+def test_fortran_binding_mirrors_the_header():
+    """include/magudi_gb300.f90 (the ISO_C_BINDING module a Fortran caller
+    uses): its bind(C) types list the C structs' fields in the same order
+    with the same C types, and every bind(C) function names an entry point
+    of the header. (No Fortran compiler here: the check is textual.)"""
+    import ctypes as C
+    path = os.path.join(ROOT, "include", "magudi_gb300.f90")
+    types = _fortran_types(path)
+    kinds = {C.c_int: "integer(c_int)", C.c_double: "real(c_double)", C.c_char: "character(kind=c_char)",
+             C.c_void_p: "type(c_ptr)"}
+    for cname, pyt in (("mgd_options", capi.Options), ("mgd_block_desc", capi.BlockDesc),
+                       ("mgd_patch_desc", capi.PatchDesc), ("mgd_acoustic_source", capi.AcousticSource)):
+        ours = types[cname]
+        assert [f[0] for f in ours] == [f[0] for f in pyt._fields_], cname
+        for (fname, fkind, _), (_, ctype) in zip(ours, pyt._fields_):
+            if issubclass(ctype, C._Pointer):
+                base = C.c_void_p
+            elif issubclass(ctype, C.Array):
+                base = ctype._type_
+            else:
+                base = ctype
+            assert fkind == kinds[base], (cname, fname)
+    names = set(re.findall(r'bind\(C, name="(\w+)"\)', open(path).read())) - {"strlen"}
+    declared = set(declared_functions()) | {"mgd_last_error"}
+    assert names and names <= declared, names - declared
+    region = open(os.path.join(ROOT, "include", "RegionGB300.f90")).read()
+    assert "t_Region%computeRhs" in region and "mgd_compute_rhs(" in region
