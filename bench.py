@@ -53,15 +53,19 @@ def parse():
     ap.add_argument("--cpu-warmup-rk-steps", type=int, default=20,
                     help="RK4 steps of each warm-up sample of the CPU legs (--impl reference)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-other-workloads", action="store_true",
+                    help="skip the Taylor-Green and jet samples of the default line")
     ap.add_argument("--rk-steps", type=int, default=N_STEPS,
                     help="RK4 steps per gradient evaluation (profiling runs use a few)")
-    ap.add_argument("--workload", default="gradient", choices=["gradient", "sweep", "tgv", "jet", "msgrad", "tangent"],
+    ap.add_argument("--workload", default="gradient",
+                    choices=["gradient", "sweep", "tgv", "jet", "msgrad", "tangent", "fdcheck"],
                     help="gradient: the forward + adjoint gradient evaluation (default); sweep: the batched "
                          "gradient-check sweep of 64 monopole instances of mixed grid sizes; tgv: the 3D "
                          "Taylor-Green vortex forward + adjoint (terminal kinetic energy, constant CFL); jet: "
                          "the three-block curvilinear 3D jet forward + adjoint; msgrad: the monopole gradient with "
                          "the 960 steps split into --ms-segments time segments run concurrently; tangent: the "
-                         "monopole forward run followed by the linearized (tangent) run along it")
+                         "monopole forward run followed by the linearized (tangent) run along it; fdcheck: the "
+                         "reference's gradient-accuracy table at 201x201 x 960 steps, the 20 amplitudes as one batch")
     ap.add_argument("--ms-segments", type=int, default=8)
     ap.add_argument("--tgv-n", type=int, default=256)
     ap.add_argument("--tgv-steps", type=int, default=10, help="RK4 steps of the Taylor-Green sample (of the 2000-step run)")
@@ -102,9 +106,17 @@ def problem(n_steps=N_STEPS):
     return configs.monopole_2d(n=GRID, n_steps=n_steps, save_interval=SAVE_INTERVAL)
 
 
+def _tuned_flags():
+    try:
+        return open(os.path.join(ROOT, "oracle", "_build", "tuned_flags.txt")).read().strip()
+    except OSError:
+        return ""
+
+
 CPU_LEGS = {
     "strict": "oracle/oracle.cpp built -O3 -fno-fast-math -ffp-contract=off -fopenmp (the parity checker)",
-    "tuned": "oracle/oracle.cpp built with the reference's release flags -O3 -ffast-math -funroll-loops -fopenmp",
+    "tuned": ("oracle/oracle.cpp built with the reference's release flags -O3 -ffast-math -funroll-loops "
+              + (_tuned_flags() + " " if _tuned_flags() else "") + "-fopenmp"),
 }
 
 
@@ -301,6 +313,93 @@ def run_reference(args):
         "e2e": {"value": value, "unit": "Mpt-RHS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def other_workloads(torch, steps=2, warmup=1):
+    """Configs 3 and 5 beside the headline line, each as a bounded sample:
+    the 256^3 Taylor-Green vortex (10 of its 2000 constant-CFL steps,
+    forward + adjoint of the terminal kinetic energy) and the three-block
+    curvilinear jet at half its linear size (4.9 M points, 8 of its 1000
+    steps, forward + adjoint). Each reports its device-timed Mpt-RHS/s (RHS
+    evaluations of the forward and adjoint passes), the strict oracle's rate
+    and the GPU-vs-oracle parity of J and the adjoint state on a reduced grid
+    of the same problem (the oracle on the full grids would take hours)."""
+    import numpy as np
+    from magudi_gb300 import capi, configs
+    from magudi_gb300.solver import Solver
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    oracle_lib.set_threads(os.cpu_count())
+    out = {}
+
+    def rel(a, b):
+        return float(np.linalg.norm(np.ravel(a) - np.ravel(b)) / np.linalg.norm(np.ravel(b)))
+
+    def timed(P, n_steps, S):
+        s = Solver(P)
+        q0 = [b.initial_state for b in P.blocks]
+
+        def step():
+            for bi, q in enumerate(q0, start=1):
+                s.set_field(bi, capi.FIELD_CONSERVED, q)
+            J = s.run_forward(n_steps, S)
+            G = s.run_adjoint()
+            return J, G
+
+        for _ in range(warmup):
+            step()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(steps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            J, G = step()
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t)
+        pts = sum(b.n_points for b in P.blocks)
+        sec = statistics.mean(ts)
+        s.close()
+        return {"value": pts * 8 * n_steps / sec / 1e6, "unit": "Mpt-RHS/s", "seconds_per_sample": sec,
+                "grid_points": pts, "rk4_steps": n_steps, "save_interval": S, "J": J}
+
+    def parity_and_cpu(Pg, Po, n_steps, S, adjoint_field=True):
+        g, o = Solver(Pg), oracle_lib.Oracle(Po)
+        Jg = g.run_forward(n_steps, S)
+        t = time.perf_counter()
+        Jo = o.run_forward(n_steps, S)
+        o.run_adjoint()
+        sec = time.perf_counter() - t
+        g.run_adjoint()
+        lam = rel(np.concatenate([g.get_field(b, capi.FIELD_ADJOINT).ravel() for b in range(1, len(Pg.blocks) + 1)]),
+                  np.concatenate([o.get_field(b, capi.FIELD_ADJOINT).ravel() for b in range(1, len(Po.blocks) + 1)]))
+        pts = sum(b.n_points for b in Po.blocks)
+        g.close()
+        return ({"J_rel": abs(Jg - Jo) / abs(Jo), "adjoint_state_rel": lam, "grid_points": pts, "rk4_steps": n_steps,
+                 "tolerance": 1e-10},
+                {"value": pts * 8 * n_steps / sec / 1e6, "unit": "Mpt-RHS/s", "cores": os.cpu_count(), "kind": "port",
+                 "build": "strict", "sample": f"oracle on {pts} points, {n_steps} RK4 steps forward + adjoint "
+                                              f"({sec:.1f} s)"})
+
+    progress("config 3: Taylor-Green 256^3 sample")
+    tgv = timed(configs.taylor_green_3d(n=256, n_steps=10, save_interval=5), 10, 5)
+    small = configs.taylor_green_3d(n=32, n_steps=10, save_interval=5)
+    par, cpu = parity_and_cpu(small, configs.taylor_green_3d(n=32, n_steps=10, save_interval=5), 10, 5)
+    tgv.update({"workload": "3D Taylor-Green vortex 256^3, PLANE-periodic, Re 1600, M 0.1, constant CFL 0.5, "
+                            "forward + adjoint of the terminal kinetic energy: 10 of the 2000 steps",
+                "parity_reduced": par, "cpu_baseline_reduced": cpu})
+    out["taylor_green_256"] = tgv
+    progress("config 5: three-block jet sample")
+    dims = dict(nx=192, ny_core=96, ny_side=86, nz=96)
+    jet = timed(configs.jet_3block_3d(n_steps=8, save_interval=4, **dims), 8, 4)
+    tiny = dict(nx=40, ny_core=25, ny_side=25, nz=25)
+    par, cpu = parity_and_cpu(configs.jet_3block_3d(n_steps=4, save_interval=2, **tiny),
+                              configs.jet_3block_3d(n_steps=4, save_interval=2, **tiny), 4, 2)
+    jet.update({"workload": "3D three-block curvilinear jet at half the linear size of the 39.4 M-point case "
+                            "(192x96x96 + 2 x 192x86x96), Mach 1.3, Re 2500, solenoidal inflow excitation, "
+                            "block-interface SATs: 8 of the 1000 steps, forward + adjoint",
+                "parity_reduced": par, "cpu_baseline_reduced": cpu})
+    out["jet_three_block_half"] = jet
+    return out
 
 
 def run_ours(args):
@@ -524,6 +623,12 @@ def run_ours(args):
             "legs": {k: {"value": v["value"], "seconds": v["seconds"], "flags": CPU_LEGS[k],
                          "J_rel_vs_strict": abs(v["J"] - legs["strict"]["J"]) / abs(legs["strict"]["J"])}
                      for k, v in legs.items()}}
+    if rank == 0 and world == 1 and not args.no_other_workloads:
+        # release the 201x201 context (its trajectory holds about 22 GB) first
+        s.close()
+        del s
+        torch.cuda.empty_cache()
+        line["other_workloads"] = other_workloads(torch)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -571,6 +676,18 @@ def run_sweep(args):
         for s, q in zip(solvers, q0):
             s.set_field(1, capi.FIELD_CONSERVED, q)
 
+    # the per-step graph path of the same batch, timed once beside the
+    # persistent single launch (the default)
+    batch.persistent(0)
+    reset()
+    batch.run_forward(n_steps)
+    reset()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    graph_costs = batch.run_forward(n_steps)
+    torch.cuda.synchronize()
+    t_graph = time.perf_counter() - t
+    batch.persistent(1)
     for _ in range(args.warmup):
         reset()
         batch.run_forward(n_steps)
@@ -621,11 +738,17 @@ def run_sweep(args):
         "data": "synthetic (quiescent monopole states, gradient-direction control forcing computed in-process)",
         "config": {"workload": f"{len(cases)} 2D monopole instances, sizes drawn with seed 0 from "
                                f"{list(sweep.SIZES)} (squared), control amplitude 10^(-2-0.25k), k = i mod 20, "
-                               f"{n_steps} RK4 steps forward each, one batched launch per stage kernel",
+                               f"{n_steps} RK4 steps forward each, all steps of all instances in one persistent "
+                               f"launch",
                    "instances": len(cases), "rk4_steps": n_steps, "total_points": pts,
                    "l2": "working set (all instances) larger than L2",
                    "parallelism": f"instances sharded round-robin over {world} GPU(s)" if world > 1 else "single GPU"},
         "mpt_rhs_per_s": pts * 4 * n_steps / sec / 1e6,
+        "launch": {"mode": "one persistent cooperative launch for all steps, captured in a CUDA graph",
+                   "ctas": batch.persistent_grid()},
+        "per_step_graphs": {"value": len(cases) / t_graph, "unit": "solves/s", "seconds": t_graph,
+                            "max_rel_diff_J": max(abs(a - b) / abs(b) for a, b in zip(graph_costs, costs)),
+                            "path": "one CUDA graph of batched stage kernels per RK4 step"},
         "plain_single_solve": {"value": len(cases) / t_plain, "unit": "solves/s", "seconds": t_plain,
                                "path": "mgd_run_forward per instance, one after another"},
         "speedup_vs_plain": t_plain / sec,
@@ -643,6 +766,58 @@ def run_sweep(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_fdcheck(args):
+    """The reference's gradient-accuracy procedure (README.md:118-165) at the
+    headline configuration: the 201x201 monopole, 960 RK4 steps, checkpoints
+    every 10 steps. One forward + adjoint run gives J0, Grad0 and the control
+    gradient g; then one batch runs the forward with the control forcing
+    A_k g for A_k = 10^(-2-0.25k), k = 0..19 (bin/ZAXPY.f90 on the device),
+    plus A = 0, and the line reports the reference's table: A_k, J_k,
+    (J_k - J0)/A_k and its relative error against Grad0."""
+    import torch
+    from magudi_gb300 import configs, sweep
+    from magudi_gb300.solver import Batch, Solver
+
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    n_steps = args.rk_steps
+    P = configs.monopole_2d(n=GRID, n_steps=n_steps, save_interval=SAVE_INTERVAL)
+    base = Solver(P)
+    t = time.perf_counter()
+    J0 = base.run_forward(n_steps, SAVE_INTERVAL)
+    G0 = base.run_adjoint()
+    g = base.gradient(4 * n_steps)
+    t_grad = time.perf_counter() - t
+    amps = [0.0] + [10.0 ** (-2.0 - 0.25 * k) for k in range(20)]
+    solvers = []
+    for a in amps:
+        Pc = configs.monopole_2d(n=GRID, n_steps=n_steps, save_interval=SAVE_INTERVAL, controller_switch=True)
+        s = Solver(Pc)
+        s.set_control_forcing(a * g)
+        solvers.append(s)
+    batch = Batch(solvers)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    costs = batch.run_forward(n_steps)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t
+    J0b = costs[0]
+    rows = sweep.fd_errors(J0b, G0, amps[1:], costs[1:])
+    best = min(r[3] for r in rows)
+    line = {
+        "metric": "gradient accuracy (FD sweep)", "value": best, "unit": "min relative error",
+        "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": (t_grad + t_batch) * 1e3, "higher_is_better": False,
+        "dtype": "f64", "data": "synthetic (quiescent monopole)",
+        "config": {"workload": f"2D acoustic monopole {GRID}x{GRID}, {n_steps} RK4 steps, checkpoints every "
+                               f"{SAVE_INTERVAL}: adjoint gradient, then the forward with control forcing A_k g, "
+                               f"A_k = 10^(-2-0.25k), k = 0..19, as one batch of {len(amps)} instances"},
+        "J0": J0, "J0_batch": J0b, "grad0": G0, "gradient_seconds": t_grad, "batch_seconds": t_batch,
+        "table": [{"A": a, "J": J, "fd_gradient": fdg, "rel_error": e} for a, J, fdg, e in rows],
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 def run_tgv(args):
@@ -956,6 +1131,8 @@ def main():
         run_msgrad(args)
     elif args.workload == "tangent":
         run_tangent(args)
+    elif args.workload == "fdcheck":
+        run_fdcheck(args)
     else:
         run_ours(args)
 

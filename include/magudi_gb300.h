@@ -362,6 +362,14 @@ int mgd_batch_create(mgd_ctx* const* instances, int n_instances, mgd_batch** bat
 int mgd_batch_run_forward(mgd_batch* batch, int n_steps, double t0, double* costs);
 int mgd_batch_destroy(mgd_batch* batch);
 const char* mgd_batch_last_error(const mgd_batch* batch);
+/* How a batch runs (no reference counterpart): mode 1 (the default) runs
+ * all steps of mgd_batch_run_forward as one persistent cooperative launch,
+ * captured in a CUDA graph, with grid barriers between the stage phases;
+ * mode 0 launches one graph of batched stage kernels per step; other values
+ * only report. Returns the mode in effect. Both give the same costs. */
+int mgd_batch_persistent(mgd_batch* batch, int mode);
+/* CTAs of the persistent launch (co-resident on the device). */
+int mgd_batch_persistent_grid(mgd_batch* batch);
 long long mgd_batch_kernel_launches(mgd_batch* batch, int reset);
 
 /* ---- files around the hot path (host code; no GPU needed) ---- */
@@ -422,6 +430,17 @@ int mgd_profile_stage_kernels(mgd_ctx* ctx, int mode, int reps, double* avg_ms, 
  * device with the library's table-driven power function (fast) and with
  * CUDA's pow (ref), for checking the viscosity law's error bound. */
 int mgd_selftest_pow(const double* x, int n, double e, double* fast, double* ref);
+
+/* Self-test of the grid barrier of the persistent batched kernel (no
+ * reference counterpart): a cooperative launch of n_blocks CTAs meets
+ * `rounds` times at a barrier that expects `expected` arrivals; after each
+ * meeting CTA 0 sums stamps the others wrote before it, into *checksum
+ * (rounds (rounds + 1) / 2 * n_blocks (n_blocks + 1) / 2 when every round
+ * completes). A wait gives up after `limit` polls of about 100 ns: with
+ * expected > n_blocks no round completes and *status = 1 (0 otherwise);
+ * the kernel then returns and the context stays usable. */
+int mgd_selftest_grid_barrier(int n_blocks, int expected, int rounds, long long limit, int* status,
+                              long long* checksum);
 
 /* Forward RHS without any device allocation (no counterpart in the
  * reference). For callers that must not allocate device memory when they

@@ -2945,6 +2945,12 @@ int mgd_profile_stage_kernels(mgd_ctx* h, int mode, int reps, double* avg_ms, in
 
 // Self-test of the table-driven power function used by the viscosity law:
 // evaluates x[i]^e with it (fast) and with CUDA's pow (ref) on the current device.
+int mgd_selftest_grid_barrier(int n_blocks, int expected, int rounds, long long limit, int* status,
+                              long long* checksum) {
+  if (n_blocks < 1 || expected < 1 || rounds < 1 || limit < 1 || !status || !checksum) return 1;
+  return selftestGridBarrier(n_blocks, (unsigned int)expected, rounds, limit, status, checksum) ? 1 : 0;
+}
+
 int mgd_selftest_pow(const double* x, int n, double e, double* fast, double* ref) {
   if (n <= 0) return 0;
   double *dx = nullptr, *df = nullptr, *dr = nullptr;

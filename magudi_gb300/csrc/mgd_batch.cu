@@ -33,6 +33,17 @@ struct mgd_batch {
   int* dCounters = nullptr;
   cudaGraphExec_t graph = nullptr;
   long long nodes = 0, launches = 0;
+  // persistent run: one cooperative launch of all steps (default), captured
+  // in a graph per step count
+  bool persistent = true;
+  int4* dUnitsA = nullptr;
+  unsigned int* dBarrier = nullptr;
+  int* dStatus = nullptr;
+  PersistentPlan plan;
+  int persistentGrid = 0;
+  cudaGraphExec_t graphP = nullptr;
+  int graphPSteps = 0;
+  bool graphPCaptured = false;
 };
 
 static int bfail(mgd_batch* b, const std::string& m) {
@@ -63,6 +74,10 @@ static bool sameOptions(const mgd_options& a, const mgd_options& b) {
 static void destroyBatch(mgd_batch* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->graphP) cudaGraphExecDestroy(b->graphP);
+  cudaFree(b->dUnitsA);
+  cudaFree(b->dBarrier);
+  cudaFree(b->dStatus);
   cudaFree(b->dEntries);
   for (int k = 0; k < BK_COUNT; ++k) cudaFree(b->dMap[k]);
   cudaFree(b->dCounters);
@@ -99,6 +114,10 @@ int mgd_batch_create(mgd_ctx* const* instances, int n_instances, mgd_batch** out
     }
     if (!c.blocks[0].exc.empty()) {
       g_batchCreateError = "batched runs do not take solenoidal-excitation patches";
+      return 1;
+    }
+    if (c.opts.enable_solution_limits) {
+      g_batchCreateError = "batched runs do not check solution limits; run the instance with mgd_run_forward";
       return 1;
     }
   }
@@ -173,7 +192,88 @@ int mgd_batch_create(mgd_ctx* const* instances, int n_instances, mgd_batch** out
     return 1;
   }
   b->L.entries = b->dEntries;
+  // work of the persistent run: phase A = gradient/flux tiles, dissipation
+  // (tile, component) pairs, functional blocks (heaviest first); phase B =
+  // the divergence tiles (the BK_RHS map)
+  {
+    std::vector<int4> unitsA;
+    const int nU = c0.nU;
+    for (int i = 0; i < n_instances; ++i)
+      for (int j = 0; j < b->tiles[i][BK_GRAD].blocks(); ++j) unitsA.push_back(make_int4(0, i, j, 0));
+    if (c0.phys.dissipation)
+      for (int i = 0; i < n_instances; ++i)
+        for (int j = 0; j < b->tiles[i][BK_DISS].blocks(); ++j)
+          for (int cc = 0; cc < nU; ++cc) unitsA.push_back(make_int4(1, i, j, cc));
+    for (int i = 0; i < n_instances; ++i)
+      for (int j = 0; j < reductionBlocks(b->inst[i]->c.blocks[0]); ++j) unitsA.push_back(make_int4(2, i, j, 0));
+    if (cudaMalloc((void**)&b->dUnitsA, unitsA.size() * sizeof(int4)) != cudaSuccess ||
+        cudaMemcpy(b->dUnitsA, unitsA.data(), unitsA.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMalloc((void**)&b->dBarrier, 2 * sizeof(unsigned int)) != cudaSuccess ||
+        cudaMalloc((void**)&b->dStatus, sizeof(int)) != cudaSuccess) {
+      g_batchCreateError = "device allocation failed for the persistent run";
+      destroyBatch(b);
+      return 1;
+    }
+    b->plan.unitsA = b->dUnitsA;
+    b->plan.nA = (int)unitsA.size();
+    b->plan.unitsB = b->dMap[BK_RHS];
+    b->plan.nB = b->L.blocks[BK_RHS];
+    b->plan.barrier = b->dBarrier;
+    b->plan.status = b->dStatus;
+    // about 100 ns per poll: a wait gives up after about a second (a stage
+    // phase of the largest batches takes milliseconds)
+    b->plan.spinLimit = 1LL << 23;
+    b->persistentGrid = std::min(persistentGridSize(c0), std::max(b->plan.nA, b->plan.nB));
+    if (b->persistentGrid < 1) b->persistent = false;
+  }
   *out = b;
+  return 0;
+}
+
+int mgd_batch_persistent(mgd_batch* batch, int mode) {
+  if (!batch) return -1;
+  if (mode == 0 || mode == 1) batch->persistent = mode == 1 && batch->persistentGrid > 0;
+  return batch->persistent ? 1 : 0;
+}
+
+int mgd_batch_persistent_grid(mgd_batch* batch) { return batch ? batch->persistentGrid : 0; }
+
+// The persistent run: barrier and status reset, then one cooperative launch
+// of every step, captured once per step count in a graph (launched directly
+// when the capture is refused).
+static int runPersistent(mgd_batch* b, int n_steps, bool functional) {
+  Context& c0 = b->inst[0]->c;
+  BATCH_TRY(b, cudaMemsetAsync(b->dBarrier, 0, 2 * sizeof(unsigned int), b->stream));
+  BATCH_TRY(b, cudaMemsetAsync(b->dStatus, 0, sizeof(int), b->stream));
+  if (!b->graphP || b->graphPSteps != n_steps) {
+    if (b->graphP) cudaGraphExecDestroy(b->graphP);
+    b->graphP = nullptr;
+    b->graphPCaptured = false;
+    cudaGraph_t g = nullptr;
+    const long long before = c0.launches;
+    if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const cudaError_t le = launchBatchPersistent(c0, b->dEntries, b->plan, n_steps, functional, b->persistentGrid,
+                                                   b->stream);
+      const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+      if (le == cudaSuccess && ce == cudaSuccess && g && cudaGraphInstantiate(&b->graphP, g, 0) == cudaSuccess)
+        b->graphPCaptured = true;
+      if (g) cudaGraphDestroy(g);
+    }
+    c0.launches = before;
+    cudaGetLastError();
+    b->graphPSteps = n_steps;
+  }
+  if (b->graphPCaptured) {
+    BATCH_TRY(b, cudaGraphLaunch(b->graphP, b->stream));
+  } else {
+    BATCH_TRY(b, launchBatchPersistent(c0, b->dEntries, b->plan, n_steps, functional, b->persistentGrid, b->stream));
+  }
+  b->launches += 1;
+  BATCH_TRY(b, cudaStreamSynchronize(b->stream));
+  BATCH_TRY(b, cudaGetLastError());
+  int status = 0;
+  BATCH_TRY(b, cudaMemcpy(&status, b->dStatus, sizeof(int), cudaMemcpyDeviceToHost));
+  if (status) return bfail(b, "persistent batched run: a grid-barrier wait ran out of its spin limit");
   return 0;
 }
 
@@ -213,6 +313,14 @@ int mgd_batch_run_forward(mgd_batch* b, int n_steps, double t0, double* costs) {
   BATCH_TRY(b, cudaMemcpyAsync(b->dCounters, init, sizeof init, cudaMemcpyHostToDevice, b->stream));
   Context& c0 = b->inst[0]->c;
   const bool functional = c0.opts.enable_functional != 0;
+  if (b->persistent) {
+    if (runPersistent(b, n_steps, functional)) return 1;
+    for (int i = 0; i < n; ++i) {
+      Context& c = b->inst[i]->c;
+      if (finishForwardRun(c, &costs[i])) return bfail(b, "instance " + std::to_string(i) + ": " + c.error);
+    }
+    return 0;
+  }
   if (!b->graph) {
     const long long before = c0.launches;
     cudaGraph_t g = nullptr;

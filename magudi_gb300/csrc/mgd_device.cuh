@@ -63,7 +63,16 @@ __device__ __forceinline__ int wrapIndex(int i, int n, int per) {
 // Follows applyOperator_{1,2,3} (src/StencilOperatorImpl.f90:35-457):
 // sum over taps left to right, boundary rows from the left block and its
 // (skew-)reflection on the right.
-template <int OP>
+// Load of a stencil tap: through the read-only data path (NC), or from L2
+// (ld.global.cg) for data that the same kernel launch writes elsewhere
+// (the persistent batched kernel), which the non-coherent path may serve stale.
+template <bool NC>
+__device__ __forceinline__ double tap(const double* p) {
+  if constexpr (NC) return __ldg(p);
+  else return __ldcg(p);
+}
+
+template <int OP, bool NC = true>
 __device__ __forceinline__ double applyOp(const double* __restrict__ line, int i, const Axis& ax) {
   using S = OpShape<OP>;
   const double* __restrict__ cin = c_ops.interior[ax.scheme][OP];
@@ -74,9 +83,9 @@ __device__ __forceinline__ double applyOp(const double* __restrict__ line, int i
     if (i < S::depth) {
       // boundary closure rows are rare: keep them compact (few registers)
       const double* __restrict__ row = &g_opLeft[ax.scheme][OP][i * S::width];
-      double s = __ldg(row) * __ldg(line);
+      double s = __ldg(row) * tap<NC>(line);
 #pragma unroll 1
-      for (int k = 1; k < S::width; ++k) s += __ldg(row + k) * __ldg(line + k * st);
+      for (int k = 1; k < S::width; ++k) s += __ldg(row + k) * tap<NC>(line + k * st);
       return s;
     }
     if (i >= ax.n - S::depth) {
@@ -85,38 +94,38 @@ __device__ __forceinline__ double applyOp(const double* __restrict__ line, int i
       if (asym) {
         // explicit right block, columns left to right
         const double* __restrict__ row = &g_opRight[ax.scheme][OP][m * S::width];
-        double s = __ldg(row) * __ldg(end);
+        double s = __ldg(row) * tap<NC>(end);
 #pragma unroll 1
-        for (int k = 1; k < S::width; ++k) s += __ldg(row + k) * __ldg(end + k * st);
+        for (int k = 1; k < S::width; ++k) s += __ldg(row + k) * tap<NC>(end + k * st);
         return s;
       }
       const double* __restrict__ row = &g_opLeft[ax.scheme][OP][m * S::width];
       // right block = reflection of the left block, negated for skew operators
-      double s = __ldg(row + S::width - 1) * __ldg(end);
+      double s = __ldg(row + S::width - 1) * tap<NC>(end);
 #pragma unroll 1
-      for (int k = 1; k < S::width; ++k) s += __ldg(row + S::width - 1 - k) * __ldg(end + k * st);
+      for (int k = 1; k < S::width; ++k) s += __ldg(row + S::width - 1 - k) * tap<NC>(end + k * st);
       return S::skew ? -s : s;
     }
     const double* __restrict__ c = line + (long long)i * st;
     if (S::skew) {
-      double s = cin[S::half + 1] * (__ldg(c + st) - __ldg(c - st));
+      double s = cin[S::half + 1] * (tap<NC>(c + st) - tap<NC>(c - st));
 #pragma unroll
-      for (int j = 2; j <= S::half; ++j) s += cin[S::half + j] * (__ldg(c + j * st) - __ldg(c - j * st));
+      for (int j = 2; j <= S::half; ++j) s += cin[S::half + j] * (tap<NC>(c + j * st) - tap<NC>(c - j * st));
       return s;
     } else if (asym) {
-      double s = cin[0] * __ldg(c - S::half * st);
+      double s = cin[0] * tap<NC>(c - S::half * st);
 #pragma unroll
-      for (int j = 1 - S::half; j <= S::half; ++j) s += cin[S::half + j] * __ldg(c + j * st);
+      for (int j = 1 - S::half; j <= S::half; ++j) s += cin[S::half + j] * tap<NC>(c + j * st);
       return s;
     } else {
-      double s = cin[S::half + 1] * (__ldg(c + st) + __ldg(c - st));
+      double s = cin[S::half + 1] * (tap<NC>(c + st) + tap<NC>(c - st));
 #pragma unroll
-      for (int j = 2; j <= S::half; ++j) s += cin[S::half + j] * (__ldg(c + j * st) + __ldg(c - j * st));
-      return s + cin[S::half] * __ldg(c);
+      for (int j = 2; j <= S::half; ++j) s += cin[S::half + j] * (tap<NC>(c + j * st) + tap<NC>(c - j * st));
+      return s + cin[S::half] * tap<NC>(c);
     }
   }
   // periodic: interior stencil everywhere with wrapped indices
-  auto at = [&](int j) { return __ldg(line + (long long)wrapIndex(i + j, ax.n, ax.per) * st); };
+  auto at = [&](int j) { return tap<NC>(line + (long long)wrapIndex(i + j, ax.n, ax.per) * st); };
   if (asym) {
     double s = cin[0] * at(-S::half);
 #pragma unroll

@@ -350,6 +350,23 @@ struct BatchEntry {
   int controller;
 };
 
+// Work of the persistent batched run (one launch for all steps): phase A
+// units {kind, instance, tile, component} (kind 0 gradient/flux tile, 1
+// dissipation tile and component, 2 functional reduction block), phase B
+// tiles {instance, tile} (divergence and RK update of every component, then
+// the primitives). barrier = {arrivals, generation} of the grid barrier
+// between phases; status = 0, or 1 when a barrier wait ran out of its spin
+// limit (the kernel then returns early and the host reports the error).
+struct PersistentPlan {
+  const int4* unitsA = nullptr;
+  int nA = 0;
+  const int2* unitsB = nullptr;
+  int nB = 0;
+  unsigned int* barrier = nullptr;
+  int* status = nullptr;
+  long long spinLimit = 0;
+};
+
 // Block maps of a batched launch: entry k of a map is (instance, block within
 // the instance) for thread block k.
 enum BatchKernel { BK_GRAD = 0, BK_DISS, BK_RHS, BK_PRIMS, BK_FUNC, BK_COUNT };
@@ -479,6 +496,16 @@ void launchBatchForwardDivergence(Context& c, const BatchLaunch& L, int rkStage,
 void launchBatchPrims(Context& c, const BatchLaunch& L, cudaStream_t s);
 void launchBatchFunctional(Context& c, const BatchLaunch& L, int stage, cudaStream_t s);
 void launchStepAdvanceOn(int* counters, int delta, cudaStream_t s);
+// The whole batched forward run (n_steps RK4 steps of every instance) as one
+// cooperative launch of a persistent kernel with grid barriers between the
+// stage phases, on stream s; `grid` CTAs (at most the co-resident number,
+// persistentGridSize). Returns the launch status.
+cudaError_t launchBatchPersistent(Context& c, const BatchEntry* entries, const PersistentPlan& plan, int nSteps,
+                                  int functional, int grid, cudaStream_t s);
+int persistentGridSize(const Context& c);
+// Grid-barrier self-test (see mgd_selftest_grid_barrier); 0 or a CUDA error.
+int selftestGridBarrier(int nBlocks, unsigned int expected, int rounds, long long limit, int* status,
+                        long long* sum);
 void launchSetCounters(int* counters, int step, int segBase, cudaStream_t s);
 constexpr int kBatchThreads = 128;
 constexpr int kMaxExcitationModes = 256;  // modes of one solenoidal-excitation patch

@@ -363,7 +363,7 @@ enum { GF_FLUX = 1, GF_STRESS = 4, GF_STORE = 8 };
 // lanes then form stress and fluxes, lane d writes the contravariant flux of
 // direction d, and the stores of the stage slot and the SAT vectors are split
 // between the lanes.
-template <int ND, bool CURV, bool VISC, int LANES = 1>
+template <int ND, bool CURV, bool VISC, int LANES = 1, bool NC = true>
 __device__ __forceinline__ void gradFluxPoint(const BlockView& B, const Physics& P, const RunScalars& rs, int flags,
                                               int stage, const Tile& T, int blk) {
   static_assert(LANES == 1 || (LANES == 2 && ND == 2), "two lanes per point only in 2D");
@@ -398,9 +398,9 @@ __device__ __forceinline__ void gradFluxPoint(const BlockView& B, const Physics&
       const long long bd = d ? I.base[1] : I.base[0];
       const int id = d ? I.idx[1] : I.idx[0];
       const Axis ax = d ? B.ax[1] : B.ax[0];
-      const double a0 = applyOp<OP_D1>(B.prim + N * L.u(0) + bd, id, ax);
-      const double a1 = applyOp<OP_D1>(B.prim + N * L.u(1) + bd, id, ax);
-      const double aT = applyOp<OP_D1>(B.prim + N * L.T() + bd, id, ax);
+      const double a0 = applyOp<OP_D1, NC>(B.prim + N * L.u(0) + bd, id, ax);
+      const double a1 = applyOp<OP_D1, NC>(B.prim + N * L.u(1) + bd, id, ax);
+      const double aT = applyOp<OP_D1, NC>(B.prim + N * L.T() + bd, id, ax);
       const unsigned pair = 3u << (threadIdx.x & 30);
       const double b0 = __shfl_xor_sync(pair, a0, 1);
       const double b1 = __shfl_xor_sync(pair, a1, 1);
@@ -412,8 +412,8 @@ __device__ __forceinline__ void gradFluxPoint(const BlockView& B, const Physics&
 #pragma unroll
       for (int d = 0; d < ND; ++d) {
 #pragma unroll
-        for (int c = 0; c < ND; ++c) du[c][d] = applyOp<OP_D1>(B.prim + N * L.u(c) + I.base[d], I.idx[d], B.ax[d]);
-        dT[d] = applyOp<OP_D1>(B.prim + N * L.T() + I.base[d], I.idx[d], B.ax[d]);
+        for (int c = 0; c < ND; ++c) du[c][d] = applyOp<OP_D1, NC>(B.prim + N * L.u(c) + I.base[d], I.idx[d], B.ax[d]);
+        dT[d] = applyOp<OP_D1, NC>(B.prim + N * L.T() + I.base[d], I.idx[d], B.ax[d]);
       }
     }
     double gu[ND][ND], gT[ND];
@@ -568,23 +568,25 @@ __global__ void __launch_bounds__(2 * kMaxTile) kGradFluxPair(BlockView B, Physi
 // thread per point and component. Composite: dq_c = sign * amount * sum_i
 // Dc_i src_c. Non-composite, first sweep: dq_{i,c} = sign * (-amount arc_i) D_i src_c.
 // ---------------------------------------------------------------------------
-template <int ND>
+// comp < 0: the component is blockIdx.y (a launch over (tiles, components)).
+template <int ND, bool NC = true>
 __device__ __forceinline__ void dissipationPoint(const BlockView& B, const Physics& P, const double* __restrict__ src,
-                                                 double sign, const Tile& T, int blk) {
+                                                 double sign, const Tile& T, int blk, int comp = -1) {
   long long p;
   PointIndex I;
   if (!locate(B, T, blk, p, I)) return;
   constexpr int nU = ND + 2;
-  const int c = blockIdx.y;
+  const int c = comp >= 0 ? comp : (int)blockIdx.y;
   const long long N = B.N;
   const double* x = src + N * c;
   if (P.composite) {
-    double s = applyOp<OP_DCOMP>(x + I.base[0], I.idx[0], B.ax[0]);
-    for (int d = 1; d < ND; ++d) s += applyOp<OP_DCOMP>(x + I.base[d], I.idx[d], B.ax[d]);
+    double s = applyOp<OP_DCOMP, NC>(x + I.base[0], I.idx[0], B.ax[0]);
+    for (int d = 1; d < ND; ++d) s += applyOp<OP_DCOMP, NC>(x + I.base[d], I.idx[d], B.ax[d]);
     B.dq[p + N * c] = (sign * P.dissipationAmount) * s;
   } else {
     for (int d = 0; d < ND; ++d)
-      B.dq[p + N * (d * nU + c)] = (sign * B.arcA[p + N * d]) * applyOp<OP_DISS>(x + I.base[d], I.idx[d], B.ax[d]);
+      B.dq[p + N * (d * nU + c)] =
+          (sign * B.arcA[p + N * d]) * applyOp<OP_DISS, NC>(x + I.base[d], I.idx[d], B.ax[d]);
   }
 }
 
@@ -595,14 +597,14 @@ __global__ void __launch_bounds__(kMaxTile) kDissipation(BlockView B, Physics P,
   dissipationPoint<ND>(B, P, src, sign, T, blockIdx.x);
 }
 
-template <int ND>
+template <int ND, bool NC = true>
 __device__ __forceinline__ double dissipationTerm(const BlockView& B, const Physics& P, const PointIndex& I,
                                                   long long p, int c) {
   constexpr int nU = ND + 2;
   const long long N = B.N;
   if (P.composite) return B.dq[p + N * c];
-  double s = applyOp<OP_DISST>(B.dq + N * c + I.base[0], I.idx[0], B.ax[0]);
-  for (int i = 1; i < ND; ++i) s += applyOp<OP_DISST>(B.dq + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
+  double s = applyOp<OP_DISST, NC>(B.dq + N * c + I.base[0], I.idx[0], B.ax[0]);
+  for (int i = 1; i < ND; ++i) s += applyOp<OP_DISST, NC>(B.dq + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
   return s;
 }
 
@@ -611,22 +613,24 @@ __device__ __forceinline__ double dissipationTerm(const BlockView& B, const Phys
 // src/RhsHelperImpl.f90:330-351, src/RegionImpl.f90:1968-2023) fused with
 // that component's RK4 forward stage update (src/RK4IntegratorImpl.f90:104-158).
 // ---------------------------------------------------------------------------
-template <int ND>
+// comp < 0: the component is blockIdx.y (a launch over (tiles, components)).
+template <int ND, bool NC = true>
 __device__ __forceinline__ void forwardDivergencePoint(const BlockView& B, const Physics& P, const RunScalars& rs,
                                                        int rkStage, int stage, int controller, const Tile& T,
-                                                       int blk, int lin = 0, double linFactor = 0.0) {
+                                                       int blk, int lin = 0, double linFactor = 0.0,
+                                                       int comp = -1) {
   // after a solution-limit violation in this run the state stays as it is
   if (rkStage > 0 && rs.limitKey && *rs.limitKey != kNoLimitViolation) return;
   long long p;
   PointIndex I;
   if (!locate(B, T, blk, p, I)) return;
   constexpr int nU = ND + 2, E = ND + 1;
-  const int c = blockIdx.y;
+  const int c = comp >= 0 ? comp : (int)blockIdx.y;
   const long long N = B.N;
-  double s = applyOp<OP_D1>(B.fhat + N * c + I.base[0], I.idx[0], B.ax[0]);
-  for (int i = 1; i < ND; ++i) s += applyOp<OP_D1>(B.fhat + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
+  double s = applyOp<OP_D1, NC>(B.fhat + N * c + I.base[0], I.idx[0], B.ax[0]);
+  for (int i = 1; i < ND; ++i) s += applyOp<OP_D1, NC>(B.fhat + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
   double r = -s;
-  if (P.dissipation) r += dissipationTerm<ND>(B, P, I, p, c);
+  if (P.dissipation) r += dissipationTerm<ND, NC>(B, P, I, p, c);
   r = r * B.jac[p];
   for (int k = 0; k < 3; ++k) {
     const int e = B.ffOfPoint[3 * p + k];
@@ -1744,6 +1748,149 @@ __global__ void __launch_bounds__(kBlock) kFunctionalBatch(const BatchEntry* __r
 }
 
 // ---------------------------------------------------------------------------
+// Grid barrier of the persistent kernels (co-residency guaranteed by a
+// cooperative launch): bar[0] counts arrivals, bar[1] is the generation the
+// last arrival advances. A wait gives up after `limit` polls (about 100 ns
+// each), sets *err and returns false; a CTA that sees *err set also returns
+// false, so that every CTA leaves the kernel and the host reads the status.
+// The fences order each CTA's writes before its arrival and the others'
+// reads after their departure (weak loads after the acquire fence observe
+// them; stencil taps of such data use ld.global.cg, see tap()).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool gridBarrier(unsigned int* bar, unsigned int nBlocks, long long limit, int* err) {
+  __shared__ int sOk;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* vgen = bar + 1;
+    volatile int* verr = err;
+    const unsigned int gen = *vgen;
+    __threadfence();
+    const unsigned int arrived = atomicAdd(bar, 1u) + 1u;
+    int ok = 1;
+    if (arrived == nBlocks) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      long long polls = 0;
+      while (*vgen == gen) {
+        if (*verr) {
+          ok = 0;
+          break;
+        }
+        if (++polls > limit) {
+          atomicExch(err, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(100);
+      }
+    }
+    __threadfence();
+    sOk = ok;
+  }
+  __syncthreads();
+  return sOk != 0;
+}
+
+// Persistent batched forward run: every step's four RK stages for every
+// instance in one launch. Per stage, phase A (gradient/flux tiles,
+// dissipation tiles, and the functional of the stage before, which reads the
+// primitives phase A leaves alone) and phase B (divergence and RK update of
+// all components of a point, then its primitives) are separated by grid
+// barriers; the per-point arithmetic is that of the stage kernels, so the
+// results equal the per-step launches'. The step of the current phase is held
+// in shared memory and handed to the point functions through their run
+// scalars.
+template <int ND, bool CURV, bool VISC>
+__global__ void __launch_bounds__(kBatchThreads, 6) kBatchRunPersistent(const BatchEntry* __restrict__ E,
+                                                                        PersistentPlan plan, Physics P, int nSteps,
+                                                                        int functional) {
+  __shared__ int sStep, sFStep;
+  constexpr int nU = ND + 2;
+  const PrimLayout L{ND};
+  const unsigned int nBlocks = gridDim.x;
+  auto functionalUnits = [&](int fStage) {
+    for (int u = blockIdx.x; u < plan.nA; u += gridDim.x) {
+      const int4 w = plan.unitsA[u];
+      if (w.x != 2) continue;
+      RunScalars rs = E[w.y].rs;
+      rs.step = &sFStep;
+      functionalBlock(E[w.y].v, rs, fStage, L.p(), w.z);
+    }
+  };
+  for (int step = 1; step <= nSteps; ++step) {
+    for (int stage = 1; stage <= 4; ++stage) {
+      if (threadIdx.x == 0) {
+        sStep = step;
+        sFStep = stage > 1 ? step : step - 1;
+      }
+      __syncthreads();
+      const int fStage = stage > 1 ? stage - 1 : 4;
+      for (int u = blockIdx.x; u < plan.nA; u += gridDim.x) {
+        const int4 w = plan.unitsA[u];
+        const BatchEntry& e = E[w.y];
+        if (w.x == 0) {
+          RunScalars rs = e.rs;
+          rs.step = &sStep;
+          gradFluxPoint<ND, CURV, VISC, 1, false>(e.v, P, rs, GF_FLUX, stage, e.tGrad, w.z);
+        } else if (w.x == 1) {
+          dissipationPoint<ND, false>(e.v, P, e.v.q, 1.0, e.tDiss, w.z, w.w);
+        } else if (functional && sFStep >= 1) {
+          RunScalars rs = e.rs;
+          rs.step = &sFStep;
+          functionalBlock(e.v, rs, fStage, L.p(), w.z);
+        }
+      }
+      if (!gridBarrier(plan.barrier, nBlocks, plan.spinLimit, plan.status)) return;
+      for (int u = blockIdx.x; u < plan.nB; u += gridDim.x) {
+        const int2 w = plan.unitsB[u];
+        const BatchEntry& e = E[w.x];
+        RunScalars rs = e.rs;
+        rs.step = &sStep;
+        for (int c = 0; c < nU; ++c)
+          forwardDivergencePoint<ND, false>(e.v, P, rs, stage, stage, e.controller, e.tRhs, w.y, 0, 0.0, c);
+        long long p;
+        PointIndex I;
+        if (locate(e.v, e.tRhs, w.y, p, I)) {
+          const long long N = e.v.N;
+          double q[nU], pr[6 + ND];
+          for (int c = 0; c < nU; ++c) q[c] = e.v.q[p + N * c];
+          primitives<ND>(q, P, pr);
+          for (int c = 0; c < 6 + ND; ++c) e.v.prim[p + N * c] = pr[c];
+        }
+      }
+      if (!gridBarrier(plan.barrier, nBlocks, plan.spinLimit, plan.status)) return;
+    }
+  }
+  // the functional of the last stage
+  if (functional) {
+    if (threadIdx.x == 0) sFStep = nSteps;
+    __syncthreads();
+    functionalUnits(4);
+  }
+}
+
+// Self-test of the grid barrier: `rounds` rounds in which every CTA writes its
+// round stamp, meets the others at the barrier and CTA 0 sums all stamps
+// (checking that each CTA sees the others' writes after the barrier). With
+// `expected` above the number of CTAs the barrier can never complete: every
+// wait runs out after `limit` polls and the kernel returns with status 1.
+__global__ void kBarrierSelfTest(unsigned int* bar, int* err, long long limit, unsigned int expected, int rounds,
+                                 long long* stamps, long long* sum) {
+  for (int r = 1; r <= rounds; ++r) {
+    if (threadIdx.x == 0) stamps[blockIdx.x] = (long long)r * (blockIdx.x + 1);
+    if (!gridBarrier(bar, expected, limit, err)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      long long t = 0;
+      for (unsigned int b = 0; b < gridDim.x; ++b) t += *(volatile long long*)(stamps + b);
+      sum[0] += t;
+    }
+    if (!gridBarrier(bar, expected, limit, err)) return;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Constant-CFL step size (computeTimeStepSize, src/CNSHelperImpl.f90:913-982):
 // block minima of the advective and viscous bounds over the non-hole points,
 // then one block takes the minimum and, inside a run, records it for the step,
@@ -2232,6 +2379,82 @@ void launchSolutionLimits(Context& c, DevBlock& b, int blockIndex, const int* st
   else
     pdl(kSolutionLimits<3>, gridFor(b.v.N), kBlock, on(c, s), b.v, L, step, stage, blockIndex, key);
   MGD_LAUNCH(c);
+}
+
+template <int ND, bool CURV, bool VISC>
+static int persistentOccupancy() {
+  int perSm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kBatchRunPersistent<ND, CURV, VISC>, kBatchThreads, 0);
+  return perSm;
+}
+
+int selftestGridBarrier(int nBlocks, unsigned int expected, int rounds, long long limit, int* status,
+                        long long* sum) {
+  unsigned int* bar = nullptr;
+  int* err = nullptr;
+  long long *stamps = nullptr, *dsum = nullptr;
+  cudaError_t e = cudaMalloc((void**)&bar, 2 * sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&stamps, (size_t)nBlocks * sizeof(long long));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&dsum, sizeof(long long));
+  if (e == cudaSuccess) e = cudaMemset(bar, 0, 2 * sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMemset(err, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(dsum, 0, sizeof(long long));
+  if (e == cudaSuccess) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(nBlocks);
+    cfg.blockDim = dim3(32);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, kBarrierSelfTest, bar, err, limit, expected, rounds, stamps, dsum);
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(status, err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(sum, dsum, sizeof(long long), cudaMemcpyDeviceToHost);
+  cudaFree(bar);
+  cudaFree(err);
+  cudaFree(stamps);
+  cudaFree(dsum);
+  return e == cudaSuccess ? 0 : (int)e;
+}
+
+int persistentGridSize(const Context& c) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const bool curv = c.opts.curvilinear != 0, visc = c.phys.viscous != 0;
+  int perSm = 0;
+  if (c.nD == 2) perSm = curv ? (visc ? persistentOccupancy<2, true, true>() : persistentOccupancy<2, true, false>())
+                              : (visc ? persistentOccupancy<2, false, true>() : persistentOccupancy<2, false, false>());
+  else perSm = curv ? (visc ? persistentOccupancy<3, true, true>() : persistentOccupancy<3, true, false>())
+                    : (visc ? persistentOccupancy<3, false, true>() : persistentOccupancy<3, false, false>());
+  return perSm * sms;
+}
+
+cudaError_t launchBatchPersistent(Context& c, const BatchEntry* entries, const PersistentPlan& plan, int nSteps,
+                                  int functional, int grid, cudaStream_t s) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kBatchThreads);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const bool curv = c.opts.curvilinear != 0, visc = c.phys.viscous != 0;
+  MGD_LAUNCH(c);
+#define PK(ND, CU, VI) cudaLaunchKernelEx(&cfg, kBatchRunPersistent<ND, CU, VI>, entries, plan, c.phys, nSteps, functional)
+  if (c.nD == 2) {
+    if (curv) return visc ? PK(2, true, true) : PK(2, true, false);
+    return visc ? PK(2, false, true) : PK(2, false, false);
+  }
+  if (curv) return visc ? PK(3, true, true) : PK(3, true, false);
+  return visc ? PK(3, false, true) : PK(3, false, false);
+#undef PK
 }
 
 void launchStepAdvanceOn(int* counters, int delta, cudaStream_t s) { pdl(kStepAdvance, 1, 32, s, counters, delta); }

@@ -92,6 +92,13 @@ def load_library(build_if_missing=True):
     L.mgd_stage_tile.restype = C.c_int
     L.mgd_stage_tile.argtypes = [ctx, C.c_int, C.POINTER(C.c_int), C.c_int]
     L.mgd_check_solution_limits.argtypes = [ctx, C.POINTER(C.c_int)]
+    L.mgd_batch_persistent.restype = C.c_int
+    L.mgd_batch_persistent.argtypes = [C.c_void_p, C.c_int]
+    L.mgd_batch_persistent_grid.restype = C.c_int
+    L.mgd_batch_persistent_grid.argtypes = [C.c_void_p]
+    L.mgd_selftest_grid_barrier.restype = C.c_int
+    L.mgd_selftest_grid_barrier.argtypes = [C.c_int, C.c_int, C.c_int, C.c_longlong, C.POINTER(C.c_int),
+                                            C.POINTER(C.c_longlong)]
     _lib = L
     return L
 
@@ -353,9 +360,11 @@ class Solver:
 
 
 class Batch:
-    """Forward runs of many Solvers at once (mgd_batch_*): one launch per
-    stage kernel for the whole batch, one CUDA graph per RK4 step. The
-    solvers keep their own grids, states and control forcings."""
+    """Forward runs of many Solvers at once (mgd_batch_*): by default all
+    steps of every instance in one persistent cooperative launch (captured in
+    a CUDA graph); persistent(0) switches to one graph of batched stage
+    kernels per RK4 step. The solvers keep their own grids, states and
+    control forcings."""
 
     def __init__(self, solvers):
         self.L = load_library()
@@ -374,6 +383,14 @@ class Batch:
 
     def kernel_launches(self, reset=False):
         return self.L.mgd_batch_kernel_launches(self.h, int(reset))
+
+    def persistent(self, mode=None):
+        """The run mode: 1 persistent single launch, 0 one graph per step
+        (mode None only reports)."""
+        return self.L.mgd_batch_persistent(self.h, -1 if mode is None else int(mode))
+
+    def persistent_grid(self):
+        return self.L.mgd_batch_persistent_grid(self.h)
 
     def close(self):
         if getattr(self, "h", None):

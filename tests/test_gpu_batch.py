@@ -68,3 +68,53 @@ def test_batch_rejects_mismatched_options():
     b = Solver(small_monopole(dt=0.04))
     with pytest.raises(Exception):
         Batch([a, b])
+
+
+def test_persistent_launch_equals_per_step_graphs_and_oracle():
+    """The default run is one persistent cooperative launch for all steps;
+    its costs and final states equal the per-step graph path's bit for bit
+    (same per-point arithmetic and reduction layout) and the oracle's."""
+    grads = {sz: _gradient_direction(*sz) for sz in SIZES}
+    cases = [(SIZES[i % len(SIZES)], 10.0 ** (-2.0 - 0.25 * i)) for i in range(5)]
+
+    def make():
+        return [_controlled(n, ny, a * grads[(n, ny)])[1] for (n, ny), a in cases]
+
+    per_step, persistent = make(), make()
+    b0, b1 = Batch(per_step), Batch(persistent)
+    assert b0.persistent(0) == 0 and b1.persistent() == 1 and b1.persistent_grid() > 0
+    b1.kernel_launches(reset=True)
+    c0, c1 = b0.run_forward(N_STEPS), b1.run_forward(N_STEPS)
+    assert b1.kernel_launches() == 1
+    assert np.array_equal(c0, c1)
+    for s0, s1 in zip(per_step, persistent):
+        assert np.array_equal(s0.get_field(1, capi.FIELD_CONSERVED), s1.get_field(1, capi.FIELD_CONSERVED))
+    for i, ((n, ny), a) in enumerate(cases):
+        P = small_monopole(n=n, ny=ny, n_steps=N_STEPS, controller_switch=True)
+        o = oracle_lib.Oracle(P)
+        o.set_control_forcing(a * grads[(n, ny)])
+        Jo = o.run_forward(N_STEPS, keep_stages=False)
+        assert abs(c1[i] - Jo) <= 1e-10 * abs(Jo)
+    # a second run of the same length reuses the captured launch
+    for s in persistent:
+        s.set_field(1, capi.FIELD_CONSERVED, s.problem.blocks[0].initial_state)
+    assert np.array_equal(b1.run_forward(N_STEPS), c1)
+
+
+def test_grid_barrier_completes_and_its_wait_runs_out_without_a_fault():
+    """The persistent kernel's grid barrier: 64 CTAs meet 50 times and see
+    each other's writes; then a barrier that expects one CTA more than the
+    launch has (an arrival that never comes) gives up after its poll limit,
+    returns status 1, and the context stays usable."""
+    import ctypes as C
+    from magudi_gb300.solver import load_library
+    L = load_library()
+    status, checksum = C.c_int(-1), C.c_longlong(0)
+    assert L.mgd_selftest_grid_barrier(64, 64, 50, 1 << 24, C.byref(status), C.byref(checksum)) == 0
+    assert status.value == 0 and checksum.value == (50 * 51 // 2) * (64 * 65 // 2)
+    assert L.mgd_selftest_grid_barrier(16, 17, 3, 2000, C.byref(status), C.byref(checksum)) == 0
+    assert status.value == 1
+    # the device still runs work afterwards
+    s = Solver(small_monopole())
+    s.compute_rhs(capi.FORWARD, 0.0)
+    assert np.all(np.isfinite(s.get_field(1, capi.FIELD_RHS)))
