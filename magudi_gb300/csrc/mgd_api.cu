@@ -2458,7 +2458,18 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
   else launchAdjointInitial(c, b, c.opts.adjoint_forcing_switch ? -dtT / 6.0 : 0.0);
   long long nodesRec = 0, nodesAdj = 0;
   setProgrammaticLaunch(!twoLanes);
-  struct Restore { ~Restore() { setProgrammaticLaunch(true); } } restore;
+  struct Restore {
+    ~Restore() {
+      setProgrammaticLaunch(true);
+      setLaunchPriority(false, 0);
+    }
+  } restore;
+  // The adjoint is the critical path; the recomputation of the next segment
+  // has slack (a segment's forward stages take less time than its adjoint
+  // stages), so its kernels launch at the lowest priority and take the SM
+  // time the adjoint leaves.
+  int prioLeast = 0, prioGreatest = 0;
+  cudaDeviceGetStreamPriorityRange(&prioLeast, &prioGreatest);
   for (int half = 0; half < c.stageHalves; ++half) {
     RunScalars ra = runScalars(c);
     if (terminal) ra.adjointForcingSwitch = 0;  // no forcing during the run
@@ -2466,11 +2477,13 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
     RunScalars rr = ra;
     rr.step = recCounters;
     rr.segBase = recCounters + 1;
+    if (twoLanes) setLaunchPriority(true, prioLeast);
     if (!resident && capture(c, &c.gRecomputeH[half], &nodesRec, [&]() {
           for (int i = 1; i <= 4; ++i) forwardStage(c, rb, i, rr, false, controller, true, false, &recLanes);
           launchStepAdvanceOn(recCounters, 1, recLanes.main);
         }, recLanes.main))
       return 1;
+    if (twoLanes) setLaunchPriority(true, prioGreatest);
     if (capture(c, &c.gAdjointH[half], &nodesAdj, [&]() {
           for (int i = 4; i >= 1; --i) {
             if (!full) {
@@ -2493,8 +2506,10 @@ int mgd_run_adjoint(mgd_ctx* h, double* sensitivity) {
     const int half = k % c.stageHalves;
     CUDA_TRY(c, cudaMemcpyAsync(rb.v.q, c.dSnapshots + (size_t)k * nU * N, (size_t)nU * N * sizeof(double),
                                 cudaMemcpyDeviceToDevice, recLanes.main));
+    if (twoLanes) setLaunchPriority(true, prioLeast);
     launchPrims(c, rb, rb.v.q, false, nullptr, 0, recLanes.main);
     launchSetCounters(recCounters, L + 1, L, recLanes.main);
+    if (twoLanes) setLaunchPriority(true, prioGreatest);
     for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gRecomputeH[half], recLanes.main));
     c.launches += 2 + (long long)(end - L) * nodesRec;
     if (twoLanes) CUDA_TRY(c, cudaEventRecord(c.evRecDone[half], recLanes.main));
@@ -3152,7 +3167,10 @@ int mgd_tune_run(mgd_ctx* h, int n_steps, int save_interval, int with_adjoint, d
   if (c.nD == 2)
     cands = {{8, 8, 1}, {16, 4, 1}, {32, 2, 1}, {64, 1, 1}, {8, 16, 1}, {16, 8, 1},
              {32, 4, 1}, {64, 2, 1}, {128, 1, 1}, {16, 16, 1}, {32, 8, 1},
-             {8, 12, 1}, {16, 6, 1}, {16, 10, 1}, {8, 20, 1}, {16, 12, 1}, {32, 6, 1}};
+             {8, 12, 1}, {16, 6, 1}, {16, 10, 1}, {8, 20, 1}, {16, 12, 1}, {32, 6, 1},
+             // one-warp tiles: four times the CTAs of the 128-point tiles, so
+             // that a single wave of small grids spreads more evenly
+             {8, 4, 1}, {4, 8, 1}, {16, 2, 1}};
   else
     cands = {{8, 4, 2}, {16, 2, 2}, {32, 2, 1}, {8, 8, 2}, {16, 4, 2}, {32, 2, 2}, {32, 4, 1},
              {16, 8, 1}, {8, 4, 4}, {64, 2, 1}, {16, 4, 4}};

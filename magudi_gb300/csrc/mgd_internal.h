@@ -403,6 +403,9 @@ int autotuneTile(Context& c, DevBlock& b, int kernel, const int (*cands)[3], int
 // ----- launchers (mgd_kernels.cu) -----
 // Programmatic dependent launch for the launches that follow on this thread.
 void setProgrammaticLaunch(bool on);
+// Launch priority for the launches that follow on this thread (on = false:
+// each launch takes its stream's priority).
+void setLaunchPriority(bool on, int priority);
 // Every launcher takes the stream it launches on; the context stream when 0.
 void uploadOperatorTables();
 // Primitive variables of qSrc (or, when stage > 0, of the stage-buffer slot

@@ -59,8 +59,31 @@ __device__ __forceinline__ void pdlEnter() {
 // other stream's kernels could use, so the checkpoint recomputation and the
 // adjoint launch without it.
 static thread_local bool t_programmaticLaunch = true;
+static thread_local int t_launchPriority = 0;  // 0: the stream's own priority
+static thread_local bool t_priorityOn = false;
 
 void setProgrammaticLaunch(bool on) { t_programmaticLaunch = on; }
+void setLaunchPriority(bool on, int priority) {
+  t_priorityOn = on;
+  t_launchPriority = priority;
+}
+
+// Attributes of a launch: programmatic stream serialization (when on) and
+// the launch priority (when set).
+static int launchAttributes(cudaLaunchAttribute* attr) {
+  int n = 0;
+  if (t_programmaticLaunch) {
+    attr[n].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[n].val.programmaticStreamSerializationAllowed = 1;
+    ++n;
+  }
+  if (t_priorityOn) {
+    attr[n].id = cudaLaunchAttributePriority;
+    attr[n].val.priority = t_launchPriority;
+    ++n;
+  }
+  return n;
+}
 
 template <typename... KArgs, typename... Args>
 static void pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args&&... args) {
@@ -69,15 +92,11 @@ static void pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s,
   cfg.blockDim = block;
   cfg.dynamicSmemBytes = 0;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchAttribute attr[2];
   cfg.attrs = attr;
-  cfg.numAttrs = t_programmaticLaunch ? 1 : 0;
+  cfg.numAttrs = launchAttributes(attr);
   cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
-
-
 
 // pdl with dynamic shared memory.
 template <typename... KArgs, typename... Args>
@@ -87,11 +106,9 @@ static void pdlShared(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t sm
   cfg.blockDim = block;
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchAttribute attr[2];
   cfg.attrs = attr;
-  cfg.numAttrs = t_programmaticLaunch ? 1 : 0;
+  cfg.numAttrs = launchAttributes(attr);
   cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
