@@ -262,6 +262,17 @@ KERNEL_UNITS = {
     # b2 4, lambda 4 written; ffOfPoint 3 + iblank 1 ints
     "adjoint_assemble_rk": {"bytes": 8 * (4 + 3 + 1 + 3 + 4 + 1 + 4 + 1 + 1 + 4 + 4 + 4 + 4) + 4 * 4, "flops": 47},
 }
+# Algorithmic FP64 operations per grid point of the 201x201 monopole RHS:
+# the reference's operation list as the oracle restates it, counted by the
+# operation-counting build of the oracle (oracle/build_opcount.sh; adds,
+# multiplies, divides and square roots; tests/test_opcount.py recounts them).
+# adjoint_core is the part of computeRhsAdjoint that the adjoint-core kernel
+# performs (adjoint derivatives of lambda, the (A - B1)^T and B2^T products);
+# the GPU kernels evaluate the same terms with fewer operations (the
+# executed counts are in KERNEL_UNITS), so a rate over these counts is the
+# reference-equivalent FP64 rate.
+ALGORITHMIC_FLOPS = {"forward_rhs": 406.8, "adjoint_rhs": 1073.2, "adjoint_core": 725.1, "dissipation": 126.4}
+
 # DRAM bytes (read + write) per launch from an ncu capture of the 201x201
 # gradient workload (dram__bytes_read.sum + dram__bytes_write.sum, three
 # launches, cold L2 between the profiler's passes); kernels not captured are
@@ -554,8 +565,13 @@ def run_ours(args):
     units = KERNEL_UNITS[dominant]
     t_launch = kern[dominant] / 1e3
     achieved_gbs = units["bytes"] * pts / t_launch / 1e9
-    achieved_tf = units["flops"] * pts / t_launch / 1e12
+    alg_flops = ALGORITHMIC_FLOPS.get(dominant, units["flops"])
+    achieved_tf = alg_flops * pts / t_launch / 1e12
+    executed_tf = units["flops"] * pts / t_launch / 1e12
     fp64 = fp64_peak(torch, clk)
+    # whole RHS: the reference's operation count over the stage kernels' time
+    t_fwd = sum(kern[k] for k in FORWARD_KERNELS if k != "forward_functional") / 1e3
+    t_adj = sum(kern[k] for k in ADJOINT_KERNELS if k != "adjoint_gradient_sensitivity") / 1e3
     mode_text = {False: "checkpoints every %d steps, each segment's forward states recomputed on the device beside "
                         "the adjoint (UniformCheckpointer)" % SAVE_INTERVAL,
                  True: "resident trajectory: every stage's state, primitives, stress and heat flux kept on the device "
@@ -585,7 +601,18 @@ def run_ours(args):
         "roofline": {"bound": "fp64", "kernel": dominant, "achieved": achieved_tf, "peak": fp64["peak_tflops"],
                      "unit": "TFLOP/s", "frac": achieved_tf / fp64["peak_tflops"],
                      "traffic": MEASURED_TRAFFIC.get(dominant), "peak_source": fp64["source"],
-                     "peak_nominal_tflops": fp64["nominal_tflops"], "flops_per_point": units["flops"],
+                     "peak_nominal_tflops": fp64["nominal_tflops"],
+                     "flops_per_point": alg_flops,
+                     "flops_source": "reference operation list, counted by the operation-counting oracle build",
+                     "executed": {"flops_per_point": units["flops"], "achieved_tflops": executed_tf,
+                                  "frac": executed_tf / fp64["peak_tflops"],
+                                  "source": "FP64 instructions the kernel executes (ncu, 2 x DFMA + DADD + DMUL)"},
+                     "rhs": {"forward": {"flops_per_point": ALGORITHMIC_FLOPS["forward_rhs"],
+                                         "achieved_tflops": ALGORITHMIC_FLOPS["forward_rhs"] * pts / t_fwd / 1e12,
+                                         "stage_kernels_ms": t_fwd * 1e3},
+                             "adjoint": {"flops_per_point": ALGORITHMIC_FLOPS["adjoint_rhs"],
+                                         "achieved_tflops": ALGORITHMIC_FLOPS["adjoint_rhs"] * pts / t_adj / 1e12,
+                                         "stage_kernels_ms": t_adj * 1e3}},
                      "hbm": {"achieved_gbs": achieved_gbs, "peak_gbs": peaks["hbm_gbs"],
                              "frac": achieved_gbs / peaks["hbm_gbs"], "bytes_per_point": units["bytes"],
                              "peak_source": peak_kind},

@@ -63,13 +63,16 @@ __device__ __forceinline__ int wrapIndex(int i, int n, int per) {
 // Follows applyOperator_{1,2,3} (src/StencilOperatorImpl.f90:35-457):
 // sum over taps left to right, boundary rows from the left block and its
 // (skew-)reflection on the right.
-// Load of a stencil tap: through the read-only data path (NC), or from L2
-// (ld.global.cg) for data that the same kernel launch writes elsewhere
-// (the persistent batched kernel), which the non-coherent path may serve stale.
+// Load of a stencil tap: through the read-only data path (NC), or as an
+// ordinary cached load (ld.global.ca) for data that the same kernel launch
+// writes elsewhere (the persistent batched kernel). The read-only path lies
+// outside the memory model and may serve such data stale; ordinary loads
+// after the acquiring fence of a grid barrier see the other CTAs' writes and
+// still share L1 lines between neighbouring points within a phase.
 template <bool NC>
 __device__ __forceinline__ double tap(const double* p) {
   if constexpr (NC) return __ldg(p);
-  else return __ldcg(p);
+  else return __ldca(p);
 }
 
 template <int OP, bool NC = true>

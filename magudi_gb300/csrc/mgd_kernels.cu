@@ -1771,8 +1771,9 @@ __global__ void __launch_bounds__(kBlock) kFunctionalBatch(const BatchEntry* __r
 // each), sets *err and returns false; a CTA that sees *err set also returns
 // false, so that every CTA leaves the kernel and the host reads the status.
 // The fences order each CTA's writes before its arrival and the others'
-// reads after their departure (weak loads after the acquire fence observe
-// them; stencil taps of such data use ld.global.cg, see tap()).
+// reads after their departure: the fence after the wait acquires, so the
+// ordinary loads that follow observe the other CTAs' writes (stencil taps of
+// such data avoid the read-only path, see tap()).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ bool gridBarrier(unsigned int* bar, unsigned int nBlocks, long long limit, int* err) {
   __shared__ int sOk;
@@ -1803,6 +1804,7 @@ __device__ __forceinline__ bool gridBarrier(unsigned int* bar, unsigned int nBlo
         __nanosleep(100);
       }
     }
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
     __threadfence();
     sOk = ok;
   }

@@ -34,6 +34,24 @@
 #include <omp.h>
 #endif
 
+// Sections of the operation-counting build (oracle/build_opcount.sh): the
+// arithmetic inside a marked scope is attributed to that section. No effect
+// in the ordinary builds.
+#ifndef ORC_SECTION
+#define ORC_SECTION(s)
+#endif
+enum {
+  SEC_OTHER = 0,
+  SEC_STATE = 1,              // updateState: primitives, transport, gradients, stress, heat flux
+  SEC_FORWARD = 2,            // computeRhsForward without its dissipation
+  SEC_DISSIPATION = 3,        // addDissipation
+  SEC_ADJOINT = 4,            // computeRhsAdjoint: adjoint derivatives and the Jacobian-transpose products
+  SEC_FARFIELD_ADJ = 5,       // addFarFieldAdjointPenalty
+  SEC_PATCHES = 6,            // patchUpdateRhs: SATs, sponge, actuator, cost-target forcing
+  SEC_REGION = 7,             // computeRhs epilogue: 1/det, acoustic sources, holes
+  SEC_ADJOINT_DIFFUSION = 9   // computeRhsAdjoint: adjoint derivative of the viscous diffusion, map to q
+};
+
 namespace orc {
 
 enum { SYMMETRIC = 0, SKEW_SYMMETRIC = 1, ASYMMETRIC = 2 };
@@ -671,7 +689,10 @@ struct Dual {
   double v = 0.0;
   double d[5] = {0, 0, 0, 0, 0};
   Dual() = default;
-  Dual(double x) : v(x) {}
+  Dual(double x) : v(x) {}  // keep-double (the operation-counting build keeps this signature)
+#ifdef ORC_OPCOUNT
+  Dual(Real x) : v(x) {}
+#endif
 };
 static inline double value(double x) { return x; }
 static inline double value(const Dual& x) { return x.v; }
@@ -684,14 +705,14 @@ static inline Dual operator/(const Dual& a, const Dual& b) {
   for (int k = 0; k < 5; ++k) r.d[k] = (a.d[k] * b.v - a.v * b.d[k]) / (b.v * b.v);
   return r;
 }
-static inline Dual operator+(const Dual& a, double b) { return a + Dual(b); }
-static inline Dual operator+(double a, const Dual& b) { return Dual(a) + b; }
-static inline Dual operator-(const Dual& a, double b) { return a - Dual(b); }
-static inline Dual operator-(double a, const Dual& b) { return Dual(a) - b; }
-static inline Dual operator*(const Dual& a, double b) { Dual r(a.v * b); for (int k = 0; k < 5; ++k) r.d[k] = a.d[k] * b; return r; }
-static inline Dual operator*(double a, const Dual& b) { return b * a; }
-static inline Dual operator/(const Dual& a, double b) { return a / Dual(b); }
-static inline Dual operator/(double a, const Dual& b) { return Dual(a) / b; }
+static inline Dual operator+(const Dual& a, double b) { return a + Dual(b); }  // keep-double
+static inline Dual operator+(double a, const Dual& b) { return Dual(a) + b; }  // keep-double
+static inline Dual operator-(const Dual& a, double b) { return a - Dual(b); }  // keep-double
+static inline Dual operator-(double a, const Dual& b) { return Dual(a) - b; }  // keep-double
+static inline Dual operator*(const Dual& a, double b) { Dual r(a.v * b); for (int k = 0; k < 5; ++k) r.d[k] = a.d[k] * b; return r; }  // keep-double
+static inline Dual operator*(double a, const Dual& b) { return b * a; }  // keep-double
+static inline Dual operator/(const Dual& a, double b) { return a / Dual(b); }  // keep-double
+static inline Dual operator/(double a, const Dual& b) { return Dual(a) / b; }  // keep-double
 static inline Dual& operator+=(Dual& a, const Dual& b) { a = a + b; return a; }
 static inline Dual sqrt(const Dual& a) {
   Dual r(std::sqrt(a.v));
@@ -1142,6 +1163,7 @@ static void computeGradient(Region& R, Block& b, const double* f, int ncomp, dou
 // (src/CNSHelperImpl.f90:3-87), computeTransportVariables (:89-177) and
 // computeStressTensor (:353-458).
 static void updateState(Region& R, Block& b, const double* q) {
+  ORC_SECTION(SEC_STATE);
   const int nD = R.nD;
   const long long N = b.N;
   const double g = R.o.ratio_of_specific_heats;
@@ -1511,6 +1533,7 @@ static void normalizeMollifiers(Region& R) {
 
 // addDissipation, src/RhsHelperImpl.f90:10-87 (composite and non-composite paths).
 static void addDissipation(Region& R, Block& b, int mode) {
+  ORC_SECTION(SEC_DISSIPATION);
   const int nD = R.nD, nU = R.nU;
   const long long N = b.N;
   const double amount = mode == MGD_ADJOINT ? -R.o.dissipation_amount : R.o.dissipation_amount;
@@ -1535,6 +1558,7 @@ static void addDissipation(Region& R, Block& b, int mode) {
 
 // computeRhsForward, src/RhsHelperImpl.f90:254-354.
 static void computeRhsForward(Region& R, Block& b, int bi) {
+  ORC_SECTION(SEC_FORWARD);
   const int nD = R.nD, nU = R.nU;
   const long long N = b.N;
   std::vector<double> f1(N * nU * nD), f2(N * nU * nD);
@@ -1588,6 +1612,7 @@ static void computeRhsForward(Region& R, Block& b, int bi) {
 
 // addFarFieldAdjointPenalty, src/RhsHelperImpl.f90:89-250.
 static void addFarFieldAdjointPenalty(Region& R, Block& b, int bi) {
+  ORC_SECTION(SEC_FARFIELD_ADJ);
   const int nD = R.nD, nU = R.nU;
   const long long N = b.N;
   bool any = false;
@@ -1707,6 +1732,7 @@ static void addInterfaceAdjointPenalty(Region& R, Block& b, int bi) {
 
 // computeRhsAdjoint, src/RhsHelperImpl.f90:356-596.
 static void computeRhsAdjoint(Region& R, Block& b, int bi) {
+  ORC_SECTION(SEC_ADJOINT);
   const int nD = R.nD, nU = R.nU;
   const long long N = b.N;
   const double g = R.o.ratio_of_specific_heats;
@@ -1764,6 +1790,9 @@ static void computeRhsAdjoint(Region& R, Block& b, int bi) {
       for (int jj = 0; jj < nD; ++jj)
         for (int r = 0; r < nU - 1; ++r) temp1[N * (r + 1 + nU * jj) + k] = ad[r + (nU - 1) * jj];
     }
+    // the adjoint derivative of the viscous diffusion and its map to the
+    // conservative variables (a section of its own in the counting build)
+    ORC_SECTION(SEC_ADJOINT_DIFFUSION);
     for (int jj = 0; jj < nD; ++jj) apply(b.adjointFirstDerivative[jj], &temp1[N * (1 + nU * jj)], nU - 1, b.gs, jj);
 #pragma omp parallel for collapse(2) schedule(static)
     for (int c = 0; c < nU - 1; ++c)
@@ -1893,6 +1922,7 @@ static void computeRhsLinearized(Region& R, Block& b, int bi) {
 // src/SpongePatchImpl.f90:65-165, src/ActuatorPatchImpl.f90:108-181,
 // src/CostTargetPatchImpl.f90:72-136).
 static void patchUpdateRhs(Region& R, Patch& p, Block& b, int mode, double adjointForcingFactor, double time = 0.0) {
+  ORC_SECTION(SEC_PATCHES);
   const int nD = R.nD, nU = R.nU;
   const long long N = b.N;
   const double g = R.o.ratio_of_specific_heats;
@@ -2271,6 +2301,7 @@ static void computeRhs(Region& R, int mode, double time, double adjointForcingFa
   // partner block's arrays directly (src/RegionImpl.f90:1923-1960)
   if (mode == MGD_ADJOINT && R.o.viscous)
     for (size_t bi = 0; bi < R.blocks.size(); ++bi) addInterfaceAdjointPenalty(R, R.blocks[bi], (int)bi);
+  ORC_SECTION(SEC_REGION);
   for (Block& b : R.blocks)
 #pragma omp parallel for collapse(2) schedule(static)
     for (int j = 0; j < R.nU; ++j)
@@ -2777,6 +2808,18 @@ void* orc_create(const mgd_options* o) {
 void orc_destroy(void* h) { delete (Region*)h; }
 
 const char* orc_last_error(void* h) { return ((Region*)h)->error.c_str(); }
+
+#ifdef ORC_OPCOUNT
+// Operation counts per section (opcount.h): out[section * 5 + kind], kinds
+// add/subtract, multiply, divide, square root, special functions.
+void orc_opcount(long long* out, int reset) {
+  for (int s = 0; s < oc::kSections; ++s)
+    for (int k = 0; k < oc::KINDS; ++k) {
+      if (out) out[s * oc::KINDS + k] = oc::counts[s][k];
+      if (reset) oc::counts[s][k] = 0;
+    }
+}
+#endif
 
 int orc_set_threads(int n) {
 #ifdef _OPENMP

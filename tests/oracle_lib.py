@@ -16,6 +16,9 @@ LIB_PATH = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
 # The same source built with the reference's release flags (-O3 -ffast-math
 # -funroll-loops): the timed CPU leg of the bench, never the parity checker.
 TUNED_LIB_PATH = os.path.join(ROOT, "oracle", "_build", "liboracle_tuned.so")
+# The operation-counting build (oracle/build_opcount.sh): counts the FP64
+# operations of the reference's operation list per section of the RHS.
+OPCOUNT_LIB_PATH = os.path.join(ROOT, "oracle", "_build", "liboracle_opcount.so")
 
 _libs = {}
 
@@ -28,10 +31,15 @@ def lib(variant="strict"):
     """The oracle library: "strict" (IEEE arithmetic, the checker) or
     "tuned" (fast-math release build, for CPU timing)."""
     if variant not in _libs:
-        path = LIB_PATH if variant == "strict" else TUNED_LIB_PATH
+        path = {"strict": LIB_PATH, "tuned": TUNED_LIB_PATH, "opcount": OPCOUNT_LIB_PATH}[variant]
         if not os.path.exists(path):
-            build()
+            if variant == "opcount":
+                subprocess.check_call(["bash", os.path.join(ROOT, "oracle", "build_opcount.sh")])
+            else:
+                build()
         L = C.CDLL(path)
+        if variant == "opcount":
+            L.orc_opcount.argtypes = [C.POINTER(C.c_longlong), C.c_int]
         L.orc_create.restype = C.c_void_p
         L.orc_create.argtypes = [C.POINTER(capi.Options)]
         L.orc_destroy.argtypes = [C.c_void_p]
@@ -71,6 +79,19 @@ def lib(variant="strict"):
 
 def set_threads(n, variant="strict"):
     return lib(variant).orc_set_threads(n)
+
+
+SECTIONS = {0: "other", 1: "state", 2: "forward", 3: "dissipation", 4: "adjoint", 5: "farfield_adjoint",
+            6: "patches", 7: "region", 9: "adjoint_diffusion"}
+OP_KINDS = ("add", "mul", "div", "sqrt", "special")
+
+
+def opcounts(reset=True):
+    """{section: {kind: count}} of the operation-counting build since the last reset."""
+    buf = (C.c_longlong * (16 * 5))()
+    lib("opcount").orc_opcount(buf, int(reset))
+    return {SECTIONS.get(sec, str(sec)): {k: buf[sec * 5 + i] for i, k in enumerate(OP_KINDS)}
+            for sec in range(16) if any(buf[sec * 5 + i] for i in range(5))}
 
 
 def operator(which, scheme=capi.SBP_48):
