@@ -208,7 +208,7 @@ int mgd_batch_create(mgd_ctx* const* instances, int n_instances, mgd_batch** out
       for (int j = 0; j < reductionBlocks(b->inst[i]->c.blocks[0]); ++j) unitsA.push_back(make_int4(2, i, j, 0));
     if (cudaMalloc((void**)&b->dUnitsA, unitsA.size() * sizeof(int4)) != cudaSuccess ||
         cudaMemcpy(b->dUnitsA, unitsA.data(), unitsA.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMalloc((void**)&b->dBarrier, 2 * sizeof(unsigned int)) != cudaSuccess ||
+        cudaMalloc((void**)&b->dBarrier, 3 * sizeof(unsigned int)) != cudaSuccess ||
         cudaMalloc((void**)&b->dStatus, sizeof(int)) != cudaSuccess) {
       g_batchCreateError = "device allocation failed for the persistent run";
       destroyBatch(b);
@@ -243,7 +243,7 @@ int mgd_batch_persistent_grid(mgd_batch* batch) { return batch ? batch->persiste
 // when the capture is refused).
 static int runPersistent(mgd_batch* b, int n_steps, bool functional) {
   Context& c0 = b->inst[0]->c;
-  BATCH_TRY(b, cudaMemsetAsync(b->dBarrier, 0, 2 * sizeof(unsigned int), b->stream));
+  BATCH_TRY(b, cudaMemsetAsync(b->dBarrier, 0, 3 * sizeof(unsigned int), b->stream));
   BATCH_TRY(b, cudaMemsetAsync(b->dStatus, 0, sizeof(int), b->stream));
   if (!b->graphP || b->graphPSteps != n_steps) {
     if (b->graphP) cudaGraphExecDestroy(b->graphP);

@@ -355,8 +355,9 @@ struct BatchEntry {
 // dissipation tile and component, 2 functional reduction block), phase B
 // tiles {instance, tile} (divergence and RK update of every component, then
 // the primitives). barrier = {arrivals, generation} of the grid barrier
-// between phases; status = 0, or 1 when a barrier wait ran out of its spin
-// limit (the kernel then returns early and the host reports the error).
+// between phases, and barrier[2] the work counter the CTAs draw a phase's
+// units from; status = 0, or 1 when a barrier wait ran out of its spin limit
+// (the kernel then returns early and the host reports the error).
 struct PersistentPlan {
   const int4* unitsA = nullptr;
   int nA = 0;
@@ -511,6 +512,11 @@ int selftestGridBarrier(int nBlocks, unsigned int expected, int rounds, long lon
                         long long* sum);
 void launchSetCounters(int* counters, int step, int segBase, cudaStream_t s);
 constexpr int kBatchThreads = 128;
+// Resident CTAs per SM that the persistent batched kernel is compiled for
+// (its register budget is 65536 / (128 x this)).
+#ifndef MGD_PERSISTENT_MIN_BLOCKS
+#define MGD_PERSISTENT_MIN_BLOCKS 6
+#endif
 constexpr int kMaxExcitationModes = 256;  // modes of one solenoidal-excitation patch
 
 // Blocks of the fixed-layout reductions (functional, sensitivity).

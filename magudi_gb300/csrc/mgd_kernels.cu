@@ -1767,15 +1767,18 @@ __global__ void __launch_bounds__(kBlock) kFunctionalBatch(const BatchEntry* __r
 // ---------------------------------------------------------------------------
 // Grid barrier of the persistent kernels (co-residency guaranteed by a
 // cooperative launch): bar[0] counts arrivals, bar[1] is the generation the
-// last arrival advances. A wait gives up after `limit` polls (about 100 ns
-// each), sets *err and returns false; a CTA that sees *err set also returns
-// false, so that every CTA leaves the kernel and the host reads the status.
+// last arrival advances; the last arrival also zeroes *work (when given), the
+// work counter the CTAs draw the next phase's units from. A wait gives up
+// after `limit` polls (about 100 ns each), sets *err and returns false; a CTA
+// that sees *err set also returns false, so that every CTA leaves the kernel
+// and the host reads the status.
 // The fences order each CTA's writes before its arrival and the others'
 // reads after their departure: the fence after the wait acquires, so the
 // ordinary loads that follow observe the other CTAs' writes (stencil taps of
 // such data avoid the read-only path, see tap()).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool gridBarrier(unsigned int* bar, unsigned int nBlocks, long long limit, int* err) {
+__device__ __forceinline__ bool gridBarrier(unsigned int* bar, unsigned int nBlocks, long long limit, int* err,
+                                            unsigned int* work = nullptr) {
   __shared__ int sOk;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -1787,6 +1790,9 @@ __device__ __forceinline__ bool gridBarrier(unsigned int* bar, unsigned int nBlo
     int ok = 1;
     if (arrived == nBlocks) {
       atomicExch(bar, 0u);
+      // every CTA has finished the phase: nobody draws from the counter
+      // until the generation advances
+      if (work) atomicExch(work, 0u);
       __threadfence();
       atomicAdd(bar + 1, 1u);
     } else {
@@ -1818,35 +1824,38 @@ __device__ __forceinline__ bool gridBarrier(unsigned int* bar, unsigned int nBlo
 // primitives phase A leaves alone) and phase B (divergence and RK update of
 // all components of a point, then its primitives) are separated by grid
 // barriers; the per-point arithmetic is that of the stage kernels, so the
-// results equal the per-step launches'. The step of the current phase is held
-// in shared memory and handed to the point functions through their run
-// scalars.
+// results equal the per-step launches'. The CTAs draw the units of a phase
+// one at a time from a work counter (plan.barrier[2]), in list order (the
+// heavy gradient/flux tiles first), so that a CTA that finishes early takes
+// more work, as the hardware's block scheduler would give it; the last CTA to
+// reach a barrier zeroes the counter for the next phase. The step of the
+// current phase is held in shared memory and handed to the point functions
+// through their run scalars.
+__device__ __forceinline__ int drawUnit(unsigned int* work) {
+  __shared__ int sUnit;
+  __syncthreads();  // every thread has read the previous unit
+  if (threadIdx.x == 0) sUnit = (int)atomicAdd(work, 1u);
+  __syncthreads();
+  return sUnit;
+}
+
 template <int ND, bool CURV, bool VISC>
-__global__ void __launch_bounds__(kBatchThreads, 6) kBatchRunPersistent(const BatchEntry* __restrict__ E,
-                                                                        PersistentPlan plan, Physics P, int nSteps,
-                                                                        int functional) {
+__global__ void __launch_bounds__(kBatchThreads, MGD_PERSISTENT_MIN_BLOCKS)
+    kBatchRunPersistent(const BatchEntry* __restrict__ E, PersistentPlan plan, Physics P, int nSteps,
+                        int functional) {
   __shared__ int sStep, sFStep;
   constexpr int nU = ND + 2;
   const PrimLayout L{ND};
   const unsigned int nBlocks = gridDim.x;
-  auto functionalUnits = [&](int fStage) {
-    for (int u = blockIdx.x; u < plan.nA; u += gridDim.x) {
-      const int4 w = plan.unitsA[u];
-      if (w.x != 2) continue;
-      RunScalars rs = E[w.y].rs;
-      rs.step = &sFStep;
-      functionalBlock(E[w.y].v, rs, fStage, L.p(), w.z);
-    }
-  };
+  unsigned int* work = plan.barrier + 2;
   for (int step = 1; step <= nSteps; ++step) {
     for (int stage = 1; stage <= 4; ++stage) {
       if (threadIdx.x == 0) {
         sStep = step;
         sFStep = stage > 1 ? step : step - 1;
       }
-      __syncthreads();
       const int fStage = stage > 1 ? stage - 1 : 4;
-      for (int u = blockIdx.x; u < plan.nA; u += gridDim.x) {
+      for (int u = drawUnit(work); u < plan.nA; u = drawUnit(work)) {
         const int4 w = plan.unitsA[u];
         const BatchEntry& e = E[w.y];
         if (w.x == 0) {
@@ -1861,8 +1870,8 @@ __global__ void __launch_bounds__(kBatchThreads, 6) kBatchRunPersistent(const Ba
           functionalBlock(e.v, rs, fStage, L.p(), w.z);
         }
       }
-      if (!gridBarrier(plan.barrier, nBlocks, plan.spinLimit, plan.status)) return;
-      for (int u = blockIdx.x; u < plan.nB; u += gridDim.x) {
+      if (!gridBarrier(plan.barrier, nBlocks, plan.spinLimit, plan.status, work)) return;
+      for (int u = drawUnit(work); u < plan.nB; u = drawUnit(work)) {
         const int2 w = plan.unitsB[u];
         const BatchEntry& e = E[w.x];
         RunScalars rs = e.rs;
@@ -1879,14 +1888,20 @@ __global__ void __launch_bounds__(kBatchThreads, 6) kBatchRunPersistent(const Ba
           for (int c = 0; c < 6 + ND; ++c) e.v.prim[p + N * c] = pr[c];
         }
       }
-      if (!gridBarrier(plan.barrier, nBlocks, plan.spinLimit, plan.status)) return;
+      if (!gridBarrier(plan.barrier, nBlocks, plan.spinLimit, plan.status, work)) return;
     }
   }
   // the functional of the last stage
   if (functional) {
     if (threadIdx.x == 0) sFStep = nSteps;
     __syncthreads();
-    functionalUnits(4);
+    for (int u = blockIdx.x; u < plan.nA; u += gridDim.x) {
+      const int4 w = plan.unitsA[u];
+      if (w.x != 2) continue;
+      RunScalars rs = E[w.y].rs;
+      rs.step = &sFStep;
+      functionalBlock(E[w.y].v, rs, 4, L.p(), w.z);
+    }
   }
 }
 
