@@ -881,12 +881,15 @@ def run_tgv(args):
     clocks.start()
     times = []
     J = None
+    # the timed steps in an NVTX range (ncu --nvtx --nvtx-include "gradient/")
+    torch.cuda.nvtx.range_push("gradient")
     for _ in range(args.steps):
         torch.cuda.synchronize()
         t = time.perf_counter()
         J = step()
         torch.cuda.synchronize()
         times.append(time.perf_counter() - t)
+    torch.cuda.nvtx.range_pop()
     clk = clocks.stop()
     sec = statistics.mean(times)
     pts = args.tgv_n ** 3

@@ -364,9 +364,11 @@ int mgd_batch_destroy(mgd_batch* batch);
 const char* mgd_batch_last_error(const mgd_batch* batch);
 /* How a batch runs (no reference counterpart): mode 1 (the default) runs
  * all steps of mgd_batch_run_forward as one persistent cooperative launch,
- * captured in a CUDA graph, with grid barriers between the stage phases;
- * mode 0 launches one graph of batched stage kernels per step; other values
- * only report. Returns the mode in effect. Both give the same costs. */
+ * captured in a CUDA graph, whose CTAs draw (instance, stage phase, tile)
+ * units from a device work queue, each unit waiting only for its own
+ * instance's previous phase; mode 0 launches one graph of batched stage
+ * kernels per step; other values only report. Returns the mode in effect.
+ * Both give the same costs, bit for bit. */
 int mgd_batch_persistent(mgd_batch* batch, int mode);
 /* CTAs of the persistent launch (co-resident on the device). */
 int mgd_batch_persistent_grid(mgd_batch* batch);
@@ -431,9 +433,10 @@ int mgd_profile_stage_kernels(mgd_ctx* ctx, int mode, int reps, double* avg_ms, 
  * CUDA's pow (ref), for checking the viscosity law's error bound. */
 int mgd_selftest_pow(const double* x, int n, double e, double* fast, double* ref);
 
-/* Self-test of the grid barrier of the persistent batched kernel (no
- * reference counterpart): a cooperative launch of n_blocks CTAs meets
- * `rounds` times at a barrier that expects `expected` arrivals; after each
+/* Self-test of the bounded wait of the persistent batched kernel (no
+ * reference counterpart), used as a grid barrier: a cooperative launch of
+ * n_blocks CTAs meets `rounds` times at a barrier that expects `expected`
+ * arrivals; after each
  * meeting CTA 0 sums stamps the others wrote before it, into *checksum
  * (rounds (rounds + 1) / 2 * n_blocks (n_blocks + 1) / 2 when every round
  * completes). A wait gives up after `limit` polls of about 100 ns: with

@@ -37,7 +37,9 @@ struct mgd_batch {
   // in a graph per step count
   bool persistent = true;
   int4* dUnitsA = nullptr;
-  unsigned int* dBarrier = nullptr;
+  int4* dUnitsB = nullptr;
+  int4* dCounts = nullptr;              // per instance {round A, B, C units}
+  unsigned long long* dQueue = nullptr;  // {next unit, done[instance]...}
   int* dStatus = nullptr;
   PersistentPlan plan;
   int persistentGrid = 0;
@@ -76,7 +78,9 @@ static void destroyBatch(mgd_batch* b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   if (b->graphP) cudaGraphExecDestroy(b->graphP);
   cudaFree(b->dUnitsA);
-  cudaFree(b->dBarrier);
+  cudaFree(b->dUnitsB);
+  cudaFree(b->dCounts);
+  cudaFree(b->dQueue);
   cudaFree(b->dStatus);
   cudaFree(b->dEntries);
   for (int k = 0; k < BK_COUNT; ++k) cudaFree(b->dMap[k]);
@@ -192,11 +196,13 @@ int mgd_batch_create(mgd_ctx* const* instances, int n_instances, mgd_batch** out
     return 1;
   }
   b->L.entries = b->dEntries;
-  // work of the persistent run: phase A = gradient/flux tiles, dissipation
-  // (tile, component) pairs, functional blocks (heaviest first); phase B =
-  // the divergence tiles (the BK_RHS map)
+  // work of the persistent run: round A = gradient/flux tiles, dissipation
+  // (tile, component) pairs, functional blocks (heaviest first); round B =
+  // divergence (tile, component) pairs (the BK_RHS map with the components);
+  // round C = blocks of points for the primitives (the BK_PRIMS map)
   {
-    std::vector<int4> unitsA;
+    std::vector<int4> unitsA, unitsB;
+    std::vector<int4> counts(n_instances, make_int4(0, 0, 0, 0));
     const int nU = c0.nU;
     for (int i = 0; i < n_instances; ++i)
       for (int j = 0; j < b->tiles[i][BK_GRAD].blocks(); ++j) unitsA.push_back(make_int4(0, i, j, 0));
@@ -206,9 +212,18 @@ int mgd_batch_create(mgd_ctx* const* instances, int n_instances, mgd_batch** out
           for (int cc = 0; cc < nU; ++cc) unitsA.push_back(make_int4(1, i, j, cc));
     for (int i = 0; i < n_instances; ++i)
       for (int j = 0; j < reductionBlocks(b->inst[i]->c.blocks[0]); ++j) unitsA.push_back(make_int4(2, i, j, 0));
+    for (int cc = 0; cc < nU; ++cc)
+      for (const int2& m : maps[BK_RHS]) unitsB.push_back(make_int4(m.x, m.y, cc, 0));
+    for (const int4& u : unitsA) counts[u.y].x += 1;
+    for (const int4& u : unitsB) counts[u.x].y += 1;
+    for (const int2& m : maps[BK_PRIMS]) counts[m.x].z += 1;
     if (cudaMalloc((void**)&b->dUnitsA, unitsA.size() * sizeof(int4)) != cudaSuccess ||
         cudaMemcpy(b->dUnitsA, unitsA.data(), unitsA.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMalloc((void**)&b->dBarrier, 3 * sizeof(unsigned int)) != cudaSuccess ||
+        cudaMalloc((void**)&b->dUnitsB, unitsB.size() * sizeof(int4)) != cudaSuccess ||
+        cudaMemcpy(b->dUnitsB, unitsB.data(), unitsB.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMalloc((void**)&b->dCounts, counts.size() * sizeof(int4)) != cudaSuccess ||
+        cudaMemcpy(b->dCounts, counts.data(), counts.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMalloc((void**)&b->dQueue, (1 + (size_t)n_instances) * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc((void**)&b->dStatus, sizeof(int)) != cudaSuccess) {
       g_batchCreateError = "device allocation failed for the persistent run";
       destroyBatch(b);
@@ -216,12 +231,16 @@ int mgd_batch_create(mgd_ctx* const* instances, int n_instances, mgd_batch** out
     }
     b->plan.unitsA = b->dUnitsA;
     b->plan.nA = (int)unitsA.size();
-    b->plan.unitsB = b->dMap[BK_RHS];
-    b->plan.nB = b->L.blocks[BK_RHS];
-    b->plan.barrier = b->dBarrier;
+    b->plan.unitsB = b->dUnitsB;
+    b->plan.nB = (int)unitsB.size();
+    b->plan.unitsC = b->dMap[BK_PRIMS];
+    b->plan.nC = b->L.blocks[BK_PRIMS];
+    b->plan.counts = b->dCounts;
+    b->plan.work = b->dQueue;
+    b->plan.done = b->dQueue + 1;
     b->plan.status = b->dStatus;
-    // about 100 ns per poll: a wait gives up after about a second (a stage
-    // phase of the largest batches takes milliseconds)
+    // about 100 ns per poll: a wait gives up after about a second (a unit
+    // waits at most for the units of one round of its instance, milliseconds)
     b->plan.spinLimit = 1LL << 23;
     b->persistentGrid = std::min(persistentGridSize(c0), std::max(b->plan.nA, b->plan.nB));
     if (b->persistentGrid < 1) b->persistent = false;
@@ -238,12 +257,12 @@ int mgd_batch_persistent(mgd_batch* batch, int mode) {
 
 int mgd_batch_persistent_grid(mgd_batch* batch) { return batch ? batch->persistentGrid : 0; }
 
-// The persistent run: barrier and status reset, then one cooperative launch
+// The persistent run: work queue and status reset, then one cooperative launch
 // of every step, captured once per step count in a graph (launched directly
 // when the capture is refused).
 static int runPersistent(mgd_batch* b, int n_steps, bool functional) {
   Context& c0 = b->inst[0]->c;
-  BATCH_TRY(b, cudaMemsetAsync(b->dBarrier, 0, 3 * sizeof(unsigned int), b->stream));
+  BATCH_TRY(b, cudaMemsetAsync(b->dQueue, 0, (1 + b->inst.size()) * sizeof(unsigned long long), b->stream));
   BATCH_TRY(b, cudaMemsetAsync(b->dStatus, 0, sizeof(int), b->stream));
   if (!b->graphP || b->graphPSteps != n_steps) {
     if (b->graphP) cudaGraphExecDestroy(b->graphP);
@@ -273,7 +292,7 @@ static int runPersistent(mgd_batch* b, int n_steps, bool functional) {
   BATCH_TRY(b, cudaGetLastError());
   int status = 0;
   BATCH_TRY(b, cudaMemcpy(&status, b->dStatus, sizeof(int), cudaMemcpyDeviceToHost));
-  if (status) return bfail(b, "persistent batched run: a grid-barrier wait ran out of its spin limit");
+  if (status) return bfail(b, "persistent batched run: a wait for a unit's inputs ran out of its spin limit");
   return 0;
 }
 

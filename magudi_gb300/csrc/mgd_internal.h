@@ -350,20 +350,25 @@ struct BatchEntry {
   int controller;
 };
 
-// Work of the persistent batched run (one launch for all steps): phase A
-// units {kind, instance, tile, component} (kind 0 gradient/flux tile, 1
-// dissipation tile and component, 2 functional reduction block), phase B
-// tiles {instance, tile} (divergence and RK update of every component, then
-// the primitives). barrier = {arrivals, generation} of the grid barrier
-// between phases, and barrier[2] the work counter the CTAs draw a phase's
-// units from; status = 0, or 1 when a barrier wait ran out of its spin limit
-// (the kernel then returns early and the host reports the error).
+// Work of the persistent batched run (one launch for all steps), three
+// rounds per RK stage: round A units {kind, instance, tile, component} (kind
+// 0 gradient/flux tile, 1 dissipation tile and component, 2 functional
+// reduction block), round B units {instance, tile, component} (divergence and
+// RK update), round C units {instance, block of kBatchThreads points}
+// (primitives); counts[i] = {A, B, C units} of instance i. work = the next
+// unit of the run's global order, done[i] = units of instance i completed
+// (both zeroed before a launch); status = 0, or 1 when a wait ran out of its
+// spin limit (the kernel then returns early and the host reports the error).
 struct PersistentPlan {
   const int4* unitsA = nullptr;
   int nA = 0;
-  const int2* unitsB = nullptr;
+  const int4* unitsB = nullptr;
   int nB = 0;
-  unsigned int* barrier = nullptr;
+  const int2* unitsC = nullptr;
+  int nC = 0;
+  const int4* counts = nullptr;
+  unsigned long long* work = nullptr;
+  unsigned long long* done = nullptr;
   int* status = nullptr;
   long long spinLimit = 0;
 };
@@ -512,10 +517,23 @@ int selftestGridBarrier(int nBlocks, unsigned int expected, int rounds, long lon
                         long long* sum);
 void launchSetCounters(int* counters, int step, int segBase, cudaStream_t s);
 constexpr int kBatchThreads = 128;
-// Resident CTAs per SM that the persistent batched kernel is compiled for
-// (its register budget is 65536 / (128 x this)).
+// Resident CTAs per SM that the persistent batched kernel is compiled for,
+// 2D and 3D (its register budget is 65536 / (128 x this)). One kernel holds
+// the register budget of its largest phase (the gradient/flux tiles) in
+// every phase; at 64 2D monopole instances 12 CTAs per SM (40 registers, the
+// flux phase spilling to L1) ran faster than 6, 8, 10 or 16. The 3D flux
+// tiles need about twice the registers.
 #ifndef MGD_PERSISTENT_MIN_BLOCKS
-#define MGD_PERSISTENT_MIN_BLOCKS 6
+#define MGD_PERSISTENT_MIN_BLOCKS 12
+#endif
+#ifndef MGD_PERSISTENT_MIN_BLOCKS_3D
+#define MGD_PERSISTENT_MIN_BLOCKS_3D 6
+#endif
+constexpr int persistentMinBlocks(int nD) { return nD == 2 ? MGD_PERSISTENT_MIN_BLOCKS : MGD_PERSISTENT_MIN_BLOCKS_3D; }
+// Consecutive units the persistent batched kernel's CTAs draw at a time
+// (2: fewer draws and acquires than 1, a shorter tail than 4 or 8).
+#ifndef MGD_PERSISTENT_CHUNK
+#define MGD_PERSISTENT_CHUNK 2
 #endif
 constexpr int kMaxExcitationModes = 256;  // modes of one solenoidal-excitation patch
 

@@ -196,7 +196,13 @@ __device__ __forceinline__ PointIndex pointIndex(const BlockView& B, long long p
 }
 
 // Grid point of this thread in tile-block b under tiling T; false when the
-// tile overhangs the grid.
+// tile overhangs the grid. Along each axis the tile order puts the two edge
+// tiles first (0, n-1, 1, 2, ..., n-2): the edge tiles carry the boundary
+// closures and the SAT work, and the block scheduler hands out low block
+// indices first, so the heavy tiles spread over the SMs instead of landing,
+// with the last block row, on a few of them at the end.
+__device__ __forceinline__ int edgeTilesFirst(int k, int n) { return (k == 0 || n < 2) ? k : (k == 1 ? n - 1 : k - 1); }
+
 __device__ __forceinline__ bool locateAt(const BlockView& B, const Tile& T, int b, int t, long long& p,
                                          PointIndex& r) {
   // x / d by multiply-high with the tile's reciprocals (x >= 0, 32-bit)
@@ -205,7 +211,9 @@ __device__ __forceinline__ bool locateAt(const BlockView& B, const Tile& T, int 
   };
   const int t0 = q(t, 0), b0 = q(b, 2);
   const int lx = t - t0 * T.t[0], lz = q(t, 1), ly = t0 - lz * T.t[1];
-  const int bx = b - b0 * T.n[0], bz = q(b, 3), by = b0 - bz * T.n[1];
+  const int bz0 = q(b, 3);
+  const int bx = edgeTilesFirst(b - b0 * T.n[0], T.n[0]), by = edgeTilesFirst(b0 - bz0 * T.n[1], T.n[1]),
+            bz = edgeTilesFirst(bz0, T.n[2]);
   r.idx[0] = bx * T.t[0] + lx;
   r.idx[1] = by * T.t[1] + ly;
   r.idx[2] = bz * T.t[2] + lz;
@@ -1765,162 +1773,208 @@ __global__ void __launch_bounds__(kBlock) kFunctionalBatch(const BatchEntry* __r
 }
 
 // ---------------------------------------------------------------------------
-// Grid barrier of the persistent kernels (co-residency guaranteed by a
-// cooperative launch): bar[0] counts arrivals, bar[1] is the generation the
-// last arrival advances; the last arrival also zeroes *work (when given), the
-// work counter the CTAs draw the next phase's units from. A wait gives up
-// after `limit` polls (about 100 ns each), sets *err and returns false; a CTA
-// that sees *err set also returns false, so that every CTA leaves the kernel
-// and the host reads the status.
-// The fences order each CTA's writes before its arrival and the others'
-// reads after their departure: the fence after the wait acquires, so the
-// ordinary loads that follow observe the other CTAs' writes (stencil taps of
-// such data avoid the read-only path, see tap()).
+// Bounded wait of the persistent kernels, run by thread 0 of a CTA: polls the
+// monotonic counter *count (about 100 ns per poll) until it reaches `need`.
+// It gives up after `limit` polls, sets *err and returns false; it also
+// returns false once another CTA has set *err, so that every CTA leaves the
+// kernel and the host reads the status. The acquire fence after the wait
+// (which also discards the SM's L1 lines) lets the CTA's loads after its next
+// CTA barrier see what the counted producers wrote before their releases
+// (__threadfence, then the atomic add to *count).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool gridBarrier(unsigned int* bar, unsigned int nBlocks, long long limit, int* err,
-                                            unsigned int* work = nullptr) {
+__device__ __forceinline__ bool waitCount(const unsigned long long* count, unsigned long long need, long long limit,
+                                          int* err) {
+  volatile const unsigned long long* vc = count;
+  volatile int* verr = err;
+  long long polls = 0;
+  bool ok = true;
+  while (*vc < need) {
+    if (*verr) {
+      ok = false;
+      break;
+    }
+    if (++polls > limit) {
+      atomicExch(err, 1);
+      ok = false;
+      break;
+    }
+    __nanosleep(64);
+  }
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
+  return ok;
+}
+
+// Persistent batched forward run: every step's four RK stages for every
+// instance in one launch, scheduled as a device work queue.
+//
+// The run is a sequence of rounds, three per RK stage, each the work of one
+// stage kernel of the per-step path: A (gradient/flux tiles, dissipation
+// (tile, component) units, and the functional blocks of the stage before),
+// B (divergence and RK update, per (tile, component)) and C (primitives of
+// the new state, per block of points); after the last stage one more A in
+// which only the functional blocks of the last stage work. All units of all
+// rounds form one global order, round by round (within a round the unit
+// lists' order: heavy gradient/flux tiles first). CTAs draw the next chunk of
+// K consecutive units of that order from one counter and work them in order.
+// A unit of instance i in round r depends only on instance i's units of
+// round r-1: before working, the CTA waits until done[i], the count of
+// instance i's completed units, reaches the number of its units in all
+// rounds before r; after the unit it adds one to done[i]. Instances
+// therefore advance independently, with no grid-wide barrier, and a CTA that
+// would wait for instance i's last units of a round takes units of the other
+// instances meanwhile (they come between them in the order).
+//
+// Progress: a unit waits only for units that come earlier in the global
+// order, which were drawn earlier by co-resident CTAs (cooperative launch)
+// and are worked in order within a chunk; the earliest incomplete unit has
+// nothing left to wait for. Every wait gives up after plan.spinLimit polls,
+// sets *plan.status and leaves; the others see the status at their next poll
+// and leave too.
+//
+// Memory order: the producer's threads write, meet at a CTA barrier, and its
+// thread 0 fences and then adds to done[i] (release); the consumer's thread 0
+// reads done[i], fences (acquire, which also discards the SM's L1 lines) and
+// meets its threads at a CTA barrier before they read. A CTA acquires once
+// per (instance, round) in a row: the inputs of a round stay unchanged until
+// all of the round's units are done, and no unit of an earlier round of that
+// instance is still running to load older copies. Data of round r is
+// written only by round r's units and read only by later rounds' units (or
+// by units of round r that write other arrays), so ordinary cached loads see
+// the producers' values. The per-point arithmetic is that of the stage
+// kernels, so the results equal the per-step launches'.
+template <int ND, bool CURV, bool VISC>
+__global__ void __launch_bounds__(kBatchThreads, persistentMinBlocks(ND))
+    kBatchRunPersistent(const BatchEntry* __restrict__ E, PersistentPlan plan, Physics P, int nSteps,
+                        int functional) {
+  __shared__ long long sBase;
+  __shared__ int sUnit, sPhase, sStep, sFStep, sStage, sInst;
+  constexpr int nU = ND + 2;
+  constexpr int K = MGD_PERSISTENT_CHUNK;
+  const PrimLayout L{ND};
+  const long long perStage = (long long)plan.nA + plan.nB + plan.nC;
+  const long long nRun = 4LL * nSteps * perStage + (functional ? plan.nA : 0);
+  // thread 0: the (instance, round) whose inputs this CTA last acquired
+  int heldInst = -1;
+  long long heldRound = -1;
+  for (;;) {
+    __syncthreads();  // every thread has finished the previous chunk
+    if (threadIdx.x == 0) sBase = (long long)atomicAdd(plan.work, (unsigned long long)K);
+    __syncthreads();
+    const long long base = sBase;
+    if (base >= nRun) return;
+    const int nk = (int)(nRun - base < K ? nRun - base : K);
+    for (int k = 0; k < nk; ++k) {
+      if (threadIdx.x == 0) {
+        const long long g = base + k;
+        const long long s = g / perStage;
+        long long off = g - s * perStage;
+        int phase = 0, inst;
+        if (off < plan.nA) {
+          inst = plan.unitsA[off].y;
+        } else if (off < plan.nA + plan.nB) {
+          phase = 1;
+          off -= plan.nA;
+          inst = plan.unitsB[off].x;
+        } else {
+          phase = 2;
+          off -= plan.nA + plan.nB;
+          inst = plan.unitsC[off].x;
+        }
+        const long long round = 3 * s + phase;
+        bool ok = true;
+        if (inst != heldInst || round != heldRound) {
+          const int4 cnt = plan.counts[inst];
+          const unsigned long long need = (unsigned long long)s * (unsigned long long)(cnt.x + cnt.y + cnt.z) +
+                                          (phase >= 1 ? (unsigned long long)cnt.x : 0ULL) +
+                                          (phase == 2 ? (unsigned long long)cnt.y : 0ULL);
+          ok = waitCount(plan.done + inst, need, plan.spinLimit, plan.status);
+          heldInst = inst;
+          heldRound = round;
+        }
+        const int step = (int)(s / 4) + 1, stage = (int)(s % 4) + 1;
+        sStep = step;
+        sStage = stage;
+        sFStep = stage > 1 ? step : step - 1;
+        sInst = inst;
+        sPhase = ok ? phase : -1;
+        sUnit = (int)off;
+      }
+      __syncthreads();
+      const int phase = sPhase;
+      if (phase < 0) return;
+      const int u = sUnit, stage = sStage;
+      if (phase == 0) {
+        // round A, or the closing functional round (stage index past the run)
+        const int4 w = plan.unitsA[u];
+        const BatchEntry& e = E[w.y];
+        const bool closing = sStep > nSteps;
+        if (w.x == 0 && !closing) {
+          RunScalars rs = e.rs;
+          rs.step = &sStep;
+          gradFluxPoint<ND, CURV, VISC, 1, false>(e.v, P, rs, GF_FLUX, stage, e.tGrad, w.z);
+        } else if (w.x == 1 && !closing) {
+          dissipationPoint<ND, false>(e.v, P, e.v.q, 1.0, e.tDiss, w.z, w.w);
+        } else if (w.x == 2 && functional && sFStep >= 1) {
+          RunScalars rs = e.rs;
+          rs.step = &sFStep;
+          functionalBlock(e.v, rs, stage > 1 ? stage - 1 : 4, L.p(), w.z);
+        }
+      } else if (phase == 1) {
+        const int4 w = plan.unitsB[u];
+        const BatchEntry& e = E[w.x];
+        RunScalars rs = e.rs;
+        rs.step = &sStep;
+        forwardDivergencePoint<ND, false>(e.v, P, rs, stage, stage, e.controller, e.tRhs, w.y, 0, 0.0, w.z);
+      } else {
+        const int2 w = plan.unitsC[u];
+        const BlockView& B = E[w.x].v;
+        const long long p = (long long)w.y * kBatchThreads + threadIdx.x;
+        if (p < B.N) {
+          double q[nU], pr[6 + ND];
+          for (int c = 0; c < nU; ++c) q[c] = B.q[p + B.N * c];
+          primitives<ND>(q, P, pr);
+          for (int c = 0; c < 6 + ND; ++c) B.prim[p + B.N * c] = pr[c];
+        }
+      }
+      __syncthreads();  // the unit's writes precede the release below
+      if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(plan.done + sInst, 1ULL);
+      }
+    }
+  }
+}
+
+// Self-test of the persistent kernels' bounded wait: `rounds` rounds in
+// which every CTA writes its round stamp, adds one to a counter (release) and
+// waits until the counter reaches round x `expected`; CTA 0 then sums all
+// stamps (checking that each CTA sees the others' writes after the wait), and
+// a second meeting keeps the stamps of the next round from overwriting them
+// early. With `expected` above the number of CTAs no round completes: every
+// wait runs out after `limit` polls and the kernel returns with status 1.
+__device__ __forceinline__ bool meet(unsigned long long* count, unsigned long long need, long long limit, int* err) {
   __shared__ int sOk;
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned int* vgen = bar + 1;
-    volatile int* verr = err;
-    const unsigned int gen = *vgen;
     __threadfence();
-    const unsigned int arrived = atomicAdd(bar, 1u) + 1u;
-    int ok = 1;
-    if (arrived == nBlocks) {
-      atomicExch(bar, 0u);
-      // every CTA has finished the phase: nobody draws from the counter
-      // until the generation advances
-      if (work) atomicExch(work, 0u);
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
-      long long polls = 0;
-      while (*vgen == gen) {
-        if (*verr) {
-          ok = 0;
-          break;
-        }
-        if (++polls > limit) {
-          atomicExch(err, 1);
-          ok = 0;
-          break;
-        }
-        __nanosleep(100);
-      }
-    }
-    asm volatile("fence.acq_rel.gpu;" ::: "memory");
-    __threadfence();
-    sOk = ok;
+    atomicAdd(count, 1ULL);
+    sOk = waitCount(count, need, limit, err);
   }
   __syncthreads();
   return sOk != 0;
 }
 
-// Persistent batched forward run: every step's four RK stages for every
-// instance in one launch. Per stage, phase A (gradient/flux tiles,
-// dissipation tiles, and the functional of the stage before, which reads the
-// primitives phase A leaves alone) and phase B (divergence and RK update of
-// all components of a point, then its primitives) are separated by grid
-// barriers; the per-point arithmetic is that of the stage kernels, so the
-// results equal the per-step launches'. The CTAs draw the units of a phase
-// one at a time from a work counter (plan.barrier[2]), in list order (the
-// heavy gradient/flux tiles first), so that a CTA that finishes early takes
-// more work, as the hardware's block scheduler would give it; the last CTA to
-// reach a barrier zeroes the counter for the next phase. The step of the
-// current phase is held in shared memory and handed to the point functions
-// through their run scalars.
-__device__ __forceinline__ int drawUnit(unsigned int* work) {
-  __shared__ int sUnit;
-  __syncthreads();  // every thread has read the previous unit
-  if (threadIdx.x == 0) sUnit = (int)atomicAdd(work, 1u);
-  __syncthreads();
-  return sUnit;
-}
-
-template <int ND, bool CURV, bool VISC>
-__global__ void __launch_bounds__(kBatchThreads, MGD_PERSISTENT_MIN_BLOCKS)
-    kBatchRunPersistent(const BatchEntry* __restrict__ E, PersistentPlan plan, Physics P, int nSteps,
-                        int functional) {
-  __shared__ int sStep, sFStep;
-  constexpr int nU = ND + 2;
-  const PrimLayout L{ND};
-  const unsigned int nBlocks = gridDim.x;
-  unsigned int* work = plan.barrier + 2;
-  for (int step = 1; step <= nSteps; ++step) {
-    for (int stage = 1; stage <= 4; ++stage) {
-      if (threadIdx.x == 0) {
-        sStep = step;
-        sFStep = stage > 1 ? step : step - 1;
-      }
-      const int fStage = stage > 1 ? stage - 1 : 4;
-      for (int u = drawUnit(work); u < plan.nA; u = drawUnit(work)) {
-        const int4 w = plan.unitsA[u];
-        const BatchEntry& e = E[w.y];
-        if (w.x == 0) {
-          RunScalars rs = e.rs;
-          rs.step = &sStep;
-          gradFluxPoint<ND, CURV, VISC, 1, false>(e.v, P, rs, GF_FLUX, stage, e.tGrad, w.z);
-        } else if (w.x == 1) {
-          dissipationPoint<ND, false>(e.v, P, e.v.q, 1.0, e.tDiss, w.z, w.w);
-        } else if (functional && sFStep >= 1) {
-          RunScalars rs = e.rs;
-          rs.step = &sFStep;
-          functionalBlock(e.v, rs, fStage, L.p(), w.z);
-        }
-      }
-      if (!gridBarrier(plan.barrier, nBlocks, plan.spinLimit, plan.status, work)) return;
-      for (int u = drawUnit(work); u < plan.nB; u = drawUnit(work)) {
-        const int2 w = plan.unitsB[u];
-        const BatchEntry& e = E[w.x];
-        RunScalars rs = e.rs;
-        rs.step = &sStep;
-        for (int c = 0; c < nU; ++c)
-          forwardDivergencePoint<ND, false>(e.v, P, rs, stage, stage, e.controller, e.tRhs, w.y, 0, 0.0, c);
-        long long p;
-        PointIndex I;
-        if (locate(e.v, e.tRhs, w.y, p, I)) {
-          const long long N = e.v.N;
-          double q[nU], pr[6 + ND];
-          for (int c = 0; c < nU; ++c) q[c] = e.v.q[p + N * c];
-          primitives<ND>(q, P, pr);
-          for (int c = 0; c < 6 + ND; ++c) e.v.prim[p + N * c] = pr[c];
-        }
-      }
-      if (!gridBarrier(plan.barrier, nBlocks, plan.spinLimit, plan.status, work)) return;
-    }
-  }
-  // the functional of the last stage
-  if (functional) {
-    if (threadIdx.x == 0) sFStep = nSteps;
-    __syncthreads();
-    for (int u = blockIdx.x; u < plan.nA; u += gridDim.x) {
-      const int4 w = plan.unitsA[u];
-      if (w.x != 2) continue;
-      RunScalars rs = E[w.y].rs;
-      rs.step = &sFStep;
-      functionalBlock(E[w.y].v, rs, 4, L.p(), w.z);
-    }
-  }
-}
-
-// Self-test of the grid barrier: `rounds` rounds in which every CTA writes its
-// round stamp, meets the others at the barrier and CTA 0 sums all stamps
-// (checking that each CTA sees the others' writes after the barrier). With
-// `expected` above the number of CTAs the barrier can never complete: every
-// wait runs out after `limit` polls and the kernel returns with status 1.
-__global__ void kBarrierSelfTest(unsigned int* bar, int* err, long long limit, unsigned int expected, int rounds,
-                                 long long* stamps, long long* sum) {
+__global__ void kBarrierSelfTest(unsigned long long* count, int* err, long long limit, unsigned int expected,
+                                 int rounds, long long* stamps, long long* sum) {
   for (int r = 1; r <= rounds; ++r) {
     if (threadIdx.x == 0) stamps[blockIdx.x] = (long long)r * (blockIdx.x + 1);
-    if (!gridBarrier(bar, expected, limit, err)) return;
+    if (!meet(count, (2ULL * r - 1) * expected, limit, err)) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       long long t = 0;
-      for (unsigned int b = 0; b < gridDim.x; ++b) t += *(volatile long long*)(stamps + b);
+      for (unsigned int b = 0; b < gridDim.x; ++b) t += stamps[b];
       sum[0] += t;
     }
-    if (!gridBarrier(bar, expected, limit, err)) return;
+    if (!meet(count, 2ULL * r * expected, limit, err)) return;
   }
 }
 
@@ -2424,14 +2478,14 @@ static int persistentOccupancy() {
 
 int selftestGridBarrier(int nBlocks, unsigned int expected, int rounds, long long limit, int* status,
                         long long* sum) {
-  unsigned int* bar = nullptr;
+  unsigned long long* bar = nullptr;
   int* err = nullptr;
   long long *stamps = nullptr, *dsum = nullptr;
-  cudaError_t e = cudaMalloc((void**)&bar, 2 * sizeof(unsigned int));
+  cudaError_t e = cudaMalloc((void**)&bar, sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMalloc((void**)&err, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc((void**)&stamps, (size_t)nBlocks * sizeof(long long));
   if (e == cudaSuccess) e = cudaMalloc((void**)&dsum, sizeof(long long));
-  if (e == cudaSuccess) e = cudaMemset(bar, 0, 2 * sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMemset(bar, 0, sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMemset(err, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(dsum, 0, sizeof(long long));
   if (e == cudaSuccess) {

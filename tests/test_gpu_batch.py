@@ -101,11 +101,30 @@ def test_persistent_launch_equals_per_step_graphs_and_oracle():
     assert np.array_equal(b1.run_forward(N_STEPS), c1)
 
 
+def test_persistent_queue_many_instances_equals_per_step_graphs():
+    """Sixteen instances of four sizes: the work queue interleaves their
+    units, and a unit waits only for its own instance's previous phase;
+    costs and states equal the per-step graph path's bit for bit."""
+    sizes = [(41, 37), (65, 63), (33, 45), (97, 81)]
+
+    def make():
+        return [Solver(small_monopole(n=sizes[i % 4][0], ny=sizes[i % 4][1], n_steps=8)) for i in range(16)]
+
+    per_step, persistent = make(), make()
+    b0, b1 = Batch(per_step), Batch(persistent)
+    b0.persistent(0)
+    assert b1.persistent() == 1
+    c0, c1 = b0.run_forward(8), b1.run_forward(8)
+    assert np.array_equal(c0, c1)
+    for s0, s1 in zip(per_step, persistent):
+        assert np.array_equal(s0.get_field(1, capi.FIELD_CONSERVED), s1.get_field(1, capi.FIELD_CONSERVED))
+
+
 def test_grid_barrier_completes_and_its_wait_runs_out_without_a_fault():
-    """The persistent kernel's grid barrier: 64 CTAs meet 50 times and see
-    each other's writes; then a barrier that expects one CTA more than the
-    launch has (an arrival that never comes) gives up after its poll limit,
-    returns status 1, and the context stays usable."""
+    """The persistent kernel's bounded wait, used as a grid barrier: 64 CTAs
+    meet 50 times and see each other's writes; then a barrier that expects
+    one CTA more than the launch has (an arrival that never comes) gives up
+    after its poll limit, returns status 1, and the context stays usable."""
     import ctypes as C
     from magudi_gb300.solver import load_library
     L = load_library()
