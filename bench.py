@@ -253,7 +253,7 @@ KERNEL_UNITS = {
     # q 4 read, prim 8 written
     "forward_primitives": {"bytes": 8 * (4 + 8), "flops": 69},
     # lambda 4, metric diagonal 2, prim (u 2, v, T, mu, la, k) 7, tau 4, hf 2, jac 1 read; rcore 4, ad 6 written
-    "adjoint_core": {"bytes": 8 * (4 + 2 + 7 + 4 + 2 + 1 + 4 + 6) + 4 * 3, "flops": 480},
+    "adjoint_core": {"bytes": 8 * (4 + 2 + 7 + 4 + 2 + 1 + 4 + 6) + 4 * 3, "flops": 469},
     # lambda 4 read, dq 4 written
     "adjoint_dissipation": {"bytes": 8 * (4 + 4), "flops": 122},
     # ad 6 read, t2 3 written

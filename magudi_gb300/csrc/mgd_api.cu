@@ -109,6 +109,9 @@ int mgd_create(const mgd_options* o, mgd_ctx** out) {
   P.g = o->ratio_of_specific_heats;
   P.gm1 = P.g - 1.0;
   P.gOverGm1 = P.g / P.gm1;
+  P.invGm1 = 1.0 / P.gm1;
+  P.gm2OverGm1 = (P.g - 2.0) / P.gm1;
+  P.invG = 1.0 / P.g;
   P.viscous = o->viscous;
   P.dissipation = o->dissipation;
   P.composite = o->composite_dissipation;

@@ -393,11 +393,16 @@ __host__ __device__ inline void incomingJacobian(const S* cv, const double* metr
 // y += (A_i - B1_i)^T w for the inviscid flux Jacobian A along metric m
 // (computeJacobianOfInviscidFlux{2D,3D}, src/CNSHelperImpl.f90:1098-1445) and
 // the first partial viscous Jacobian B1 (computeFirstPartialViscousJacobian,
-// :2412-2601), formed column by column and contracted immediately.
-template <int ND, bool VISC>
+// :2412-2601), formed column by column and contracted immediately. P
+// supplies g and the ratios 1/(g-1), (g-2)/(g-1) and 1/g computed once on
+// the host: the per-point divisions by g - 1 and g become multiplications
+// (an FP64 division is about ten FP64 instructions), which changes only
+// rounding.
+template <int ND, bool VISC, class Phys>
 __device__ __forceinline__ void addFluxJacobianTransposeProduct(
-    const double* m, const double* u, double T, double v, double g, double n,
+    const double* m, const double* u, double T, double v, const Phys& P, double n,
     const double* tau, const double* hf, const double* w, double* y) {
+  const double g = P.g;
   constexpr int nU = ND + 2, E = ND + 1;
   double U = m[0] * u[0];
   for (int d = 1; d < ND; ++d) U += m[d] * u[d];
@@ -424,9 +429,9 @@ __device__ __forceinline__ void addFluxJacobianTransposeProduct(
     // j = 0
     double s = 0.0;
     for (int d = 0; d < ND; ++d) s += (phi2 * m[d] - U * u[d]) * w[1 + d];
-    s += U * ((g - 2.0) / (g - 1.0) * phi2 - T) * w[E];
+    s += U * (P.gm2OverGm1 * phi2 - T) * w[E];
     if (VISC) {
-      const double t2 = nTv * (phi2 / (g - 1.0) - T / g);
+      const double t2 = nTv * (phi2 * P.invGm1 - T * P.invG);
       double sb = 0.0;
       for (int d = 0; d < ND; ++d) sb += t2 * ct[d] * w[1 + d];
       sb += (t2 * t1 - v * uct) * w[E];
@@ -440,7 +445,7 @@ __device__ __forceinline__ void addFluxJacobianTransposeProduct(
       const double a = d == c ? U - (g - 2.0) * u[c] * m[c] : u[d] * m[c] - (g - 1.0) * u[c] * m[d];
       s += a * w[1 + d];
     }
-    s += ((T + phi2 / (g - 1.0)) * m[c] - (g - 1.0) * U * u[c]) * w[E];
+    s += ((T + phi2 * P.invGm1) * m[c] - (g - 1.0) * U * u[c]) * w[E];
     if (VISC) {
       const double t2 = -nTv * u[c];
       double sb = 0.0;
@@ -606,10 +611,11 @@ __device__ __forceinline__ void secondPartialViscousProduct(const double* u, dou
 // leaves the remaining arithmetic unchanged; K, I and J are compile-time
 // constants once the callers' loops are unrolled. nTv = n g v / T is passed
 // in (it does not depend on the metric).
-template <int ND, bool VISC>
+template <int ND, bool VISC, class Phys>
 __device__ __forceinline__ void addFluxJacobianTransposeProductCart(
-    int K, double a, const double* u, double T, double v, double g, double nTv,
+    int K, double a, const double* u, double T, double v, const Phys& P, double nTv,
     const double* tau, const double* hf, const double* w, double* y) {
+  const double g = P.g;
   constexpr int E = ND + 1;
   const double U = a * u[K];
   double u2 = u[0] * u[0];
@@ -626,9 +632,9 @@ __device__ __forceinline__ void addFluxJacobianTransposeProductCart(
   {
     double s = 0.0;
     for (int d = 0; d < ND; ++d) s += (d == K ? phi2 * a - U * u[d] : -(U * u[d])) * w[1 + d];
-    s += U * ((g - 2.0) / (g - 1.0) * phi2 - T) * w[E];
+    s += U * (P.gm2OverGm1 * phi2 - T) * w[E];
     if (VISC) {
-      const double t2 = nTv * (phi2 / (g - 1.0) - T / g);
+      const double t2 = nTv * (phi2 * P.invGm1 - T * P.invG);
       double sb = 0.0;
       for (int d = 0; d < ND; ++d) sb += t2 * ct[d] * w[1 + d];
       sb += (t2 * t1 - v * uct) * w[E];
@@ -644,7 +650,7 @@ __device__ __forceinline__ void addFluxJacobianTransposeProductCart(
         const double q = d == c ? U - (g - 2.0) * u[c] * a : u[d] * a;
         s += q * w[1 + d];
       }
-      s += ((T + phi2 / (g - 1.0)) * a - (g - 1.0) * U * u[c]) * w[E];
+      s += ((T + phi2 * P.invGm1) * a - (g - 1.0) * U * u[c]) * w[E];
     } else {
       s = 0.0;
       for (int d = 0; d < ND; ++d) {

@@ -137,6 +137,9 @@ struct Tile {
 // Constants of the physics and of the run.
 struct Physics {
   double g, gm1, gOverGm1, reInv, prInv, powerLawExponent, laFactor;
+  // 1/(g-1), (g-2)/(g-1) and 1/g, so that the adjoint core multiplies
+  // instead of dividing per point
+  double invGm1, gm2OverGm1, invG;
   double dissipationAmount;
   int viscous, dissipation, composite;
 };

@@ -354,7 +354,7 @@ __device__ __forceinline__ void wallSatAdjoint(const BlockView& B, const Physics
   for (int d = 0; d < ND; ++d) mn[d] = B.metrics[p + N * (ND * (B.ff.normalDir[e] - 1) + d)];
   double y[nU];
   for (int c = 0; c < nU; ++c) y[c] = 0.0;
-  addFluxJacobianTransposeProduct<ND, false>(mn, u, T, v, P.g, 0.0, nullptr, nullptr, lam, y);
+  addFluxJacobianTransposeProduct<ND, false>(mn, u, T, v, P, 0.0, nullptr, nullptr, lam, y);
   // minus sum_l m_l (dp/dq) lambda_{1+l}, dp/dq = (gamma - 1) (|u|^2 / 2, -u, 1)
   double ml = mn[0] * lam[1];
   for (int l = 1; l < ND; ++l) ml += mn[l] * lam[1 + l];
@@ -912,10 +912,10 @@ __device__ __forceinline__ void adjointCoreDirection(const BlockView& B, const P
   for (int c = 0; c < nU; ++c) w[c] = applyOp<OP_D1ADJ>(B.lam + N * c + Ix.base[I], Ix.idx[I], B.ax[I]);
   for (int c = 0; c < nU; ++c) y[c] = 0.0;
   if (CURV) {
-    addFluxJacobianTransposeProduct<ND, VISC>(m + ND * I, u, Tm, v, P.g, P.powerLawExponent, tau, hf, w, y);
+    addFluxJacobianTransposeProduct<ND, VISC>(m + ND * I, u, Tm, v, P, P.powerLawExponent, tau, hf, w, y);
   } else {
     const double nTv = VISC ? P.powerLawExponent * P.g * v / Tm : 0.0;
-    addFluxJacobianTransposeProductCart<ND, VISC>(I, m[ND * I + I], u, Tm, v, P.g, nTv, tau, hf, w, y);
+    addFluxJacobianTransposeProductCart<ND, VISC>(I, m[ND * I + I], u, Tm, v, P, nTv, tau, hf, w, y);
   }
   if (VISC) {
 #pragma unroll
@@ -960,12 +960,12 @@ __device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physi
   if (CURV) {
 #pragma unroll
     for (int i = 0; i < ND; ++i)
-      addFluxJacobianTransposeProduct<ND, VISC>(m + ND * i, u, Tm, v, P.g, P.powerLawExponent, tau, hf, w[i], y);
+      addFluxJacobianTransposeProduct<ND, VISC>(m + ND * i, u, Tm, v, P, P.powerLawExponent, tau, hf, w[i], y);
   } else {
     const double nTv = VISC ? P.powerLawExponent * P.g * v / Tm : 0.0;
 #pragma unroll
     for (int i = 0; i < ND; ++i)
-      addFluxJacobianTransposeProductCart<ND, VISC>(i, m[ND * i + i], u, Tm, v, P.g, nTv, tau, hf, w[i], y);
+      addFluxJacobianTransposeProductCart<ND, VISC>(i, m[ND * i + i], u, Tm, v, P, nTv, tau, hf, w[i], y);
   }
   double ad[ND][nV];
   if (VISC) {

@@ -120,6 +120,32 @@ def test_persistent_queue_many_instances_equals_per_step_graphs():
         assert np.array_equal(s0.get_field(1, capi.FIELD_CONSERVED), s1.get_field(1, capi.FIELD_CONSERVED))
 
 
+def test_persistent_queue_3d_equals_per_step_graphs_and_single_solves():
+    """3D instances (periodic Taylor-Green grids of two sizes at a fixed step
+    size): the persistent kernel's 3D form equals the per-step graph path bit
+    for bit, and the single-solve path to rounding."""
+    from magudi_gb300 import configs
+
+    def problem(n):
+        P = configs.taylor_green_3d(n=n, n_steps=6, dt=2e-3, save_interval=6)
+        P.options.enable_functional = False
+        return P
+
+    sizes = (12, 16, 12)
+    per_step = [Solver(problem(n)) for n in sizes]
+    persistent = [Solver(problem(n)) for n in sizes]
+    b0, b1 = Batch(per_step), Batch(persistent)
+    b0.persistent(0)
+    assert b1.persistent() == 1
+    b0.run_forward(6)
+    b1.run_forward(6)
+    for s0, s1 in zip(per_step, persistent):
+        assert np.array_equal(s0.get_field(1, capi.FIELD_CONSERVED), s1.get_field(1, capi.FIELD_CONSERVED))
+    single = Solver(problem(16))
+    single.run_forward(6, 6)
+    assert rel_err(persistent[1].get_field(1, capi.FIELD_CONSERVED), single.get_field(1, capi.FIELD_CONSERVED)) < 1e-13
+
+
 def test_grid_barrier_completes_and_its_wait_runs_out_without_a_fault():
     """The persistent kernel's bounded wait, used as a grid barrier: 64 CTAs
     meet 50 times and see each other's writes; then a barrier that expects
