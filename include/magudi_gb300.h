@@ -321,15 +321,15 @@ int mgd_set_patch_control_forcing(mgd_ctx* ctx, const double* forcing);
 
 /* Resident trajectory (no reference counterpart; the reference always
  * recomputes checkpoint segments, src/SolverImpl.f90:1027-1245 with
- * UniformCheckpointer): with enable != 0, mgd_run_forward of a single-block
- * context also stores every RK stage's state, primitives, stress and heat
- * flux on the device when the 4 x n_steps stage slots fit in max_bytes
+ * UniformCheckpointer): with enable != 0, mgd_run_forward also stores every
+ * RK stage's state, primitives, stress and heat flux of every block on the
+ * device when the 4 x n_steps stage slots of all blocks fit in max_bytes
  * (<= 0: half of the free device memory), and the following mgd_run_adjoint
  * reads them instead of recomputing the segments between checkpoints. The
  * results are identical either way. mgd_run_linearized reads the same slots
- * and leaves them for a later mgd_run_adjoint. Runs that do not fit and
- * multi-block contexts recompute as usual. Off by default: a forward-only
- * user would hold the slots for nothing. */
+ * and leaves them for a later mgd_run_adjoint. Runs that do not fit
+ * recompute as usual. Off by default: a forward-only user would hold the
+ * slots for nothing. */
 int mgd_set_trajectory_storage(mgd_ctx* ctx, int enable, double max_bytes);
 
 /* adjoint_nonzero_initial_condition (src/SolverImpl.f90:1027-1102, set per

@@ -198,6 +198,11 @@ int mgd_destroy(mgd_ctx* h) {
   for (void* p : c.shadowAllocations) cudaFree(p);
   if (c.stream2) cudaStreamDestroy(c.stream2);
   if (c.side2) cudaStreamDestroy(c.side2);
+  for (int k = 0; k < MGD_MAX_BLOCKS; ++k) {
+    if (c.blockStreams[k]) cudaStreamDestroy(c.blockStreams[k]);
+    if (c.evBlockJoin[k]) cudaEventDestroy(c.evBlockJoin[k]);
+  }
+  if (c.evBlockFork) cudaEventDestroy(c.evBlockFork);
   for (int k = 0; k < 8; ++k) {
     cudaEventDestroy(c.evFork[k]);
     cudaEventDestroy(c.evJoin[k]);
@@ -2187,6 +2192,40 @@ static int reduceRegion(Context& c, int nSlots, std::vector<double>& out) {
 }
 
 // One forward RK stage of every block; store writes the stage slots.
+// Streams of the blocks of a region, created once per context (outside any
+// capture).
+static int ensureBlockStreams(Context& c) {
+  if (c.evBlockFork) return 0;
+  for (size_t bi = 0; bi < c.blocks.size() && bi < MGD_MAX_BLOCKS; ++bi) {
+    CUDA_TRY(c, cudaStreamCreateWithFlags(&c.blockStreams[bi], cudaStreamNonBlocking));
+    CUDA_TRY(c, cudaEventCreateWithFlags(&c.evBlockJoin[bi], cudaEventDisableTiming));
+  }
+  CUDA_TRY(c, cudaEventCreateWithFlags(&c.evBlockFork, cudaEventDisableTiming));
+  return 0;
+}
+
+// The same work for every block of a region, each block on its own stream,
+// forked from the context's stream and joined back into it (inside a capture
+// the block streams become parallel branches of the graph). A block's stage
+// kernels read and write only that block's arrays, so they may overlap; the
+// interface kernels, which read the partner blocks, run between a join and
+// the next fork.
+template <class F>
+static void forEachBlockConcurrently(Context& c, F f) {
+  const int n = (int)c.blocks.size();
+  if (n == 1 || !c.evBlockFork) {
+    for (int bi = 0; bi < n; ++bi) f(bi, c.stream);
+    return;
+  }
+  cudaEventRecord(c.evBlockFork, c.stream);
+  for (int bi = 0; bi < n; ++bi) {
+    cudaStreamWaitEvent(c.blockStreams[bi], c.evBlockFork, 0);
+    f(bi, c.blockStreams[bi]);
+    cudaEventRecord(c.evBlockJoin[bi], c.blockStreams[bi]);
+  }
+  for (int bi = 0; bi < n; ++bi) cudaStreamWaitEvent(c.stream, c.evBlockJoin[bi], 0);
+}
+
 static void regionRunStage(Context& c, std::vector<RunScalars>& rs, int i, bool controller, bool store,
                            bool functional) {
   const BlockRefs refs = blockRefs(c);
@@ -2200,21 +2239,24 @@ static void regionRunStage(Context& c, std::vector<RunScalars>& rs, int i, bool 
     launchExcitation(c, b, rs[bi], i, false, false, c.side);
   }
   cudaEventRecord(c.evJoin[0], c.side);
-  for (size_t bi = 0; bi < c.blocks.size(); ++bi) launchGradFlux(c, c.blocks[bi], true, false, &rs[bi], i, store);
+  forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
+    launchGradFlux(c, c.blocks[bi], true, false, &rs[bi], i, store, s);
+  });
   for (DevBlock& b : c.blocks) launchInterfaceSat(c, b, refs);
   cudaStreamWaitEvent(c.stream, c.evJoin[0], 0);
-  for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+  forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
     DevBlock& b = c.blocks[bi];
-    launchForwardDivergence(c, b, i, rs[bi], false, controller && bi == 0);
-    launchPrims(c, b, b.v.q, false);
-    if (functional) launchFunctional(c, b, rs[bi], i);
-  }
+    launchForwardDivergence(c, b, i, rs[bi], false, controller && bi == 0, s);
+    launchPrims(c, b, b.v.q, false, nullptr, 0, s);
+    if (functional) launchFunctional(c, b, rs[bi], i, s);
+  });
 }
 
 static int regionRunForward(Context& c, int n_steps, int save_interval, double t0, double* cost) {
   if (c.opts.functional_type != MGD_FUNCTIONAL_SOUND) return fail(c, "multi-block runs use the SOUND functional");
   const bool cflMode = c.opts.use_constant_cfl != 0;
   if (prepareForwardRun(c, n_steps, save_interval, t0, false)) return 1;
+  if (ensureBlockStreams(c)) return 1;
   const long long nSnap = n_steps / save_interval + 2;
   for (DevBlock& b : c.blocks) {
     if (growDevice(c, &b.runSnap, &b.runSnapCap, nSnap * c.nU * b.v.N)) return 1;
@@ -2224,12 +2266,40 @@ static int regionRunForward(Context& c, int n_steps, int save_interval, double t
   }
   const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
   const bool functional = c.opts.enable_functional != 0;
+  // with a resident trajectory the flux kernels of every block also store
+  // every stage's state, primitives, stress and heat flux (4 n_steps full
+  // slots per block), which the adjoint and tangent runs then read instead
+  // of recomputing checkpoint segments
+  bool resident = false;
+  c.trajectorySteps = 0;
+  const long long fullPer = c.nU + PrimLayout{c.nD}.count() + c.nD * c.nD + c.nD;
+  if (c.trajectoryStorage) {
+    size_t freeB = 0, totalB = 0;
+    CUDA_TRY(c, cudaMemGetInfo(&freeB, &totalB));
+    long long pts = 0, held = 0;
+    for (DevBlock& b : c.blocks) {
+      pts += b.v.N;
+      held += b.runStageCap;
+    }
+    const double need = 4.0 * n_steps * (double)(fullPer * pts) * sizeof(double);
+    const double budget =
+        c.trajectoryMaxBytes > 0.0 ? c.trajectoryMaxBytes : 0.5 * ((double)freeB + (double)held * sizeof(double));
+    resident = need <= budget;
+    if (resident)
+      for (DevBlock& b : c.blocks)
+        if (growDevice(c, &b.runStage, &b.runStageCap, 4LL * n_steps * fullPer * b.v.N)) return 1;
+  }
   std::vector<RunScalars> rs;
   const bool limits = c.opts.enable_solution_limits != 0;
   for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
     rs.push_back(blockRunScalars(c, c.blocks[bi], bi == 0));
     if (limits) rs.back().limitKey = c.dLimitKey;
+    if (resident) {
+      rs.back().slotFull = 1;
+      rs.back().slotStride = fullPer * c.blocks[bi].v.N;
+    }
   }
+  if (resident) c.slotFull = 1;
   if (setCounters(c, 1, 0)) return 1;
   if (capture(c, &c.gForward, &c.nodesForward, [&]() {
         // constant CFL: the step size from every block's state at the start of the step
@@ -2239,7 +2309,7 @@ static int regionRunForward(Context& c, int n_steps, int save_interval, double t
           if (limits)
             for (size_t bi = 0; bi < c.blocks.size(); ++bi)
               launchSolutionLimits(c, c.blocks[bi], (int)bi, c.dCounters, i, c.dLimitKey);
-          regionRunStage(c, rs, i, controller, false, functional);
+          regionRunStage(c, rs, i, controller, resident, functional);
         }
         for (DevBlock& b : c.blocks) launchSnapshot(c, b, b.runSnap, save_interval, false);
         launchStepAdvance(c, 1);
@@ -2264,15 +2334,22 @@ static int regionRunForward(Context& c, int n_steps, int save_interval, double t
       for (int i = 0; i < 4; ++i) J = J + kRkNorm[i] * c.stepDt[s] * vals[(size_t)4 * s + i];
   }
   *cost = J;
+  c.trajectorySteps = resident ? n_steps : 0;
   if (const int st = limitOutcome(c, cost, false)) {
     c.limitViolated = st == MGD_SOLUTION_LIMITS;
+    c.trajectorySteps = 0;
     return st;
   }
   return 0;
 }
 
 static int regionRunAdjoint(Context& c, double* sensitivity) {
-  const int nU = c.nU, nD = c.nD, T = c.runSteps, S = c.saveInterval;
+  if (ensureBlockStreams(c)) return 1;
+  const int nU = c.nU, nD = c.nD, T = c.runSteps;
+  // a resident trajectory of this run: one segment over all steps, every
+  // stage read from its slot, no recomputation
+  const bool resident = c.trajectorySteps == T;
+  const int S = resident ? T : c.saveInterval;
   const double dtT = c.stepDt[T - 1];
   // stage slots: full (state, primitives, stress, heat flux) when they fit in half the free memory
   size_t freeB = 0, totalB = 0;
@@ -2283,7 +2360,8 @@ static int regionRunAdjoint(Context& c, double* sensitivity) {
     held += b.runStageCap;
   }
   const long long fullPer = nU + PrimLayout{nD}.count() + nD * nD + nD;
-  const bool full = (double)(4LL * S * fullPer * pts) * sizeof(double) <= 0.5 * ((double)freeB + held * 8.0);
+  const bool full =
+      resident || (double)(4LL * S * fullPer * pts) * sizeof(double) <= 0.5 * ((double)freeB + held * 8.0);
   for (DevBlock& b : c.blocks) {
     const long long stride = (full ? fullPer : nU) * b.v.N;
     if (growDevice(c, &b.runStage, &b.runStageCap, 4LL * S * stride)) return 1;
@@ -2304,7 +2382,7 @@ static int regionRunAdjoint(Context& c, double* sensitivity) {
     launchPrims(c, b, b.v.q, false);
     launchAdjointInitial(c, b, c.opts.adjoint_forcing_switch ? -dtT / 6.0 : 0.0);
   }
-  if (capture(c, &c.gRecomputeH[0], &c.nodesRecompute, [&]() {
+  if (!resident && capture(c, &c.gRecomputeH[0], &c.nodesRecompute, [&]() {
         for (int i = 1; i <= 4; ++i) regionRunStage(c, rs, i, controller, true, false);
         launchStepAdvance(c, 1);
       }))
@@ -2312,14 +2390,15 @@ static int regionRunAdjoint(Context& c, double* sensitivity) {
   if (capture(c, &c.gAdjointH[0], &c.nodesAdjoint, [&]() {
         for (int i = 4; i >= 1; --i) {
           if (!full)
-            for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+            forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
               DevBlock& b = c.blocks[bi];
-              launchPrims(c, b, nullptr, true, &rs[bi], i);
-              if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs[bi], i, false);
-            }
+              launchPrims(c, b, nullptr, true, &rs[bi], i, s);
+              if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs[bi], i, false, s);
+            });
           // dissipation, excitation and gradient/sensitivity of every block on
           // the side stream (they read lambda and the forward state of the
-          // stage); interface SATs, cores and diffusion on the main stream
+          // stage); interface SATs on the main stream, then the cores and
+          // diffusion of the blocks on their own streams
           cudaEventRecord(c.evFork[1], c.stream);
           cudaStreamWaitEvent(c.side, c.evFork[1], 0);
           for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
@@ -2331,14 +2410,15 @@ static int regionRunAdjoint(Context& c, double* sensitivity) {
           cudaEventRecord(c.evJoin[1], c.side);
           for (size_t bi = 0; bi < c.blocks.size(); ++bi)
             launchInterfaceSatAdjoint(c, c.blocks[bi], refs, &rs[bi], i, full);
-          for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+          forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
             DevBlock& b = c.blocks[bi];
-            launchAdjointCore(c, b, rs[bi], i, full);
-            launchAdjointDiffusion(c, b);
-          }
+            launchAdjointCore(c, b, rs[bi], i, full, s);
+            launchAdjointDiffusion(c, b, s);
+          });
           cudaStreamWaitEvent(c.stream, c.evJoin[1], 0);
-          for (size_t bi = 0; bi < c.blocks.size(); ++bi)
-            launchAdjointAssemble(c, c.blocks[bi], i, rs[bi], i, 0.0, false, full);
+          forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
+            launchAdjointAssemble(c, c.blocks[bi], i, rs[bi], i, 0.0, false, full, s);
+          });
         }
         launchStepAdvance(c, -1);
       }))
@@ -2346,16 +2426,19 @@ static int regionRunAdjoint(Context& c, double* sensitivity) {
   const int nSeg = (T + S - 1) / S;
   for (int k = nSeg - 1; k >= 0; --k) {
     const int L = k * S, end = std::min(T, L + S);
-    for (DevBlock& b : c.blocks) {
-      CUDA_TRY(c, cudaMemcpyAsync(b.v.q, b.runSnap + (size_t)k * nU * b.v.N, (size_t)nU * b.v.N * sizeof(double),
-                                  cudaMemcpyDeviceToDevice, c.stream));
-      launchPrims(c, b, b.v.q, false);
+    if (!resident) {
+      for (DevBlock& b : c.blocks) {
+        CUDA_TRY(c, cudaMemcpyAsync(b.v.q, b.runSnap + (size_t)k * nU * b.v.N, (size_t)nU * b.v.N * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, c.stream));
+        launchPrims(c, b, b.v.q, false);
+      }
+      launchSetCounters(c.dCounters, L + 1, L, c.stream);
+      for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gRecomputeH[0], c.stream));
+      c.launches += (long long)(end - L) * c.nodesRecompute;
     }
-    launchSetCounters(c.dCounters, L + 1, L, c.stream);
-    for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gRecomputeH[0], c.stream));
     launchSetCounters(c.dCounters, end, L, c.stream);
     for (int s = end; s >= L + 1; --s) CUDA_TRY(c, cudaGraphLaunch(c.gAdjointH[0], c.stream));
-    c.launches += (long long)(end - L) * (c.nodesRecompute + c.nodesAdjoint);
+    c.launches += (long long)(end - L) * c.nodesAdjoint;
   }
   if (checkLaunch(c)) return 1;
   std::vector<double> vals;
@@ -2990,7 +3073,12 @@ int mgd_selftest_pow(const double* x, int n, double e, double* fast, double* ref
 // with the block-interface SATs between the blocks' fluxes and divergences.
 static int regionRunLinearized(Context& c, const double* delta_forcing, long long n_entries, double* delta_cost) {
   if (refuseLinearized(c)) return 1;
-  const int nU = c.nU, nD = c.nD, T = c.runSteps, S = c.saveInterval;
+  if (ensureBlockStreams(c)) return 1;
+  const int nU = c.nU, nD = c.nD, T = c.runSteps;
+  // a resident trajectory of this run: one segment, no recomputation (and the
+  // slots stay intact for a following adjoint run)
+  const bool resident = c.trajectorySteps == T;
+  const int S = resident ? T : c.saveInterval;
   const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
   const bool deltaControl = c.opts.enable_controller && c.opts.controller_switch && delta_forcing && n_entries > 0 &&
                             c.actuatorPoints > 0;
@@ -3016,7 +3104,8 @@ static int regionRunLinearized(Context& c, const double* delta_forcing, long lon
     held += b.runStageCap;
   }
   const long long fullPer = nU + PrimLayout{nD}.count() + nD * nD + nD;
-  const bool full = (double)(4LL * S * fullPer * pts) * sizeof(double) <= 0.5 * ((double)freeB + held * 8.0);
+  const bool full =
+      resident || (double)(4LL * S * fullPer * pts) * sizeof(double) <= 0.5 * ((double)freeB + held * 8.0);
   for (DevBlock& b : c.blocks) {
     const long long stride = (full ? fullPer : nU) * b.v.N;
     if (growDevice(c, &b.runStage, &b.runStageCap, 4LL * S * stride)) return 1;
@@ -3056,27 +3145,28 @@ static int regionRunLinearized(Context& c, const double* delta_forcing, long lon
     }
   } graphs{&gRec, &gLin};
   long long nodesRec = 0, nodesLin = 0;
-  if (capture(c, &gRec, &nodesRec, [&]() {
+  if (!resident && capture(c, &gRec, &nodesRec, [&]() {
         for (int i = 1; i <= 4; ++i) regionRunStage(c, rs, i, controller, true, false);
         launchStepAdvance(c, 1);
       }))
     return 1;
   if (capture(c, &gLin, &nodesLin, [&]() {
         for (int i = 1; i <= 4; ++i) {
-          for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+          forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
             DevBlock& b = c.blocks[bi];
             if (!full) {
-              launchPrims(c, b, nullptr, true, &rs[bi], i);
-              if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs[bi], i, false);
+              launchPrims(c, b, nullptr, true, &rs[bi], i, s);
+              if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs[bi], i, false, s);
             }
-            if (functional) launchFunctionalTangent(c, b, rl[bi], i, full);
-            if (c.phys.dissipation) launchDissipation(c, b, b.v.lam, 1.0);
-            launchLinearizedFlux(c, b, rl[bi], i, full);
-          }
+            if (functional) launchFunctionalTangent(c, b, rl[bi], i, full, s);
+            if (c.phys.dissipation) launchDissipation(c, b, b.v.lam, 1.0, s);
+            launchLinearizedFlux(c, b, rl[bi], i, full, s);
+          });
           for (size_t bi = 0; bi < c.blocks.size(); ++bi)
             launchInterfaceSatLinearized(c, c.blocks[bi], refs, &rl[bi], i, full);
-          for (size_t bi = 0; bi < c.blocks.size(); ++bi)
-            launchLinearizedDivergence(c, c.blocks[bi], i, rl[bi], 0.0, i, deltaControl && bi == 0);
+          forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
+            launchLinearizedDivergence(c, c.blocks[bi], i, rl[bi], 0.0, i, deltaControl && bi == 0, s);
+          });
         }
         launchStepAdvance(c, 1);
       }))
@@ -3084,16 +3174,19 @@ static int regionRunLinearized(Context& c, const double* delta_forcing, long lon
   const int nSeg = (T + S - 1) / S;
   for (int k = 0; k < nSeg; ++k) {
     const int L = k * S, end = std::min(T, L + S);
-    for (DevBlock& b : c.blocks) {
-      CUDA_TRY(c, cudaMemcpyAsync(b.v.q, b.runSnap + (size_t)k * nU * b.v.N, (size_t)nU * b.v.N * sizeof(double),
-                                  cudaMemcpyDeviceToDevice, c.stream));
-      launchPrims(c, b, b.v.q, false);
+    if (!resident) {
+      for (DevBlock& b : c.blocks) {
+        CUDA_TRY(c, cudaMemcpyAsync(b.v.q, b.runSnap + (size_t)k * nU * b.v.N, (size_t)nU * b.v.N * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, c.stream));
+        launchPrims(c, b, b.v.q, false);
+      }
+      launchSetCounters(c.dCounters, L + 1, L, c.stream);
+      for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(gRec, c.stream));
+      c.launches += 1 + (long long)(end - L) * nodesRec;
     }
     launchSetCounters(c.dCounters, L + 1, L, c.stream);
-    for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(gRec, c.stream));
-    launchSetCounters(c.dCounters, L + 1, L, c.stream);
     for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(gLin, c.stream));
-    c.launches += 2 + (long long)(end - L) * (nodesRec + nodesLin);
+    c.launches += 1 + (long long)(end - L) * nodesLin;
   }
   for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
     DevBlock& b = c.blocks[bi];

@@ -258,6 +258,10 @@ struct Context {
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;          // second stream for concurrent graph branches
   cudaEvent_t evFork[8] = {}, evJoin[8] = {};
+  // one stream per block of a region (created at the first region run), on
+  // which the blocks' stage kernels run concurrently between fork and join
+  cudaStream_t blockStreams[MGD_MAX_BLOCKS] = {};
+  cudaEvent_t evBlockFork = nullptr, evBlockJoin[MGD_MAX_BLOCKS] = {};
   // lanes of the checkpoint recomputation, which runs beside the adjoint
   cudaStream_t stream2 = nullptr, side2 = nullptr;
   cudaEvent_t evRecDone[2] = {}, evAdjDone[2] = {};

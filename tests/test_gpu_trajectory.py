@@ -78,3 +78,41 @@ def test_wall_channel_with_resident_trajectory():
         s.set_adjoint_nonzero_initial_condition(True)
         s.run_adjoint()
     assert np.array_equal(a.get_field(1, capi.FIELD_ADJOINT), b.get_field(1, capi.FIELD_ADJOINT))
+
+
+@pytest.mark.parametrize("rotate", [False, True])
+def test_two_block_resident_trajectory_is_bitwise_the_checkpointed_gradient(rotate):
+    """A region of two blocks meeting at an interface (a transposing one with
+    `rotate`): with trajectory storage the forward run keeps every block's
+    stage slots and the adjoint and tangent runs read them, with no
+    recomputation; J, the sensitivity, the gradient, both blocks' adjoint
+    states and a tangent run in between are those of the checkpointed runs,
+    bit for bit."""
+    P = configs.two_block_2d(functional=True, rotate_second=rotate, n_steps=24, dt=0.05)
+    a, b = Solver(P), Solver(P)
+    b.set_trajectory_storage(True)
+    rng = np.random.default_rng(8)
+    dq0 = [1e-3 * rng.standard_normal((4, blk.n_points)) for blk in P.blocks]
+    results = []
+    for s in (a, b):
+        J = s.run_forward(P.n_steps, 5)
+        lam_before = [s.get_field(bi, capi.FIELD_ADJOINT) for bi in (1, 2)]
+        for bi in (1, 2):
+            s.set_field(bi, capi.FIELD_ADJOINT, dq0[bi - 1])
+        s.run_linearized()
+        tangent = [s.get_field(bi, capi.FIELD_ADJOINT) for bi in (1, 2)]
+        for bi in (1, 2):
+            s.set_field(bi, capi.FIELD_ADJOINT, lam_before[bi - 1])
+        G = s.run_adjoint()
+        results.append((J, G, s.gradient(4 * P.n_steps), [s.get_field(bi, capi.FIELD_ADJOINT) for bi in (1, 2)],
+                        tangent))
+    ra, rb = results
+    assert ra[0] == rb[0] and ra[1] == rb[1]
+    assert np.array_equal(ra[2], rb[2])
+    for k in (3, 4):
+        for x, y in zip(ra[k], rb[k]):
+            assert np.array_equal(x, y)
+    o = oracle_lib.Oracle(P)
+    Jo = o.run_forward(P.n_steps, 5)
+    Go = o.run_adjoint()
+    assert abs(rb[0] - Jo) <= 1e-10 * abs(Jo) and abs(rb[1] - Go) <= 1e-10 * abs(Go)
