@@ -1209,6 +1209,14 @@ static int finalizeBlock(Context& c, int bi, const double* mollifierTotals) {
     }
     b.hostFfPoint = ffPoint;
     b.hostFfSigned = ffSigned;
+    if (b.nInterfaceEntries > 0) {
+      std::vector<int> ifList;
+      for (int k = 0; k < nFF; ++k)
+        if (ffKind[k] == SAT_INTERFACE) ifList.push_back(k);
+      chk(devAlloc(b, &ff.ifList, ifList.size()));
+      if (e != cudaSuccess) return fail(c, "device allocation failed for the interface entries");
+      CUDA_TRY(c, cudaMemcpy(ff.ifList, ifList.data(), ifList.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
     CUDA_TRY(c, cudaMemcpy(ff.kind, ffKind.data(), nFF * sizeof(int), cudaMemcpyHostToDevice));
     CUDA_TRY(c, cudaMemcpy(ff.wallInv, ffWallInv.data(), nFF * sizeof(double), cudaMemcpyHostToDevice));
     CUDA_TRY(c, cudaMemcpy(ff.wallVisc, ffWallVisc.data(), nFF * sizeof(double), cudaMemcpyHostToDevice));
@@ -2242,7 +2250,8 @@ static void regionRunStage(Context& c, std::vector<RunScalars>& rs, int i, bool 
   forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
     launchGradFlux(c, c.blocks[bi], true, false, &rs[bi], i, store, s);
   });
-  for (DevBlock& b : c.blocks) launchInterfaceSat(c, b, refs);
+  // the interface SATs read the partner blocks' fluxes: after the join
+  forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) { launchInterfaceSat(c, c.blocks[bi], refs, s); });
   cudaStreamWaitEvent(c.stream, c.evJoin[0], 0);
   forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
     DevBlock& b = c.blocks[bi];
@@ -2408,8 +2417,9 @@ static int regionRunAdjoint(Context& c, double* sensitivity) {
             launchGradientSensitivity(c, b, rs[bi], i, c.side);
           }
           cudaEventRecord(c.evJoin[1], c.side);
-          for (size_t bi = 0; bi < c.blocks.size(); ++bi)
-            launchInterfaceSatAdjoint(c, c.blocks[bi], refs, &rs[bi], i, full);
+          forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
+            launchInterfaceSatAdjoint(c, c.blocks[bi], refs, &rs[bi], i, full, s);
+          });
           forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
             DevBlock& b = c.blocks[bi];
             launchAdjointCore(c, b, rs[bi], i, full, s);
@@ -3162,8 +3172,9 @@ static int regionRunLinearized(Context& c, const double* delta_forcing, long lon
             if (c.phys.dissipation) launchDissipation(c, b, b.v.lam, 1.0, s);
             launchLinearizedFlux(c, b, rl[bi], i, full, s);
           });
-          for (size_t bi = 0; bi < c.blocks.size(); ++bi)
-            launchInterfaceSatLinearized(c, c.blocks[bi], refs, &rl[bi], i, full);
+          forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
+            launchInterfaceSatLinearized(c, c.blocks[bi], refs, &rl[bi], i, full, s);
+          });
           forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
             launchLinearizedDivergence(c, c.blocks[bi], i, rl[bi], 0.0, i, deltaControl && bi == 0, s);
           });

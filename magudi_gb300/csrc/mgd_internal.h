@@ -48,6 +48,7 @@ struct FarFieldEntries {
   double* ifVis = nullptr;       // 2: viscous penalty of this side and of the partner (signed, / H0)
   double* ifVisc = nullptr;      // nU: sum_j F_v(:, j) m_L,j of this side (component 0 zero)
   double* ifAd = nullptr;        // nD x (nU-1): interface terms of the adjoint viscous diffusion
+  int* ifList = nullptr;         // the block's interface entries, ascending
   double* M = nullptr;       // nU*nU: inviscidPenaltyAmount * jacobian * A+(target), column-major
   double* sigV = nullptr;    // viscousPenaltyAmount * jacobian
   double* sigVRaw = nullptr; // viscousPenaltyAmount

@@ -1622,47 +1622,66 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSatLinearized(BlockView B, P
   }
 }
 
+// Lanes of kInterfaceSatAdjoint: one per (interface entry, left-state
+// component l, side). A warp-wide FP64 instruction occupies its SM
+// sub-partition's FP64 pipe for the same time whatever the number of active
+// lanes, so the per-entry work is spread over 2 nU lanes (and, with one warp
+// per CTA, over many sub-partitions) instead of running as 2 nU passes in one
+// lane.
+template <int ND>
+struct InterfaceLanes {
+  static constexpr int perEntry = 2 * (ND + 2);          // (l, side) pairs
+  static constexpr int entriesPerWarp = 32 / perEntry;  // 4 in 2D, 3 in 3D
+};
+
 template <int ND, bool VISC>
-__global__ void __launch_bounds__(kBlock) kInterfaceSatAdjoint(BlockView B, Physics P, BlockRefs R, RunScalars rs,
-                                                                int stage, int fromSlot) {
+__global__ void __launch_bounds__(32) kInterfaceSatAdjoint(BlockView B, Physics P, BlockRefs R, RunScalars rs,
+                                                            int stage, int fromSlot, int nEntries) {
   pdlEnter();
-  const int e = blockIdx.x * kBlock + threadIdx.x;
-  if (e >= B.ff.n || B.ff.kind[e] != SAT_INTERFACE) return;
   constexpr int nU = ND + 2, nV = ND + 1;
+  constexpr int G = InterfaceLanes<ND>::perEntry, EW = InterfaceLanes<ND>::entriesPerWarp;
   using D = DualN<1>;
-  const long long N = B.N, p = B.ff.point[e];
-  const int pb = B.ff.partnerBlock[e];
-  const long long pp = B.ff.partnerPoint[e], NR = R.N[pb];
+  __shared__ double part[32][nU];
+  const int lane = threadIdx.x, g = lane / G, k = lane - g * G;
+  const int l = k >> 1, side = k & 1;
+  const int idx = blockIdx.x * EW + g;
+  const bool active = g < EW && idx < nEntries;
+  const int e = active ? B.ff.ifList[idx] : 0;
+  const long long N = B.N;
   const PrimLayout L{ND};
-  // forward state of both sides: the blocks' arrays, or their stage slots in a run
   const FwdState fs = forwardState<ND>(B, rs, stage, fromSlot != 0);
-  const double* qRb = R.q[pb];
-  if (fromSlot) {
-    const int slot = ((*rs.step) - (*rs.segBase) - 1) * 4 + stage - 1;
-    qRb = R.stage[pb] + (long long)slot * R.slotStride[pb];
-  }
-  double qL[nU], qR[nU], dq[nU], lamL[nU], lamR[nU], mL[ND], mR[ND];
-  for (int c = 0; c < nU; ++c) {
-    qL[c] = fs.q[p + N * c];
-    qR[c] = qRb[pp + NR * c];
-    dq[c] = qL[c] - qR[c];
-    lamL[c] = B.lam[p + N * c];
-    lamR[c] = R.lam[pb][pp + NR * c];
-  }
-  for (int d = 0; d < ND; ++d) {
-    mL[d] = B.metrics[p + N * (ND * (B.ff.normalDir[e] - 1) + d)];
-    mR[d] = B.ff.metricsR[(long long)e * ND + d];
-  }
-  const double jac = B.jac[p];
-  const double sL = B.ff.ifInv[2 * e] * jac, sR = -B.ff.ifInv[2 * e + 1] * jac;
-  double sat[nU];
-  for (int c = 0; c < nU; ++c) sat[c] = 0.0;
-  // One forward-mode pass per left-state component l: the Roe average and both
-  // sides' incoming Jacobians on single-derivative dual numbers seeded with
-  // d/dq_L[l] give sum_ij lambda_i (dA_ij/dq_l) dq_j; the first pass also
-  // gives A^T lambda. (One derivative per pass keeps the duals in registers.)
-#pragma unroll 1
-  for (int l = 0; l < nU; ++l) {
+  double qL[nU], qR[nU], dq[nU], lamL[nU], lamR[nU], mL[ND], mR[ND], jac = 0.0, sL = 0.0, sR = 0.0;
+  long long p = 0;
+  double contrib[nU];
+  for (int c = 0; c < nU; ++c) contrib[c] = 0.0;
+  if (active) {
+    p = B.ff.point[e];
+    const int pb = B.ff.partnerBlock[e];
+    const long long pp = B.ff.partnerPoint[e], NR = R.N[pb];
+    // forward state of both sides: the blocks' arrays, or their stage slots in a run
+    const double* qRb = R.q[pb];
+    if (fromSlot) {
+      const int slot = ((*rs.step) - (*rs.segBase) - 1) * 4 + stage - 1;
+      qRb = R.stage[pb] + (long long)slot * R.slotStride[pb];
+    }
+    for (int c = 0; c < nU; ++c) {
+      qL[c] = fs.q[p + N * c];
+      qR[c] = qRb[pp + NR * c];
+      dq[c] = qL[c] - qR[c];
+      lamL[c] = B.lam[p + N * c];
+      lamR[c] = R.lam[pb][pp + NR * c];
+    }
+    for (int d = 0; d < ND; ++d) {
+      mL[d] = B.metrics[p + N * (ND * (B.ff.normalDir[e] - 1) + d)];
+      mR[d] = B.ff.metricsR[(long long)e * ND + d];
+    }
+    jac = B.jac[p];
+    sL = B.ff.ifInv[2 * e] * jac;
+    sR = -B.ff.ifInv[2 * e + 1] * jac;
+    // This lane's share: the Roe average and one side's incoming Jacobian on
+    // single-derivative dual numbers seeded with d/dq_L[l] give
+    // sum_ij lambda_i (dA_ij/dq_l) dq_j into component l; the l = 0 lanes
+    // also give that side's A^T lambda into every component.
     D dL[nU], dR[nU], roe[nU];
     for (int c = 0; c < nU; ++c) {
       dL[c] = D(qL[c]);
@@ -1670,26 +1689,33 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSatAdjoint(BlockView B, Phys
       dR[c] = D(qR[c]);
     }
     roeAverage<ND, D>(dL, dR, P.g, roe);
-#pragma unroll 1
-    for (int side = 0; side < 2; ++side) {
-      D A[nU * nU];
-      incomingJacobian<ND, D>(roe, side == 0 ? mL : mR, P.g, side == 0 ? B.ff.dirL[e] : B.ff.dirR[e], A);
-      const double* lam = side == 0 ? lamL : lamR;
-      const double sInv = side == 0 ? sL : sR;
-      if (l == 0)
-        for (int r = 0; r < nU; ++r) {
-          double t = A[nU * r].v * lam[0];
-          for (int c = 1; c < nU; ++c) t += A[c + nU * r].v * lam[c];
-          sat[r] += sInv * t;
-        }
-      double t = 0.0;
-      for (int i = 0; i < nU; ++i) {
-        double w = 0.0;
-        for (int j = 0; j < nU; ++j) w += A[i + nU * j].d[0] * dq[j];
-        t += w * lam[i];
+    D A[nU * nU];
+    incomingJacobian<ND, D>(roe, side == 0 ? mL : mR, P.g, side == 0 ? B.ff.dirL[e] : B.ff.dirR[e], A);
+    const double* lam = side == 0 ? lamL : lamR;
+    const double sInv = side == 0 ? sL : sR;
+    if (l == 0)
+      for (int r = 0; r < nU; ++r) {
+        double t = A[nU * r].v * lam[0];
+        for (int c = 1; c < nU; ++c) t += A[c + nU * r].v * lam[c];
+        contrib[r] = sInv * t;
       }
-      sat[l] += sInv * t;
+    double t = 0.0;
+    for (int i = 0; i < nU; ++i) {
+      double w = 0.0;
+      for (int j = 0; j < nU; ++j) w += A[i + nU * j].d[0] * dq[j];
+      t += w * lam[i];
     }
+    contrib[l] += sInv * t;
+  }
+  for (int c = 0; c < nU; ++c) part[lane][c] = contrib[c];
+  __syncwarp();
+  if (!active || k != 0) return;
+  // the entry's lanes' shares summed in lane order, then the viscous terms
+  double sat[nU];
+  for (int c = 0; c < nU; ++c) {
+    double t = part[lane][c];
+    for (int j = 1; j < G; ++j) t += part[lane + j][c];
+    sat[c] = t;
   }
   double u[ND];
   for (int d = 0; d < ND; ++d) u[d] = fs.prim[p + N * L.u(d)];
@@ -1698,12 +1724,12 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSatAdjoint(BlockView B, Phys
     const double v = fs.prim[p + N * L.v()], T = fs.prim[p + N * L.T()];
     for (int c = 0; c < ND * ND; ++c) tau[c] = fs.tau[p + N * c];
     for (int d = 0; d < ND; ++d) hf[d] = fs.hf[p + N * d];
-    for (int side = 0; side < 2; ++side) {
+    for (int sd = 0; sd < 2; ++sd) {
       double y[nU];
       for (int c = 0; c < nU; ++c) y[c] = 0.0;
-      firstPartialViscousTransposeProduct<ND>(side == 0 ? mL : mR, u, T, v, P.g, P.powerLawExponent, tau, hf,
-                                              side == 0 ? lamL : lamR, y);
-      const double sVis = side == 0 ? -B.ff.ifVis[2 * e] : B.ff.ifVis[2 * e + 1];
+      firstPartialViscousTransposeProduct<ND>(sd == 0 ? mL : mR, u, T, v, P.g, P.powerLawExponent, tau, hf,
+                                              sd == 0 ? lamL : lamR, y);
+      const double sVis = sd == 0 ? -B.ff.ifVis[2 * e] : B.ff.ifVis[2 * e + 1];
       for (int c = 0; c < nU; ++c) sat[c] += sVis * jac * y[c];
     }
   }
@@ -1711,14 +1737,14 @@ __global__ void __launch_bounds__(kBlock) kInterfaceSatAdjoint(BlockView B, Phys
   if (VISC) {
     const double mu = fs.prim[p + N * L.mu()], la = fs.prim[p + N * L.la()], kd = fs.prim[p + N * L.k()];
     double* a = B.ff.ifAd + (long long)e * ND * nV;
-    for (int l = 0; l < ND; ++l) {
+    for (int dl = 0; dl < ND; ++dl) {
       double ml[ND];
-      for (int d = 0; d < ND; ++d) ml[d] = B.metrics[p + N * (ND * l + d)];
+      for (int d = 0; d < ND; ++d) ml[d] = B.metrics[p + N * (ND * dl + d)];
       double tL[nV], tR[nV];
       for (int c = 0; c < nV; ++c) tL[c] = tR[c] = 0.0;
       secondPartialViscousTransposeProduct<ND>(u, mu, la, kd, jac, mL, ml, &lamL[1], tL);
       secondPartialViscousTransposeProduct<ND>(u, mu, la, kd, jac, mR, ml, &lamR[1], tR);
-      for (int c = 0; c < nV; ++c) a[l * nV + c] = B.ff.ifVis[2 * e] * tL[c] - B.ff.ifVis[2 * e + 1] * tR[c];
+      for (int c = 0; c < nV; ++c) a[dl * nV + c] = B.ff.ifVis[2 * e] * tL[c] - B.ff.ifVis[2 * e + 1] * tR[c];
     }
   }
 }
@@ -2591,17 +2617,18 @@ void launchInterfaceSat(Context& c, DevBlock& b, const BlockRefs& r, cudaStream_
 void launchInterfaceSatAdjoint(Context& c, DevBlock& b, const BlockRefs& r, const RunScalars* rs, int stage,
                                bool fromSlot, cudaStream_t s) {
   if (b.nInterfaceEntries == 0) return;
-  const int G = gridFor(b.v.ff.n);
   RunScalars x{};
   if (rs) x = *rs;
-  const int fs = fromSlot ? 1 : 0;
+  const int fs = fromSlot ? 1 : 0, n = b.nInterfaceEntries;
   MGD_LAUNCH(c);
   if (c.nD == 2) {
-    if (c.phys.viscous) pdl(kInterfaceSatAdjoint<2, true>, G, kBlock, on(c, s), b.v, c.phys, r, x, stage, fs);
-    else pdl(kInterfaceSatAdjoint<2, false>, G, kBlock, on(c, s), b.v, c.phys, r, x, stage, fs);
+    const int G = (n + InterfaceLanes<2>::entriesPerWarp - 1) / InterfaceLanes<2>::entriesPerWarp;
+    if (c.phys.viscous) pdl(kInterfaceSatAdjoint<2, true>, G, 32, on(c, s), b.v, c.phys, r, x, stage, fs, n);
+    else pdl(kInterfaceSatAdjoint<2, false>, G, 32, on(c, s), b.v, c.phys, r, x, stage, fs, n);
   } else {
-    if (c.phys.viscous) pdl(kInterfaceSatAdjoint<3, true>, G, kBlock, on(c, s), b.v, c.phys, r, x, stage, fs);
-    else pdl(kInterfaceSatAdjoint<3, false>, G, kBlock, on(c, s), b.v, c.phys, r, x, stage, fs);
+    const int G = (n + InterfaceLanes<3>::entriesPerWarp - 1) / InterfaceLanes<3>::entriesPerWarp;
+    if (c.phys.viscous) pdl(kInterfaceSatAdjoint<3, true>, G, 32, on(c, s), b.v, c.phys, r, x, stage, fs, n);
+    else pdl(kInterfaceSatAdjoint<3, false>, G, 32, on(c, s), b.v, c.phys, r, x, stage, fs, n);
   }
 }
 
