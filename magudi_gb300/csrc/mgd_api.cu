@@ -201,8 +201,11 @@ int mgd_destroy(mgd_ctx* h) {
   for (int k = 0; k < MGD_MAX_BLOCKS; ++k) {
     if (c.blockStreams[k]) cudaStreamDestroy(c.blockStreams[k]);
     if (c.evBlockJoin[k]) cudaEventDestroy(c.evBlockJoin[k]);
+    if (c.blockStreams2[k]) cudaStreamDestroy(c.blockStreams2[k]);
+    if (c.evBlockJoin2[k]) cudaEventDestroy(c.evBlockJoin2[k]);
   }
   if (c.evBlockFork) cudaEventDestroy(c.evBlockFork);
+  if (c.evBlockFork2) cudaEventDestroy(c.evBlockFork2);
   for (int k = 0; k < 8; ++k) {
     cudaEventDestroy(c.evFork[k]);
     cudaEventDestroy(c.evJoin[k]);
@@ -2200,65 +2203,100 @@ static int reduceRegion(Context& c, int nSlots, std::vector<double>& out) {
 }
 
 // One forward RK stage of every block; store writes the stage slots.
-// Streams of the blocks of a region, created once per context (outside any
-// capture).
+// Streams of the blocks of a region, two sets (the adjoint lane and the
+// recomputation lane of a checkpointed adjoint run), created once per context
+// (outside any capture).
 static int ensureBlockStreams(Context& c) {
   if (c.evBlockFork) return 0;
   for (size_t bi = 0; bi < c.blocks.size() && bi < MGD_MAX_BLOCKS; ++bi) {
     CUDA_TRY(c, cudaStreamCreateWithFlags(&c.blockStreams[bi], cudaStreamNonBlocking));
     CUDA_TRY(c, cudaEventCreateWithFlags(&c.evBlockJoin[bi], cudaEventDisableTiming));
+    CUDA_TRY(c, cudaStreamCreateWithFlags(&c.blockStreams2[bi], cudaStreamNonBlocking));
+    CUDA_TRY(c, cudaEventCreateWithFlags(&c.evBlockJoin2[bi], cudaEventDisableTiming));
   }
+  CUDA_TRY(c, cudaEventCreateWithFlags(&c.evBlockFork2, cudaEventDisableTiming));
   CUDA_TRY(c, cudaEventCreateWithFlags(&c.evBlockFork, cudaEventDisableTiming));
   return 0;
 }
 
-// The same work for every block of a region, each block on its own stream,
-// forked from the context's stream and joined back into it (inside a capture
-// the block streams become parallel branches of the graph). A block's stage
-// kernels read and write only that block's arrays, so they may overlap; the
-// interface kernels, which read the partner blocks, run between a join and
-// the next fork.
-template <class F>
-static void forEachBlockConcurrently(Context& c, F f) {
-  const int n = (int)c.blocks.size();
-  if (n == 1 || !c.evBlockFork) {
-    for (int bi = 0; bi < n; ++bi) f(bi, c.stream);
-    return;
-  }
-  cudaEventRecord(c.evBlockFork, c.stream);
-  for (int bi = 0; bi < n; ++bi) {
-    cudaStreamWaitEvent(c.blockStreams[bi], c.evBlockFork, 0);
-    f(bi, c.blockStreams[bi]);
-    cudaEventRecord(c.evBlockJoin[bi], c.blockStreams[bi]);
-  }
-  for (int bi = 0; bi < n; ++bi) cudaStreamWaitEvent(c.stream, c.evBlockJoin[bi], 0);
+// The streams and events one lane of a region run issues on: its main
+// stream, a side stream for the dissipation and excitation branch, and one
+// stream per block.
+struct RegionLanes {
+  cudaStream_t main, side;
+  cudaEvent_t fork, join;
+  cudaStream_t* blockStreams;
+  cudaEvent_t blockFork;
+  cudaEvent_t* blockJoin;
+};
+
+static RegionLanes mainRegionLanes(Context& c) {
+  return {c.stream, c.side, c.evFork[0], c.evJoin[0], c.blockStreams, c.evBlockFork, c.evBlockJoin};
 }
 
-static void regionRunStage(Context& c, std::vector<RunScalars>& rs, int i, bool controller, bool store,
-                           bool functional) {
-  const BlockRefs refs = blockRefs(c);
+// The same work for every block of a region, each block on its own stream,
+// forked from the lane's main stream and joined back into it (inside a
+// capture the block streams become parallel branches of the graph). A
+// block's stage kernels read and write only that block's arrays, so they may
+// overlap; the interface kernels, which read the partner blocks, run between
+// a join and the next fork.
+template <class F>
+static void forEachBlockConcurrently(Context& c, const RegionLanes& L, F f) {
+  const int n = (int)c.blocks.size();
+  if (n == 1 || !L.blockFork) {
+    for (int bi = 0; bi < n; ++bi) f(bi, L.main);
+    return;
+  }
+  cudaEventRecord(L.blockFork, L.main);
+  for (int bi = 0; bi < n; ++bi) {
+    cudaStreamWaitEvent(L.blockStreams[bi], L.blockFork, 0);
+    f(bi, L.blockStreams[bi]);
+    cudaEventRecord(L.blockJoin[bi], L.blockStreams[bi]);
+  }
+  for (int bi = 0; bi < n; ++bi) cudaStreamWaitEvent(L.main, L.blockJoin[bi], 0);
+}
+
+template <class F>
+static void forEachBlockConcurrently(Context& c, F f) {
+  forEachBlockConcurrently(c, mainRegionLanes(c), f);
+}
+
+// One forward RK stage of every block of a region on lane L: the blocks'
+// views in `blocks` (the context's blocks, or the recomputation lane's
+// shadows), their run scalars, and the references the interface SATs read
+// the partner blocks through.
+static void regionRunStage(Context& c, std::vector<DevBlock*>& blocks, std::vector<RunScalars>& rs, int i,
+                           bool controller, bool store, bool functional, const RegionLanes& L,
+                           const BlockRefs& refs) {
   // dissipation and excitation of every block on the side stream beside the
   // flux and interface kernels; both only read the state of the stage
-  cudaEventRecord(c.evFork[0], c.stream);
-  cudaStreamWaitEvent(c.side, c.evFork[0], 0);
-  for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
-    DevBlock& b = c.blocks[bi];
-    if (c.phys.dissipation) launchDissipation(c, b, b.v.q, 1.0, c.side);
-    launchExcitation(c, b, rs[bi], i, false, false, c.side);
+  cudaEventRecord(L.fork, L.main);
+  cudaStreamWaitEvent(L.side, L.fork, 0);
+  for (size_t bi = 0; bi < blocks.size(); ++bi) {
+    DevBlock& b = *blocks[bi];
+    if (c.phys.dissipation) launchDissipation(c, b, b.v.q, 1.0, L.side);
+    launchExcitation(c, b, rs[bi], i, false, false, L.side);
   }
-  cudaEventRecord(c.evJoin[0], c.side);
-  forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
-    launchGradFlux(c, c.blocks[bi], true, false, &rs[bi], i, store, s);
+  cudaEventRecord(L.join, L.side);
+  forEachBlockConcurrently(c, L, [&](int bi, cudaStream_t s) {
+    launchGradFlux(c, *blocks[bi], true, false, &rs[bi], i, store, s);
   });
   // the interface SATs read the partner blocks' fluxes: after the join
-  forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) { launchInterfaceSat(c, c.blocks[bi], refs, s); });
-  cudaStreamWaitEvent(c.stream, c.evJoin[0], 0);
-  forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
-    DevBlock& b = c.blocks[bi];
+  forEachBlockConcurrently(c, L, [&](int bi, cudaStream_t s) { launchInterfaceSat(c, *blocks[bi], refs, s); });
+  cudaStreamWaitEvent(L.main, L.join, 0);
+  forEachBlockConcurrently(c, L, [&](int bi, cudaStream_t s) {
+    DevBlock& b = *blocks[bi];
     launchForwardDivergence(c, b, i, rs[bi], false, controller && bi == 0, s);
     launchPrims(c, b, b.v.q, false, nullptr, 0, s);
     if (functional) launchFunctional(c, b, rs[bi], i, s);
   });
+}
+
+static void regionRunStage(Context& c, std::vector<RunScalars>& rs, int i, bool controller, bool store,
+                           bool functional) {
+  std::vector<DevBlock*> blocks;
+  for (DevBlock& b : c.blocks) blocks.push_back(&b);
+  regionRunStage(c, blocks, rs, i, controller, store, functional, mainRegionLanes(c), blockRefs(c));
 }
 
 static int regionRunForward(Context& c, int n_steps, int save_interval, double t0, double* cost) {
@@ -2352,6 +2390,53 @@ static int regionRunForward(Context& c, int n_steps, int save_interval, double t
   return 0;
 }
 
+// The recomputation lane's forward work arrays of every block of a region
+// (its own state, primitives, fluxes, dissipation, RK buffers, SAT vectors,
+// interface fluxes and excitation values over the blocks' grid and patch
+// data), allocated once.
+static int ensureRegionShadow(Context& c) {
+  if (c.regionShadow.size() == c.blocks.size()) return 0;
+  c.regionShadow.clear();
+  const int nD = c.nD, nU = c.nU;
+  cudaError_t e = cudaSuccess;
+  auto alloc = [&](double** p, long long n) {
+    const cudaError_t x = cudaMalloc((void**)p, (size_t)std::max(1LL, n) * sizeof(double));
+    if (x == cudaSuccess) c.shadowAllocations.push_back(*p);
+    else e = x;
+  };
+  for (DevBlock& b : c.blocks) {
+    const long long N = b.v.N;
+    BlockView v = b.v;
+    long long nExc = 0;
+    for (const ExcPatch& X : b.exc) nExc = std::max(nExc, (long long)X.off + X.nE);
+    double *ffv = nullptr, *ifv = nullptr;
+    alloc(&v.q, N * nU);
+    alloc(&v.prim, N * PrimLayout{nD}.count());
+    alloc(&v.fhat, N * nD * nU);
+    alloc(&v.dq, N * nD * nU);
+    alloc(&v.b1, N * nU);
+    alloc(&v.b2, N * nU);
+    alloc(&ffv, (long long)v.ff.n * nU);
+    if (v.ff.ifVisc) alloc(&ifv, (long long)v.ff.n * nU);
+    if (v.excF) alloc(&v.excF, 3 * nExc);
+    if (e != cudaSuccess) {
+      c.regionShadow.clear();
+      return fail(c, std::string("device allocation failed for the recomputation: ") + cudaGetErrorString(e));
+    }
+    v.ff.visc = ffv;
+    if (v.ff.ifVisc) v.ff.ifVisc = ifv;
+    c.regionShadow.push_back(v);
+  }
+  return 0;
+}
+
+// Solver%runAdjoint over a multi-block region (UniformCheckpointer). With a
+// resident trajectory one segment reads every stage from its slots. Else,
+// when two halves of full stage slots and the recomputation lane's work
+// arrays fit, segment k-1 is recomputed on the second lanes (own streams, own
+// work arrays, own step counters, the other half of the slots, lowest launch
+// priority) while the adjoint consumes segment k; otherwise the segments are
+// recomputed in line.
 static int regionRunAdjoint(Context& c, double* sensitivity) {
   if (ensureBlockStreams(c)) return 1;
   const int nU = c.nU, nD = c.nD, T = c.runSteps;
@@ -2360,95 +2445,190 @@ static int regionRunAdjoint(Context& c, double* sensitivity) {
   const bool resident = c.trajectorySteps == T;
   const int S = resident ? T : c.saveInterval;
   const double dtT = c.stepDt[T - 1];
-  // stage slots: full (state, primitives, stress, heat flux) when they fit in half the free memory
+  // stage slots: full (state, primitives, stress, heat flux) when they fit in
+  // half the free memory, in two halves with the second lane when those fit
   size_t freeB = 0, totalB = 0;
   CUDA_TRY(c, cudaMemGetInfo(&freeB, &totalB));
-  long long pts = 0, held = 0;
+  long long pts = 0, held = 0, ffEntries = 0;
   for (DevBlock& b : c.blocks) {
     pts += b.v.N;
     held += b.runStageCap;
+    ffEntries += b.v.ff.n;
   }
   const long long fullPer = nU + PrimLayout{nD}.count() + nD * nD + nD;
-  const bool full =
-      resident || (double)(4LL * S * fullPer * pts) * sizeof(double) <= 0.5 * ((double)freeB + held * 8.0);
-  for (DevBlock& b : c.blocks) {
-    const long long stride = (full ? fullPer : nU) * b.v.N;
-    if (growDevice(c, &b.runStage, &b.runStageCap, 4LL * S * stride)) return 1;
+  const double budget = 0.5 * ((double)freeB + held * 8.0);
+  const double shadowBytes = c.regionShadow.size() == c.blocks.size()
+                                 ? 0.0
+                                 : 8.0 * ((double)pts * (4 * nU + PrimLayout{nD}.count() + 2 * nD * nU) +
+                                          2.0 * ffEntries * nU);
+  const bool twoLanes =
+      !resident && (double)(2 * 4LL * S * fullPer * pts) * sizeof(double) + shadowBytes <= budget;
+  const bool full = resident || twoLanes || (double)(4LL * S * fullPer * pts) * sizeof(double) <= budget;
+  const int halves = twoLanes ? 2 : 1;
+  std::vector<long long> halfSize(c.blocks.size());
+  for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+    DevBlock& b = c.blocks[bi];
+    halfSize[bi] = 4LL * S * (full ? fullPer : nU) * b.v.N;
+    if (growDevice(c, &b.runStage, &b.runStageCap, halves * halfSize[bi])) return 1;
   }
+  if (twoLanes && ensureRegionShadow(c)) return 1;
   // the slot stride differs per block: the run scalars and the references carry each block's
   c.slotFull = full ? 1 : 0;
   const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
-  std::vector<RunScalars> rs;
-  for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
-    RunScalars r = blockRunScalars(c, c.blocks[bi], bi == 0);
-    r.slotFull = c.slotFull;
-    r.slotStride = (full ? fullPer : nU) * c.blocks[bi].v.N;
-    rs.push_back(r);
+  int* recCounters = twoLanes ? c.dCounters + 4 : c.dCounters;
+  // run scalars and references of the adjoint lane (ra) and of the
+  // recomputation (rr) for each half of the slots
+  std::vector<RunScalars> ra[2], rr[2];
+  BlockRefs aRefs[2];
+  for (int h = 0; h < halves; ++h) {
+    aRefs[h] = runRefs(c);
+    for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+      DevBlock& b = c.blocks[bi];
+      RunScalars r = blockRunScalars(c, b, bi == 0);
+      r.slotFull = c.slotFull;
+      r.slotStride = (full ? fullPer : nU) * b.v.N;
+      r.stageBuf = b.runStage + h * halfSize[bi];
+      ra[h].push_back(r);
+      r.step = recCounters;
+      r.segBase = recCounters + 1;
+      rr[h].push_back(r);
+      aRefs[h].stage[bi] = r.stageBuf;
+      aRefs[h].slotStride[bi] = r.slotStride;
+    }
   }
-  BlockRefs refs = runRefs(c);
-  for (size_t bi = 0; bi < c.blocks.size(); ++bi) refs.slotStride[bi] = rs[bi].slotStride;
+  // the blocks the recomputation runs on, and the references its interface
+  // SATs read the partners through
+  std::vector<DevBlock> shadowBlocks;
+  std::vector<DevBlock*> recBlocks;
+  BlockRefs recRefs = blockRefs(c);
+  if (twoLanes) {
+    shadowBlocks = c.blocks;
+    for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+      shadowBlocks[bi].v = c.regionShadow[bi];
+      recRefs.q[bi] = c.regionShadow[bi].q;
+      recRefs.ifVisc[bi] = c.regionShadow[bi].ff.ifVisc;
+    }
+    for (DevBlock& b : shadowBlocks) recBlocks.push_back(&b);
+  } else {
+    for (DevBlock& b : c.blocks) recBlocks.push_back(&b);
+  }
+  const RegionLanes recLanes =
+      twoLanes ? RegionLanes{c.stream2, c.side2, c.evFork[2], c.evJoin[2], c.blockStreams2, c.evBlockFork2,
+                             c.evBlockJoin2}
+               : mainRegionLanes(c);
   for (DevBlock& b : c.blocks) {
     launchPrims(c, b, b.v.q, false);
     launchAdjointInitial(c, b, c.opts.adjoint_forcing_switch ? -dtT / 6.0 : 0.0);
   }
-  if (!resident && capture(c, &c.gRecomputeH[0], &c.nodesRecompute, [&]() {
-        for (int i = 1; i <= 4; ++i) regionRunStage(c, rs, i, controller, true, false);
-        launchStepAdvance(c, 1);
-      }))
-    return 1;
-  if (capture(c, &c.gAdjointH[0], &c.nodesAdjoint, [&]() {
-        for (int i = 4; i >= 1; --i) {
-          if (!full)
+  setProgrammaticLaunch(!twoLanes);
+  struct Restore {
+    ~Restore() {
+      setProgrammaticLaunch(true);
+      setLaunchPriority(false, 0);
+    }
+  } restore;
+  // the adjoint is the critical path: the recomputation's kernels launch at
+  // the lowest priority and take the SM time the adjoint leaves
+  int prioLeast = 0, prioGreatest = 0;
+  cudaDeviceGetStreamPriorityRange(&prioLeast, &prioGreatest);
+  long long nodesRec = 0, nodesAdj = 0;
+  for (int h = 0; h < halves; ++h) {
+    if (twoLanes) setLaunchPriority(true, prioLeast);
+    if (!resident && capture(c, &c.gRecomputeH[h], &nodesRec, [&]() {
+          for (int i = 1; i <= 4; ++i)
+            regionRunStage(c, recBlocks, rr[h], i, controller, true, false, recLanes, recRefs);
+          launchStepAdvanceOn(recCounters, 1, recLanes.main);
+        }, recLanes.main))
+      return 1;
+    if (twoLanes) setLaunchPriority(true, prioGreatest);
+    std::vector<RunScalars>& rs = ra[h];
+    const BlockRefs& refs = aRefs[h];
+    if (capture(c, &c.gAdjointH[h], &nodesAdj, [&]() {
+          for (int i = 4; i >= 1; --i) {
+            if (!full)
+              forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
+                DevBlock& b = c.blocks[bi];
+                launchPrims(c, b, nullptr, true, &rs[bi], i, s);
+                if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs[bi], i, false, s);
+              });
+            // dissipation, excitation and gradient/sensitivity of every block on
+            // the side stream (they read lambda and the forward state of the
+            // stage); interface SATs, then the cores and diffusion, then the
+            // assembly, each block on its own stream
+            cudaEventRecord(c.evFork[1], c.stream);
+            cudaStreamWaitEvent(c.side, c.evFork[1], 0);
+            for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+              DevBlock& b = c.blocks[bi];
+              if (c.phys.dissipation) launchDissipation(c, b, b.v.lam, -1.0, c.side);
+              launchExcitation(c, b, rs[bi], i, true, full, c.side);
+              launchGradientSensitivity(c, b, rs[bi], i, c.side);
+            }
+            cudaEventRecord(c.evJoin[1], c.side);
+            forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
+              launchInterfaceSatAdjoint(c, c.blocks[bi], refs, &rs[bi], i, full, s);
+            });
             forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
               DevBlock& b = c.blocks[bi];
-              launchPrims(c, b, nullptr, true, &rs[bi], i, s);
-              if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs[bi], i, false, s);
+              launchAdjointCore(c, b, rs[bi], i, full, s);
+              launchAdjointDiffusion(c, b, s);
             });
-          // dissipation, excitation and gradient/sensitivity of every block on
-          // the side stream (they read lambda and the forward state of the
-          // stage); interface SATs on the main stream, then the cores and
-          // diffusion of the blocks on their own streams
-          cudaEventRecord(c.evFork[1], c.stream);
-          cudaStreamWaitEvent(c.side, c.evFork[1], 0);
-          for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
-            DevBlock& b = c.blocks[bi];
-            if (c.phys.dissipation) launchDissipation(c, b, b.v.lam, -1.0, c.side);
-            launchExcitation(c, b, rs[bi], i, true, full, c.side);
-            launchGradientSensitivity(c, b, rs[bi], i, c.side);
+            cudaStreamWaitEvent(c.stream, c.evJoin[1], 0);
+            forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
+              launchAdjointAssemble(c, c.blocks[bi], i, rs[bi], i, 0.0, false, full, s);
+            });
           }
-          cudaEventRecord(c.evJoin[1], c.side);
-          forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
-            launchInterfaceSatAdjoint(c, c.blocks[bi], refs, &rs[bi], i, full, s);
-          });
-          forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
-            DevBlock& b = c.blocks[bi];
-            launchAdjointCore(c, b, rs[bi], i, full, s);
-            launchAdjointDiffusion(c, b, s);
-          });
-          cudaStreamWaitEvent(c.stream, c.evJoin[1], 0);
-          forEachBlockConcurrently(c, [&](int bi, cudaStream_t s) {
-            launchAdjointAssemble(c, c.blocks[bi], i, rs[bi], i, 0.0, false, full, s);
-          });
-        }
-        launchStepAdvance(c, -1);
-      }))
-    return 1;
+          launchStepAdvance(c, -1);
+        }))
+      return 1;
+  }
+  c.nodesRecompute = nodesRec;
+  c.nodesAdjoint = nodesAdj;
   const int nSeg = (T + S - 1) / S;
+  // UniformCheckpointer: reload the snapshots of segment k and recompute its stages
+  auto recompute = [&](int k) -> int {
+    const int L = k * S, end = std::min(T, L + S);
+    const int h = k % halves;
+    if (twoLanes) setLaunchPriority(true, prioLeast);
+    for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
+      DevBlock& b = *recBlocks[bi];
+      CUDA_TRY(c, cudaMemcpyAsync(b.v.q, c.blocks[bi].runSnap + (size_t)k * nU * b.v.N,
+                                  (size_t)nU * b.v.N * sizeof(double), cudaMemcpyDeviceToDevice, recLanes.main));
+      launchPrims(c, b, b.v.q, false, nullptr, 0, recLanes.main);
+    }
+    launchSetCounters(recCounters, L + 1, L, recLanes.main);
+    if (twoLanes) setLaunchPriority(true, prioGreatest);
+    for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gRecomputeH[h], recLanes.main));
+    c.launches += (long long)(end - L) * nodesRec;
+    if (twoLanes) CUDA_TRY(c, cudaEventRecord(c.evRecDone[h], recLanes.main));
+    return 0;
+  };
+  if (twoLanes) {
+    // the second lanes start after everything issued so far on the main stream
+    CUDA_TRY(c, cudaEventRecord(c.evFork[3], c.stream));
+    CUDA_TRY(c, cudaStreamWaitEvent(c.stream2, c.evFork[3], 0));
+  }
+  if (!resident && recompute(nSeg - 1)) return 1;
   for (int k = nSeg - 1; k >= 0; --k) {
     const int L = k * S, end = std::min(T, L + S);
-    if (!resident) {
-      for (DevBlock& b : c.blocks) {
-        CUDA_TRY(c, cudaMemcpyAsync(b.v.q, b.runSnap + (size_t)k * nU * b.v.N, (size_t)nU * b.v.N * sizeof(double),
-                                    cudaMemcpyDeviceToDevice, c.stream));
-        launchPrims(c, b, b.v.q, false);
+    const int h = k % halves;
+    if (twoLanes) {
+      CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.evRecDone[h], 0));
+      if (k >= 1) {
+        // segment k-1 reuses the half that the adjoint of segment k+1 read
+        if (k + 1 <= nSeg - 1) CUDA_TRY(c, cudaStreamWaitEvent(c.stream2, c.evAdjDone[(k + 1) % 2], 0));
+        if (recompute(k - 1)) return 1;
       }
-      launchSetCounters(c.dCounters, L + 1, L, c.stream);
-      for (int s = L + 1; s <= end; ++s) CUDA_TRY(c, cudaGraphLaunch(c.gRecomputeH[0], c.stream));
-      c.launches += (long long)(end - L) * c.nodesRecompute;
     }
     launchSetCounters(c.dCounters, end, L, c.stream);
-    for (int s = end; s >= L + 1; --s) CUDA_TRY(c, cudaGraphLaunch(c.gAdjointH[0], c.stream));
-    c.launches += (long long)(end - L) * c.nodesAdjoint;
+    for (int s = end; s >= L + 1; --s) CUDA_TRY(c, cudaGraphLaunch(c.gAdjointH[h], c.stream));
+    c.launches += 1 + (long long)(end - L) * nodesAdj;
+    if (twoLanes) CUDA_TRY(c, cudaEventRecord(c.evAdjDone[h], c.stream));
+    if (!twoLanes && !resident && k >= 1 && recompute(k - 1)) return 1;
+  }
+  if (twoLanes) {
+    // join the second lanes back into the main stream
+    CUDA_TRY(c, cudaEventRecord(c.evJoin[3], c.stream2));
+    CUDA_TRY(c, cudaStreamWaitEvent(c.stream, c.evJoin[3], 0));
   }
   if (checkLaunch(c)) return 1;
   std::vector<double> vals;

@@ -263,6 +263,13 @@ struct Context {
   // which the blocks' stage kernels run concurrently between fork and join
   cudaStream_t blockStreams[MGD_MAX_BLOCKS] = {};
   cudaEvent_t evBlockFork = nullptr, evBlockJoin[MGD_MAX_BLOCKS] = {};
+  // the second set, for the recomputation lane of a region's adjoint run
+  cudaStream_t blockStreams2[MGD_MAX_BLOCKS] = {};
+  cudaEvent_t evBlockFork2 = nullptr, evBlockJoin2[MGD_MAX_BLOCKS] = {};
+  // the recomputation lane's own forward work arrays of every block of a
+  // region (state, primitives, fluxes, dissipation, RK buffers, SAT vectors,
+  // interface fluxes, excitation values)
+  std::vector<BlockView> regionShadow;
   // lanes of the checkpoint recomputation, which runs beside the adjoint
   cudaStream_t stream2 = nullptr, side2 = nullptr;
   cudaEvent_t evRecDone[2] = {}, evAdjDone[2] = {};
