@@ -1900,7 +1900,7 @@ static int ensureStageBuffer(Context& c, DevBlock& b, int S) {
   CUDA_TRY(c, cudaMemGetInfo(&freeB, &totalB));
   const double budget = 0.5 * ((double)freeB + (double)c.stageBufCapacity * sizeof(double));
   int pick = 2;
-  for (int k = 0; k < 3; ++k)
+  for (int k = N <= MGD_TWO_LANE_MAX_POINTS ? 0 : 1; k < 3; ++k)
     if ((double)(options[k][0] * options[k][2]) * sizeof(double) <= budget) {
       pick = k;
       break;
@@ -2461,8 +2461,8 @@ static int regionRunAdjoint(Context& c, double* sensitivity) {
                                  ? 0.0
                                  : 8.0 * ((double)pts * (4 * nU + PrimLayout{nD}.count() + 2 * nD * nU) +
                                           2.0 * ffEntries * nU);
-  const bool twoLanes =
-      !resident && (double)(2 * 4LL * S * fullPer * pts) * sizeof(double) + shadowBytes <= budget;
+  const bool twoLanes = !resident && pts <= MGD_TWO_LANE_MAX_POINTS &&
+                        (double)(2 * 4LL * S * fullPer * pts) * sizeof(double) + shadowBytes <= budget;
   const bool full = resident || twoLanes || (double)(4LL * S * fullPer * pts) * sizeof(double) <= budget;
   const int halves = twoLanes ? 2 : 1;
   std::vector<long long> halfSize(c.blocks.size());

@@ -532,6 +532,12 @@ int selftestGridBarrier(int nBlocks, unsigned int expected, int rounds, long lon
                         long long* sum);
 void launchSetCounters(int* counters, int step, int segBase, cudaStream_t s);
 constexpr int kBatchThreads = 128;
+// Grids of up to this many points (all blocks of a region) recompute the
+// checkpoint segments on a second lane beside the adjoint; larger grids fill
+// the GPU with either lane alone and recompute each segment in line.
+#ifndef MGD_TWO_LANE_MAX_POINTS
+#define MGD_TWO_LANE_MAX_POINTS (1LL << 21)
+#endif
 // Resident CTAs per SM that the persistent batched kernel is compiled for,
 // 2D and 3D (its register budget is 65536 / (128 x this)). One kernel holds
 // the register budget of its largest phase (the gradient/flux tiles) in
