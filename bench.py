@@ -69,6 +69,9 @@ def parse():
     ap.add_argument("--ms-segments", type=int, default=8)
     ap.add_argument("--tgv-n", type=int, default=256)
     ap.add_argument("--tgv-steps", type=int, default=10, help="RK4 steps of the Taylor-Green sample (of the 2000-step run)")
+    ap.add_argument("--dissipation-tma", type=int, default=-1, choices=[-1, 0, 1],
+                    help="tgv workload: composite dissipation staged by the tensor memory accelerator (1) or read "
+                         "through L1 (0); -1 keeps the library's default")
     ap.add_argument("--jet-steps", type=int, default=8, help="RK4 steps of the jet sample (of the 1000-step run)")
     ap.add_argument("--jet-save-interval", type=int, default=4)
     ap.add_argument("--jet-scale", type=float, default=1.0, help="grid scale of the jet (1 = 39.4 M points)")
@@ -864,6 +867,8 @@ def run_tgv(args):
     P = configs.taylor_green_3d(n=args.tgv_n, n_steps=n_steps)
     S = P.save_interval
     s = Solver(P)
+    if args.dissipation_tma >= 0:
+        s.dissipation_tma(args.dissipation_tma)
     q0 = P.blocks[0].initial_state
     from magudi_gb300 import capi
 
@@ -902,6 +907,7 @@ def run_tgv(args):
                                f"dissipation, constant CFL 0.5, forward + discrete adjoint of the terminal "
                                f"kinetic energy; sample of {n_steps} of the 2000 steps, checkpoint every {S}",
                    "grid": f"{args.tgv_n}^3", "rk4_steps": n_steps, "save_interval": S,
+                   "dissipation_form": "tensor-memory-accelerator staging" if s.dissipation_tma() else "L1",
                    "l2": "working set larger than L2", "parallelism": "single GPU"},
         "J": J, "dt_first": float(dts[0]), "dt_last": float(dts[-1]),
         "projected_2000_step_gradient_s": sec / n_steps * 2000,

@@ -490,6 +490,15 @@ int mgd_gradient_lanes(mgd_ctx* ctx, int lanes);
  * context, 0 only reports it; returns the form in effect (3D: 1), or -1. */
 int mgd_adjoint_core_lanes(mgd_ctx* ctx, int lanes);
 
+/* Measurement and test hook (no reference counterpart): the form of the
+ * composite dissipation of 3D blocks that are PLANE-periodic along all axes
+ * (and whose sizes are multiples of 32 x 16 x 16): operands staged in shared
+ * memory by the tensor memory accelerator (1) or read through the L1 cache
+ * (0, the default: the kernel is FP64-bound and measured faster that way).
+ * mode = 0 or 1 sets it, -1 only reports it; returns the setting in effect,
+ * or -1. Both forms give the same results to rounding. */
+int mgd_dissipation_tma(mgd_ctx* ctx, int mode);
+
 /* Run-level autotuner (no reference counterpart): chooses the thread-block
  * tiles of the six stage kernels (and the 2D gradient/flux form) by timing
  * whole checkpointed runs, mgd_run_forward(n_steps, save_interval) followed

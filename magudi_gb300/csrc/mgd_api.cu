@@ -60,6 +60,19 @@ static void freeBlock(DevBlock& b) {
 static int checkLaunch(Context& c) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(c, std::string("kernel launch: ") + cudaGetErrorString(e));
+  if (c.tmaLaunched) {
+    // a kernel that waits on tensor-memory-accelerator copies records a wait
+    // that ran out in the error word
+    c.tmaLaunched = false;
+    int flag = 0;
+    e = cudaMemcpyAsync(&flag, c.dKernelError, sizeof flag, cudaMemcpyDeviceToHost, c.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+    if (e != cudaSuccess) return fail(c, std::string("kernel error word: ") + cudaGetErrorString(e));
+    if (flag) {
+      cudaMemsetAsync(c.dKernelError, 0, sizeof(int), c.stream);
+      return fail(c, "a wait for a tensor-memory-accelerator copy ran out of its poll limit");
+    }
+  }
   return 0;
 }
 
@@ -159,6 +172,8 @@ int mgd_create(const mgd_options* o, mgd_ctx** out) {
   cudaMemset(c.dApiTime, 0, sizeof(double));
   cudaMalloc((void**)&c.dLimitKey, sizeof(unsigned long long));
   cudaMemset(c.dLimitKey, 0xFF, sizeof(unsigned long long));
+  cudaMalloc((void**)&c.dKernelError, sizeof(int));
+  cudaMemset(c.dKernelError, 0, sizeof(int));
   if (cudaGetLastError() != cudaSuccess) {
     g_createError = "device allocation failed";
     delete h;
@@ -183,6 +198,7 @@ int mgd_destroy(mgd_ctx* h) {
     cudaFree(b.runPartials);
   }
   cudaFree(c.dLimitKey);
+  cudaFree(c.dKernelError);
   cudaFree(c.dCounters); cudaFree(c.dApiAmp); cudaFree(c.dAmp); cudaFree(c.dForcing);
   cudaFree(c.dApiTime); cudaFree(c.dStageTime); cudaFree(c.dDeltaForcing); cudaFree(c.dApiForcing);
   cudaFree(c.dGradient); cudaFree(c.dPartials); cudaFree(c.dStageValues);
@@ -260,6 +276,16 @@ int mgd_adjoint_core_lanes(mgd_ctx* h, int lanes) {
   if (lanes > 0 && c.nD == 2)
     for (auto& b : c.blocks) b.coreLanes = lanes;
   return c.nD == 2 && !c.blocks.empty() ? c.blocks[0].coreLanes : 1;
+}
+
+int mgd_dissipation_tma(mgd_ctx* h, int mode) {
+  Context& c = h->c;
+  if (mode < -1 || mode > 1) {
+    fail(c, "mgd_dissipation_tma: mode must be -1, 0 or 1");
+    return -1;
+  }
+  if (mode >= 0) c.useTmaDissipation = mode == 1;
+  return c.useTmaDissipation ? 1 : 0;
 }
 
 int mgd_gradient_lanes(mgd_ctx* h, int lanes) {

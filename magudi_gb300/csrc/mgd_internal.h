@@ -342,6 +342,13 @@ struct Context {
   // solution limits: device key of the first violation of the current run,
   // and whether the last forward run stopped at one
   unsigned long long* dLimitKey = nullptr;
+  // composite dissipation of fully periodic 3D blocks staged by the tensor
+  // memory accelerator (off by default: the FP64-bound kernel measured 11%
+  // slower staged than through L1); its kernel's error word (a bounded wait
+  // ran out) and whether such a kernel was launched since the last check
+  bool useTmaDissipation = false;
+  int* dKernelError = nullptr;
+  bool tmaLaunched = false;
   bool limitViolated = false;
   std::string limitMessage;
   cudaGraphExec_t gForward = nullptr, gRecomputeH[2] = {}, gAdjointH[2] = {};

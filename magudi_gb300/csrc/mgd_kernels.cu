@@ -11,7 +11,9 @@
 // Adjoint RK stage: kAdjointCore (per point) beside kDissipation and
 // kGradientSensitivity; kAdjointDiffusion and kAdjointAssemble (per point and
 // component) finish the adjoint RHS and its RK update.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <cstdio>
 #include <algorithm>
@@ -620,6 +622,245 @@ __global__ void __launch_bounds__(kMaxTile) kDissipation(BlockView B, Physics P,
                                                          double sign, Tile T) {
   pdlEnter();
   dissipationPoint<ND>(B, P, src, sign, T, blockIdx.x);
+}
+
+// ---------------------------------------------------------------------------
+// Composite dissipation of 3D blocks that are PLANE-periodic along all three
+// axes, with the operands staged in shared memory by the tensor memory
+// accelerator (cp.async.bulk.tensor). A CTA owns a TX x TY column of points
+// and marches through ZC planes of it: a ring of RING planes of the column
+// (z - 4 .. z + 4 and the one being prefetched) feeds the z stencil, and the
+// four halo strips of the current plane (4 points beyond each x and y edge,
+// their coordinates wrapped, so that no copy leaves the grid or overlaps
+// another) feed the x and y stencils. Each tap then reads shared memory
+// instead of global memory. The arithmetic, its order included, is that of
+// dissipationPoint (periodic interior stencil of each axis, x + y + z, times
+// sign x amount). One elected thread issues the copies; every wait on a copy
+// is bounded, and a wait that runs out sets *err, waits (bounded) for the
+// CTA's copies in flight and leaves.
+// ---------------------------------------------------------------------------
+namespace tmadiss {
+#ifndef MGD_TMA_TX
+#define MGD_TMA_TX 32
+#endif
+#ifndef MGD_TMA_TY
+#define MGD_TMA_TY 16
+#endif
+#ifndef MGD_TMA_ZC
+#define MGD_TMA_ZC 16
+#endif
+constexpr int TX = MGD_TMA_TX, TY = MGD_TMA_TY, H = 4, ZC = MGD_TMA_ZC, RING = 2 * H + 2;
+constexpr int PLANE = TX * TY, STRIP_X = H * TY, STRIP_Y = TX * H;
+constexpr int HALO = 2 * STRIP_X + 2 * STRIP_Y;  // left, right, bottom, top
+constexpr unsigned PLANE_BYTES = PLANE * 8, HALO_BYTES = HALO * 8;
+constexpr size_t SMEM = (size_t)(RING * PLANE + 2 * HALO) * 8 + (RING + 2) * 8 + 128;
+}  // namespace tmadiss
+
+__device__ __forceinline__ unsigned smemAddr(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbarInit(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbarExpectTx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(bar)), "r"(bytes)
+               : "memory");
+}
+
+// Polls the barrier's phase with the given parity; false after `limit` polls.
+__device__ __forceinline__ bool mbarWait(unsigned long long* bar, unsigned parity, long long limit) {
+  const unsigned a = smemAddr(bar);
+  for (long long k = 0; k < limit; ++k) {
+    unsigned done = 0;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// A (x, y, z, component) box of the 4D tensor map into shared memory,
+// completing on the barrier.
+__device__ __forceinline__ void tmaLoad4(void* dst, const CUtensorMap* map, int x, int y, int z, int c,
+                                         unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(smemAddr(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(c), "r"(smemAddr(bar))
+      : "memory");
+}
+
+__global__ void __launch_bounds__(tmadiss::TX* tmadiss::TY)
+    kDissipationTma3(BlockView B, Physics P, const __grid_constant__ CUtensorMap mapC,
+                     const __grid_constant__ CUtensorMap mapX, const __grid_constant__ CUtensorMap mapY, double sign,
+                     int* err, long long limit) {
+  using namespace tmadiss;
+  pdlEnter();
+  extern __shared__ unsigned char smemRaw[];
+  // 128-byte aligned buffers: the ring of planes, two halo sets, the barriers
+  double* ring = reinterpret_cast<double*>((reinterpret_cast<size_t>(smemRaw) + 127) & ~size_t(127));
+  double* halo = ring + RING * PLANE;
+  unsigned long long* barC = reinterpret_cast<unsigned long long*>(halo + 2 * HALO);
+  unsigned long long* barH = barC + RING;
+  const int nx = B.gs[0], ny = B.gs[1], nz = B.gs[2];
+  const int tilesX = nx / TX;
+  const int x0 = (blockIdx.x % tilesX) * TX, y0 = (blockIdx.x / tilesX) * TY, z0 = blockIdx.y * ZC;
+  const int comp = blockIdx.z;
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  const bool leader = threadIdx.x == 0;
+  auto wrap = [](int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); };
+  // plane z0 - H + k lives in ring slot k % RING; its fills so far give the parity
+  auto loadPlane = [&](int k) {
+    const int slot = k % RING;
+    mbarExpectTx(&barC[slot], PLANE_BYTES);
+    tmaLoad4(ring + slot * PLANE, &mapC, x0, y0, wrap(z0 - H + k, nz), comp, &barC[slot]);
+  };
+  auto loadHalo = [&](int i) {  // the halo strips of plane z0 + i into set i % 2
+    const int set = i % 2, z = z0 + i;
+    double* h = halo + set * HALO;
+    mbarExpectTx(&barH[set], HALO_BYTES);
+    tmaLoad4(h, &mapX, wrap(x0 - H, nx), y0, z, comp, &barH[set]);
+    tmaLoad4(h + STRIP_X, &mapX, wrap(x0 + TX, nx), y0, z, comp, &barH[set]);
+    tmaLoad4(h + 2 * STRIP_X, &mapY, x0, wrap(y0 - H, ny), z, comp, &barH[set]);
+    tmaLoad4(h + 2 * STRIP_X + STRIP_Y, &mapY, x0, wrap(y0 + TY, ny), z, comp, &barH[set]);
+  };
+  if (leader) {
+    for (int k = 0; k < RING; ++k) mbarInit(&barC[k], 1);
+    mbarInit(&barH[0], 1);
+    mbarInit(&barH[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (leader) {
+    for (int k = 0; k <= 2 * H; ++k) loadPlane(k);
+    loadHalo(0);
+  }
+  const double* __restrict__ cin = c_ops.interior[B.ax[0].scheme][OP_DCOMP];
+  const double f = sign * P.dissipationAmount;
+  const long long N = B.N;
+  // bounded drain of every copy issued up to iteration i (after a wait ran out)
+  auto drain = [&](int i) {
+    for (int k = 0; k < RING && k <= i + 2 * H + 1; ++k) {
+      const int last = k + ((i + 2 * H + 1 - k) / RING) * RING;  // the slot's latest fill
+      if (last <= i + 2 * H + 1) mbarWait(&barC[k], (last / RING) & 1, limit);
+    }
+    for (int j = (i > 0 ? i - 1 : 0); j <= i + 1 && j < ZC; ++j) mbarWait(&barH[j % 2], (j / 2) & 1, limit);
+  };
+  // Each plane's fill is waited for once, when it first enters the stencil
+  // (the first iteration waits for the nine the prologue loaded); one CTA
+  // barrier per iteration both closes the previous iteration's reads of the
+  // buffers refilled next and votes on whether any wait ran out.
+  bool ok = true;
+  for (int i = 0; i < ZC; ++i) {
+    if (__syncthreads_or(!ok)) {
+      if (leader) atomicExch(err, 1);
+      drain(i);
+      return;
+    }
+    // prefetch the next plane of the ring and the next halo set; both buffers
+    // were last read in iteration i - 1, which the barrier above closed
+    if (leader && i + 1 < ZC) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      loadPlane(i + 2 * H + 1);
+      loadHalo(i + 1);
+    }
+    for (int k = (i == 0 ? 0 : i + 2 * H); k <= i + 2 * H; ++k)
+      ok = ok && mbarWait(&barC[k % RING], (k / RING) & 1, limit);
+    ok = ok && mbarWait(&barH[i % 2], (i / 2) & 1, limit);
+    const double* c0 = ring + ((i + H) % RING) * PLANE;
+    const double* h = halo + (i % 2) * HALO;
+    const int q = ty * TX + tx;
+    auto xAt = [&](int d) {  // value at x offset d in [-H, H] of the current plane
+      const int xx = tx + d;
+      if (xx < 0) return h[ty * H + xx + H];
+      if (xx >= TX) return h[STRIP_X + ty * H + xx - TX];
+      return c0[ty * TX + xx];
+    };
+    auto yAt = [&](int d) {
+      const int yy = ty + d;
+      if (yy < 0) return h[2 * STRIP_X + (yy + H) * TX + tx];
+      if (yy >= TY) return h[2 * STRIP_X + STRIP_Y + (yy - TY) * TX + tx];
+      return c0[yy * TX + tx];
+    };
+    auto zAt = [&](int d) { return ring[((i + H + d) % RING) * PLANE + q]; };
+    double sx = cin[H + 1] * (xAt(1) + xAt(-1));
+#pragma unroll
+    for (int j = 2; j <= H; ++j) sx += cin[H + j] * (xAt(j) + xAt(-j));
+    sx = sx + cin[H] * c0[q];
+    double sy = cin[H + 1] * (yAt(1) + yAt(-1));
+#pragma unroll
+    for (int j = 2; j <= H; ++j) sy += cin[H + j] * (yAt(j) + yAt(-j));
+    sy = sy + cin[H] * c0[q];
+    double sz = cin[H + 1] * (zAt(1) + zAt(-1));
+#pragma unroll
+    for (int j = 2; j <= H; ++j) sz += cin[H + j] * (zAt(j) + zAt(-j));
+    sz = sz + cin[H] * c0[q];
+    double s = sx;
+    s += sy;
+    s += sz;
+    const long long p = (x0 + tx) + (long long)nx * ((y0 + ty) + (long long)ny * (z0 + i));
+    B.dq[p + N * comp] = f * s;
+  }
+  if (__syncthreads_or(!ok)) {
+    if (leader) atomicExch(err, 1);
+    drain(ZC - 1);
+  }
+}
+
+// Whether a block's composite dissipation can run as kDissipationTma3.
+bool tmaDissipationEligible(const Context& c, const DevBlock& b) {
+  using namespace tmadiss;
+  if (c.nD != 3 || !c.phys.dissipation || !c.phys.composite || !c.useTmaDissipation) return false;
+  for (int d = 0; d < 3; ++d)
+    if (b.v.ax[d].per != 1) return false;
+  return b.v.gs[0] % TX == 0 && b.v.gs[1] % TY == 0 && b.v.gs[2] % ZC == 0 && b.v.gs[0] >= TX &&
+         b.v.gs[1] >= TY && b.v.gs[2] >= 2 * H + 1;
+}
+
+// The 4D (x, y, z, component) tensor map of nComp component planes of a
+// block starting at base, with the given box.
+static bool encodeTensorMap(const DevBlock& b, const double* base, int nComp, unsigned boxX, unsigned boxY,
+                            CUtensorMap* out) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return false;
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  const cuuint64_t dims[4] = {(cuuint64_t)b.v.gs[0], (cuuint64_t)b.v.gs[1], (cuuint64_t)b.v.gs[2],
+                              (cuuint64_t)nComp};
+  const cuuint64_t strides[3] = {(cuuint64_t)b.v.gs[0] * 8, (cuuint64_t)b.v.gs[0] * b.v.gs[1] * 8,
+                                 (cuuint64_t)b.v.N * 8};
+  const cuuint32_t box[4] = {boxX, boxY, 1, 1};
+  const cuuint32_t elem[4] = {1, 1, 1, 1};
+  return encode(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<double*>(base), dims, strides, box, elem,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Launches kDissipationTma3 on src; false (nothing launched) when the tensor
+// maps cannot be made.
+static bool launchDissipationTma(Context& c, DevBlock& b, const double* src, double sign, cudaStream_t st) {
+  using namespace tmadiss;
+  CUtensorMap mapC, mapX, mapY;
+  if (!encodeTensorMap(b, src, c.nU, TX, TY, &mapC) || !encodeTensorMap(b, src, c.nU, H, TY, &mapX) ||
+      !encodeTensorMap(b, src, c.nU, TX, H, &mapY))
+    return false;
+  const dim3 grid((b.v.gs[0] / TX) * (b.v.gs[1] / TY), b.v.gs[2] / ZC, c.nU);
+  ++c.launches;
+  pdlShared(kDissipationTma3, grid, TX * TY, SMEM, st, b.v, c.phys, mapC, mapX, mapY, sign, c.dKernelError,
+            (long long)1 << 24);
+  c.tmaLaunched = true;
+  return true;
 }
 
 template <int ND, bool NC = true>
@@ -2261,6 +2502,7 @@ void launchGradFlux(Context& c, DevBlock& b, bool writeFlux, bool writeStress, c
 
 void launchDissipation(Context& c, DevBlock& b, const double* src, double sign, cudaStream_t s) {
   if (!c.phys.dissipation) return;
+  if (tmaDissipationEligible(c, b) && launchDissipationTma(c, b, src, sign, on(c, s))) return;
   const Tile T = b.tDiss;
   const dim3 grid(T.blocks(), c.nU);
   MGD_LAUNCH(c);

@@ -85,6 +85,8 @@ def load_library(build_if_missing=True):
     L.mgd_gradient_lanes.argtypes = [ctx, C.c_int]
     L.mgd_adjoint_core_lanes.restype = C.c_int
     L.mgd_adjoint_core_lanes.argtypes = [ctx, C.c_int]
+    L.mgd_dissipation_tma.restype = C.c_int
+    L.mgd_dissipation_tma.argtypes = [ctx, C.c_int]
     L.mgd_set_trajectory_storage.restype = C.c_int
     L.mgd_set_trajectory_storage.argtypes = [ctx, C.c_int, C.c_double]
     L.mgd_tune_run.restype = C.c_int
@@ -341,6 +343,14 @@ class Solver:
         if tile:
             self._check(self.L.mgd_stage_tile(self.h, int(kernel), t, 0))
         return tuple(t)
+
+    def dissipation_tma(self, mode=-1):
+        """Composite dissipation of fully periodic 3D blocks staged by the
+        tensor memory accelerator (1) or read through L1 (0); -1 reports."""
+        r = self.L.mgd_dissipation_tma(self.h, int(mode))
+        if r < 0:
+            raise MagudiError(self.L.mgd_last_error(self.h).decode())
+        return r
 
     def adjoint_core_lanes(self, lanes=0):
         """Form of the 2D adjoint core: 1 or 2 threads per point (lanes = 0
