@@ -492,7 +492,7 @@ int mgd_adjoint_core_lanes(mgd_ctx* ctx, int lanes);
 
 /* Measurement and test hook (no reference counterpart): the form of the
  * composite dissipation of 3D blocks that are PLANE-periodic along all axes
- * (and whose sizes are multiples of 32 x 16 x 16): operands staged in shared
+ * (and whose sizes are multiples of 32 x 8 x 16): operands staged in shared
  * memory by the tensor memory accelerator (1) or read through the L1 cache
  * (0, the default: the kernel is FP64-bound and measured faster that way).
  * mode = 0 or 1 sets it, -1 only reports it; returns the setting in effect,

@@ -343,7 +343,7 @@ struct Context {
   // and whether the last forward run stopped at one
   unsigned long long* dLimitKey = nullptr;
   // composite dissipation of fully periodic 3D blocks staged by the tensor
-  // memory accelerator (off by default: the FP64-bound kernel measured 11%
+  // memory accelerator (off by default: the FP64-bound kernel measured 2%
   // slower staged than through L1); its kernel's error word (a bounded wait
   // ran out) and whether such a kernel was launched since the last check
   bool useTmaDissipation = false;

@@ -628,7 +628,8 @@ __global__ void __launch_bounds__(kMaxTile) kDissipation(BlockView B, Physics P,
 // Composite dissipation of 3D blocks that are PLANE-periodic along all three
 // axes, with the operands staged in shared memory by the tensor memory
 // accelerator (cp.async.bulk.tensor). A CTA owns a TX x TY column of points
-// and marches through ZC planes of it: a ring of RING planes of the column
+// (32 x 8 with 16 planes per CTA ran fastest at 128^3 among 32 x 16 and
+// 32 x 8 columns with 8, 16 or 32 planes) and marches through ZC planes of it: a ring of RING planes of the column
 // (z - 4 .. z + 4 and the one being prefetched) feeds the z stencil, and the
 // four halo strips of the current plane (4 points beyond each x and y edge,
 // their coordinates wrapped, so that no copy leaves the grid or overlaps
@@ -644,7 +645,7 @@ namespace tmadiss {
 #define MGD_TMA_TX 32
 #endif
 #ifndef MGD_TMA_TY
-#define MGD_TMA_TY 16
+#define MGD_TMA_TY 8
 #endif
 #ifndef MGD_TMA_ZC
 #define MGD_TMA_ZC 16
@@ -856,6 +857,14 @@ static bool launchDissipationTma(Context& c, DevBlock& b, const double* src, dou
       !encodeTensorMap(b, src, c.nU, TX, H, &mapY))
     return false;
   const dim3 grid((b.v.gs[0] / TX) * (b.v.gs[1] / TY), b.v.gs[2] / ZC, c.nU);
+  static bool smemSet = false;
+  if (!smemSet) {
+    // column shapes whose buffers exceed the default 48 KB of dynamic shared memory
+    if (cudaFuncSetAttribute(kDissipationTma3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM) !=
+        cudaSuccess)
+      return false;
+    smemSet = true;
+  }
   ++c.launches;
   pdlShared(kDissipationTma3, grid, TX * TY, SMEM, st, b.v, c.phys, mapC, mapX, mapY, sign, c.dKernelError,
             (long long)1 << 24);
