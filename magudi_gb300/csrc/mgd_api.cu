@@ -446,10 +446,19 @@ int mgd_add_block(mgd_ctx* h, const mgd_block_desc* desc, const double* coordina
   v.nD = c.nD;
   v.nU = c.nU;
   for (int i = 0; i < 3; ++i) v.gs[i] = i < c.nD ? desc->grid_size[i] : 1;
-  for (int i = 0; i < c.nD; ++i)
-    if (v.gs[i] < 2 * 12 + 1 && desc->periodicity_type[i] == MGD_PERIODIC_NONE)
+  for (int i = 0; i < c.nD; ++i) {
+    const int per = desc->periodicity_type[i];
+    if (per != MGD_PERIODIC_NONE && per != MGD_PERIODIC_PLANE && per != MGD_PERIODIC_OVERLAP)
+      return fail(c, "periodicity_type must be MGD_PERIODIC_NONE, _PLANE or _OVERLAP");
+    if (v.gs[i] < 2 * 12 + 1 && per == MGD_PERIODIC_NONE)
       return fail(c, "each non-periodic direction needs at least 25 points (the closure windows of the kernels' "
                      "operator tables)");
+    // a stencil tap i +- 4 wraps once: PLANE needs a period of at least 4
+    // points, OVERLAP (period n - 1) at least 5 points
+    if ((per == MGD_PERIODIC_PLANE && v.gs[i] < 4) || (per == MGD_PERIODIC_OVERLAP && v.gs[i] < 5))
+      return fail(c, "a PLANE-periodic direction needs at least 4 points and an OVERLAP-periodic one at least 5 "
+                     "(the stencils reach 4 points to either side)");
+  }
   v.N = (long long)v.gs[0] * v.gs[1] * v.gs[2];
   for (int i = 0; i < 3; ++i) {
     v.ax[i].n = v.gs[i];

@@ -2846,6 +2846,15 @@ int orc_add_block(void* h, const mgd_block_desc* d, const double* coords, const 
     R.error = "SBP 1-2 has no non-composite dissipation operator";
     return 1;
   }
+  // the ghost fill of a periodic direction copies 4 points from the other end
+  // (src/MPIHelperImpl.f90:113-390 on one process): PLANE needs at least 4
+  // points, OVERLAP (which skips the duplicated end point) at least 5
+  for (int i = 0; i < R.nD; ++i)
+    if ((d->periodicity_type[i] == MGD_PERIODIC_PLANE && b.gs[i] < 4) ||
+        (d->periodicity_type[i] == MGD_PERIODIC_OVERLAP && b.gs[i] < 5)) {
+      R.error = "a PLANE-periodic direction needs at least 4 points and an OVERLAP-periodic one at least 5";
+      return 1;
+    }
   auto d1 = orc::firstDerivativeOf(scheme);
   auto diss = R.o.composite_dissipation ? orc::compositeDissipationOf(scheme) : orc::dissipationOf(scheme);
   auto dissT = orc::dissipationTransposeOf(scheme);

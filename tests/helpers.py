@@ -68,3 +68,33 @@ def solenoidal_forcing_numpy(patch, x, y, t):
     fx = S * np.sum(t1 * (w * t4 - 2.0 * g * dy[:, None] * t3), axis=1)
     fy = S * np.sum(t3 * (w * t2 - 2.0 * g * dx[:, None] * t1), axis=1)
     return fx, fy
+
+
+def annulus_o_grid(n_theta=33, n_r=25, r0=1.0, r1=3.0, dt=0.01, n_steps=6, save_interval=3):
+    """2D O-grid around an annulus: direction 1 runs clockwise around it with
+    OVERLAP periodicity (the last point repeats the first), direction 2 runs
+    outward. Curvilinear, viscous, dissipation, far-field SATs on both
+    circles, a Gaussian pressure pulse in a quiescent gas and the terminal
+    kinetic-energy functional."""
+    from magudi_gb300.problem import Block, Options, Patch, Problem, quiescent_state
+    gamma = 1.4
+    th = -2.0 * np.pi * np.arange(n_theta) / (n_theta - 1)
+    r = r0 + (r1 - r0) * np.arange(n_r) / (n_r - 1)
+    R, TH = np.meshgrid(r, th, indexing="ij")  # (n_r, n_theta): theta fastest
+    x, y = R * np.cos(TH), R * np.sin(TH)
+    x[:, -1], y[:, -1] = x[:, 0], y[:, 0]  # the duplicated point is the same point
+    N = n_theta * n_r
+    q = quiescent_state(N, 2, gamma)
+    xr, yr = x.ravel(), y.ravel()
+    pulse = 0.01 * np.exp(-((xr - 2.0) ** 2 + yr ** 2) / 0.2)
+    q[3] += pulse / (gamma - 1.0)
+    opts = Options(
+        n_dimensions=2, viscous=True, dissipation=True, composite_dissipation=True, curvilinear=True,
+        use_constant_cfl=False, time_step_size=dt, enable_functional=True, functional_type=1,
+        reynolds_number=200.0, dissipation_amount=0.01)
+    block = Block(grid_size=(n_theta, n_r, 1), coordinates=np.ascontiguousarray(np.stack([xr, yr])),
+                  periodicity_type=(2, 0, 0), initial_state=q, target_state=quiescent_state(N, 2, gamma),
+                  mean_pressure=np.full(N, 1.0 / gamma))
+    patches = [Patch("farField.inner", "SAT_FAR_FIELD", 1, 2, (1, -1, 1, 1, 1, -1)),
+               Patch("farField.outer", "SAT_FAR_FIELD", 1, -2, (1, -1, -1, -1, 1, -1))]
+    return Problem(options=opts, blocks=[block], patches=patches, n_steps=n_steps, save_interval=save_interval)

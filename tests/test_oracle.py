@@ -727,3 +727,21 @@ def test_per_call_control_flow_with_control_forcing_reproduces_the_runs():
     Jp, Gp = per_call_gradient(oracle_lib.Oracle(P), P, P.n_steps, 4, f)
     assert abs(Jp - J) <= 1e-12 * abs(J)
     assert abs(Gp - G) <= 1e-12 * abs(G)
+
+
+@pytest.mark.parametrize("periodicity, n, ok", [(capi.PERIODIC_PLANE, 3, False), (capi.PERIODIC_PLANE, 4, True),
+                                                (capi.PERIODIC_OVERLAP, 4, False), (capi.PERIODIC_OVERLAP, 5, True)])
+def test_periodic_block_size_limits(periodicity, n, ok):
+    """The ghost fill of a periodic direction copies 4 points from the other
+    end: PLANE needs 4 points and OVERLAP 5; smaller blocks are refused.
+    PLANE: a Taylor-Green box; OVERLAP: an O-grid around an annulus."""
+    from helpers import annulus_o_grid
+    P = annulus_o_grid(n_theta=n) if periodicity == capi.PERIODIC_OVERLAP else configs.taylor_green_3d(n=n, dt=0.01)
+    if not ok:
+        with pytest.raises(RuntimeError, match="periodic direction needs at least"):
+            oracle_lib.Oracle(P)
+        return
+    o = oracle_lib.Oracle(P)
+    o.update_state()
+    o.compute_rhs(capi.FORWARD, 0.0)
+    assert np.all(np.isfinite(o.get_field(1, capi.FIELD_RHS)))
