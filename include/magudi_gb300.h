@@ -195,7 +195,11 @@ int mgd_destroy(mgd_ctx* ctx);
 
 /* Grid%setup + Grid%update (src/GridImpl.f90:487-1066): adds block
  * number (count of earlier calls + 1) with its coordinates (N, nD) and iblank
- * (N); metrics, 1/det, H*det and arc lengths are computed on the device. */
+ * (N); metrics, 1/det, H*det and arc lengths are computed on the device.
+ * Each direction needs at least 25 points when it is not periodic (the
+ * operators' closure windows), 4 when PLANE-periodic and 5 when
+ * OVERLAP-periodic (the stencils reach 4 points to either side and wrap
+ * once); smaller blocks are refused with an error. */
 int mgd_add_block(mgd_ctx* ctx, const mgd_block_desc* block,
                   const double* coordinates, const int* iblank);
 
