@@ -141,6 +141,7 @@ int mgd_create(const mgd_options* o, mgd_ctx** out) {
       P.laFactor = o->bulk_viscosity_ratio - 2.0 / 3.0;
     }
   }
+  P.powerLaw = P.powerLawExponent > 0.0 ? 1 : 0;
   if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) {
     g_createError = "cudaStreamCreate failed";
     delete h;

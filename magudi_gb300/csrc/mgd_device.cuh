@@ -148,6 +148,12 @@ __device__ __forceinline__ double applyOp(const double* __restrict__ line, int i
   }
 }
 
+// x != 0.0 with integer operations: false for +0 and -0 only, as the
+// comparison is (NaN and every other value compare unequal to zero). GB300
+// runs double-precision compares on the FP64 pipe, which the stage kernels
+// keep busy; integer tests leave it to the arithmetic.
+__device__ __forceinline__ bool nonzero(double x) { return (__double_as_longlong(x) << 1) != 0; }
+
 // ---------------------------------------------------------------------------
 // x^n for x > 0 in FP64 with few FP64 operations, after P. T. P. Tang's
 // table-driven logarithm and exponential (ACM TOMS 15(2), 1989; 16(4), 1990):
@@ -166,7 +172,8 @@ struct PowTables {
 __device__ __forceinline__ double fastPowPositive(double x, double n, const PowTables* __restrict__ tab) {
   const long long bits = __double_as_longlong(x);
   const int be = (int)((bits >> 52) & 0x7FF);
-  if (!(x > 0.0) || be == 0 || be == 0x7FF) return pow(x, n);
+  // bits <= 0: x is -0, +0 or negative (the NaNs and infinities have be == 0x7FF)
+  if (bits <= 0 || be == 0 || be == 0x7FF) return pow(x, n);
   const int e = be - 1023;
   const int j = (int)((bits >> 45) & 0x7F);
   const double m = __longlong_as_double((bits & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);

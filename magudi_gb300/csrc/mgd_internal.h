@@ -143,6 +143,7 @@ struct Physics {
   double invGm1, gm2OverGm1, invG;
   double dissipationAmount;
   int viscous, dissipation, composite;
+  int powerLaw;  // powerLawExponent > 0: mu follows the power law of T
 };
 
 struct RunScalars {

@@ -246,7 +246,7 @@ __device__ __forceinline__ void primitives(const double* q, const Physics& P, do
   out[1 + ND] = pr;
   out[2 + ND] = T;
   double mu = P.reInv;
-  if (P.powerLawExponent > 0.0) mu = fastPowPositive(P.gm1 * T, P.powerLawExponent, &g_powTables) * P.reInv;
+  if (P.powerLaw) mu = fastPowPositive(P.gm1 * T, P.powerLawExponent, &g_powTables) * P.reInv;
   out[3 + ND] = mu;
   out[4 + ND] = P.laFactor * mu;
   out[5 + ND] = mu * P.prInv;
@@ -918,9 +918,9 @@ __device__ __forceinline__ void forwardDivergencePoint(const BlockView& B, const
     // linearized: the sponge acts on the perturbation (q here), the cost
     // target adds its stored adjoint forcing (src/SpongePatchImpl.f90:142-158,
     // src/CostTargetPatchImpl.f90:104-133); no sources, no control
-    if (S != 0.0) r -= S * q;
-    if (linFactor != 0.0 && B.tgtCount[p] != 0.0) r += linFactor * B.adjF[kc];
-  } else if (S != 0.0) {
+    if (nonzero(S)) r -= S * q;
+    if (nonzero(linFactor) && nonzero(B.tgtCount[p])) r += linFactor * B.adjF[kc];
+  } else if (nonzero(S)) {
     r -= S * (q - B.qt[kc]);
   }
   if (!lin && B.excIdx && (c == 1 || c == 2 || c == E)) {
@@ -1383,19 +1383,19 @@ __device__ __forceinline__ void adjointAssemblePoint(const BlockView& B, const P
   const long long kc = p + N * c;
   const double lam = B.lam[kc];
   const double S = B.sponge[p];
-  if (S != 0.0) r += S * lam;
+  if (nonzero(S)) r += S * lam;
   if (B.excIdx && c <= 2) {
     const int e = B.excIdx[p];
     if (e >= 0) r += B.excF[3LL * e + c];
   }
   const double cnt = B.tgtCount[p];
   if (api) {
-    if (cnt != 0.0 && apiFactor != 0.0) r += apiFactor * B.adjF[kc];
-  } else if (cnt != 0.0) {
+    if (nonzero(cnt) && nonzero(apiFactor)) r += apiFactor * B.adjF[kc];
+  } else if (nonzero(cnt)) {
     const bool finalStage = (*rs.step == 1 && stage == 1);
-    const double factor = (!rs.adjointForcingSwitch || finalStage) ? 0.0
-                          : (stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0));
-    if (factor != 0.0) {
+    // factor 0 without the adjoint forcing and at the final stage, else 2, 0.5 or 1 by stage
+    if (rs.adjointForcingSwitch && !finalStage) {
+      const double factor = stage == 4 ? 2.0 : (stage == 2 ? 0.5 : 1.0);
       const double F = -2.0 * B.mt[p] * P.gm1 * (fs.prim[p + N * L.p()] - B.meanP[p]);
       double f;
       if (c == E) {
