@@ -228,7 +228,23 @@ def fp64_peak(torch, clocks):
     sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     mhz = (clocks or {}).get("sm_max_mhz") or 2070.0
     return {"peak_tflops": 2.0 * n ** 3 / best / 1e12, "source": "measured: cuBLAS DGEMM 6144^3, best of 8",
-            "nominal_tflops": sms * 4 * mhz * 1e6 / 1e12}
+            "nominal_tflops": sms * 4 * mhz * 1e6 / 1e12, "pipe_probe": fp64_pipe_probe()}
+
+
+def fp64_pipe_probe():
+    """DFMA lane-operations per clock per SM with 1, 2, 3, 4 and 8 warps on
+    every SM (mgd_selftest_fp64_rate): how the FP64 rate splits over the
+    SM's sub-partitions, which sets the floor of a kernel with few warps."""
+    import ctypes as C
+    from magudi_gb300.solver import load_library
+    L = load_library()
+    rates = {}
+    for w in (1, 2, 3, 4, 8):
+        r = C.c_double()
+        if L.mgd_selftest_fp64_rate(w, C.byref(r)) == 0:
+            rates[str(w)] = round(r.value, 3)
+    return {"dfma_lane_ops_per_clock_per_sm_by_warps_per_sm": rates,
+            "source": "mgd_selftest_fp64_rate: one CTA per SM, 4 independent DFMA chains per thread"}
 
 
 def measured_peaks():
@@ -604,7 +620,7 @@ def run_ours(args):
         "roofline": {"bound": "fp64", "kernel": dominant, "achieved": achieved_tf, "peak": fp64["peak_tflops"],
                      "unit": "TFLOP/s", "frac": achieved_tf / fp64["peak_tflops"],
                      "traffic": MEASURED_TRAFFIC.get(dominant), "peak_source": fp64["source"],
-                     "peak_nominal_tflops": fp64["nominal_tflops"],
+                     "peak_nominal_tflops": fp64["nominal_tflops"], "fp64_pipe_probe": fp64["pipe_probe"],
                      "flops_per_point": alg_flops,
                      "flops_source": "reference operation list, counted by the operation-counting oracle build",
                      "executed": {"flops_per_point": units["flops"], "achieved_tflops": executed_tf,

@@ -449,6 +449,15 @@ int mgd_selftest_pow(const double* x, int n, double e, double* fast, double* ref
 int mgd_selftest_grid_barrier(int n_blocks, int expected, int rounds, long long limit, int* status,
                               long long* checksum);
 
+/* FP64 throughput probe (no reference counterpart): one CTA of
+ * warps_per_sm (1..32) warps on every SM of the current device, each thread
+ * running four independent DFMA chains; *lane_ops_per_clock receives the
+ * DFMA lane-operations per clock per SM at the device's maximum clock. On
+ * GB300 it rises by about 0.47 per warp up to 4 warps and stays near 1.9
+ * beyond: each of the 4 sub-partitions has its own FP64 pipe, which a
+ * warp-wide DFMA holds for about 64 cycles. */
+int mgd_selftest_fp64_rate(int warps_per_sm, double* lane_ops_per_clock);
+
 /* Forward RHS without any device allocation (no counterpart in the
  * reference). For callers that must not allocate device memory when they
  * evaluate an RHS -- a host that reserved its device-memory budget up front

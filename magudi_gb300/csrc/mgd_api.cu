@@ -3270,14 +3270,21 @@ int mgd_profile_stage_kernels(mgd_ctx* h, int mode, int reps, double* avg_ms, in
   return 0;
 }
 
-// Self-test of the table-driven power function used by the viscosity law:
-// evaluates x[i]^e with it (fast) and with CUDA's pow (ref) on the current device.
+// Self-test of the persistent kernel's bounded grid barrier.
 int mgd_selftest_grid_barrier(int n_blocks, int expected, int rounds, long long limit, int* status,
                               long long* checksum) {
   if (n_blocks < 1 || expected < 1 || rounds < 1 || limit < 1 || !status || !checksum) return 1;
   return selftestGridBarrier(n_blocks, (unsigned int)expected, rounds, limit, status, checksum) ? 1 : 0;
 }
 
+// FP64 throughput with warps_per_sm warps on every SM.
+int mgd_selftest_fp64_rate(int warps_per_sm, double* lane_ops_per_clock) {
+  if (warps_per_sm < 1 || warps_per_sm > 32 || !lane_ops_per_clock) return 1;
+  return selftestFp64Rate(warps_per_sm, lane_ops_per_clock) ? 1 : 0;
+}
+
+// Self-test of the table-driven power function used by the viscosity law:
+// evaluates x[i]^e with it (fast) and with CUDA's pow (ref) on the current device.
 int mgd_selftest_pow(const double* x, int n, double e, double* fast, double* ref) {
   if (n <= 0) return 0;
   double *dx = nullptr, *df = nullptr, *dr = nullptr;

@@ -536,6 +536,7 @@ cudaError_t launchBatchPersistent(Context& c, const BatchEntry* entries, const P
                                   int functional, int grid, cudaStream_t s);
 int persistentGridSize(const Context& c);
 // Grid-barrier self-test (see mgd_selftest_grid_barrier); 0 or a CUDA error.
+int selftestFp64Rate(int warpsPerSm, double* laneOpsPerClock);
 int selftestGridBarrier(int nBlocks, unsigned int expected, int rounds, long long limit, int* status,
                         long long* sum);
 void launchSetCounters(int* counters, int step, int segBase, cudaStream_t s);

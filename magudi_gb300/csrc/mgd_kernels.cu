@@ -2786,6 +2786,49 @@ int selftestGridBarrier(int nBlocks, unsigned int expected, int rounds, long lon
   return e == cudaSuccess ? 0 : (int)e;
 }
 
+// FP64 throughput probe: every thread runs four independent DFMA chains of
+// `iters` steps and writes one value (out holds gridDim.x * blockDim.x).
+__global__ void kFp64Chains(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1.0, x2 = x0 + 2.0, x3 = x0 + 3.0;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b);
+    x1 = fma(x1, a, b);
+    x2 = fma(x2, a, b);
+    x3 = fma(x3, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = (x0 + x1) + (x2 + x3);
+}
+
+int selftestFp64Rate(int warpsPerSm, double* laneOpsPerClock) {
+  int dev = 0, sms = 0, clockKHz = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&clockKHz, cudaDevAttrClockRate, dev);
+  const int threads = 32 * warpsPerSm, iters = 4096;
+  double* out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaMalloc((void**)&out, (size_t)sms * threads * sizeof(double));
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) {
+    // one CTA per SM: a warm-up launch, then the timed one
+    kFp64Chains<<<sms, threads>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(e0);
+    kFp64Chains<<<sms, threads>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(e1);
+    e = cudaEventSynchronize(e1);
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  if (e == cudaSuccess)
+    *laneOpsPerClock = (double)threads * iters * 4 / (ms * 1e-3) / ((double)clockKHz * 1e3);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(out);
+  return e == cudaSuccess ? 0 : (int)e;
+}
+
 int persistentGridSize(const Context& c) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);

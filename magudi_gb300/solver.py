@@ -98,6 +98,8 @@ def load_library(build_if_missing=True):
     L.mgd_batch_persistent.argtypes = [C.c_void_p, C.c_int]
     L.mgd_batch_persistent_grid.restype = C.c_int
     L.mgd_batch_persistent_grid.argtypes = [C.c_void_p]
+    L.mgd_selftest_fp64_rate.restype = C.c_int
+    L.mgd_selftest_fp64_rate.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.mgd_selftest_grid_barrier.restype = C.c_int
     L.mgd_selftest_grid_barrier.argtypes = [C.c_int, C.c_int, C.c_int, C.c_longlong, C.POINTER(C.c_int),
                                             C.POINTER(C.c_longlong)]
