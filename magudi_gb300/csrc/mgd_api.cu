@@ -1527,17 +1527,20 @@ void forwardStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, bo
 }
 
 // One adjoint RK stage (rkStage 4..1) or the adjoint RHS alone (rkStage 0).
-// The adjoint dissipation and, when recording, the gradient/sensitivity
-// kernel read lambda on the side stream beside the core and diffusion
-// kernels; all join before the assembly kernel updates lambda.
+// The wall and far-field SAT vectors, the adjoint dissipation and, when
+// recording, the gradient/sensitivity kernel read lambda on the side stream
+// beside the core and diffusion kernels; all join before the assembly
+// kernel updates lambda.
 void adjointStage(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage, double apiFactor, bool api,
                   bool fromSlot, bool record, const Lanes* lanes) {
   const Lanes L = lanes ? *lanes : Lanes{c.stream, c.side, c.evFork[1], c.evJoin[1]};
   const bool exc = !b.exc.empty();
-  const bool side = c.phys.dissipation != 0 || record || exc;
+  const bool sat = b.v.ff.n > b.nInterfaceEntries;
+  const bool side = c.phys.dissipation != 0 || record || exc || sat;
   if (side) {
     cudaEventRecord(L.fork, L.main);
     cudaStreamWaitEvent(L.side, L.fork, 0);
+    if (sat) launchAdjointSatVectors(c, b, rs, stage, fromSlot, L.side);
     if (c.phys.dissipation) launchDissipation(c, b, b.v.lam, -1.0, L.side);
     if (record) launchGradientSensitivity(c, b, rs, stage, L.side);
     if (exc) launchExcitation(c, b, rs, stage, true, fromSlot, L.side);
@@ -1589,6 +1592,7 @@ void regionAdjointStage(Context& c, int rkStage, const RunScalars& rs, double ap
     launchDissipation(c, b, b.v.lam, -1.0);
     launchExcitation(c, b, rs, 1, true, false);
     launchAdjointCore(c, b, rs, 1, false);
+    launchAdjointSatVectors(c, b, rs, 1, false);
     launchAdjointDiffusion(c, b);
   }
   for (DevBlock& b : c.blocks) launchAdjointAssemble(c, b, rkStage, rs, 1, apiFactor, true, false);
@@ -2587,14 +2591,16 @@ static int regionRunAdjoint(Context& c, double* sensitivity) {
                 launchPrims(c, b, nullptr, true, &rs[bi], i, s);
                 if (c.phys.viscous) launchGradFlux(c, b, false, true, &rs[bi], i, false, s);
               });
-            // dissipation, excitation and gradient/sensitivity of every block on
-            // the side stream (they read lambda and the forward state of the
-            // stage); interface SATs, then the cores and diffusion, then the
-            // assembly, each block on its own stream
+            // wall and far-field SAT vectors, dissipation, excitation and
+            // gradient/sensitivity of every block on the side stream (they read
+            // lambda and the forward state of the stage); interface SATs, then
+            // the cores and diffusion, then the assembly, each block on its own
+            // stream
             cudaEventRecord(c.evFork[1], c.stream);
             cudaStreamWaitEvent(c.side, c.evFork[1], 0);
             for (size_t bi = 0; bi < c.blocks.size(); ++bi) {
               DevBlock& b = c.blocks[bi];
+              launchAdjointSatVectors(c, b, rs[bi], i, full, c.side);
               if (c.phys.dissipation) launchDissipation(c, b, b.v.lam, -1.0, c.side);
               launchExcitation(c, b, rs[bi], i, true, full, c.side);
               launchGradientSensitivity(c, b, rs[bi], i, c.side);

@@ -485,6 +485,10 @@ void launchAdjointCore(Context& c, DevBlock& b, const RunScalars& rs, int stage,
 void launchExcitation(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool adjoint, bool fromSlot,
                       cudaStream_t s = 0);
 // Adjoint: divergence of the viscous diffusion (per component).
+// The adjoint SAT vectors of the block's wall and far-field entries; they
+// run beside the adjoint core and must complete before the assembly.
+void launchAdjointSatVectors(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool fromSlot,
+                             cudaStream_t s = 0);
 void launchAdjointDiffusion(Context& c, DevBlock& b, cudaStream_t s = 0);
 // Adjoint: final assembly, SATs, cost-target forcing and the RK4 adjoint update.
 void launchAdjointAssemble(Context& c, DevBlock& b, int rkStage, const RunScalars& rs, int stage, double apiFactor,

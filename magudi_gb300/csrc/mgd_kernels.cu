@@ -1082,8 +1082,8 @@ __global__ void __launch_bounds__(kBlock) kGradientSensitivity(BlockView B, RunS
 // ---------------------------------------------------------------------------
 // The point's share of the adjoint core once the direction sums y (nU) and
 // ad (nD x (nU-1)) are formed: the far-field viscous adjoint penalty and the
-// interface terms added to ad, rcore and ad stored, and the adjoint SAT
-// vector of each wall or far-field entry at the point.
+// interface terms added to ad, rcore and ad stored. The SAT vectors of the
+// wall and far-field entries come from kAdjointSatVectors.
 template <int ND, bool VISC>
 __device__ __forceinline__ void adjointCoreFinish(const BlockView& B, const Physics& P, long long p,
                                                   const FwdState& fs, const double* m, const double* u, double Tm,
@@ -1121,13 +1121,43 @@ __device__ __forceinline__ void adjointCoreFinish(const BlockView& B, const Phys
     for (int j = 0; j < ND; ++j)
       for (int c = 0; c < nV; ++c) B.ad[p + N * (j * nV + c)] = ad[j][c];
   }
-  for (int k = 0; k < 3; ++k) {
-    const int e = B.ffOfPoint[3 * p + k];
-    if (e < 0) continue;
-    if (B.ff.kind[e] == SAT_INTERFACE) continue;  // kInterfaceSatAdjoint
-    if (B.ff.kind[e] != SAT_FAR_FIELD) {
-      wallSatAdjoint<ND, VISC>(B, P, e, p, u, Tm, v, lp, B.ff.visc + (long long)e * nU);
-      continue;
+}
+
+// The adjoint SAT vector of every wall and far-field entry (B.ff.visc), one
+// thread per entry: the far-field adjoint SAT (src/FarFieldPatchImpl.f90:
+// 237-257) and the wall SATs (src/ImpenetrableWallImpl.f90,
+// src/IsothermalWallImpl.f90). They depend only on the entry's point (its
+// lambda and forward state), not on the core's sums, so they run beside the
+// adjoint core instead of inside it, where a few lanes of each boundary warp
+// carried them while the rest of the warp waited; the assembly kernel reads
+// them. Interface entries belong to kInterfaceSatAdjoint.
+template <int ND, bool VISC>
+__global__ void __launch_bounds__(kBlock) kAdjointSatVectors(BlockView B, Physics P, RunScalars rs, int stage,
+                                                            int fromSlot) {
+  pdlEnter();
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= B.ff.n) return;
+  const int kind = B.ff.kind[e];
+  if (kind == SAT_INTERFACE) return;
+  constexpr int nU = ND + 2;
+  const long long N = B.N;
+  const PrimLayout L{ND};
+  const long long p = B.ff.point[e];
+  const FwdState fs = forwardState<ND>(B, rs, stage, fromSlot != 0);
+  double u[ND];
+  for (int d = 0; d < ND; ++d) u[d] = fs.prim[p + N * L.u(d)];
+  const double v = fs.prim[p + N * L.v()], Tm = fs.prim[p + N * L.T()];
+  double lp[nU];
+  for (int c = 0; c < nU; ++c) lp[c] = B.lam[p + N * c];
+  if (kind != SAT_FAR_FIELD) {
+    wallSatAdjoint<ND, VISC>(B, P, e, p, u, Tm, v, lp, B.ff.visc + (long long)e * nU);
+    return;
+  }
+  {
+    double tau[ND * ND], hf[ND];
+    if (VISC) {
+      for (int c = 0; c < ND * ND; ++c) tau[c] = fs.tau[p + N * c];
+      for (int d = 0; d < ND; ++d) hf[d] = fs.hf[p + N * d];
     }
     const double* M = B.ff.M + (long long)e * nU * nU;
     double z[nU];
@@ -2634,6 +2664,21 @@ void launchAdjointCore(Context& c, DevBlock& b, const RunScalars& rs, int stage,
     else { if (visc) AC(3, false, true); else AC(3, false, false); }
   }
 #undef AC
+}
+
+void launchAdjointSatVectors(Context& c, DevBlock& b, const RunScalars& rs, int stage, bool fromSlot,
+                             cudaStream_t s) {
+  const int n = b.v.ff.n;
+  if (n - b.nInterfaceEntries <= 0) return;  // no wall or far-field entry
+  MGD_LAUNCH(c);
+  const int fs = fromSlot ? 1 : 0;
+  if (c.nD == 2) {
+    if (c.phys.viscous) pdl(kAdjointSatVectors<2, true>, gridFor(n), kBlock, on(c, s), b.v, c.phys, rs, stage, fs);
+    else pdl(kAdjointSatVectors<2, false>, gridFor(n), kBlock, on(c, s), b.v, c.phys, rs, stage, fs);
+  } else {
+    if (c.phys.viscous) pdl(kAdjointSatVectors<3, true>, gridFor(n), kBlock, on(c, s), b.v, c.phys, rs, stage, fs);
+    else pdl(kAdjointSatVectors<3, false>, gridFor(n), kBlock, on(c, s), b.v, c.phys, rs, stage, fs);
+  }
 }
 
 void launchAdjointDiffusion(Context& c, DevBlock& b, cudaStream_t s) {
