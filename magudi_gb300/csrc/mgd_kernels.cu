@@ -1084,7 +1084,7 @@ __global__ void __launch_bounds__(kBlock) kGradientSensitivity(BlockView B, RunS
 // ad (nD x (nU-1)) are formed: the far-field viscous adjoint penalty and the
 // interface terms added to ad, rcore and ad stored. The SAT vectors of the
 // wall and far-field entries come from kAdjointSatVectors.
-template <int ND, bool VISC>
+template <int ND, bool CURV, bool VISC>
 __device__ __forceinline__ void adjointCoreFinish(const BlockView& B, const Physics& P, long long p,
                                                   const FwdState& fs, const double* m, const double* u, double Tm,
                                                   double v, const double* tau, const double* hf, const double* y,
@@ -1101,13 +1101,18 @@ __device__ __forceinline__ void adjointCoreFinish(const BlockView& B, const Phys
     for (int k = 0; k < 3; ++k) {
       const int e = B.ffOfPoint[3 * p + k];
       if (e < 0 || B.ff.kind[e] != SAT_FAR_FIELD) continue;
+      const int nd = B.ff.normalDir[e] - 1;
       double mn[ND];  // metric row of the normal direction, read from memory (no dynamic register index)
-      for (int d = 0; d < ND; ++d) mn[d] = B.metrics[p + N * (ND * (B.ff.normalDir[e] - 1) + d)];
+      for (int d = 0; d < ND; ++d) mn[d] = CURV || d == nd ? B.metrics[p + N * (ND * nd + d)] : 0.0;
       const double sv = B.ff.sigVRaw[e];
       for (int l = 0; l < ND; ++l) {
         double t[nV];
         for (int c = 0; c < nV; ++c) t[c] = 0.0;
-        secondPartialViscousTransposeProduct<ND>(u, mu, la, kd, jac, mn, m + ND * l, &lp[1], t);
+        if (CURV)
+          secondPartialViscousTransposeProduct<ND>(u, mu, la, kd, jac, mn, m + ND * l, &lp[1], t);
+        else
+          secondPartialViscousTransposeProductCart<ND>(u, mu, la, kd, jac, nd, B.metrics[p + N * (ND * nd + nd)], l,
+                                                       m[ND * l + l], &lp[1], t);
         for (int c = 0; c < nV; ++c) ad[l][c] += sv * t[c];
       }
     }
@@ -1264,7 +1269,7 @@ __device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physi
       }
     }
   }
-  adjointCoreFinish<ND, VISC>(B, P, p, fs, m, u, Tm, v, tau, hf, y, ad);
+  adjointCoreFinish<ND, CURV, VISC>(B, P, p, fs, m, u, Tm, v, tau, hf, y, ad);
 }
 
 // The adjoint core with nD threads per point: thread block = tile threads x
@@ -1335,7 +1340,7 @@ __global__ void __launch_bounds__(2 * kMaxTile) kAdjointCoreSplit(BlockView B, P
         for (int i = 1; i < ND; ++i) t += share[((long long)i * K + k) * TT + pt];
         ad[j][c] = t;
       }
-  adjointCoreFinish<ND, VISC>(B, P, p, fs, m, u, Tm, v, tau, hf, y, ad);
+  adjointCoreFinish<ND, CURV, VISC>(B, P, p, fs, m, u, Tm, v, tau, hf, y, ad);
 }
 
 template <int ND, bool CURV, bool VISC>
