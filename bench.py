@@ -300,7 +300,7 @@ MEASURED_TRAFFIC = {"adjoint_core": 7202048 + 0}
 FORWARD_KERNELS = ["forward_gradient_flux", "forward_dissipation", "forward_divergence_rk", "forward_primitives",
                    "forward_functional"]
 ADJOINT_KERNELS = ["adjoint_core", "adjoint_dissipation", "adjoint_diffusion", "adjoint_assemble_rk",
-                   "adjoint_gradient_sensitivity"]
+                   "adjoint_gradient_sensitivity", "adjoint_sat_vectors"]
 
 
 def run_reference(args):

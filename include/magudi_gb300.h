@@ -426,10 +426,14 @@ int mgd_load_control_forcing(mgd_ctx* ctx, const char* prefix, long long n_entri
 int mgd_control_zaxpy(mgd_ctx* ctx, double a, int accumulate);
 
 /* Measurement hook (no reference counterpart): times each kernel of one RK
- * stage separately with CUDA events on the context stream; forward gives 2
- * durations [gradient/flux, divergence+RK], adjoint 4 [primitives, stress,
- * part A, part B], in milliseconds per launch averaged over reps launches.
- * Needs a preceding mgd_run_forward; leaves the state changed. */
+ * stage separately with CUDA events on the context stream, reps launches
+ * back to back without programmatic dependent launch, and writes the mean
+ * milliseconds per launch. Forward (MGD_FORWARD) gives 5 durations
+ * [gradient/flux, dissipation, divergence+RK, primitives, functional],
+ * adjoint 6 [core, dissipation, diffusion, assembly+RK,
+ * gradient/sensitivity, wall and far-field SAT vectors]; *n_kernels is the
+ * count, avg_ms must hold 6. Needs a preceding mgd_run_forward; leaves the
+ * state changed. */
 int mgd_profile_stage_kernels(mgd_ctx* ctx, int mode, int reps, double* avg_ms, int* n_kernels);
 
 /* Self-test (no reference counterpart): evaluates x[i]^e on the current

@@ -3243,6 +3243,12 @@ int mgd_profile_stage_kernels(mgd_ctx* h, int mode, int reps, double* avg_ms, in
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   const bool controller = c.opts.enable_controller && c.opts.controller_switch && c.dForcing;
+  // each kernel back to back without programmatic launch: an early-launched
+  // copy would wait on the SMs beside the running one and slow it
+  setProgrammaticLaunch(false);
+  struct Restore {
+    ~Restore() { setProgrammaticLaunch(true); }
+  } restore;
   auto timeIt = [&](auto fn) {
     fn();  // warm
     cudaEventRecord(e0, c.stream);
@@ -3267,8 +3273,9 @@ int mgd_profile_stage_kernels(mgd_ctx* h, int mode, int reps, double* avg_ms, in
     avg_ms[2] = c.phys.viscous ? timeIt([&] { launchAdjointDiffusion(c, b); }) : 0.0;
     avg_ms[3] = timeIt([&] { launchAdjointAssemble(c, b, 3, rs, 3, 0.0, false, false); });
     avg_ms[4] = timeIt([&] { launchGradientSensitivity(c, b, rs, 3); });
+    avg_ms[5] = b.v.ff.n > b.nInterfaceEntries ? timeIt([&] { launchAdjointSatVectors(c, b, rs, 3, false); }) : 0.0;
   }
-  *n_kernels = 5;
+  *n_kernels = mode == MGD_FORWARD ? 5 : 6;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (checkLaunch(c)) return 1;
