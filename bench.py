@@ -625,7 +625,8 @@ def run_ours(args):
                      "flops_source": "reference operation list, counted by the operation-counting oracle build",
                      "executed": {"flops_per_point": units["flops"], "achieved_tflops": executed_tf,
                                   "frac": executed_tf / fp64["peak_tflops"],
-                                  "source": "FP64 instructions the kernel executes (ncu, 2 x DFMA + DADD + DMUL)"},
+                                  "source": "FP64 instructions the kernel executes (ncu, 2 x DFMA + DADD + DMUL), "
+                                            "counted for the one-thread-per-point form of the 2D kernels"},
                      "rhs": {"forward": {"flops_per_point": ALGORITHMIC_FLOPS["forward_rhs"],
                                          "achieved_tflops": ALGORITHMIC_FLOPS["forward_rhs"] * pts / t_fwd / 1e12,
                                          "stage_kernels_ms": t_fwd * 1e3},
