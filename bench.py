@@ -293,10 +293,11 @@ KERNEL_UNITS = {
 ALGORITHMIC_FLOPS = {"forward_rhs": 406.8, "adjoint_rhs": 1073.2, "adjoint_core": 725.1, "dissipation": 126.4}
 
 # DRAM bytes (read + write) per launch from an ncu capture of the 201x201
-# gradient workload (dram__bytes_read.sum + dram__bytes_write.sum, three
-# launches, cold L2 between the profiler's passes); kernels not captured are
-# reported as null. The capture and its command are summarised under profiles/.
-MEASURED_TRAFFIC = {"adjoint_core": 7202048 + 0}
+# gradient workload (dram__bytes_read.sum + dram__bytes_write.sum of one
+# launch of the tuned two-threads-per-point adjoint core, cold L2 between the
+# profiler's passes); kernels not captured are reported as null. The capture
+# and its command are summarised under profiles/.
+MEASURED_TRAFFIC = {"adjoint_core": 7101696 + 0}
 FORWARD_KERNELS = ["forward_gradient_flux", "forward_dissipation", "forward_divergence_rk", "forward_primitives",
                    "forward_functional"]
 ADJOINT_KERNELS = ["adjoint_core", "adjoint_dissipation", "adjoint_diffusion", "adjoint_assemble_rk",
