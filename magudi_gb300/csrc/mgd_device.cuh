@@ -75,7 +75,7 @@ __device__ __forceinline__ double tap(const double* p) {
   else return __ldca(p);
 }
 
-template <int OP, bool NC = true>
+template <int OP, bool NC = true, int CU = 1>
 __device__ __forceinline__ double applyOp(const double* __restrict__ line, int i, const Axis& ax) {
   using S = OpShape<OP>;
   const double* __restrict__ cin = c_ops.interior[ax.scheme][OP];
@@ -84,10 +84,11 @@ __device__ __forceinline__ double applyOp(const double* __restrict__ line, int i
   const long long st = ax.stride;
   if (ax.per == 0) {
     if (i < S::depth) {
-      // boundary closure rows are rare: keep them compact (few registers)
+      // boundary closure rows: CU taps' loads in flight at a time (the sum
+      // keeps its order either way)
       const double* __restrict__ row = &g_opLeft[ax.scheme][OP][i * S::width];
       double s = __ldg(row) * tap<NC>(line);
-#pragma unroll 1
+#pragma unroll CU
       for (int k = 1; k < S::width; ++k) s += __ldg(row + k) * tap<NC>(line + k * st);
       return s;
     }
@@ -98,14 +99,14 @@ __device__ __forceinline__ double applyOp(const double* __restrict__ line, int i
         // explicit right block, columns left to right
         const double* __restrict__ row = &g_opRight[ax.scheme][OP][m * S::width];
         double s = __ldg(row) * tap<NC>(end);
-#pragma unroll 1
+#pragma unroll CU
         for (int k = 1; k < S::width; ++k) s += __ldg(row + k) * tap<NC>(end + k * st);
         return s;
       }
       const double* __restrict__ row = &g_opLeft[ax.scheme][OP][m * S::width];
       // right block = reflection of the left block, negated for skew operators
       double s = __ldg(row + S::width - 1) * tap<NC>(end);
-#pragma unroll 1
+#pragma unroll CU
       for (int k = 1; k < S::width; ++k) s += __ldg(row + S::width - 1 - k) * tap<NC>(end + k * st);
       return S::skew ? -s : s;
     }

@@ -44,6 +44,13 @@ static void uploadPowTables() {
 
 constexpr int kBlock = 128;      // pointwise kernels
 constexpr int kMaxTile = 256;    // largest stage-kernel tile
+// Taps of a boundary closure row loaded together by the stage kernels: at
+// 2D sizes the kernels are single waves whose edge tiles end last, so their
+// closure rows issue four loads at a time; 3D kernels and the persistent
+// batched kernel (NC = false, one register budget for all its phases) keep
+// one at a time and the registers that saves.
+template <int ND, bool NC = true>
+constexpr int kClosureUnroll = (ND == 2 && NC) ? 4 : 1;
 
 // Programmatic dependent launch: every kernel lets the next kernel in its
 // stream start launching as soon as all of its own blocks are running, and
@@ -425,9 +432,9 @@ __device__ __forceinline__ void gradFluxPoint(const BlockView& B, const Physics&
       const long long bd = d ? I.base[1] : I.base[0];
       const int id = d ? I.idx[1] : I.idx[0];
       const Axis ax = d ? B.ax[1] : B.ax[0];
-      const double a0 = applyOp<OP_D1, NC>(B.prim + N * L.u(0) + bd, id, ax);
-      const double a1 = applyOp<OP_D1, NC>(B.prim + N * L.u(1) + bd, id, ax);
-      const double aT = applyOp<OP_D1, NC>(B.prim + N * L.T() + bd, id, ax);
+      const double a0 = applyOp<OP_D1, NC, kClosureUnroll<ND, NC>>(B.prim + N * L.u(0) + bd, id, ax);
+      const double a1 = applyOp<OP_D1, NC, kClosureUnroll<ND, NC>>(B.prim + N * L.u(1) + bd, id, ax);
+      const double aT = applyOp<OP_D1, NC, kClosureUnroll<ND, NC>>(B.prim + N * L.T() + bd, id, ax);
       const unsigned pair = 3u << (threadIdx.x & 30);
       const double b0 = __shfl_xor_sync(pair, a0, 1);
       const double b1 = __shfl_xor_sync(pair, a1, 1);
@@ -439,8 +446,8 @@ __device__ __forceinline__ void gradFluxPoint(const BlockView& B, const Physics&
 #pragma unroll
       for (int d = 0; d < ND; ++d) {
 #pragma unroll
-        for (int c = 0; c < ND; ++c) du[c][d] = applyOp<OP_D1, NC>(B.prim + N * L.u(c) + I.base[d], I.idx[d], B.ax[d]);
-        dT[d] = applyOp<OP_D1, NC>(B.prim + N * L.T() + I.base[d], I.idx[d], B.ax[d]);
+        for (int c = 0; c < ND; ++c) du[c][d] = applyOp<OP_D1, NC, kClosureUnroll<ND, NC>>(B.prim + N * L.u(c) + I.base[d], I.idx[d], B.ax[d]);
+        dT[d] = applyOp<OP_D1, NC, kClosureUnroll<ND, NC>>(B.prim + N * L.T() + I.base[d], I.idx[d], B.ax[d]);
       }
     }
     double gu[ND][ND], gT[ND];
@@ -607,13 +614,13 @@ __device__ __forceinline__ void dissipationPoint(const BlockView& B, const Physi
   const long long N = B.N;
   const double* x = src + N * c;
   if (P.composite) {
-    double s = applyOp<OP_DCOMP, NC>(x + I.base[0], I.idx[0], B.ax[0]);
-    for (int d = 1; d < ND; ++d) s += applyOp<OP_DCOMP, NC>(x + I.base[d], I.idx[d], B.ax[d]);
+    double s = applyOp<OP_DCOMP, NC, kClosureUnroll<ND, NC>>(x + I.base[0], I.idx[0], B.ax[0]);
+    for (int d = 1; d < ND; ++d) s += applyOp<OP_DCOMP, NC, kClosureUnroll<ND, NC>>(x + I.base[d], I.idx[d], B.ax[d]);
     B.dq[p + N * c] = (sign * P.dissipationAmount) * s;
   } else {
     for (int d = 0; d < ND; ++d)
       B.dq[p + N * (d * nU + c)] =
-          (sign * B.arcA[p + N * d]) * applyOp<OP_DISS, NC>(x + I.base[d], I.idx[d], B.ax[d]);
+          (sign * B.arcA[p + N * d]) * applyOp<OP_DISS, NC, kClosureUnroll<ND, NC>>(x + I.base[d], I.idx[d], B.ax[d]);
   }
 }
 
@@ -878,8 +885,8 @@ __device__ __forceinline__ double dissipationTerm(const BlockView& B, const Phys
   constexpr int nU = ND + 2;
   const long long N = B.N;
   if (P.composite) return B.dq[p + N * c];
-  double s = applyOp<OP_DISST, NC>(B.dq + N * c + I.base[0], I.idx[0], B.ax[0]);
-  for (int i = 1; i < ND; ++i) s += applyOp<OP_DISST, NC>(B.dq + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
+  double s = applyOp<OP_DISST, NC, kClosureUnroll<ND, NC>>(B.dq + N * c + I.base[0], I.idx[0], B.ax[0]);
+  for (int i = 1; i < ND; ++i) s += applyOp<OP_DISST, NC, kClosureUnroll<ND, NC>>(B.dq + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
   return s;
 }
 
@@ -902,8 +909,8 @@ __device__ __forceinline__ void forwardDivergencePoint(const BlockView& B, const
   constexpr int nU = ND + 2, E = ND + 1;
   const int c = comp >= 0 ? comp : (int)blockIdx.y;
   const long long N = B.N;
-  double s = applyOp<OP_D1, NC>(B.fhat + N * c + I.base[0], I.idx[0], B.ax[0]);
-  for (int i = 1; i < ND; ++i) s += applyOp<OP_D1, NC>(B.fhat + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
+  double s = applyOp<OP_D1, NC, kClosureUnroll<ND, NC>>(B.fhat + N * c + I.base[0], I.idx[0], B.ax[0]);
+  for (int i = 1; i < ND; ++i) s += applyOp<OP_D1, NC, kClosureUnroll<ND, NC>>(B.fhat + N * (i * nU + c) + I.base[i], I.idx[i], B.ax[i]);
   double r = -s;
   if (P.dissipation) r += dissipationTerm<ND, NC>(B, P, I, p, c);
   r = r * B.jac[p];
@@ -1194,7 +1201,7 @@ __device__ __forceinline__ void adjointCoreDirection(const BlockView& B, const P
   const long long N = B.N;
   double w[nU];
 #pragma unroll
-  for (int c = 0; c < nU; ++c) w[c] = applyOp<OP_D1ADJ>(B.lam + N * c + Ix.base[I], Ix.idx[I], B.ax[I]);
+  for (int c = 0; c < nU; ++c) w[c] = applyOp<OP_D1ADJ, true, kClosureUnroll<ND>>(B.lam + N * c + Ix.base[I], Ix.idx[I], B.ax[I]);
   for (int c = 0; c < nU; ++c) y[c] = 0.0;
   if (CURV) {
     addFluxJacobianTransposeProduct<ND, VISC>(m + ND * I, u, Tm, v, P, P.powerLawExponent, tau, hf, w, y);
@@ -1229,7 +1236,7 @@ __device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physi
 #pragma unroll
   for (int i = 0; i < ND; ++i)
 #pragma unroll
-    for (int c = 0; c < nU; ++c) w[i][c] = applyOp<OP_D1ADJ>(B.lam + N * c + I.base[i], I.idx[i], B.ax[i]);
+    for (int c = 0; c < nU; ++c) w[i][c] = applyOp<OP_D1ADJ, true, kClosureUnroll<ND>>(B.lam + N * c + I.base[i], I.idx[i], B.ax[i]);
   double m[ND * ND];
   for (int c = 0; c < ND * ND; ++c) m[c] = (CURV || (c % (ND + 1)) == 0) ? B.metrics[p + N * c] : 0.0;
   double u[ND];
@@ -1360,8 +1367,8 @@ __device__ __forceinline__ void adjointDiffusionPoint(const BlockView& B, const 
   constexpr int nV = ND + 1;
   const int c = blockIdx.y;
   const long long N = B.N;
-  double s = applyOp<OP_D1ADJ>(B.ad + N * c + I.base[0], I.idx[0], B.ax[0]);
-  for (int j = 1; j < ND; ++j) s += applyOp<OP_D1ADJ>(B.ad + N * (j * nV + c) + I.base[j], I.idx[j], B.ax[j]);
+  double s = applyOp<OP_D1ADJ, true, kClosureUnroll<ND>>(B.ad + N * c + I.base[0], I.idx[0], B.ax[0]);
+  for (int j = 1; j < ND; ++j) s += applyOp<OP_D1ADJ, true, kClosureUnroll<ND>>(B.ad + N * (j * nV + c) + I.base[j], I.idx[j], B.ax[j]);
   B.t2[p + N * c] = s;
 }
 
@@ -1540,7 +1547,7 @@ __global__ void __launch_bounds__(kMaxTile) kLinearizedFlux(BlockView B, Physics
 #pragma unroll
     for (int j = 0; j < ND; ++j)
 #pragma unroll
-      for (int c = 0; c < nV; ++c) dt[j][c] = applyOp<OP_D1>(B.t2 + N * c + I.base[j], I.idx[j], B.ax[j]);
+      for (int c = 0; c < nV; ++c) dt[j][c] = applyOp<OP_D1, true, kClosureUnroll<ND>>(B.t2 + N * c + I.base[j], I.idx[j], B.ax[j]);
   }
 #pragma unroll
   for (int i = 0; i < ND; ++i) {
