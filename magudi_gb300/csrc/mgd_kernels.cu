@@ -1092,9 +1092,8 @@ __global__ void __launch_bounds__(kBlock) kGradientSensitivity(BlockView B, RunS
 // interface terms added to ad, rcore and ad stored. The SAT vectors of the
 // wall and far-field entries come from kAdjointSatVectors.
 template <int ND, bool CURV, bool VISC>
-__device__ __forceinline__ void adjointCoreFinish(const BlockView& B, const Physics& P, long long p,
-                                                  const FwdState& fs, const double* m, const double* u, double Tm,
-                                                  double v, const double* tau, const double* hf, const double* y,
+__device__ __forceinline__ void adjointCoreFinish(const BlockView& B, long long p, const FwdState& fs,
+                                                  const double* m, const double* u, const double* y,
                                                   double (*ad)[ND + 1]) {
   constexpr int nU = ND + 2, nV = ND + 1;
   const long long N = B.N;
@@ -1276,7 +1275,7 @@ __device__ __forceinline__ void adjointCorePoint(const BlockView& B, const Physi
       }
     }
   }
-  adjointCoreFinish<ND, CURV, VISC>(B, P, p, fs, m, u, Tm, v, tau, hf, y, ad);
+  adjointCoreFinish<ND, CURV, VISC>(B, p, fs, m, u, y, ad);
 }
 
 // The adjoint core with nD threads per point: thread block = tile threads x
@@ -1347,7 +1346,7 @@ __global__ void __launch_bounds__(2 * kMaxTile) kAdjointCoreSplit(BlockView B, P
         for (int i = 1; i < ND; ++i) t += share[((long long)i * K + k) * TT + pt];
         ad[j][c] = t;
       }
-  adjointCoreFinish<ND, CURV, VISC>(B, P, p, fs, m, u, Tm, v, tau, hf, y, ad);
+  adjointCoreFinish<ND, CURV, VISC>(B, p, fs, m, u, y, ad);
 }
 
 template <int ND, bool CURV, bool VISC>
