@@ -623,7 +623,10 @@ def run_ours(args):
                      "traffic": MEASURED_TRAFFIC.get(dominant), "peak_source": fp64["source"],
                      "peak_nominal_tflops": fp64["nominal_tflops"], "fp64_pipe_probe": fp64["pipe_probe"],
                      "flops_per_point": alg_flops,
-                     "flops_source": "reference operation list, counted by the operation-counting oracle build",
+                     "flops_source": ("reference operation list, counted by the operation-counting oracle build"
+                                      if dominant in ALGORITHMIC_FLOPS else
+                                      "FP64 operations the kernel executes: the operation list has no separate count "
+                                      "for this kernel's share of the RHS"),
                      "executed": {"flops_per_point": units["flops"], "achieved_tflops": executed_tf,
                                   "frac": executed_tf / fp64["peak_tflops"],
                                   "source": "FP64 instructions the kernel executes (ncu, 2 x DFMA + DADD + DMUL), "
