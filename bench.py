@@ -289,8 +289,13 @@ KERNEL_UNITS = {
 # performs (adjoint derivatives of lambda, the (A - B1)^T and B2^T products);
 # the GPU kernels evaluate the same terms with fewer operations (the
 # executed counts are in KERNEL_UNITS), so a rate over these counts is the
-# reference-equivalent FP64 rate.
-ALGORITHMIC_FLOPS = {"forward_rhs": 406.8, "adjoint_rhs": 1073.2, "adjoint_core": 725.1, "dissipation": 126.4}
+# reference-equivalent FP64 rate. forward_gradient_flux is the part of
+# updateState after the transport variables (velocity and temperature
+# gradients, stress, heat flux: 95.7) plus the part of computeRhsForward
+# before the derivatives (Cartesian fluxes and their transform: 34.0), which
+# the gradient/flux kernel performs.
+ALGORITHMIC_FLOPS = {"forward_rhs": 406.8, "adjoint_rhs": 1073.2, "adjoint_core": 725.1, "dissipation": 126.4,
+                     "forward_gradient_flux": 129.7}
 
 # DRAM bytes (read + write) per launch from an ncu capture of the 201x201
 # gradient workload (dram__bytes_read.sum + dram__bytes_write.sum of one

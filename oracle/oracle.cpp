@@ -49,7 +49,9 @@ enum {
   SEC_FARFIELD_ADJ = 5,       // addFarFieldAdjointPenalty
   SEC_PATCHES = 6,            // patchUpdateRhs: SATs, sponge, actuator, cost-target forcing
   SEC_REGION = 7,             // computeRhs epilogue: 1/det, acoustic sources, holes
-  SEC_ADJOINT_DIFFUSION = 9   // computeRhsAdjoint: adjoint derivative of the viscous diffusion, map to q
+  SEC_ADJOINT_DIFFUSION = 9,  // computeRhsAdjoint: adjoint derivative of the viscous diffusion, map to q
+  SEC_STATE_GRADIENT = 10,    // the part of updateState after the transport variables: gradients, stress, heat flux
+  SEC_FORWARD_FLUX = 11       // the part of computeRhsForward before the derivatives: fluxes and their transform
 };
 
 namespace orc {
@@ -1195,6 +1197,8 @@ static void updateState(Region& R, Block& b, const double* q) {
       b.thermalDiffusivity[p] = mu * R.prInv;
     }
   }
+  {
+  ORC_SECTION(SEC_STATE_GRADIENT);
   computeGradient(R, b, b.velocity.data(), nD, b.stressTensor.data());
   // in-place stress, src/CNSHelperImpl.f90:405-455
 #pragma omp parallel for schedule(static)
@@ -1225,6 +1229,7 @@ static void updateState(Region& R, Block& b, const double* q) {
   for (int d = 0; d < nD; ++d)
     for (long long p = 0; p < N; ++p)
       b.heatFlux[N * d + p] = -b.thermalDiffusivity[p] * b.heatFlux[N * d + p];
+  }
 }
 
 // computeCartesianInviscidFluxes / computeCartesianViscousFluxes,
@@ -1563,6 +1568,8 @@ static void computeRhsForward(Region& R, Block& b, int bi) {
   const long long N = b.N;
   std::vector<double> f1(N * nU * nD), f2(N * nU * nD);
   std::fill(b.rightHandSide.begin(), b.rightHandSide.end(), 0.0);
+  {
+  ORC_SECTION(SEC_FORWARD_FLUX);
   cartesianFluxes(R, b, b.conservedVariables.data(), f1.data(), R.o.viscous ? f2.data() : nullptr);
   if (R.o.viscous)
 #pragma omp parallel for schedule(static)
@@ -1599,6 +1606,7 @@ static void computeRhsForward(Region& R, Block& b, int bi) {
         }
         f2[N * (c + nU * i) + p] = s;
       }
+  }
   for (int i = 0; i < nD; ++i) apply(b.firstDerivative[i], &f2[N * nU * i], nU, b.gs, i);
 #pragma omp parallel for collapse(2) schedule(static)
   for (int c = 0; c < nU; ++c)

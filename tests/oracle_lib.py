@@ -82,7 +82,7 @@ def set_threads(n, variant="strict"):
 
 
 SECTIONS = {0: "other", 1: "state", 2: "forward", 3: "dissipation", 4: "adjoint", 5: "farfield_adjoint",
-            6: "patches", 7: "region", 9: "adjoint_diffusion"}
+            6: "patches", 7: "region", 9: "adjoint_diffusion", 10: "state_gradient", 11: "forward_flux"}
 OP_KINDS = ("add", "mul", "div", "sqrt", "special")
 
 

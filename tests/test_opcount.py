@@ -36,6 +36,7 @@ def test_frozen_counts_match_the_counting_oracle():
         "adjoint_rhs": sum(_flops(c) for c in ad.values()) / N,
         "adjoint_core": _flops(ad["adjoint"]) / N,
         "dissipation": _flops(ad["dissipation"]) / N,
+        "forward_gradient_flux": (_flops(fw["state_gradient"]) + _flops(fw["forward_flux"])) / N,
     }
     for k, v in counted.items():
         assert abs(bench.ALGORITHMIC_FLOPS[k] - v) <= 0.005 * v, (k, v)
