@@ -289,6 +289,50 @@ module MagudiGB300
        type(c_ptr), value :: ctx
      end function mgd_wait_io
 
+     ! the actuator streams and ZAXPY of magudi's optimisation drivers
+     ! (.gradient_<patch>.dat / .control_forcing_<patch>.dat, bin/ZAXPY.f90)
+     integer(c_int) function mgd_save_gradient(ctx, prefix, n_entries) bind(C, name="mgd_save_gradient")
+       import :: c_int, c_ptr, c_char, c_long_long
+       type(c_ptr), value :: ctx
+       character(kind=c_char), intent(in) :: prefix(*)
+       integer(c_long_long), value :: n_entries
+     end function mgd_save_gradient
+
+     integer(c_int) function mgd_load_control_forcing(ctx, prefix, n_entries) &
+          bind(C, name="mgd_load_control_forcing")
+       import :: c_int, c_ptr, c_char, c_long_long
+       type(c_ptr), value :: ctx
+       character(kind=c_char), intent(in) :: prefix(*)
+       integer(c_long_long), value :: n_entries
+     end function mgd_load_control_forcing
+
+     integer(c_int) function mgd_control_zaxpy(ctx, a, accumulate) bind(C, name="mgd_control_zaxpy")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx
+       real(c_double), value :: a
+       integer(c_int), value :: accumulate
+     end function mgd_control_zaxpy
+
+     ! the step sizes of the last forward run, one per step (the adjoint run uses the same)
+     integer(c_int) function mgd_get_step_sizes(ctx, host, n_steps) bind(C, name="mgd_get_step_sizes")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx, host
+       integer(c_int), value :: n_steps
+     end function mgd_get_step_sizes
+
+     ! the actuator patches' quadrature weights H*det (mgd_actuator_patch_size entries, 0 on holes)
+     integer(c_int) function mgd_actuator_weights(ctx, out) bind(C, name="mgd_actuator_weights")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ctx, out
+     end function mgd_actuator_weights
+
+     ! forward RHS of device arrays q and rhs without any device allocation
+     integer(c_int) function mgd_forward_rhs_noalloc(ctx, q, time, rhs) bind(C, name="mgd_forward_rhs_noalloc")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: ctx, q, rhs
+       real(c_double), value :: time
+     end function mgd_forward_rhs_noalloc
+
      integer(c_size_t) function c_strlen(s) bind(C, name="strlen")
        import :: c_size_t, c_ptr
        type(c_ptr), value :: s
