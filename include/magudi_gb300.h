@@ -457,7 +457,7 @@ int mgd_selftest_grid_barrier(int n_blocks, int expected, int rounds, long long 
  * warps_per_sm (1..32) warps on every SM of the current device, each thread
  * running four independent DFMA chains; *lane_ops_per_clock receives the
  * DFMA lane-operations per clock per SM at the device's maximum clock. On
- * GB300 it rises by about 0.47 per warp up to 4 warps and stays near 1.9
+ * GB300 it rises by about 0.49 per warp up to 4 warps and stays near 1.97
  * beyond: each of the 4 sub-partitions has its own FP64 pipe, which a
  * warp-wide DFMA holds for about 64 cycles. */
 int mgd_selftest_fp64_rate(int warps_per_sm, double* lane_ops_per_clock);
